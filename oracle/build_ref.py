@@ -1,0 +1,99 @@
+"""Build the reference program from its own sources for one configuration.
+
+TEST INFRASTRUCTURE ONLY.  The reference (caravangelo/inflation-easy) fixes N
+and its feature switches at compile time in src/parameters.h.  This recipe
+copies src/ of the read-only reference tree into a git-ignored build folder
+under oracle/_ref/<tag>/, sets the compile-time lines of parameters.h (the same
+regex patching the reference's own tests/regression_main_n16.py:71-76 does),
+and compiles it with g++ using the reference Makefile's flags plus
+-ffp-contract=off (IEEE evaluation, so the x86 and Arm builds agree), linking
+oracle/ref_driver.cpp, which runs the unmodified main() and dumps state.
+
+Nothing here is shipped or used by the product; only tests and the golden
+fixture generator call it, and only where the reference tree is present.
+
+    python oracle/build_ref.py --N 16 --numerical 0 --sigw 0 --deltaN 1
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_ROOT = Path(os.environ.get("IE_REFERENCE_ROOT", "/root/reference"))
+
+
+def ref_available() -> bool:
+    return (REF_ROOT / "src" / "evolution.cpp").is_file()
+
+
+def tag_for(N: int, numerical: int, sigw: int, deltaN: int) -> str:
+    return f"n{N}_{'usr' if numerical else 'hill'}_sigw{sigw}_dn{deltaN}"
+
+
+def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8) -> Path:
+    """Returns the path of the built driver binary (cached by configuration)."""
+    if not ref_available():
+        raise FileNotFoundError(f"reference sources not found under {REF_ROOT}")
+    tag = tag_for(N, numerical, sigw, deltaN)
+    out = HERE / "_ref" / tag
+    exe = out / "ie_ref"
+    if exe.is_file():
+        return exe
+    src = out / "src"
+    if src.exists():
+        shutil.rmtree(src)
+    src.mkdir(parents=True)
+    for p in (REF_ROOT / "src").iterdir():
+        shutil.copy(p, src / p.name)
+    ph = src / "parameters.h"
+    txt = ph.read_text()
+    subs = [
+        (r"#define numerical_potential \d+", f"#define numerical_potential {numerical}"),
+        (r"#define perform_deltaN \d+", f"#define perform_deltaN {deltaN}"),
+        (r"#define calculate_SIGW \d+", f"#define calculate_SIGW {sigw}"),
+        (r"#define post_inflation \d+", "#define post_inflation 0"),
+        (r"const int N = \d+;", f"const int N = {N};"),
+    ]
+    for pat, rep in subs:
+        txt, n = re.subn(pat, rep, txt, count=1)
+        if n != 1:
+            raise RuntimeError(f"could not patch {pat!r} in parameters.h")
+    ph.write_text(txt)
+    flags = ["-std=c++17", "-O3", "-DNDEBUG", "-ffp-contract=off", "-fopenmp", f"-I{src}"]
+    objs = []
+    procs = []
+    for cpp in sorted(src.glob("*.cpp")):
+        obj = out / (cpp.stem + ".o")
+        extra = ["-Dmain=ie_ref_main"] if cpp.name == "main.cpp" else []
+        procs.append(subprocess.Popen(["g++", *flags, *extra, "-c", str(cpp), "-o", str(obj)]))
+        objs.append(str(obj))
+    drv = out / "ref_driver.o"
+    procs.append(subprocess.Popen(["g++", *flags, "-c", str(HERE / "ref_driver.cpp"), "-o", str(drv)]))
+    objs.append(str(drv))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("reference compilation failed")
+    wrap = ["-Wl,--wrap=_Z4savei"] + (["-Wl,--wrap=_Z5saveNv"] if deltaN else [])
+    subprocess.check_call(["g++", "-fopenmp", *wrap, *objs, "-o", str(exe), "-lm"])
+    for o in objs:
+        os.unlink(o)
+    return exe
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--N", type=int, required=True)
+    ap.add_argument("--numerical", type=int, default=0)
+    ap.add_argument("--sigw", type=int, default=0)
+    ap.add_argument("--deltaN", type=int, default=1)
+    a = ap.parse_args()
+    print(build(a.N, a.numerical, a.sigw, a.deltaN))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1445 @@
+/*
+ * ieo.c -- CPU oracle for the InflationEasy lattice hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see ieo.h).  This is a restatement of the
+ * algorithm of caravangelo/inflation-easy, written from its behaviour, in C
+ * with an explicit state struct.  Floating-point expressions are evaluated in
+ * exactly the order the reference evaluates them, and reductions run serially
+ * in the reference's loop order, because the oracle is pinned bit-for-bit
+ * against the reference program built from source (oracle/build_ref.sh).
+ * Compile with -ffp-contract=off: fused multiply-adds would change results.
+ *
+ * Parity: pinned (tests/test_oracle_pin.py compares the full results/ .dat
+ * output and full-precision field dumps with the reference program).
+ */
+#include "ieo.h"
+
+#include <errno.h>
+#include <float.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct { double re, im; } cplx_d;
+typedef struct { float re, im; } cplx_f;
+
+struct ieo_state {
+    ieo_params p;
+    size_t gs;                 /* N^3 */
+    double pi;                 /* 2*asin(1), src/main.h:26 */
+    /* fields, src/main.cpp:16-29 */
+    double *f, *fd, *deltaN, *fny, *fdny;
+    float *h[6], *hd[6], *hny[6], *hdny[6];
+    /* scalars, src/main.cpp:31-35 */
+    double t, t0, a, ad, ad2, astep, Ne, phiref, hubble_init;
+    /* table, src/main.cpp:38-43 */
+    int ntab;
+    double *tphi, *tV, *tdV;
+    int *lstart;
+    /* rand_uniform statics, src/initialize.cpp:18-31 */
+    int rng_started, rng_next;
+    /* set_mode statics, src/initialize.cpp:56-59 */
+    int sm_started;
+    double sm_norm, sm_hbterm;
+    int err;
+    char errmsg[512];
+};
+
+static inline double pw2(double x) { return x * x; }
+
+static void set_err(ieo_state* S, const char* fmt, ...) {
+    if (S->err) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(S->errmsg, sizeof(S->errmsg), fmt, ap);
+    va_end(ap);
+    S->err = 1;
+}
+
+/* ------------------------------------------------------------------------- */
+/* parameters                                                                */
+/* ------------------------------------------------------------------------- */
+
+/* src/runtime_parameters.cpp:17-112 */
+void ieo_params_defaults(ieo_params* p, int N, int numerical) {
+    memset(p, 0, sizeof(*p));
+    p->N = N;
+    p->numerical_potential = numerical;
+    p->perform_deltaN = 1;
+    p->calculate_SIGW = 0;
+    p->criterion = numerical ? 1 : -1;
+    p->seed = 8;
+    p->rescale_s = 0.0;
+    p->af = 2.0 * N;
+    p->V0 = numerical ? 3e-9 : 3.338e-13;
+    p->rescale_B = sqrt(p->V0);
+    p->ns = 0.97;
+    if (numerical) {
+        p->initial_field = 2.9181235049318586;
+        p->initial_derivative = -0.06727651095116181;
+        p->L = 10.0;
+        p->dt = 0.001;
+        p->output_freq = 500;
+        p->output_infrequent_freq = 500;
+        p->dN = 0.0001;
+        p->Nend = 5.0;
+    } else {
+        p->initial_field = 0.0935;
+        p->initial_derivative = 0.000796;
+        p->L = 10.0;
+        p->dt = 0.0005;
+        p->output_freq = 200;
+        p->output_infrequent_freq = 200;
+        p->dN = 0.0000001;
+        p->Nend = 0.001;
+    }
+    p->use_phiref_manual = 0;
+    p->phiref_manual_value = 0.0;
+    p->high_cutoff_index = 0.0;
+    p->low_cutoff_index = 0.0;
+    p->forcing_cutoff = 0;
+    p->output_spectra = 1;
+    p->output_histogram = 1;
+    p->output_energy = 1;
+    p->output_box3D = 0;
+    p->output_box2D = 0;
+    p->screen_updates = 1;
+    p->nbins = 256;
+    p->int_err = 5;
+    p->int_errN = 5;
+    p->dx = p->L / (double)N;
+}
+
+/* src/runtime_parameters.cpp:342-354 */
+void ieo_params_finalize(ieo_params* p, int rescale_B_given, int af_given) {
+    if (!rescale_B_given) p->rescale_B = sqrt(p->V0);
+    if (!af_given) p->af = 2.0 * p->N;
+    p->dx = p->L / (double)p->N;
+}
+
+static char* trim(char* s) {
+    while (*s == ' ' || *s == '\t' || *s == '\r' || *s == '\n' || *s == '\f' || *s == '\v') ++s;
+    char* e = s + strlen(s);
+    while (e > s && (e[-1] == ' ' || e[-1] == '\t' || e[-1] == '\r' || e[-1] == '\n' || e[-1] == '\f' || e[-1] == '\v')) --e;
+    *e = 0;
+    return s;
+}
+
+static int parse_d(const char* v, double* out) {
+    char* end;
+    errno = 0;
+    double x = strtod(v, &end);
+    if (end == v || errno) return 0;
+    while (*end == ' ' || *end == '\t') ++end;
+    if (*end) return 0;
+    *out = x;
+    return 1;
+}
+
+static int parse_i(const char* v, int* out) {
+    char* end;
+    errno = 0;
+    long x = strtol(v, &end, 10);
+    if (end == v || errno) return 0;
+    while (*end == ' ' || *end == '\t') ++end;
+    if (*end) return 0;
+    *out = (int)x;
+    return 1;
+}
+
+/* src/runtime_parameters.cpp:195-365.  N and the feature switches are accepted
+ * as keys here because the oracle takes them at run time. */
+int ieo_params_load(ieo_params* p, const char* path) {
+    FILE* fp = fopen(path, "r");
+    if (!fp) {
+        ieo_params_finalize(p, 0, 0);
+        return -1;
+    }
+    int B_given = 0, af_given = 0;
+    char buf[4096];
+    while (fgets(buf, sizeof buf, fp)) {
+        char* hash = strchr(buf, '#');
+        if (hash) *hash = 0;
+        char* line = trim(buf);
+        if (!*line) continue;
+        char* eq = strchr(line, '=');
+        if (!eq) continue;
+        *eq = 0;
+        char* key = trim(line);
+        char* val = trim(eq + 1);
+        double d; int i;
+#define KD(name, field) else if (!strcmp(key, name) && parse_d(val, &d)) p->field = d;
+#define KI(name, field) else if (!strcmp(key, name) && parse_i(val, &i)) p->field = i;
+#define KB(name, field) else if (!strcmp(key, name) && parse_i(val, &i)) p->field = (i != 0);
+        if (0) {}
+        KI("seed", seed)
+        KD("rescale_s", rescale_s)
+        else if (!strcmp(key, "af") && parse_d(val, &d)) { p->af = d; af_given = 1; }
+        KD("V0", V0)
+        else if (!strcmp(key, "rescale_B") && parse_d(val, &d)) { p->rescale_B = d; B_given = 1; }
+        KD("ns", ns)
+        KD("initial_field", initial_field)
+        KD("initial_derivative", initial_derivative)
+        KD("L", L)
+        KD("dt", dt)
+        KI("output_freq", output_freq)
+        KI("output_infrequent_freq", output_infrequent_freq)
+        KD("dN", dN)
+        KD("Nend", Nend)
+        KB("use_phiref_manual", use_phiref_manual)
+        KD("phiref_manual_value", phiref_manual_value)
+        KD("high_cutoff_index", high_cutoff_index)
+        KD("low_cutoff_index", low_cutoff_index)
+        KB("forcing_cutoff", forcing_cutoff)
+        KB("output_spectra", output_spectra)
+        KB("output_histogram", output_histogram)
+        KB("output_energy", output_energy)
+        KB("output_box3D", output_box3D)
+        KB("output_box2D", output_box2D)
+        KB("screen_updates", screen_updates)
+        KI("nbins", nbins)
+        else if (!strcmp(key, "int_err") && parse_i(val, &i)) p->int_err = i < 1 ? 1 : i;
+        else if (!strcmp(key, "int_errN") && parse_i(val, &i)) p->int_errN = i < 1 ? 1 : i;
+        KI("N", N)
+        KB("numerical_potential", numerical_potential)
+        KB("perform_deltaN", perform_deltaN)
+        KB("calculate_SIGW", calculate_SIGW)
+        KI("criterion", criterion)
+#undef KD
+#undef KI
+#undef KB
+    }
+    fclose(fp);
+    ieo_params_finalize(p, B_given, af_given);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* state                                                                     */
+/* ------------------------------------------------------------------------- */
+
+void ieo_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+ieo_state* ieo_create(const ieo_params* p) {
+    ieo_state* S = (ieo_state*)calloc(1, sizeof(ieo_state));
+    if (!S) return NULL;
+    S->p = *p;
+    S->p.dx = p->L / (double)p->N;
+    const size_t N = (size_t)p->N;
+    S->gs = N * N * N;
+    S->pi = 2.0 * asin(1.0);
+    S->f = (double*)calloc(S->gs, sizeof(double));
+    S->fd = (double*)calloc(S->gs, sizeof(double));
+    S->deltaN = (double*)calloc(S->gs, sizeof(double));
+    S->fny = (double*)calloc(N * 2 * N, sizeof(double));
+    S->fdny = (double*)calloc(N * 2 * N, sizeof(double));
+    if (p->calculate_SIGW) {
+        for (int c = 0; c < 6; ++c) {
+            S->h[c] = (float*)calloc(S->gs, sizeof(float));
+            S->hd[c] = (float*)calloc(S->gs, sizeof(float));
+            S->hny[c] = (float*)calloc(N * 2 * N, sizeof(float));
+            S->hdny[c] = (float*)calloc(N * 2 * N, sizeof(float));
+        }
+    }
+    S->lstart = (int*)calloc(S->gs, sizeof(int));
+    S->astep = 1.0; S->a = 1.0; S->ad = 0.0; S->ad2 = 0.0; S->Ne = 0.0;
+    S->t = 0.0; S->t0 = 0.0; S->phiref = 0.0; S->hubble_init = 0.0;
+    return S;
+}
+
+void ieo_destroy(ieo_state* S) {
+    if (!S) return;
+    free(S->f); free(S->fd); free(S->deltaN); free(S->fny); free(S->fdny);
+    for (int c = 0; c < 6; ++c) { free(S->h[c]); free(S->hd[c]); free(S->hny[c]); free(S->hdny[c]); }
+    free(S->tphi); free(S->tV); free(S->tdV); free(S->lstart);
+    free(S);
+}
+
+const ieo_params* ieo_get_params(const ieo_state* S) { return &S->p; }
+double* ieo_f(ieo_state* S) { return S->f; }
+double* ieo_fd(ieo_state* S) { return S->fd; }
+double* ieo_deltaN(ieo_state* S) { return S->deltaN; }
+double* ieo_fnyquist(ieo_state* S) { return S->fny; }
+double* ieo_fdnyquist(ieo_state* S) { return S->fdny; }
+float* ieo_h(ieo_state* S, int c) { return S->h[c]; }
+float* ieo_hd(ieo_state* S, int c) { return S->hd[c]; }
+const char* ieo_last_error(const ieo_state* S) { return S->err ? S->errmsg : ""; }
+
+void ieo_get_scalars(const ieo_state* S, ieo_scalars* o) {
+    o->t = S->t; o->a = S->a; o->ad = S->ad; o->ad2 = S->ad2; o->astep = S->astep;
+    o->Ne = S->Ne; o->phiref = S->phiref; o->hubble_init = S->hubble_init;
+}
+void ieo_set_scalars(ieo_state* S, const ieo_scalars* i) {
+    S->t = i->t; S->a = i->a; S->ad = i->ad; S->ad2 = i->ad2; S->astep = i->astep;
+    S->Ne = i->Ne; S->phiref = i->phiref; S->hubble_init = i->hubble_init;
+}
+
+int ieo_set_table(ieo_state* S, const double* phi, const double* V, const double* dV, int n) {
+    free(S->tphi); free(S->tV); free(S->tdV);
+    S->tphi = (double*)malloc(sizeof(double) * n);
+    S->tV = (double*)malloc(sizeof(double) * n);
+    S->tdV = (double*)malloc(sizeof(double) * n);
+    memcpy(S->tphi, phi, sizeof(double) * n);
+    memcpy(S->tV, V, sizeof(double) * n);
+    memcpy(S->tdV, dV, sizeof(double) * n);
+    S->ntab = n;
+    return 0;
+}
+
+static inline size_t IDX(int N, int i, int j, int k) {
+    return ((size_t)i * N + (size_t)j) * N + (size_t)k;
+}
+
+/* ------------------------------------------------------------------------- */
+/* potential, src/potential.cpp                                              */
+/* ------------------------------------------------------------------------- */
+
+/* find_bracketing_index, src/potential.cpp:11-50.  Returns -1 on error. */
+static int bracket(ieo_state* S, double v, int start) {
+    const int n = S->ntab;
+    const double* x = S->tphi;
+    if (n < 2) { set_err(S, "Numerical potential table must contain at least two points.\n"); return -1; }
+    if (v > x[0] || v < x[n - 1]) {
+        set_err(S, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n", v, x[n - 1], x[0]);
+        return -1;
+    }
+    if (start <= 1) {
+        int lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+            const int mid = lo + (hi - lo) / 2;
+            if (x[mid] >= v) lo = mid; else hi = mid;
+        }
+        return hi;
+    }
+    int l = start < 1 ? 1 : (start > n - 1 ? n - 1 : start);
+    while (l < n && x[l] >= v) ++l;
+    while (l > 1 && x[l - 1] < v) --l;
+    if (l <= 0 || l >= n) { set_err(S, "Interpolation index out of bounds for field value %.17g.\n", v); return -1; }
+    return l;
+}
+
+/* interpolate_from_table, src/potential.cpp:52-68 */
+static double interp(ieo_state* S, double v, int l, const double* y) {
+    const double x0 = S->tphi[l - 1], x1 = S->tphi[l];
+    const double y0 = y[l - 1], y1 = y[l];
+    if (x0 == x1) { set_err(S, "Interpolation failed due to repeated field grid points.\n"); return 0.0; }
+    return y1 + (v - x1) * (y0 - y1) / (x0 - x1);
+}
+
+/* analytic hilltop, src/potential.cpp:77-83 */
+static inline double hill_V(const ieo_params* p, double v) {
+    return p->V0 * (1.0 - (1.0 - p->ns) / 4.0 * pw2(v)) / pw2(p->rescale_B);
+}
+static inline double hill_dV(const ieo_params* p, double v) {
+    return -p->V0 * (1.0 - p->ns) / 2.0 * v / pw2(p->rescale_B);
+}
+
+/* potential(), src/potential.cpp:91-98 */
+double ieo_potential(ieo_state* S, double v) {
+    if (S->p.numerical_potential) {
+        const int l = bracket(S, v, 1);
+        if (l < 0) return 0.0;
+        return interp(S, v, l, S->tV) / pw2(S->p.rescale_B);
+    }
+    return hill_V(&S->p, v);
+}
+
+/* potential_derivative(i,j,k), src/potential.cpp:103-112 */
+static inline double pot_deriv_site(ieo_state* S, size_t id) {
+    if (S->p.numerical_potential) {
+        const int l = bracket(S, S->f[id], S->lstart[id]);
+        if (l < 0) return 0.0;
+        S->lstart[id] = (l - S->p.int_err) > 1 ? (l - S->p.int_err) : 1;
+        return interp(S, S->f[id], l, S->tdV) / pw2(S->p.rescale_B);
+    }
+    return hill_dV(&S->p, S->f[id]);
+}
+
+/* potential_energy(), src/potential.cpp:151-171 (serial) */
+double ieo_potential_energy(ieo_state* S) {
+    double pot = 0.0;
+    const size_t gs = S->gs;
+    if (S->p.numerical_potential) {
+        for (size_t id = 0; id < gs; ++id) {
+            const int l = bracket(S, S->f[id], S->lstart[id]);
+            if (l < 0) return 0.0;
+            pot += interp(S, S->f[id], l, S->tV) / pw2(S->p.rescale_B);
+            S->lstart[id] = (l - S->p.int_err) > 1 ? (l - S->p.int_err) : 1;
+        }
+    } else {
+        for (size_t id = 0; id < gs; ++id) pot += ieo_potential(S, S->f[id]);
+    }
+    pot /= (double)gs;
+    return pot;
+}
+
+/* pot_ratio(i,j,k), src/potential.cpp:177-192 */
+static inline double pot_ratio_site(ieo_state* S, size_t id) {
+    double pot, der;
+    if (S->p.numerical_potential) {
+        const int l = bracket(S, S->f[id], S->lstart[id]);
+        if (l < 0) return 0.0;
+        pot = interp(S, S->f[id], l, S->tV);
+        der = interp(S, S->f[id], l, S->tdV);
+        S->lstart[id] = (l - S->p.int_errN) > 1 ? (l - S->p.int_errN) : 1;
+    } else {
+        pot = hill_V(&S->p, S->f[id]);
+        der = hill_dV(&S->p, S->f[id]);
+    }
+    return der / pot;
+}
+
+/* ------------------------------------------------------------------------- */
+/* RNG and initial conditions, src/initialize.cpp                            */
+/* ------------------------------------------------------------------------- */
+
+/* Park-Miller minimal standard generator with Schrage's factorisation and a
+ * 99-call warm-up, src/initialize.cpp:13-31. */
+static void rng_advance(ieo_state* S) {
+    S->rng_next = 16807 * (S->rng_next % 127773) - 2836 * (S->rng_next / 127773);
+    if (S->rng_next < 0) S->rng_next += 2147483647;
+}
+
+double ieo_rand_uniform(ieo_state* S) {
+    if (S->p.seed < 1) return 0.33;
+    if (!S->rng_started) {
+        S->rng_next = S->p.seed;
+    }
+    if (!(S->rng_next > 0)) {
+        printf("Invalid seed used in random number function. Using seed=1\n");
+        S->rng_next = 1;
+    }
+    if (!S->rng_started) {
+        S->rng_started = 1;
+        for (int w = 1; w < 100; ++w) rng_advance(S);
+    }
+    rng_advance(S);
+    return (double)S->rng_next / (double)2147483647;
+}
+
+/* set_mode, src/initialize.cpp:53-89 (its statics live in the state) */
+static void set_mode(ieo_state* S, double p2, double p2lat, double m2, double* field, double* deriv, int real) {
+    double phase, amplitude, rms_amplitude, omega;
+    double re_f_left, im_f_left;
+    const ieo_params* p = &S->p;
+    if (!S->sm_started) {
+        S->sm_norm = p->rescale_B * pow(p->L / pw2(p->dx), 1.5);
+        S->sm_hbterm = -S->hubble_init;
+        S->sm_started = 1;
+    }
+    const double ii = p->L / (2.0 * S->pi) * sqrt(p2lat);
+    omega = (p2 + m2 > 0.0) ? sqrt(p2 + m2) : sqrt(p2);
+    rms_amplitude = (omega > 0.0) ? S->sm_norm / sqrt(2.0 * omega) : 0.0;
+    if (p->high_cutoff_index > 0 && (ii > p->high_cutoff_index || ii < p->low_cutoff_index)) rms_amplitude = 0.0;
+    amplitude = rms_amplitude * sqrt(log(1.0 / ieo_rand_uniform(S)));
+    phase = 2.0 * S->pi * ieo_rand_uniform(S);
+    re_f_left = amplitude * cos(phase);
+    im_f_left = amplitude * sin(phase);
+    field[0] = re_f_left;
+    field[1] = im_f_left;
+    deriv[0] = omega * im_f_left + S->sm_hbterm * field[0];
+    deriv[1] = -omega * re_f_left + S->sm_hbterm * field[1];
+    if (real == 1) { field[1] = 0.0; deriv[1] = 0.0; }
+}
+
+/* initialize(), src/initialize.cpp:93-114 */
+int ieo_initialize(ieo_state* S) {
+    const ieo_params* p = &S->p;
+    if (p->dt > p->dx / sqrt(3.0)) {
+        set_err(S, "Time step too large. Courant condition violated: dt/dx = %f\n", p->dt / p->dx);
+        return 1;
+    }
+    S->t0 = 0.0;
+    S->hubble_init = sqrt(ieo_potential(S, p->initial_field) / 3.0);
+    if (S->err) return 1;
+    S->ad = S->hubble_init;
+    memset(S->lstart, 0, sizeof(int) * S->gs);
+    return 0;
+}
+
+/* initializef(), src/initialize.cpp:118-214 */
+int ieo_initializef(ieo_state* S) {
+    const ieo_params* p = &S->p;
+    const int N = p->N;
+    const double pi = S->pi;
+    double* f = S->f;
+    double* fd = S->fd;
+    double p2, p2lat, mass_sq = 0.0;
+    const double dp2 = pw2(2.0 * pi / p->L);
+    int i, j, k, iconj, jconj;
+    double px, py, pz;
+
+    if (p->dt > p->dx / sqrt(3.0)) {
+        set_err(S, "Time step too large. Courant condition violated: dt/dx = %f\n", p->dt / p->dx);
+        return 1;
+    }
+    memset(f, 0, sizeof(double) * S->gs);
+    memset(fd, 0, sizeof(double) * S->gs);
+    S->hubble_init = sqrt((0.5 * pw2(p->initial_derivative) + ieo_potential(S, p->initial_field)) / 3.0);
+    if (S->err) return 1;
+    S->ad = S->hubble_init;
+
+    double (*fny)[2] = (double (*)[2])S->fny;      /* element [i*N + j] = fny[i][2j..2j+1] */
+    double (*fdny)[2] = (double (*)[2])S->fdny;
+    const double NL = (double)N / p->L;
+    for (i = 0; i < N; i++) {
+        px = (i <= N / 2 ? i : i - N);
+        iconj = (i == 0 ? 0 : N - i);
+        for (j = 0; j < N; j++) {
+            py = (j <= N / 2 ? j : j - N);
+            for (k = 1; k < N / 2; k++) {
+                pz = k;
+                p2lat = dp2 * (pw2(px) + pw2(py) + pw2(pz));
+                p2 = 4.0 * pw2(NL) * (pw2(sin(px * pi / N)) + pw2(sin(py * pi / N)) + pw2(sin(pz * pi / N)));
+                set_mode(S, p2, p2lat, mass_sq, &f[IDX(N, i, j, 2 * k)], &fd[IDX(N, i, j, 2 * k)], 0);
+            }
+            if (j > N / 2 || (i > N / 2 && (j == 0 || j == N / 2))) {
+                jconj = (j == 0 ? 0 : N - j);
+                p2lat = dp2 * (pw2(px) + pw2(py));
+                p2 = 4.0 * pw2(NL) * (pw2(sin(px * pi / N)) + pw2(sin(py * pi / N)));
+                set_mode(S, p2, p2lat, mass_sq, &f[IDX(N, i, j, 0)], &fd[IDX(N, i, j, 0)], 0);
+                f[IDX(N, iconj, jconj, 0)] = f[IDX(N, i, j, 0)];
+                f[IDX(N, iconj, jconj, 1)] = -f[IDX(N, i, j, 1)];
+                fd[IDX(N, iconj, jconj, 0)] = fd[IDX(N, i, j, 0)];
+                fd[IDX(N, iconj, jconj, 1)] = -fd[IDX(N, i, j, 1)];
+                p2lat = dp2 * (pw2(px) + pw2(py) + pw2(N / 2));
+                p2 = 4.0 * pw2(NL) * (pw2(sin(px * pi / N)) + pw2(sin(py * pi / N)) + 1.0);
+                set_mode(S, p2, p2lat, mass_sq, fny[(size_t)i * N + j], fdny[(size_t)i * N + j], 0);
+                fny[(size_t)iconj * N + jconj][0] = fny[(size_t)i * N + j][0];
+                fny[(size_t)iconj * N + jconj][1] = -fny[(size_t)i * N + j][1];
+                fdny[(size_t)iconj * N + jconj][0] = fdny[(size_t)i * N + j][0];
+                fdny[(size_t)iconj * N + jconj][1] = -fdny[(size_t)i * N + j][1];
+            } else if ((i == 0 || i == N / 2) && (j == 0 || j == N / 2)) {
+                p2lat = dp2 * (pw2(px) + pw2(py));
+                p2 = 4.0 * pw2(NL) * (pw2(sin(px * pi / N)) + pw2(sin(py * pi / N)));
+                if (p2 > 0.0) set_mode(S, p2, p2lat, mass_sq, &f[IDX(N, i, j, 0)], &fd[IDX(N, i, j, 0)], 1);
+                p2lat = dp2 * (pw2(px) + pw2(py) + pw2(N / 2));
+                p2 = 4.0 * pw2(NL) * (pw2(sin(px * pi / N)) + pw2(sin(py * pi / N)) + 1.0);
+                set_mode(S, p2, p2lat, mass_sq, fny[(size_t)i * N + j], fdny[(size_t)i * N + j], 1);
+            }
+        }
+    }
+    f[0] = 0.0; f[1] = 0.0; fd[0] = 0.0; fd[1] = 0.0;
+
+    ieo_fftrn_d(f, S->fny, N, -1);
+    ieo_fftrn_d(fd, S->fdny, N, -1);
+
+    for (size_t id = 0; id < S->gs; ++id) {
+        f[id] += p->initial_field;
+        fd[id] += p->initial_derivative;
+    }
+    double vard = 0.0;
+    for (size_t id = 0; id < S->gs; ++id) vard += pw2(fd[id]);
+    const double deriv_energy_in = 0.5 * vard / (double)S->gs;
+    const double pe = ieo_potential_energy(S);
+    if (S->err) return 1;
+    const double ge = ieo_gradient_energy(S);
+    S->hubble_init = sqrt((deriv_energy_in + pe + ge) / 3.0);
+    S->ad = S->hubble_init;
+    return 0;
+}
+
+/* initializeGW(), src/initialize.cpp:236-243 */
+void ieo_initializeGW(ieo_state* S) {
+    if (!S->p.calculate_SIGW) return;
+    for (int c = 0; c < 6; ++c) {
+        memset(S->h[c], 0, sizeof(float) * S->gs);
+        memset(S->hd[c], 0, sizeof(float) * S->gs);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* leapfrog, src/evolution.cpp                                               */
+/* ------------------------------------------------------------------------- */
+
+/* lapl<double>, src/evolution.cpp:34-51: (k+1)+(k-1)+(j+1)+(j-1)+(i+1)+(i-1)-6f */
+#define LAPL_AT(T, F, N, i, j, k, ip, im, jp, jm, kp, km)                    \
+    ((F)[IDX(N, i, j, kp)] + (F)[IDX(N, i, j, km)] + (F)[IDX(N, i, jp, k)] +  \
+     (F)[IDX(N, i, jm, k)] + (F)[IDX(N, ip, j, k)] + (F)[IDX(N, im, j, k)] -   \
+     (T)6 * (F)[IDX(N, i, j, k)])
+
+/* gradient_energy(), src/evolution.cpp:130-136 (serial) */
+double ieo_gradient_energy(ieo_state* S) {
+    const int N = S->p.N;
+    const double* f = S->f;
+    double gradient = 0.0;
+    const double norm = pw2(1.0 / (S->a * S->p.dx));
+    for (int i = 0; i < N; ++i) {
+        const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+        for (int j = 0; j < N; ++j) {
+            const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+            for (int k = 0; k < N; ++k) {
+                const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                gradient -= f[IDX(N, i, j, k)] * LAPL_AT(double, f, N, i, j, k, ip, im, jp, jm, kp, km);
+            }
+        }
+    }
+    return 0.5 * gradient * norm / (double)S->gs;
+}
+
+/* kin_energy(), src/evolution.cpp:139-145 */
+double ieo_kin_energy(ieo_state* S) {
+    double e = 0.0;
+    for (size_t id = 0; id < S->gs; ++id) e += pw2(S->fd[id]);
+    e /= (double)S->gs;
+    return 0.5 * pow(S->a, 2.0 * S->p.rescale_s - 2.0) * e;
+}
+
+/* evolve_derivs(d), src/evolution.cpp:150-257 */
+int ieo_evolve_derivs(ieo_state* S, double d) {
+    const ieo_params* p = &S->p;
+    const int N = p->N;
+    const double s = p->rescale_s;
+    const double laplnorm = pow(S->a, -2.0 * s) / pw2(p->dx);
+    const double sfev1 = s + 1.0;
+    const double sfev2 = -2.0 * s + 2.0;
+
+    const double ge = ieo_gradient_energy(S);
+    const double pe = ieo_potential_energy(S);
+    if (S->err) return 1;
+    S->ad2 = (-2.0 * S->ad - 2.0 * S->a / d / sfev1 * (
+        1.0 - sqrt(1.0 + 2.0 * d * sfev1 * S->ad / S->a +
+        pw2(d) * sfev1 * pow(S->a, sfev2) * (2.0 * ge / 3.0 + pe)))) / d;
+    S->ad += 0.5 * d * S->ad2;
+
+    const double friction = (2.0 + s) * S->ad / S->a;
+    const double potnorm = pow(S->a, 2.0 - 2.0 * s);
+    double* f = S->f;
+    double* fd = S->fd;
+
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; ++i) {
+        const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+        for (int j = 0; j < N; ++j) {
+            const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+            for (int k = 0; k < N; ++k) {
+                const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                const size_t id = IDX(N, i, j, k);
+                fd[id] += d * (laplnorm * LAPL_AT(double, f, N, i, j, k, ip, im, jp, jm, kp, km)
+                               - friction * fd[id]
+                               - potnorm * pot_deriv_site(S, id));
+            }
+        }
+    }
+    if (S->err) return 1;
+
+    if (p->calculate_SIGW) {
+        const double srcAmp = 2.0 * pow(S->a, -2.0 * s);
+        const double half_over_dx = 0.5 / p->dx;
+        #pragma omp parallel for schedule(static)
+        for (int i = 0; i < N; ++i) {
+            const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+            for (int j = 0; j < N; ++j) {
+                const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+                for (int k = 0; k < N; ++k) {
+                    const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                    const size_t id = IDX(N, i, j, k);
+                    /* dfdx<double>, src/evolution.cpp:55-77 */
+                    const double gx = (f[IDX(N, ip, j, k)] - f[IDX(N, im, j, k)]) * half_over_dx;
+                    const double gy = (f[IDX(N, i, jp, k)] - f[IDX(N, i, jm, k)]) * half_over_dx;
+                    const double gz = (f[IDX(N, i, j, kp)] - f[IDX(N, i, j, km)]) * half_over_dx;
+                    const double T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+                    for (int c = 0; c < 6; ++c) {
+                        const float* h = S->h[c];
+                        const float lapf = LAPL_AT(float, h, N, i, j, k, ip, im, jp, jm, kp, km);
+                        const double lap_h = (double)lapf;
+                        const double rhs = d * (laplnorm * lap_h - friction * (double)S->hd[c][id] + srcAmp * T[c]);
+                        S->hd[c][id] += (float)rhs;
+                    }
+                }
+            }
+        }
+    }
+    S->ad += 0.5 * d * S->ad2;
+    return 0;
+}
+
+/* evolve_fields(d), src/evolution.cpp:260-284 */
+void ieo_evolve_fields(ieo_state* S, double d) {
+    S->t += d;
+    double* f = S->f;
+    const double* fd = S->fd;
+    const long gs = (long)S->gs;
+    #pragma omp parallel for schedule(static)
+    for (long id = 0; id < gs; ++id) f[id] += d * fd[id];
+    if (S->p.calculate_SIGW) {
+        for (int c = 0; c < 6; ++c) {
+            float* h = S->h[c];
+            const float* hd = S->hd[c];
+            #pragma omp parallel for schedule(static)
+            for (long id = 0; id < gs; ++id) h[id] += (float)(d * hd[id]);
+        }
+    }
+    S->a += d * S->ad;
+}
+
+/* inflation_rescaled_step, src/evolution.cpp:338-340 */
+double ieo_rescaled_step(const ieo_state* S, double astep) {
+    return S->p.dt * pow(astep, S->p.rescale_s - 1.0);
+}
+
+int ieo_leapfrog_steps(ieo_state* S, int nsteps) {
+    int n = 0;
+    while (n < nsteps && S->a <= S->p.af) {
+        const double d = ieo_rescaled_step(S, S->astep);
+        if (ieo_evolve_derivs(S, d)) return -1;
+        ieo_evolve_fields(S, d);
+        ++n;
+        S->astep = S->a;
+    }
+    return n;
+}
+
+/* ------------------------------------------------------------------------- */
+/* FFT: radix-2 FFTEASY variant of src/ffteasy.hpp                           */
+/* ------------------------------------------------------------------------- */
+
+/* One macro body per precision keeps the two instantiations identical. */
+#define DEFINE_FFT(T, CPLX, SFX, SIN, COS, ASIN)                                                      \
+static void fftc1_##SFX(T* fr, int n, int skip, int forward) {                                        \
+    int b, index1, index2, trans_size, trans;                                                          \
+    const T pi2 = (T)4 * ASIN((T)1);                                                                   \
+    T pi2n, cospi2n, sinpi2n;                                                                          \
+    CPLX wb, temp1, temp2;                                                                             \
+    CPLX* c = (CPLX*)fr;                                                                               \
+    for (index1 = 1, index2 = 0; index1 < n; ++index1) {                                               \
+        for (b = n / 2; index2 >= b; b >>= 1) index2 -= b;                                             \
+        index2 += b;                                                                                   \
+        if (index2 > index1) {                                                                         \
+            temp1 = c[(size_t)index2 * skip];                                                          \
+            c[(size_t)index2 * skip] = c[(size_t)index1 * skip];                                       \
+            c[(size_t)index1 * skip] = temp1;                                                          \
+        }                                                                                              \
+    }                                                                                                  \
+    for (trans_size = 2; trans_size <= n; trans_size <<= 1) {                                          \
+        pi2n = (T)forward * pi2 / (T)trans_size;                                                       \
+        cospi2n = COS(pi2n);                                                                           \
+        sinpi2n = SIN(pi2n);                                                                           \
+        wb.re = (T)1; wb.im = (T)0;                                                                    \
+        for (b = 0; b < trans_size / 2; ++b) {                                                         \
+            for (trans = 0; trans < n / trans_size; ++trans) {                                         \
+                size_t i1 = (size_t)(trans * trans_size + b) * skip;                                   \
+                size_t i2 = i1 + (size_t)(trans_size / 2) * skip;                                      \
+                temp1 = c[i1];                                                                         \
+                temp2 = c[i2];                                                                         \
+                c[i1].re = temp1.re + wb.re * temp2.re - wb.im * temp2.im;                             \
+                c[i1].im = temp1.im + wb.re * temp2.im + wb.im * temp2.re;                             \
+                c[i2].re = temp1.re - wb.re * temp2.re + wb.im * temp2.im;                             \
+                c[i2].im = temp1.im - wb.re * temp2.im - wb.im * temp2.re;                             \
+            }                                                                                          \
+            temp1 = wb;                                                                                \
+            wb.re = cospi2n * temp1.re - sinpi2n * temp1.im;                                           \
+            wb.im = cospi2n * temp1.im + sinpi2n * temp1.re;                                           \
+        }                                                                                              \
+    }                                                                                                  \
+    if (forward < 0) {                                                                                 \
+        for (size_t q = 0; q < (size_t)skip * n; q += skip) {                                          \
+            c[q].re /= (T)n;                                                                           \
+            c[q].im /= (T)n;                                                                           \
+        }                                                                                              \
+    }                                                                                                  \
+}                                                                                                      \
+static void fftcn_##SFX(T* fr, int ndims, const int* size, int forward) {                             \
+    size_t planesize = 1, skip = 1, totalsize = 1;                                                     \
+    for (int dim = 0; dim < ndims; ++dim) totalsize *= size[dim];                                      \
+    for (int dim = ndims - 1; dim >= 0; --dim) {                                                       \
+        planesize *= size[dim];                                                                        \
+        for (size_t i = 0; i < totalsize; i += planesize)                                              \
+            for (size_t j = 0; j < skip; ++j)                                                          \
+                fftc1_##SFX(fr + 2 * (i + j), size[dim], (int)skip, forward);                          \
+        skip *= size[dim];                                                                             \
+    }                                                                                                  \
+}                                                                                                      \
+static void fftrn3_##SFX(T* fr, T* fnyq, int N, int forward) {                                        \
+    int size[3] = {N, N, N / 2};                                                                       \
+    const T pi2n = ((T)4 * ASIN((T)1)) / (T)N;                                                         \
+    const T cospi2n = COS(pi2n);                                                                       \
+    const T sinpi2n = SIN(pi2n);                                                                       \
+    CPLX wb, temp1, temp2;                                                                             \
+    CPLX* c = (CPLX*)fr;                                                                               \
+    CPLX* cny = (CPLX*)fnyq;                                                                           \
+    const size_t rowlen = (size_t)(N / 2);                                                             \
+    const size_t totalsize = (size_t)N * N * rowlen;                                                   \
+    const T fw = (T)forward;                                                                           \
+    if (forward == 1) {                                                                                \
+        fftcn_##SFX(fr, 3, size, 1);                                                                   \
+        for (size_t r = 0; r < totalsize / rowlen; ++r) cny[r] = c[r * rowlen];                        \
+    }                                                                                                  \
+    int ii = 0, jj = 0;                                                                                \
+    for (size_t index = 0; index < totalsize; index += rowlen) {                                       \
+        const int in_ = (ii == 0) ? 0 : N - ii, jn_ = (jj == 0) ? 0 : N - jj;                          \
+        const size_t rneg = (size_t)in_ * N + (size_t)jn_;                                             \
+        const size_t indexneg = rneg * rowlen;                                                         \
+        wb.re = (T)1; wb.im = (T)0;                                                                    \
+        for (int b = 1; b < N / 4; ++b) {                                                              \
+            temp1 = wb;                                                                                \
+            wb.re = cospi2n * temp1.re - sinpi2n * temp1.im;                                           \
+            wb.im = cospi2n * temp1.im + sinpi2n * temp1.re;                                           \
+            temp1 = c[index + b];                                                                      \
+            temp2 = c[indexneg + N / 2 - b];                                                           \
+            c[index + b].re = (T)0.5 * (temp1.re + temp2.re + fw * wb.re * (temp1.im + temp2.im) + wb.im * (temp1.re - temp2.re)); \
+            c[index + b].im = (T)0.5 * (temp1.im - temp2.im - fw * wb.re * (temp1.re - temp2.re) + wb.im * (temp1.im + temp2.im)); \
+            c[indexneg + N / 2 - b].re = (T)0.5 * (temp1.re + temp2.re - fw * wb.re * (temp1.im + temp2.im) - wb.im * (temp1.re - temp2.re)); \
+            c[indexneg + N / 2 - b].im = (T)0.5 * (-temp1.im + temp2.im - fw * wb.re * (temp1.re - temp2.re) + wb.im * (temp1.im + temp2.im)); \
+        }                                                                                              \
+        temp1 = c[index];                                                                              \
+        temp2 = cny[rneg];                                                                             \
+        c[index].re = (T)0.5 * (temp1.re + temp2.re + fw * (temp1.im + temp2.im));                     \
+        c[index].im = (T)0.5 * (temp1.im - temp2.im - fw * (temp1.re - temp2.re));                     \
+        cny[rneg].re = (T)0.5 * (temp1.re + temp2.re - fw * (temp1.im + temp2.im));                    \
+        cny[rneg].im = (T)0.5 * (-temp1.im + temp2.im - fw * (temp1.re - temp2.re));                   \
+        if (++jj == N) { jj = 0; ++ii; }                                                               \
+    }                                                                                                  \
+    if (forward == -1) fftcn_##SFX(fr, 3, size, -1);                                                   \
+}
+
+DEFINE_FFT(double, cplx_d, d, sin, cos, asin)
+DEFINE_FFT(float, cplx_f, f, sinf, cosf, asinf)
+
+void ieo_fftrn_d(double* f, double* fny, int N, int forward) { fftrn3_d(f, fny, N, forward); }
+void ieo_fftrn_f(float* f, float* fny, int N, int forward) { fftrn3_f(f, fny, N, forward); }
+void ieo_fftc1_d(double* f, int n, int skip, int forward) { fftc1_d(f, n, skip, forward); }
+
+/* ------------------------------------------------------------------------- */
+/* spectra, src/output.cpp:63-151 and 466-625                                */
+/* ------------------------------------------------------------------------- */
+
+int ieo_numbins(int N) { return (int)(1.73205 * (N / 2)) + 1; }
+
+/* write_isotropic_spectrum_from_fft_r2c binning, src/output.cpp:63-151.
+ * Serial in the reference's (i, j, k) order. */
+void ieo_bin_spectrum(int N, const double* ff, const double* nyq, int* counts, double* f2) {
+    const int numbins = ieo_numbins(N);
+    for (int b = 0; b < numbins; ++b) { counts[b] = 0; f2[b] = 0.0; }
+    for (int i = 0; i < N; i++) {
+        const int px = (i <= N / 2 ? i : i - N);
+        for (int j = 0; j < N; j++) {
+            const int py = (j <= N / 2 ? j : j - N);
+            for (int k = 1; k < N / 2; k++) {
+                const int pz = k;
+                const double pm = sqrt(pw2((double)px) + pw2((double)py) + pw2((double)pz));
+                const int bin = (int)lround(pm);
+                if (bin < 0 || bin >= numbins) continue;
+                const double re = ff[IDX(N, i, j, 2 * k)];
+                const double im = ff[IDX(N, i, j, 2 * k + 1)];
+                const double fp2 = re * re + im * im;
+                counts[bin] += 2;
+                f2[bin] += 2.0 * fp2;
+            }
+            for (int k = 0; k <= N / 2; k += N / 2) {
+                const int pz = k;
+                const double pm = sqrt(pw2((double)px) + pw2((double)py) + pw2((double)pz));
+                const int bin = (int)lround(pm);
+                if (bin < 0 || bin >= numbins) continue;
+                double fp2;
+                if (k == 0) {
+                    const double re = ff[IDX(N, i, j, 0)], im = ff[IDX(N, i, j, 1)];
+                    fp2 = re * re + im * im;
+                } else {
+                    const double re = nyq[(size_t)i * 2 * N + 2 * j], im = nyq[(size_t)i * 2 * N + 2 * j + 1];
+                    fp2 = re * re + im * im;
+                }
+                counts[bin] += 1;
+                f2[bin] += fp2;
+            }
+        }
+    }
+}
+
+/* spectraf() without printing, src/output.cpp:297-406 (forcing cutoff off) */
+void ieo_spectrum_f(ieo_state* S, int* counts, double* f2) {
+    const int N = S->p.N;
+    ieo_fftrn_d(S->f, S->fny, N, 1);
+    ieo_bin_spectrum(N, S->f, S->fny, counts, f2);
+    ieo_fftrn_d(S->f, S->fny, N, -1);
+}
+
+/* write_gw_spectrum_impl, src/output.cpp:466-625 (float arithmetic) */
+void ieo_gw_spectrum(ieo_state* S, int which, double to_phys, int* counts, float* f2, double* f2d) {
+    const int N = S->p.N;
+    const double dx = S->p.dx;
+    const double pi = S->pi;
+    const int numbins = (int)(sqrt(3.0) * (N / 2)) + 1;
+    const int i_max_out = (int)floor(0.80 * numbins);
+    float** H = which ? S->hd : S->h;
+    float** HN = which ? S->hdny : S->hny;
+    static const int comp_of[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+    for (int b = 0; b < numbins; ++b) { counts[b] = 0; f2[b] = 0.f; if (f2d) f2d[b] = 0.0; }
+    for (int c = 0; c < 6; ++c) ieo_fftrn_f(H[c], HN[c], N, 1);
+
+    for (int i = 0; i < N; ++i) {
+        const int px = (i <= N / 2 ? i : i - N);
+        for (int j = 0; j < N; ++j) {
+            const int py = (j <= N / 2 ? j : j - N);
+            /* interior modes, src/output.cpp:490-547 */
+            for (int k = 1; k < N / 2; ++k) {
+                const int pz = k;
+                const float kx = (2.f / (float)dx) * sinf((float)pi * px / (float)N);
+                const float ky = (2.f / (float)dx) * sinf((float)pi * py / (float)N);
+                const float kz = (2.f / (float)dx) * sinf((float)pi * pz / (float)N);
+                const float kt2 = kx * kx + ky * ky + kz * kz;
+                if (kt2 == 0.f) continue;
+                const int bin = (int)lroundf(sqrtf((float)(px * px + py * py + pz * pz)));
+                if (bin >= i_max_out) continue;
+                const size_t im_ = IDX(N, i, j, 2 * k);
+                float Cr[3][3], Ci[3][3];
+                for (int l = 0; l < 3; ++l) for (int m = 0; m < 3; ++m) {
+                    const int cc = comp_of[l][m];
+                    float re = H[cc][im_], imv = H[cc][im_ + 1];
+                    if (which) { re = (float)((double)re * to_phys); imv = (float)((double)imv * to_phys); }
+                    Cr[l][m] = re; Ci[l][m] = imv;
+                }
+                const float inv = 1.0f / sqrtf(kt2);
+                const float kh[3] = {kx * inv, ky * inv, kz * inv};
+                float P[3][3];
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) P[a][b] = (a == b ? 1.f : 0.f) - kh[a] * kh[b];
+                float Ar[3][3], Ai[3][3], Tr = 0.f, Ti = 0.f;
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) {
+                    float r = 0.f, q = 0.f;
+                    for (int l = 0; l < 3; ++l) for (int m = 0; m < 3; ++m) {
+                        const float pal = P[a][l], pbm = P[b][m];
+                        r += pal * Cr[l][m] * pbm;
+                        q += pal * Ci[l][m] * pbm;
+                    }
+                    Ar[a][b] = r; Ai[a][b] = q;
+                }
+                for (int l = 0; l < 3; ++l) for (int m = 0; m < 3; ++m) { Tr += P[l][m] * Cr[l][m]; Ti += P[l][m] * Ci[l][m]; }
+                float fp2 = 0.f;
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) {
+                    const float Xr = Ar[a][b] - 0.5f * P[a][b] * Tr;
+                    const float Xi = Ai[a][b] - 0.5f * P[a][b] * Ti;
+                    fp2 += Xr * Xr + Xi * Xi;
+                }
+                counts[bin] += 2;
+                f2[bin] += 2.f * fp2;
+                if (f2d) f2d[bin] += (double)(2.f * fp2);
+            }
+            /* special planes k = 0 and k = N/2, src/output.cpp:550-612 */
+            for (int q2 = 0; q2 <= 1; ++q2) {
+                const int k = q2 * (N / 2);
+                const int pz = k;
+                const float kx = (2.f / (float)dx) * sinf((float)pi * px / (float)N);
+                const float ky = (2.f / (float)dx) * sinf((float)pi * py / (float)N);
+                const float kz = (2.f / (float)dx) * sinf((float)pi * pz / (float)N);
+                const float kt2 = kx * kx + ky * ky + kz * kz;
+                if (kt2 == 0.f) continue;
+                const int bin = (int)lroundf(sqrtf((float)(px * px + py * py + pz * pz)));
+                if (bin >= i_max_out) continue;
+                float Cr[3][3], Ci[3][3];
+                for (int l = 0; l < 3; ++l) for (int m = 0; m < 3; ++m) {
+                    const int cc = comp_of[l][m];
+                    float re, imv;
+                    if (k == 0) { re = H[cc][IDX(N, i, j, 0)]; imv = H[cc][IDX(N, i, j, 0) + 1]; }
+                    else { re = HN[cc][(size_t)i * 2 * N + 2 * j]; imv = HN[cc][(size_t)i * 2 * N + 2 * j + 1]; }
+                    if (which) { re = (float)((double)re * to_phys); imv = (float)((double)imv * to_phys); }
+                    Cr[l][m] = re; Ci[l][m] = imv;
+                }
+                const float inv = 1.0f / sqrtf(kt2);
+                const float kh[3] = {kx * inv, ky * inv, kz * inv};
+                float P[3][3];
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) P[a][b] = (a == b ? 1.f : 0.f) - kh[a] * kh[b];
+                float Ar[3][3], Ai[3][3], Tr = 0.f, Ti = 0.f;
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) {
+                    float r = 0.f, q = 0.f;
+                    for (int l = 0; l < 3; ++l) for (int m = 0; m < 3; ++m) {
+                        const float pal = P[a][l], pbm = P[b][m];
+                        r += pal * Cr[l][m] * pbm;
+                        q += pal * Ci[l][m] * pbm;
+                    }
+                    Ar[a][b] = r; Ai[a][b] = q;
+                }
+                for (int l = 0; l < 3; ++l) for (int m = 0; m < 3; ++m) { Tr += P[l][m] * Cr[l][m]; Ti += P[l][m] * Ci[l][m]; }
+                float fp2 = 0.f;
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) {
+                    const float Xr = Ar[a][b] - 0.5f * P[a][b] * Tr;
+                    const float Xi = Ai[a][b] - 0.5f * P[a][b] * Ti;
+                    fp2 += Xr * Xr + Xi * Xi;
+                }
+                counts[bin] += 1;
+                f2[bin] += fp2;
+                if (f2d) f2d[bin] += (double)fp2;
+            }
+        }
+    }
+    for (int c = 0; c < 6; ++c) ieo_fftrn_f(H[c], HN[c], N, -1);
+}
+
+/* ------------------------------------------------------------------------- */
+/* deltaN, src/evolution.cpp:1004-1375                                       */
+/* ------------------------------------------------------------------------- */
+
+/* initializeN(), src/initialize.cpp:219-232 */
+int ieo_initializeN(ieo_state* S) {
+    const double s = S->p.rescale_s;
+    for (size_t id = 0; id < S->gs; ++id) {
+        if (S->p.numerical_potential) S->lstart[id] -= 100;
+        const double H_lat = sqrt(ieo_potential(S, S->f[id]) / 3.0);
+        S->fd[id] = S->fd[id] * pow(S->a, s - 1.0) / H_lat;
+        S->deltaN[id] = 0.0;
+    }
+    return S->err;
+}
+
+/* evolve_derivsN(d), src/evolution.cpp:1004-1012 */
+int ieo_evolve_derivsN(ieo_state* S, double d) {
+    double* fd = S->fd;
+    const long gs = (long)S->gs;
+    #pragma omp parallel for schedule(static)
+    for (long id = 0; id < gs; ++id) {
+        fd[id] += d * (-(3.0 - 0.5 * pw2(fd[id])) * (fd[id] + pot_ratio_site(S, (size_t)id)));
+    }
+    return S->err;
+}
+
+static inline int dn_active(ieo_state* S, double v) {
+    if (S->p.criterion > 0) return fabs(v) > fabs(S->phiref);
+    if (S->p.criterion < 0) return fabs(v) < fabs(S->phiref);
+    return ieo_potential(S, v) > ieo_potential(S, S->phiref);
+}
+
+/* evolve_fieldsN(d), src/evolution.cpp:1015-1037 */
+void ieo_evolve_fieldsN(ieo_state* S, double d) {
+    S->t += d;
+    double* f = S->f;
+    const double* fd = S->fd;
+    double* dn = S->deltaN;
+    const long gs = (long)S->gs;
+    #pragma omp parallel for schedule(static)
+    for (long id = 0; id < gs; ++id) {
+        if (dn_active(S, f[id])) {
+            dn[id] += d;
+            f[id] += d * fd[id];
+        }
+    }
+    S->a += d * S->ad;
+}
+
+/* get_phiref(), src/evolution.cpp:1271-1288 */
+double ieo_get_phiref(ieo_state* S) {
+    double fref = S->f[0];
+    for (size_t id = 0; id < S->gs; ++id) {
+        const double v = S->f[id];
+        int take;
+        if (S->p.criterion > 0) take = fabs(v) < fabs(fref);
+        else if (S->p.criterion < 0) take = fabs(v) > fabs(fref);
+        else take = ieo_potential(S, v) < ieo_potential(S, fref);
+        if (take) fref = v;
+    }
+    return fref;
+}
+
+int ieo_deltaN_steps(ieo_state* S, int max_steps) {
+    int n = 0;
+    while (n < max_steps && S->Ne <= S->p.Nend) {
+        if (ieo_evolve_derivsN(S, S->p.dN)) return -1;
+        ieo_evolve_fieldsN(S, S->p.dN);
+        S->Ne += S->p.dN;
+        ++n;
+    }
+    return n;
+}
+
+/* saveN() float accumulator, src/output.cpp:1527-1537 */
+float ieo_saveN_mean(const ieo_state* S, double cutoff) {
+    float Nmean = 0.f;
+    for (size_t id = 0; id < S->gs; ++id)
+        if (S->deltaN[id] <= cutoff) Nmean = (float)((double)Nmean + S->deltaN[id]);
+    Nmean = Nmean / (float)S->gs;
+    return Nmean;
+}
+
+/* ------------------------------------------------------------------------- */
+/* program, src/main.cpp:103-146 and src/output.cpp                          */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    char dir[1024];
+    FILE *output, *means, *vars, *velocity, *sf, *energy, *conservation, *spectra, *spectratimes,
+         *histogram, *histogramtimes, *spectraGW, *spectraGWdot, *modes, *spectraN, *histogramN,
+         *histogramtimesN, *box2d_phi, *box2d_phidot, *box2d_deltaN, *box3d, *info;
+    time_t tstart;
+} outfiles;
+
+static FILE* open_out(ieo_state* S, outfiles* O, FILE** slot, const char* name) {
+    if (*slot) return *slot;
+    char path[1200];
+    snprintf(path, sizeof path, "%s/%s.dat", O->dir, name);
+    *slot = fopen(path, "w");
+    if (!*slot) set_err(S, "Failed to open output file: %s\n", path);
+    return *slot;
+}
+
+/* write_isotropic_spectrum_from_fft_r2c printing, src/output.cpp:143-150 */
+static void print_spectrum(FILE* out, int N, double L, const int* counts, double* f2, double norm1) {
+    const int numbins = ieo_numbins(N);
+    const double dp = 2.0 * (2.0 * asin(1.0)) / L;
+    for (int i = 0; i < numbins; i++) {
+        const double pi_ = dp * i;
+        if (counts[i] > 0) f2[i] /= (double)counts[i];
+        fprintf(out, "%e %d %e\n", pi_, counts[i], norm1 * f2[i]);
+    }
+    fprintf(out, "\n");
+    fflush(out);
+}
+
+/* meansvars, src/output.cpp:204-269 */
+static int out_meansvars(ieo_state* S, outfiles* O) {
+    FILE* m = open_out(S, O, &O->means, "means");
+    FILE* v = open_out(S, O, &O->vars, "variance");
+    FILE* ve = open_out(S, O, &O->velocity, "velocity");
+    if (S->err) return 1;
+    fprintf(m, "%f", S->t); fprintf(m, " %e", S->a);
+    fprintf(ve, "%f", S->t); fprintf(ve, " %e", S->a);
+    fprintf(v, "%f", S->t); fprintf(v, " %e", S->a);
+    double av = 0., vel = 0., var = 0.;
+    for (size_t id = 0; id < S->gs; ++id) { av += S->f[id]; vel += S->fd[id]; var += pw2(S->f[id]); }
+    av = av / (double)S->gs;
+    vel = vel / (double)S->gs;
+    vel = vel * pow(S->a, S->p.rescale_s - 1.0) * S->p.rescale_B;
+    fprintf(m, " %e", av); fprintf(ve, " %e", vel); fprintf(v, " %e", var - pw2(av));
+    if (av + DBL_MAX == av || (av != 0. && av / av != 1.)) {
+        set_err(S, "Unstable solution developed. Scalar field not numerical at t=%f\n", S->t);
+        fflush(m); fflush(v);
+        return 1;
+    }
+    fprintf(m, "\n"); fprintf(v, "\n"); fprintf(ve, "\n");
+    fflush(m); fflush(v); fflush(ve);
+    return 0;
+}
+
+/* scale, src/output.cpp:272-293 */
+static void out_scale(ieo_state* S, outfiles* O) {
+    FILE* fp = open_out(S, O, &O->sf, "sf");
+    if (!fp) return;
+    const double s = S->p.rescale_s, B = S->p.rescale_B, a = S->a;
+    fprintf(fp, "%f %f %e %e\n", S->t, a, S->ad * B * pow(a, s - 2.0),
+            pw2(B) * pow(a, 2.0 * s - 2.0) * (S->ad2 + (s - 1.0) * pw2(S->ad) / a));
+    fflush(fp);
+}
+
+/* energy, src/output.cpp:983-1026 */
+static int out_energy(ieo_state* S, outfiles* O) {
+    FILE* e = open_out(S, O, &O->energy, "energy");
+    FILE* c = open_out(S, O, &O->conservation, "conservation");
+    if (S->err) return 1;
+    const double B = S->p.rescale_B;
+    double totalE = 0.;
+    fprintf(e, "%f", S->t); fprintf(e, " %e", S->a);
+    const double de = ieo_kin_energy(S); totalE += de; fprintf(e, " %e", de * B);
+    const double ge = ieo_gradient_energy(S); totalE += ge; fprintf(e, " %e", ge * B);
+    const double pe = ieo_potential_energy(S); totalE += pe; fprintf(e, " %e", pe * B);
+    fprintf(e, "\n"); fflush(e);
+    fprintf(c, "%e %e %e\n", S->t, S->a, 3.0 * pow(S->a, 2.0 * S->p.rescale_s - 4.0) * pw2(S->ad) / (totalE));
+    fflush(c);
+    return S->err;
+}
+
+/* histograms / histogramsN, src/output.cpp:1070-1135 and 1220-1277 */
+static void out_histogram(ieo_state* S, const double* x, FILE* hist, FILE* times, int deltaN_style) {
+    const int nbins = S->p.nbins;
+    if (deltaN_style) fprintf(times, "%f %e", S->t, S->a);
+    else { fprintf(times, "%f", S->t); fprintf(times, " %e", S->a); }
+    double bmin = x[0], bmax = bmin;
+    for (size_t id = 0; id < S->gs; ++id) {
+        bmin = (x[id] < bmin ? x[id] : bmin);
+        bmax = (x[id] > bmax ? x[id] : bmax);
+    }
+    double df = (bmax - bmin) / (double)nbins;
+    if (!isfinite(df) || df <= 0.0) df = 1.0;
+    double* binfreq = (double*)calloc(nbins > 0 ? nbins : 1, sizeof(double));
+    int numpts = 0;
+    for (size_t id = 0; id < S->gs; ++id) {
+        int binnum = (int)((x[id] - bmin) / df);
+        if (x[id] == bmax) binnum = nbins - 1;
+        if (binnum >= 0 && binnum < nbins) { binfreq[binnum]++; numpts++; }
+    }
+    if (numpts == 0) numpts = 1;
+    for (int i = 0; i < nbins; i++) fprintf(hist, "%e\n", binfreq[i] / (double)numpts);
+    fprintf(hist, "\n");
+    fflush(hist);
+    if (deltaN_style) fprintf(times, " %e %e\n", bmin, df);
+    else { fprintf(times, " %e %e", bmin, df); fprintf(times, "\n"); }
+    fflush(times);
+    free(binfreq);
+}
+
+static void out_box2d(ieo_state* S, FILE* fp, const double* x, double scale, int scaled) {
+    const int N = S->p.N;
+    const int i = (N < 64) ? 5 : 50;
+    for (int j = 0; j < N; j++) for (int k = 0; k < N; k++) {
+        if (scaled) fprintf(fp, "%.17g\n", x[IDX(N, i, j, k)] * scale);
+        else fprintf(fp, "%.17g\n", x[IDX(N, i, j, k)]);
+    }
+    fprintf(fp, "\n");
+    fflush(fp);
+}
+
+/* spectraGW / spectraGWdot printing, src/output.cpp:618-624 */
+static void out_gw(ieo_state* S, outfiles* O, int which) {
+    FILE* fp = which ? open_out(S, O, &O->spectraGWdot, "spectraGWdot") : open_out(S, O, &O->spectraGW, "spectraGW");
+    if (!fp) return;
+    const int N = S->p.N;
+    const int numbins = (int)(sqrt(3.0) * (N / 2)) + 1;
+    int* counts = (int*)calloc(numbins, sizeof(int));
+    float* f2 = (float*)calloc(numbins, sizeof(float));
+    const double to_phys = which ? S->p.rescale_B * pow(S->a, S->p.rescale_s - 1.0) : 1.0;
+    ieo_gw_spectrum(S, which, to_phys, counts, f2, NULL);
+    const float dp = 2.f * (float)S->pi / (float)S->p.L;
+    const float norm1 = 0.5f * pow(S->p.L / S->p.rescale_B, 3) / pow((double)(float)N, 6);
+    for (int i = 0; i < numbins; ++i) {
+        const float pi_ = dp * i;
+        if (counts[i] > 0) f2[i] /= (float)counts[i];
+        fprintf(fp, "%e %d %e\n", pi_, counts[i], norm1 * f2[i]);
+    }
+    fprintf(fp, "\n");
+    fflush(fp);
+    free(counts); free(f2);
+}
+
+/* save(), src/output.cpp:1469-1503 */
+static int out_save(ieo_state* S, outfiles* O, int infrequent) {
+    const ieo_params* p = &S->p;
+    if (S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt * pow(S->astep, p->rescale_s - 1));
+    if (out_meansvars(S, O)) return 1;
+    out_scale(S, O);
+    if (infrequent) {
+        if (p->output_box3D) {
+            FILE* fp = open_out(S, O, &O->box3d, "box");
+            for (size_t id = 0; id < S->gs; ++id) fprintf(fp, "%.17g\n", S->f[id]);
+            fprintf(fp, "\n");
+        }
+        if (p->output_box2D) {
+            out_box2d(S, open_out(S, O, &O->box2d_phi, "snapshots_2d_phi"), S->f, 0, 0);
+            out_box2d(S, open_out(S, O, &O->box2d_phidot, "snapshots_2d_phidot"), S->fd, p->rescale_B, 1);
+        }
+        if (p->output_energy && out_energy(S, O)) return 1;
+        if (p->output_spectra) {
+            FILE* sp = open_out(S, O, &O->spectra, "spectra");
+            FILE* st = open_out(S, O, &O->spectratimes, "spectratimes");
+            if (S->err) return 1;
+            const int nb = ieo_numbins(p->N);
+            int* counts = (int*)calloc(nb, sizeof(int));
+            double* f2 = (double*)calloc(nb, sizeof(double));
+            const double norm1 = pow(p->L / p->rescale_B, 3) / pow((double)p->N, 6);
+            ieo_fftrn_d(S->f, S->fny, p->N, 1);
+            ieo_bin_spectrum(p->N, S->f, S->fny, counts, f2);
+            print_spectrum(sp, p->N, p->L, counts, f2, norm1);
+            fprintf(st, "%f %e\n", S->t, S->a);
+            fflush(st);
+            if (p->high_cutoff_index > 0 && p->forcing_cutoff) {
+                set_err(S, "forcing_cutoff is not supported by this oracle\n");
+                free(counts); free(f2);
+                return 1;
+            }
+            ieo_fftrn_d(S->f, S->fny, p->N, -1);
+            free(counts); free(f2);
+            if (p->calculate_SIGW) { out_gw(S, O, 0); out_gw(S, O, 1); }
+        }
+        if (p->output_histogram)
+            out_histogram(S, S->f, open_out(S, O, &O->histogram, "histogram"),
+                          open_out(S, O, &O->histogramtimes, "histogramtimes"), 0);
+    }
+    if (S->t > 0.) ieo_evolve_fields(S, .5 * p->dt * pow(S->astep, p->rescale_s - 1));
+    return S->err;
+}
+
+/* get_modes, src/output.cpp:674-738 */
+static void out_modes(ieo_state* S, outfiles* O) {
+    FILE* fp = open_out(S, O, &O->modes, "modes");
+    if (!fp) return;
+    const int N = S->p.N;
+    const double L = S->p.L, pi = S->pi;
+    const int numbins = (int)(sqrt(3.0) * (N / 2)) + 1;
+    int* np = (int*)calloc(numbins + 1, sizeof(int));
+    double* pp = (double*)calloc(numbins + 1, sizeof(double));
+    for (int i = 0; i < N; i++) {
+        const int px = (i <= N / 2 ? i : i - N);
+        for (int j = 0; j < N; j++) {
+            const int py = (j <= N / 2 ? j : j - N);
+            for (int k = 1; k < N / 2; k++) {
+                const int pz = k;
+                const double pm = sqrt(pw2((double)px) + pw2((double)py) + pw2((double)pz));
+                const double pph = sqrt(4.0 * pw2((double)N / (double)L) * (pw2(sin((double)px * pi / N)) + pw2(sin((double)py * pi / N)) + pw2(sin((double)pz * pi / N))));
+                np[(int)pm] += 2;
+                pp[(int)pm] += 2.0 * pph;
+            }
+            for (int k = 0; k <= N / 2; k += N / 2) {
+                const int pz = k;
+                const double pm = sqrt(pw2((double)px) + pw2((double)py) + pw2((double)pz));
+                const double pph = sqrt(4.0 * pw2((double)N / (double)L) * (pw2(sin((double)px * pi / N)) + pw2(sin((double)py * pi / N)) + pw2(sin((double)pz * pi / N))));
+                np[(int)pm]++;
+                pp[(int)pm] += pph;
+            }
+        }
+    }
+    for (int i = 0; i < numbins; i++) {
+        if (np[i] > 0) pp[i] = pp[i] / np[i];
+        fprintf(fp, "%e\n", S->p.rescale_B * pp[i]);
+    }
+    fprintf(fp, "\n");
+    fflush(fp);
+    free(np); free(pp);
+}
+
+/* saveN(), src/output.cpp:1522-1560, with spectraN() of :1140-1169 */
+static int out_saveN(ieo_state* S, outfiles* O) {
+    const ieo_params* p = &S->p;
+    if (S->t > 0.) ieo_evolve_fieldsN(S, -.5 * p->dN);
+    const double cutoff = p->Nend - p->dN;
+    const float Nmean = ieo_saveN_mean(S, cutoff);
+    for (size_t id = 0; id < S->gs; ++id) S->deltaN[id] -= Nmean;
+    out_histogram(S, S->deltaN, open_out(S, O, &O->histogramN, "histogramN"),
+                  open_out(S, O, &O->histogramtimesN, "histogramtimesN"), 1);
+    if (p->output_box2D) out_box2d(S, open_out(S, O, &O->box2d_deltaN, "snapshots_2d_deltaN"), S->deltaN, 0, 0);
+    for (size_t id = 0; id < S->gs; ++id)
+        if (S->deltaN[id] > (cutoff - Nmean)) S->deltaN[id] = 0;
+    if (p->output_spectra) {
+        FILE* sp = open_out(S, O, &O->spectraN, "spectraN");
+        if (!sp) return 1;
+        double m = 0.0;
+        for (size_t id = 0; id < S->gs; ++id) m += S->deltaN[id];
+        m /= (double)S->gs;
+        for (size_t id = 0; id < S->gs; ++id) S->deltaN[id] -= m;
+        const int nb = ieo_numbins(p->N);
+        int* counts = (int*)calloc(nb, sizeof(int));
+        double* f2 = (double*)calloc(nb, sizeof(double));
+        const double norm1 = pow(p->L / p->rescale_B, 3) / pow((double)p->N, 6);
+        ieo_fftrn_d(S->deltaN, S->fny, p->N, 1);
+        ieo_bin_spectrum(p->N, S->deltaN, S->fny, counts, f2);
+        print_spectrum(sp, p->N, p->L, counts, f2, norm1);
+        ieo_fftrn_d(S->deltaN, S->fny, p->N, -1);
+        free(counts); free(f2);
+    }
+    if (S->t > 0.) ieo_evolve_fieldsN(S, .5 * p->dN);
+    return S->err;
+}
+
+static int load_table_file(const char* path, double** out, int* n) {
+    FILE* fp = fopen(path, "r");
+    if (!fp) return -1;
+    int cap = 2048, m = 0;
+    double* v = (double*)malloc(sizeof(double) * cap);
+    double x;
+    while (fscanf(fp, "%lf", &x) == 1) {
+        if (m == cap) { cap *= 2; v = (double*)realloc(v, sizeof(double) * cap); }
+        v[m++] = x;
+    }
+    fclose(fp);
+    if (m == 0) { free(v); return -2; }
+    *out = v;
+    *n = m;
+    return 0;
+}
+
+static void close_all(outfiles* O) {
+    FILE** all[] = {&O->output, &O->means, &O->vars, &O->velocity, &O->sf, &O->energy, &O->conservation,
+                    &O->spectra, &O->spectratimes, &O->histogram, &O->histogramtimes, &O->spectraGW,
+                    &O->spectraGWdot, &O->modes, &O->spectraN, &O->histogramN, &O->histogramtimesN,
+                    &O->box2d_phi, &O->box2d_phidot, &O->box2d_deltaN, &O->box3d, &O->info};
+    for (size_t q = 0; q < sizeof(all) / sizeof(all[0]); ++q)
+        if (*all[q]) { fclose(*all[q]); *all[q] = NULL; }
+}
+
+int ieo_run_program(const ieo_params* p, const char* results_dir, const char* inputs_dir) {
+    outfiles O;
+    memset(&O, 0, sizeof O);
+    snprintf(O.dir, sizeof O.dir, "%s", results_dir);
+    mkdir(results_dir, 0777);
+    ieo_state* S = ieo_create(p);
+    if (!S) return 1;
+    int rc = 1;
+    char path[1200];
+    snprintf(path, sizeof path, "%s/output.txt", results_dir);
+    O.output = fopen(path, "w");
+    if (!O.output) goto done;
+    if (p->numerical_potential) {
+        double *x = NULL, *V = NULL, *dV = NULL;
+        int n1, n2, n3;
+        char q[1200];
+        snprintf(q, sizeof q, "%s/field_values.dat", inputs_dir);
+        if (load_table_file(q, &x, &n1)) goto done;
+        snprintf(q, sizeof q, "%s/potential.dat", inputs_dir);
+        if (load_table_file(q, &V, &n2)) goto done;
+        snprintf(q, sizeof q, "%s/potential_derivative.dat", inputs_dir);
+        if (load_table_file(q, &dV, &n3)) goto done;
+        ieo_set_table(S, x, V, dV, n1);
+        free(x); free(V); free(dV);
+    }
+    /* initialize_simulation(), src/initialize.cpp:40-48 */
+    if (ieo_initialize(S)) goto done;
+    if (ieo_initializef(S)) goto done;
+    ieo_initializeGW(S);
+    {
+        FILE* info = open_out(S, &O, &O.info, "info");
+        time(&O.tstart);
+        if (info) { fprintf(info, "Grid size=%d^%d\nL=%f\n", p->N, 3, p->L); fflush(info); }
+    }
+    if (out_save(S, &O, 1)) goto done;
+    S->t = S->t0;
+
+    /* run_evolution_loop(), leapfrog branch, src/evolution.cpp:909-997 */
+    {
+        int numsteps = 0;
+        ieo_evolve_fields(S, 0.5 * p->dt);
+        while (S->a <= p->af) {
+            const double d = ieo_rescaled_step(S, S->astep);
+            if (ieo_evolve_derivs(S, d)) goto done;
+            ieo_evolve_fields(S, d);
+            numsteps++;
+            if (numsteps % p->output_freq == 0 && S->a < p->af)
+                if (out_save(S, &O, (numsteps % p->output_infrequent_freq == 0) ? 1 : 0)) goto done;
+            fprintf(O.output, "scale factor a = %f\n", S->a);
+            fprintf(O.output, "numsteps %i\n\n", numsteps);
+            if (numsteps % p->output_freq == 0) fflush(O.output);
+            S->astep = S->a;
+        }
+        fflush(O.output);
+        if (out_save(S, &O, 1)) goto done;
+        ieo_evolve_fields(S, -0.5 * ieo_rescaled_step(S, S->astep));
+        out_modes(S, &O);
+    }
+
+    /* run_deltaN_loop(), leapfrog branch, src/evolution.cpp:1291-1375 */
+    if (p->perform_deltaN) {
+        fprintf(O.output, "Starting deltaN calculation\n");
+        int numsteps = 0;
+        S->Ne = 0.0;
+        if (ieo_initializeN(S)) goto done;
+        ieo_evolve_fieldsN(S, 0.5 * p->dN);
+        S->phiref = p->use_phiref_manual ? p->phiref_manual_value : ieo_get_phiref(S);
+        while (S->Ne <= p->Nend) {
+            if (ieo_evolve_derivsN(S, p->dN)) goto done;
+            ieo_evolve_fieldsN(S, p->dN);
+            S->Ne += p->dN;
+            numsteps++;
+            fprintf(O.output, "N = %f\n\n", S->Ne);
+            if (numsteps % p->output_freq == 0) fflush(O.output);
+        }
+        if (out_saveN(S, &O)) goto done;
+        fflush(O.output);
+        ieo_evolve_fieldsN(S, -0.5 * p->dN);
+    }
+    fprintf(O.output, "InflationEasy program finished\n");
+    rc = 0;
+done:
+    if (rc && S->err) {
+        fprintf(stderr, "%s", S->errmsg);
+    }
+    close_all(&O);
+    ieo_destroy(S);
+    return rc;
+}

@@ -1,0 +1,145 @@
+/*
+ * ieo.h -- CPU oracle for the InflationEasy lattice hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA engine
+ * is compared against; it is never linked into, loaded by, or called from the
+ * product (libiegpu / ie_gpu_main).  Only tests/, __graft_entry__.smoke() and
+ * the cpu_baseline / --impl reference legs of bench.py may use it.
+ *
+ * It restates, in plain C with explicit state (no globals), the algorithm of
+ * caravangelo/inflation-easy for the leapfrog evolution path, keeping every
+ * floating-point operation in the reference's order so that results are
+ * bit-identical to the reference built from source (see oracle/build_ref.py and
+ * tests/test_oracle_pin.py).  Each function cites the reference file:line it
+ * follows.  Parity status: pinned (bit-exact against the reference program at
+ * N=16/32, hilltop and tabulated potentials, SIGW on/off, deltaN on).
+ *
+ * Lattice layout: flat index (i*N + j)*N + k, k fastest (src/main.h:34-38).
+ * N is a run-time value here (the reference fixes it at compile time).
+ */
+#ifndef IEO_H
+#define IEO_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Run-time parameters, one field per params.txt key of
+ * src/runtime_parameters.cpp:17-112 plus the compile-time switches of
+ * src/parameters.h:22-66 (here run-time). */
+typedef struct {
+    int N;
+    int numerical_potential;   /* 0: hilltop (src/potential.cpp:77-83), 1: table */
+    int perform_deltaN;
+    int calculate_SIGW;
+    int criterion;             /* +1 monotonic, -1 antimonotonic, 0 generic (src/parameters.h:60-66) */
+    int seed;
+    double rescale_s, af, V0, rescale_B, ns;
+    double initial_field, initial_derivative, L, dt;
+    int output_freq, output_infrequent_freq;
+    double dN, Nend;
+    int use_phiref_manual;
+    double phiref_manual_value;
+    double high_cutoff_index, low_cutoff_index;
+    int forcing_cutoff;
+    int output_spectra, output_histogram, output_energy, output_box3D, output_box2D;
+    int screen_updates, nbins, int_err, int_errN;
+    double dx;
+} ieo_params;
+
+typedef struct ieo_state ieo_state;
+
+/* Defaults of src/runtime_parameters.cpp:17-112 for a given N and potential. */
+void ieo_params_defaults(ieo_params* p, int N, int numerical_potential);
+/* params.txt parser following src/runtime_parameters.cpp:195-365 (plus the
+ * keys N, numerical_potential, perform_deltaN, calculate_SIGW, which the
+ * reference fixes at compile time).  Returns 0, or -1 if the file is missing. */
+int ieo_params_load(ieo_params* p, const char* path);
+/* Derived quantities (rescale_B default, af default, dx):
+ * src/runtime_parameters.cpp:342-354. */
+void ieo_params_finalize(ieo_params* p, int rescale_B_given, int af_given);
+
+ieo_state* ieo_create(const ieo_params* p);
+void ieo_destroy(ieo_state* S);
+void ieo_set_threads(int n);
+const ieo_params* ieo_get_params(const ieo_state* S);
+
+/* Tabulated potential: phi must be sorted descending (src/potential.cpp:18). */
+int ieo_set_table(ieo_state* S, const double* phi, const double* V, const double* dV, int n);
+
+/* Field access (pointers into the state; N^3 elements). */
+double* ieo_f(ieo_state* S);
+double* ieo_fd(ieo_state* S);
+double* ieo_deltaN(ieo_state* S);
+double* ieo_fnyquist(ieo_state* S);   /* N x 2N */
+double* ieo_fdnyquist(ieo_state* S);
+float*  ieo_h(ieo_state* S, int c);
+float*  ieo_hd(ieo_state* S, int c);
+
+typedef struct { double t, a, ad, ad2, astep, Ne, phiref, hubble_init; } ieo_scalars;
+void ieo_get_scalars(const ieo_state* S, ieo_scalars* out);
+void ieo_set_scalars(ieo_state* S, const ieo_scalars* in);
+
+/* Error reporting: the reference prints and exit(1)s; the oracle records the
+ * message and returns nonzero from the calling function. */
+const char* ieo_last_error(const ieo_state* S);
+
+/* ---- RNG + initial conditions: src/initialize.cpp:18-232 ---- */
+double ieo_rand_uniform(ieo_state* S);
+int ieo_initialize(ieo_state* S);      /* src/initialize.cpp:93-114 */
+int ieo_initializef(ieo_state* S);     /* src/initialize.cpp:118-214 */
+void ieo_initializeGW(ieo_state* S);   /* src/initialize.cpp:236-243 */
+
+/* ---- potential: src/potential.cpp ---- */
+double ieo_potential(ieo_state* S, double v);
+double ieo_potential_energy(ieo_state* S);
+
+/* ---- leapfrog: src/evolution.cpp ---- */
+double ieo_gradient_energy(ieo_state* S);
+double ieo_kin_energy(ieo_state* S);
+int ieo_evolve_derivs(ieo_state* S, double d);
+void ieo_evolve_fields(ieo_state* S, double d);
+double ieo_rescaled_step(const ieo_state* S, double astep);
+/* Runs `nsteps` iterations of the leapfrog loop body of
+ * src/evolution.cpp:937-945 without output; stops early once a > af.
+ * Returns the number of steps taken (or -1 on error). */
+int ieo_leapfrog_steps(ieo_state* S, int nsteps);
+
+/* ---- FFT: src/ffteasy.hpp ---- */
+void ieo_fftrn_d(double* f, double* fny, int N, int forward);
+void ieo_fftrn_f(float* f, float* fny, int N, int forward);
+void ieo_fftc1_d(double* f, int n, int skip, int forward);
+
+/* ---- spectra: src/output.cpp:63-151 (without printing) ---- */
+int ieo_numbins(int N);
+/* Bins an r2c field already in k-space; f2 holds the raw sums (before /count). */
+void ieo_bin_spectrum(int N, const double* field_fft, const double* nyq, int* counts, double* f2);
+/* spectraf(): forward FFT of f, bin, inverse FFT (f is modified in place at
+ * round-off level, as in the reference). */
+void ieo_spectrum_f(ieo_state* S, int* counts, double* f2);
+/* GW TT spectrum, src/output.cpp:466-625.  mode: 0 = h, 1 = hd (DoubleThenFloat
+ * scaling with to_phys).  f2_float gets the reference's float accumulators;
+ * f2_double (may be NULL) gets the same per-mode float values summed in double. */
+void ieo_gw_spectrum(ieo_state* S, int which, double to_phys, int* counts, float* f2_float, double* f2_double);
+
+/* ---- deltaN: src/evolution.cpp:1004-1375, src/initialize.cpp:219-232 ---- */
+int ieo_initializeN(ieo_state* S);
+int ieo_evolve_derivsN(ieo_state* S, double d);
+void ieo_evolve_fieldsN(ieo_state* S, double d);
+double ieo_get_phiref(ieo_state* S);
+/* Loop of src/evolution.cpp:1321-1329 (no output).  Returns steps taken. */
+int ieo_deltaN_steps(ieo_state* S, int max_steps);
+/* saveN float-accumulator mean, src/output.cpp:1527-1537. */
+float ieo_saveN_mean(const ieo_state* S, double cutoff);
+
+/* Whole program, src/main.cpp:103-146, writing the reference's results/ .dat
+ * files into results_dir (inputs_dir holds field_values.dat, potential.dat,
+ * potential_derivative.dat when numerical_potential = 1). */
+int ieo_run_program(const ieo_params* p, const char* results_dir, const char* inputs_dir);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,67 @@
+// ref_driver.cpp -- full-precision dump driver for the reference program.
+//
+// TEST INFRASTRUCTURE ONLY.  oracle/build_ref.py compiles the unmodified
+// reference sources (src/*.cpp of caravangelo/inflation-easy, with only the
+// compile-time lines of src/parameters.h set per configuration) together with
+// this file.  The reference's main() (src/main.cpp:103-146) is compiled as
+// ie_ref_main() and run unchanged; this driver only observes it:
+//   * the linker wraps save(int) and saveN() (--wrap) so the background
+//     scalars are traced at full precision each time the reference saves;
+//   * after the run the final lattice state is written in binary.
+// Usage: ie_ref <workdir>   (workdir holds params.txt and inputs/)
+#include "main.h"
+
+#include <cstdio>
+#include <cstring>
+#include <unistd.h>
+
+int ie_ref_main();
+
+static FILE* g_trace = nullptr;
+
+extern "C" void __real__Z4savei(int);
+extern "C" void __wrap__Z4savei(int infrequent) {
+    if (g_trace)
+        std::fprintf(g_trace, "save %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, t, a, ad, ad2, astep);
+    __real__Z4savei(infrequent);
+}
+
+#if perform_deltaN
+extern "C" void __real__Z5saveNv();
+extern "C" void __wrap__Z5saveNv() {
+    if (g_trace) std::fprintf(g_trace, "saveN %.17g %.17g %.17g %.17g\n", t, a, Ne, phiref);
+    __real__Z5saveNv();
+}
+#endif
+
+template <typename T>
+static void dump(FILE* fp, const std::vector<T>& v) {
+    std::fwrite(v.data(), sizeof(T), v.size(), fp);
+}
+
+int main(int argc, char** argv) {
+    if (argc < 2 || chdir(argv[1]) != 0) {
+        std::fprintf(stderr, "usage: ie_ref <workdir>\n");
+        return 2;
+    }
+    g_trace = std::fopen("trace.txt", "w");
+    const int rc = ie_ref_main();
+    std::fclose(g_trace);
+    g_trace = nullptr;
+    FILE* fp = std::fopen("state.bin", "wb");
+    const double scal[8] = {t, a, ad, ad2, astep, Ne, phiref, hubble_init};
+    const int hdr[4] = {N, perform_deltaN, calculate_SIGW, numerical_potential};
+    std::fwrite(hdr, sizeof(int), 4, fp);
+    std::fwrite(scal, sizeof(double), 8, fp);
+    dump(fp, f);
+    dump(fp, fd);
+#if perform_deltaN
+    dump(fp, deltaN);
+#endif
+#if calculate_SIGW
+    for (int c = 0; c < 6; ++c) dump(fp, hij[c]);
+    for (int c = 0; c < 6; ++c) dump(fp, hijd[c]);
+#endif
+    std::fclose(fp);
+    return rc;
+}
