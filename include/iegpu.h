@@ -1,0 +1,195 @@
+/*
+ * iegpu.h -- C ABI of the GB300 (sm_103a) InflationEasy evolution engine.
+ *
+ * The reference program (caravangelo/inflation-easy) reaches its physics
+ * through free functions over global state (src/main.h:137-205).  This header
+ * is the drop-in boundary for that hot path: each entry point names the
+ * reference function it replaces.  The host keeps the reference's driver,
+ * params.txt handling and output formats; the lattice state lives on the GPU
+ * inside an opaque context.
+ *
+ * Conventions
+ *  - Every call returns an int status (IEGPU_OK = 0).  Nothing exits or
+ *    throws across the ABI; iegpu_last_error() gives the message the
+ *    reference would have printed before exit(1).
+ *  - Host arrays use the reference layout: N^3 values, flat index
+ *    (i*N + j)*N + k, k fastest (src/main.h:34-38); Nyquist planes are N x 2N
+ *    (src/main.cpp:27-29).  Arrays are copied; no pointer is retained.
+ *  - Background scalars (t, a, ad, ad2, astep) travel in iegpu_bg and the
+ *    host copy is authoritative between calls.
+ *  - One context = one lattice = one CUDA stream; a context is not
+ *    re-entrant.  Calls are stream-ordered and synchronise before returning
+ *    results to the host.
+ */
+#ifndef IEGPU_H
+#define IEGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct iegpu_ctx iegpu_ctx;
+
+/* ---- status codes ---------------------------------------------------- */
+#define IEGPU_OK            0
+#define IEGPU_EINVAL        1  /* bad argument or configuration */
+#define IEGPU_ECUDA         2  /* CUDA runtime error */
+#define IEGPU_ERANGE        3  /* field outside the potential table, src/potential.cpp:19-27 */
+#define IEGPU_ENAN          4  /* non-finite field mean, src/output.cpp:251-258 */
+#define IEGPU_ECOURANT      5  /* dt > dx/sqrt(3), src/initialize.cpp:94-97 */
+#define IEGPU_ENOMEM        6  /* device allocation failed */
+#define IEGPU_ETABLE        7  /* repeated table nodes, src/potential.cpp:62-65 */
+#define IEGPU_EUNSUPPORTED  8  /* feature not available in this form */
+#define IEGPU_ETIMEOUT      9  /* a bounded device wait gave up */
+
+/* ---- configuration --------------------------------------------------- */
+#define IEGPU_POT_HILLTOP   0  /* analytic hilltop, src/potential.cpp:77-83 */
+#define IEGPU_POT_TABLE     1  /* tabulated V, V' (numerical_potential = 1) */
+
+#define IEGPU_FORM_FP64     0  /* plain FP64: per-site arithmetic in the reference's order */
+#define IEGPU_FORM_SPLIT    1  /* FP32 perturbations about an FP64 background */
+
+#define IEGPU_CRIT_GENERIC        0  /* evolve while V(phi) > V(phiref) */
+#define IEGPU_CRIT_MONOTONIC      1  /* evolve while |phi| > |phiref| */
+#define IEGPU_CRIT_ANTIMONOTONIC (-1) /* evolve while |phi| < |phiref| */
+
+typedef struct {
+    int N;            /* points per side: power of two, 8 <= N <= 1024 (src/parameters.h:42-44) */
+    int potential;    /* IEGPU_POT_*            (src/parameters.h:26)  */
+    int sigw;         /* evolve h_ij            (calculate_SIGW)        */
+    int form;         /* IEGPU_FORM_*                                    */
+    int criterion;    /* IEGPU_CRIT_*           (src/parameters.h:60-66) */
+    double L;         /* comoving box size                               */
+    double dt;        /* base time step                                  */
+    double rescale_s; /* field-rescaling exponent                        */
+    double rescale_B; /* time rescaling B                                */
+    double V0, ns;    /* hilltop parameters                              */
+} iegpu_config;
+
+/* Background scalars of src/main.cpp:31-33. */
+typedef struct {
+    double t, a, ad, ad2, astep;
+} iegpu_bg;
+
+/* Field selectors for upload/download/FFT/spectra. */
+#define IEGPU_F       0   /* phi             (f)        */
+#define IEGPU_FD      1   /* phi'            (fd)       */
+#define IEGPU_DELTAN  2   /* deltaN map      (deltaN)   */
+#define IEGPU_H(c)   (8 + (c))   /* h_ij packed component c = 0..5 (xx,yy,zz,xy,xz,yz) */
+#define IEGPU_HD(c)  (16 + (c))  /* h_ij' */
+
+/* ---- context ---------------------------------------------------------- */
+int  iegpu_version(void);
+const char* iegpu_strerror(int code);
+/* Allocates the device state for one lattice.  Replaces the global vectors
+ * of src/main.cpp:16-29 and the sizing in src/initialize.cpp:118-120. */
+int  iegpu_create(const iegpu_config* cfg, struct iegpu_ctx** out);
+int  iegpu_destroy(struct iegpu_ctx* ctx);
+const char* iegpu_last_error(const struct iegpu_ctx* ctx);
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void* iegpu_stream(struct iegpu_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+long long iegpu_launch_count(const struct iegpu_ctx* ctx);
+
+/* Tabulated potential (inputs/field_values.dat, potential.dat,
+ * potential_derivative.dat; src/main.cpp:46-50).  phi sorted descending. */
+int  iegpu_set_table(struct iegpu_ctx* ctx, const double* phi, const double* V, const double* dV, int n);
+
+/* ---- state transfer --------------------------------------------------- */
+/* field: IEGPU_F, IEGPU_FD, IEGPU_DELTAN (double), IEGPU_H(c), IEGPU_HD(c)
+ * (float).  nyquist (N x 2N, same type) may be NULL. */
+int  iegpu_upload(struct iegpu_ctx* ctx, int field, const void* host, const void* nyquist);
+int  iegpu_download(struct iegpu_ctx* ctx, int field, void* host, void* nyquist);
+/* x += value at every site (initializef background add, src/initialize.cpp:197-200). */
+int  iegpu_add(struct iegpu_ctx* ctx, int field, double value);
+
+/* ---- initial conditions (src/initialize.cpp) -------------------------- */
+/* initialize() + initializef(), src/initialize.cpp:93-214, on the device:
+ * Bunch-Davies modes with the reference's Park-Miller stream (seed; seed < 1
+ * gives the reference's constant 0.33 draws), the zero mode removed, the
+ * inverse r2c FFT, and the homogeneous values phi0, dphi0 added.  The mode
+ * cutoff of set_mode applies when high_cutoff_index > 0.  *hubble_init
+ * receives sqrt((kinetic + potential + gradient)/3) of the new lattice at
+ * a = 1 (src/initialize.cpp:202-212).  Fails with IEGPU_ECOURANT when
+ * dt > dx/sqrt(3). */
+int  iegpu_bunch_davies(struct iegpu_ctx* ctx, int seed, double phi0, double dphi0,
+                        double high_cutoff_index, double low_cutoff_index, double* hubble_init);
+
+/* ---- leapfrog (src/evolution.cpp) ------------------------------------- */
+/* evolve_fields(d), src/evolution.cpp:260-284: t += d; f += d fd; h += d hd; a += d ad. */
+int  iegpu_evolve_fields(struct iegpu_ctx* ctx, double d, iegpu_bg* bg);
+/* evolve_derivs(d), src/evolution.cpp:150-257: Friedmann half-kicks of ad
+ * around the kick of fd (and hd when SIGW is on). */
+int  iegpu_evolve_derivs(struct iegpu_ctx* ctx, double d, iegpu_bg* bg);
+/* The leapfrog branch of run_evolution_loop, src/evolution.cpp:937-945:
+ *   while (a <= af && steps < max_steps) {
+ *       d = dt*astep^(s-1); evolve_derivs(d); evolve_fields(d); astep = a; }
+ * runs entirely on the device (CUDA graph).  *steps_taken receives the number
+ * of steps; a_trace (may be NULL) receives a after each step, as written to
+ * results/output.txt by report_step (src/evolution.cpp:926-927). */
+int  iegpu_leapfrog(struct iegpu_ctx* ctx, double af, int max_steps, iegpu_bg* bg,
+                    int* steps_taken, double* a_trace);
+/* kin_energy(), gradient_energy(), potential_energy():
+ * src/evolution.cpp:130-145, src/potential.cpp:151-171.  out[3] = {kin, grad, pot}. */
+int  iegpu_energies(struct iegpu_ctx* ctx, const iegpu_bg* bg, double out[3]);
+
+/* ---- measurement ------------------------------------------------------ */
+/* CUDA events recorded on the context's stream: start, then stop returns the
+ * elapsed device time in milliseconds (synchronising on the stop event). */
+int  iegpu_timer_start(struct iegpu_ctx* ctx);
+int  iegpu_timer_stop(struct iegpu_ctx* ctx, float* ms);
+/* Like iegpu_leapfrog, but each kernel is launched on its own with a pair of
+ * CUDA events around it; ms_out[0] accumulates the reduction kernel's device
+ * time, ms_out[1] the kick/drift kernel's.  For profiling only. */
+int  iegpu_profile_leapfrog(struct iegpu_ctx* ctx, double af, int nsteps, iegpu_bg* bg, double* ms_out, int nk);
+
+/* ---- diagnostics (src/output.cpp) ------------------------------------- */
+/* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */
+int  iegpu_means(struct iegpu_ctx* ctx, double out[3]);
+/* histograms()/histogramsN(), src/output.cpp:1070-1135/1220-1277.
+ * freq[nbins] = counts / numpts; *bmin, *df as printed to histogramtimes.
+ * 1 <= nbins <= 8192. */
+int  iegpu_histogram(struct iegpu_ctx* ctx, int field, int nbins, double* bmin, double* df, double* freq);
+/* fftrnd / fftrnf of src/ffteasy.hpp:127-190 in place on a device field and
+ * its Nyquist plane (forward = +1 or -1). */
+int  iegpu_fft(struct iegpu_ctx* ctx, int field, int forward);
+/* Number of spectrum bins: (int)(1.73205*(N/2)) + 1, src/output.cpp:69. */
+int  iegpu_numbins(int N);
+/* spectraf() / spectraN() core, src/output.cpp:297-406, 1140-1169: forward
+ * FFT, isotropic binning (write_isotropic_spectrum_from_fft_r2c,
+ * src/output.cpp:63-151), inverse FFT.  counts[nbins] (exact integers) and
+ * f2[nbins] = sum of weighted |X_k|^2 per bin (before /count and norm1). */
+int  iegpu_spectrum(struct iegpu_ctx* ctx, int field, int* counts, double* f2, int nbins);
+/* spectraGW()/spectraGWdot() core, src/output.cpp:466-648: forward FFT of
+ * the six h (which = 0) or h' (which = 1, scaled by to_phys), TT projection
+ * per mode in float as the reference, binning (bins < floor(0.8*numbins)),
+ * inverse FFT.  f2 accumulates the per-mode float values in double. */
+int  iegpu_gw_spectrum(struct iegpu_ctx* ctx, int which, double to_phys, int* counts, double* f2, int nbins);
+
+/* ---- deltaN (src/evolution.cpp:1004-1375) ----------------------------- */
+/* initializeN(), src/initialize.cpp:219-232: fd <- fd*a^(s-1)/sqrt(V/3), deltaN = 0. */
+int  iegpu_initializeN(struct iegpu_ctx* ctx, double a);
+/* get_phiref(), src/evolution.cpp:1271-1288 (first extremal site in loop order). */
+int  iegpu_get_phiref(struct iegpu_ctx* ctx, double* phiref);
+/* evolve_fieldsN(d) (src/evolution.cpp:1015-1037) on the lattice; the scalar
+ * updates t += d, a += d*ad are left to the caller. */
+int  iegpu_evolve_fieldsN(struct iegpu_ctx* ctx, double d, double phiref);
+/* evolve_derivsN(d), src/evolution.cpp:1004-1012. */
+int  iegpu_evolve_derivsN(struct iegpu_ctx* ctx, double d);
+/* nsteps iterations of { evolve_derivsN(dN); evolve_fieldsN(dN); } with each
+ * site's state held in registers for the whole run. */
+int  iegpu_deltaN_steps(struct iegpu_ctx* ctx, double dN, int nsteps, double phiref);
+/* saveN() mean, src/output.cpp:1527-1537: sequential float accumulation of
+ * deltaN over sites with deltaN <= cutoff, divided by N^3 in float. */
+int  iegpu_saveN_mean(struct iegpu_ctx* ctx, double cutoff, float* nmean);
+/* deltaN -= value (src/output.cpp:1539-1542, 161-163). */
+int  iegpu_shift(struct iegpu_ctx* ctx, int field, double value);
+/* x = (x > threshold) ? 0 : x  (src/output.cpp:1549-1553). */
+int  iegpu_zero_above(struct iegpu_ctx* ctx, int field, double threshold);
+/* Sum of a field over the lattice (build_deltaN_linear mean, src/output.cpp:156-164). */
+int  iegpu_sum(struct iegpu_ctx* ctx, int field, double* sum);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,523 @@
+// ctx.cu -- C ABI entry points (include/iegpu.h): context lifetime, state
+// transfer, and dispatch to the kernels of the other translation units.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "iegpu_internal.cuh"
+#include "pot.cuh"
+
+#define IEGPU_VERSION 1
+
+namespace iegpu {
+
+int set_error(iegpu_ctx* c, int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+int check_cuda(iegpu_ctx* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return IEGPU_OK;
+    return set_error(c, IEGPU_ECUDA, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+int sync_and_check(iegpu_ctx* c, const char* what) {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return check_cuda(c, e, what);
+}
+
+bool is_double_field(int field) { return field == IEGPU_F || field == IEGPU_FD || field == IEGPU_DELTAN; }
+
+double* dfield(iegpu_ctx* c, int field) {
+    if (field == IEGPU_F) return c->f[c->cur];
+    if (field == IEGPU_FD) return c->fd;
+    if (field == IEGPU_DELTAN) return c->dn;
+    return nullptr;
+}
+
+double* dnyq(iegpu_ctx* c, int field) {
+    if (field == IEGPU_F) return c->fny;
+    if (field == IEGPU_FD) return c->fdny;
+    if (field == IEGPU_DELTAN) return c->fny;  // spectraN reuses the f Nyquist plane (src/output.cpp:1161)
+    return nullptr;
+}
+
+float* ffield(iegpu_ctx* c, int field) {
+    if (!c->cfg.sigw) return nullptr;
+    if (field >= 8 && field < 14) return c->h[c->cur][field - 8];
+    if (field >= 16 && field < 22) return c->hd[field - 16];
+    return nullptr;
+}
+
+float* fnyq(iegpu_ctx* c, int field) {
+    if (!c->cfg.sigw) return nullptr;
+    if (field >= 8 && field < 14) return c->hny[field - 8];
+    if (field >= 16 && field < 22) return c->hdny[field - 16];
+    return nullptr;
+}
+
+int valid_field(iegpu_ctx* c, int field) {
+    if (is_double_field(field)) return 1;
+    return ffield(c, field) != nullptr;
+}
+
+// potential(v), src/potential.cpp:91-98, on the host (binary search + interp).
+double host_potential(const iegpu_ctx* c, double v) {
+    const PotDev& P = c->pot;
+    if (!P.table) return (P.V0 * (1.0 - P.c1 * (v * v))) / P.B2;
+    const std::vector<double>& x = c->htab_x;
+    const int n = (int)x.size();
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int mid = lo + (hi - lo) / 2;
+        if (x[mid] >= v) lo = mid; else hi = mid;
+    }
+    const int l = hi;
+    const double x0 = x[l - 1], x1 = x[l], y0 = c->htab_V[l - 1], y1 = c->htab_V[l];
+    return (y1 + (v - x1) * (y0 - y1) / (x0 - x1)) / P.B2;
+}
+
+template <typename T>
+static int dalloc(iegpu_ctx* c, T** p, size_t n) {
+    if (cudaMalloc(p, sizeof(T) * (n ? n : 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(c, IEGPU_ENOMEM, "device allocation of %zu bytes failed", sizeof(T) * n);
+    }
+    return IEGPU_OK;
+}
+
+static void free_all(iegpu_ctx* c) {
+    fp64_destroy_graphs(c);
+    fft_free(c);
+    for (int q = 0; q < 2; ++q) cudaFree(c->f[q]);
+    cudaFree(c->fd); cudaFree(c->dn); cudaFree(c->fny); cudaFree(c->fdny);
+    for (int q = 0; q < 6; ++q) {
+        cudaFree(c->h[0][q]); cudaFree(c->h[1][q]); cudaFree(c->hd[q]); cudaFree(c->hny[q]); cudaFree(c->hdny[q]);
+    }
+    cudaFree(c->tab); cudaFree(c->tkey);
+    cudaFree(c->ctl); cudaFree(c->part); cudaFree(c->counter); cudaFree(c->a_trace);
+    cudaFree(c->spec_part); cudaFree(c->spec_cnt); cudaFree(c->misc);
+    if (c->ctl_h) cudaFreeHost(c->ctl_h);
+    if (c->misc_h) cudaFreeHost(c->misc_h);
+    for (int q = 0; q < 4; ++q)
+        if (c->ev[q]) cudaEventDestroy(c->ev[q]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+}  // namespace iegpu
+
+using namespace iegpu;
+
+extern "C" {
+
+int iegpu_version(void) { return IEGPU_VERSION; }
+
+const char* iegpu_strerror(int code) {
+    switch (code) {
+        case IEGPU_OK: return "ok";
+        case IEGPU_EINVAL: return "invalid argument";
+        case IEGPU_ECUDA: return "CUDA error";
+        case IEGPU_ERANGE: return "field value outside the numerical potential range";
+        case IEGPU_ENAN: return "unstable solution (non-finite mean)";
+        case IEGPU_ECOURANT: return "Courant condition violated";
+        case IEGPU_ENOMEM: return "device out of memory";
+        case IEGPU_ETABLE: return "invalid potential table";
+        case IEGPU_EUNSUPPORTED: return "unsupported in this form";
+        case IEGPU_ETIMEOUT: return "device wait timed out";
+        default: return "unknown error";
+    }
+}
+
+int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
+    if (!cfg || !out) return IEGPU_EINVAL;
+    *out = nullptr;
+    const int N = cfg->N;
+    if (N < 8 || N > 1024 || (N & (N - 1))) return IEGPU_EINVAL;
+    if (cfg->form != IEGPU_FORM_FP64) return IEGPU_EUNSUPPORTED;
+    if (!(cfg->L > 0) || !(cfg->dt > 0) || !(cfg->rescale_B > 0)) return IEGPU_EINVAL;
+    iegpu_ctx* c = new (std::nothrow) iegpu_ctx();
+    if (!c) return IEGPU_ENOMEM;
+    c->cfg = *cfg;
+    c->N = N;
+    while ((1 << c->lg) < N) ++c->lg;
+    c->gs = (size_t)N * N * N;
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return IEGPU_ECUDA;
+    }
+    c->sms = prop.multiProcessorCount;
+    int rc = IEGPU_OK;
+    if (check_cuda(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream create")) rc = IEGPU_ECUDA;
+    const size_t gs = c->gs, ny = (size_t)N * 2 * N;
+    if (!rc) rc = dalloc(c, &c->f[0], gs);
+    if (!rc) rc = dalloc(c, &c->f[1], gs);
+    if (!rc) rc = dalloc(c, &c->fd, gs);
+    if (!rc) rc = dalloc(c, &c->dn, gs);
+    if (!rc) rc = dalloc(c, &c->fny, ny);
+    if (!rc) rc = dalloc(c, &c->fdny, ny);
+    if (!rc && cfg->sigw) {
+        for (int q = 0; q < 6 && !rc; ++q) {
+            rc = dalloc(c, &c->h[0][q], gs);
+            if (!rc) rc = dalloc(c, &c->h[1][q], gs);
+            if (!rc) rc = dalloc(c, &c->hd[q], gs);
+            if (!rc) rc = dalloc(c, &c->hny[q], ny);
+            if (!rc) rc = dalloc(c, &c->hdny[q], ny);
+        }
+    }
+    c->red_grid = c->sms * 4;
+    const long long sites = (long long)gs;
+    if (c->red_grid * 256LL > sites) c->red_grid = (int)((sites + 255) / 256);
+    c->spec_blocks = c->sms * 2;
+    const int nb = iegpu_numbins(N) + 1;
+    if (!rc) rc = dalloc(c, &c->ctl, 1);
+    if (!rc) rc = dalloc(c, &c->part, (size_t)c->red_grid * 4);
+    if (!rc) rc = dalloc(c, &c->counter, 1);
+    if (!rc) rc = dalloc(c, &c->spec_part, (size_t)c->spec_blocks * nb + 65536);
+    if (!rc) rc = dalloc(c, &c->spec_cnt, (size_t)c->spec_blocks * nb);
+    if (!rc) rc = dalloc(c, &c->misc, (size_t)4 * nb + N + 64);
+    if (!rc && check_cuda(c, cudaMallocHost(&c->ctl_h, sizeof(DevCtl)), "pinned alloc")) rc = IEGPU_ENOMEM;
+    if (!rc && check_cuda(c, cudaMallocHost(&c->misc_h, sizeof(double) * ((size_t)4 * nb + N + 64)), "pinned alloc")) rc = IEGPU_ENOMEM;
+    if (!rc) {
+        // zero-initialised state, as the reference's vectors (src/initialize.cpp:119-120)
+        cudaMemsetAsync(c->f[0], 0, sizeof(double) * gs, c->stream);
+        cudaMemsetAsync(c->f[1], 0, sizeof(double) * gs, c->stream);
+        cudaMemsetAsync(c->fd, 0, sizeof(double) * gs, c->stream);
+        cudaMemsetAsync(c->dn, 0, sizeof(double) * gs, c->stream);
+        cudaMemsetAsync(c->fny, 0, sizeof(double) * ny, c->stream);
+        cudaMemsetAsync(c->fdny, 0, sizeof(double) * ny, c->stream);
+        for (int q = 0; q < 6 && cfg->sigw; ++q) {
+            cudaMemsetAsync(c->h[0][q], 0, sizeof(float) * gs, c->stream);
+            cudaMemsetAsync(c->h[1][q], 0, sizeof(float) * gs, c->stream);
+            cudaMemsetAsync(c->hd[q], 0, sizeof(float) * gs, c->stream);
+            cudaMemsetAsync(c->hny[q], 0, sizeof(float) * ny, c->stream);
+            cudaMemsetAsync(c->hdny[q], 0, sizeof(float) * ny, c->stream);
+        }
+        cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), c->stream);
+        cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream);
+        rc = sync_and_check(c, "create");
+    }
+    // hilltop constants with the reference's evaluation order (src/potential.cpp:77-83)
+    PotDev& P = c->pot;
+    P.table = cfg->potential == IEGPU_POT_TABLE;
+    P.V0 = cfg->V0;
+    P.c1 = (1.0 - cfg->ns) / 4.0;
+    P.c2 = -cfg->V0 * (1.0 - cfg->ns) / 2.0;
+    P.B2 = cfg->rescale_B * cfg->rescale_B;
+    for (int q = 0; q < 4 && !rc; ++q)
+        if (check_cuda(c, cudaEventCreate(&c->ev[q]), "event create")) rc = IEGPU_ECUDA;
+    if (!rc) rc = fft_init(c);
+    if (rc) {
+        const int code = rc;
+        free_all(c);
+        delete c;
+        return code;
+    }
+    *out = c;
+    return IEGPU_OK;
+}
+
+int iegpu_destroy(iegpu_ctx* c) {
+    if (!c) return IEGPU_EINVAL;
+    cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+    return IEGPU_OK;
+}
+
+const char* iegpu_last_error(const iegpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
+void* iegpu_stream(iegpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+long long iegpu_launch_count(const iegpu_ctx* c) { return c ? c->launches : 0; }
+
+int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const double* dV, int n) {
+    if (!c || !phi || !V || !dV || n < 2) return c ? set_error(c, IEGPU_ETABLE, "Numerical potential table must contain at least two points.\n") : IEGPU_EINVAL;
+    for (int l = 1; l < n; ++l) {
+        if (phi[l - 1] == phi[l]) return set_error(c, IEGPU_ETABLE, "Interpolation failed due to repeated field grid points.\n");
+        if (!(phi[l - 1] > phi[l])) return set_error(c, IEGPU_ETABLE, "field table must be sorted in descending order");
+    }
+    // packed: x, V, dV, dxl, dyV, dydV, slopeV (n each) + keys
+    std::vector<double> h((size_t)7 * n, 0.0);
+    std::vector<long long> k((size_t)n);
+    for (int l = 0; l < n; ++l) {
+        h[l] = phi[l];
+        h[n + l] = V[l];
+        h[2 * n + l] = dV[l];
+        k[l] = order_key(phi[l]);
+        if (l >= 1) {
+            h[3 * n + l] = phi[l - 1] - phi[l];
+            h[4 * n + l] = V[l - 1] - V[l];
+            h[5 * n + l] = dV[l - 1] - dV[l];
+            h[6 * n + l] = (V[l - 1] - V[l]) / (phi[l - 1] - phi[l]);
+        }
+    }
+    cudaFree(c->tab);
+    cudaFree(c->tkey);
+    c->tab = nullptr;
+    c->tkey = nullptr;
+    if (dalloc(c, &c->tab, h.size()) || dalloc(c, &c->tkey, k.size())) return IEGPU_ENOMEM;
+    if (check_cuda(c, cudaMemcpy(c->tab, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice), "table upload") ||
+        check_cuda(c, cudaMemcpy(c->tkey, k.data(), sizeof(long long) * k.size(), cudaMemcpyHostToDevice), "table upload"))
+        return IEGPU_ECUDA;
+    c->htab_x.assign(phi, phi + n);
+    c->htab_V.assign(V, V + n);
+    c->htab_dV.assign(dV, dV + n);
+    c->ntab = n;
+    PotDev& P = c->pot;
+    P.n = n;
+    P.x = c->tab;
+    P.V = c->tab + n;
+    P.dV = c->tab + 2 * n;
+    P.dxl = c->tab + 3 * n;
+    P.dyV = c->tab + 4 * n;
+    P.dydV = c->tab + 5 * n;
+    P.slopeV = c->tab + 6 * n;
+    P.key = c->tkey;
+    fp64_destroy_graphs(c);  // graphs hold the potential by value
+    return IEGPU_OK;
+}
+
+static int need_table(iegpu_ctx* c) {
+    if (c->pot.table && c->ntab < 2) return set_error(c, IEGPU_ETABLE, "numerical potential selected but no table was set");
+    return IEGPU_OK;
+}
+
+int iegpu_upload(iegpu_ctx* c, int field, const void* host, const void* nyquist) {
+    if (!c || !host) return IEGPU_EINVAL;
+    if (!valid_field(c, field)) return set_error(c, IEGPU_EINVAL, "unknown field %d", field);
+    const size_t ny = (size_t)c->N * 2 * c->N;
+    if (is_double_field(field)) {
+        if (check_cuda(c, cudaMemcpy(dfield(c, field), host, sizeof(double) * c->gs, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
+        if (nyquist && check_cuda(c, cudaMemcpy(dnyq(c, field), nyquist, sizeof(double) * ny, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
+    } else {
+        if (check_cuda(c, cudaMemcpy(ffield(c, field), host, sizeof(float) * c->gs, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
+        if (nyquist && check_cuda(c, cudaMemcpy(fnyq(c, field), nyquist, sizeof(float) * ny, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
+    }
+    return IEGPU_OK;
+}
+
+int iegpu_download(iegpu_ctx* c, int field, void* host, void* nyquist) {
+    if (!c || !host) return IEGPU_EINVAL;
+    if (!valid_field(c, field)) return set_error(c, IEGPU_EINVAL, "unknown field %d", field);
+    if (sync_and_check(c, "download")) return IEGPU_ECUDA;
+    const size_t ny = (size_t)c->N * 2 * c->N;
+    if (is_double_field(field)) {
+        if (check_cuda(c, cudaMemcpy(host, dfield(c, field), sizeof(double) * c->gs, cudaMemcpyDeviceToHost), "download")) return IEGPU_ECUDA;
+        if (nyquist && check_cuda(c, cudaMemcpy(nyquist, dnyq(c, field), sizeof(double) * ny, cudaMemcpyDeviceToHost), "download")) return IEGPU_ECUDA;
+    } else {
+        if (check_cuda(c, cudaMemcpy(host, ffield(c, field), sizeof(float) * c->gs, cudaMemcpyDeviceToHost), "download")) return IEGPU_ECUDA;
+        if (nyquist && check_cuda(c, cudaMemcpy(nyquist, fnyq(c, field), sizeof(float) * ny, cudaMemcpyDeviceToHost), "download")) return IEGPU_ECUDA;
+    }
+    return IEGPU_OK;
+}
+
+int iegpu_add(iegpu_ctx* c, int field, double value) {
+    if (!c) return IEGPU_EINVAL;
+    return field_add(c, field, value);
+}
+
+int iegpu_shift(iegpu_ctx* c, int field, double value) {
+    if (!c) return IEGPU_EINVAL;
+    return field_add(c, field, -value);
+}
+
+int iegpu_zero_above(iegpu_ctx* c, int field, double threshold) {
+    if (!c) return IEGPU_EINVAL;
+    return field_zero_above(c, field, threshold);
+}
+
+int iegpu_sum(iegpu_ctx* c, int field, double* sum) {
+    if (!c || !sum) return IEGPU_EINVAL;
+    return field_sum(c, field, sum);
+}
+
+int iegpu_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    return fp64_evolve_fields(c, d, bg);
+}
+
+int iegpu_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (int rc = need_table(c)) return rc;
+    return fp64_evolve_derivs(c, d, bg);
+}
+
+int iegpu_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps_taken, double* a_trace) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (int rc = need_table(c)) return rc;
+    return fp64_leapfrog(c, af, max_steps, bg, steps_taken, a_trace);
+}
+
+int iegpu_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]) {
+    if (!c || !bg || !out) return IEGPU_EINVAL;
+    if (int rc = need_table(c)) return rc;
+    return fp64_energies(c, bg, out);
+}
+
+int iegpu_bunch_davies(iegpu_ctx* c, int seed, double phi0, double dphi0, double hi_cut, double lo_cut,
+                       double* hubble_init) {
+    if (!c || !hubble_init) return IEGPU_EINVAL;
+    if (int rc = need_table(c)) return rc;
+    const double dx = c->cfg.L / (double)c->N;
+    if (c->cfg.dt > dx / std::sqrt(3.0))
+        return set_error(c, IEGPU_ECOURANT, "Time step too large. Courant condition violated: dt/dx = %f\n", c->cfg.dt / dx);
+    if (c->pot.table && (phi0 > c->htab_x.front() || phi0 < c->htab_x.back()))
+        return set_error(c, IEGPU_ERANGE, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n",
+                         phi0, c->htab_x.back(), c->htab_x.front());
+    // hubble_init before the modes are drawn (src/initialize.cpp:125-131): set_mode's hbterm
+    const double h0 = std::sqrt((0.5 * dphi0 * dphi0 + host_potential(c, phi0)) / 3.0);
+    int rc = bunch_davies(c, seed, phi0, dphi0, h0, hi_cut, lo_cut);
+    if (rc) return rc;
+    iegpu_bg b{0.0, 1.0, 0.0, 0.0, 1.0};
+    double e[3];
+    rc = fp64_energies(c, &b, e);
+    if (rc) return rc;
+    *hubble_init = std::sqrt((e[0] + e[2] + e[1]) / 3.0);
+    return IEGPU_OK;
+}
+
+int iegpu_timer_start(iegpu_ctx* c) {
+    if (!c) return IEGPU_EINVAL;
+    return check_cuda(c, cudaEventRecord(c->ev[3], c->stream), "timer start");
+}
+
+int iegpu_timer_stop(iegpu_ctx* c, float* ms) {
+    if (!c || !ms) return IEGPU_EINVAL;
+    if (check_cuda(c, cudaEventRecord(c->ev[0], c->stream), "timer stop")) return IEGPU_ECUDA;
+    if (check_cuda(c, cudaEventSynchronize(c->ev[0]), "timer sync")) return IEGPU_ECUDA;
+    return check_cuda(c, cudaEventElapsedTime(ms, c->ev[3], c->ev[0]), "timer elapsed");
+}
+
+int iegpu_profile_leapfrog(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms_out, int nk) {
+    if (!c || !bg || !ms_out || nsteps < 0) return IEGPU_EINVAL;
+    if (int rc = need_table(c)) return rc;
+    return fp64_profile(c, af, nsteps, bg, ms_out, nk);
+}
+
+int iegpu_means(iegpu_ctx* c, double out[3]) {
+    if (!c || !out) return IEGPU_EINVAL;
+    return field_means(c, out);
+}
+
+int iegpu_histogram(iegpu_ctx* c, int field, int nbins, double* bmin, double* df, double* freq) {
+    // bin counters live in shared memory: at most 8192 bins
+    if (!c || !bmin || !df || !freq || nbins <= 0 || nbins > 8192) return c ? set_error(c, IEGPU_EINVAL, "bad histogram arguments (1 <= nbins <= 8192)") : IEGPU_EINVAL;
+    return field_histogram(c, field, nbins, bmin, df, freq);
+}
+
+int iegpu_fft(iegpu_ctx* c, int field, int forward) {
+    if (!c || (forward != 1 && forward != -1)) return IEGPU_EINVAL;
+    if (!valid_field(c, field)) return set_error(c, IEGPU_EINVAL, "unknown field %d", field);
+    int rc;
+    if (is_double_field(field)) rc = fft_d(c, dfield(c, field), dnyq(c, field), forward);
+    else rc = fft_f(c, ffield(c, field), fnyq(c, field), forward);
+    if (rc) return rc;
+    return sync_and_check(c, "fft");
+}
+
+int iegpu_numbins(int N) { return (int)(1.73205 * (N / 2)) + 1; }
+
+int iegpu_spectrum(iegpu_ctx* c, int field, int* counts, double* f2, int nbins) {
+    if (!c || !counts || !f2) return IEGPU_EINVAL;
+    if (!is_double_field(field)) return set_error(c, IEGPU_EINVAL, "spectra are defined for f, fd and deltaN");
+    if (nbins != iegpu_numbins(c->N)) return set_error(c, IEGPU_EINVAL, "nbins must be %d", iegpu_numbins(c->N));
+    double* x = dfield(c, field);
+    double* ny = dnyq(c, field);
+    int rc = fft_d(c, x, ny, 1);
+    if (!rc) rc = spectrum_bin_d(c, x, ny, counts, f2, nbins);
+    if (!rc) rc = fft_d(c, x, ny, -1);
+    if (!rc) rc = sync_and_check(c, "spectrum");
+    return rc;
+}
+
+int iegpu_gw_spectrum(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins) {
+    if (!c || !counts || !f2 || (which != 0 && which != 1)) return IEGPU_EINVAL;
+    if (!c->cfg.sigw) return set_error(c, IEGPU_EUNSUPPORTED, "context was created without SIGW");
+    if (nbins != iegpu_numbins(c->N)) return set_error(c, IEGPU_EINVAL, "nbins must be %d", iegpu_numbins(c->N));
+    for (int q = 0; q < 6; ++q) {
+        float* x = which ? c->hd[q] : c->h[c->cur][q];
+        float* ny = which ? c->hdny[q] : c->hny[q];
+        if (int rc = fft_f(c, x, ny, 1)) return rc;
+    }
+    int rc = gw_bin(c, which, to_phys, counts, f2, nbins);
+    for (int q = 0; q < 6 && !rc; ++q) {
+        float* x = which ? c->hd[q] : c->h[c->cur][q];
+        float* ny = which ? c->hdny[q] : c->hny[q];
+        rc = fft_f(c, x, ny, -1);
+    }
+    if (!rc) rc = sync_and_check(c, "gw spectrum");
+    return rc;
+}
+
+int iegpu_initializeN(iegpu_ctx* c, double a) {
+    if (!c) return IEGPU_EINVAL;
+    if (int rc = need_table(c)) return rc;
+    int rc = deltaN_init(c, a);
+    if (!rc) rc = sync_and_check(c, "initializeN");
+    if (!rc) {
+        int e = 0;
+        cudaMemcpy(&e, &c->ctl->error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e) {
+            double v = 0;
+            cudaMemcpy(&v, &c->ctl->errval, sizeof(double), cudaMemcpyDeviceToHost);
+            rc = set_error(c, IEGPU_ERANGE, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n", v,
+                           c->htab_x.back(), c->htab_x.front());
+        }
+    }
+    return rc;
+}
+
+int iegpu_get_phiref(iegpu_ctx* c, double* phiref) {
+    if (!c || !phiref) return IEGPU_EINVAL;
+    return get_phiref(c, phiref);
+}
+
+static int deltaN_run(iegpu_ctx* c, double d, int nsteps, double phiref, int dd, int df) {
+    if (int rc = need_table(c)) return rc;
+    if (check_cuda(c, cudaMemsetAsync(&c->ctl->error, 0, sizeof(int), c->stream), "memset")) return IEGPU_ECUDA;
+    int rc = deltaN_steps(c, d, nsteps, phiref, dd, df);
+    if (!rc) rc = sync_and_check(c, "deltaN");
+    if (!rc) {
+        int e = 0;
+        cudaMemcpy(&e, &c->ctl->error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e) {
+            double v = 0;
+            cudaMemcpy(&v, &c->ctl->errval, sizeof(double), cudaMemcpyDeviceToHost);
+            rc = set_error(c, IEGPU_ERANGE, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n", v,
+                           c->htab_x.back(), c->htab_x.front());
+        }
+    }
+    return rc;
+}
+
+int iegpu_evolve_fieldsN(iegpu_ctx* c, double d, double phiref) {
+    if (!c) return IEGPU_EINVAL;
+    return deltaN_run(c, d, 1, phiref, 0, 1);
+}
+
+int iegpu_evolve_derivsN(iegpu_ctx* c, double d) {
+    if (!c) return IEGPU_EINVAL;
+    return deltaN_run(c, d, 1, 0.0, 1, 0);
+}
+
+int iegpu_deltaN_steps(iegpu_ctx* c, double dN, int nsteps, double phiref) {
+    if (!c || nsteps < 0) return IEGPU_EINVAL;
+    if (nsteps == 0) return IEGPU_OK;
+    return deltaN_run(c, dN, nsteps, phiref, 1, 1);
+}
+
+int iegpu_saveN_mean(iegpu_ctx* c, double cutoff, float* nmean) {
+    if (!c || !nmean) return IEGPU_EINVAL;
+    return saveN_mean(c, cutoff, nmean);
+}
+
+}  // extern "C"

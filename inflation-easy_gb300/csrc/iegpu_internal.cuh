@@ -1,0 +1,190 @@
+// iegpu_internal.cuh -- shared definitions of the GB300 InflationEasy engine.
+//
+// Device layout (one context = one N^3 lattice, all in HBM):
+//   plain FP64 form:  f[2] (ping-pong, N^3 double), fd (N^3 double, updated in
+//                     place), deltaN (N^3 double), Nyquist planes (N x 2N).
+//   SIGW:             h[2][6] (ping-pong, N^3 float each), hd[6] (N^3 float).
+// Index (i*N + j)*N + k with k fastest, the reference's layout
+// (src/main.h:34-38), so uploads and downloads are plain copies.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/iegpu.h"
+
+namespace iegpu {
+
+constexpr int kThreads = 256;
+
+// Background scalars and per-step coefficients, resident on the device so the
+// leapfrog loop never returns to the host between steps.
+struct DevBg {
+    double t, a, ad, ad2, astep;
+};
+
+struct DevStep {
+    double d;          // rescaled step dt*astep^(s-1)       (src/evolution.cpp:938)
+    double laplnorm;   // a^(-2s)/dx^2                       (src/evolution.cpp:153)
+    double friction;   // (2+s) ad/a after the first half-kick (src/evolution.cpp:167)
+    double potnorm;    // a^(2-2s)                           (src/evolution.cpp:168)
+    double srcAmp;     // 2 a^(-2s)                          (src/evolution.cpp:185)
+    int active;        // 0 once the loop has ended
+    int pad;
+};
+
+struct DevCtl {
+    DevBg bg;
+    DevStep st;
+    double af;
+    double d_given;     // kick-only mode (evolve_derivs) step size
+    int steps_done;
+    int steps_limit;
+    int done;
+    int mode;           // kModeLeapfrog or kModeKick
+    int error;          // first device-side error code
+    int pad;
+    double errval;      // offending value for IEGPU_ERANGE
+};
+
+constexpr int kModeLeapfrog = 0;
+constexpr int kModeKick = 1;
+
+// Potential description passed by value to kernels.
+struct PotDev {
+    int table;          // 0 hilltop, 1 tabulated
+    int n;              // table length
+    double V0, c1, c2, B2;  // hilltop: V = V0(1 - c1 v^2)/B2, V' = (c2 v)/B2
+    const double* x;        // table nodes (descending)
+    const long long* key;   // monotone integer keys of x
+    const double* V;        // V at nodes
+    const double* dV;       // V' at nodes
+    const double* dxl;      // x[l-1] - x[l]
+    const double* dyV;      // V[l-1] - V[l]
+    const double* dydV;     // dV[l-1] - dV[l]
+    const double* slopeV;   // dyV/dxl (reductions only)
+};
+
+struct FftTw {
+    // complex-pass twiddles for line length M, per direction, stage-major
+    // (stage s uses entries [2^(s-1)-1, 2^s-1)), computed on the host with the
+    // reference's recurrence; unpack twiddles for b = 1..N/4-1.
+    double2* c_fwd_d[2];   // [0]: length N, [1]: length N/2
+    double2* c_inv_d[2];
+    double2* unpack_d;
+    float2* c_fwd_f[2];
+    float2* c_inv_f[2];
+    float2* unpack_f;
+};
+
+}  // namespace iegpu
+
+struct iegpu_ctx {
+    iegpu_config cfg;
+    int N = 0, lg = 0;
+    size_t gs = 0;          // N^3
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    long long launches = 0;
+
+    // plain FP64 state
+    double* f[2] = {nullptr, nullptr};
+    int cur = 0;
+    double* fd = nullptr;
+    double* dn = nullptr;
+    double* fny = nullptr;
+    double* fdny = nullptr;
+    // SIGW state
+    float* h[2][6] = {};
+    float* hd[6] = {};
+    float* hny[6] = {};
+    float* hdny[6] = {};
+
+    // table (device copies, plus the host copy for scalar evaluations)
+    std::vector<double> htab_x, htab_V, htab_dV;
+    int ntab = 0;
+    double* tab = nullptr;      // packed arrays, see iegpu_set_table
+    long long* tkey = nullptr;
+    iegpu::PotDev pot{};
+
+    // control and scratch
+    iegpu::DevCtl* ctl = nullptr;      // device
+    iegpu::DevCtl* ctl_h = nullptr;    // pinned host mirror
+    double* part = nullptr;            // per-CTA reduction partials
+    unsigned* counter = nullptr;       // last-CTA detection
+    int red_grid = 0;
+    double* a_trace = nullptr;
+    int a_trace_cap = 0;
+    double* spec_part = nullptr;       // spectrum partials [blocks][nbins]
+    int* spec_cnt = nullptr;
+    int spec_blocks = 0;
+    double* misc = nullptr;            // small device scratch (sums, min/max)
+    double* misc_h = nullptr;          // pinned mirror
+    iegpu::FftTw tw{};
+
+    // timing events
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    // leapfrog graphs: [parity of the current buffer]
+    cudaGraphExec_t lf_exec[2] = {nullptr, nullptr};
+    int lf_steps = 0;
+};
+
+namespace iegpu {
+
+int set_error(iegpu_ctx* c, int code, const char* fmt, ...);
+int check_cuda(iegpu_ctx* c, cudaError_t e, const char* what);
+int sync_and_check(iegpu_ctx* c, const char* what);
+bool is_double_field(int field);
+double* dfield(iegpu_ctx* c, int field);
+float* ffield(iegpu_ctx* c, int field);
+double* dnyq(iegpu_ctx* c, int field);
+float* fnyq(iegpu_ctx* c, int field);
+int valid_field(iegpu_ctx* c, int field);
+// potential(v) of src/potential.cpp:91-98 evaluated on the host.
+double host_potential(const iegpu_ctx* c, double v);
+
+// pow(x, y) for the exponents the leapfrog uses with rescale_s = 0; exact
+// products and quotients there, CUDA pow otherwise.
+__host__ __device__ inline double pow_exp(double x, double y) {
+    if (y == 0.0) return 1.0;
+    if (y == 1.0) return x;
+    if (y == 2.0) return x * x;
+    if (y == -1.0) return 1.0 / x;
+    return pow(x, y);
+}
+
+// --- launchers implemented in the .cu files ---------------------------------
+// leapfrog_fp64.cu
+int fp64_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace);
+int fp64_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg);
+int fp64_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
+int fp64_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]);
+int fp64_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk);
+void fp64_destroy_graphs(iegpu_ctx* c);
+// fft.cu
+int fft_init(iegpu_ctx* c);
+void fft_free(iegpu_ctx* c);
+int fft_d(iegpu_ctx* c, double* f, double* fny, int forward);
+int fft_f(iegpu_ctx* c, float* f, float* fny, int forward);
+// spectra.cu
+int spectrum_bin_d(iegpu_ctx* c, const double* f, const double* fny, int* counts, double* f2, int nbins);
+int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins);
+// reduce.cu
+int field_means(iegpu_ctx* c, double out[3]);
+int field_sum(iegpu_ctx* c, int field, double* out);
+int field_histogram(iegpu_ctx* c, int field, int nbins, double* bmin, double* df, double* freq);
+int field_add(iegpu_ctx* c, int field, double v);
+int field_zero_above(iegpu_ctx* c, int field, double thr);
+int saveN_mean(iegpu_ctx* c, double cutoff, float* out);
+int get_phiref(iegpu_ctx* c, double* out);
+// ic.cu
+int bunch_davies(iegpu_ctx* c, int seed, double phi0, double dphi0, double hubble, double hi_cut, double lo_cut);
+// deltaN.cu
+int deltaN_init(iegpu_ctx* c, double a);
+int deltaN_steps(iegpu_ctx* c, double dN, int nsteps, double phiref, int do_derivs, int do_fields);
+
+}  // namespace iegpu

@@ -1,0 +1,474 @@
+// leapfrog_fp64.cu -- plain FP64 leapfrog of src/evolution.cpp:150-284.
+//
+// Compiled with -fmad=false: every per-site expression is evaluated with the
+// reference's operation order and rounding (no contraction), so a site given
+// the same inputs produces the same bits as the reference CPU code.
+//
+// One leapfrog step is two kernels, captured in a CUDA graph:
+//   k_reduce  reads f (7-point stencil) and accumulates sum f*lapl(f) and the
+//             potential sum (gradient_energy / potential_energy,
+//             src/evolution.cpp:130-136, src/potential.cpp:151-171); the last
+//             CTA to finish combines the partials in a fixed order and runs
+//             the Friedmann update of src/evolution.cpp:153-168 on the device.
+//   k_kick    kick of fd (and hd) with the fused Laplacian + V', then the
+//             drift f += d fd into the other f buffer (ping-pong), and
+//             h += (float)(d hd) (src/evolution.cpp:170-281).
+// Algorithmic HBM traffic per site-update: 40 B (read f twice, fd; write f, fd),
+// 32 B of which are the reference's own state update.
+#include <cstdarg>
+#include <cstdio>
+
+#include "iegpu_internal.cuh"
+#include "pot.cuh"
+#include "reduce.cuh"
+
+namespace iegpu {
+
+struct SigwPtrs {
+    const float* hs[6];
+    float* hdst[6];
+    float* hd[6];
+};
+
+struct StepConst {
+    double dt, s, dx, gs, half_over_dx;
+};
+
+struct Nbr {
+    long long c, kp, km, jp, jm, ip, im;
+};
+
+__device__ __forceinline__ Nbr neighbours(long long id, int lg) {
+    const int m = (1 << lg) - 1;
+    const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
+    Nbr n;
+    n.c = id;
+    n.kp = id - k + ((k + 1) & m);
+    n.km = id - k + ((k - 1) & m);
+    n.jp = id + ((long long)(((j + 1) & m) - j) << lg);
+    n.jm = id + ((long long)(((j - 1) & m) - j) << lg);
+    n.ip = id + ((long long)(((i + 1) & m) - i) << (2 * lg));
+    n.im = id + ((long long)(((i - 1) & m) - i) << (2 * lg));
+    return n;
+}
+
+// lapl<T>, src/evolution.cpp:34-51: (k+1)+(k-1)+(j+1)+(j-1)+(i+1)+(i-1)-6f
+template <typename T>
+__device__ __forceinline__ T lapl7(const T* __restrict__ f, const Nbr& n, T fc) {
+    return __ldg(&f[n.kp]) + __ldg(&f[n.km]) + __ldg(&f[n.jp]) + __ldg(&f[n.jm]) + __ldg(&f[n.ip]) +
+           __ldg(&f[n.im]) - T(6) * fc;
+}
+
+// Friedmann update and step coefficients (src/evolution.cpp:153-168, 256,
+// 283, 938, 944).  Runs in one thread.  G = sum f*lapl(f), Pn = potential sum
+// (hilltop: sum f^2; table: sum V*B^2).
+__device__ void step_scalars(DevCtl* ctl, const PotDev& P, const StepConst& K, double G, double Pn,
+                             double* a_trace) {
+    DevCtl& C = *ctl;
+    double d;
+    if (C.mode == kModeLeapfrog) {
+        if (!(C.bg.a <= C.af) || C.steps_done >= C.steps_limit) {
+            C.st.active = 0;
+            C.done = 1;
+            return;
+        }
+        d = K.dt * pow_exp(C.bg.astep, K.s - 1.0);
+    } else {
+        d = C.d_given;
+    }
+    const double a = C.bg.a;
+    double ad = C.bg.ad;
+    const double s = K.s;
+    const double laplnorm = pow_exp(a, -2.0 * s) / (K.dx * K.dx);
+    const double sfev1 = s + 1.0;
+    const double sfev2 = -2.0 * s + 2.0;
+    const double gradient = -G;
+    const double grad = 0.5 * gradient * ((1.0 / (a * K.dx)) * (1.0 / (a * K.dx))) / K.gs;
+    double pot;
+    if (P.table) pot = (Pn / P.B2) / K.gs;
+    else pot = (P.V0 * (K.gs - P.c1 * Pn) / P.B2) / K.gs;
+    const double ad2 = (-2.0 * ad - 2.0 * a / d / sfev1 *
+                        (1.0 - sqrt(1.0 + 2.0 * d * sfev1 * ad / a +
+                                    (d * d) * sfev1 * pow_exp(a, sfev2) * (2.0 * grad / 3.0 + pot)))) / d;
+    ad += 0.5 * d * ad2;
+    C.st.d = d;
+    C.st.laplnorm = laplnorm;
+    C.st.friction = (2.0 + s) * ad / a;
+    C.st.potnorm = pow_exp(a, 2.0 - 2.0 * s);
+    C.st.srcAmp = 2.0 * pow_exp(a, -2.0 * s);
+    C.st.active = 1;
+    ad += 0.5 * d * ad2;
+    C.bg.ad = ad;
+    C.bg.ad2 = ad2;
+    if (C.mode == kModeLeapfrog) {
+        C.bg.t += d;
+        C.bg.a = a + d * ad;
+        C.bg.astep = C.bg.a;
+        if (a_trace) a_trace[C.steps_done] = C.bg.a;
+        C.steps_done += 1;
+    }
+}
+
+template <bool TABLE>
+__global__ void __launch_bounds__(kThreads) k_reduce(const double* __restrict__ f, PotDev P, DevCtl* ctl,
+                                                     double* part, unsigned* counter, double* a_trace, int lg,
+                                                     StepConst K) {
+    if (ctl->mode == kModeLeapfrog && ctl->done) return;
+    const long long gs = 1LL << (3 * lg);
+    double v[2] = {0.0, 0.0};
+    bool bad = false;
+    for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
+        const Nbr n = neighbours(id, lg);
+        const double fc = __ldg(&f[id]);
+        v[0] += fc * lapl7(f, n, fc);
+        if (TABLE) {
+            bool oor;
+            v[1] += V_table_sum_term(P, fc, &oor);
+            if (oor) { flag_error(ctl, IEGPU_ERANGE, fc); bad = true; }
+        } else {
+            v[1] += fc * fc;
+        }
+    }
+    (void)bad;
+    block_sum<2>(v);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = v[0];
+        part[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!arrive_last(counter)) return;
+    if (threadIdx.x < 32) {
+        double tot[2];
+        sum_partials<2>(part, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            *counter = 0;
+            if (ctl->error) {
+                ctl->st.active = 0;
+                ctl->done = 1;
+            } else {
+                step_scalars(ctl, P, K, tot[0], tot[1], a_trace);
+            }
+        }
+    }
+}
+
+template <bool TABLE, bool SIGW, int MODE>
+__global__ void __launch_bounds__(kThreads) k_kick(const double* __restrict__ fs, double* __restrict__ fdst,
+                                                   double* __restrict__ fd, SigwPtrs sg, PotDev P, DevCtl* ctl,
+                                                   int lg, double half_over_dx) {
+    const DevStep st = ctl->st;
+    if (!st.active) return;
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const Nbr n = neighbours(id, lg);
+    const double fc = __ldg(&fs[id]);
+    const double lap = lapl7(fs, n, fc);
+    bool oor;
+    const double dv = dV_exact<TABLE>(P, fc, &oor);
+    if (TABLE && oor) flag_error(ctl, IEGPU_ERANGE, fc);
+    const double fdo = fd[id];
+    const double fdn = fdo + st.d * (st.laplnorm * lap - st.friction * fdo - st.potnorm * dv);
+    fd[id] = fdn;
+    if (MODE == kModeLeapfrog) fdst[id] = fc + st.d * fdn;
+    if (SIGW) {
+        // dfdx<double>, src/evolution.cpp:55-77, and the six tensor updates
+        // of src/evolution.cpp:183-254 (float storage, double right-hand side).
+        const double gx = (__ldg(&fs[n.ip]) - __ldg(&fs[n.im])) * half_over_dx;
+        const double gy = (__ldg(&fs[n.jp]) - __ldg(&fs[n.jm])) * half_over_dx;
+        const double gz = (__ldg(&fs[n.kp]) - __ldg(&fs[n.km])) * half_over_dx;
+        const double T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float* h = sg.hs[c];
+            const float hc = __ldg(&h[id]);
+            const float lf = lapl7(h, n, hc);
+            const float hdo = sg.hd[c][id];
+            const double rhs = st.d * (st.laplnorm * (double)lf - st.friction * (double)hdo + st.srcAmp * T[c]);
+            const float hdn = hdo + (float)rhs;
+            sg.hd[c][id] = hdn;
+            if (MODE == kModeLeapfrog) sg.hdst[c][id] = hc + (float)(st.d * (double)hdn);
+        }
+    }
+}
+
+// evolve_fields drift, src/evolution.cpp:265-281 (in place).
+template <bool SIGW>
+__global__ void __launch_bounds__(kThreads) k_drift(double* __restrict__ f, const double* __restrict__ fd,
+                                                    SigwPtrs sg, long long gs, double d) {
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (id >= gs) return;
+    f[id] = f[id] + d * fd[id];
+    if (SIGW) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sg.hdst[c][id] = sg.hdst[c][id] + (float)(d * (double)sg.hd[c][id]);
+    }
+}
+
+// Lattice sums for kin_energy / gradient_energy / potential_energy.
+template <bool TABLE>
+__global__ void __launch_bounds__(kThreads) k_energy_sums(const double* __restrict__ f, const double* __restrict__ fd,
+                                                          PotDev P, DevCtl* ctl, double* part, int lg) {
+    const long long gs = 1LL << (3 * lg);
+    double v[3] = {0.0, 0.0, 0.0};
+    for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
+        const Nbr n = neighbours(id, lg);
+        const double fc = __ldg(&f[id]);
+        v[0] += fc * lapl7(f, n, fc);
+        if (TABLE) {
+            bool oor;
+            v[1] += V_table_sum_term(P, fc, &oor);
+            if (oor) flag_error(ctl, IEGPU_ERANGE, fc);
+        } else {
+            v[1] += fc * fc;
+        }
+        const double q = __ldg(&fd[id]);
+        v[2] += q * q;
+    }
+    block_sum<3>(v);
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = v[0];
+        part[3 * blockIdx.x + 1] = v[1];
+        part[3 * blockIdx.x + 2] = v[2];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static StepConst step_const(const iegpu_ctx* c) {
+    StepConst K;
+    K.dt = c->cfg.dt;
+    K.s = c->cfg.rescale_s;
+    K.dx = c->cfg.L / (double)c->N;
+    K.gs = (double)c->gs;
+    K.half_over_dx = 0.5 / K.dx;
+    return K;
+}
+
+static SigwPtrs sigw_ptrs(iegpu_ctx* c, int src) {
+    SigwPtrs s{};
+    if (!c->cfg.sigw) return s;
+    for (int q = 0; q < 6; ++q) {
+        s.hs[q] = c->h[src][q];
+        s.hdst[q] = c->h[src ^ 1][q];
+        s.hd[q] = c->hd[q];
+    }
+    return s;
+}
+
+static void launch_reduce(iegpu_ctx* c, int src) {
+    const StepConst K = step_const(c);
+    if (c->pot.table)
+        k_reduce<true><<<c->red_grid, kThreads, 0, c->stream>>>(c->f[src], c->pot, c->ctl, c->part, c->counter, c->a_trace, c->lg, K);
+    else
+        k_reduce<false><<<c->red_grid, kThreads, 0, c->stream>>>(c->f[src], c->pot, c->ctl, c->part, c->counter, c->a_trace, c->lg, K);
+    c->launches++;
+}
+
+template <int MODE>
+static void launch_kick(iegpu_ctx* c, int src) {
+    const unsigned grid = (unsigned)(c->gs / kThreads);
+    const SigwPtrs sg = sigw_ptrs(c, src);
+    const double hodx = 0.5 / (c->cfg.L / (double)c->N);
+    double* fdst = c->f[src ^ 1];
+    const bool tab = c->pot.table != 0, sig = c->cfg.sigw != 0;
+    if (tab && sig) k_kick<true, true, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    else if (tab) k_kick<true, false, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    else if (sig) k_kick<false, true, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    else k_kick<false, false, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    c->launches++;
+}
+
+void fp64_destroy_graphs(iegpu_ctx* c) {
+    for (int p = 0; p < 2; ++p) {
+        if (c->lf_exec[p]) cudaGraphExecDestroy(c->lf_exec[p]);
+        c->lf_exec[p] = nullptr;
+    }
+}
+
+// Steps per graph launch; even, so a full graph returns to its start buffer.
+static int graph_steps(const iegpu_ctx* c) { return c->N <= 64 ? 32 : 8; }
+
+static int build_graphs(iegpu_ctx* c) {
+    const int L = graph_steps(c);
+    for (int p = 0; p < 2; ++p) {
+        cudaGraph_t g;
+        if (check_cuda(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture")) return IEGPU_ECUDA;
+        const long long before = c->launches;
+        for (int s = 0; s < L; ++s) {
+            const int src = (p + s) & 1;
+            launch_reduce(c, src);
+            launch_kick<kModeLeapfrog>(c, src);
+        }
+        c->launches = before;
+        if (check_cuda(c, cudaStreamEndCapture(c->stream, &g), "graph capture end")) return IEGPU_ECUDA;
+        cudaError_t e = cudaGraphInstantiate(&c->lf_exec[p], g, 0);
+        cudaGraphDestroy(g);
+        if (check_cuda(c, e, "graph instantiate")) return IEGPU_ECUDA;
+    }
+    c->lf_steps = L;
+    return IEGPU_OK;
+}
+
+static int upload_ctl(iegpu_ctx* c) {
+    return check_cuda(c, cudaMemcpyAsync(c->ctl, c->ctl_h, sizeof(DevCtl), cudaMemcpyHostToDevice, c->stream), "control upload");
+}
+
+static int read_ctl(iegpu_ctx* c) {
+    if (check_cuda(c, cudaMemcpyAsync(c->ctl_h, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, c->stream), "control download"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "leapfrog")) return IEGPU_ECUDA;
+    if (c->ctl_h->error == IEGPU_ERANGE) {
+        const double v = c->ctl_h->errval;
+        return set_error(c, IEGPU_ERANGE, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n", v,
+                         c->htab_x.empty() ? 0.0 : c->htab_x.back(), c->htab_x.empty() ? 0.0 : c->htab_x.front());
+    }
+    return IEGPU_OK;
+}
+
+static void fill_ctl(iegpu_ctx* c, const iegpu_bg* bg, int mode) {
+    DevCtl& C = *c->ctl_h;
+    memset(&C, 0, sizeof C);
+    C.bg.t = bg->t;
+    C.bg.a = bg->a;
+    C.bg.ad = bg->ad;
+    C.bg.ad2 = bg->ad2;
+    C.bg.astep = bg->astep;
+    C.mode = mode;
+}
+
+static void copy_bg(const iegpu_ctx* c, iegpu_bg* bg) {
+    const DevBg& B = c->ctl_h->bg;
+    bg->t = B.t;
+    bg->a = B.a;
+    bg->ad = B.ad;
+    bg->ad2 = B.ad2;
+    bg->astep = B.astep;
+}
+
+int fp64_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace) {
+    if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
+    if (steps) *steps = 0;
+    if (max_steps == 0) return IEGPU_OK;
+    if (max_steps > c->a_trace_cap) {
+        if (c->a_trace) cudaFree(c->a_trace);
+        c->a_trace = nullptr;
+        c->a_trace_cap = 0;
+        const int cap = max_steps < 1024 ? 1024 : max_steps;
+        if (check_cuda(c, cudaMalloc(&c->a_trace, sizeof(double) * (size_t)cap), "a_trace alloc")) return IEGPU_ENOMEM;
+        c->a_trace_cap = cap;
+        fp64_destroy_graphs(c);  // graphs captured the old pointer
+    }
+    if (!c->lf_exec[0]) {
+        int rc = build_graphs(c);
+        if (rc) return rc;
+    }
+    fill_ctl(c, bg, kModeLeapfrog);
+    c->ctl_h->af = af;
+    c->ctl_h->steps_limit = max_steps;
+    if (upload_ctl(c)) return IEGPU_ECUDA;
+    const int L = c->lf_steps;
+    const int launches = (max_steps + L - 1) / L;
+    const int start = c->cur;
+    for (int q = 0; q < launches; ++q) {
+        // a full graph of L (even) steps returns to the start buffer
+        if (check_cuda(c, cudaGraphLaunch(c->lf_exec[start], c->stream), "graph launch")) return IEGPU_ECUDA;
+        c->launches += 2LL * L;
+    }
+    int rc = read_ctl(c);
+    const int taken = c->ctl_h->steps_done;
+    // kernels after the last active step exit at once; the buffer holding the
+    // newest f is decided by how many steps ran.
+    c->cur = (start + taken) & 1;
+    if (rc) return rc;
+    copy_bg(c, bg);
+    if (steps) *steps = taken;
+    if (a_trace && taken > 0) {
+        if (check_cuda(c, cudaMemcpy(a_trace, c->a_trace, sizeof(double) * taken, cudaMemcpyDeviceToHost), "a_trace download"))
+            return IEGPU_ECUDA;
+    }
+    return IEGPU_OK;
+}
+
+int fp64_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk) {
+    for (int q = 0; q < nk; ++q) ms[q] = 0.0;
+    fill_ctl(c, bg, kModeLeapfrog);
+    c->ctl_h->af = af;
+    c->ctl_h->steps_limit = nsteps;
+    if (upload_ctl(c)) return IEGPU_ECUDA;
+    const int start = c->cur;
+    for (int s = 0; s < nsteps; ++s) {
+        const int src = (start + s) & 1;
+        float t0 = 0.f, t1 = 0.f;
+        cudaEventRecord(c->ev[0], c->stream);
+        launch_reduce(c, src);
+        cudaEventRecord(c->ev[1], c->stream);
+        launch_kick<kModeLeapfrog>(c, src);
+        cudaEventRecord(c->ev[2], c->stream);
+        if (check_cuda(c, cudaEventSynchronize(c->ev[2]), "profile")) return IEGPU_ECUDA;
+        cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]);
+        if (nk > 0) ms[0] += t0;
+        if (nk > 1) ms[1] += t1;
+    }
+    int rc = read_ctl(c);
+    const int taken = c->ctl_h->steps_done;
+    c->cur = (start + taken) & 1;
+    if (rc) return rc;
+    copy_bg(c, bg);
+    return IEGPU_OK;
+}
+
+int fp64_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    fill_ctl(c, bg, kModeKick);
+    c->ctl_h->d_given = d;
+    if (upload_ctl(c)) return IEGPU_ECUDA;
+    launch_reduce(c, c->cur);
+    launch_kick<kModeKick>(c, c->cur);
+    int rc = read_ctl(c);
+    if (rc) return rc;
+    copy_bg(c, bg);
+    return IEGPU_OK;
+}
+
+int fp64_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    // scalar part on the host, exactly as src/evolution.cpp:262,283
+    bg->t += d;
+    const unsigned grid = (unsigned)((c->gs + kThreads - 1) / kThreads);
+    SigwPtrs sg{};
+    if (c->cfg.sigw)
+        for (int q = 0; q < 6; ++q) { sg.hdst[q] = c->h[c->cur][q]; sg.hd[q] = c->hd[q]; }
+    if (c->cfg.sigw) k_drift<true><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, sg, (long long)c->gs, d);
+    else k_drift<false><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, sg, (long long)c->gs, d);
+    c->launches++;
+    bg->a += d * bg->ad;
+    return sync_and_check(c, "evolve_fields");
+}
+
+int fp64_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]) {
+    const int grid = c->red_grid;
+    c->ctl_h->error = 0;
+    if (check_cuda(c, cudaMemsetAsync(&c->ctl->error, 0, sizeof(int), c->stream), "memset")) return IEGPU_ECUDA;
+    if (c->pot.table) k_energy_sums<true><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, c->pot, c->ctl, c->part, c->lg);
+    else k_energy_sums<false><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, c->pot, c->ctl, c->part, c->lg);
+    c->launches++;
+    std::vector<double> h((size_t)grid * 3);
+    if (check_cuda(c, cudaMemcpyAsync(h.data(), c->part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream), "energy partials"))
+        return IEGPU_ECUDA;
+    int rc = read_ctl(c);
+    if (rc) return rc;
+    double G = 0, Pn = 0, K2 = 0;
+    for (int b = 0; b < grid; ++b) { G += h[3 * b]; Pn += h[3 * b + 1]; K2 += h[3 * b + 2]; }
+    const double gs = (double)c->gs, a = bg->a, s = c->cfg.rescale_s, dx = c->cfg.L / (double)c->N;
+    const double B2 = c->pot.B2;
+    // kin_energy, src/evolution.cpp:139-145
+    out[0] = 0.5 * pow(a, 2.0 * s - 2.0) * (K2 / gs);
+    // gradient_energy, src/evolution.cpp:130-136
+    const double norm = (1.0 / (a * dx)) * (1.0 / (a * dx));
+    out[1] = 0.5 * (-G) * norm / gs;
+    // potential_energy, src/potential.cpp:151-171
+    if (c->pot.table) out[2] = (Pn / B2) / gs;
+    else out[2] = (c->pot.V0 * (gs - c->pot.c1 * Pn) / B2) / gs;
+    return IEGPU_OK;
+}
+
+}  // namespace iegpu

@@ -1,0 +1,62 @@
+// reduce.cuh -- deterministic block and grid reductions.
+//
+// Every reduction runs in a fixed order (warp shuffle tree, then warps in
+// index order, then per-CTA partials in CTA order), so a given launch
+// configuration always returns the same bits.
+#pragma once
+#include "iegpu_internal.cuh"
+
+namespace iegpu {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block of NV values per thread; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+    __shared__ double sh[NV][kThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = warp_sum(v[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[q][w] = v[q];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double x = lane < (kThreads / 32) ? sh[q][lane] : 0.0;
+            v[q] = warp_sum(x);
+        }
+    }
+    __syncthreads();
+}
+
+// Sum of part[b*NV + q] over b = 0..nb-1 by warp 0 in a fixed order; the
+// result is valid in lane 0.
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double* part, int nb, double (&out)[NV]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = 0.0;
+        for (int b = lane; b < nb; b += 32) s += __ldcg(&part[(size_t)b * NV + q]);
+        out[q] = warp_sum(s);
+    }
+}
+
+// Last-CTA detection after each CTA wrote its partials.
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    return last;
+}
+
+}  // namespace iegpu

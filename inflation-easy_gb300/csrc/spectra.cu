@@ -1,0 +1,319 @@
+// spectra.cu -- isotropic shell binning of r2c spectra.
+//
+// Scalar spectra follow write_isotropic_spectrum_from_fft_r2c
+// (src/output.cpp:63-151): the bin of mode (px, py, pz) is
+// lround(sqrt(px^2+py^2+pz^2)); interior modes 1 <= k < N/2 carry weight 2,
+// the k = 0 column and the Nyquist plane weight 1.  Tensor spectra follow
+// write_gw_spectrum_impl (src/output.cpp:466-625): per mode, the lattice
+// momentum k_i = (2/dx) sin(pi p_i/N), the projector P = 1 - khat khat and the
+// TT part Lambda = P C P - P tr(PC)/2 of the 3x3 complex matrix C of the six
+// h components, all in float with the reference's operation order (the
+// sin table is computed on the host with the reference's float expression);
+// bins stop below floor(0.8*numbins).
+//
+// Binning is deterministic: along k the bin index is non-decreasing, so each
+// warp takes 32 consecutive k of one (i, j) row, combines equal bins with a
+// segmented shuffle scan, and the segment tails add into that warp's own
+// shared-memory histogram.  Warps, then CTAs, are combined in index order.
+// Compiled with -fmad=false.
+#include <cmath>
+#include <vector>
+
+#include "iegpu_internal.cuh"
+
+namespace iegpu {
+
+constexpr int kSpecWarps = 4;
+constexpr int kSpecThreads = kSpecWarps * 32;
+
+__device__ __forceinline__ int round_sqrt_int(int n) {
+    // lround(sqrt(n)) for integer n >= 0 (never a tie)
+    int b = (int)(sqrtf((float)n) + 0.5f);
+    while (b * b + b < n) ++b;
+    while (b > 0 && b * b - b >= n) --b;
+    return b;
+}
+
+// Adds (key, value, count) from all lanes into the warp's histogram; keys are
+// non-decreasing across valid lanes, invalid lanes carry unique negative keys.
+__device__ __forceinline__ void warp_segment_add(int key, double v, int cnt, double* wbin, int* wcnt) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double ov = __shfl_up_sync(0xffffffffu, v, o);
+        const int oc = __shfl_up_sync(0xffffffffu, cnt, o);
+        const int ok = __shfl_up_sync(0xffffffffu, key, o);
+        if (lane >= o && ok == key) { v += ov; cnt += oc; }
+    }
+    const int nk = __shfl_down_sync(0xffffffffu, key, 1);
+    const bool tail = (lane == 31) || (nk != key);
+    if (key >= 0 && tail) {
+        wbin[key] += v;
+        wcnt[key] += cnt;
+    }
+    __syncwarp();
+}
+
+template <typename C2>
+__device__ __forceinline__ double mag2(C2 z) { return (double)z.x * (double)z.x + (double)z.y * (double)z.y; }
+
+__global__ void __launch_bounds__(kSpecThreads) k_bin_scalar(const double2* __restrict__ c, const double2* __restrict__ ny,
+                                                             int lgN, int nbins, double* part, int* cpart) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* wb = reinterpret_cast<double*>(smem_raw);
+    int* wc = reinterpret_cast<int*>(wb + kSpecWarps * nbins);
+    const int N = 1 << lgN, M2 = N >> 1;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int q = threadIdx.x; q < kSpecWarps * nbins; q += blockDim.x) { wb[q] = 0.0; wc[q] = 0; }
+    __syncthreads();
+    double* mybin = wb + w * nbins;
+    int* mycnt = wc + w * nbins;
+    const long long rows = (long long)N * N;
+    for (long long r = (long long)blockIdx.x * kSpecWarps + w; r < rows; r += (long long)gridDim.x * kSpecWarps) {
+        const int i = (int)(r >> lgN), j = (int)(r & (N - 1));
+        const int px = (i <= M2 ? i : i - N), py = (j <= M2 ? j : j - N);
+        const int pxy = px * px + py * py;
+        for (int k0 = 1; k0 < M2; k0 += 32) {
+            const int k = k0 + lane;
+            int key = -1 - lane;
+            double v = 0.0;
+            if (k < M2) {
+                const int bin = round_sqrt_int(pxy + k * k);
+                if (bin < nbins) {
+                    const double2 z = c[r * M2 + k];
+                    const double fp2 = z.x * z.x + z.y * z.y;
+                    v = 2.0 * fp2;
+                    key = bin;
+                }
+            }
+            warp_segment_add(key, v, key >= 0 ? 2 : 0, mybin, mycnt);
+        }
+        if (lane == 0) {
+            const int b0 = round_sqrt_int(pxy);
+            if (b0 < nbins) {
+                const double2 z = c[r * M2];
+                mybin[b0] += z.x * z.x + z.y * z.y;
+                mycnt[b0] += 1;
+            }
+            const int b1 = round_sqrt_int(pxy + M2 * M2);
+            if (b1 < nbins) {
+                const double2 z = ny[r];
+                mybin[b1] += z.x * z.x + z.y * z.y;
+                mycnt[b1] += 1;
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+        double s = 0.0;
+        int n = 0;
+        for (int q = 0; q < kSpecWarps; ++q) { s += wb[q * nbins + b]; n += wc[q * nbins + b]; }
+        part[(long long)blockIdx.x * nbins + b] = s;
+        cpart[(long long)blockIdx.x * nbins + b] = n;
+    }
+}
+
+__global__ void k_bin_combine(const double* part, const int* cpart, int nblocks, int nbins, double* out, int* cout) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    double s = 0.0;
+    int n = 0;
+    for (int q = 0; q < nblocks; ++q) { s += part[(long long)q * nbins + b]; n += cpart[(long long)q * nbins + b]; }
+    out[b] = s;
+    cout[b] = n;
+}
+
+// ---- tensor (GW) spectrum -------------------------------------------------
+
+struct GwArgs {
+    const float2* c[6];
+    const float2* ny[6];
+    const float* ksin;   // (2/dx) sin(pi p/N), p = -N/2..N/2 stored at [p + N/2]
+    double to_phys_d;
+    int scale;           // 0: none, 1: (float)((double)x * to_phys)
+    int imax;            // bins >= imax are dropped
+};
+
+__device__ __forceinline__ float gw_tt(const float (&Cr)[3][3], const float (&Ci)[3][3], float kx, float ky, float kz,
+                                       float kt2) {
+    const float inv = 1.0f / sqrtf(kt2);
+    const float kh[3] = {kx * inv, ky * inv, kz * inv};
+    float P[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) P[a][b] = (a == b ? 1.f : 0.f) - kh[a] * kh[b];
+    float Ar[3][3], Ai[3][3], Tr = 0.f, Ti = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            float r = 0.f, q = 0.f;
+#pragma unroll
+            for (int l = 0; l < 3; ++l)
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    const float pal = P[a][l], pbm = P[b][m];
+                    r += pal * Cr[l][m] * pbm;
+                    q += pal * Ci[l][m] * pbm;
+                }
+            Ar[a][b] = r;
+            Ai[a][b] = q;
+        }
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            Tr += P[l][m] * Cr[l][m];
+            Ti += P[l][m] * Ci[l][m];
+        }
+    float fp2 = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float Xr = Ar[a][b] - 0.5f * P[a][b] * Tr;
+            const float Xi = Ai[a][b] - 0.5f * P[a][b] * Ti;
+            fp2 += Xr * Xr + Xi * Xi;
+        }
+    return fp2;
+}
+
+__device__ __forceinline__ void gw_load(const GwArgs& A, bool nyq, long long idx, float (&Cr)[3][3], float (&Ci)[3][3]) {
+    // packed components: 0 xx, 1 yy, 2 zz, 3 xy, 4 xz, 5 yz (src/main.h:42-64)
+    const int comp[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const float2 z = nyq ? A.ny[comp[l][m]][idx] : A.c[comp[l][m]][idx];
+            float re = z.x, im = z.y;
+            if (A.scale) {
+                re = (float)((double)re * A.to_phys_d);
+                im = (float)((double)im * A.to_phys_d);
+            }
+            Cr[l][m] = re;
+            Ci[l][m] = im;
+        }
+}
+
+__global__ void __launch_bounds__(kSpecThreads) k_bin_gw(GwArgs A, int lgN, int nbins, double* part, int* cpart) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* wb = reinterpret_cast<double*>(smem_raw);
+    int* wc = reinterpret_cast<int*>(wb + kSpecWarps * nbins);
+    const int N = 1 << lgN, M2 = N >> 1;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int q = threadIdx.x; q < kSpecWarps * nbins; q += blockDim.x) { wb[q] = 0.0; wc[q] = 0; }
+    __syncthreads();
+    double* mybin = wb + w * nbins;
+    int* mycnt = wc + w * nbins;
+    const long long rows = (long long)N * N;
+    const float* ks = A.ksin + M2;  // ks[p] for p in [-M2+1, M2]
+    for (long long r = (long long)blockIdx.x * kSpecWarps + w; r < rows; r += (long long)gridDim.x * kSpecWarps) {
+        const int i = (int)(r >> lgN), j = (int)(r & (N - 1));
+        const int px = (i <= M2 ? i : i - N), py = (j <= M2 ? j : j - N);
+        const int pxy = px * px + py * py;
+        const float kx = ks[px], ky = ks[py];
+        for (int k0 = 1; k0 < M2; k0 += 32) {
+            const int k = k0 + lane;
+            int key = -1 - lane;
+            double v = 0.0;
+            if (k < M2) {
+                const float kz = ks[k];
+                const float kt2 = kx * kx + ky * ky + kz * kz;
+                const int bin = (int)roundf(sqrtf((float)(pxy + k * k)));
+                if (kt2 != 0.f && bin < A.imax) {
+                    float Cr[3][3], Ci[3][3];
+                    gw_load(A, false, r * M2 + k, Cr, Ci);
+                    const float fp2 = gw_tt(Cr, Ci, kx, ky, kz, kt2);
+                    v = (double)(2.f * fp2);
+                    key = bin;
+                }
+            }
+            warp_segment_add(key, v, key >= 0 ? 2 : 0, mybin, mycnt);
+        }
+        if (lane < 2) {
+            // k = 0 (lane 0) and k = N/2 (lane 1); bins differ, lanes write in turn
+            for (int t = 0; t < 2; ++t) {
+                if (lane == t) {
+                    const int pz = t ? M2 : 0;
+                    const float kz = ks[pz];
+                    const float kt2 = kx * kx + ky * ky + kz * kz;
+                    const int bin = (int)roundf(sqrtf((float)(pxy + pz * pz)));
+                    if (kt2 != 0.f && bin < A.imax) {
+                        float Cr[3][3], Ci[3][3];
+                        gw_load(A, t == 1, t ? r : r * M2, Cr, Ci);
+                        const float fp2 = gw_tt(Cr, Ci, kx, ky, kz, kt2);
+                        mybin[bin] += (double)fp2;
+                        mycnt[bin] += 1;
+                    }
+                }
+                __syncwarp(0x3u);
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+        double s = 0.0;
+        int n = 0;
+        for (int q = 0; q < kSpecWarps; ++q) { s += wb[q * nbins + b]; n += wc[q * nbins + b]; }
+        part[(long long)blockIdx.x * nbins + b] = s;
+        cpart[(long long)blockIdx.x * nbins + b] = n;
+    }
+}
+
+// ---------------------------------------------------------------------------
+
+static int finish_bins(iegpu_ctx* c, int nbins, int* counts, double* f2) {
+    double* out = c->misc;
+    int* cout = reinterpret_cast<int*>(c->misc + nbins);
+    k_bin_combine<<<(nbins + 127) / 128, 128, 0, c->stream>>>(c->spec_part, c->spec_cnt, c->spec_blocks, nbins, out, cout);
+    c->launches++;
+    if (check_cuda(c, cudaMemcpyAsync(c->misc_h, c->misc, sizeof(double) * nbins + sizeof(int) * nbins,
+                                      cudaMemcpyDeviceToHost, c->stream), "spectrum download"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "spectrum")) return IEGPU_ECUDA;
+    const int* ch = reinterpret_cast<const int*>(c->misc_h + nbins);
+    for (int b = 0; b < nbins; ++b) { f2[b] = c->misc_h[b]; counts[b] = ch[b]; }
+    return IEGPU_OK;
+}
+
+int spectrum_bin_d(iegpu_ctx* c, const double* f, const double* fny, int* counts, double* f2, int nbins) {
+    const size_t smem = (size_t)kSpecWarps * nbins * (sizeof(double) + sizeof(int));
+    k_bin_scalar<<<c->spec_blocks, kSpecThreads, smem, c->stream>>>(reinterpret_cast<const double2*>(f),
+                                                                     reinterpret_cast<const double2*>(fny), c->lg, nbins,
+                                                                     c->spec_part, c->spec_cnt);
+    c->launches++;
+    return finish_bins(c, nbins, counts, f2);
+}
+
+int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins) {
+    const int N = c->N, M2 = N / 2;
+    // kx table with the reference's float expression, src/output.cpp:493-495
+    const float pi_f = (float)(2.0 * std::asin(1.0));
+    const float dx_f = (float)(c->cfg.L / (double)N);
+    std::vector<float> ks((size_t)N + 1);
+    for (int p = -M2; p <= M2; ++p) ks[(size_t)(p + M2)] = (2.f / dx_f) * std::sin(pi_f * p / (float)N);
+    // device copy lives in misc scratch after the bin outputs
+    float* dks = reinterpret_cast<float*>(c->misc + 2 * (size_t)nbins + 8);
+    if (check_cuda(c, cudaMemcpyAsync(dks, ks.data(), sizeof(float) * ks.size(), cudaMemcpyHostToDevice, c->stream), "ksin"))
+        return IEGPU_ECUDA;
+    GwArgs A{};
+    for (int q = 0; q < 6; ++q) {
+        A.c[q] = reinterpret_cast<const float2*>(which ? c->hd[q] : c->h[c->cur][q]);
+        A.ny[q] = reinterpret_cast<const float2*>(which ? c->hdny[q] : c->hny[q]);
+    }
+    A.ksin = dks;
+    A.to_phys_d = to_phys;
+    A.scale = which ? 1 : 0;
+    const int numbins = (int)(std::sqrt(3.0) * (N / 2)) + 1;
+    A.imax = (int)std::floor(0.80 * numbins);
+    const size_t smem = (size_t)kSpecWarps * nbins * (sizeof(double) + sizeof(int));
+    k_bin_gw<<<c->spec_blocks, kSpecThreads, smem, c->stream>>>(A, c->lg, nbins, c->spec_part, c->spec_cnt);
+    c->launches++;
+    return finish_bins(c, nbins, counts, f2);
+}
+
+}  // namespace iegpu

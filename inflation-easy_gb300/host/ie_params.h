@@ -1,0 +1,61 @@
+// ie_params.h -- run-time parameters of the host program.
+//
+// The keys, defaults and derived values of the reference's params.txt handling
+// (src/runtime_parameters.cpp:17-112, 195-365).  The switches the reference
+// fixes at compile time in src/parameters.h (N, numerical_potential,
+// perform_deltaN, calculate_SIGW, the deltaN criterion) are run-time keys
+// here, plus `form` (fp64 | split) for the engine's arithmetic form.
+#pragma once
+
+#include <string>
+
+struct IeParams {
+    // compile-time switches of the reference, run-time here
+    int N = 128;
+    int numerical_potential = 1;
+    int perform_deltaN = 1;
+    int calculate_SIGW = 0;
+    int criterion = 99;          // 99: derive from numerical_potential (src/parameters.h:65-71)
+    int form = 0;                // 0 fp64, 1 split
+    int ic_on_host = 0;          // 1: draw the initial modes on the host (bit-identical to the reference)
+    // src/runtime_parameters.cpp:17-112
+    int seed = 8;
+    double rescale_s = 0.0;
+    double af = 256.0;
+    double V0 = 3e-9;
+    double rescale_B = 0.0;
+    double ns = 0.97;
+    double initial_field = 2.9181235049318586;
+    double initial_derivative = -0.06727651095116181;
+    double L = 10.0;
+    double dt = 0.001;
+    int output_freq = 500;
+    int output_infrequent_freq = 500;
+    double dN = 0.0001;
+    double Nend = 5.0;
+    int use_phiref_manual = 0;
+    double phiref_manual_value = 0.0;
+    double high_cutoff_index = 0.0;
+    double low_cutoff_index = 0.0;
+    int forcing_cutoff = 0;
+    int output_spectra = 1;
+    int output_histogram = 1;
+    int output_energy = 1;
+    int output_box3D = 0;
+    int output_box2D = 0;
+    int output_bispectrum = 0;
+    int output_LOG = 0;
+    int screen_updates = 1;
+    int nbins = 256;
+    int int_err = 5;
+    int int_errN = 5;
+    double dx = 0.0;
+    std::string inflation_integrator = "leapfrog";
+    std::string deltaN_integrator = "leapfrog";
+};
+
+// Defaults of the reference for the given potential kind and N.
+void ie_params_defaults(IeParams& p, int N, int numerical);
+// Reads params.txt (missing file keeps the defaults); warns on unknown keys
+// as src/runtime_parameters.cpp:333-339 does.  Returns false on a fatal error.
+bool ie_params_load(IeParams& p, const char* path);

@@ -1,0 +1,293 @@
+"""ctypes binding of the C ABI in include/iegpu.h (libiegpu.so).
+
+This is the Python face of the drop-in boundary: the same calls a C/C++ host
+makes (see ie_gpu_main in host/), with numpy arrays in the reference layout
+(N^3, index (i*N + j)*N + k).  There is no CPU fallback: importing this module
+without a built libiegpu.so raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libiegpu.so"
+
+OK, EINVAL, ECUDA, ERANGE, ENAN, ECOURANT, ENOMEM, ETABLE, EUNSUPPORTED, ETIMEOUT = range(10)
+POT_HILLTOP, POT_TABLE = 0, 1
+FORM_FP64, FORM_SPLIT = 0, 1
+CRIT_GENERIC, CRIT_MONOTONIC, CRIT_ANTIMONOTONIC = 0, 1, -1
+F, FD, DELTAN = 0, 1, 2
+
+
+def H(c: int) -> int:
+    return 8 + c
+
+
+def HD(c: int) -> int:
+    return 16 + c
+
+
+class Config(C.Structure):
+    _fields_ = [("N", C.c_int), ("potential", C.c_int), ("sigw", C.c_int), ("form", C.c_int),
+                ("criterion", C.c_int), ("L", C.c_double), ("dt", C.c_double), ("rescale_s", C.c_double),
+                ("rescale_B", C.c_double), ("V0", C.c_double), ("ns", C.c_double)]
+
+
+class Bg(C.Structure):
+    _fields_ = [("t", C.c_double), ("a", C.c_double), ("ad", C.c_double), ("ad2", C.c_double),
+                ("astep", C.c_double)]
+
+    def as_tuple(self):
+        return (self.t, self.a, self.ad, self.ad2, self.astep)
+
+
+class IegpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"iegpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise FileNotFoundError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
+    lib = C.CDLL(str(LIB_PATH))
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    dp, ip, fp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_float)
+    sig = {
+        "iegpu_version": (I, []),
+        "iegpu_strerror": (C.c_char_p, [I]),
+        "iegpu_create": (I, [C.POINTER(Config), C.POINTER(P)]),
+        "iegpu_destroy": (I, [P]),
+        "iegpu_last_error": (C.c_char_p, [P]),
+        "iegpu_stream": (P, [P]),
+        "iegpu_launch_count": (C.c_longlong, [P]),
+        "iegpu_set_table": (I, [P, dp, dp, dp, I]),
+        "iegpu_upload": (I, [P, I, P, P]),
+        "iegpu_download": (I, [P, I, P, P]),
+        "iegpu_add": (I, [P, I, D]),
+        "iegpu_evolve_fields": (I, [P, D, C.POINTER(Bg)]),
+        "iegpu_evolve_derivs": (I, [P, D, C.POINTER(Bg)]),
+        "iegpu_leapfrog": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
+        "iegpu_energies": (I, [P, C.POINTER(Bg), dp]),
+        "iegpu_means": (I, [P, dp]),
+        "iegpu_bunch_davies": (I, [P, I, D, D, D, D, dp]),
+        "iegpu_timer_start": (I, [P]),
+        "iegpu_timer_stop": (I, [P, C.POINTER(C.c_float)]),
+        "iegpu_profile_leapfrog": (I, [P, D, I, C.POINTER(Bg), dp, I]),
+        "iegpu_histogram": (I, [P, I, I, dp, dp, dp]),
+        "iegpu_fft": (I, [P, I, I]),
+        "iegpu_numbins": (I, [I]),
+        "iegpu_spectrum": (I, [P, I, ip, dp, I]),
+        "iegpu_gw_spectrum": (I, [P, I, D, ip, dp, I]),
+        "iegpu_initializeN": (I, [P, D]),
+        "iegpu_get_phiref": (I, [P, dp]),
+        "iegpu_evolve_fieldsN": (I, [P, D, D]),
+        "iegpu_evolve_derivsN": (I, [P, D]),
+        "iegpu_deltaN_steps": (I, [P, D, I, D]),
+        "iegpu_saveN_mean": (I, [P, D, fp]),
+        "iegpu_shift": (I, [P, I, D]),
+        "iegpu_zero_above": (I, [P, I, D]),
+        "iegpu_sum": (I, [P, I, dp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray, dtype) -> C.c_void_p:
+    assert a.dtype == dtype and a.flags["C_CONTIGUOUS"], (a.dtype, dtype)
+    return C.c_void_p(a.ctypes.data)
+
+
+class Lattice:
+    """One device lattice (an iegpu context)."""
+
+    def __init__(self, N: int, L: float, dt: float, V0: float, ns: float = 0.97, rescale_B: float | None = None,
+                 rescale_s: float = 0.0, potential: int = POT_HILLTOP, sigw: bool = False, form: int = FORM_FP64,
+                 criterion: int | None = None):
+        self.lib = load()
+        if rescale_B is None:
+            rescale_B = float(np.sqrt(V0))
+        if criterion is None:
+            criterion = CRIT_MONOTONIC if potential == POT_TABLE else CRIT_ANTIMONOTONIC
+        self.cfg = Config(N, potential, int(bool(sigw)), form, criterion, L, dt, rescale_s, rescale_B, V0, ns)
+        self.N = N
+        self.sigw = bool(sigw)
+        h = C.c_void_p()
+        rc = self.lib.iegpu_create(C.byref(self.cfg), C.byref(h))
+        if rc != OK:
+            raise IegpuError(rc, self.lib.iegpu_strerror(rc).decode())
+        self.h = h
+
+    # -- plumbing ---------------------------------------------------------
+    def _check(self, rc: int) -> None:
+        if rc != OK:
+            raise IegpuError(rc, self.lib.iegpu_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.iegpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        return self.lib.iegpu_stream(self.h) or 0
+
+    @property
+    def launches(self) -> int:
+        return self.lib.iegpu_launch_count(self.h)
+
+    # -- state ------------------------------------------------------------
+    def set_table(self, phi: np.ndarray, V: np.ndarray, dV: np.ndarray) -> None:
+        phi, V, dV = (np.ascontiguousarray(x, dtype=np.float64) for x in (phi, V, dV))
+        dp = C.POINTER(C.c_double)
+        self._check(self.lib.iegpu_set_table(self.h, phi.ctypes.data_as(dp), V.ctypes.data_as(dp),
+                                             dV.ctypes.data_as(dp), len(phi)))
+
+    def upload(self, field: int, host: np.ndarray, nyquist: np.ndarray | None = None) -> None:
+        dt = np.float64 if field in (F, FD, DELTAN) else np.float32
+        host = np.ascontiguousarray(host, dtype=dt)
+        ny = None if nyquist is None else np.ascontiguousarray(nyquist, dtype=dt)
+        self._check(self.lib.iegpu_upload(self.h, field, _ptr(host, dt), None if ny is None else _ptr(ny, dt)))
+
+    def download(self, field: int, nyquist: bool = False):
+        dt = np.float64 if field in (F, FD, DELTAN) else np.float32
+        out = np.empty(self.N ** 3, dtype=dt)
+        ny = np.empty(2 * self.N * self.N, dtype=dt) if nyquist else None
+        self._check(self.lib.iegpu_download(self.h, field, _ptr(out, dt), None if ny is None else _ptr(ny, dt)))
+        return (out, ny) if nyquist else out
+
+    def add(self, field: int, value: float) -> None:
+        self._check(self.lib.iegpu_add(self.h, field, value))
+
+    # -- initial conditions -----------------------------------------------
+    def bunch_davies(self, seed: int, phi0: float, dphi0: float, high_cut: float = 0.0, low_cut: float = 0.0) -> float:
+        h = C.c_double()
+        self._check(self.lib.iegpu_bunch_davies(self.h, seed, phi0, dphi0, high_cut, low_cut, C.byref(h)))
+        return h.value
+
+    # -- leapfrog ---------------------------------------------------------
+    def evolve_fields(self, d: float, bg: Bg) -> None:
+        self._check(self.lib.iegpu_evolve_fields(self.h, d, C.byref(bg)))
+
+    def evolve_derivs(self, d: float, bg: Bg) -> None:
+        self._check(self.lib.iegpu_evolve_derivs(self.h, d, C.byref(bg)))
+
+    def leapfrog(self, af: float, max_steps: int, bg: Bg, trace: bool = False):
+        steps = C.c_int(0)
+        tr = np.zeros(max(1, max_steps), dtype=np.float64) if trace else None
+        self._check(self.lib.iegpu_leapfrog(self.h, af, max_steps, C.byref(bg), C.byref(steps),
+                                            None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
+        return (steps.value, tr[:steps.value]) if trace else steps.value
+
+    def energies(self, bg: Bg):
+        out = (C.c_double * 3)()
+        self._check(self.lib.iegpu_energies(self.h, C.byref(bg), out))
+        return tuple(out)
+
+    # -- measurement ------------------------------------------------------
+    def timer_start(self) -> None:
+        self._check(self.lib.iegpu_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_float()
+        self._check(self.lib.iegpu_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def profile_leapfrog(self, af: float, nsteps: int, bg: Bg):
+        ms = (C.c_double * 2)()
+        self._check(self.lib.iegpu_profile_leapfrog(self.h, af, nsteps, C.byref(bg), ms, 2))
+        return tuple(ms)
+
+    # -- diagnostics ------------------------------------------------------
+    def means(self):
+        out = (C.c_double * 3)()
+        self._check(self.lib.iegpu_means(self.h, out))
+        return tuple(out)
+
+    def histogram(self, field: int, nbins: int):
+        bmin, df = C.c_double(), C.c_double()
+        freq = np.zeros(nbins, dtype=np.float64)
+        self._check(self.lib.iegpu_histogram(self.h, field, nbins, C.byref(bmin), C.byref(df),
+                                             freq.ctypes.data_as(C.POINTER(C.c_double))))
+        return bmin.value, df.value, freq
+
+    def fft(self, field: int, forward: int) -> None:
+        self._check(self.lib.iegpu_fft(self.h, field, forward))
+
+    def numbins(self) -> int:
+        return self.lib.iegpu_numbins(self.N)
+
+    def spectrum(self, field: int):
+        nb = self.numbins()
+        counts = np.zeros(nb, dtype=np.int32)
+        f2 = np.zeros(nb, dtype=np.float64)
+        self._check(self.lib.iegpu_spectrum(self.h, field, counts.ctypes.data_as(C.POINTER(C.c_int)),
+                                            f2.ctypes.data_as(C.POINTER(C.c_double)), nb))
+        return counts, f2
+
+    def gw_spectrum(self, which: int, to_phys: float = 1.0):
+        nb = self.numbins()
+        counts = np.zeros(nb, dtype=np.int32)
+        f2 = np.zeros(nb, dtype=np.float64)
+        self._check(self.lib.iegpu_gw_spectrum(self.h, which, to_phys, counts.ctypes.data_as(C.POINTER(C.c_int)),
+                                               f2.ctypes.data_as(C.POINTER(C.c_double)), nb))
+        return counts, f2
+
+    # -- deltaN -----------------------------------------------------------
+    def initializeN(self, a: float) -> None:
+        self._check(self.lib.iegpu_initializeN(self.h, a))
+
+    def get_phiref(self) -> float:
+        v = C.c_double()
+        self._check(self.lib.iegpu_get_phiref(self.h, C.byref(v)))
+        return v.value
+
+    def evolve_fieldsN(self, d: float, phiref: float) -> None:
+        self._check(self.lib.iegpu_evolve_fieldsN(self.h, d, phiref))
+
+    def evolve_derivsN(self, d: float) -> None:
+        self._check(self.lib.iegpu_evolve_derivsN(self.h, d))
+
+    def deltaN_steps(self, dN: float, nsteps: int, phiref: float) -> None:
+        self._check(self.lib.iegpu_deltaN_steps(self.h, dN, nsteps, phiref))
+
+    def saveN_mean(self, cutoff: float) -> float:
+        v = C.c_float()
+        self._check(self.lib.iegpu_saveN_mean(self.h, cutoff, C.byref(v)))
+        return v.value
+
+    def shift(self, field: int, value: float) -> None:
+        self._check(self.lib.iegpu_shift(self.h, field, value))
+
+    def zero_above(self, field: int, thr: float) -> None:
+        self._check(self.lib.iegpu_zero_above(self.h, field, thr))
+
+    def sum(self, field: int) -> float:
+        v = C.c_double()
+        self._check(self.lib.iegpu_sum(self.h, field, C.byref(v)))
+        return v.value

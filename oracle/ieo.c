@@ -1066,6 +1066,18 @@ float ieo_saveN_mean(const ieo_state* S, double cutoff) {
 /* program, src/main.cpp:103-146 and src/output.cpp                          */
 /* ------------------------------------------------------------------------- */
 
+/* trace of the background scalars at each save, and full-precision copies of
+ * the printed means and spectra (program runner only) */
+static FILE* g_trace;
+static FILE* g_prec;
+
+static void prec_line(const char* tag, const double* v, int n) {
+    if (!g_prec) return;
+    fprintf(g_prec, "%s", tag);
+    for (int i = 0; i < n; ++i) fprintf(g_prec, " %.17g", v[i]);
+    fprintf(g_prec, "\n");
+}
+
 typedef struct {
     char dir[1024];
     FILE *output, *means, *vars, *velocity, *sf, *energy, *conservation, *spectra, *spectratimes,
@@ -1084,14 +1096,18 @@ static FILE* open_out(ieo_state* S, outfiles* O, FILE** slot, const char* name) 
 }
 
 /* write_isotropic_spectrum_from_fft_r2c printing, src/output.cpp:143-150 */
-static void print_spectrum(FILE* out, int N, double L, const int* counts, double* f2, double norm1) {
+static void print_spectrum(FILE* out, int N, double L, const int* counts, double* f2, double norm1, const char* tag) {
     const int numbins = ieo_numbins(N);
     const double dp = 2.0 * (2.0 * asin(1.0)) / L;
+    double* pv = (double*)malloc(sizeof(double) * numbins);
     for (int i = 0; i < numbins; i++) {
         const double pi_ = dp * i;
         if (counts[i] > 0) f2[i] /= (double)counts[i];
         fprintf(out, "%e %d %e\n", pi_, counts[i], norm1 * f2[i]);
+        pv[i] = norm1 * f2[i];
     }
+    prec_line(tag, pv, numbins);
+    free(pv);
     fprintf(out, "\n");
     fflush(out);
 }
@@ -1111,6 +1127,10 @@ static int out_meansvars(ieo_state* S, outfiles* O) {
     vel = vel / (double)S->gs;
     vel = vel * pow(S->a, S->p.rescale_s - 1.0) * S->p.rescale_B;
     fprintf(m, " %e", av); fprintf(ve, " %e", vel); fprintf(v, " %e", var - pw2(av));
+    {
+        const double q[5] = {S->t, S->a, av, vel, S->ad * S->p.rescale_B * pow(S->a, S->p.rescale_s - 2.0)};
+        prec_line("means", q, 5);
+    }
     if (av + DBL_MAX == av || (av != 0. && av / av != 1.)) {
         set_err(S, "Unstable solution developed. Scalar field not numerical at t=%f\n", S->t);
         fflush(m); fflush(v);
@@ -1197,7 +1217,14 @@ static void out_gw(ieo_state* S, outfiles* O, int which) {
     int* counts = (int*)calloc(numbins, sizeof(int));
     float* f2 = (float*)calloc(numbins, sizeof(float));
     const double to_phys = which ? S->p.rescale_B * pow(S->a, S->p.rescale_s - 1.0) : 1.0;
-    ieo_gw_spectrum(S, which, to_phys, counts, f2, NULL);
+    double* f2d = (double*)calloc(numbins, sizeof(double));
+    ieo_gw_spectrum(S, which, to_phys, counts, f2, f2d);
+    if (g_prec) {
+        const double n1 = 0.5 * pow(S->p.L / S->p.rescale_B, 3) / pow((double)N, 6);
+        for (int i = 0; i < numbins; ++i) f2d[i] = counts[i] > 0 ? n1 * f2d[i] / counts[i] : 0.0;
+        prec_line(which ? "spectrumGWdot" : "spectrumGW", f2d, numbins);
+    }
+    free(f2d);
     const float dp = 2.f * (float)S->pi / (float)S->p.L;
     const float norm1 = 0.5f * pow(S->p.L / S->p.rescale_B, 3) / pow((double)(float)N, 6);
     for (int i = 0; i < numbins; ++i) {
@@ -1213,6 +1240,8 @@ static void out_gw(ieo_state* S, outfiles* O, int which) {
 /* save(), src/output.cpp:1469-1503 */
 static int out_save(ieo_state* S, outfiles* O, int infrequent) {
     const ieo_params* p = &S->p;
+    if (g_trace)
+        fprintf(g_trace, "save %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, S->t, S->a, S->ad, S->ad2, S->astep);
     if (S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt * pow(S->astep, p->rescale_s - 1));
     if (out_meansvars(S, O)) return 1;
     out_scale(S, O);
@@ -1237,7 +1266,7 @@ static int out_save(ieo_state* S, outfiles* O, int infrequent) {
             const double norm1 = pow(p->L / p->rescale_B, 3) / pow((double)p->N, 6);
             ieo_fftrn_d(S->f, S->fny, p->N, 1);
             ieo_bin_spectrum(p->N, S->f, S->fny, counts, f2);
-            print_spectrum(sp, p->N, p->L, counts, f2, norm1);
+            print_spectrum(sp, p->N, p->L, counts, f2, norm1, "spectrum");
             fprintf(st, "%f %e\n", S->t, S->a);
             fflush(st);
             if (p->high_cutoff_index > 0 && p->forcing_cutoff) {
@@ -1298,6 +1327,7 @@ static void out_modes(ieo_state* S, outfiles* O) {
 /* saveN(), src/output.cpp:1522-1560, with spectraN() of :1140-1169 */
 static int out_saveN(ieo_state* S, outfiles* O) {
     const ieo_params* p = &S->p;
+    if (g_trace) fprintf(g_trace, "saveN %.17g %.17g %.17g %.17g\n", S->t, S->a, S->Ne, S->phiref);
     if (S->t > 0.) ieo_evolve_fieldsN(S, -.5 * p->dN);
     const double cutoff = p->Nend - p->dN;
     const float Nmean = ieo_saveN_mean(S, cutoff);
@@ -1320,7 +1350,7 @@ static int out_saveN(ieo_state* S, outfiles* O) {
         const double norm1 = pow(p->L / p->rescale_B, 3) / pow((double)p->N, 6);
         ieo_fftrn_d(S->deltaN, S->fny, p->N, 1);
         ieo_bin_spectrum(p->N, S->deltaN, S->fny, counts, f2);
-        print_spectrum(sp, p->N, p->L, counts, f2, norm1);
+        print_spectrum(sp, p->N, p->L, counts, f2, norm1, "spectrumN");
         ieo_fftrn_d(S->deltaN, S->fny, p->N, -1);
         free(counts); free(f2);
     }
@@ -1354,7 +1384,31 @@ static void close_all(outfiles* O) {
         if (*all[q]) { fclose(*all[q]); *all[q] = NULL; }
 }
 
+static void write_state(ieo_state* S, const char* path) {
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return;
+    const double scal[8] = {S->t, S->a, S->ad, S->ad2, S->astep, S->Ne, S->phiref, S->hubble_init};
+    const int hdr[4] = {S->p.N, S->p.perform_deltaN, S->p.calculate_SIGW, S->p.numerical_potential};
+    fwrite(hdr, sizeof(int), 4, fp);
+    fwrite(scal, sizeof(double), 8, fp);
+    fwrite(S->f, sizeof(double), S->gs, fp);
+    fwrite(S->fd, sizeof(double), S->gs, fp);
+    if (S->p.perform_deltaN) fwrite(S->deltaN, sizeof(double), S->gs, fp);
+    if (S->p.calculate_SIGW) {
+        for (int c = 0; c < 6; ++c) fwrite(S->h[c], sizeof(float), S->gs, fp);
+        for (int c = 0; c < 6; ++c) fwrite(S->hd[c], sizeof(float), S->gs, fp);
+    }
+    fclose(fp);
+}
+
 int ieo_run_program(const ieo_params* p, const char* results_dir, const char* inputs_dir) {
+    return ieo_run_program_dump(p, results_dir, inputs_dir, NULL);
+}
+
+/* As ieo_run_program; when dump_dir is given, also writes trace.txt (the
+ * background scalars at every save) and state.bin (the final state) there,
+ * in the format of oracle/ref_driver.cpp. */
+int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const char* inputs_dir, const char* dump_dir) {
     outfiles O;
     memset(&O, 0, sizeof O);
     snprintf(O.dir, sizeof O.dir, "%s", results_dir);
@@ -1365,6 +1419,12 @@ int ieo_run_program(const ieo_params* p, const char* results_dir, const char* in
     char path[1200];
     snprintf(path, sizeof path, "%s/output.txt", results_dir);
     O.output = fopen(path, "w");
+    if (dump_dir) {
+        snprintf(path, sizeof path, "%s/trace.txt", dump_dir);
+        g_trace = fopen(path, "w");
+        snprintf(path, sizeof path, "%s/precise.txt", dump_dir);
+        g_prec = fopen(path, "w");
+    }
     if (!O.output) goto done;
     if (p->numerical_potential) {
         double *x = NULL, *V = NULL, *dV = NULL;
@@ -1434,8 +1494,14 @@ int ieo_run_program(const ieo_params* p, const char* results_dir, const char* in
         ieo_evolve_fieldsN(S, -0.5 * p->dN);
     }
     fprintf(O.output, "InflationEasy program finished\n");
+    if (dump_dir) {
+        snprintf(path, sizeof path, "%s/state.bin", dump_dir);
+        write_state(S, path);
+    }
     rc = 0;
 done:
+    if (g_trace) { fclose(g_trace); g_trace = NULL; }
+    if (g_prec) { fclose(g_prec); g_prec = NULL; }
     if (rc && S->err) {
         fprintf(stderr, "%s", S->errmsg);
     }

@@ -138,6 +138,8 @@ float ieo_saveN_mean(const ieo_state* S, double cutoff);
  * files into results_dir (inputs_dir holds field_values.dat, potential.dat,
  * potential_derivative.dat when numerical_potential = 1). */
 int ieo_run_program(const ieo_params* p, const char* results_dir, const char* inputs_dir);
+/* Same, also writing trace.txt and state.bin into dump_dir (NULL: none). */
+int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const char* inputs_dir, const char* dump_dir);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,97 @@
+"""Generate the golden fixtures of tests/golden/ from the reference program.
+
+Runs the unmodified reference (caravangelo/inflation-easy, built from its own
+sources by oracle/build_ref.py) on small lattices and stores, per case:
+  <case>/results/*.dat     the reference's own text outputs
+  <case>/trace.txt         background scalars at every save(), full precision
+  <case>/state.npz         final f, fd, deltaN (and h, hd) in binary
+  <case>/params.txt        the params file the reference read
+This script needs the reference tree, so it runs only where that exists; the
+fixtures it writes are committed and travel without it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "oracle"))
+import build_ref  # noqa: E402
+
+HILLTOP = dict(seed=8, dt=0.001, V0=3.338e-13, ns=0.97, initial_field=0.0935, initial_derivative=0.000796, L=10.0,
+               output_freq=500, output_infrequent_freq=500, output_spectra=1, output_histogram=1, output_energy=1,
+               output_box3D=0, output_box2D=0, output_bispectrum=0, screen_updates=0, nbins=256, dN=1e-7,
+               Nend=0.001, use_phiref_manual=0, output_LOG=0)
+USR = dict(seed=8, dt=0.001, V0=3e-9, initial_field=2.9181235049318586, initial_derivative=-0.06727651095116181,
+           L=10.0, output_freq=500, output_infrequent_freq=500, output_spectra=1, output_histogram=1,
+           output_energy=1, output_box3D=0, output_box2D=1, output_bispectrum=0, screen_updates=0, nbins=256,
+           dN=1e-4, Nend=2.0, use_phiref_manual=0, output_LOG=0)
+
+# name: (N, numerical, sigw, deltaN, params)
+CASES = {
+    "n16_hilltop": (16, 0, 0, 1, HILLTOP),
+    "n16_usr_sigw": (16, 1, 1, 1, USR),
+    "n32_hilltop": (32, 0, 0, 1, HILLTOP),
+}
+
+
+def params_text(p: dict) -> str:
+    return "".join(f"{k} = {v!r}\n" if isinstance(v, float) else f"{k} = {v}\n" for k, v in p.items())
+
+
+def read_state(path: Path):
+    raw = path.read_bytes()
+    hdr = np.frombuffer(raw[:16], dtype=np.int32)
+    N, dn, sigw, _num = (int(x) for x in hdr)
+    off = 16
+    scal = np.frombuffer(raw[off:off + 64], dtype=np.float64).copy()
+    off += 64
+    gs = N ** 3
+    out = {"scalars": scal}
+    out["f"] = np.frombuffer(raw[off:off + 8 * gs], dtype=np.float64).copy(); off += 8 * gs
+    out["fd"] = np.frombuffer(raw[off:off + 8 * gs], dtype=np.float64).copy(); off += 8 * gs
+    if dn:
+        out["deltaN"] = np.frombuffer(raw[off:off + 8 * gs], dtype=np.float64).copy(); off += 8 * gs
+    if sigw:
+        out["h"] = np.frombuffer(raw[off:off + 24 * gs], dtype=np.float32).reshape(6, gs).copy(); off += 24 * gs
+        out["hd"] = np.frombuffer(raw[off:off + 24 * gs], dtype=np.float32).reshape(6, gs).copy(); off += 24 * gs
+    return out
+
+
+def main() -> None:
+    if not build_ref.ref_available():
+        raise SystemExit("reference tree not available; fixtures are generated where it is")
+    for name, (N, num, sigw, dn, p) in CASES.items():
+        exe = build_ref.build(N, num, sigw, dn)
+        work = ROOT / "oracle" / "_ref" / f"golden_{name}"
+        if work.exists():
+            shutil.rmtree(work)
+        work.mkdir(parents=True)
+        (work / "params.txt").write_text(params_text(p))
+        os.symlink(HERE / "inputs", work / "inputs")
+        subprocess.run([str(exe), str(work)], check=True, stdout=subprocess.DEVNULL)
+        dst = HERE / name
+        if dst.exists():
+            shutil.rmtree(dst)
+        (dst / "results").mkdir(parents=True)
+        for f in sorted((work / "results").iterdir()):
+            if f.name in ("info.dat", "output.txt"):
+                continue
+            shutil.copy(f, dst / "results" / f.name)
+        shutil.copy(work / "trace.txt", dst / "trace.txt")
+        shutil.copy(work / "params.txt", dst / "params.txt")
+        st = read_state(work / "state.bin")
+        np.savez_compressed(dst / "state.npz", **st)
+        print(name, "ok")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,262 @@
+"""Parity of the CUDA engine with the oracle, operation by operation.
+
+Bit-exact where the engine's per-site arithmetic is the reference's (FFT, the
+deltaN integration, the float mean of saveN, histograms, bin counts); within
+stated tolerances where a lattice-wide sum is formed in a different order
+(the Friedmann update, spectra sums):
+  * fields after leapfrog steps: max|x_gpu - x_oracle| <= 1e-9 * std(x_oracle)
+  * a, ad: relative 1e-12
+  * spectrum bins: relative 1e-12 (same modes, different summation order)
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_state(ieo, N, usr, sigw, tables, steps=0):
+    p = ieo.usr_params(N, calculate_SIGW=int(sigw)) if usr else ieo.hilltop_params(N, calculate_SIGW=int(sigw))
+    o = ieo.Oracle(p, tables if usr else None)
+    o.initialize_all()
+    o.evolve_fields(0.5 * p.dt)
+    if steps:
+        o.leapfrog_steps(steps)
+    return p, o
+
+
+def lattice_like(iegpu, p, o, usr, sigw, tables):
+    lat = iegpu.Lattice(p.N, p.L, p.dt, p.V0, p.ns, p.rescale_B,
+                        potential=iegpu.POT_TABLE if usr else iegpu.POT_HILLTOP, sigw=sigw)
+    if usr:
+        lat.set_table(*tables)
+    lat.upload(iegpu.F, o.f.copy())
+    lat.upload(iegpu.FD, o.fd.copy())
+    if sigw:
+        for c in range(6):
+            lat.upload(iegpu.H(c), o.h_(c).copy())
+            lat.upload(iegpu.HD(c), o.hd_(c).copy())
+    s = o.scalars
+    return lat, iegpu.Bg(s.t, s.a, s.ad, s.ad2, s.astep)
+
+
+def rel_field_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.std(b), 1e-300))
+
+
+@pytest.mark.parametrize("N", [8, 16, 32, 64])
+def test_fft_bit_exact(N, engine, oracle_mod):
+    rng = np.random.default_rng(N)
+    with engine.Lattice(N, 10.0, 1e-3, 3.338e-13, sigw=True) as lat:
+        x = rng.standard_normal(N ** 3)
+        ny = rng.standard_normal(2 * N * N)
+        for fwd in (1, -1):
+            lat.upload(engine.F, x, ny)
+            lat.fft(engine.F, fwd)
+            g, gny = lat.download(engine.F, nyquist=True)
+            r, rny = x.copy(), ny.copy()
+            oracle_mod.fftrn_d(r, rny, N, fwd)
+            assert np.array_equal(g, r), f"double fft {fwd}"
+            assert np.array_equal(gny, rny)
+        xf = rng.standard_normal(N ** 3).astype(np.float32)
+        nyf = rng.standard_normal(2 * N * N).astype(np.float32)
+        for fwd in (1, -1):
+            lat.upload(engine.H(2), xf, nyf)
+            lat.fft(engine.H(2), fwd)
+            g, gny = lat.download(engine.H(2), nyquist=True)
+            r, rny = xf.copy(), nyf.copy()
+            oracle_mod.fftrn_f(r, rny, N, fwd)
+            assert np.array_equal(g, r), f"float fft {fwd}"
+            assert np.array_equal(gny, rny)
+
+
+@pytest.mark.parametrize("N,usr,sigw", [(16, False, False), (32, False, False), (16, True, False), (16, True, True),
+                                        (32, True, True)])
+def test_leapfrog_matches_oracle(N, usr, sigw, engine, oracle_mod, tables):
+    p, o = oracle_state(oracle_mod, N, usr, sigw, tables)
+    lat, bg = lattice_like(engine, p, o, usr, sigw, tables)
+    with lat:
+        nsteps = 300
+        taken, trace = lat.leapfrog(p.af, nsteps, bg, trace=True)
+        assert taken == nsteps
+        o.leapfrog_steps(nsteps)
+        s = o.scalars
+        assert abs(bg.a - s.a) <= 1e-12 * s.a
+        assert abs(bg.ad - s.ad) <= 1e-12 * abs(s.ad)
+        assert abs(bg.t - s.t) <= 1e-12 * s.t
+        assert trace[-1] == bg.a
+        assert rel_field_err(lat.download(engine.F), o.f) < 1e-9
+        assert rel_field_err(lat.download(engine.FD), o.fd) < 1e-9
+        if sigw:
+            for c in range(6):
+                assert rel_field_err(lat.download(engine.H(c)), o.h_(c)) < 1e-5
+                assert rel_field_err(lat.download(engine.HD(c)), o.hd_(c)) < 1e-5
+
+
+def test_leapfrog_stops_at_af(engine, oracle_mod):
+    p, o = oracle_state(oracle_mod, 16, False, False, None)
+    lat, bg = lattice_like(engine, p, o, False, False, None)
+    with lat:
+        af = bg.a * 1.01
+        taken = lat.leapfrog(af, 100000, bg)
+        assert bg.a > af
+        p.af = af
+        o2 = oracle_mod.Oracle(p)
+        o2.initialize_all()
+        o2.evolve_fields(0.5 * p.dt)
+        assert o2.leapfrog_steps(100000) == taken
+
+
+def test_single_step_entry_points(engine, oracle_mod):
+    p, o = oracle_state(oracle_mod, 16, False, False, None, steps=10)
+    lat, bg = lattice_like(engine, p, o, False, False, None)
+    with lat:
+        d = o.rescaled_step(o.scalars.astep)
+        lat.evolve_derivs(d, bg)
+        o.evolve_derivs(d)
+        lat.evolve_fields(d, bg)
+        o.evolve_fields(d)
+        s = o.scalars
+        assert abs(bg.ad - s.ad) <= 1e-13 * abs(s.ad)
+        assert abs(bg.a - s.a) <= 1e-14 * s.a
+        assert rel_field_err(lat.download(engine.F), o.f) < 1e-12
+
+
+def test_energies_and_means(engine, oracle_mod, tables):
+    for usr in (False, True):
+        p, o = oracle_state(oracle_mod, 16, usr, False, tables, steps=20)
+        lat, bg = lattice_like(engine, p, o, usr, False, tables)
+        with lat:
+            k, g, v = lat.energies(bg)
+            ko, go, vo = o.energies()
+            assert np.isclose(k, ko, rtol=1e-12) and np.isclose(v, vo, rtol=1e-12)
+            assert np.isclose(g, go, rtol=1e-6, atol=1e-12 * abs(vo))
+            sf, sfd, sf2 = lat.means()
+            assert np.isclose(sf, o.f.sum(), rtol=1e-13)
+            assert np.isclose(sfd, o.fd.sum(), rtol=1e-12)
+            assert np.isclose(sf2, (o.f ** 2).sum(), rtol=1e-13)
+
+
+@pytest.mark.parametrize("N", [16, 32, 64])
+def test_spectrum_matches_oracle(N, engine, oracle_mod):
+    p, o = oracle_state(oracle_mod, N, False, False, None, steps=50)
+    lat, bg = lattice_like(engine, p, o, False, False, None)
+    with lat:
+        counts, f2 = lat.spectrum(engine.F)
+        oc, of2 = o.spectrum_f()
+        assert np.array_equal(counts, oc)
+        assert np.allclose(f2, of2, rtol=1e-12, atol=0)
+        # the in-place FFT round trip leaves the same bits as the reference's
+        assert np.array_equal(lat.download(engine.F), o.f)
+
+
+def test_gw_spectrum_matches_oracle(engine, oracle_mod, tables):
+    p, o = oracle_state(oracle_mod, 16, True, True, tables, steps=100)
+    lat, bg = lattice_like(engine, p, o, True, True, tables)
+    with lat:
+        for which, tp in ((0, 1.0), (1, p.rescale_B / o.scalars.a)):
+            counts, f2 = lat.gw_spectrum(which, tp)
+            oc, of2, of2d = o.gw_spectrum(which, tp)
+            assert np.array_equal(counts, oc)
+            assert np.allclose(f2, of2d, rtol=1e-12, atol=0)
+            # against the reference's float accumulators
+            m = oc > 0
+            assert np.allclose(f2[m], of2[m], rtol=1e-4)
+        for c in range(6):
+            assert np.array_equal(lat.download(engine.H(c)), o.h_(c))
+
+
+@pytest.mark.parametrize("usr", [False, True])
+def test_deltaN_bit_exact(usr, engine, oracle_mod, tables):
+    p, o = oracle_state(oracle_mod, 16, usr, False, tables, steps=30)
+    lat, bg = lattice_like(engine, p, o, usr, False, tables)
+    with lat:
+        lat.initializeN(o.scalars.a)
+        o.initializeN()
+        assert np.array_equal(lat.download(engine.FD), o.fd)
+        lat.evolve_fieldsN(0.5 * p.dN, 0.0 if usr else 0.0)
+        s = o.scalars
+        s.phiref = 0.0
+        o.set_scalars(s)
+        o.evolve_fieldsN(0.5 * p.dN)
+        phiref = lat.get_phiref()
+        assert phiref == o.get_phiref()
+        s = o.scalars
+        s.phiref = phiref
+        o.set_scalars(s)
+        lat.deltaN_steps(p.dN, 400, phiref)
+        o.deltaN_steps(400)
+        for fld, ref in ((engine.F, o.f), (engine.FD, o.fd), (engine.DELTAN, o.deltaN)):
+            assert np.array_equal(lat.download(fld), ref)
+
+
+def test_saveN_mean_histogram_and_zeroing(engine, oracle_mod):
+    N = 16
+    rng = np.random.default_rng(5)
+    dn = 1e-3 + 1e-6 * rng.standard_normal(N ** 3)
+    dn[::7] = 2e-3
+    p = oracle_mod.hilltop_params(N)
+    o = oracle_mod.Oracle(p)
+    o.deltaN[:] = dn
+    with engine.Lattice(N, p.L, p.dt, p.V0) as lat:
+        lat.upload(engine.DELTAN, dn)
+        cutoff = 1.5e-3
+        m = lat.saveN_mean(cutoff)
+        assert np.float32(m) == np.float32(o.saveN_mean(cutoff))
+        lat.shift(engine.DELTAN, float(m))
+        x = dn - np.float64(np.float32(m))
+        assert np.array_equal(lat.download(engine.DELTAN), x)
+        bmin, df, freq = lat.histogram(engine.DELTAN, 256)
+        assert bmin == x.min() and df == (x.max() - x.min()) / 256
+        b = ((x - bmin) / df).astype(int)
+        b[x == x.max()] = 255
+        want = np.bincount(b[(b >= 0) & (b < 256)], minlength=256) / N ** 3
+        assert np.array_equal(freq, want)
+        lat.zero_above(engine.DELTAN, cutoff - m)
+        x[x > cutoff - np.float64(np.float32(m))] = 0
+        assert np.array_equal(lat.download(engine.DELTAN), x)
+        assert np.isclose(lat.sum(engine.DELTAN), x.sum(), rtol=1e-14)
+
+
+def test_table_range_error_is_reported(engine, oracle_mod, tables):
+    p, o = oracle_state(oracle_mod, 8, True, False, tables)
+    lat, bg = lattice_like(engine, p, o, True, False, tables)
+    with lat:
+        f = o.f.copy()
+        f[17] = 3.6  # above the top node 3.5
+        lat.upload(engine.F, f)
+        with pytest.raises(engine.IegpuError) as e:
+            lat.leapfrog(p.af, 4, bg)
+        assert e.value.code == engine.ERANGE
+        assert "outside the numerical potential range" in str(e.value)
+
+
+@pytest.mark.parametrize("N,usr", [(16, False), (32, True), (64, False)])
+def test_device_initial_conditions(N, usr, engine, oracle_mod, tables):
+    p = oracle_mod.usr_params(N) if usr else oracle_mod.hilltop_params(N)
+    o = oracle_mod.Oracle(p, tables if usr else None)
+    o.initialize_all()
+    with engine.Lattice(N, p.L, p.dt, p.V0, p.ns, p.rescale_B,
+                        potential=engine.POT_TABLE if usr else engine.POT_HILLTOP) as lat:
+        if usr:
+            lat.set_table(*tables)
+        H = lat.bunch_davies(p.seed, p.initial_field, p.initial_derivative)
+        # same uniforms, same dispersion; only log/sin/cos come from another
+        # maths library, so the fluctuations agree to a few ulps of themselves
+        for fld, ref in ((engine.F, o.f), (engine.FD, o.fd)):
+            got = lat.download(fld)
+            assert np.max(np.abs(got - ref)) / np.std(ref) < 1e-12
+        assert abs(H - o.scalars.hubble_init) <= 1e-13 * H
+
+
+def test_device_initial_conditions_seed_semantics(engine, oracle_mod):
+    N = 8
+    for seed in (0, 1, 12345):
+        p = oracle_mod.hilltop_params(N, seed=seed)
+        o = oracle_mod.Oracle(p)
+        o.initialize_all()
+        with engine.Lattice(N, p.L, p.dt, p.V0, p.ns, p.rescale_B) as lat:
+            lat.bunch_davies(seed, p.initial_field, p.initial_derivative)
+            got = lat.download(engine.F)
+            assert np.max(np.abs(got - o.f)) <= 1e-12 * max(np.std(o.f), 1e-300) + 1e-15 * abs(p.initial_field)

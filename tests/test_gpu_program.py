@@ -1,0 +1,143 @@
+"""End-to-end parity of the host program (ie_gpu_main, which drives the CUDA
+engine through the C ABI) with the reference.
+
+1. Against the golden fixtures made by the reference program itself: every
+   results file is compared number by number at its printed precision, the
+   final lattice state element by element.
+2. Against the oracle program on the hilltop workload at N = 64 (the
+   reference's own CPU-sized case) at full precision:
+     a, H, <phi> at every save        relative 1e-10
+     P_dphi and P_zeta per k-bin      relative 1e-8 (bins with modes)
+     k-shell bin counts               exact
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, INPUTS, PKG
+
+pytestmark = pytest.mark.gpu
+
+MAIN = PKG / "_build" / "ie_gpu_main"
+
+CASES = {
+    "n16_hilltop": (16, 0, 0),
+    "n16_usr_sigw": (16, 1, 1),
+    "n32_hilltop": (32, 0, 0),
+}
+
+
+def run_main(tmp_path, params_text, N, numerical, sigw):
+    wd = tmp_path / "gpu"
+    wd.mkdir()
+    text = params_text + f"N = {N}\nnumerical_potential = {numerical}\ncalculate_SIGW = {sigw}\nperform_deltaN = 1\n"
+    (wd / "params.txt").write_text(text)
+    os.symlink(INPUTS, wd / "inputs")
+    (wd / "dump").mkdir()
+    r = subprocess.run([str(MAIN), "params.txt", "results", "dump"], cwd=wd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return wd
+
+
+def parse_numbers(path):
+    rows = []
+    for line in path.read_text().splitlines():
+        if line.strip():
+            rows.append([float(x) for x in line.split()])
+    return rows
+
+
+def compare_text(ref_path, got_path, rel, field_std=None):
+    a, b = parse_numbers(ref_path), parse_numbers(got_path)
+    assert len(a) == len(b), f"{ref_path.name}: {len(a)} vs {len(b)} rows"
+    A = np.array([x for r in a for x in r])
+    B = np.array([x for r in b for x in r])
+    assert A.shape == B.shape, ref_path.name
+    if field_std is not None:
+        err = np.max(np.abs(A - B)) / field_std
+        assert err < rel, f"{ref_path.name}: {err}"
+        return
+    scale = np.max(np.abs(A)) if A.size else 0.0
+    bad = np.abs(A - B) > rel * np.abs(A) + 1e-12 * scale
+    assert not bad.any(), f"{ref_path.name}: {A[bad][:5]} vs {B[bad][:5]}"
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_program_matches_reference_fixtures(case, tmp_path):
+    N, num, sigw = CASES[case]
+    src = GOLDEN / case
+    wd = run_main(tmp_path, (src / "params.txt").read_text(), N, num, sigw)
+    ref_state = np.load(src / "state.npz")
+    names = sorted(x.name for x in (src / "results").iterdir())
+    got_names = sorted(x.name for x in (wd / "results").iterdir() if x.name not in ("info.dat", "output.txt"))
+    assert names == got_names
+    for name in names:
+        if name.startswith("snapshots_2d"):
+            key = {"phi": "f", "phidot": "fd", "deltaN": "deltaN"}[name[len("snapshots_2d_"):-4]]
+            std = float(np.std(ref_state[key]))
+            tol = 1e-6 if key == "deltaN" else 1e-8
+            compare_text(src / "results" / name, wd / "results" / name, tol, field_std=std)
+        elif name.startswith("histogram") and not name.startswith("histogramtimes"):
+            a = np.concatenate([np.array(r) for r in parse_numbers(src / "results" / name)])
+            b = np.concatenate([np.array(r) for r in parse_numbers(wd / "results" / name)])
+            assert np.max(np.abs(a - b)) <= 2.0 / N ** 3 + 1e-12, name
+        elif name.startswith("spectraGW"):
+            compare_text(src / "results" / name, wd / "results" / name, 2e-5)
+        else:
+            compare_text(src / "results" / name, wd / "results" / name, 2e-6)
+    import ieo
+    got = ieo.read_state(wd / "dump" / "state.bin")
+    for key, tol in (("f", 1e-8), ("fd", 1e-8), ("deltaN", 1e-5)):
+        ref = ref_state[key]
+        d = np.abs(got[key] - ref)
+        if key == "deltaN":
+            zeta = ref - ref.mean()
+            assert np.max(d) / np.std(zeta) < tol, key
+        else:
+            assert np.max(d) / np.std(ref) < tol, key
+    # background scalars at every save, full precision
+    ta = [l.split() for l in (src / "trace.txt").read_text().splitlines()]
+    tb = [l.split() for l in (wd / "dump" / "trace.txt").read_text().splitlines()]
+    assert len(ta) == len(tb)
+    for x, y in zip(ta, tb):
+        assert x[0] == y[0]
+        for u, v in zip(x[2:] if x[0] == "save" else x[1:], y[2:] if y[0] == "save" else y[1:]):
+            u, v = float(u), float(v)
+            assert abs(u - v) <= 1e-10 * abs(u) + 1e-300, (x, y)
+
+
+def _precise(path):
+    out = {}
+    for line in path.read_text().splitlines():
+        tag, *vals = line.split()
+        out.setdefault(tag, []).append(np.array([float(v) for v in vals]))
+    return out
+
+
+@pytest.mark.parametrize("N,numerical", [(64, 0), (32, 1)])
+def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mod):
+    src = GOLDEN / ("n16_usr_sigw" if numerical else "n16_hilltop")
+    text = (src / "params.txt").read_text()
+    wd = run_main(tmp_path, text, N, numerical, 0)
+    p = oracle_mod.params_from_text(text, N, bool(numerical), False)
+    od = tmp_path / "oracle"
+    od.mkdir()
+    assert oracle_mod.run_program(p, od / "results", INPUTS, od) == 0
+    g, o = _precise(wd / "dump" / "precise.txt"), _precise(od / "precise.txt")
+    assert len(g["means"]) == len(o["means"])
+    for x, y in zip(g["means"], o["means"]):
+        assert np.allclose(x[[1, 2, 4]], y[[1, 2, 4]], rtol=1e-10, atol=0)  # a, <phi>, H
+    for tag in ("spectrum", "spectrumN"):
+        assert len(g[tag]) == len(o[tag])
+        for x, y in zip(g[tag], o[tag]):
+            m = np.arange(len(y)) >= 1
+            assert np.allclose(x[m], y[m], rtol=1e-8, atol=0), tag
+    # exact bin counts
+    for name in ("spectra.dat", "spectraN.dat"):
+        ca = [r[1] for r in parse_numbers(wd / "results" / name)]
+        cb = [r[1] for r in parse_numbers(od / "results" / name)]
+        assert ca == cb

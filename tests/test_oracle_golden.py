@@ -1,0 +1,39 @@
+"""The oracle against the golden fixtures made by the reference program.
+
+Each fixture in tests/golden/<case>/ was produced by the unmodified reference
+(tests/golden/make_golden.py).  The oracle, run on the same params.txt, must
+reproduce every results file byte for byte, the full-precision trace of the
+background scalars at each save(), and the final lattice state bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, INPUTS
+
+CASES = {
+    "n16_hilltop": (16, False, False),
+    "n16_usr_sigw": (16, True, True),
+    "n32_hilltop": (32, False, False),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_oracle_reproduces_reference_outputs(case, oracle_mod, tmp_path):
+    N, numerical, sigw = CASES[case]
+    src = GOLDEN / case
+    p = oracle_mod.params_from_text((src / "params.txt").read_text(), N, numerical, sigw)
+    rc = oracle_mod.run_program(p, tmp_path / "results", INPUTS, tmp_path)
+    assert rc == 0
+    golden_files = sorted(x.name for x in (src / "results").iterdir())
+    assert golden_files, "empty fixture"
+    for name in golden_files:
+        a = (src / "results" / name).read_bytes()
+        b = (tmp_path / "results" / name).read_bytes()
+        assert a == b, f"{case}: {name} differs"
+    assert (src / "trace.txt").read_text() == (tmp_path / "trace.txt").read_text()
+    ref = np.load(src / "state.npz")
+    got = oracle_mod.read_state(tmp_path / "state.bin")
+    for key in ref.files:
+        assert np.array_equal(ref[key], got[key]), f"{case}: state {key} differs"

@@ -1,0 +1,52 @@
+"""Pin the oracle against the reference program built from its own sources.
+
+Runs only where the reference tree is available (it is read at build time by
+oracle/build_ref.py); elsewhere the committed golden fixtures
+(test_oracle_golden.py) carry the same check.  Configurations beyond the
+fixtures: hilltop with SIGW, USR without SIGW, USR at N = 32.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, INPUTS, ORACLE
+
+sys.path.insert(0, str(ORACLE))
+import build_ref  # noqa: E402
+
+pytestmark = pytest.mark.skipif(not build_ref.ref_available(), reason="reference tree not present")
+
+HILL = (GOLDEN / "n16_hilltop" / "params.txt").read_text()
+USR = (GOLDEN / "n16_usr_sigw" / "params.txt").read_text()
+
+CASES = [
+    (16, False, True, HILL),
+    (16, True, False, USR),
+    (32, True, True, USR),
+]
+
+
+@pytest.mark.parametrize("N,numerical,sigw,text", CASES)
+def test_oracle_matches_reference(N, numerical, sigw, text, oracle_mod, tmp_path):
+    exe = build_ref.build(N, int(numerical), int(sigw), 1)
+    wd = tmp_path / "ref"
+    wd.mkdir()
+    (wd / "params.txt").write_text(text)
+    os.symlink(INPUTS, wd / "inputs")
+    subprocess.run([str(exe), str(wd)], check=True, stdout=subprocess.DEVNULL)
+    p = oracle_mod.params_from_text(text, N, numerical, sigw)
+    assert oracle_mod.run_program(p, tmp_path / "results", INPUTS, tmp_path) == 0
+    for f in sorted((wd / "results").iterdir()):
+        if f.name == "info.dat":
+            continue
+        assert f.read_bytes() == (tmp_path / "results" / f.name).read_bytes(), f.name
+    assert (wd / "trace.txt").read_text() == (tmp_path / "trace.txt").read_text()
+    ref = oracle_mod.read_state(wd / "state.bin")
+    got = oracle_mod.read_state(tmp_path / "state.bin")
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), k
