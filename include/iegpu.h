@@ -126,7 +126,10 @@ int  iegpu_evolve_derivs(struct iegpu_ctx* ctx, double d, iegpu_bg* bg);
  *       d = dt*astep^(s-1); evolve_derivs(d); evolve_fields(d); astep = a; }
  * runs entirely on the device (CUDA graph).  *steps_taken receives the number
  * of steps; a_trace (may be NULL) receives a after each step, as written to
- * results/output.txt by report_step (src/evolution.cpp:926-927). */
+ * results/output.txt by report_step (src/evolution.cpp:926-927).  The final
+ * "astep = a" of the last step taken is left to the caller, who runs its
+ * report/save first (save() drifts with the old astep, src/output.cpp:1472)
+ * and then sets bg->astep = bg->a before the next call. */
 int  iegpu_leapfrog(struct iegpu_ctx* ctx, double af, int max_steps, iegpu_bg* bg,
                     int* steps_taken, double* a_trace);
 /* kin_energy(), gradient_energy(), potential_energy():

@@ -36,6 +36,7 @@ UNITS = {
     "deltaN.cu": ["-fmad=false"],
     "reduce_ops.cu": ["-fmad=false"],
     "ic.cu": ["-fmad=false"],
+    "split_fp32.cu": [],
 }
 
 

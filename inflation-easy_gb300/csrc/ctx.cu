@@ -96,6 +96,10 @@ static int dalloc(iegpu_ctx* c, T** p, size_t n) {
 
 static void free_all(iegpu_ctx* c) {
     fp64_destroy_graphs(c);
+    split_destroy_graphs(c);
+    for (int q = 0; q < 2; ++q) { cudaFree(c->sp[q]); cudaFree(c->spi[q]); }
+    cudaFree(c->sctl);
+    if (c->sctl_h) cudaFreeHost(c->sctl_h);
     fft_free(c);
     for (int q = 0; q < 2; ++q) cudaFree(c->f[q]);
     cudaFree(c->fd); cudaFree(c->dn); cudaFree(c->fny); cudaFree(c->fdny);
@@ -141,7 +145,7 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
     *out = nullptr;
     const int N = cfg->N;
     if (N < 8 || N > 1024 || (N & (N - 1))) return IEGPU_EINVAL;
-    if (cfg->form != IEGPU_FORM_FP64) return IEGPU_EUNSUPPORTED;
+    if (cfg->form != IEGPU_FORM_FP64 && cfg->form != IEGPU_FORM_SPLIT) return IEGPU_EINVAL;
     if (!(cfg->L > 0) || !(cfg->dt > 0) || !(cfg->rescale_B > 0)) return IEGPU_EINVAL;
     iegpu_ctx* c = new (std::nothrow) iegpu_ctx();
     if (!c) return IEGPU_ENOMEM;
@@ -180,8 +184,29 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
     if (c->red_grid * 256LL > sites) c->red_grid = (int)((sites + 255) / 256);
     c->spec_blocks = c->sms * 2;
     const int nb = iegpu_numbins(N) + 1;
+    // partial sums: 6 per reduction CTA, or 3 per CTA of the split step kernel
+    // (at most max(8 per SM, number of 8x32 tiles))
+    const long long tiles = (long long)(N / (N >= 32 ? 8 : (N >= 16 ? 16 : 8))) * (N / (N >= 32 ? 32 : N));
+    const long long step_ctas = tiles > 8LL * c->sms ? tiles : 8LL * c->sms;
+    c->part_cap = (int)(6 * c->red_grid + 3 * step_ctas + 64);
     if (!rc) rc = dalloc(c, &c->ctl, 1);
-    if (!rc) rc = dalloc(c, &c->part, (size_t)c->red_grid * 4);
+    if (!rc) rc = dalloc(c, &c->part, (size_t)c->part_cap);
+    if (!rc && cfg->form == IEGPU_FORM_SPLIT) {
+        for (int q = 0; q < 2 && !rc; ++q) {
+            rc = dalloc(c, &c->sp[q], gs);
+            if (!rc) rc = dalloc(c, &c->spi[q], gs);
+        }
+        if (!rc) rc = dalloc(c, &c->sctl, 1);
+        if (!rc && check_cuda(c, cudaMallocHost(&c->sctl_h, sizeof(SplitCtl)), "pinned alloc")) rc = IEGPU_ENOMEM;
+        if (!rc) {
+            memset(c->sctl_h, 0, sizeof(SplitCtl));
+            cudaMemsetAsync(c->sctl, 0, sizeof(SplitCtl), c->stream);
+            for (int q = 0; q < 2; ++q) {
+                cudaMemsetAsync(c->sp[q], 0, sizeof(float) * gs, c->stream);
+                cudaMemsetAsync(c->spi[q], 0, sizeof(float) * gs, c->stream);
+            }
+        }
+    }
     if (!rc) rc = dalloc(c, &c->counter, 1);
     if (!rc) rc = dalloc(c, &c->spec_part, (size_t)c->spec_blocks * nb + 65536);
     if (!rc) rc = dalloc(c, &c->spec_cnt, (size_t)c->spec_blocks * nb);
@@ -283,7 +308,32 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
     P.slopeV = c->tab + 6 * n;
     P.key = c->tkey;
     fp64_destroy_graphs(c);  // graphs hold the potential by value
+    split_destroy_graphs(c);
     return IEGPU_OK;
+}
+
+static bool is_split(const iegpu_ctx* c) { return c->cfg.form == IEGPU_FORM_SPLIT; }
+// F or FD held in the split representation (not the FP64 buffers)
+static bool split_field(const iegpu_ctx* c, int field) {
+    return is_split(c) && !c->split_mat && (field == IEGPU_F || field == IEGPU_FD);
+}
+
+// Split form: bring F and FD into the FP64 buffers (deltaN stage and FP64-only
+// diagnostics).
+static int split_materialize_both(iegpu_ctx* c) {
+    int rc = split_materialize(c, 0, c->f[c->cur]);
+    if (!rc) rc = split_materialize(c, 1, c->fd);
+    return rc;
+}
+
+// Split form: the FP64 field buffer -> background (its mean) + perturbation.
+static int split_absorb_field(iegpu_ctx* c, int field) {
+    double* x = field == IEGPU_F ? c->f[c->cur] : c->fd;
+    double sum = 0.0;
+    int rc = field_sum(c, field, &sum);
+    if (rc) return rc;
+    (void)x;
+    return split_absorb(c, field == IEGPU_F ? 0 : 1, x, sum / (double)c->gs);
 }
 
 static int need_table(iegpu_ctx* c) {
@@ -298,6 +348,11 @@ int iegpu_upload(iegpu_ctx* c, int field, const void* host, const void* nyquist)
     if (is_double_field(field)) {
         if (check_cuda(c, cudaMemcpy(dfield(c, field), host, sizeof(double) * c->gs, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
         if (nyquist && check_cuda(c, cudaMemcpy(dnyq(c, field), nyquist, sizeof(double) * ny, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
+        if (is_split(c) && (field == IEGPU_F || field == IEGPU_FD)) {
+            c->split_mat = 0;
+            if (int rc = split_absorb_field(c, field)) return rc;
+            return sync_and_check(c, "upload");
+        }
     } else {
         if (check_cuda(c, cudaMemcpy(ffield(c, field), host, sizeof(float) * c->gs, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
         if (nyquist && check_cuda(c, cudaMemcpy(fnyq(c, field), nyquist, sizeof(float) * ny, cudaMemcpyHostToDevice), "upload")) return IEGPU_ECUDA;
@@ -310,6 +365,10 @@ int iegpu_download(iegpu_ctx* c, int field, void* host, void* nyquist) {
     if (!valid_field(c, field)) return set_error(c, IEGPU_EINVAL, "unknown field %d", field);
     if (sync_and_check(c, "download")) return IEGPU_ECUDA;
     const size_t ny = (size_t)c->N * 2 * c->N;
+    if (split_field(c, field)) {
+        if (int rc = split_materialize(c, field == IEGPU_F ? 0 : 1, dfield(c, field))) return rc;
+        if (sync_and_check(c, "download")) return IEGPU_ECUDA;
+    }
     if (is_double_field(field)) {
         if (check_cuda(c, cudaMemcpy(host, dfield(c, field), sizeof(double) * c->gs, cudaMemcpyDeviceToHost), "download")) return IEGPU_ECUDA;
         if (nyquist && check_cuda(c, cudaMemcpy(nyquist, dnyq(c, field), sizeof(double) * ny, cudaMemcpyDeviceToHost), "download")) return IEGPU_ECUDA;
@@ -322,6 +381,13 @@ int iegpu_download(iegpu_ctx* c, int field, void* host, void* nyquist) {
 
 int iegpu_add(iegpu_ctx* c, int field, double value) {
     if (!c) return IEGPU_EINVAL;
+    if (split_field(c, field)) {
+        // a constant shifts the FP64 background only
+        if (check_cuda(c, cudaMemcpy(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost), "ctl")) return IEGPU_ECUDA;
+        if (field == IEGPU_F) c->sctl_h->phibar += value;
+        else c->sctl_h->pibar += value;
+        return check_cuda(c, cudaMemcpy(c->sctl, c->sctl_h, sizeof(SplitCtl), cudaMemcpyHostToDevice), "ctl");
+    }
     return field_add(c, field, value);
 }
 
@@ -337,29 +403,67 @@ int iegpu_zero_above(iegpu_ctx* c, int field, double threshold) {
 
 int iegpu_sum(iegpu_ctx* c, int field, double* sum) {
     if (!c || !sum) return IEGPU_EINVAL;
+    if (split_field(c, field)) {
+        double v[6];
+        if (int rc = split_sums(c, v)) return rc;
+        *sum = (double)c->gs * (field == IEGPU_F ? c->sctl_h->phibar : c->sctl_h->pibar) + (field == IEGPU_F ? v[0] : v[2]);
+        return IEGPU_OK;
+    }
     return field_sum(c, field, sum);
+}
+
+static int split_running(iegpu_ctx* c) {
+    if (c->split_mat) return set_error(c, IEGPU_EUNSUPPORTED, "the split-form lattice was handed to the deltaN stage; upload F and FD to evolve it again");
+    return IEGPU_OK;
 }
 
 int iegpu_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg) {
     if (!c || !bg) return IEGPU_EINVAL;
+    if (is_split(c)) {
+        if (int rc = split_running(c)) return rc;
+        return split_evolve_fields(c, d, bg);
+    }
     return fp64_evolve_fields(c, d, bg);
 }
 
 int iegpu_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg) {
     if (!c || !bg) return IEGPU_EINVAL;
     if (int rc = need_table(c)) return rc;
+    if (is_split(c)) {
+        if (int rc = split_running(c)) return rc;
+        return split_evolve_derivs(c, d, bg);
+    }
     return fp64_evolve_derivs(c, d, bg);
 }
 
 int iegpu_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps_taken, double* a_trace) {
     if (!c || !bg) return IEGPU_EINVAL;
     if (int rc = need_table(c)) return rc;
+    if (is_split(c)) {
+        if (int rc = split_running(c)) return rc;
+        return split_leapfrog(c, af, max_steps, bg, steps_taken, a_trace);
+    }
     return fp64_leapfrog(c, af, max_steps, bg, steps_taken, a_trace);
 }
 
 int iegpu_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]) {
     if (!c || !bg || !out) return IEGPU_EINVAL;
     if (int rc = need_table(c)) return rc;
+    if (is_split(c) && !c->split_mat) {
+        double v[6];
+        if (int rc = split_sums(c, v)) return rc;
+        const double gs = (double)c->gs, a = bg->a, s = c->cfg.rescale_s, dx = c->cfg.L / (double)c->N;
+        const double pb = c->sctl_h->phibar, qb = c->sctl_h->pibar;
+        const PotDev& P = c->pot;
+        // <fd^2> = pibar^2 + 2 pibar <dpi> + <dpi^2>
+        const double fd2 = qb * qb + 2.0 * qb * (v[2] / gs) + v[3] / gs;
+        out[0] = 0.5 * pow(a, 2.0 * s - 2.0) * fd2;
+        out[1] = 0.5 * v[4] * ((1.0 / (a * dx)) * (1.0 / (a * dx))) / gs;
+        const double Vbar = host_potential(c, pb);
+        if (P.table) out[2] = Vbar + (v[5] / P.B2) / gs;
+        else out[2] = Vbar - (P.V0 * P.c1 / P.B2) * (2.0 * pb * v[0] + v[1]) / gs;
+        return IEGPU_OK;
+    }
     return fp64_energies(c, bg, out);
 }
 
@@ -382,7 +486,14 @@ int iegpu_bunch_davies(iegpu_ctx* c, int seed, double phi0, double dphi0, double
     rc = fp64_energies(c, &b, e);
     if (rc) return rc;
     *hubble_init = std::sqrt((e[0] + e[2] + e[1]) / 3.0);
-    return IEGPU_OK;
+    if (is_split(c)) {
+        // split form: the FP64 fields become background + FP32 perturbation
+        c->split_mat = 0;
+        rc = split_absorb_field(c, IEGPU_F);
+        if (!rc) rc = split_absorb_field(c, IEGPU_FD);
+        if (!rc) rc = sync_and_check(c, "split initial conditions");
+    }
+    return rc;
 }
 
 int iegpu_timer_start(iegpu_ctx* c) {
@@ -400,15 +511,38 @@ int iegpu_timer_stop(iegpu_ctx* c, float* ms) {
 int iegpu_profile_leapfrog(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms_out, int nk) {
     if (!c || !bg || !ms_out || nsteps < 0) return IEGPU_EINVAL;
     if (int rc = need_table(c)) return rc;
+    if (is_split(c)) {
+        // one fused kernel per step: time the graph-free launch of each step
+        for (int q = 0; q < nk; ++q) ms_out[q] = 0.0;
+        float ms = 0.f;
+        if (int rc = iegpu_timer_start(c)) return rc;
+        int taken = 0;
+        if (int rc = split_leapfrog(c, af, nsteps, bg, &taken, nullptr)) return rc;
+        if (int rc = iegpu_timer_stop(c, &ms)) return rc;
+        if (nk > 1) ms_out[1] = ms;
+        return IEGPU_OK;
+    }
     return fp64_profile(c, af, nsteps, bg, ms_out, nk);
 }
 
 int iegpu_means(iegpu_ctx* c, double out[3]) {
     if (!c || !out) return IEGPU_EINVAL;
+    if (is_split(c) && !c->split_mat) {
+        double v[6];
+        if (int rc = split_sums(c, v)) return rc;
+        const double gs = (double)c->gs, pb = c->sctl_h->phibar, qb = c->sctl_h->pibar;
+        out[0] = gs * pb + v[0];
+        out[1] = gs * qb + v[2];
+        out[2] = gs * pb * pb + 2.0 * pb * v[0] + v[1];
+        return IEGPU_OK;
+    }
     return field_means(c, out);
 }
 
 int iegpu_histogram(iegpu_ctx* c, int field, int nbins, double* bmin, double* df, double* freq) {
+    if (c && split_field(c, field) && is_double_field(field)) {
+        if (int rc = split_materialize(c, field == IEGPU_F ? 0 : 1, dfield(c, field))) return rc;
+    }
     // bin counters live in shared memory: at most 8192 bins
     if (!c || !bmin || !df || !freq || nbins <= 0 || nbins > 8192) return c ? set_error(c, IEGPU_EINVAL, "bad histogram arguments (1 <= nbins <= 8192)") : IEGPU_EINVAL;
     return field_histogram(c, field, nbins, bmin, df, freq);
@@ -417,6 +551,8 @@ int iegpu_histogram(iegpu_ctx* c, int field, int nbins, double* bmin, double* df
 int iegpu_fft(iegpu_ctx* c, int field, int forward) {
     if (!c || (forward != 1 && forward != -1)) return IEGPU_EINVAL;
     if (!valid_field(c, field)) return set_error(c, IEGPU_EINVAL, "unknown field %d", field);
+    if (split_field(c, field))
+        return set_error(c, IEGPU_EUNSUPPORTED, "in-place FFT of f/fd is provided by the FP64 form; the split form uses iegpu_bunch_davies and iegpu_spectrum");
     int rc;
     if (is_double_field(field)) rc = fft_d(c, dfield(c, field), dnyq(c, field), forward);
     else rc = fft_f(c, ffield(c, field), fnyq(c, field), forward);
@@ -432,6 +568,20 @@ int iegpu_spectrum(iegpu_ctx* c, int field, int* counts, double* f2, int nbins) 
     if (nbins != iegpu_numbins(c->N)) return set_error(c, IEGPU_EINVAL, "nbins must be %d", iegpu_numbins(c->N));
     double* x = dfield(c, field);
     double* ny = dnyq(c, field);
+    if (split_field(c, field)) {
+        // spectrum of the FP32 perturbation, taken in FP64; the k = 0 mode
+        // (bin 0, count 1) is the lattice sum of background + perturbation
+        double v[6];
+        int rc = split_sums(c, v);
+        if (!rc) rc = split_to_double(c, field == IEGPU_F ? 0 : 1, x);
+        if (!rc) rc = fft_d(c, x, ny, 1);
+        if (!rc) rc = spectrum_bin_d(c, x, ny, counts, f2, nbins);
+        if (rc) return rc;
+        const double k0 = (double)c->gs * (field == IEGPU_F ? c->sctl_h->phibar : c->sctl_h->pibar) +
+                          (field == IEGPU_F ? v[0] : v[2]);
+        f2[0] = k0 * k0;
+        return IEGPU_OK;
+    }
     int rc = fft_d(c, x, ny, 1);
     if (!rc) rc = spectrum_bin_d(c, x, ny, counts, f2, nbins);
     if (!rc) rc = fft_d(c, x, ny, -1);
@@ -461,6 +611,11 @@ int iegpu_gw_spectrum(iegpu_ctx* c, int which, double to_phys, int* counts, doub
 int iegpu_initializeN(iegpu_ctx* c, double a) {
     if (!c) return IEGPU_EINVAL;
     if (int rc = need_table(c)) return rc;
+    if (is_split(c) && !c->split_mat) {
+        // the deltaN integration is FP64: hand over phibar + dphi, pibar + dpi
+        if (int rc = split_materialize_both(c)) return rc;
+        c->split_mat = 1;
+    }
     int rc = deltaN_init(c, a);
     if (!rc) rc = sync_and_check(c, "initializeN");
     if (!rc) {
@@ -478,11 +633,16 @@ int iegpu_initializeN(iegpu_ctx* c, double a) {
 
 int iegpu_get_phiref(iegpu_ctx* c, double* phiref) {
     if (!c || !phiref) return IEGPU_EINVAL;
+    if (split_field(c, IEGPU_F)) {
+        if (int rc = split_materialize(c, 0, c->f[c->cur])) return rc;
+    }
     return get_phiref(c, phiref);
 }
 
 static int deltaN_run(iegpu_ctx* c, double d, int nsteps, double phiref, int dd, int df) {
     if (int rc = need_table(c)) return rc;
+    if (is_split(c) && !c->split_mat)
+        return set_error(c, IEGPU_EINVAL, "call iegpu_initializeN before the deltaN steps");
     if (check_cuda(c, cudaMemsetAsync(&c->ctl->error, 0, sizeof(int), c->stream), "memset")) return IEGPU_ECUDA;
     int rc = deltaN_steps(c, d, nsteps, phiref, dd, df);
     if (!rc) rc = sync_and_check(c, "deltaN");

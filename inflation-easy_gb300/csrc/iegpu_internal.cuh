@@ -67,6 +67,37 @@ struct PotDev {
     const double* slopeV;   // dyV/dxl (reductions only)
 };
 
+// Split form (FP32 perturbations about an FP64 background).
+constexpr int kWin = 24;  // table brackets per window
+
+// Window of table brackets around a background value phibar: brackets
+// l0 .. l0+n-1, node offsets u[q] = x[l0-1+q] - phibar (descending), and per
+// bracket the line A[q] + s[q]*dphi = F(phibar + dphi) - F(phibar).
+struct SplitWin {
+    int l0, n, ok, pad;
+    float u[kWin + 1];
+    float A[kWin];
+    float s[kWin];
+};
+
+struct SplitCtl {
+    DevBg bg;
+    double phibar, pibar;   // FP64 background
+    double af, d_given, errval, dd;
+    int steps_done, steps_limit, done, mode, error, active;
+    // coefficients of the coming step, in FP32 for the lattice
+    float d, lapl, fric, pn, kv, srcAmp;
+    SplitWin wk;   // V' window around phibar of the coming step (kick)
+    SplitWin wv;   // V window around phibar after it (sums of the new dphi)
+    double sums[3];
+};
+
+struct SigwSplit {
+    const float* hs[6];
+    float* hdst[6];
+    float* hd[6];
+};
+
 struct FftTw {
     // complex-pass twiddles for line length M, per direction, stage-major
     // (stage s uses entries [2^(s-1)-1, 2^s-1)), computed on the host with the
@@ -125,6 +156,16 @@ struct iegpu_ctx {
     double* misc_h = nullptr;          // pinned mirror
     iegpu::FftTw tw{};
 
+    // split form state
+    float* sp[2] = {nullptr, nullptr};    // dphi (ping-pong)
+    float* spi[2] = {nullptr, nullptr};   // dpi  (ping-pong)
+    iegpu::SplitCtl* sctl = nullptr;      // device
+    iegpu::SplitCtl* sctl_h = nullptr;    // pinned host mirror
+    cudaGraphExec_t sp_exec[2] = {nullptr, nullptr};
+    int sp_steps = 0;
+    int split_mat = 0;                    // FP64 buffers hold the field (deltaN stage)
+    int part_cap = 0;
+
     // timing events
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
@@ -181,6 +222,15 @@ int field_add(iegpu_ctx* c, int field, double v);
 int field_zero_above(iegpu_ctx* c, int field, double thr);
 int saveN_mean(iegpu_ctx* c, double cutoff, float* out);
 int get_phiref(iegpu_ctx* c, double* out);
+// split_fp32.cu
+int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace);
+int split_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg);
+int split_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
+int split_sums(iegpu_ctx* c, double out[6]);
+int split_materialize(iegpu_ctx* c, int which, double* out);
+int split_to_double(iegpu_ctx* c, int which, double* out);
+int split_absorb(iegpu_ctx* c, int which, const double* in, double mean);
+void split_destroy_graphs(iegpu_ctx* c);
 // ic.cu
 int bunch_davies(iegpu_ctx* c, int seed, double phi0, double dphi0, double hubble, double hi_cut, double lo_cut);
 // deltaN.cu

@@ -67,7 +67,16 @@ __device__ void step_scalars(DevCtl* ctl, const PotDev& P, const StepConst& K, d
     DevCtl& C = *ctl;
     double d;
     if (C.mode == kModeLeapfrog) {
-        if (!(C.bg.a <= C.af) || C.steps_done >= C.steps_limit) {
+        // loop body of src/evolution.cpp:937-945; "astep = a" closes an
+        // iteration after its report, so the last step of a call leaves it
+        // to the caller (the reference's save() still sees the old astep).
+        if (C.steps_done >= C.steps_limit) {
+            C.st.active = 0;
+            C.done = 1;
+            return;
+        }
+        if (C.steps_done > 0) C.bg.astep = C.bg.a;
+        if (!(C.bg.a <= C.af)) {
             C.st.active = 0;
             C.done = 1;
             return;
@@ -103,7 +112,6 @@ __device__ void step_scalars(DevCtl* ctl, const PotDev& P, const StepConst& K, d
     if (C.mode == kModeLeapfrog) {
         C.bg.t += d;
         C.bg.a = a + d * ad;
-        C.bg.astep = C.bg.a;
         if (a_trace) a_trace[C.steps_done] = C.bg.a;
         C.steps_done += 1;
     }

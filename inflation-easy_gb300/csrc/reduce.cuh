@@ -27,9 +27,10 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
     }
     __syncthreads();
     if (w == 0) {
+        const int nw = (int)(blockDim.x >> 5);
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
-            double x = lane < (kThreads / 32) ? sh[q][lane] : 0.0;
+            double x = lane < nw ? sh[q][lane] : 0.0;
             v[q] = warp_sum(x);
         }
     }

@@ -1,0 +1,792 @@
+// split_fp32.cu -- the split-precision form of the leapfrog.
+//
+// The field is stored as phi = phibar(t) + dphi(x), phi' = pibar(t) + dpi(x):
+// the homogeneous background (phibar, pibar) and the scale factor in FP64, the
+// perturbations dphi, dpi (and h_ij) in FP32.  In exact arithmetic this is the
+// reference's leapfrog (src/evolution.cpp:150-284) written for the two parts:
+//   pibar' = pibar + d(-friction pibar - potnorm V'(phibar))
+//   dpi'   = dpi + d(laplnorm lapl(dphi) - friction dpi - potnorm [V'(phibar+dphi) - V'(phibar)])
+//   phibar' = phibar + d pibar',  dphi' = dphi + d dpi'
+// The potential difference is exact for the hilltop (V' linear); for the
+// tabulated potential each bracket l is a line, so V'(phibar+dphi) - V'(phibar)
+// = A_l + s_l dphi with A_l, s_l formed in FP64 once per step for a window of
+// brackets around phibar.
+//
+// One kernel per step.  Each CTA owns a TJ x TK tile of (j, k) columns and
+// marches along i through a chunk of planes, keeping three planes of dphi in
+// shared memory.  Besides the tile it recomputes the step on a one-cell halo
+// on the +j and +k sides, which gives the new dphi on every forward
+// neighbour, so the same pass also accumulates the sums the next step's
+// Friedmann update needs: sum (dphi(x+e) - dphi(x))^2 (= -sum dphi lapl dphi,
+// the gradient energy), sum dphi and sum dphi^2 (hilltop potential) or sum of
+// V differences (table).  Sums are Kahan-compensated in FP32 per thread and
+// combined in FP64.  The last CTA to finish runs the FP64 Friedmann and
+// background update for the next step.  HBM traffic per site-update:
+// read dphi, dpi; write dphi, dpi = 16 B (ping-pong buffers), halos from L2.
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <vector>
+
+#include "iegpu_internal.cuh"
+#include "pot.cuh"
+#include "reduce.cuh"
+
+namespace iegpu {
+
+// ---------------------------------------------------------------------------
+// windows of table brackets around a background value
+// ---------------------------------------------------------------------------
+
+// Window around phibar: brackets l0 .. l0+n-1; u[q] = x[l0-1+q] - phibar.
+__device__ void build_window(SplitWin& W, const PotDev& P, const double* y, const double* dy, double phibar,
+                             int* err) {
+    W.ok = 0;
+    if (!P.table) return;
+    bool oor;
+    const int lb = table_bracket(P, phibar, &oor);
+    if (oor) { *err = 1; return; }
+    int l0 = lb - kWin / 2;
+    if (l0 < 1) l0 = 1;
+    int n = kWin;
+    if (l0 + n - 1 > P.n - 1) n = P.n - 1 - l0 + 1;
+    W.l0 = l0;
+    W.n = n;
+    // value of the tabulated function at phibar (its own bracket)
+    const double Fbar = y[lb] + (phibar - P.x[lb]) * (dy[lb] / P.dxl[lb]);
+    for (int q = 0; q <= n; ++q) W.u[q] = (float)(P.x[l0 - 1 + q] - phibar);
+    for (int q = 0; q < n; ++q) {
+        const int l = l0 + q;
+        const double s = dy[l] / P.dxl[l];
+        W.s[q] = (float)s;
+        W.A[q] = (float)((y[l] + (phibar - P.x[l]) * s) - Fbar);
+    }
+    W.ok = 1;
+}
+
+// Bracket q of the window with u[q+1] < v <= u[q]; -1 outside the window.
+__device__ __forceinline__ int window_find(const float* u, int n, float v) {
+    if (!(v <= u[0] && v > u[n])) return -1;
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (u[mid] >= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// scalar update (one thread): Friedmann, background, coefficients, windows
+// ---------------------------------------------------------------------------
+
+struct SplitConst {
+    double dt, s, dx, gs;
+};
+
+// V(phibar)/B^2 and V'(phibar)/B^2 (src/potential.cpp:77-98)
+__device__ void bar_potential(const PotDev& P, double phibar, double* V, double* dV) {
+    if (P.table) {
+        bool oor;
+        const int l = table_bracket(P, phibar, &oor);
+        *V = table_interp(P, P.V, P.dyV, phibar, l) / P.B2;
+        *dV = table_interp(P, P.dV, P.dydV, phibar, l) / P.B2;
+    } else {
+        *V = (P.V0 * (1.0 - P.c1 * (phibar * phibar))) / P.B2;
+        *dV = (P.c2 * phibar) / P.B2;
+    }
+}
+
+// sums: [0] sum of squared forward differences of dphi, [1] sum dphi,
+// [2] hilltop: sum dphi^2 / table: sum of V differences (table units)
+__device__ void split_scalars(SplitCtl& C, const PotDev& P, const SplitConst& K, const double* sums, double* a_trace) {
+    double d;
+    if (C.mode == kModeLeapfrog) {
+        if (C.steps_done >= C.steps_limit) { C.active = 0; C.done = 1; return; }
+        if (C.steps_done > 0) C.bg.astep = C.bg.a;
+        if (!(C.bg.a <= C.af)) { C.active = 0; C.done = 1; return; }
+        d = K.dt * pow_exp(C.bg.astep, K.s - 1.0);
+    } else {
+        d = C.d_given;
+    }
+    const double a = C.bg.a, s = K.s;
+    double ad = C.bg.ad;
+    const double grad = 0.5 * sums[0] * ((1.0 / (a * K.dx)) * (1.0 / (a * K.dx))) / K.gs;
+    double Vbar, dVbar;
+    bar_potential(P, C.phibar, &Vbar, &dVbar);
+    double pot;
+    if (P.table) pot = Vbar + (sums[2] / P.B2) / K.gs;
+    else pot = Vbar - (P.V0 * P.c1 / P.B2) * (2.0 * C.phibar * sums[1] + sums[2]) / K.gs;
+    const double sfev1 = s + 1.0, sfev2 = -2.0 * s + 2.0;
+    const double ad2 = (-2.0 * ad - 2.0 * a / d / sfev1 *
+                        (1.0 - sqrt(1.0 + 2.0 * d * sfev1 * ad / a +
+                                    (d * d) * sfev1 * pow_exp(a, sfev2) * (2.0 * grad / 3.0 + pot)))) / d;
+    ad += 0.5 * d * ad2;
+    const double laplnorm = pow_exp(a, -2.0 * s) / (K.dx * K.dx);
+    const double friction = (2.0 + s) * ad / a;
+    const double potnorm = pow_exp(a, 2.0 - 2.0 * s);
+    const double srcAmp = 2.0 * pow_exp(a, -2.0 * s);
+    ad += 0.5 * d * ad2;
+    // background kick (homogeneous mode of the lattice kick)
+    C.pibar = C.pibar + d * (-friction * C.pibar - potnorm * dVbar);
+    int err = 0;
+    build_window(C.wk, P, P.dV, P.dydV, C.phibar, &err);
+    C.d = (float)d;
+    C.lapl = (float)laplnorm;
+    C.fric = (float)friction;
+    C.pn = (float)(potnorm / P.B2);
+    C.kv = (float)(potnorm * P.c2 / P.B2);
+    C.srcAmp = (float)srcAmp;
+    C.dd = d;
+    C.bg.ad = ad;
+    C.bg.ad2 = ad2;
+    C.active = 1;
+    if (C.mode == kModeLeapfrog) {
+        C.phibar = C.phibar + d * C.pibar;
+        C.bg.t += d;
+        C.bg.a = a + d * ad;
+        if (a_trace) a_trace[C.steps_done] = C.bg.a;
+        C.steps_done += 1;
+    }
+    build_window(C.wv, P, P.V, P.dyV, C.phibar, &err);
+    if (err && !C.error) { C.error = IEGPU_ERANGE; C.errval = C.phibar; C.active = 0; C.done = 1; }
+}
+
+// ---------------------------------------------------------------------------
+// Kahan accumulator
+// ---------------------------------------------------------------------------
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ void finish_sums(double (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+                                            double* part, unsigned* counter, double* a_trace) {
+    block_sum<3>(v);
+    if (threadIdx.x == 0) {
+        part[3 * (blockIdx.x + gridDim.x * blockIdx.y)] = v[0];
+        part[3 * (blockIdx.x + gridDim.x * blockIdx.y) + 1] = v[1];
+        part[3 * (blockIdx.x + gridDim.x * blockIdx.y) + 2] = v[2];
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1);
+    __syncthreads();
+    if (!last) return;
+    if (threadIdx.x < 32) {
+        double tot[3];
+        sum_partials<3>(part, gridDim.x * gridDim.y, tot);
+        if (threadIdx.x == 0) {
+            *counter = 0;
+            SplitCtl& C = *ctl;
+            C.sums[0] = tot[0];
+            C.sums[1] = tot[1];
+            C.sums[2] = tot[2];
+            if (C.error) { C.active = 0; C.done = 1; }
+            else split_scalars(C, P, K, tot, a_trace);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// Sums of the current dphi (start of a leapfrog call): thread per site.
+template <bool TABLE>
+__global__ void __launch_bounds__(kThreads) k_split_prime(const float* __restrict__ x, SplitCtl* ctl, PotDev P,
+                                                          SplitConst K, double* part, unsigned* counter,
+                                                          double* a_trace, int lg) {
+    __shared__ float su[kWin + 1], sA[kWin], ss[kWin];
+    __shared__ int sn;
+    if (threadIdx.x == 0) sn = 0;
+    if (TABLE) {
+        // every CTA forms the window around the current phibar itself
+        if (threadIdx.x == 0) {
+            SplitWin W;
+            int err = 0;
+            build_window(W, P, P.V, P.dyV, ctl->phibar, &err);
+            sn = err ? -1 : W.n;
+            for (int q = 0; q <= W.n && !err; ++q) su[q] = W.u[q];
+            for (int q = 0; q < W.n && !err; ++q) { sA[q] = W.A[q]; ss[q] = W.s[q]; }
+        }
+    }
+    __syncthreads();
+    const long long gs = 1LL << (3 * lg);
+    const int m = (1 << lg) - 1;
+    Kahan g, s1, s2;
+    bool bad = TABLE && sn < 0;
+    for (long long id = (long long)(blockIdx.x + gridDim.x * blockIdx.y) * kThreads + threadIdx.x; id < gs;
+         id += (long long)gridDim.x * gridDim.y * kThreads) {
+        const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
+        const float xc = x[id];
+        const float xk = x[id - k + ((k + 1) & m)];
+        const float xj = x[id + ((long long)(((j + 1) & m) - j) << lg)];
+        const float xi = x[id + ((long long)(((i + 1) & m) - i) << (2 * lg))];
+        const float dk = xk - xc, dj = xj - xc, di = xi - xc;
+        g.add(dk * dk + dj * dj + di * di);
+        s1.add(xc);
+        if (TABLE) {
+            const int q = bad ? -1 : window_find(su, sn, xc);
+            if (q < 0) bad = true;
+            else s2.add(sA[q] + ss[q] * xc);
+        } else {
+            s2.add(xc * xc);
+        }
+    }
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums(v, ctl, P, K, part, counter, a_trace);
+}
+
+struct SplitBufs {
+    const float* xs;   // dphi (step n)
+    float* xd;         // dphi (step n+1)
+    const float* ps;   // dpi  (n-1/2)
+    float* pd;         // dpi  (n+1/2)
+};
+
+// The fused step.  Block (tile, chunk); TK = tile width along k (warp lanes).
+template <bool TABLE, int TK>
+__global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
+                                                    unsigned* counter, double* a_trace, int lg, int TJ, int CH) {
+    extern __shared__ __align__(16) float smem[];
+    const int N = 1 << lg, m = N - 1;
+    const int RS = TK + 3;                 // ring row stride (k from -1 .. TK+1)
+    const int RP = (TJ + 3) * RS;          // ring plane size
+    const int NS = TK + 1;                 // new-plane row stride (k from 0 .. TK)
+    const int NP = (TJ + 1) * NS;          // new-plane size
+    float* ring = smem;                    // 3 planes
+    float* nw = ring + 3 * RP;             // 2 planes
+    float* wk = nw + 2 * NP;               // kick window: u[kWin+1], A[kWin], s[kWin]
+    float* wv = wk + 3 * kWin + 1;         // potential window
+    __shared__ int nk_s, nv_s, active_s;
+    __shared__ float cf[6];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    if (tid == 0) {
+        const SplitCtl& C = *ctl;
+        active_s = C.active;
+        cf[0] = C.d; cf[1] = C.lapl; cf[2] = C.fric; cf[3] = C.pn; cf[4] = C.kv;
+        nk_s = C.wk.n;
+        nv_s = C.wv.n;
+    }
+    if (TABLE) {
+        for (int q = tid; q <= kWin; q += nthr) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q < kWin; q += nthr) {
+            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
+            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+        }
+    }
+    __syncthreads();
+    if (!active_s) return;
+    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const int ntj = N / TJ;
+    const int tj = blockIdx.x % ntj, tk = blockIdx.x / ntj;
+    const int j0 = tj * TJ, k0 = tk * TK, i0 = blockIdx.y * CH;
+    const int cells = (TJ + 1) * (TK + 1);
+
+    auto load_plane = [&](int i) {
+        float* dst = ring + ((i + 3 * N) % 3) * RP;
+        const long long pb = (long long)(i & m) << (2 * lg);
+        for (int e = tid; e < RP; e += nthr) {
+            const int r = e / RS, c = e - r * RS;
+            const int jj = (j0 + r - 1) & m, kk = (k0 + c - 1) & m;
+            dst[e] = B.xs[pb + ((long long)jj << lg) + kk];
+        }
+    };
+
+    Kahan g, s1, s2;
+    bool bad = false;
+    load_plane(i0 - 1);
+    load_plane(i0);
+    for (int p = 0; p <= CH; ++p) {
+        const int i = i0 + p;
+        load_plane(i + 1);
+        __syncthreads();
+        const float* pc = ring + ((i + 3 * N) % 3) * RP;
+        const float* pu = ring + ((i + 1 + 3 * N) % 3) * RP;
+        const float* pl = ring + ((i - 1 + 3 * N) % 3) * RP;
+        float* nc = nw + (p & 1) * NP;
+        const long long pb = (long long)(i & m) << (2 * lg);
+        for (int cix = tid; cix < cells; cix += nthr) {
+            int jl, kl;
+            if (cix < TJ * TK) { jl = cix / TK; kl = cix - jl * TK; }
+            else {
+                const int h = cix - TJ * TK;
+                if (h <= TK) { jl = TJ; kl = h; }
+                else { jl = h - (TK + 1); kl = TK; }
+            }
+            const int o = (jl + 1) * RS + (kl + 1);
+            const float x = pc[o];
+            const float lap = pc[o + 1] + pc[o - 1] + pc[o + RS] + pc[o - RS] + pu[o] + pl[o] - 6.f * x;
+            const long long gi = pb + ((long long)((j0 + jl) & m) << lg) + ((k0 + kl) & m);
+            const float pi0 = B.ps[gi];
+            float dv;
+            if (TABLE) {
+                const int q = window_find(wk, nk_s, x);
+                if (q < 0) { bad = true; dv = 0.f; }
+                else dv = pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
+            } else {
+                dv = kv * x;
+            }
+            const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
+            const float xn = x + d * pin;
+            nc[jl * NS + kl] = xn;
+            if (jl < TJ && kl < TK && p < CH) {
+                B.xd[gi] = xn;
+                B.pd[gi] = pin;
+                s1.add(xn);
+                if (TABLE) {
+                    const int q = window_find(wv, nv_s, xn);
+                    if (q < 0) bad = true;
+                    else s2.add(wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * xn);
+                } else {
+                    s2.add(xn * xn);
+                }
+            }
+        }
+        __syncthreads();
+        const float* np_ = nw + ((p + 1) & 1) * NP;  // previous plane's new values
+        for (int cix = tid; cix < TJ * TK; cix += nthr) {
+            const int jl = cix / TK, kl = cix - jl * TK;
+            const float xc = nc[jl * NS + kl];
+            if (p < CH) {
+                const float dk = nc[jl * NS + kl + 1] - xc;
+                const float dj = nc[(jl + 1) * NS + kl] - xc;
+                g.add(dk * dk + dj * dj);
+            }
+            if (p >= 1) {
+                const float di = xc - np_[jl * NS + kl];
+                g.add(di * di);
+            }
+        }
+    }
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums(v, ctl, P, K, part, counter, a_trace);
+}
+
+// SIGW in the split form: h kick and drift for the coming step, before the
+// scalar step kernel replaces the coefficients (src/evolution.cpp:183-254,
+// 272-281 with the source built from the FP32 dphi gradients).
+__global__ void __launch_bounds__(kThreads) k_split_h(const float* __restrict__ x, SigwSplit S, const SplitCtl* ctl,
+                                                      int lg, float half_over_dx, int kick_only) {
+    const int active = ctl->active;
+    if (!active) return;
+    const float d = ctl->d, lap_n = ctl->lapl, fric = ctl->fric, src = ctl->srcAmp;
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const int m = (1 << lg) - 1;
+    const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
+    const long long kp = id - k + ((k + 1) & m), km = id - k + ((k - 1) & m);
+    const long long jp = id + ((long long)(((j + 1) & m) - j) << lg), jm = id + ((long long)(((j - 1) & m) - j) << lg);
+    const long long ip = id + ((long long)(((i + 1) & m) - i) << (2 * lg));
+    const long long im = id + ((long long)(((i - 1) & m) - i) << (2 * lg));
+    const float gx = (x[ip] - x[im]) * half_over_dx;
+    const float gy = (x[jp] - x[jm]) * half_over_dx;
+    const float gz = (x[kp] - x[km]) * half_over_dx;
+    const float T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const float* h = S.hs[c];
+        const float hc = h[id];
+        const float lf = h[kp] + h[km] + h[jp] + h[jm] + h[ip] + h[im] - 6.f * hc;
+        const float hdo = S.hd[c][id];
+        const float hdn = hdo + d * (lap_n * lf - fric * hdo + src * T[c]);
+        S.hd[c][id] = hdn;
+        if (!kick_only) S.hdst[c][id] = hc + d * hdn;
+    }
+}
+
+// evolve_fields in the split form (in place): dphi += d dpi, h += d hd, and
+// phibar += d pibar for the background.
+__global__ void k_split_drift(float* __restrict__ x, const float* __restrict__ p, SigwSplit S, int sigw, long long gs,
+                              double d, SplitCtl* ctl) {
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id == 0) ctl->phibar = ctl->phibar + d * ctl->pibar;
+    if (id >= gs) return;
+    const float df = (float)d;
+    x[id] = x[id] + df * p[id];
+    if (sigw) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) S.hdst[c][id] = S.hdst[c][id] + df * S.hd[c][id];
+    }
+}
+
+// Kick only (evolve_derivs): dpi += d(...) with the current coefficients.
+template <bool TABLE>
+__global__ void __launch_bounds__(kThreads) k_split_kick(const float* __restrict__ x, float* __restrict__ p,
+                                                         const SplitCtl* ctl, int lg) {
+    __shared__ float wk[3 * kWin + 1];
+    __shared__ int nk;
+    if (!ctl->active) return;
+    if (TABLE) {
+        for (int q = threadIdx.x; q <= kWin; q += blockDim.x) wk[q] = ctl->wk.u[q];
+        for (int q = threadIdx.x; q < kWin; q += blockDim.x) { wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q]; }
+        if (threadIdx.x == 0) nk = ctl->wk.n;
+        __syncthreads();
+    }
+    const float d = ctl->d, lap_n = ctl->lapl, fric = ctl->fric, pn = ctl->pn, kv = ctl->kv;
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const int m = (1 << lg) - 1;
+    const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
+    const float xc = x[id];
+    const float lap = x[id - k + ((k + 1) & m)] + x[id - k + ((k - 1) & m)] +
+                      x[id + ((long long)(((j + 1) & m) - j) << lg)] + x[id + ((long long)(((j - 1) & m) - j) << lg)] +
+                      x[id + ((long long)(((i + 1) & m) - i) << (2 * lg))] +
+                      x[id + ((long long)(((i - 1) & m) - i) << (2 * lg))] - 6.f * xc;
+    float dv;
+    if (TABLE) {
+        const int q = window_find(wk, nk, xc);
+        dv = q < 0 ? 0.f : pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * xc);
+    } else {
+        dv = kv * xc;
+    }
+    const float p0 = p[id];
+    p[id] = p0 + d * (lap_n * lap - fric * p0 - dv);
+}
+
+// f64 = bar + (double)x  (materialise the full field)
+__global__ void k_split_materialize(const float* __restrict__ x, double* __restrict__ out, long long gs,
+                                    const SplitCtl* ctl, int which) {
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= gs) return;
+    const double bar = which ? ctl->pibar : ctl->phibar;
+    out[id] = bar + (double)x[id];
+}
+
+// x = (float)(in - bar) with bar = mean of in (given)
+__global__ void k_split_absorb(const double* __restrict__ in, float* __restrict__ x, long long gs, double bar) {
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= gs) return;
+    x[id] = (float)(in[id] - bar);
+}
+
+// (double) x for spectra of the perturbation
+__global__ void k_split_to_double(const float* __restrict__ x, double* __restrict__ out, long long gs) {
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < gs) out[id] = (double)x[id];
+}
+
+// Lattice sums of the split state for energies / means:
+// [0] sum dphi, [1] sum dphi^2, [2] sum dpi, [3] sum dpi^2, [4] sum sq forward diffs, [5] sum dV (table units)
+template <bool TABLE>
+__global__ void __launch_bounds__(kThreads) k_split_sums(const float* __restrict__ x, const float* __restrict__ p,
+                                                         const SplitCtl* ctl, PotDev P, double* part, int lg) {
+    __shared__ float su[kWin + 1], sA[kWin], ss[kWin];
+    __shared__ int sn;
+    if (TABLE && threadIdx.x == 0) {
+        SplitWin W;
+        int err = 0;
+        build_window(W, P, P.V, P.dyV, ctl->phibar, &err);
+        sn = err ? -1 : W.n;
+        for (int q = 0; q <= W.n && !err; ++q) su[q] = W.u[q];
+        for (int q = 0; q < W.n && !err; ++q) { sA[q] = W.A[q]; ss[q] = W.s[q]; }
+    }
+    __syncthreads();
+    const long long gs = 1LL << (3 * lg);
+    const int m = (1 << lg) - 1;
+    Kahan a0, a1, a2, a3, a4, a5;
+    for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
+        const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
+        const float xc = x[id];
+        const float dk = x[id - k + ((k + 1) & m)] - xc;
+        const float dj = x[id + ((long long)(((j + 1) & m) - j) << lg)] - xc;
+        const float di = x[id + ((long long)(((i + 1) & m) - i) << (2 * lg))] - xc;
+        const float pc = p[id];
+        a0.add(xc);
+        a1.add(xc * xc);
+        a2.add(pc);
+        a3.add(pc * pc);
+        a4.add(dk * dk + dj * dj + di * di);
+        if (TABLE) {
+            const int q = sn < 0 ? -1 : window_find(su, sn, xc);
+            if (q >= 0) a5.add(sA[q] + ss[q] * xc);
+        }
+    }
+    double v[6] = {a0.value(), a1.value(), a2.value(), a3.value(), a4.value(), a5.value()};
+    block_sum<6>(v);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 6; ++q) part[6 * blockIdx.x + q] = v[q];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static SplitConst split_const(const iegpu_ctx* c) {
+    SplitConst K;
+    K.dt = c->cfg.dt;
+    K.s = c->cfg.rescale_s;
+    K.dx = c->cfg.L / (double)c->N;
+    K.gs = (double)c->gs;
+    return K;
+}
+
+struct StepGeom {
+    int TK, TJ, CH, tiles, chunks;
+    size_t smem;
+};
+
+static StepGeom step_geom(const iegpu_ctx* c) {
+    StepGeom g;
+    const int N = c->N;
+    g.TK = N >= 32 ? 32 : N;
+    g.TJ = 256 / g.TK;
+    if (g.TJ > N) g.TJ = N;
+    g.tiles = (N / g.TJ) * (N / g.TK);
+    // about 8 resident CTAs per SM; at least 8 planes per chunk
+    int chunks = 1;
+    while (chunks * 2 <= N / 8 && g.tiles * chunks * 2 <= c->sms * 8) chunks *= 2;
+    g.chunks = chunks;
+    g.CH = N / chunks;
+    const int RS = g.TK + 3, RP = (g.TJ + 3) * RS, NP = (g.TJ + 1) * (g.TK + 1);
+    g.smem = sizeof(float) * (3 * RP + 2 * NP + 2 * (3 * kWin + 1));
+    return g;
+}
+
+static void launch_prime(iegpu_ctx* c, int src) {
+    const SplitConst K = split_const(c);
+    dim3 grid(c->red_grid, 1);
+    if (c->pot.table)
+        k_split_prime<true><<<grid, kThreads, 0, c->stream>>>(c->sp[src], c->sctl, c->pot, K, c->part, c->counter, c->a_trace, c->lg);
+    else
+        k_split_prime<false><<<grid, kThreads, 0, c->stream>>>(c->sp[src], c->sctl, c->pot, K, c->part, c->counter, c->a_trace, c->lg);
+    c->launches++;
+}
+
+static SigwSplit sigw_split(iegpu_ctx* c, int src) {
+    SigwSplit S{};
+    if (!c->cfg.sigw) return S;
+    for (int q = 0; q < 6; ++q) {
+        S.hs[q] = c->h[src][q];
+        S.hdst[q] = c->h[src ^ 1][q];
+        S.hd[q] = c->hd[q];
+    }
+    return S;
+}
+
+static void launch_step(iegpu_ctx* c, int src) {
+    const SplitConst K = split_const(c);
+    if (c->cfg.sigw) {
+        const float hodx = (float)(0.5 / K.dx);
+        k_split_h<<<(unsigned)(c->gs / kThreads), kThreads, 0, c->stream>>>(c->sp[src], sigw_split(c, src), c->sctl,
+                                                                            c->lg, hodx, 0);
+        c->launches++;
+    }
+    const StepGeom g = step_geom(c);
+    SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
+    dim3 grid(g.tiles, g.chunks);
+#define IEGPU_SPLIT_LAUNCH(TAB, TKV)                                                                          \
+    k_split_step<TAB, TKV><<<grid, g.TJ * TKV, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part, c->counter, \
+                                                                    c->a_trace, c->lg, g.TJ, g.CH)
+    const bool tab = c->pot.table != 0;
+    if (g.TK == 32) { if (tab) IEGPU_SPLIT_LAUNCH(true, 32); else IEGPU_SPLIT_LAUNCH(false, 32); }
+    else if (g.TK == 16) { if (tab) IEGPU_SPLIT_LAUNCH(true, 16); else IEGPU_SPLIT_LAUNCH(false, 16); }
+    else { if (tab) IEGPU_SPLIT_LAUNCH(true, 8); else IEGPU_SPLIT_LAUNCH(false, 8); }
+#undef IEGPU_SPLIT_LAUNCH
+    c->launches++;
+}
+
+void split_destroy_graphs(iegpu_ctx* c) {
+    for (int p = 0; p < 2; ++p) {
+        if (c->sp_exec[p]) cudaGraphExecDestroy(c->sp_exec[p]);
+        c->sp_exec[p] = nullptr;
+    }
+}
+
+static int split_graph_steps(const iegpu_ctx* c) { return c->N <= 64 ? 32 : 8; }
+
+static int split_build_graphs(iegpu_ctx* c) {
+    const int L = split_graph_steps(c);
+    for (int p = 0; p < 2; ++p) {
+        cudaGraph_t gph;
+        if (check_cuda(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture")) return IEGPU_ECUDA;
+        const long long before = c->launches;
+        for (int s = 0; s < L; ++s) launch_step(c, (p + s) & 1);
+        c->launches = before;
+        if (check_cuda(c, cudaStreamEndCapture(c->stream, &gph), "graph capture end")) return IEGPU_ECUDA;
+        cudaError_t e = cudaGraphInstantiate(&c->sp_exec[p], gph, 0);
+        cudaGraphDestroy(gph);
+        if (check_cuda(c, e, "graph instantiate")) return IEGPU_ECUDA;
+    }
+    c->sp_steps = L;
+    return IEGPU_OK;
+}
+
+static int sctl_up(iegpu_ctx* c) {
+    return check_cuda(c, cudaMemcpyAsync(c->sctl, c->sctl_h, sizeof(SplitCtl), cudaMemcpyHostToDevice, c->stream), "split control upload");
+}
+
+static int sctl_down(iegpu_ctx* c) {
+    if (check_cuda(c, cudaMemcpyAsync(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost, c->stream), "split control download"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "split")) return IEGPU_ECUDA;
+    if (c->sctl_h->error == IEGPU_ERANGE) {
+        return set_error(c, IEGPU_ERANGE,
+                         "Field value near %.17g is outside the numerical potential range [%.17g, %.17g].\n",
+                         c->sctl_h->errval, c->htab_x.empty() ? 0.0 : c->htab_x.back(),
+                         c->htab_x.empty() ? 0.0 : c->htab_x.front());
+    }
+    return IEGPU_OK;
+}
+
+static void sctl_fill(iegpu_ctx* c, const iegpu_bg* bg, int mode) {
+    SplitCtl& C = *c->sctl_h;
+    C.bg.t = bg->t;
+    C.bg.a = bg->a;
+    C.bg.ad = bg->ad;
+    C.bg.ad2 = bg->ad2;
+    C.bg.astep = bg->astep;
+    C.mode = mode;
+    C.steps_done = 0;
+    C.steps_limit = 0;
+    C.done = 0;
+    C.error = 0;
+    C.active = 0;
+}
+
+static void sctl_bg(const iegpu_ctx* c, iegpu_bg* bg) {
+    const DevBg& B = c->sctl_h->bg;
+    bg->t = B.t;
+    bg->a = B.a;
+    bg->ad = B.ad;
+    bg->ad2 = B.ad2;
+    bg->astep = B.astep;
+}
+
+// The host mirror of the split control holds phibar/pibar between calls; it
+// is refreshed from the device after every call that changes them.
+int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace) {
+    if (steps) *steps = 0;
+    if (max_steps <= 0) return max_steps < 0 ? set_error(c, IEGPU_EINVAL, "max_steps must be >= 0") : IEGPU_OK;
+    if (max_steps > c->a_trace_cap) {
+        if (c->a_trace) cudaFree(c->a_trace);
+        c->a_trace = nullptr;
+        c->a_trace_cap = 0;
+        const int cap = max_steps < 1024 ? 1024 : max_steps;
+        if (check_cuda(c, cudaMalloc(&c->a_trace, sizeof(double) * (size_t)cap), "a_trace alloc")) return IEGPU_ENOMEM;
+        c->a_trace_cap = cap;
+        split_destroy_graphs(c);
+        fp64_destroy_graphs(c);
+    }
+    if (!c->sp_exec[0]) {
+        int rc = split_build_graphs(c);
+        if (rc) return rc;
+    }
+    sctl_fill(c, bg, kModeLeapfrog);
+    c->sctl_h->af = af;
+    c->sctl_h->steps_limit = max_steps;
+    if (sctl_up(c)) return IEGPU_ECUDA;
+    const int start = c->cur;
+    launch_prime(c, start);  // sums of the current state -> coefficients of step 0
+    const int L = c->sp_steps;
+    const int launches = (max_steps + L - 1) / L;
+    for (int q = 0; q < launches; ++q) {
+        if (check_cuda(c, cudaGraphLaunch(c->sp_exec[start], c->stream), "graph launch")) return IEGPU_ECUDA;
+        c->launches += (long long)L * (c->cfg.sigw ? 2 : 1);
+    }
+    int rc = sctl_down(c);
+    const int taken = c->sctl_h->steps_done;
+    c->cur = (start + taken) & 1;
+    if (rc) return rc;
+    sctl_bg(c, bg);
+    if (steps) *steps = taken;
+    if (a_trace && taken > 0 &&
+        check_cuda(c, cudaMemcpy(a_trace, c->a_trace, sizeof(double) * taken, cudaMemcpyDeviceToHost), "a_trace"))
+        return IEGPU_ECUDA;
+    return IEGPU_OK;
+}
+
+int split_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    sctl_fill(c, bg, kModeKick);
+    c->sctl_h->d_given = d;
+    c->sctl_h->steps_limit = 1;
+    if (sctl_up(c)) return IEGPU_ECUDA;
+    launch_prime(c, c->cur);
+    const unsigned grid = (unsigned)(c->gs / kThreads);
+    if (c->cfg.sigw) {
+        const float hodx = (float)(0.5 / (c->cfg.L / (double)c->N));
+        k_split_h<<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], sigw_split(c, c->cur), c->sctl, c->lg, hodx, 1);
+        c->launches++;
+    }
+    if (c->pot.table) k_split_kick<true><<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->lg);
+    else k_split_kick<false><<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->lg);
+    c->launches++;
+    int rc = sctl_down(c);
+    if (rc) return rc;
+    sctl_bg(c, bg);
+    return IEGPU_OK;
+}
+
+int split_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    bg->t += d;
+    SigwSplit S{};
+    if (c->cfg.sigw)
+        for (int q = 0; q < 6; ++q) { S.hdst[q] = c->h[c->cur][q]; S.hd[q] = c->hd[q]; }
+    k_split_drift<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], S, c->cfg.sigw,
+                                                                          (long long)c->gs, d, c->sctl);
+    c->launches++;
+    bg->a += d * bg->ad;
+    if (check_cuda(c, cudaMemcpyAsync(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost, c->stream), "split ctl"))
+        return IEGPU_ECUDA;
+    return sync_and_check(c, "split evolve_fields");
+}
+
+// sums of the split state: [sum dphi, sum dphi^2, sum dpi, sum dpi^2, sum sq diffs, sum dV]
+int split_sums(iegpu_ctx* c, double out[6]) {
+    const int g = c->red_grid;
+    if (c->pot.table) k_split_sums<true><<<g, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->pot, c->part, c->lg);
+    else k_split_sums<false><<<g, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->pot, c->part, c->lg);
+    c->launches++;
+    std::vector<double> h((size_t)g * 6);
+    if (check_cuda(c, cudaMemcpyAsync(h.data(), c->part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream), "split sums"))
+        return IEGPU_ECUDA;
+    if (check_cuda(c, cudaMemcpyAsync(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost, c->stream), "split ctl"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "split sums")) return IEGPU_ECUDA;
+    for (int q = 0; q < 6; ++q) out[q] = 0.0;
+    for (int b = 0; b < g; ++b)
+        for (int q = 0; q < 6; ++q) out[q] += h[6 * (size_t)b + q];
+    return IEGPU_OK;
+}
+
+int split_materialize(iegpu_ctx* c, int which, double* out) {
+    const float* x = which ? c->spi[c->cur] : c->sp[c->cur];
+    k_split_materialize<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(x, out, (long long)c->gs, c->sctl, which);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "materialize");
+}
+
+int split_to_double(iegpu_ctx* c, int which, double* out) {
+    const float* x = which ? c->spi[c->cur] : c->sp[c->cur];
+    k_split_to_double<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(x, out, (long long)c->gs);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "to double");
+}
+
+// Takes an FP64 field already on the device: bar = its mean, x = in - bar.
+int split_absorb(iegpu_ctx* c, int which, const double* in, double mean) {
+    float* x = which ? c->spi[c->cur] : c->sp[c->cur];
+    k_split_absorb<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(in, x, (long long)c->gs, mean);
+    c->launches++;
+    if (which) c->sctl_h->pibar = mean;
+    else c->sctl_h->phibar = mean;
+    // only the background fields of the control block change here
+    const size_t off = which ? offsetof(SplitCtl, pibar) : offsetof(SplitCtl, phibar);
+    return check_cuda(c, cudaMemcpyAsync(reinterpret_cast<char*>(c->sctl) + off, reinterpret_cast<char*>(c->sctl_h) + off,
+                                         sizeof(double), cudaMemcpyHostToDevice, c->stream), "absorb");
+}
+
+}  // namespace iegpu

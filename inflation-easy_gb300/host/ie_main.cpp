@@ -249,7 +249,9 @@ void initialize_fields_host() {
 }
 
 void initialize_fields() {
-    if (P.ic_on_host) {
+    if (P.ic_on_host && P.form == 1)
+        std::fprintf(stderr, "ic_on_host applies to the FP64 form; the split form draws its modes on the device.\n");
+    if (P.ic_on_host && P.form == 0) {
         initialize_fields_host();
         return;
     }

@@ -1,0 +1,102 @@
+"""The split-precision form (FP32 perturbations about an FP64 background)
+against the FP64 oracle.
+
+Tolerances (the form's stated error budget):
+  * perturbation fields after 300 steps: max|x - x_oracle| <= 1e-4 * std(x_oracle - mean)
+  * a, ad, t: relative 1e-9 (FP64 background; lattice sums formed from FP32 data)
+  * P_dphi per k-bin (bins >= 1): relative 1e-4; bin counts exact
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from test_gpu_parity import oracle_state
+
+pytestmark = pytest.mark.gpu
+
+
+def split_like(engine, p, o, usr, sigw, tables):
+    lat = engine.Lattice(p.N, p.L, p.dt, p.V0, p.ns, p.rescale_B, form=engine.FORM_SPLIT,
+                         potential=engine.POT_TABLE if usr else engine.POT_HILLTOP, sigw=sigw)
+    if usr:
+        lat.set_table(*tables)
+    lat.upload(engine.F, o.f.copy())
+    lat.upload(engine.FD, o.fd.copy())
+    if sigw:
+        for c in range(6):
+            lat.upload(engine.H(c), o.h_(c).copy())
+            lat.upload(engine.HD(c), o.hd_(c).copy())
+    s = o.scalars
+    return lat, engine.Bg(s.t, s.a, s.ad, s.ad2, s.astep)
+
+
+def pert_err(got, ref):
+    d = ref - ref.mean()
+    return float(np.max(np.abs(got - ref)) / np.std(d))
+
+
+def test_split_round_trip(engine, oracle_mod):
+    p, o = oracle_state(oracle_mod, 32, False, False, None)
+    lat, bg = split_like(engine, p, o, False, False, None)
+    with lat:
+        f = lat.download(engine.F)
+        assert pert_err(f, o.f) < 1e-6
+        sf, sfd, sf2 = lat.means()
+        assert np.isclose(sf, o.f.sum(), rtol=1e-13)
+        assert np.isclose(sfd, o.fd.sum(), rtol=1e-12)
+        assert np.isclose(sf2, (o.f ** 2).sum(), rtol=1e-12)
+        k, g, v = lat.energies(bg)
+        ko, go, vo = o.energies()
+        assert np.isclose(k, ko, rtol=1e-10) and np.isclose(v, vo, rtol=1e-12)
+        assert np.isclose(g, go, rtol=1e-4)
+
+
+@pytest.mark.parametrize("N,usr,sigw", [(32, False, False), (32, True, False), (16, True, True), (64, False, False)])
+def test_split_leapfrog_matches_fp64(N, usr, sigw, engine, oracle_mod, tables):
+    p, o = oracle_state(oracle_mod, N, usr, sigw, tables)
+    lat, bg = split_like(engine, p, o, usr, sigw, tables)
+    with lat:
+        taken = lat.leapfrog(p.af, 300, bg)
+        assert taken == 300
+        o.leapfrog_steps(300)
+        s = o.scalars
+        for got, ref in ((bg.a, s.a), (bg.ad, s.ad), (bg.t, s.t)):
+            assert abs(got - ref) <= 1e-9 * abs(ref)
+        assert pert_err(lat.download(engine.F), o.f) < 1e-4
+        assert pert_err(lat.download(engine.FD), o.fd) < 1e-4
+        if sigw:
+            for c in range(6):
+                h = lat.download(engine.H(c))
+                ref = o.h_(c)
+                assert np.max(np.abs(h - ref)) <= 1e-3 * np.std(ref)
+
+
+def test_split_spectrum(engine, oracle_mod):
+    p, o = oracle_state(oracle_mod, 32, False, False, None, steps=100)
+    lat, bg = split_like(engine, p, o, False, False, None)
+    with lat:
+        counts, f2 = lat.spectrum(engine.F)
+        oc, of2 = o.spectrum_f()
+        assert np.array_equal(counts, oc)
+        assert np.isclose(f2[0], of2[0], rtol=1e-12)
+        assert np.allclose(f2[1:], of2[1:], rtol=1e-6)
+
+
+def test_split_deltaN_stage(engine, oracle_mod, tables):
+    p, o = oracle_state(oracle_mod, 16, True, False, tables, steps=30)
+    lat, bg = split_like(engine, p, o, True, False, tables)
+    with lat:
+        lat.initializeN(o.scalars.a)
+        o.initializeN()
+        lat.evolve_fieldsN(0.5 * p.dN, 0.0)
+        o.evolve_fieldsN(0.5 * p.dN)
+        phiref = lat.get_phiref()
+        s = o.scalars
+        s.phiref = o.get_phiref()
+        o.set_scalars(s)
+        assert abs(phiref - s.phiref) <= 1e-12 * abs(phiref)
+        lat.deltaN_steps(p.dN, 200, phiref)
+        o.deltaN_steps(200)
+        dn = lat.download(engine.DELTAN)
+        assert np.max(np.abs(dn - o.deltaN)) <= 3 * p.dN
