@@ -17,7 +17,7 @@ __device__ __forceinline__ double warp_sum(double v) {
 // Sum over the block of NV values per thread; result valid in thread 0.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV]) {
-    __shared__ double sh[NV][kThreads / 32];
+    __shared__ double sh[NV][32];  // up to 32 warps per block
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < NV; ++q) v[q] = warp_sum(v[q]);

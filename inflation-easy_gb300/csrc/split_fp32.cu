@@ -39,7 +39,7 @@ namespace iegpu {
 // ---------------------------------------------------------------------------
 
 // Window around phibar: brackets l0 .. l0+n-1; u[q] = x[l0-1+q] - phibar.
-__device__ void build_window(SplitWin& W, const PotDev& P, const double* y, const double* dy, double phibar,
+__device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, const double* y, const double* dy, double phibar,
                              int* err) {
     W.ok = 0;
     if (!P.table) return;
@@ -99,7 +99,7 @@ __device__ void bar_potential(const PotDev& P, double phibar, double* V, double*
 
 // sums: [0] sum of squared forward differences of dphi, [1] sum dphi,
 // [2] hilltop: sum dphi^2 / table: sum of V differences (table units)
-__device__ void split_scalars(SplitCtl& C, const PotDev& P, const SplitConst& K, const double* sums, double* a_trace) {
+__device__ __noinline__ void split_scalars(SplitCtl& C, const PotDev& P, const SplitConst& K, const double* sums, double* a_trace) {
     double d;
     if (C.mode == kModeLeapfrog) {
         if (C.steps_done >= C.steps_limit) { C.active = 0; C.done = 1; return; }
@@ -256,18 +256,48 @@ struct SplitBufs {
     float* pd;         // dpi  (n+1/2)
 };
 
+// Asynchronous global -> shared copies (cp.async), so the planes a CTA will
+// need next are in flight while it works on the current one.
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int n>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory"); }
+
+constexpr int kPrefetch = 3;   // planes in flight ahead of the one being computed
+constexpr int kPhiSlots = 6;   // three stencil planes + kPrefetch
+constexpr int kPiSlots = 4;    // one plane in use + kPrefetch
+constexpr int kColOff = 4;     // shared-memory column of k = 0 (16-byte aligned rows)
+
+// Shared-memory floats of the step kernel for tile TJ x TK.
+__host__ __device__ inline int split_step_smem_floats(int TJ, int TK) {
+    const int RS = TK + 8;
+    return kPhiSlots * (TJ + 3) * RS + kPiSlots * (TJ + 1) * RS + 2 * (TJ + 1) * (TK + 1) + 2 * (3 * kWin + 1);
+}
+
 // The fused step.  Block (tile, chunk); TK = tile width along k (warp lanes).
+// Shared rows hold k = -1 .. TK+1 at columns kColOff-1 .. kColOff+TK+1 with
+// the tile interior 16-byte aligned, so each interior row segment arrives as
+// TK/4 16-byte copies and the three halo columns as 4-byte copies.
 template <bool TABLE, int TK>
-__global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
+__global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
                                                     unsigned* counter, double* a_trace, int lg, int TJ, int CH) {
     extern __shared__ __align__(16) float smem[];
     const int N = 1 << lg, m = N - 1;
-    const int RS = TK + 3;                 // ring row stride (k from -1 .. TK+1)
-    const int RP = (TJ + 3) * RS;          // ring plane size
+    constexpr int RS = TK + 8;             // row stride (floats, multiple of 4)
+    const int RP = (TJ + 3) * RS;          // dphi plane: rows j = -1 .. TJ+1
+    const int PP = (TJ + 1) * RS;          // dpi plane: rows j = 0 .. TJ
     const int NS = TK + 1;                 // new-plane row stride (k from 0 .. TK)
     const int NP = (TJ + 1) * NS;          // new-plane size
-    float* ring = smem;                    // 3 planes
-    float* nw = ring + 3 * RP;             // 2 planes
+    float* ring = smem;                    // kPhiSlots dphi planes
+    float* pis = ring + kPhiSlots * RP;    // kPiSlots dpi planes
+    float* nw = pis + kPiSlots * PP;       // 2 planes of new dphi
     float* wk = nw + 2 * NP;               // kick window: u[kWin+1], A[kWin], s[kWin]
     float* wv = wk + 3 * kWin + 1;         // potential window
     __shared__ int nk_s, nv_s, active_s;
@@ -294,28 +324,56 @@ __global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, 
     const int tj = blockIdx.x % ntj, tk = blockIdx.x / ntj;
     const int j0 = tj * TJ, k0 = tk * TK, i0 = blockIdx.y * CH;
     const int cells = (TJ + 1) * (TK + 1);
+    constexpr int QV = TK / 4;             // 16-byte segments per interior row
 
-    auto load_plane = [&](int i) {
-        float* dst = ring + ((i + 3 * N) % 3) * RP;
-        const long long pb = (long long)(i & m) << (2 * lg);
-        for (int e = tid; e < RP; e += nthr) {
-            const int r = e / RS, c = e - r * RS;
-            const int jj = (j0 + r - 1) & m, kk = (k0 + c - 1) & m;
-            dst[e] = B.xs[pb + ((long long)jj << lg) + kk];
+    // dphi plane i (rows j0-1 .. j0+TJ+1, columns k0-1 .. k0+TK+1)
+    auto issue_phi = [&](int i) {
+        float* dst = ring + ((i - i0 + 1) % kPhiSlots) * RP;
+        const float* src = B.xs + ((long long)(i & m) << (2 * lg));
+        const int ops = (TJ + 3) * (QV + 3);
+        for (int o = tid; o < ops; o += nthr) {
+            const int r = o / (QV + 3), w = o - r * (QV + 3);
+            const float* row = src + ((long long)((j0 + r - 1) & m) << lg);
+            float* srow = dst + r * RS;
+            if (w < QV) cp_async16(srow + kColOff + 4 * w, row + k0 + 4 * w);
+            else {
+                const int kl = (w == QV) ? -1 : TK + (w - QV - 1);
+                cp_async4(srow + kColOff + kl, row + ((k0 + kl) & m));
+            }
+        }
+    };
+    // dpi plane i (rows j0 .. j0+TJ, columns k0 .. k0+TK)
+    auto issue_pi = [&](int i) {
+        float* dst = pis + ((i - i0) % kPiSlots) * PP;
+        const float* src = B.ps + ((long long)(i & m) << (2 * lg));
+        const int ops = (TJ + 1) * (QV + 1);
+        for (int o = tid; o < ops; o += nthr) {
+            const int r = o / (QV + 1), w = o - r * (QV + 1);
+            const float* row = src + ((long long)((j0 + r) & m) << lg);
+            float* srow = dst + r * RS;
+            if (w < QV) cp_async16(srow + kColOff + 4 * w, row + k0 + 4 * w);
+            else cp_async4(srow + kColOff + TK, row + ((k0 + TK) & m));
         }
     };
 
     Kahan g, s1, s2;
     bool bad = false;
-    load_plane(i0 - 1);
-    load_plane(i0);
+    issue_phi(i0 - 1);
+    issue_phi(i0);
+    cp_commit();
+    for (int q = 0; q < kPrefetch; ++q) {
+        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+        if (q <= CH) issue_pi(i0 + q);
+        cp_commit();
+    }
     for (int p = 0; p <= CH; ++p) {
         const int i = i0 + p;
-        load_plane(i + 1);
+        cp_wait<kPrefetch - 1>();
         __syncthreads();
-        const float* pc = ring + ((i + 3 * N) % 3) * RP;
-        const float* pu = ring + ((i + 1 + 3 * N) % 3) * RP;
-        const float* pl = ring + ((i - 1 + 3 * N) % 3) * RP;
+        const float* pc = ring + ((p + 1) % kPhiSlots) * RP;
+        const float* pu = ring + ((p + 2) % kPhiSlots) * RP;
+        const float* pl = ring + (p % kPhiSlots) * RP;
+        const float* pp = pis + (p % kPiSlots) * PP;
         float* nc = nw + (p & 1) * NP;
         const long long pb = (long long)(i & m) << (2 * lg);
         for (int cix = tid; cix < cells; cix += nthr) {
@@ -326,11 +384,10 @@ __global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, 
                 if (h <= TK) { jl = TJ; kl = h; }
                 else { jl = h - (TK + 1); kl = TK; }
             }
-            const int o = (jl + 1) * RS + (kl + 1);
+            const int o = (jl + 1) * RS + (kl + kColOff);
             const float x = pc[o];
             const float lap = pc[o + 1] + pc[o - 1] + pc[o + RS] + pc[o - RS] + pu[o] + pl[o] - 6.f * x;
-            const long long gi = pb + ((long long)((j0 + jl) & m) << lg) + ((k0 + kl) & m);
-            const float pi0 = B.ps[gi];
+            const float pi0 = pp[jl * RS + kl + kColOff];
             float dv;
             if (TABLE) {
                 const int q = window_find(wk, nk_s, x);
@@ -343,6 +400,7 @@ __global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, 
             const float xn = x + d * pin;
             nc[jl * NS + kl] = xn;
             if (jl < TJ && kl < TK && p < CH) {
+                const long long gi = pb + ((long long)(j0 + jl) << lg) + (k0 + kl);
                 B.xd[gi] = xn;
                 B.pd[gi] = pin;
                 s1.add(xn);
@@ -356,6 +414,10 @@ __global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, 
             }
         }
         __syncthreads();
+        // planes kPrefetch ahead (the slots of planes no longer needed)
+        if (p + kPrefetch + 1 <= CH + 1) issue_phi(i + 1 + kPrefetch);
+        if (p + kPrefetch <= CH) issue_pi(i + kPrefetch);
+        cp_commit();
         const float* np_ = nw + ((p + 1) & 1) * NP;  // previous plane's new values
         for (int cix = tid; cix < TJ * TK; cix += nthr) {
             const int jl = cix / TK, kl = cix - jl * TK;
@@ -371,6 +433,165 @@ __global__ void __launch_bounds__(256) k_split_step(SplitBufs B, SplitCtl* ctl, 
             }
         }
     }
+    cp_wait<0>();
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums(v, ctl, P, K, part, counter, a_trace);
+}
+
+// Full-row variant of the step for 32 <= N <= 512: a tile is TJ rows of
+// complete k lines, so the k direction is periodic inside shared memory and
+// needs no halo.  Warp w computes row j0+w for w = 0..TJ (row TJ is the +j
+// halo row whose new values only feed the j differences of row TJ-1); lane l
+// handles k = l + 32c, c < C = N/32.  The planes come in through a cp.async
+// ring kRowPrefetch planes ahead.  Row partial sums are added per plane into
+// Kahan-compensated per-thread accumulators.
+constexpr int kRowPrefetch = 2;
+constexpr int kRowPhiSlots = 3 + kRowPrefetch;
+constexpr int kRowPiSlots = 1 + kRowPrefetch;
+
+__host__ __device__ inline int split_row_smem_floats(int TJ, int N) {
+    return kRowPhiSlots * (TJ + 3) * N + kRowPiSlots * (TJ + 1) * N + (TJ + 1) * N + 2 * (3 * kWin + 1);
+}
+
+template <bool TABLE, int C, int TJ>
+__global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
+                                                              double* part, unsigned* counter, double* a_trace,
+                                                              int CH) {
+    constexpr int N = 32 * C, m = N - 1;
+    constexpr int lgN = (C == 1) ? 5 : (C == 2) ? 6 : (C == 4) ? 7 : (C == 8) ? 8 : 9;
+    constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
+    extern __shared__ __align__(16) float smem[];
+    float* ring = smem;
+    float* pis = ring + kRowPhiSlots * RP;
+    float* nb = pis + kRowPiSlots * PP;
+    float* wk = nb + (TJ + 1) * N;
+    float* wv = wk + 3 * kWin + 1;
+    __shared__ int nk_s, nv_s, active_s;
+    __shared__ float cf[6];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        const SplitCtl& Cc = *ctl;
+        active_s = Cc.active;
+        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
+        nk_s = Cc.wk.n;
+        nv_s = Cc.wv.n;
+    }
+    if (TABLE) {
+        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q < kWin; q += NTH) {
+            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
+            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+        }
+    }
+    __syncthreads();
+    if (!active_s) return;
+    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const int j0 = blockIdx.x * TJ, i0 = blockIdx.y * CH;
+
+    auto issue_phi = [&](int i) {
+        float* dst = ring + ((i - i0 + 1) % kRowPhiSlots) * RP;
+        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 3) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
+        }
+    };
+    auto issue_pi = [&](int i) {
+        float* dst = pis + ((i - i0) % kRowPiSlots) * PP;
+        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 1) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
+        }
+    };
+
+    Kahan g, s1, s2;
+    bool bad = false;
+    float xprev[C];
+    issue_phi(i0 - 1);
+    issue_phi(i0);
+    cp_commit();
+    for (int q = 0; q < kRowPrefetch; ++q) {
+        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+        if (q <= CH) issue_pi(i0 + q);
+        cp_commit();
+    }
+    const int jl = w;              // row of this warp (TJ: halo row)
+    const bool interior = jl < TJ;
+    for (int p = 0; p <= CH; ++p) {
+        const int i = i0 + p;
+        cp_wait<kRowPrefetch - 1>();
+        __syncthreads();
+        const float* pc = ring + ((p + 1) % kRowPhiSlots) * RP + (jl + 1) * N;
+        const float* pu = ring + ((p + 2) % kRowPhiSlots) * RP + (jl + 1) * N;
+        const float* pl = ring + (p % kRowPhiSlots) * RP + (jl + 1) * N;
+        const float* pp = pis + (p % kRowPiSlots) * PP + jl * N;
+        float xnew[C];
+        float rs1 = 0.f, rs2 = 0.f;
+        const bool store = interior && p < CH;
+        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int k = lane + 32 * c;
+            const float x = pc[k];
+            const float lap = pc[(k + 1) & m] + pc[(k - 1) & m] + pc[k + N] + pc[k - N] + pu[k] + pl[k] - 6.f * x;
+            const float pi0 = pp[k];
+            float dv;
+            if (TABLE) {
+                const int q = window_find(wk, nk_s, x);
+                if (q < 0) { bad = true; dv = 0.f; }
+                else dv = pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
+            } else {
+                dv = kv * x;
+            }
+            const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
+            const float xn = x + d * pin;
+            xnew[c] = xn;
+            nb[jl * N + k] = xn;
+            if (store) {
+                B.xd[gb + k] = xn;
+                B.pd[gb + k] = pin;
+                rs1 += xn;
+                if (TABLE) {
+                    const int q = window_find(wv, nv_s, xn);
+                    if (q < 0) bad = true;
+                    else rs2 += wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * xn;
+                } else {
+                    rs2 += xn * xn;
+                }
+            }
+        }
+        __syncthreads();
+        // planes kRowPrefetch ahead go into the slots no longer needed
+        if (p + kRowPrefetch + 1 <= CH + 1) issue_phi(i + 1 + kRowPrefetch);
+        if (p + kRowPrefetch <= CH) issue_pi(i + kRowPrefetch);
+        cp_commit();
+        if (interior) {
+            float rg = 0.f;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int k = lane + 32 * c;
+                if (p < CH) {
+                    const float dk = nb[jl * N + ((k + 1) & m)] - xnew[c];
+                    const float dj = nb[(jl + 1) * N + k] - xnew[c];
+                    rg += dk * dk + dj * dj;
+                }
+                if (p >= 1) {
+                    const float di = xnew[c] - xprev[c];
+                    rg += di * di;
+                }
+                xprev[c] = xnew[c];
+            }
+            g.add(rg);
+            if (store) { s1.add(rs1); s2.add(rs2); }
+        }
+    }
+    cp_wait<0>();
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
@@ -537,22 +758,36 @@ static SplitConst split_const(const iegpu_ctx* c) {
 struct StepGeom {
     int TK, TJ, CH, tiles, chunks;
     size_t smem;
+    bool rows;   // full-row kernel (32 <= N <= 512)
 };
 
 static StepGeom step_geom(const iegpu_ctx* c) {
     StepGeom g;
     const int N = c->N;
+    if (N >= 32 && N <= 512) {
+        g.rows = true;
+        g.TK = N;
+        g.TJ = N == 512 ? 4 : 8;
+        g.tiles = N / g.TJ;
+        // about two resident CTAs per SM, at least 8 planes per chunk
+        int chunks = 1;
+        while (chunks * 2 <= N / 8 && g.tiles * chunks * 2 <= c->sms * 2) chunks *= 2;
+        g.chunks = chunks;
+        g.CH = N / chunks;
+        g.smem = sizeof(float) * (size_t)split_row_smem_floats(g.TJ, N);
+        return g;
+    }
+    g.rows = false;
     g.TK = N >= 32 ? 32 : N;
     g.TJ = 256 / g.TK;
     if (g.TJ > N) g.TJ = N;
     g.tiles = (N / g.TJ) * (N / g.TK);
-    // about 8 resident CTAs per SM; at least 8 planes per chunk
+    // one wave of resident CTAs (4 per SM at 64 registers); at least 8 planes per chunk
     int chunks = 1;
-    while (chunks * 2 <= N / 8 && g.tiles * chunks * 2 <= c->sms * 8) chunks *= 2;
+    while (chunks * 2 <= N / 8 && g.tiles * chunks * 2 <= c->sms * 4) chunks *= 2;
     g.chunks = chunks;
     g.CH = N / chunks;
-    const int RS = g.TK + 3, RP = (g.TJ + 3) * RS, NP = (g.TJ + 1) * (g.TK + 1);
-    g.smem = sizeof(float) * (3 * RP + 2 * NP + 2 * (3 * kWin + 1));
+    g.smem = sizeof(float) * (size_t)split_step_smem_floats(g.TJ, g.TK);
     return g;
 }
 
@@ -588,6 +823,30 @@ static void launch_step(iegpu_ctx* c, int src) {
     const StepGeom g = step_geom(c);
     SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
     dim3 grid(g.tiles, g.chunks);
+    if (g.rows) {
+        const bool tab = c->pot.table != 0;
+#define IEGPU_ROWS(TAB, CC, TJV)                                                                                 \
+    do {                                                                                                      \
+        static bool attr = false;                                                                             \
+        if (!attr) {                                                                                          \
+            cudaFuncSetAttribute(k_split_rows<TAB, CC, TJV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                 (int)g.smem);                                                                \
+            attr = true;                                                                                      \
+        }                                                                                                     \
+        k_split_rows<TAB, CC, TJV><<<grid, (TJV + 1) * 32, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part, \
+                                                                             c->counter, c->a_trace, g.CH);     \
+    } while (0)
+        switch (c->N) {
+            case 32: if (tab) IEGPU_ROWS(true, 1, 8); else IEGPU_ROWS(false, 1, 8); break;
+            case 64: if (tab) IEGPU_ROWS(true, 2, 8); else IEGPU_ROWS(false, 2, 8); break;
+            case 128: if (tab) IEGPU_ROWS(true, 4, 8); else IEGPU_ROWS(false, 4, 8); break;
+            case 256: if (tab) IEGPU_ROWS(true, 8, 8); else IEGPU_ROWS(false, 8, 8); break;
+            default: if (tab) IEGPU_ROWS(true, 16, 4); else IEGPU_ROWS(false, 16, 4); break;
+        }
+#undef IEGPU_ROWS
+        c->launches++;
+        return;
+    }
 #define IEGPU_SPLIT_LAUNCH(TAB, TKV)                                                                          \
     k_split_step<TAB, TKV><<<grid, g.TJ * TKV, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part, c->counter, \
                                                                     c->a_trace, c->lg, g.TJ, g.CH)

@@ -95,7 +95,8 @@ def test_split_deltaN_stage(engine, oracle_mod, tables):
         s = o.scalars
         s.phiref = o.get_phiref()
         o.set_scalars(s)
-        assert abs(phiref - s.phiref) <= 1e-12 * abs(phiref)
+        # phi = phibar + (double)dphi carries the FP32 rounding of dphi (~1e-7 of dphi)
+        assert abs(phiref - s.phiref) <= 1e-6 * np.std(o.f)
         lat.deltaN_steps(p.dN, 200, phiref)
         o.deltaN_steps(200)
         dn = lat.download(engine.DELTAN)
