@@ -8,7 +8,11 @@ kick + drift of every site) run by the engine.  A step is one leapfrog step of
 the whole 256^3 lattice; value = steps * 256^3 / device time.  The lattice
 state (384 MB in FP64) is larger than L2, so no flush is needed between steps.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--form fp64]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+The headline value is the split form (FP32 perturbations about an FP64
+background); the plain FP64 form is measured on the same workload and reported
+under "forms".
 
 --impl reference times the reference's own CPU algorithm for the same step
 (the oracle port of it, oracle/ieo.c, OpenMP on all host cores; the reference
@@ -38,9 +42,9 @@ N_DEFAULT = 256
 WORKLOAD = dict(L=10.0, dt=1e-3, V0=3.338e-13, ns=0.965, phi0=0.0935, dphi0=0.000796, seed=8)
 METRIC = "site-updates/s at 256^3 (leapfrog: Friedmann + kick + drift per site)"
 UNIT = "site-updates/s"
-# algorithmic HBM bytes per site of each kernel of one FP64 step
-BYTES_KICK_FP64 = 32   # read f, fd; write f, fd
-BYTES_REDUCE_FP64 = 8  # read f
+# algorithmic HBM bytes per site of the dominant kernel of one step
+BYTES_STEP_SPLIT = 16  # split form: read dphi, dpi; write dphi, dpi (FP32)
+BYTES_KICK_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
 
 
 def dist_env():
@@ -179,47 +183,86 @@ def reference_arm(args):
     return 0
 
 
-def engine_arm(args):
-    ws, rank, local = dist_env()
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None):
+    """Times `steps` leapfrog steps of one form; returns a dict of figures."""
     import numpy as np
-
-    import iegpu
-    N = args.n
-    lat, bg = make_lattice(iegpu, N)
-    af = 1e30  # time a fixed number of steps
-    lat.leapfrog(af, args.warmup, bg)
+    w = WORKLOAD
+    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=form)
+    H = lat.bunch_davies(w["seed"], w["phi0"], w["dphi0"])
+    bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
+    lat.evolve_fields(0.5 * w["dt"], bg)   # first half drift, src/evolution.cpp:935
+    af = 1e30  # a fixed number of steps is timed
+    lat.leapfrog(af, warmup, bg)   # the first call also runs the launch-shape autotuner (split form)
     bg.astep = bg.a  # the loop's "astep = a", src/evolution.cpp:944
+    shape = lat.autotune(bg) if form == iegpu.FORM_SPLIT else None
     if dist:
         dist.barrier()
     launches0 = lat.launches
-    cvd = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip()
-    with Clocks(int(cvd) if cvd.isdigit() else local) as clk:
-        lat.timer_start()
-        taken = lat.leapfrog(af, args.steps, bg)
-        ms = lat.timer_stop()
+    clk = Clocks(clocks_index) if clocks_index is not None else None
+    if clk:
+        clk.__enter__()
+    lat.timer_start()
+    taken = lat.leapfrog(af, steps, bg)
+    ms = lat.timer_stop()
+    if clk:
+        clk.__exit__(None, None, None)
     bg.astep = bg.a
     launches = lat.launches - launches0
-    assert taken == args.steps
+    assert taken == steps
     tmax = ms
     if dist:
         import torch
         t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         tmax = float(t.item())
-        dist.barrier()
-    value = ws * args.steps * N ** 3 / (tmax * 1e-3)
-
-    # dominant kernel, timed live with CUDA events around each launch
-    prof_steps = min(50, args.steps)
-    ms_red, ms_kick = lat.profile_leapfrog(af, prof_steps, bg)
+    out = {"ms": tmax, "launches": launches, "clocks": clk.summary() if clk else None, "shape": shape}
+    # per-kernel device time, CUDA events around each launch (same stream)
+    prof_steps = min(50, steps)
+    ms0, ms1 = lat.profile_leapfrog(af, prof_steps, bg)
     bg.astep = bg.a
-    kick_ms = ms_kick / prof_steps
-    red_ms = ms_red / prof_steps
-    achieved = BYTES_KICK_FP64 * N ** 3 / (kick_ms * 1e-3) / 1e9
+    out["kernel_ms"] = ms1 / prof_steps
+    out["aux_ms"] = ms0 / (prof_steps if form == iegpu.FORM_FP64 else 1)
+    if e2e_too:
+        # end to end through the C ABI: host buffers in, steps, host buffers out
+        f_host = lat.download(iegpu.F)
+        fd_host = lat.download(iegpu.FD)
+        pinned = "numpy"
+        try:
+            import torch
+            f_host = torch.from_numpy(f_host).pin_memory().numpy()
+            fd_host = torch.from_numpy(fd_host).pin_memory().numpy()
+            pinned = "pinned"
+        except Exception:
+            pass
+        t0 = time.perf_counter()
+        lat.upload(iegpu.F, f_host)
+        lat.upload(iegpu.FD, fd_host)
+        lat.leapfrog(af, steps, bg)
+        f_out = lat.download(iegpu.F)
+        fd_out = lat.download(iegpu.FD)
+        te2e = time.perf_counter() - t0
+        if dist:
+            import torch
+            t = torch.tensor([te2e], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te2e = float(t.item())
+        assert np.isfinite(f_out[:4]).all() and np.isfinite(fd_out[:4]).all()
+        out["e2e_s"] = te2e
+        out["pinned"] = pinned
+    lat.close()
+    return out
+
+
+def engine_arm(args):
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    import iegpu
+    N = args.n
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip()
+    smi_index = int(cvd) if cvd.isdigit() else local
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -227,61 +270,53 @@ def engine_arm(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    traffic = None
+    traffic_per_site = {}
     try:
-        tr = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
-        if "kick_fp64_bytes_per_site" in tr:
-            traffic = tr["kick_fp64_bytes_per_site"] * N ** 3
+        traffic_per_site = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
     except (OSError, ValueError):
         pass
 
-    # end to end through the C ABI: host buffers in, steps, host buffers out
-    f_host = lat.download(iegpu.F)
-    fd_host = lat.download(iegpu.FD)
-    pinned = "numpy"
-    try:
-        import torch
-        tf = torch.from_numpy(f_host).pin_memory()
-        tfd = torch.from_numpy(fd_host).pin_memory()
-        f_host, fd_host = tf.numpy(), tfd.numpy()
-        pinned = "pinned"
-    except Exception:
-        pass
-    e2e_steps = args.steps
-    t0 = time.perf_counter()
-    lat.upload(iegpu.F, f_host)
-    lat.upload(iegpu.FD, fd_host)
-    lat.leapfrog(af, e2e_steps, bg)
-    f_out = lat.download(iegpu.F)
-    fd_out = lat.download(iegpu.FD)
-    te2e = time.perf_counter() - t0
-    if dist:
-        import torch
-        t = torch.tensor([te2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te2e = float(t.item())
-    assert np.isfinite(f_out[:4]).all() and np.isfinite(fd_out[:4]).all()
-    bytes_state = 2 * 8 * N ** 3
-    e2e = {"value": ws * e2e_steps * N ** 3 / te2e, "unit": UNIT, "h2d_bytes_per_step": bytes_state / e2e_steps,
-           "d2h_bytes_per_step": bytes_state / e2e_steps,
-           "note": f"iegpu_upload(f, fd) + iegpu_leapfrog({e2e_steps} steps) + iegpu_download(f, fd), "
-                   f"{pinned} host buffers, wall clock"}
+    # headline: the split form (FP32 perturbations, FP64 background)
+    sp = measure_form(iegpu, iegpu.FORM_SPLIT, N, args.steps, args.warmup, smi_index, True, dist)
+    value = ws * args.steps * N ** 3 / (sp["ms"] * 1e-3)
+    # the plain FP64 form on the same workload (fewer steps: it is ~15x slower)
+    fp_steps = max(3, min(args.steps, 300))
+    fp = measure_form(iegpu, iegpu.FORM_FP64, N, fp_steps, args.warmup, None, False, dist)
+    fp_value = ws * fp_steps * N ** 3 / (fp["ms"] * 1e-3)
     if rank != 0:
         return 0
+
+    achieved = BYTES_STEP_SPLIT * N ** 3 / (sp["kernel_ms"] * 1e-3) / 1e9
+    fp_achieved = BYTES_KICK_FP64 * N ** 3 / (fp["kernel_ms"] * 1e-3) / 1e9
+    tr = traffic_per_site.get("split_step_bytes_per_site")
+    bytes_state = 2 * 8 * N ** 3
+    e2e = {"value": ws * args.steps * N ** 3 / sp["e2e_s"], "unit": UNIT,
+           "h2d_bytes_per_step": bytes_state / args.steps, "d2h_bytes_per_step": bytes_state / args.steps,
+           "note": f"iegpu_upload(f, fd as FP64) + iegpu_leapfrog({args.steps} steps) + iegpu_download(f, fd), "
+                   f"{sp['pinned']} host buffers, wall clock"}
     cpu = cpu_baseline(N, os.cpu_count() or 1) if ws == 1 else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"hilltop leapfrog, N={N}^3, plain FP64 form (params.analytic.txt, ns=0.965, "
-                                   f"seed 8, device Bunch-Davies initial conditions)",
-                       "N": N, "form": "fp64", "l2": "state 384 MB > L2 129 MB: no flush needed",
+            "warmup": args.warmup, "ms_per_step": sp["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"hilltop leapfrog, N={N}^3, split form: FP32 dphi/dpi about an FP64 background "
+                                   f"(params.analytic.txt, ns=0.965, seed 8, device Bunch-Davies initial conditions)",
+                       "N": N, "form": "split", "l2": "state > L2 (129 MB) each step: no flush needed",
+                       "autotuned_shape": sp["shape"],
                        "parallelism": f"replicas x{ws}"},
-            "forms": {"fp64": {"value": value, "ms_per_step": tmax / args.steps}},
+            "forms": {"split": {"value": value, "ms_per_step": sp["ms"] / args.steps, "steps": args.steps},
+                      "fp64": {"value": fp_value, "ms_per_step": fp["ms"] / fp_steps, "steps": fp_steps,
+                               "kernel": "k_kick (FP64 kick + drift)", "kernel_ms": fp["kernel_ms"],
+                               "reduce_kernel_ms": fp["aux_ms"], "achieved_gbs": fp_achieved,
+                               "frac_of_measured_hbm": fp_achieved / peak,
+                               "note": "per-site arithmetic in the reference's order (-fmad=false); FP64 ALU bound"},
+                      "split_over_fp64": value / fp_value},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_kick (FP64 kick + drift)",
-                         "algorithmic_bytes_per_site": BYTES_KICK_FP64, "kernel_ms": kick_ms,
-                         "reduce_kernel_ms": red_ms, "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)"},
-            "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e}
+                         "frac": achieved / peak, "traffic": None if tr is None else tr * N ** 3,
+                         "kernel": "k_split_rows (fused kick + drift + next-step Friedmann sums)",
+                         "algorithmic_bytes_per_site": BYTES_STEP_SPLIT, "kernel_ms": sp["kernel_ms"],
+                         "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)"},
+            "gpu_launches": sp["launches"], "clocks": sp["clocks"], "e2e": e2e}
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -291,8 +326,8 @@ def engine_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=15000)
+    ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     args = ap.parse_args()

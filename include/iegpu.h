@@ -142,9 +142,17 @@ int  iegpu_energies(struct iegpu_ctx* ctx, const iegpu_bg* bg, double out[3]);
 int  iegpu_timer_start(struct iegpu_ctx* ctx);
 int  iegpu_timer_stop(struct iegpu_ctx* ctx, float* ms);
 /* Like iegpu_leapfrog, but each kernel is launched on its own with a pair of
- * CUDA events around it; ms_out[0] accumulates the reduction kernel's device
- * time, ms_out[1] the kick/drift kernel's.  For profiling only. */
+ * CUDA events around it.  FP64 form: ms_out[0] accumulates the reduction
+ * kernel's device time, ms_out[1] the kick/drift kernel's.  Split form:
+ * ms_out[0] is the priming reduction, ms_out[1] the fused step kernels'
+ * total.  For profiling only. */
 int  iegpu_profile_leapfrog(struct iegpu_ctx* ctx, double af, int nsteps, iegpu_bg* bg, double* ms_out, int nk);
+
+/* Split form: run the launch-shape autotuner now (it otherwise runs on the
+ * first iegpu_leapfrog call) and report the chosen shape of the step kernel:
+ * rows per tile, planes prefetched, plane chunks.  The lattice state is left
+ * unchanged. */
+int  iegpu_autotune(struct iegpu_ctx* ctx, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */
 /* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */

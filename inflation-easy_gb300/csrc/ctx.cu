@@ -512,17 +512,22 @@ int iegpu_profile_leapfrog(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, do
     if (!c || !bg || !ms_out || nsteps < 0) return IEGPU_EINVAL;
     if (int rc = need_table(c)) return rc;
     if (is_split(c)) {
-        // one fused kernel per step: time the graph-free launch of each step
-        for (int q = 0; q < nk; ++q) ms_out[q] = 0.0;
-        float ms = 0.f;
-        if (int rc = iegpu_timer_start(c)) return rc;
-        int taken = 0;
-        if (int rc = split_leapfrog(c, af, nsteps, bg, &taken, nullptr)) return rc;
-        if (int rc = iegpu_timer_stop(c, &ms)) return rc;
-        if (nk > 1) ms_out[1] = ms;
-        return IEGPU_OK;
+        if (int rc = split_running(c)) return rc;
+        return split_profile(c, af, nsteps, bg, ms_out, nk);
     }
     return fp64_profile(c, af, nsteps, bg, ms_out, nk);
+}
+
+int iegpu_autotune(iegpu_ctx* c, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (is_split(c) && !c->split_mat) {
+        if (int rc = need_table(c)) return rc;
+        if (int rc = split_autotune(c, bg)) return rc;
+    }
+    if (rows) *rows = c->row_cfg.TJ;
+    if (prefetch) *prefetch = c->row_cfg.PF;
+    if (chunks) *chunks = c->row_cfg.chunks;
+    return IEGPU_OK;
 }
 
 int iegpu_means(iegpu_ctx* c, double out[3]) {

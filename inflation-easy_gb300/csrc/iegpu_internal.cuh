@@ -92,6 +92,13 @@ struct SplitCtl {
     double sums[3];
 };
 
+// Launch shape of the split row kernel (chosen by the autotuner).
+struct RowCfg {
+    int TJ = 0;       // rows per tile (0: untuned default)
+    int PF = 2;       // planes prefetched
+    int chunks = 1;   // plane ranges along i
+};
+
 struct SigwSplit {
     const float* hs[6];
     float* hdst[6];
@@ -164,6 +171,8 @@ struct iegpu_ctx {
     cudaGraphExec_t sp_exec[2] = {nullptr, nullptr};
     int sp_steps = 0;
     int split_mat = 0;                    // FP64 buffers hold the field (deltaN stage)
+    iegpu::RowCfg row_cfg;                // split row-kernel launch shape
+    int tuned = 0;
     int part_cap = 0;
 
     // timing events
@@ -225,6 +234,8 @@ int get_phiref(iegpu_ctx* c, double* out);
 // split_fp32.cu
 int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace);
 int split_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg);
+int split_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk);
+int split_autotune(iegpu_ctx* c, const iegpu_bg* bg);
 int split_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
 int split_sums(iegpu_ctx* c, double out[6]);
 int split_materialize(iegpu_ctx* c, int which, double* out);

@@ -448,18 +448,17 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
 // handles k = l + 32c, c < C = N/32.  The planes come in through a cp.async
 // ring kRowPrefetch planes ahead.  Row partial sums are added per plane into
 // Kahan-compensated per-thread accumulators.
-constexpr int kRowPrefetch = 2;
-constexpr int kRowPhiSlots = 3 + kRowPrefetch;
-constexpr int kRowPiSlots = 1 + kRowPrefetch;
-
-__host__ __device__ inline int split_row_smem_floats(int TJ, int N) {
-    return kRowPhiSlots * (TJ + 3) * N + kRowPiSlots * (TJ + 1) * N + (TJ + 1) * N + 2 * (3 * kWin + 1);
+__host__ __device__ inline int split_row_smem_floats(int TJ, int N, int PF) {
+    return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + (TJ + 1) * N + 2 * (3 * kWin + 1);
 }
 
-template <bool TABLE, int C, int TJ>
+// PF = planes prefetched ahead; the i range [0, N) is cut into `chunks`
+// nearly equal plane ranges (any count, so the grid can match the SMs).
+template <bool TABLE, int C, int TJ, int PF>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                               double* part, unsigned* counter, double* a_trace,
-                                                              int CH) {
+                                                              int chunks) {
+    constexpr int kRowPrefetch = PF, kRowPhiSlots = 3 + PF, kRowPiSlots = 1 + PF;
     constexpr int N = 32 * C, m = N - 1;
     constexpr int lgN = (C == 1) ? 5 : (C == 2) ? 6 : (C == 4) ? 7 : (C == 8) ? 8 : 9;
     constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
@@ -489,7 +488,9 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
     __syncthreads();
     if (!active_s) return;
     const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
-    const int j0 = blockIdx.x * TJ, i0 = blockIdx.y * CH;
+    const int j0 = blockIdx.x * TJ;
+    const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
+    const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
 
     auto issue_phi = [&](int i) {
         float* dst = ring + ((i - i0 + 1) % kRowPhiSlots) * RP;
@@ -597,6 +598,215 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
     }
     double v[3] = {g.value(), s1.value(), s2.value()};
     finish_sums(v, ctl, P, K, part, counter, a_trace);
+}
+
+// Vector variant of the row kernel for N >= 128: lane l owns the four
+// consecutive sites k = 4(l + 32v) .. +3, v < C4 = N/128, so plane rows move
+// with 128-bit shared and global accesses and the k +- 1 neighbours across
+// lanes come by warp shuffles.  The new planes are double-buffered, which
+// leaves one barrier per plane: iteration p finishes the differences of plane
+// p-1 and computes plane p.
+__host__ __device__ inline int split_row4_smem_floats(int TJ, int N, int PF) {
+    return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + 2 * (TJ + 1) * N + 2 * (3 * kWin + 1);
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+template <bool TABLE>
+__device__ __forceinline__ float split_dv(float x, const float* wk, int nk, float pn, float kv, bool& bad) {
+    if (TABLE) {
+        const int q = window_find(wk, nk, x);
+        if (q < 0) { bad = true; return 0.f; }
+        return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
+    }
+    return kv * x;
+}
+
+template <bool TABLE>
+__device__ __forceinline__ float split_v(float x, const float* wv, int nv, bool& bad) {
+    if (TABLE) {
+        const int q = window_find(wv, nv, x);
+        if (q < 0) { bad = true; return 0.f; }
+        return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
+    }
+    return x * x;
+}
+
+template <bool TABLE, int C4, int TJ, int PF>
+__global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
+                                                               double* part, unsigned* counter, double* a_trace,
+                                                               int chunks) {
+    constexpr int N = 128 * C4, m = N - 1;
+    constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
+    constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
+    constexpr int PHS = 3 + PF, PIS = 1 + PF;
+    extern __shared__ __align__(16) float smem[];
+    float* ring = smem;
+    float* pis = ring + PHS * RP;
+    float* nb = pis + PIS * PP;
+    float* wk = nb + 2 * NBP;
+    float* wv = wk + 3 * kWin + 1;
+    __shared__ int nk_s, nv_s, active_s;
+    __shared__ float cf[6];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        const SplitCtl& Cc = *ctl;
+        active_s = Cc.active;
+        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
+        nk_s = Cc.wk.n;
+        nv_s = Cc.wv.n;
+    }
+    if (TABLE) {
+        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q < kWin; q += NTH) {
+            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
+            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+        }
+    }
+    __syncthreads();
+    if (!active_s) return;
+    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const int nk = nk_s, nv = nv_s;
+    const int j0 = blockIdx.x * TJ;
+    const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
+    const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
+
+    auto issue_phi = [&](int i) {
+        float* dst = ring + ((i - i0 + 1) % PHS) * RP;
+        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 3) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
+        }
+    };
+    auto issue_pi = [&](int i) {
+        float* dst = pis + ((i - i0) % PIS) * PP;
+        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 1) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
+        }
+    };
+
+    Kahan g, s1, s2;
+    bool bad = false;
+    const int jl = w;
+    const bool interior = jl < TJ;
+    float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
+    issue_phi(i0 - 1);
+    issue_phi(i0);
+    cp_commit();
+    for (int q = 0; q < PF; ++q) {
+        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+        if (q <= CH) issue_pi(i0 + q);
+        cp_commit();
+    }
+    // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
+    auto diffs = [&](int p, bool kj) {
+        const float* nr = nb + ((p - 1) & 1) * NBP;
+        float rg = 0.f;
+#pragma unroll
+        for (int v = 0; v < C4; ++v) {
+            const int k = 4 * (lane + 32 * v);
+            const float4 xc = xp1[v];
+            if (kj) {
+                // x(k+4): lane+1's first element, or the next vector's lane 0 (periodic)
+                const float nxt_same = __shfl_down_sync(0xffffffffu, xc.x, 1);
+                const float nxt_wrap = __shfl_sync(0xffffffffu, xp1[(v + 1) % C4].x, 0);
+                const float x4 = lane == 31 ? nxt_wrap : nxt_same;
+                const float4 up = ld4(nr + (jl + 1) * N + k);
+                const float a0 = xc.y - xc.x, a1 = xc.z - xc.y, a2 = xc.w - xc.z, a3 = x4 - xc.w;
+                const float b0 = up.x - xc.x, b1 = up.y - xc.y, b2 = up.z - xc.z, b3 = up.w - xc.w;
+                rg += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + b0 * b0 + b1 * b1 + b2 * b2 + b3 * b3;
+            }
+            if (p >= 2) {
+                const float4 xo = xp2[v];
+                const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+                rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+            }
+        }
+        g.add(rg);
+    };
+    for (int p = 0; p <= CH; ++p) {
+        const int i = i0 + p;
+        cp_wait<PF - 1>();
+        __syncthreads();
+        // planes PF ahead go into the slots of planes no longer read
+        if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
+        if (p + PF <= CH) issue_pi(i + PF);
+        cp_commit();
+        if (interior && p >= 1) diffs(p, true);
+        const float* pc = ring + ((p + 1) % PHS) * RP + (jl + 1) * N;
+        const float* pu = ring + ((p + 2) % PHS) * RP + (jl + 1) * N;
+        const float* pl = ring + (p % PHS) * RP + (jl + 1) * N;
+        const float* pp = pis + (p % PIS) * PP + jl * N;
+        float* nw = nb + (p & 1) * NBP + jl * N;
+        const bool store = interior && p < CH;
+        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
+        float4 xs[C4];
+#pragma unroll
+        for (int v = 0; v < C4; ++v) xs[v] = ld4(pc + 4 * (lane + 32 * v));
+        float rs1 = 0.f, rs2 = 0.f;
+#pragma unroll
+        for (int v = 0; v < C4; ++v) {
+            const int k = 4 * (lane + 32 * v);
+            const float4 x = xs[v];
+            // k-1 and k+4 with periodic wrap across vectors and the row
+            const float lft_same = __shfl_up_sync(0xffffffffu, x.w, 1);
+            const float lft_wrap = __shfl_sync(0xffffffffu, xs[(v + C4 - 1) % C4].w, 31);
+            const float rgt_same = __shfl_down_sync(0xffffffffu, x.x, 1);
+            const float rgt_wrap = __shfl_sync(0xffffffffu, xs[(v + 1) % C4].x, 0);
+            const float xl = lane == 0 ? lft_wrap : lft_same;
+            const float xr = lane == 31 ? rgt_wrap : rgt_same;
+            const float4 up = ld4(pc + k + N), dn = ld4(pc + k - N), iu = ld4(pu + k), il = ld4(pl + k);
+            const float4 pi = ld4(pp + k);
+            float4 lap;
+            lap.x = (x.y + xl) + (up.x + dn.x) + (iu.x + il.x) - 6.f * x.x;
+            lap.y = (x.z + x.x) + (up.y + dn.y) + (iu.y + il.y) - 6.f * x.y;
+            lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
+            lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
+            float4 pin, xn;
+            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, pn, kv, bad));
+            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, pn, kv, bad));
+            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, pn, kv, bad));
+            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, pn, kv, bad));
+            xn.x = x.x + d * pin.x;
+            xn.y = x.y + d * pin.y;
+            xn.z = x.z + d * pin.z;
+            xn.w = x.w + d * pin.w;
+            st4(nw + k, xn);
+            if (store) {
+                st4(B.xd + gb + k, xn);
+                st4(B.pd + gb + k, pin);
+                rs1 += (xn.x + xn.y) + (xn.z + xn.w);
+                rs2 += (split_v<TABLE>(xn.x, wv, nv, bad) + split_v<TABLE>(xn.y, wv, nv, bad)) +
+                       (split_v<TABLE>(xn.z, wv, nv, bad) + split_v<TABLE>(xn.w, wv, nv, bad));
+            }
+            xp2[v] = xp1[v];
+            xp1[v] = xn;
+        }
+        if (store) { s1.add(rs1); s2.add(rs2); }
+    }
+    // the last pair (CH-1, CH) along i
+    if (interior) {
+        float rg = 0.f;
+#pragma unroll
+        for (int v = 0; v < C4; ++v) {
+            const float4 xc = xp1[v], xo = xp2[v];
+            const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+            rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+        }
+        g.add(rg);
+    }
+    cp_wait<0>();
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v3[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums(v3, ctl, P, K, part, counter, a_trace);
 }
 
 // SIGW in the split form: h kick and drift for the coming step, before the
@@ -756,10 +966,40 @@ static SplitConst split_const(const iegpu_ctx* c) {
 }
 
 struct StepGeom {
-    int TK, TJ, CH, tiles, chunks;
+    int TK, TJ, CH, tiles, chunks, PF = 0;
     size_t smem;
     bool rows;   // full-row kernel (32 <= N <= 512)
 };
+
+// Shared memory one row-kernel CTA needs, and how many fit on an SM.
+static size_t row_smem_bytes(int N, int TJ, int PF) {
+    return sizeof(float) * (size_t)(N >= 128 ? split_row4_smem_floats(TJ, N, PF) : split_row_smem_floats(TJ, N, PF));
+}
+
+static int row_ctas_per_sm(int N, int TJ, int PF) {
+    const size_t smem = row_smem_bytes(N, TJ, PF) + 1024;
+    const size_t per_sm = 228 * 1024;
+    int by_smem = (int)(per_sm / smem);
+    const int by_regs = 65536 / ((TJ + 1) * 32 * 72);
+    int n = by_smem < by_regs ? by_smem : by_regs;
+    return n < 1 ? (smem <= 227 * 1024 ? 1 : 0) : n;
+}
+
+// Untuned choice: 8-row tiles (4 at N = 512), two planes prefetched, and a
+// chunk count that makes the grid one wave of resident CTAs.
+static RowCfg default_row_cfg(const iegpu_ctx* c) {
+    RowCfg r;
+    const int N = c->N;
+    r.TJ = N >= 512 ? 4 : 8;
+    r.PF = 2;
+    const int per_sm = row_ctas_per_sm(N, r.TJ, r.PF);
+    const int tiles = N / r.TJ;
+    int chunks = (c->sms * (per_sm > 0 ? per_sm : 1)) / tiles;
+    if (chunks < 1) chunks = 1;
+    if (chunks > N / 8) chunks = N / 8 > 0 ? N / 8 : 1;
+    r.chunks = chunks;
+    return r;
+}
 
 static StepGeom step_geom(const iegpu_ctx* c) {
     StepGeom g;
@@ -767,14 +1007,14 @@ static StepGeom step_geom(const iegpu_ctx* c) {
     if (N >= 32 && N <= 512) {
         g.rows = true;
         g.TK = N;
-        g.TJ = N == 512 ? 4 : 8;
+        RowCfg rc = c->row_cfg;
+        if (rc.TJ == 0) rc = default_row_cfg(c);
+        g.TJ = rc.TJ;
+        g.PF = rc.PF;
         g.tiles = N / g.TJ;
-        // about two resident CTAs per SM, at least 8 planes per chunk
-        int chunks = 1;
-        while (chunks * 2 <= N / 8 && g.tiles * chunks * 2 <= c->sms * 2) chunks *= 2;
-        g.chunks = chunks;
-        g.CH = N / chunks;
-        g.smem = sizeof(float) * (size_t)split_row_smem_floats(g.TJ, N);
+        g.chunks = rc.chunks;
+        g.CH = N / rc.chunks;
+        g.smem = row_smem_bytes(N, g.TJ, g.PF);
         return g;
     }
     g.rows = false;
@@ -812,6 +1052,57 @@ static SigwSplit sigw_split(iegpu_ctx* c, int src) {
     return S;
 }
 
+template <bool TAB, int CC, int TJV, int PFV>
+static void rows_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    static size_t attr = 0;
+    if (attr < g.smem) {
+        cudaFuncSetAttribute(k_split_rows<TAB, CC, TJV, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        attr = g.smem;
+    }
+    k_split_rows<TAB, CC, TJV, PFV><<<grid, (TJV + 1) * 32, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part,
+                                                                                  c->counter, c->a_trace, g.chunks);
+}
+
+template <bool TAB, int C4, int TJV, int PFV>
+static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    static size_t attr = 0;
+    if (attr < g.smem) {
+        cudaFuncSetAttribute(k_split_rows4<TAB, C4, TJV, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        attr = g.smem;
+    }
+    k_split_rows4<TAB, C4, TJV, PFV><<<grid, (TJV + 1) * 32, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part,
+                                                                                   c->counter, c->a_trace, g.chunks);
+}
+
+template <bool TAB, int C4>
+static void rows4_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (g.TJ == 4) { if (g.PF == 1) rows4_one<TAB, C4, 4, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 4, 2>(c, B, K, grid, g); }
+    else { if (g.PF == 1) rows4_one<TAB, C4, 8, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 8, 2>(c, B, K, grid, g); }
+}
+
+template <bool TAB, int CC>
+static void rows_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (g.TJ == 4) { if (g.PF == 1) rows_one<TAB, CC, 4, 1>(c, B, K, grid, g); else rows_one<TAB, CC, 4, 2>(c, B, K, grid, g); }
+    else { if (g.PF == 1) rows_one<TAB, CC, 8, 1>(c, B, K, grid, g); else rows_one<TAB, CC, 8, 2>(c, B, K, grid, g); }
+}
+
+template <bool TAB>
+static void rows_c(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    switch (c->N) {
+        case 32: rows_tj<TAB, 1>(c, B, K, grid, g); break;
+        case 64: rows_tj<TAB, 2>(c, B, K, grid, g); break;
+        case 128: rows4_tj<TAB, 1>(c, B, K, grid, g); break;
+        case 256: rows4_tj<TAB, 2>(c, B, K, grid, g); break;
+        default: rows4_tj<TAB, 4>(c, B, K, grid, g); break;
+    }
+}
+
+static void launch_rows(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (c->pot.table) rows_c<true>(c, B, K, grid, g);
+    else rows_c<false>(c, B, K, grid, g);
+    c->launches++;
+}
+
 static void launch_step(iegpu_ctx* c, int src) {
     const SplitConst K = split_const(c);
     if (c->cfg.sigw) {
@@ -824,27 +1115,7 @@ static void launch_step(iegpu_ctx* c, int src) {
     SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
     dim3 grid(g.tiles, g.chunks);
     if (g.rows) {
-        const bool tab = c->pot.table != 0;
-#define IEGPU_ROWS(TAB, CC, TJV)                                                                                 \
-    do {                                                                                                      \
-        static bool attr = false;                                                                             \
-        if (!attr) {                                                                                          \
-            cudaFuncSetAttribute(k_split_rows<TAB, CC, TJV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
-                                 (int)g.smem);                                                                \
-            attr = true;                                                                                      \
-        }                                                                                                     \
-        k_split_rows<TAB, CC, TJV><<<grid, (TJV + 1) * 32, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part, \
-                                                                             c->counter, c->a_trace, g.CH);     \
-    } while (0)
-        switch (c->N) {
-            case 32: if (tab) IEGPU_ROWS(true, 1, 8); else IEGPU_ROWS(false, 1, 8); break;
-            case 64: if (tab) IEGPU_ROWS(true, 2, 8); else IEGPU_ROWS(false, 2, 8); break;
-            case 128: if (tab) IEGPU_ROWS(true, 4, 8); else IEGPU_ROWS(false, 4, 8); break;
-            case 256: if (tab) IEGPU_ROWS(true, 8, 8); else IEGPU_ROWS(false, 8, 8); break;
-            default: if (tab) IEGPU_ROWS(true, 16, 4); else IEGPU_ROWS(false, 16, 4); break;
-        }
-#undef IEGPU_ROWS
-        c->launches++;
+        launch_rows(c, B, K, grid, g);
         return;
     }
 #define IEGPU_SPLIT_LAUNCH(TAB, TKV)                                                                          \
@@ -925,9 +1196,74 @@ static void sctl_bg(const iegpu_ctx* c, iegpu_bg* bg) {
     bg->astep = B.astep;
 }
 
+int split_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk);
+
+// Autotuner of the row kernel's launch shape: rows per tile (TJ), planes
+// prefetched (PF) and plane chunks (grid height).  Each candidate runs one
+// warm-up and three timed steps (CUDA events, stream-ordered) from a saved copy
+// of the live state, which is restored afterwards; the fastest shape is kept
+// for the life of the context.
+int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
+    const int N = c->N;
+    c->tuned = 1;
+    if (N < 32 || N > 512) return IEGPU_OK;
+    std::vector<RowCfg> cands;
+    for (int TJ : {4, 8}) {
+        if (TJ > N) continue;
+        for (int PF : {1, 2}) {
+            const int per_sm = row_ctas_per_sm(N, TJ, PF);
+            if (per_sm < 1) continue;
+            const int tiles = N / TJ;
+            for (int waves : {1, 2}) {
+                int ch = (waves * c->sms * per_sm) / tiles;
+                if (ch < 1) ch = 1;
+                if (ch > N / 8) ch = N / 8 > 0 ? N / 8 : 1;
+                RowCfg r;
+                r.TJ = TJ;
+                r.PF = PF;
+                r.chunks = ch;
+                bool dup = false;
+                for (const RowCfg& q : cands) dup |= (q.TJ == r.TJ && q.PF == r.PF && q.chunks == r.chunks);
+                if (!dup) cands.push_back(r);
+            }
+        }
+    }
+    // save the live state into the idle FP64 buffer
+    float* save = reinterpret_cast<float*>(c->f[c->cur ^ 1]);
+    const int cur0 = c->cur;
+    const SplitCtl ctl0 = *c->sctl_h;
+    if (check_cuda(c, cudaMemcpyAsync(save, c->sp[cur0], sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune save") ||
+        check_cuda(c, cudaMemcpyAsync(save + c->gs, c->spi[cur0], sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune save"))
+        return IEGPU_ECUDA;
+    double best = 1e300;
+    RowCfg pick = default_row_cfg(c);
+    for (const RowCfg& r : cands) {
+        c->row_cfg = r;
+        iegpu_bg b = *bg0;
+        double ms[2] = {0.0, 0.0};
+        int rc = split_profile(c, 1e300, 4, &b, ms, 2);
+        // restore
+        c->cur = cur0;
+        *c->sctl_h = ctl0;
+        if (check_cuda(c, cudaMemcpyAsync(c->sp[cur0], save, sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune restore") ||
+            check_cuda(c, cudaMemcpyAsync(c->spi[cur0], save + c->gs, sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune restore"))
+            return IEGPU_ECUDA;
+        if (rc) return rc;
+        if (ms[1] < best) { best = ms[1]; pick = r; }
+    }
+    c->row_cfg = pick;
+    if (sctl_up(c)) return IEGPU_ECUDA;
+    split_destroy_graphs(c);
+    return sync_and_check(c, "autotune");
+}
+
 // The host mirror of the split control holds phibar/pibar between calls; it
 // is refreshed from the device after every call that changes them.
 int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace) {
+    if (!c->tuned && max_steps > 0) {
+        int rc = split_autotune(c, bg);
+        if (rc) return rc;
+    }
     if (steps) *steps = 0;
     if (max_steps <= 0) return max_steps < 0 ? set_error(c, IEGPU_EINVAL, "max_steps must be >= 0") : IEGPU_OK;
     if (max_steps > c->a_trace_cap) {
@@ -965,6 +1301,47 @@ int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* st
     if (a_trace && taken > 0 &&
         check_cuda(c, cudaMemcpy(a_trace, c->a_trace, sizeof(double) * taken, cudaMemcpyDeviceToHost), "a_trace"))
         return IEGPU_ECUDA;
+    return IEGPU_OK;
+}
+
+// As split_leapfrog, launching each step kernel on its own between two CUDA
+// events: ms[0] = the priming reduction, ms[1] = the step kernels' total.
+int split_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk) {
+    for (int q = 0; q < nk; ++q) ms[q] = 0.0;
+    if (nsteps > c->a_trace_cap) {
+        if (c->a_trace) cudaFree(c->a_trace);
+        c->a_trace = nullptr;
+        c->a_trace_cap = 0;
+        const int cap = nsteps < 1024 ? 1024 : nsteps;
+        if (check_cuda(c, cudaMalloc(&c->a_trace, sizeof(double) * (size_t)cap), "a_trace alloc")) return IEGPU_ENOMEM;
+        c->a_trace_cap = cap;
+        split_destroy_graphs(c);
+        fp64_destroy_graphs(c);
+    }
+    sctl_fill(c, bg, kModeLeapfrog);
+    c->sctl_h->af = af;
+    c->sctl_h->steps_limit = nsteps;
+    if (sctl_up(c)) return IEGPU_ECUDA;
+    const int start = c->cur;
+    float t = 0.f;
+    cudaEventRecord(c->ev[1], c->stream);
+    launch_prime(c, start);
+    cudaEventRecord(c->ev[2], c->stream);
+    if (check_cuda(c, cudaEventSynchronize(c->ev[2]), "profile")) return IEGPU_ECUDA;
+    cudaEventElapsedTime(&t, c->ev[1], c->ev[2]);
+    if (nk > 0) ms[0] += t;
+    for (int s = 0; s < nsteps; ++s) {
+        cudaEventRecord(c->ev[1], c->stream);
+        launch_step(c, (start + s) & 1);
+        cudaEventRecord(c->ev[2], c->stream);
+        if (check_cuda(c, cudaEventSynchronize(c->ev[2]), "profile")) return IEGPU_ECUDA;
+        cudaEventElapsedTime(&t, c->ev[1], c->ev[2]);
+        if (nk > 1) ms[1] += t;
+    }
+    int rc = sctl_down(c);
+    c->cur = (start + c->sctl_h->steps_done) & 1;
+    if (rc) return rc;
+    sctl_bg(c, bg);
     return IEGPU_OK;
 }
 

@@ -80,6 +80,7 @@ def load() -> C.CDLL:
         "iegpu_energies": (I, [P, C.POINTER(Bg), dp]),
         "iegpu_means": (I, [P, dp]),
         "iegpu_bunch_davies": (I, [P, I, D, D, D, D, dp]),
+        "iegpu_autotune": (I, [P, C.POINTER(Bg), ip, ip, ip]),
         "iegpu_timer_start": (I, [P]),
         "iegpu_timer_stop": (I, [P, C.POINTER(C.c_float)]),
         "iegpu_profile_leapfrog": (I, [P, D, I, C.POINTER(Bg), dp, I]),
@@ -210,6 +211,11 @@ class Lattice:
         return tuple(out)
 
     # -- measurement ------------------------------------------------------
+    def autotune(self, bg: Bg):
+        r, p, ch = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.iegpu_autotune(self.h, C.byref(bg), C.byref(r), C.byref(p), C.byref(ch)))
+        return {"rows": r.value, "prefetch": p.value, "chunks": ch.value}
+
     def timer_start(self) -> None:
         self._check(self.lib.iegpu_timer_start(self.h))
 

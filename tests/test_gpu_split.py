@@ -101,3 +101,17 @@ def test_split_deltaN_stage(engine, oracle_mod, tables):
         o.deltaN_steps(200)
         dn = lat.download(engine.DELTAN)
         assert np.max(np.abs(dn - o.deltaN)) <= 3 * p.dN
+
+
+def test_split_autotune_keeps_state(engine, oracle_mod):
+    p, o = oracle_state(oracle_mod, 64, False, False, None, steps=5)
+    lat, bg = split_like(engine, p, o, False, False, None)
+    with lat:
+        before = lat.download(engine.F)
+        shape = lat.autotune(bg)
+        assert shape["rows"] in (4, 8) and shape["prefetch"] in (1, 2) and shape["chunks"] >= 1
+        assert np.array_equal(lat.download(engine.F), before)
+        taken = lat.leapfrog(p.af, 50, bg)
+        o.leapfrog_steps(50)
+        assert taken == 50
+        assert pert_err(lat.download(engine.F), o.f) < 1e-4
