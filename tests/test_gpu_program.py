@@ -95,12 +95,17 @@ def test_program_matches_reference_fixtures(case, tmp_path):
     # fields: the per-site arithmetic is the reference's, but the lattice sums
     # that feed the Friedmann update are re-associated, so the two runs drift
     # apart by a few units in the last place of the background value
-    for key, base in (("f", "f"), ("fd", "fd")):
-        ref = ref_state[key]
-        d = np.abs(got[key] - ref)
-        ulps = np.max(d / np.spacing(np.abs(ref)))
-        print(f"{case} {key}: max dev {np.max(d):.3e} = {ulps:.0f} ulp, std {np.std(ref):.3e}")
-        assert ulps < 4096, key
+    ref = ref_state["f"]
+    d = np.abs(got["f"] - ref)
+    ulps = np.max(d / np.spacing(np.abs(ref)))
+    print(f"{case} f: max dev {np.max(d):.3e} = {ulps:.0f} ulp of f, std {np.std(ref):.3e}")
+    assert ulps < 4096
+    # fd ends the deltaN stage in e-fold units, near zero at many sites, so it
+    # is compared against its own spread
+    ref = ref_state["fd"]
+    d = np.abs(got["fd"] - ref)
+    print(f"{case} fd: max dev {np.max(d):.3e}, std {np.std(ref):.3e}")
+    assert np.max(d) <= 1e-3 * np.std(ref)
     ref = ref_state["deltaN"]
     zeta = ref - ref.mean()
     d = np.abs(got["deltaN"] - ref)
