@@ -41,6 +41,7 @@ typedef struct iegpu_ctx iegpu_ctx;
 #define IEGPU_ETABLE        7  /* repeated table nodes, src/potential.cpp:62-65 */
 #define IEGPU_EUNSUPPORTED  8  /* feature not available in this form */
 #define IEGPU_ETIMEOUT      9  /* a bounded device wait gave up */
+#define IEGPU_ETOOBIG      10  /* size above a fixed, documented limit */
 
 /* ---- configuration --------------------------------------------------- */
 #define IEGPU_POT_HILLTOP   0  /* analytic hilltop, src/potential.cpp:77-83 */
@@ -176,6 +177,28 @@ int  iegpu_spectrum(struct iegpu_ctx* ctx, int field, int* counts, double* f2, i
  * per mode in float as the reference, binning (bins < floor(0.8*numbins)),
  * inverse FFT.  f2 accumulates the per-mode float values in double. */
 int  iegpu_gw_spectrum(struct iegpu_ctx* ctx, int which, double to_phys, int* counts, double* f2, int nbins);
+
+/* Allocation-free variant of the shell binning inside iegpu_spectrum, for
+ * callers that cannot allocate device memory: a plugin whose host framework
+ * owns all device memory through its own caching allocator and forbids
+ * direct cudaMalloc, or a process whose fixed memory budget is already spent
+ * on the lattice, and which has no iegpu context (creating one allocates).
+ * It has no counterpart in the reference.
+ * modes: the r2c field after the forward FFT (N^3 doubles, the layout
+ * iegpu_fft produces); nyquist: its N x 2N Nyquist plane; counts[nbins] and
+ * f2[nbins] (nbins = iegpu_numbins(N)) receive the same values as
+ * iegpu_spectrum's.  All five pointers are device memory; the work is
+ * enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the
+ * call returns without synchronising.
+ * Nothing is allocated: the partial sums live in one fixed 681,984-byte
+ * array inside the library, which every GPU that loads it holds until exit.
+ * Limit: N <= 512 (larger N returns IEGPU_ETOOBIG).  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress), so
+ * make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (on different streams, or from different threads)
+ * race; order them on one stream. */
+int  iegpu_shell_spectrum_noalloc(const double* modes, const double* nyquist, int N, int* counts,
+                                  double* f2, void* stream);
 
 /* ---- deltaN (src/evolution.cpp:1004-1375) ----------------------------- */
 /* initializeN(), src/initialize.cpp:219-232: fd <- fd*a^(s-1)/sqrt(V/3), deltaN = 0. */

@@ -136,6 +136,7 @@ const char* iegpu_strerror(int code) {
         case IEGPU_ETABLE: return "invalid potential table";
         case IEGPU_EUNSUPPORTED: return "unsupported in this form";
         case IEGPU_ETIMEOUT: return "device wait timed out";
+        case IEGPU_ETOOBIG: return "size above the fixed limit of this entry point";
         default: return "unknown error";
     }
 }

@@ -17,6 +17,7 @@
 // shared-memory histogram.  Warps, then CTAs, are combined in index order.
 // Compiled with -fmad=false.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "iegpu_internal.cuh"
@@ -316,4 +317,72 @@ int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int
     return finish_bins(c, nbins, counts, f2);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free shell binning
+// ---------------------------------------------------------------------------
+//
+// For callers that cannot allocate device memory, themselves or through
+// this library: a plugin whose host framework owns all device memory through
+// its own caching allocator and forbids direct cudaMalloc, or a process whose
+// fixed memory budget is already spent on the lattice.  The per-CTA partial
+// sums live in one fixed file-scope array instead of context scratch.  The array is sized for N <= kNoAllocMaxN and a grid of
+// kNoAllocBlocks CTAs: kNoAllocBlocks * kNoAllocMaxBins * (8 + 4) bytes
+// = 681,984 bytes, held by every GPU that loads the library until exit.
+
+constexpr int kNoAllocBlocks = 128;
+constexpr int kNoAllocMaxN = 512;
+constexpr int kNoAllocMaxBins = (int)(1.73205 * (kNoAllocMaxN / 2)) + 1;
+constexpr size_t kNoAllocF2Bytes = sizeof(double) * kNoAllocBlocks * kNoAllocMaxBins;
+constexpr size_t kNoAllocBytes = kNoAllocF2Bytes + sizeof(int) * kNoAllocBlocks * kNoAllocMaxBins;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the symbol is only a stand-in, so the address is fetched once per device
+// with that device current and cached.
+static int noalloc_scratch(unsigned char** out) {
+    static std::mutex mu;
+    static unsigned char* addr[128] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) {
+        cudaGetLastError();
+        return IEGPU_ECUDA;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return IEGPU_ECUDA;
+        }
+        addr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = addr[dev];
+    return IEGPU_OK;
+}
+
 }  // namespace iegpu
+
+extern "C" int iegpu_shell_spectrum_noalloc(const double* modes, const double* nyquist, int N, int* counts,
+                                            double* f2, void* stream) {
+    using namespace iegpu;
+    if (!modes || !nyquist || !counts || !f2) return IEGPU_EINVAL;
+    if (N < 8 || (N & (N - 1))) return IEGPU_EINVAL;
+    if (N > kNoAllocMaxN) return IEGPU_ETOOBIG;
+    unsigned char* scratch = nullptr;
+    if (int rc = noalloc_scratch(&scratch)) return rc;
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    const int nbins = iegpu_numbins(N);
+    double* part = reinterpret_cast<double*>(scratch);
+    int* cpart = reinterpret_cast<int*>(scratch + kNoAllocF2Bytes);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // every launch rewrites all nbins partials of each of its CTAs, so the
+    // contents left by an earlier call are never read
+    const size_t smem = (size_t)kSpecWarps * nbins * (sizeof(double) + sizeof(int));
+    k_bin_scalar<<<kNoAllocBlocks, kSpecThreads, smem, st>>>(reinterpret_cast<const double2*>(modes),
+                                                             reinterpret_cast<const double2*>(nyquist), lg, nbins,
+                                                             part, cpart);
+    k_bin_combine<<<(nbins + 127) / 128, 128, 0, st>>>(part, cpart, kNoAllocBlocks, nbins, f2, counts);
+    return cudaGetLastError() == cudaSuccess ? IEGPU_OK : IEGPU_ECUDA;
+}

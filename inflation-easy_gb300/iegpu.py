@@ -15,7 +15,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "libiegpu.so"
 
-OK, EINVAL, ECUDA, ERANGE, ENAN, ECOURANT, ENOMEM, ETABLE, EUNSUPPORTED, ETIMEOUT = range(10)
+OK, EINVAL, ECUDA, ERANGE, ENAN, ECOURANT, ENOMEM, ETABLE, EUNSUPPORTED, ETIMEOUT, ETOOBIG = range(11)
 POT_HILLTOP, POT_TABLE = 0, 1
 FORM_FP64, FORM_SPLIT = 0, 1
 CRIT_GENERIC, CRIT_MONOTONIC, CRIT_ANTIMONOTONIC = 0, 1, -1
@@ -98,6 +98,7 @@ def load() -> C.CDLL:
         "iegpu_shift": (I, [P, I, D]),
         "iegpu_zero_above": (I, [P, I, D]),
         "iegpu_sum": (I, [P, I, dp]),
+        "iegpu_shell_spectrum_noalloc": (I, [P, P, I, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
