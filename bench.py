@@ -313,7 +313,7 @@ def engine_arm(args):
                       "split_over_fp64": value / fp_value},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None if tr is None else tr * N ** 3,
-                         "kernel": "k_split_rows (fused kick + drift + next-step Friedmann sums)",
+                         "kernel": "k_split_rows4 (fused kick + drift + next-step Friedmann sums, N >= 128; k_split_rows below)",
                          "algorithmic_bytes_per_site": BYTES_STEP_SPLIT, "kernel_ms": sp["kernel_ms"],
                          "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)"},
             "gpu_launches": sp["launches"], "clocks": sp["clocks"], "e2e": e2e}

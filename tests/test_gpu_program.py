@@ -111,15 +111,25 @@ def test_program_matches_reference_fixtures(case, tmp_path):
     d = np.abs(got["deltaN"] - ref)
     print(f"{case} deltaN: max dev {np.max(d):.3e}, std(zeta) {np.std(zeta):.3e}")
     assert np.max(d) / np.std(zeta) < 1e-3
-    # background scalars at every save, full precision
+    # background scalars at every save, full precision: t, a, ad, astep (and
+    # t, a, Ne, phiref at saveN) relative 1e-10.  ad2 is the Friedmann
+    # solution -2ad - 2a/(d(s+1)) (1 - sqrt(1 + x)) with x = O(d): two
+    # cancellations, each losing about log10(1/d) digits, turn the ulp-level
+    # differences of its inputs into ~1e-9 relative, so it gets 1e-6.
     ta = [l.split() for l in (src / "trace.txt").read_text().splitlines()]
     tb = [l.split() for l in (wd / "dump" / "trace.txt").read_text().splitlines()]
     assert len(ta) == len(tb)
+    worst_ad2 = 0.0
     for x, y in zip(ta, tb):
         assert x[0] == y[0]
-        for u, v in zip(x[2:] if x[0] == "save" else x[1:], y[2:] if y[0] == "save" else y[1:]):
+        for col, (u, v) in enumerate(zip(x[2:] if x[0] == "save" else x[1:], y[2:] if y[0] == "save" else y[1:])):
             u, v = float(u), float(v)
-            assert abs(u - v) <= 1e-10 * abs(u) + 1e-300, (x, y)
+            if x[0] == "save" and col == 3:
+                worst_ad2 = max(worst_ad2, abs(u - v) / max(abs(u), 1e-300))
+                assert abs(u - v) <= 1e-6 * abs(u) + 1e-300, (x, y)
+            else:
+                assert abs(u - v) <= 1e-10 * abs(u) + 1e-300, (x, y)
+    print(f"{case} ad2: max rel dev {worst_ad2:.3e}")
 
 
 def _precise(path):
