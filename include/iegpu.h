@@ -21,8 +21,8 @@
  *    re-entrant.  Calls are stream-ordered and synchronise before returning
  *    results to the host.
  */
-#ifndef IEGPU_H
-#define IEGPU_H
+#ifndef IEGPU_ABI_H
+#define IEGPU_ABI_H
 
 #ifdef __cplusplus
 extern "C" {
@@ -154,6 +154,9 @@ int  iegpu_profile_leapfrog(struct iegpu_ctx* ctx, double af, int nsteps, iegpu_
  * rows per tile, planes prefetched, plane chunks.  The lattice state is left
  * unchanged. */
 int  iegpu_autotune(struct iegpu_ctx* ctx, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
+/* Split form, 32 <= N <= 512: fix the step kernel's launch shape instead of
+ * tuning it (rows 4 or 8, prefetch 1 or 2, 1 <= chunks <= N/8). */
+int  iegpu_set_shape(struct iegpu_ctx* ctx, int rows, int prefetch, int chunks);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */
 /* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */
@@ -222,6 +225,65 @@ int  iegpu_shift(struct iegpu_ctx* ctx, int field, double value);
 int  iegpu_zero_above(struct iegpu_ctx* ctx, int field, double threshold);
 /* Sum of a field over the lattice (build_deltaN_linear mean, src/output.cpp:156-164). */
 int  iegpu_sum(struct iegpu_ctx* ctx, int field, double* sum);
+
+/* ---- ensembles ---------------------------------------------------------
+ * The reference evolves one lattice per process; these entry points evolve
+ * many independent lattices (seeds, sizes) in one set of device buffers, in
+ * the split form: per leapfrog step one kernel launch for all the lattices of
+ * one size, the sizes side by side as parallel branches of a CUDA graph of
+ * 16 steps.  Every lattice b follows the
+ * reference's program with its own a(t), H and stop condition a > af[b]:
+ * initial conditions (src/initialize.cpp:93-214), the leapfrog loop
+ * (src/evolution.cpp:934-945), the deltaN stage (src/evolution.cpp:1291-1375)
+ * and saveN's zeta (src/output.cpp:1522-1560).  Arrays of `count` entries
+ * are indexed by lattice.  N in {32, 64, 128, 256}. */
+typedef struct iegpu_ens iegpu_ens;
+/* cfg: everything but N is shared; form must be IEGPU_FORM_SPLIT, sigw 0. */
+int  iegpu_ens_create(const iegpu_config* cfg, const int* Ns, int count, struct iegpu_ens** out);
+int  iegpu_ens_destroy(struct iegpu_ens* ens);
+const char* iegpu_ens_last_error(const struct iegpu_ens* ens);
+long long iegpu_ens_launch_count(const struct iegpu_ens* ens);
+void* iegpu_ens_stream(struct iegpu_ens* ens);
+int  iegpu_ens_set_table(struct iegpu_ens* ens, const double* phi, const double* V, const double* dV, int n);
+/* iegpu_bunch_davies for every lattice with seeds[b]: lattice b gets the same
+ * fields as a single lattice of its size and seed; hubble_init[count]. */
+int  iegpu_ens_bunch_davies(struct iegpu_ens* ens, const int* seeds, double phi0, double dphi0,
+                            double high_cutoff_index, double low_cutoff_index, double* hubble_init);
+/* evolve_fields(d[b]) of every lattice (src/evolution.cpp:260-284). */
+int  iegpu_ens_evolve_fields(struct iegpu_ens* ens, const double* d, iegpu_bg* bg);
+/* iegpu_leapfrog for every lattice at once: lattice b stops after max_steps
+ * or once a > af[b]; steps[count] (may be NULL) receives the steps taken.  As
+ * there, the final "astep = a" is left to the caller. */
+int  iegpu_ens_leapfrog(struct iegpu_ens* ens, const double* af, int max_steps, iegpu_bg* bg, int* steps);
+/* nsteps steps launched one by one between CUDA events: *ms_prime = the
+ * priming reduction, *ms_steps = the step kernels' total device time. */
+int  iegpu_ens_profile(struct iegpu_ens* ens, int nsteps, iegpu_bg* bg, double* ms_prime, double* ms_steps);
+/* Times candidate launch shapes of every lattice size on the live state
+ * (restored afterwards) and keeps the fastest; rows, prefetch and chunks
+ * (arrays of count, may be NULL) receive each lattice's shape. */
+int  iegpu_ens_autotune(struct iegpu_ens* ens, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
+/* Sets the launch shape of the lattices of size N, as iegpu_set_shape. */
+int  iegpu_ens_set_shape(struct iegpu_ens* ens, int N, int rows, int prefetch, int chunks);
+int  iegpu_ens_timer_start(struct iegpu_ens* ens);
+int  iegpu_ens_timer_stop(struct iegpu_ens* ens, float* ms);
+/* N_b^3 doubles of lattice b: IEGPU_F / IEGPU_FD (phibar + dphi, pibar + dpi,
+ * or the FP64 fields once the deltaN stage has begun), IEGPU_DELTAN. */
+int  iegpu_ens_download(struct iegpu_ens* ens, int lattice, int field, double* host);
+/* The deltaN stage of every lattice, run_deltaN_loop (src/evolution.cpp:1291-1375)
+ * with the leapfrog integrator, then saveN's Nmean and deltaN -= Nmean
+ * (src/output.cpp:1522-1542): afterwards IEGPU_DELTAN holds zeta.
+ * phiref[count] and nmean[count] may be NULL.  A site stops being integrated
+ * once it has reached the end surface, so fd there is not advanced further. */
+int  iegpu_ens_deltaN(struct iegpu_ens* ens, iegpu_bg* bg, double dN, double Nend, int use_phiref_manual,
+                      double phiref_manual, double* phiref, float* nmean);
+/* spectraN of every lattice (src/output.cpp:1140-1170): counts/f2 hold
+ * lattice b's iegpu_numbins(N_b) bins after those of lattices 0 .. b-1. */
+int  iegpu_ens_zeta_spectra(struct iegpu_ens* ens, int* counts, double* f2);
+/* Pooled one-point histogram of zeta over the lattices of size N (0: all):
+ * nbins bins over [-nsigma*sigma, +nsigma*sigma], sigma the pooled standard
+ * deviation; outside[0], outside[1]: values below and above the range. */
+int  iegpu_ens_zeta_histogram(struct iegpu_ens* ens, int N, int nbins, double nsigma, double* sigma, double* lo,
+                              double* width, long long* counts, long long* outside);
 
 #ifdef __cplusplus
 }

@@ -37,6 +37,8 @@ UNITS = {
     "reduce_ops.cu": ["-fmad=false"],
     "ic.cu": ["-fmad=false"],
     "split_fp32.cu": [],
+    "ensemble.cu": [],
+    "ensemble_dn.cu": ["-fmad=false"],
 }
 
 

@@ -531,6 +531,12 @@ int iegpu_autotune(iegpu_ctx* c, const iegpu_bg* bg, int* rows, int* prefetch, i
     return IEGPU_OK;
 }
 
+int iegpu_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
+    if (!c) return IEGPU_EINVAL;
+    if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "the launch shape belongs to the split form");
+    return split_set_shape(c, rows, prefetch, chunks);
+}
+
 int iegpu_means(iegpu_ctx* c, double out[3]) {
     if (!c || !out) return IEGPU_EINVAL;
     if (is_split(c) && !c->split_mat) {

@@ -92,6 +92,12 @@ struct SplitCtl {
     double sums[3];
 };
 
+// Per-lattice constants of the split step: base step, rescaling exponent,
+// lattice spacing, number of sites.
+struct SplitConst {
+    double dt, s, dx, gs;
+};
+
 // Launch shape of the split row kernel (chosen by the autotuner).
 struct RowCfg {
     int TJ = 0;       // rows per tile (0: untuned default)
@@ -236,6 +242,7 @@ int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* st
 int split_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg);
 int split_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk);
 int split_autotune(iegpu_ctx* c, const iegpu_bg* bg);
+int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks);
 int split_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
 int split_sums(iegpu_ctx* c, double out[6]);
 int split_materialize(iegpu_ctx* c, int which, double* out);

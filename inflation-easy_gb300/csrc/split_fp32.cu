@@ -28,257 +28,21 @@
 #include <cstdio>
 #include <vector>
 
-#include "iegpu_internal.cuh"
-#include "pot.cuh"
-#include "reduce.cuh"
+#include "split_kernels.cuh"
 
 namespace iegpu {
-
-// ---------------------------------------------------------------------------
-// windows of table brackets around a background value
-// ---------------------------------------------------------------------------
-
-// Window around phibar: brackets l0 .. l0+n-1; u[q] = x[l0-1+q] - phibar.
-__device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, const double* y, const double* dy, double phibar,
-                             int* err) {
-    W.ok = 0;
-    if (!P.table) return;
-    bool oor;
-    const int lb = table_bracket(P, phibar, &oor);
-    if (oor) { *err = 1; return; }
-    int l0 = lb - kWin / 2;
-    if (l0 < 1) l0 = 1;
-    int n = kWin;
-    if (l0 + n - 1 > P.n - 1) n = P.n - 1 - l0 + 1;
-    W.l0 = l0;
-    W.n = n;
-    // value of the tabulated function at phibar (its own bracket)
-    const double Fbar = y[lb] + (phibar - P.x[lb]) * (dy[lb] / P.dxl[lb]);
-    for (int q = 0; q <= n; ++q) W.u[q] = (float)(P.x[l0 - 1 + q] - phibar);
-    for (int q = 0; q < n; ++q) {
-        const int l = l0 + q;
-        const double s = dy[l] / P.dxl[l];
-        W.s[q] = (float)s;
-        W.A[q] = (float)((y[l] + (phibar - P.x[l]) * s) - Fbar);
-    }
-    W.ok = 1;
-}
-
-// Bracket q of the window with u[q+1] < v <= u[q]; -1 outside the window.
-__device__ __forceinline__ int window_find(const float* u, int n, float v) {
-    if (!(v <= u[0] && v > u[n])) return -1;
-    int lo = 0, hi = n;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (u[mid] >= v) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// ---------------------------------------------------------------------------
-// scalar update (one thread): Friedmann, background, coefficients, windows
-// ---------------------------------------------------------------------------
-
-struct SplitConst {
-    double dt, s, dx, gs;
-};
-
-// V(phibar)/B^2 and V'(phibar)/B^2 (src/potential.cpp:77-98)
-__device__ void bar_potential(const PotDev& P, double phibar, double* V, double* dV) {
-    if (P.table) {
-        bool oor;
-        const int l = table_bracket(P, phibar, &oor);
-        *V = table_interp(P, P.V, P.dyV, phibar, l) / P.B2;
-        *dV = table_interp(P, P.dV, P.dydV, phibar, l) / P.B2;
-    } else {
-        *V = (P.V0 * (1.0 - P.c1 * (phibar * phibar))) / P.B2;
-        *dV = (P.c2 * phibar) / P.B2;
-    }
-}
-
-// sums: [0] sum of squared forward differences of dphi, [1] sum dphi,
-// [2] hilltop: sum dphi^2 / table: sum of V differences (table units)
-__device__ __noinline__ void split_scalars(SplitCtl& C, const PotDev& P, const SplitConst& K, const double* sums, double* a_trace) {
-    double d;
-    if (C.mode == kModeLeapfrog) {
-        if (C.steps_done >= C.steps_limit) { C.active = 0; C.done = 1; return; }
-        if (C.steps_done > 0) C.bg.astep = C.bg.a;
-        if (!(C.bg.a <= C.af)) { C.active = 0; C.done = 1; return; }
-        d = K.dt * pow_exp(C.bg.astep, K.s - 1.0);
-    } else {
-        d = C.d_given;
-    }
-    const double a = C.bg.a, s = K.s;
-    double ad = C.bg.ad;
-    const double grad = 0.5 * sums[0] * ((1.0 / (a * K.dx)) * (1.0 / (a * K.dx))) / K.gs;
-    double Vbar, dVbar;
-    bar_potential(P, C.phibar, &Vbar, &dVbar);
-    double pot;
-    if (P.table) pot = Vbar + (sums[2] / P.B2) / K.gs;
-    else pot = Vbar - (P.V0 * P.c1 / P.B2) * (2.0 * C.phibar * sums[1] + sums[2]) / K.gs;
-    const double sfev1 = s + 1.0, sfev2 = -2.0 * s + 2.0;
-    const double ad2 = (-2.0 * ad - 2.0 * a / d / sfev1 *
-                        (1.0 - sqrt(1.0 + 2.0 * d * sfev1 * ad / a +
-                                    (d * d) * sfev1 * pow_exp(a, sfev2) * (2.0 * grad / 3.0 + pot)))) / d;
-    ad += 0.5 * d * ad2;
-    const double laplnorm = pow_exp(a, -2.0 * s) / (K.dx * K.dx);
-    const double friction = (2.0 + s) * ad / a;
-    const double potnorm = pow_exp(a, 2.0 - 2.0 * s);
-    const double srcAmp = 2.0 * pow_exp(a, -2.0 * s);
-    ad += 0.5 * d * ad2;
-    // background kick (homogeneous mode of the lattice kick)
-    C.pibar = C.pibar + d * (-friction * C.pibar - potnorm * dVbar);
-    int err = 0;
-    build_window(C.wk, P, P.dV, P.dydV, C.phibar, &err);
-    C.d = (float)d;
-    C.lapl = (float)laplnorm;
-    C.fric = (float)friction;
-    C.pn = (float)(potnorm / P.B2);
-    C.kv = (float)(potnorm * P.c2 / P.B2);
-    C.srcAmp = (float)srcAmp;
-    C.dd = d;
-    C.bg.ad = ad;
-    C.bg.ad2 = ad2;
-    C.active = 1;
-    if (C.mode == kModeLeapfrog) {
-        C.phibar = C.phibar + d * C.pibar;
-        C.bg.t += d;
-        C.bg.a = a + d * ad;
-        if (a_trace) a_trace[C.steps_done] = C.bg.a;
-        C.steps_done += 1;
-    }
-    build_window(C.wv, P, P.V, P.dyV, C.phibar, &err);
-    if (err && !C.error) { C.error = IEGPU_ERANGE; C.errval = C.phibar; C.active = 0; C.done = 1; }
-}
-
-// ---------------------------------------------------------------------------
-// Kahan accumulator
-// ---------------------------------------------------------------------------
-
-struct Kahan {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float v) {
-        const float y = v - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
-__device__ __forceinline__ void finish_sums(double (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
-                                            double* part, unsigned* counter, double* a_trace) {
-    block_sum<3>(v);
-    if (threadIdx.x == 0) {
-        part[3 * (blockIdx.x + gridDim.x * blockIdx.y)] = v[0];
-        part[3 * (blockIdx.x + gridDim.x * blockIdx.y) + 1] = v[1];
-        part[3 * (blockIdx.x + gridDim.x * blockIdx.y) + 2] = v[2];
-    }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1);
-    __syncthreads();
-    if (!last) return;
-    if (threadIdx.x < 32) {
-        double tot[3];
-        sum_partials<3>(part, gridDim.x * gridDim.y, tot);
-        if (threadIdx.x == 0) {
-            *counter = 0;
-            SplitCtl& C = *ctl;
-            C.sums[0] = tot[0];
-            C.sums[1] = tot[1];
-            C.sums[2] = tot[2];
-            if (C.error) { C.active = 0; C.done = 1; }
-            else split_scalars(C, P, K, tot, a_trace);
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
 
-// Sums of the current dphi (start of a leapfrog call): thread per site.
+// The sums of the current dphi at the start of a leapfrog call, all CTAs of one lattice.
 template <bool TABLE>
 __global__ void __launch_bounds__(kThreads) k_split_prime(const float* __restrict__ x, SplitCtl* ctl, PotDev P,
                                                           SplitConst K, double* part, unsigned* counter,
                                                           double* a_trace, int lg) {
-    __shared__ float su[kWin + 1], sA[kWin], ss[kWin];
-    __shared__ int sn;
-    if (threadIdx.x == 0) sn = 0;
-    if (TABLE) {
-        // every CTA forms the window around the current phibar itself
-        if (threadIdx.x == 0) {
-            SplitWin W;
-            int err = 0;
-            build_window(W, P, P.V, P.dyV, ctl->phibar, &err);
-            sn = err ? -1 : W.n;
-            for (int q = 0; q <= W.n && !err; ++q) su[q] = W.u[q];
-            for (int q = 0; q < W.n && !err; ++q) { sA[q] = W.A[q]; ss[q] = W.s[q]; }
-        }
-    }
-    __syncthreads();
-    const long long gs = 1LL << (3 * lg);
-    const int m = (1 << lg) - 1;
-    Kahan g, s1, s2;
-    bool bad = TABLE && sn < 0;
-    for (long long id = (long long)(blockIdx.x + gridDim.x * blockIdx.y) * kThreads + threadIdx.x; id < gs;
-         id += (long long)gridDim.x * gridDim.y * kThreads) {
-        const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
-        const float xc = x[id];
-        const float xk = x[id - k + ((k + 1) & m)];
-        const float xj = x[id + ((long long)(((j + 1) & m) - j) << lg)];
-        const float xi = x[id + ((long long)(((i + 1) & m) - i) << (2 * lg))];
-        const float dk = xk - xc, dj = xj - xc, di = xi - xc;
-        g.add(dk * dk + dj * dj + di * di);
-        s1.add(xc);
-        if (TABLE) {
-            const int q = bad ? -1 : window_find(su, sn, xc);
-            if (q < 0) bad = true;
-            else s2.add(sA[q] + ss[q] * xc);
-        } else {
-            s2.add(xc * xc);
-        }
-    }
-    if (bad) {
-        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
-    }
-    double v[3] = {g.value(), s1.value(), s2.value()};
-    finish_sums(v, ctl, P, K, part, counter, a_trace);
-}
-
-struct SplitBufs {
-    const float* xs;   // dphi (step n)
-    float* xd;         // dphi (step n+1)
-    const float* ps;   // dpi  (n-1/2)
-    float* pd;         // dpi  (n+1/2)
-};
-
-// Asynchronous global -> shared copies (cp.async), so the planes a CTA will
-// need next are in flight while it works on the current one.
-__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int n>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory"); }
-
-constexpr int kPrefetch = 3;   // planes in flight ahead of the one being computed
-constexpr int kPhiSlots = 6;   // three stencil planes + kPrefetch
-constexpr int kPiSlots = 4;    // one plane in use + kPrefetch
-constexpr int kColOff = 4;     // shared-memory column of k = 0 (16-byte aligned rows)
-
-// Shared-memory floats of the step kernel for tile TJ x TK.
-__host__ __device__ inline int split_step_smem_floats(int TJ, int TK) {
-    const int RS = TK + 8;
-    return kPhiSlots * (TJ + 3) * RS + kPiSlots * (TJ + 1) * RS + 2 * (TJ + 1) * (TK + 1) + 2 * (3 * kWin + 1);
+    prime_body<TABLE>(x, ctl, P, K, part, counter, a_trace, lg, blockIdx.x + gridDim.x * blockIdx.y,
+                      gridDim.x * gridDim.y, nullptr);
 }
 
 // The fused step.  Block (tile, chunk); TK = tile width along k (warp lanes).
@@ -320,6 +84,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
     __syncthreads();
     if (!active_s) return;
     const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const WinCache ck = win_cache<TABLE>(wk, nk_s), cv = win_cache<TABLE>(wv, nv_s);
     const int ntj = N / TJ;
     const int tj = blockIdx.x % ntj, tk = blockIdx.x / ntj;
     const int j0 = tj * TJ, k0 = tk * TK, i0 = blockIdx.y * CH;
@@ -388,14 +153,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
             const float x = pc[o];
             const float lap = pc[o + 1] + pc[o - 1] + pc[o + RS] + pc[o - RS] + pu[o] + pl[o] - 6.f * x;
             const float pi0 = pp[jl * RS + kl + kColOff];
-            float dv;
-            if (TABLE) {
-                const int q = window_find(wk, nk_s, x);
-                if (q < 0) { bad = true; dv = 0.f; }
-                else dv = pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
-            } else {
-                dv = kv * x;
-            }
+            const float dv = split_dv<TABLE>(x, wk, nk_s, ck, pn, kv, bad);
             const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
             const float xn = x + d * pin;
             nc[jl * NS + kl] = xn;
@@ -404,13 +162,8 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
                 B.xd[gi] = xn;
                 B.pd[gi] = pin;
                 s1.add(xn);
-                if (TABLE) {
-                    const int q = window_find(wv, nv_s, xn);
-                    if (q < 0) bad = true;
-                    else s2.add(wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * xn);
-                } else {
-                    s2.add(xn * xn);
-                }
+                const float v2 = split_v<TABLE>(xn, wv, nv_s, cv, bad);
+                if (!TABLE || !bad) s2.add(v2);
             }
         }
         __syncthreads();
@@ -440,373 +193,37 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
     double v[3] = {g.value(), s1.value(), s2.value()};
     finish_sums(v, ctl, P, K, part, counter, a_trace);
 }
-
-// Full-row variant of the step for 32 <= N <= 512: a tile is TJ rows of
-// complete k lines, so the k direction is periodic inside shared memory and
-// needs no halo.  Warp w computes row j0+w for w = 0..TJ (row TJ is the +j
-// halo row whose new values only feed the j differences of row TJ-1); lane l
-// handles k = l + 32c, c < C = N/32.  The planes come in through a cp.async
-// ring kRowPrefetch planes ahead.  Row partial sums are added per plane into
-// Kahan-compensated per-thread accumulators.
-__host__ __device__ inline int split_row_smem_floats(int TJ, int N, int PF) {
-    return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + (TJ + 1) * N + 2 * (3 * kWin + 1);
-}
-
-// PF = planes prefetched ahead; the i range [0, N) is cut into `chunks`
-// nearly equal plane ranges (any count, so the grid can match the SMs).
 template <bool TABLE, int C, int TJ, int PF>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                               double* part, unsigned* counter, double* a_trace,
                                                               int chunks) {
-    constexpr int kRowPrefetch = PF, kRowPhiSlots = 3 + PF, kRowPiSlots = 1 + PF;
-    constexpr int N = 32 * C, m = N - 1;
-    constexpr int lgN = (C == 1) ? 5 : (C == 2) ? 6 : (C == 4) ? 7 : (C == 8) ? 8 : 9;
-    constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
-    extern __shared__ __align__(16) float smem[];
-    float* ring = smem;
-    float* pis = ring + kRowPhiSlots * RP;
-    float* nb = pis + kRowPiSlots * PP;
-    float* wk = nb + (TJ + 1) * N;
-    float* wv = wk + 3 * kWin + 1;
-    __shared__ int nk_s, nv_s, active_s;
-    __shared__ float cf[6];
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (tid == 0) {
-        const SplitCtl& Cc = *ctl;
-        active_s = Cc.active;
-        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
-        nk_s = Cc.wk.n;
-        nv_s = Cc.wv.n;
-    }
-    if (TABLE) {
-        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
-        for (int q = tid; q < kWin; q += NTH) {
-            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
-            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
-        }
-    }
-    __syncthreads();
-    if (!active_s) return;
-    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
-    const int j0 = blockIdx.x * TJ;
+    constexpr int N = 32 * C;
     const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
     const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
-
-    auto issue_phi = [&](int i) {
-        float* dst = ring + ((i - i0 + 1) % kRowPhiSlots) * RP;
-        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
-        constexpr int ops = (TJ + 3) * (N / 4);
-        for (int o = tid; o < ops; o += NTH) {
-            const int r = o / (N / 4), q = o - r * (N / 4);
-            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
-        }
-    };
-    auto issue_pi = [&](int i) {
-        float* dst = pis + ((i - i0) % kRowPiSlots) * PP;
-        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
-        constexpr int ops = (TJ + 1) * (N / 4);
-        for (int o = tid; o < ops; o += NTH) {
-            const int r = o / (N / 4), q = o - r * (N / 4);
-            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
-        }
-    };
-
-    Kahan g, s1, s2;
-    bool bad = false;
-    float xprev[C];
-    issue_phi(i0 - 1);
-    issue_phi(i0);
-    cp_commit();
-    for (int q = 0; q < kRowPrefetch; ++q) {
-        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
-        if (q <= CH) issue_pi(i0 + q);
-        cp_commit();
-    }
-    const int jl = w;              // row of this warp (TJ: halo row)
-    const bool interior = jl < TJ;
-    for (int p = 0; p <= CH; ++p) {
-        const int i = i0 + p;
-        cp_wait<kRowPrefetch - 1>();
-        __syncthreads();
-        const float* pc = ring + ((p + 1) % kRowPhiSlots) * RP + (jl + 1) * N;
-        const float* pu = ring + ((p + 2) % kRowPhiSlots) * RP + (jl + 1) * N;
-        const float* pl = ring + (p % kRowPhiSlots) * RP + (jl + 1) * N;
-        const float* pp = pis + (p % kRowPiSlots) * PP + jl * N;
-        float xnew[C];
-        float rs1 = 0.f, rs2 = 0.f;
-        const bool store = interior && p < CH;
-        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const int k = lane + 32 * c;
-            const float x = pc[k];
-            const float lap = pc[(k + 1) & m] + pc[(k - 1) & m] + pc[k + N] + pc[k - N] + pu[k] + pl[k] - 6.f * x;
-            const float pi0 = pp[k];
-            float dv;
-            if (TABLE) {
-                const int q = window_find(wk, nk_s, x);
-                if (q < 0) { bad = true; dv = 0.f; }
-                else dv = pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
-            } else {
-                dv = kv * x;
-            }
-            const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
-            const float xn = x + d * pin;
-            xnew[c] = xn;
-            nb[jl * N + k] = xn;
-            if (store) {
-                B.xd[gb + k] = xn;
-                B.pd[gb + k] = pin;
-                rs1 += xn;
-                if (TABLE) {
-                    const int q = window_find(wv, nv_s, xn);
-                    if (q < 0) bad = true;
-                    else rs2 += wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * xn;
-                } else {
-                    rs2 += xn * xn;
-                }
-            }
-        }
-        __syncthreads();
-        // planes kRowPrefetch ahead go into the slots no longer needed
-        if (p + kRowPrefetch + 1 <= CH + 1) issue_phi(i + 1 + kRowPrefetch);
-        if (p + kRowPrefetch <= CH) issue_pi(i + kRowPrefetch);
-        cp_commit();
-        if (interior) {
-            float rg = 0.f;
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                const int k = lane + 32 * c;
-                if (p < CH) {
-                    const float dk = nb[jl * N + ((k + 1) & m)] - xnew[c];
-                    const float dj = nb[(jl + 1) * N + k] - xnew[c];
-                    rg += dk * dk + dj * dj;
-                }
-                if (p >= 1) {
-                    const float di = xnew[c] - xprev[c];
-                    rg += di * di;
-                }
-                xprev[c] = xnew[c];
-            }
-            g.add(rg);
-            if (store) { s1.add(rs1); s2.add(rs2); }
-        }
-    }
-    cp_wait<0>();
-    if (bad) {
-        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
-    }
-    double v[3] = {g.value(), s1.value(), s2.value()};
-    finish_sums(v, ctl, P, K, part, counter, a_trace);
+    rows_body<TABLE, C, TJ, PF>(B, ctl, P, K, part, counter, a_trace, blockIdx.x * TJ, i0, CH,
+                                blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr);
 }
 
-// Vector variant of the row kernel for N >= 128: lane l owns the four
-// consecutive sites k = 4(l + 32v) .. +3, v < C4 = N/128, so plane rows move
-// with 128-bit shared and global accesses and the k +- 1 neighbours across
-// lanes come by warp shuffles.  The new planes are double-buffered, which
-// leaves one barrier per plane: iteration p finishes the differences of plane
-// p-1 and computes plane p.
-__host__ __device__ inline int split_row4_smem_floats(int TJ, int N, int PF) {
-    return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + 2 * (TJ + 1) * N + 2 * (3 * kWin + 1);
-}
-
-__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
-
-template <bool TABLE>
-__device__ __forceinline__ float split_dv(float x, const float* wk, int nk, float pn, float kv, bool& bad) {
-    if (TABLE) {
-        const int q = window_find(wk, nk, x);
-        if (q < 0) { bad = true; return 0.f; }
-        return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
-    }
-    return kv * x;
-}
-
-template <bool TABLE>
-__device__ __forceinline__ float split_v(float x, const float* wv, int nv, bool& bad) {
-    if (TABLE) {
-        const int q = window_find(wv, nv, x);
-        if (q < 0) { bad = true; return 0.f; }
-        return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
-    }
-    return x * x;
-}
 
 template <bool TABLE, int C4, int TJ, int PF>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                                double* part, unsigned* counter, double* a_trace,
                                                                int chunks) {
-    constexpr int N = 128 * C4, m = N - 1;
-    constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
-    constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
-    constexpr int PHS = 3 + PF, PIS = 1 + PF;
-    extern __shared__ __align__(16) float smem[];
-    float* ring = smem;
-    float* pis = ring + PHS * RP;
-    float* nb = pis + PIS * PP;
-    float* wk = nb + 2 * NBP;
-    float* wv = wk + 3 * kWin + 1;
-    __shared__ int nk_s, nv_s, active_s;
-    __shared__ float cf[6];
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (tid == 0) {
-        const SplitCtl& Cc = *ctl;
-        active_s = Cc.active;
-        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
-        nk_s = Cc.wk.n;
-        nv_s = Cc.wv.n;
-    }
-    if (TABLE) {
-        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
-        for (int q = tid; q < kWin; q += NTH) {
-            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
-            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
-        }
-    }
-    __syncthreads();
-    if (!active_s) return;
-    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
-    const int nk = nk_s, nv = nv_s;
-    const int j0 = blockIdx.x * TJ;
+    constexpr int N = 128 * C4;
     const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
     const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
+    rows4_body<TABLE, C4, TJ, PF>(B, ctl, P, K, part, counter, a_trace, blockIdx.x * TJ, i0, CH,
+                                  blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr);
+}
 
-    auto issue_phi = [&](int i) {
-        float* dst = ring + ((i - i0 + 1) % PHS) * RP;
-        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
-        constexpr int ops = (TJ + 3) * (N / 4);
-        for (int o = tid; o < ops; o += NTH) {
-            const int r = o / (N / 4), q = o - r * (N / 4);
-            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
-        }
-    };
-    auto issue_pi = [&](int i) {
-        float* dst = pis + ((i - i0) % PIS) * PP;
-        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
-        constexpr int ops = (TJ + 1) * (N / 4);
-        for (int o = tid; o < ops; o += NTH) {
-            const int r = o / (N / 4), q = o - r * (N / 4);
-            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
-        }
-    };
-
-    Kahan g, s1, s2;
-    bool bad = false;
-    const int jl = w;
-    const bool interior = jl < TJ;
-    float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
-    issue_phi(i0 - 1);
-    issue_phi(i0);
-    cp_commit();
-    for (int q = 0; q < PF; ++q) {
-        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
-        if (q <= CH) issue_pi(i0 + q);
-        cp_commit();
-    }
-    // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
-    auto diffs = [&](int p, bool kj) {
-        const float* nr = nb + ((p - 1) & 1) * NBP;
-        float rg = 0.f;
-#pragma unroll
-        for (int v = 0; v < C4; ++v) {
-            const int k = 4 * (lane + 32 * v);
-            const float4 xc = xp1[v];
-            if (kj) {
-                // x(k+4): lane+1's first element, or the next vector's lane 0 (periodic)
-                const float nxt_same = __shfl_down_sync(0xffffffffu, xc.x, 1);
-                const float nxt_wrap = __shfl_sync(0xffffffffu, xp1[(v + 1) % C4].x, 0);
-                const float x4 = lane == 31 ? nxt_wrap : nxt_same;
-                const float4 up = ld4(nr + (jl + 1) * N + k);
-                const float a0 = xc.y - xc.x, a1 = xc.z - xc.y, a2 = xc.w - xc.z, a3 = x4 - xc.w;
-                const float b0 = up.x - xc.x, b1 = up.y - xc.y, b2 = up.z - xc.z, b3 = up.w - xc.w;
-                rg += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + b0 * b0 + b1 * b1 + b2 * b2 + b3 * b3;
-            }
-            if (p >= 2) {
-                const float4 xo = xp2[v];
-                const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
-                rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
-            }
-        }
-        g.add(rg);
-    };
-    for (int p = 0; p <= CH; ++p) {
-        const int i = i0 + p;
-        cp_wait<PF - 1>();
-        __syncthreads();
-        // planes PF ahead go into the slots of planes no longer read
-        if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
-        if (p + PF <= CH) issue_pi(i + PF);
-        cp_commit();
-        if (interior && p >= 1) diffs(p, true);
-        const float* pc = ring + ((p + 1) % PHS) * RP + (jl + 1) * N;
-        const float* pu = ring + ((p + 2) % PHS) * RP + (jl + 1) * N;
-        const float* pl = ring + (p % PHS) * RP + (jl + 1) * N;
-        const float* pp = pis + (p % PIS) * PP + jl * N;
-        float* nw = nb + (p & 1) * NBP + jl * N;
-        const bool store = interior && p < CH;
-        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
-        float4 xs[C4];
-#pragma unroll
-        for (int v = 0; v < C4; ++v) xs[v] = ld4(pc + 4 * (lane + 32 * v));
-        float rs1 = 0.f, rs2 = 0.f;
-#pragma unroll
-        for (int v = 0; v < C4; ++v) {
-            const int k = 4 * (lane + 32 * v);
-            const float4 x = xs[v];
-            // k-1 and k+4 with periodic wrap across vectors and the row
-            const float lft_same = __shfl_up_sync(0xffffffffu, x.w, 1);
-            const float lft_wrap = __shfl_sync(0xffffffffu, xs[(v + C4 - 1) % C4].w, 31);
-            const float rgt_same = __shfl_down_sync(0xffffffffu, x.x, 1);
-            const float rgt_wrap = __shfl_sync(0xffffffffu, xs[(v + 1) % C4].x, 0);
-            const float xl = lane == 0 ? lft_wrap : lft_same;
-            const float xr = lane == 31 ? rgt_wrap : rgt_same;
-            const float4 up = ld4(pc + k + N), dn = ld4(pc + k - N), iu = ld4(pu + k), il = ld4(pl + k);
-            const float4 pi = ld4(pp + k);
-            float4 lap;
-            lap.x = (x.y + xl) + (up.x + dn.x) + (iu.x + il.x) - 6.f * x.x;
-            lap.y = (x.z + x.x) + (up.y + dn.y) + (iu.y + il.y) - 6.f * x.y;
-            lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
-            lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
-            float4 pin, xn;
-            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, pn, kv, bad));
-            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, pn, kv, bad));
-            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, pn, kv, bad));
-            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, pn, kv, bad));
-            xn.x = x.x + d * pin.x;
-            xn.y = x.y + d * pin.y;
-            xn.z = x.z + d * pin.z;
-            xn.w = x.w + d * pin.w;
-            st4(nw + k, xn);
-            if (store) {
-                st4(B.xd + gb + k, xn);
-                st4(B.pd + gb + k, pin);
-                rs1 += (xn.x + xn.y) + (xn.z + xn.w);
-                rs2 += (split_v<TABLE>(xn.x, wv, nv, bad) + split_v<TABLE>(xn.y, wv, nv, bad)) +
-                       (split_v<TABLE>(xn.z, wv, nv, bad) + split_v<TABLE>(xn.w, wv, nv, bad));
-            }
-            xp2[v] = xp1[v];
-            xp1[v] = xn;
-        }
-        if (store) { s1.add(rs1); s2.add(rs2); }
-    }
-    // the last pair (CH-1, CH) along i
-    if (interior) {
-        float rg = 0.f;
-#pragma unroll
-        for (int v = 0; v < C4; ++v) {
-            const float4 xc = xp1[v], xo = xp2[v];
-            const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
-            rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
-        }
-        g.add(rg);
-    }
-    cp_wait<0>();
-    if (bad) {
-        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
-    }
-    double v3[3] = {g.value(), s1.value(), s2.value()};
-    finish_sums(v3, ctl, P, K, part, counter, a_trace);
+// Whole planes (N = 32, 64): block y = chunk of planes.
+template <bool TABLE, int N, int NT, int PF>
+__global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_split_plane(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
+                                                    unsigned* counter, double* a_trace, int chunks) {
+    const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
+    const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
+    plane_body<TABLE, N, NT, PF>(B, ctl, P, K, part, counter, a_trace, i0, CH, blockIdx.x + gridDim.x * blockIdx.y,
+                                 gridDim.x * gridDim.y, nullptr);
 }
 
 // SIGW in the split form: h kick and drift for the coming step, before the
@@ -971,8 +388,13 @@ struct StepGeom {
     bool rows;   // full-row kernel (32 <= N <= 512)
 };
 
-// Shared memory one row-kernel CTA needs, and how many fit on an SM.
+// Shared memory one row-kernel CTA needs, and how many fit on an SM.  TJ = N
+// (N <= 64) selects the whole-plane kernel.
+static bool plane_shape(int N, int TJ) { return TJ == N && (N == 32 || N == 64); }
+static int plane_threads(int N) { return N == 32 ? 256 : 512; }
+
 static size_t row_smem_bytes(int N, int TJ, int PF) {
+    if (plane_shape(N, TJ)) return sizeof(float) * (size_t)split_plane_smem_floats(N, PF);
     return sizeof(float) * (size_t)(N >= 128 ? split_row4_smem_floats(TJ, N, PF) : split_row_smem_floats(TJ, N, PF));
 }
 
@@ -980,7 +402,8 @@ static int row_ctas_per_sm(int N, int TJ, int PF) {
     const size_t smem = row_smem_bytes(N, TJ, PF) + 1024;
     const size_t per_sm = 228 * 1024;
     int by_smem = (int)(per_sm / smem);
-    const int by_regs = 65536 / ((TJ + 1) * 32 * 72);
+    const int nthr = plane_shape(N, TJ) ? plane_threads(N) : (TJ + 1) * 32;
+    const int by_regs = 65536 / (nthr * 72);
     int n = by_smem < by_regs ? by_smem : by_regs;
     return n < 1 ? (smem <= 227 * 1024 ? 1 : 0) : n;
 }
@@ -1074,6 +497,24 @@ static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim
                                                                                    c->counter, c->a_trace, g.chunks);
 }
 
+template <bool TAB, int NV, int PFV>
+static void plane_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    constexpr int NT = NV == 32 ? 256 : 512;
+    static size_t attr = 0;
+    if (attr < g.smem) {
+        cudaFuncSetAttribute(k_split_plane<TAB, NV, NT, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        attr = g.smem;
+    }
+    k_split_plane<TAB, NV, NT, PFV><<<grid, NT, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part, c->counter,
+                                                                     c->a_trace, g.chunks);
+}
+
+template <bool TAB, int NV>
+static void plane_pf(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (g.PF == 4) plane_one<TAB, NV, 4>(c, B, K, grid, g);
+    else plane_one<TAB, NV, 2>(c, B, K, grid, g);
+}
+
 template <bool TAB, int C4>
 static void rows4_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
     if (g.TJ == 4) { if (g.PF == 1) rows4_one<TAB, C4, 4, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 4, 2>(c, B, K, grid, g); }
@@ -1089,8 +530,8 @@ static void rows_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 
 template <bool TAB>
 static void rows_c(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
     switch (c->N) {
-        case 32: rows_tj<TAB, 1>(c, B, K, grid, g); break;
-        case 64: rows_tj<TAB, 2>(c, B, K, grid, g); break;
+        case 32: if (g.TJ == 32) plane_pf<TAB, 32>(c, B, K, grid, g); else rows_tj<TAB, 1>(c, B, K, grid, g); break;
+        case 64: if (g.TJ == 64) plane_pf<TAB, 64>(c, B, K, grid, g); else rows_tj<TAB, 2>(c, B, K, grid, g); break;
         case 128: rows4_tj<TAB, 1>(c, B, K, grid, g); break;
         case 256: rows4_tj<TAB, 2>(c, B, K, grid, g); break;
         default: rows4_tj<TAB, 4>(c, B, K, grid, g); break;
@@ -1208,6 +649,18 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
     c->tuned = 1;
     if (N < 32 || N > 512) return IEGPU_OK;
     std::vector<RowCfg> cands;
+    if (N == 32 || N == 64) {
+        // whole planes: N/8 .. N/32 chunks of planes
+        for (int PF : {2, 4})
+            for (int ch = N / 8; ch >= 1 && ch >= N / 32; ch /= 2)
+                if (row_ctas_per_sm(N, N, PF) >= 1) {
+                    RowCfg r;
+                    r.TJ = N;
+                    r.PF = PF;
+                    r.chunks = ch;
+                    cands.push_back(r);
+                }
+    }
     for (int TJ : {4, 8}) {
         if (TJ > N) continue;
         for (int PF : {1, 2}) {
@@ -1255,6 +708,25 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
     if (sctl_up(c)) return IEGPU_ECUDA;
     split_destroy_graphs(c);
     return sync_and_check(c, "autotune");
+}
+
+int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
+    const int N = c->N;
+    if (N < 32 || N > 512) return set_error(c, IEGPU_EUNSUPPORTED, "the row kernel covers 32 <= N <= 512");
+    const bool plane = plane_shape(N, rows);
+    if ((!plane && ((rows != 4 && rows != 8) || (prefetch != 1 && prefetch != 2))) ||
+        (plane && prefetch != 2 && prefetch != 4) || chunks < 1 || chunks > N / 8)
+        return set_error(c, IEGPU_EINVAL,
+                         "shape: rows 4|8 with prefetch 1|2, or rows N (N <= 64, whole planes) with prefetch 2|4; "
+                         "1 <= chunks <= N/8");
+    if (3LL * (N / rows) * chunks > c->part_cap || row_ctas_per_sm(N, rows, prefetch) < 1)
+        return set_error(c, IEGPU_EINVAL, "shape does not fit this lattice's scratch");
+    c->row_cfg.TJ = rows;
+    c->row_cfg.PF = prefetch;
+    c->row_cfg.chunks = chunks;
+    c->tuned = 1;
+    split_destroy_graphs(c);
+    return IEGPU_OK;
 }
 
 // The host mirror of the split control holds phibar/pibar between calls; it

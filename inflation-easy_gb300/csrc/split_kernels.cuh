@@ -1,0 +1,907 @@
+// split_kernels.cuh -- device building blocks of the split-precision step,
+// shared by the one-lattice form and the ensemble form.
+//
+// The field is stored as phi = phibar(t) + dphi(x), phi' = pibar(t) + dpi(x)
+// (background in FP64, perturbations in FP32).  Everything here works on one
+// lattice: a step CTA owns a tile of rows and a chunk of planes, writes its
+// block sums to a partial slot, and the last CTA of the lattice to arrive
+// runs the FP64 Friedmann and background update of that lattice.
+#pragma once
+#include <cmath>
+#include <cstddef>
+
+#include "iegpu_internal.cuh"
+#include "pot.cuh"
+#include "reduce.cuh"
+
+namespace iegpu {
+
+// ---------------------------------------------------------------------------
+// windows of table brackets around a background value
+// ---------------------------------------------------------------------------
+
+// Bracket q of the window with u[q+1] < v <= u[q]; -1 outside the window.
+// The window is centred on the background value and a perturbation is a
+// small fraction of a bracket, so a walk from the middle bracket ends after
+// one or two compares (u descends strictly, so the bracket is unique).
+__device__ __forceinline__ int window_find(const float* u, int n, float v) {
+    if (!(v <= u[0] && v > u[n])) return -1;
+    int q = n >> 1;
+    while (v > u[q]) --q;
+    while (v <= u[q + 1]) ++q;
+    return q;
+}
+
+// The window's bracket of the background value (dphi = 0), kept in registers:
+// nearly every site of a step falls in it, so the lookup below is two
+// compares; the others walk the window.
+struct WinCache {
+    float hi, lo, A, s;
+};
+
+template <bool TABLE>
+__device__ __forceinline__ WinCache win_cache(const float* w, int n) {
+    WinCache c{-1.f, 1.f, 0.f, 0.f};   // empty interval
+    if (TABLE) {
+        const int q = window_find(w, n, 0.f);
+        if (q >= 0) c = WinCache{w[q], w[q + 1], w[kWin + 1 + q], w[2 * kWin + 1 + q]};
+    }
+    return c;
+}
+
+// potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop)
+template <bool TABLE>
+__device__ __forceinline__ float split_dv(float x, const float* wk, int nk, const WinCache& c, float pn, float kv,
+                                          bool& bad) {
+    if (TABLE) {
+        if (x <= c.hi && x > c.lo) return pn * (c.A + c.s * x);
+        const int q = window_find(wk, nk, x);
+        if (q < 0) { bad = true; return 0.f; }
+        return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
+    }
+    return kv * x;
+}
+
+// V(phibar + x) - V(phibar) in table units (table) or x^2 (hilltop)
+template <bool TABLE>
+__device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad) {
+    if (TABLE) {
+        if (x <= c.hi && x > c.lo) return c.A + c.s * x;
+        const int q = window_find(wv, nv, x);
+        if (q < 0) { bad = true; return 0.f; }
+        return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
+    }
+    return x * x;
+}
+
+// ---------------------------------------------------------------------------
+// scalar update (one warp): Friedmann, background, coefficients, windows
+// ---------------------------------------------------------------------------
+//
+// Every lane evaluates the FP64 scalar recurrences (identical values); the
+// table searches and the window nodes are shared out over the lanes, so the
+// update costs a few dependent loads instead of a hundred, and lane 0 writes
+// the results.
+
+// The bracket of v, as table_bracket: the count of nodes with key >= key(v),
+// clamped to [1, n-1] (the nodes descend strictly), counted by the warp.
+__device__ __forceinline__ int warp_bracket(const PotDev& P, double v) {
+    const long long kv = order_key(v);
+    int cnt = 0;
+    for (int i = threadIdx.x & 31; i < P.n; i += 32) cnt += (__ldg(&P.key[i]) >= kv) ? 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    return cnt < 1 ? 1 : (cnt > P.n - 1 ? P.n - 1 : cnt);
+}
+
+__device__ __forceinline__ bool table_out_of_range(const PotDev& P, double v) {
+    const long long kv = order_key(v);
+    return !is_nan_bits(v) && (kv > __ldg(&P.key[0]) || kv < __ldg(&P.key[P.n - 1]));
+}
+
+// build_window by a warp: lane q writes node q and bracket q.
+__device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, const double* y, const double* dy,
+                                                  double phibar, int* err) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) W.ok = 0;
+    if (!P.table) return;
+    if (table_out_of_range(P, phibar)) {
+        *err = 1;
+        return;
+    }
+    const int lb = warp_bracket(P, phibar);
+    int l0 = lb - kWin / 2;
+    if (l0 < 1) l0 = 1;
+    int n = kWin;
+    if (l0 + n - 1 > P.n - 1) n = P.n - 1 - l0 + 1;
+    // value of the tabulated function at phibar (its own bracket)
+    const double Fbar = y[lb] + (phibar - P.x[lb]) * (dy[lb] / P.dxl[lb]);
+    if (lane <= n) W.u[lane] = (float)(P.x[l0 - 1 + lane] - phibar);
+    if (lane < n) {
+        const int l = l0 + lane;
+        const double s = dy[l] / P.dxl[l];
+        W.s[lane] = (float)s;
+        W.A[lane] = (float)((y[l] + (phibar - P.x[l]) * s) - Fbar);
+    }
+    if (lane == 0) {
+        W.l0 = l0;
+        W.n = n;
+        W.ok = 1;
+    }
+}
+
+// V(phibar)/B^2 and V'(phibar)/B^2 (src/potential.cpp:77-98), by a warp
+__device__ __forceinline__ void bar_potential_warp(const PotDev& P, double phibar, double* V, double* dV) {
+    if (P.table) {
+        const int l = warp_bracket(P, phibar);
+        *V = table_interp(P, P.V, P.dyV, phibar, l) / P.B2;
+        *dV = table_interp(P, P.dV, P.dydV, phibar, l) / P.B2;
+    } else {
+        *V = (P.V0 * (1.0 - P.c1 * (phibar * phibar))) / P.B2;
+        *dV = (P.c2 * phibar) / P.B2;
+    }
+}
+
+// sums: [0] sum of squared forward differences of dphi, [1] sum dphi,
+// [2] hilltop: sum dphi^2 / table: sum of V differences (table units).
+// Called by the 32 lanes of one warp with the same sums.
+static __device__ __noinline__ void split_scalars_warp(SplitCtl& C, const PotDev& P, const SplitConst& K,
+                                                       const double* sums, double* a_trace) {
+    const bool w0 = (threadIdx.x & 31) == 0;
+    const int mode = C.mode, steps_done = C.steps_done, steps_limit = C.steps_limit, error0 = C.error;
+    double t = C.bg.t, a = C.bg.a, ad = C.bg.ad, astep = C.bg.astep;
+    double phibar = C.phibar, pibar = C.pibar;
+    const double af = C.af, d_given = C.d_given;
+    __syncwarp();   // every lane has read the control block before lane 0 writes it
+    double d;
+    if (mode == kModeLeapfrog) {
+        if (steps_done >= steps_limit) {
+            if (w0) { C.active = 0; C.done = 1; }
+            return;
+        }
+        if (steps_done > 0) astep = a;
+        if (!(a <= af)) {
+            if (w0) { C.bg.astep = astep; C.active = 0; C.done = 1; }
+            return;
+        }
+        d = K.dt * pow_exp(astep, K.s - 1.0);
+    } else {
+        d = d_given;
+    }
+    const double s = K.s;
+    const double grad = 0.5 * sums[0] * ((1.0 / (a * K.dx)) * (1.0 / (a * K.dx))) / K.gs;
+    double Vbar, dVbar;
+    bar_potential_warp(P, phibar, &Vbar, &dVbar);
+    double pot;
+    if (P.table) pot = Vbar + (sums[2] / P.B2) / K.gs;
+    else pot = Vbar - (P.V0 * P.c1 / P.B2) * (2.0 * phibar * sums[1] + sums[2]) / K.gs;
+    const double sfev1 = s + 1.0, sfev2 = -2.0 * s + 2.0;
+    const double ad2 = (-2.0 * ad - 2.0 * a / d / sfev1 *
+                        (1.0 - sqrt(1.0 + 2.0 * d * sfev1 * ad / a +
+                                    (d * d) * sfev1 * pow_exp(a, sfev2) * (2.0 * grad / 3.0 + pot)))) / d;
+    ad += 0.5 * d * ad2;
+    const double laplnorm = pow_exp(a, -2.0 * s) / (K.dx * K.dx);
+    const double friction = (2.0 + s) * ad / a;
+    const double potnorm = pow_exp(a, 2.0 - 2.0 * s);
+    const double srcAmp = 2.0 * pow_exp(a, -2.0 * s);
+    ad += 0.5 * d * ad2;
+    // background kick (homogeneous mode of the lattice kick)
+    pibar = pibar + d * (-friction * pibar - potnorm * dVbar);
+    int err = 0;
+    build_window_warp(C.wk, P, P.dV, P.dydV, phibar, &err);
+    if (mode == kModeLeapfrog) {
+        phibar = phibar + d * pibar;
+        t += d;
+    }
+    if (w0) {
+        C.d = (float)d;
+        C.lapl = (float)laplnorm;
+        C.fric = (float)friction;
+        C.pn = (float)(potnorm / P.B2);
+        C.kv = (float)(potnorm * P.c2 / P.B2);
+        C.srcAmp = (float)srcAmp;
+        C.dd = d;
+        C.bg.astep = astep;
+        C.bg.ad = ad;
+        C.bg.ad2 = ad2;
+        C.pibar = pibar;
+        C.active = 1;
+        if (mode == kModeLeapfrog) {
+            C.phibar = phibar;
+            C.bg.t = t;
+            C.bg.a = a + d * ad;
+            if (a_trace) a_trace[steps_done] = C.bg.a;
+            C.steps_done = steps_done + 1;
+        }
+    }
+    build_window_warp(C.wv, P, P.V, P.dyV, phibar, &err);
+    if (err && !error0 && w0) { C.error = IEGPU_ERANGE; C.errval = phibar; C.active = 0; C.done = 1; }
+}
+
+// One lane, for the diagnostics that build a window outside the step.
+static __device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, const double* y, const double* dy,
+                                                 double phibar, int* err) {
+    W.ok = 0;
+    if (!P.table) return;
+    bool oor;
+    const int lb = table_bracket(P, phibar, &oor);
+    if (oor) { *err = 1; return; }
+    int l0 = lb - kWin / 2;
+    if (l0 < 1) l0 = 1;
+    int n = kWin;
+    if (l0 + n - 1 > P.n - 1) n = P.n - 1 - l0 + 1;
+    W.l0 = l0;
+    W.n = n;
+    const double Fbar = y[lb] + (phibar - P.x[lb]) * (dy[lb] / P.dxl[lb]);
+    for (int q = 0; q <= n; ++q) W.u[q] = (float)(P.x[l0 - 1 + q] - phibar);
+    for (int q = 0; q < n; ++q) {
+        const int l = l0 + q;
+        const double s = dy[l] / P.dxl[l];
+        W.s[q] = (float)s;
+        W.A[q] = (float)((y[l] + (phibar - P.x[l]) * s) - Fbar);
+    }
+    W.ok = 1;
+}
+
+// ---------------------------------------------------------------------------
+// Kahan accumulator
+// ---------------------------------------------------------------------------
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// Block sums into partial slot `slot` of `nslots`; the last of the nslots CTAs
+// to arrive adds the partials in slot order and runs the scalar update.
+// `state` (may be null) is the ensemble form's per-lattice word: that CTA
+// toggles its bit 0 (the ping-pong half) after a step (`toggle`), and sets
+// bit 1 once the lattice has stopped.
+__device__ __forceinline__ void finish_sums_slot(double (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+                                                 double* part, unsigned* counter, double* a_trace, int slot,
+                                                 int nslots, int* state, bool toggle) {
+    block_sum<3>(v);
+    if (threadIdx.x == 0) {
+        part[3 * slot] = v[0];
+        part[3 * slot + 1] = v[1];
+        part[3 * slot + 2] = v[2];
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == (unsigned)nslots - 1);
+    __syncthreads();
+    if (!last) return;
+    if (threadIdx.x < 32) {
+        double tot[3];
+        sum_partials<3>(part, nslots, tot);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) tot[q] = __shfl_sync(0xffffffffu, tot[q], 0);
+        SplitCtl& C = *ctl;
+        int error = 0;
+        if (threadIdx.x == 0) {
+            *counter = 0;
+            if (state && toggle) *state ^= 1;
+            C.sums[0] = tot[0];
+            C.sums[1] = tot[1];
+            C.sums[2] = tot[2];
+            error = C.error;
+        }
+        error = __shfl_sync(0xffffffffu, error, 0);
+        if (error) {
+            if (threadIdx.x == 0) { C.active = 0; C.done = 1; }
+        } else {
+            split_scalars_warp(C, P, K, tot, a_trace);
+        }
+        __syncwarp();
+        if (threadIdx.x == 0 && state && C.done) *state |= 2;
+    }
+}
+
+__device__ __forceinline__ void finish_sums(double (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+                                            double* part, unsigned* counter, double* a_trace) {
+    finish_sums_slot(v, ctl, P, K, part, counter, a_trace, blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y,
+                     nullptr, false);
+}
+
+// Sums of the current dphi (start of a leapfrog call), thread per site:
+// One CTA's share (slot of nslots, grid-stride over the sites) of the sums.
+template <bool TABLE>
+__device__ __forceinline__ void prime_body(const float* __restrict__ x, SplitCtl* ctl, const PotDev& P,
+                                           const SplitConst& K, double* part, unsigned* counter, double* a_trace,
+                                           int lg, int slot, int nslots, int* state) {
+    __shared__ float su[kWin + 1], sA[kWin], ss[kWin];
+    __shared__ int sn;
+    __shared__ SplitWin W;
+    if (threadIdx.x == 0) sn = 0;
+    if (TABLE && threadIdx.x < 32) {
+        // every CTA forms the window around the current phibar itself
+        int err = 0;
+        build_window_warp(W, P, P.V, P.dyV, ctl->phibar, &err);
+        __syncwarp();
+        if (threadIdx.x == 0) sn = err ? -1 : W.n;
+        if (!err) {
+            if (threadIdx.x <= W.n) su[threadIdx.x] = W.u[threadIdx.x];
+            if (threadIdx.x < W.n) { sA[threadIdx.x] = W.A[threadIdx.x]; ss[threadIdx.x] = W.s[threadIdx.x]; }
+        }
+    }
+    __syncthreads();
+    const long long gs = 1LL << (3 * lg);
+    const int m = (1 << lg) - 1;
+    Kahan g, s1, s2;
+    bool bad = TABLE && sn < 0;
+    for (long long id = (long long)slot * kThreads + threadIdx.x; id < gs; id += (long long)nslots * kThreads) {
+        const int k = (int)(id & m), j = (int)((id >> lg) & m), i = (int)(id >> (2 * lg));
+        const float xc = x[id];
+        const float xk = x[id - k + ((k + 1) & m)];
+        const float xj = x[id + ((long long)(((j + 1) & m) - j) << lg)];
+        const float xi = x[id + ((long long)(((i + 1) & m) - i) << (2 * lg))];
+        const float dk = xk - xc, dj = xj - xc, di = xi - xc;
+        g.add(dk * dk + dj * dj + di * di);
+        s1.add(xc);
+        if (TABLE) {
+            const int q = bad ? -1 : window_find(su, sn, xc);
+            if (q < 0) bad = true;
+            else s2.add(sA[q] + ss[q] * xc);
+        } else {
+            s2.add(xc * xc);
+        }
+    }
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, false);
+}
+
+struct SplitBufs {
+    const float* xs;   // dphi (step n)
+    float* xd;         // dphi (step n+1)
+    const float* ps;   // dpi  (n-1/2)
+    float* pd;         // dpi  (n+1/2)
+};
+
+// Asynchronous global -> shared copies (cp.async), so the planes a CTA will
+// need next are in flight while it works on the current one.
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int n>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory"); }
+
+constexpr int kPrefetch = 3;   // planes in flight ahead of the one being computed
+constexpr int kPhiSlots = 6;   // three stencil planes + kPrefetch
+constexpr int kPiSlots = 4;    // one plane in use + kPrefetch
+constexpr int kColOff = 4;     // shared-memory column of k = 0 (16-byte aligned rows)
+
+// Shared-memory floats of the step kernel for tile TJ x TK.
+__host__ __device__ inline int split_step_smem_floats(int TJ, int TK) {
+    const int RS = TK + 8;
+    return kPhiSlots * (TJ + 3) * RS + kPiSlots * (TJ + 1) * RS + 2 * (TJ + 1) * (TK + 1) + 2 * (3 * kWin + 1);
+}
+
+
+// Full-row variant of the step for 32 <= N <= 512: a tile is TJ rows of
+// complete k lines, so the k direction is periodic inside shared memory and
+// needs no halo.  Warp w computes row j0+w for w = 0..TJ (row TJ is the +j
+// halo row whose new values only feed the j differences of row TJ-1); lane l
+// handles k = l + 32c, c < C = N/32.  The planes come in through a cp.async
+// ring kRowPrefetch planes ahead.  Row partial sums are added per plane into
+// Kahan-compensated per-thread accumulators.
+__host__ __device__ inline int split_row_smem_floats(int TJ, int N, int PF) {
+    return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + (TJ + 1) * N + 2 * (3 * kWin + 1);
+}
+
+// PF = planes prefetched ahead; the i range [0, N) is cut into `chunks`
+// nearly equal plane ranges (any count, so the grid can match the SMs).
+// One CTA: rows j0 .. j0+TJ-1, planes i0 .. i0+CH-1; its sums go to partial
+// slot `slot` of `nslots`.
+template <bool TABLE, int C, int TJ, int PF>
+__device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+                                          double* part, unsigned* counter, double* a_trace, int j0, int i0, int CH,
+                                          int slot, int nslots, int* state) {
+    constexpr int kRowPrefetch = PF, kRowPhiSlots = 3 + PF, kRowPiSlots = 1 + PF;
+    constexpr int N = 32 * C, m = N - 1;
+    constexpr int lgN = (C == 1) ? 5 : (C == 2) ? 6 : (C == 4) ? 7 : (C == 8) ? 8 : 9;
+    constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
+    extern __shared__ __align__(16) float smem[];
+    float* ring = smem;
+    float* pis = ring + kRowPhiSlots * RP;
+    float* nb = pis + kRowPiSlots * PP;
+    float* wk = nb + (TJ + 1) * N;
+    float* wv = wk + 3 * kWin + 1;
+    __shared__ int nk_s, nv_s, active_s;
+    __shared__ float cf[6];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        const SplitCtl& Cc = *ctl;
+        active_s = Cc.active;
+        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
+        nk_s = Cc.wk.n;
+        nv_s = Cc.wv.n;
+    }
+    if (TABLE) {
+        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q < kWin; q += NTH) {
+            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
+            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+        }
+    }
+    __syncthreads();
+    if (!active_s) return;
+    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const WinCache ck = win_cache<TABLE>(wk, nk_s), cv = win_cache<TABLE>(wv, nv_s);
+
+    auto issue_phi = [&](int i) {
+        float* dst = ring + ((i - i0 + 1) % kRowPhiSlots) * RP;
+        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 3) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
+        }
+    };
+    auto issue_pi = [&](int i) {
+        float* dst = pis + ((i - i0) % kRowPiSlots) * PP;
+        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 1) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
+        }
+    };
+
+    Kahan g, s1, s2;
+    bool bad = false;
+    float xprev[C];
+    issue_phi(i0 - 1);
+    issue_phi(i0);
+    cp_commit();
+    for (int q = 0; q < kRowPrefetch; ++q) {
+        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+        if (q <= CH) issue_pi(i0 + q);
+        cp_commit();
+    }
+    const int jl = w;              // row of this warp (TJ: halo row)
+    const bool interior = jl < TJ;
+    for (int p = 0; p <= CH; ++p) {
+        const int i = i0 + p;
+        cp_wait<kRowPrefetch - 1>();
+        __syncthreads();
+        const float* pc = ring + ((p + 1) % kRowPhiSlots) * RP + (jl + 1) * N;
+        const float* pu = ring + ((p + 2) % kRowPhiSlots) * RP + (jl + 1) * N;
+        const float* pl = ring + (p % kRowPhiSlots) * RP + (jl + 1) * N;
+        const float* pp = pis + (p % kRowPiSlots) * PP + jl * N;
+        float xnew[C];
+        float rs1 = 0.f, rs2 = 0.f;
+        const bool store = interior && p < CH;
+        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int k = lane + 32 * c;
+            const float x = pc[k];
+            const float lap = pc[(k + 1) & m] + pc[(k - 1) & m] + pc[k + N] + pc[k - N] + pu[k] + pl[k] - 6.f * x;
+            const float pi0 = pp[k];
+            const float dv = split_dv<TABLE>(x, wk, nk_s, ck, pn, kv, bad);
+            const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
+            const float xn = x + d * pin;
+            xnew[c] = xn;
+            nb[jl * N + k] = xn;
+            if (store) {
+                B.xd[gb + k] = xn;
+                B.pd[gb + k] = pin;
+                rs1 += xn;
+                rs2 += split_v<TABLE>(xn, wv, nv_s, cv, bad);
+            }
+        }
+        __syncthreads();
+        // planes kRowPrefetch ahead go into the slots no longer needed
+        if (p + kRowPrefetch + 1 <= CH + 1) issue_phi(i + 1 + kRowPrefetch);
+        if (p + kRowPrefetch <= CH) issue_pi(i + kRowPrefetch);
+        cp_commit();
+        if (interior) {
+            float rg = 0.f;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int k = lane + 32 * c;
+                if (p < CH) {
+                    const float dk = nb[jl * N + ((k + 1) & m)] - xnew[c];
+                    const float dj = nb[(jl + 1) * N + k] - xnew[c];
+                    rg += dk * dk + dj * dj;
+                }
+                if (p >= 1) {
+                    const float di = xnew[c] - xprev[c];
+                    rg += di * di;
+                }
+                xprev[c] = xnew[c];
+            }
+            g.add(rg);
+            if (store) { s1.add(rs1); s2.add(rs2); }
+        }
+    }
+    cp_wait<0>();
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
+}
+
+// Vector variant of the row kernel for N >= 128: lane l owns the four
+// consecutive sites k = 4(l + 32v) .. +3, v < C4 = N/128, so plane rows move
+// with 128-bit shared and global accesses and the k +- 1 neighbours across
+// lanes come by warp shuffles.  The new planes are double-buffered, which
+// leaves one barrier per plane: iteration p finishes the differences of plane
+// p-1 and computes plane p.
+__host__ __device__ inline int split_row4_smem_floats(int TJ, int N, int PF) {
+    return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + 2 * (TJ + 1) * N + 2 * (3 * kWin + 1);
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+template <bool TABLE, int C4, int TJ, int PF>
+__device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+                                           double* part, unsigned* counter, double* a_trace, int j0, int i0, int CH,
+                                           int slot, int nslots, int* state) {
+    constexpr int N = 128 * C4, m = N - 1;
+    constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
+    constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
+    constexpr int PHS = 3 + PF, PIS = 1 + PF;
+    extern __shared__ __align__(16) float smem[];
+    float* ring = smem;
+    float* pis = ring + PHS * RP;
+    float* nb = pis + PIS * PP;
+    float* wk = nb + 2 * NBP;
+    float* wv = wk + 3 * kWin + 1;
+    __shared__ int nk_s, nv_s, active_s;
+    __shared__ float cf[6];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        const SplitCtl& Cc = *ctl;
+        active_s = Cc.active;
+        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
+        nk_s = Cc.wk.n;
+        nv_s = Cc.wv.n;
+    }
+    if (TABLE) {
+        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q < kWin; q += NTH) {
+            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
+            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+        }
+    }
+    __syncthreads();
+    if (!active_s) return;
+    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const int nk = nk_s, nv = nv_s;
+    const WinCache ck = win_cache<TABLE>(wk, nk), cv = win_cache<TABLE>(wv, nv);
+
+    auto issue_phi = [&](int i) {
+        float* dst = ring + ((i - i0 + 1) % PHS) * RP;
+        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 3) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
+        }
+    };
+    auto issue_pi = [&](int i) {
+        float* dst = pis + ((i - i0) % PIS) * PP;
+        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+        constexpr int ops = (TJ + 1) * (N / 4);
+        for (int o = tid; o < ops; o += NTH) {
+            const int r = o / (N / 4), q = o - r * (N / 4);
+            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
+        }
+    };
+
+    Kahan g, s1, s2;
+    bool bad = false;
+    const int jl = w;
+    const bool interior = jl < TJ;
+    float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
+    issue_phi(i0 - 1);
+    issue_phi(i0);
+    cp_commit();
+    for (int q = 0; q < PF; ++q) {
+        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+        if (q <= CH) issue_pi(i0 + q);
+        cp_commit();
+    }
+    // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
+    auto diffs = [&](int p, bool kj) {
+        const float* nr = nb + ((p - 1) & 1) * NBP;
+        float rg = 0.f;
+#pragma unroll
+        for (int v = 0; v < C4; ++v) {
+            const int k = 4 * (lane + 32 * v);
+            const float4 xc = xp1[v];
+            if (kj) {
+                // x(k+4): lane+1's first element, or the next vector's lane 0 (periodic)
+                const float nxt_same = __shfl_down_sync(0xffffffffu, xc.x, 1);
+                const float nxt_wrap = __shfl_sync(0xffffffffu, xp1[(v + 1) % C4].x, 0);
+                const float x4 = lane == 31 ? nxt_wrap : nxt_same;
+                const float4 up = ld4(nr + (jl + 1) * N + k);
+                const float a0 = xc.y - xc.x, a1 = xc.z - xc.y, a2 = xc.w - xc.z, a3 = x4 - xc.w;
+                const float b0 = up.x - xc.x, b1 = up.y - xc.y, b2 = up.z - xc.z, b3 = up.w - xc.w;
+                rg += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + b0 * b0 + b1 * b1 + b2 * b2 + b3 * b3;
+            }
+            if (p >= 2) {
+                const float4 xo = xp2[v];
+                const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+                rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+            }
+        }
+        g.add(rg);
+    };
+    for (int p = 0; p <= CH; ++p) {
+        const int i = i0 + p;
+        cp_wait<PF - 1>();
+        __syncthreads();
+        // planes PF ahead go into the slots of planes no longer read
+        if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
+        if (p + PF <= CH) issue_pi(i + PF);
+        cp_commit();
+        if (interior && p >= 1) diffs(p, true);
+        const float* pc = ring + ((p + 1) % PHS) * RP + (jl + 1) * N;
+        const float* pu = ring + ((p + 2) % PHS) * RP + (jl + 1) * N;
+        const float* pl = ring + (p % PHS) * RP + (jl + 1) * N;
+        const float* pp = pis + (p % PIS) * PP + jl * N;
+        float* nw = nb + (p & 1) * NBP + jl * N;
+        const bool store = interior && p < CH;
+        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
+        float4 xs[C4];
+#pragma unroll
+        for (int v = 0; v < C4; ++v) xs[v] = ld4(pc + 4 * (lane + 32 * v));
+        float rs1 = 0.f, rs2 = 0.f;
+#pragma unroll
+        for (int v = 0; v < C4; ++v) {
+            const int k = 4 * (lane + 32 * v);
+            const float4 x = xs[v];
+            // k-1 and k+4 with periodic wrap across vectors and the row
+            const float lft_same = __shfl_up_sync(0xffffffffu, x.w, 1);
+            const float lft_wrap = __shfl_sync(0xffffffffu, xs[(v + C4 - 1) % C4].w, 31);
+            const float rgt_same = __shfl_down_sync(0xffffffffu, x.x, 1);
+            const float rgt_wrap = __shfl_sync(0xffffffffu, xs[(v + 1) % C4].x, 0);
+            const float xl = lane == 0 ? lft_wrap : lft_same;
+            const float xr = lane == 31 ? rgt_wrap : rgt_same;
+            const float4 up = ld4(pc + k + N), dn = ld4(pc + k - N), iu = ld4(pu + k), il = ld4(pl + k);
+            const float4 pi = ld4(pp + k);
+            float4 lap;
+            lap.x = (x.y + xl) + (up.x + dn.x) + (iu.x + il.x) - 6.f * x.x;
+            lap.y = (x.z + x.x) + (up.y + dn.y) + (iu.y + il.y) - 6.f * x.y;
+            lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
+            lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
+            float4 pin, xn;
+            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad));
+            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad));
+            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad));
+            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad));
+            xn.x = x.x + d * pin.x;
+            xn.y = x.y + d * pin.y;
+            xn.z = x.z + d * pin.z;
+            xn.w = x.w + d * pin.w;
+            st4(nw + k, xn);
+            if (store) {
+                st4(B.xd + gb + k, xn);
+                st4(B.pd + gb + k, pin);
+                rs1 += (xn.x + xn.y) + (xn.z + xn.w);
+                rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad) + split_v<TABLE>(xn.y, wv, nv, cv, bad)) +
+                       (split_v<TABLE>(xn.z, wv, nv, cv, bad) + split_v<TABLE>(xn.w, wv, nv, cv, bad));
+            }
+            xp2[v] = xp1[v];
+            xp1[v] = xn;
+        }
+        if (store) { s1.add(rs1); s2.add(rs2); }
+    }
+    // the last pair (CH-1, CH) along i
+    if (interior) {
+        float rg = 0.f;
+#pragma unroll
+        for (int v = 0; v < C4; ++v) {
+            const float4 xc = xp1[v], xo = xp2[v];
+            const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+            rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+        }
+        g.add(rg);
+    }
+    cp_wait<0>();
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v3[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
+}
+
+// Whole-plane variant of the step for small lattices (N = 32, 64): a CTA owns
+// complete (j, k) planes of its chunk of i, so j and k are periodic inside
+// shared memory and no halo rows are recomputed.  Thread t owns the float4
+// vectors q = t + v*NT (v < V) of every plane: row j = q / (N/4), sites
+// k = 4(q mod N/4) .. +3; the N/4 lanes of a row are adjacent in a warp, so
+// the k +- 1 neighbours come by shuffles.  A plane of dphi and of dpi arrives
+// as one contiguous N^2-float cp.async copy, PF planes ahead; the new planes
+// are double-buffered (one barrier per plane), as in the vector row kernel.
+__host__ __device__ inline int split_plane_smem_floats(int N, int PF) {
+    return ((3 + PF) + (1 + PF) + 2) * N * N + 2 * (3 * kWin + 1);
+}
+
+template <bool TABLE, int N, int NT, int PF>
+__device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+                                           double* part, unsigned* counter, double* a_trace, int i0, int CH,
+                                           int slot, int nslots, int* state) {
+    constexpr int m = N - 1, NN = N * N, Q = NN / 4, V = Q / NT, W = N / 4;
+    constexpr int lgN = (N == 32) ? 5 : 6;
+    constexpr int PHS = 3 + PF, PIS = 1 + PF;
+    static_assert(V * NT == Q && (N == 32 || N == 64), "plane tiling");
+    extern __shared__ __align__(16) float smem[];
+    float* ring = smem;
+    float* pis = ring + PHS * NN;
+    float* nb = pis + PIS * NN;
+    float* wk = nb + 2 * NN;
+    float* wv = wk + 3 * kWin + 1;
+    __shared__ int nk_s, nv_s, active_s;
+    __shared__ float cf[6];
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0) {
+        const SplitCtl& Cc = *ctl;
+        active_s = Cc.active;
+        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
+        nk_s = Cc.wk.n;
+        nv_s = Cc.wv.n;
+    }
+    if (TABLE) {
+        for (int q = tid; q <= kWin; q += NT) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q < kWin; q += NT) {
+            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
+            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+        }
+    }
+    __syncthreads();
+    if (!active_s) return;
+    const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
+    const int nk = nk_s, nv = nv_s;
+    const WinCache ck = win_cache<TABLE>(wk, nk), cv = win_cache<TABLE>(wv, nv);
+    // lanes of the same row: the previous and next vector (periodic in k)
+    const int rowbase = lane & ~(W - 1);
+    const int lprev = rowbase | ((lane + W - 1) & (W - 1));
+    const int lnext = rowbase | ((lane + 1) & (W - 1));
+
+    auto issue_phi = [&](int i) {
+        float* dst = ring + ((i - i0 + 1) % PHS) * NN;
+        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int q = tid + v * NT;
+            cp_async16(dst + 4 * q, src + 4 * q);
+        }
+    };
+    auto issue_pi = [&](int i) {
+        float* dst = pis + ((i - i0) % PIS) * NN;
+        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int q = tid + v * NT;
+            cp_async16(dst + 4 * q, src + 4 * q);
+        }
+    };
+
+    Kahan g, s1, s2;
+    bool bad = false;
+    float4 xp1[V], xp2[V];   // new values of this thread's vectors: plane p-1 and p-2
+    issue_phi(i0 - 1);
+    issue_phi(i0);
+    cp_commit();
+    for (int q = 0; q < PF; ++q) {
+        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+        if (q <= CH) issue_pi(i0 + q);
+        cp_commit();
+    }
+    // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
+    auto diffs = [&](int p) {
+        const float* nr = nb + ((p - 1) & 1) * NN;
+        float rg = 0.f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int q = tid + v * NT;
+            const int j = q / W, k = 4 * (q % W);
+            const float4 xc = xp1[v];
+            const float x4 = __shfl_sync(0xffffffffu, xc.x, lnext);
+            const float4 up = ld4(nr + ((j + 1) & m) * N + k);
+            const float a0 = xc.y - xc.x, a1 = xc.z - xc.y, a2 = xc.w - xc.z, a3 = x4 - xc.w;
+            const float b0 = up.x - xc.x, b1 = up.y - xc.y, b2 = up.z - xc.z, b3 = up.w - xc.w;
+            rg += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + b0 * b0 + b1 * b1 + b2 * b2 + b3 * b3;
+            if (p >= 2) {
+                const float4 xo = xp2[v];
+                const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+                rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+            }
+        }
+        g.add(rg);
+    };
+    for (int p = 0; p <= CH; ++p) {
+        const int i = i0 + p;
+        cp_wait<PF - 1>();
+        __syncthreads();
+        // planes PF ahead go into the slots of planes no longer read
+        if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
+        if (p + PF <= CH) issue_pi(i + PF);
+        cp_commit();
+        if (p >= 1) diffs(p);
+        const float* pc = ring + ((p + 1) % PHS) * NN;
+        const float* pu = ring + ((p + 2) % PHS) * NN;
+        const float* pl = ring + (p % PHS) * NN;
+        const float* pp = pis + (p % PIS) * NN;
+        float* nw = nb + (p & 1) * NN;
+        const bool store = p < CH;
+        const long long gb = (long long)(i & m) << (2 * lgN);
+        float rs1 = 0.f, rs2 = 0.f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int q = tid + v * NT;
+            const int j = q / W, k = 4 * (q % W), o = j * N + k;
+            const float4 x = ld4(pc + o);
+            const float xl = __shfl_sync(0xffffffffu, x.w, lprev);
+            const float xr = __shfl_sync(0xffffffffu, x.x, lnext);
+            const float4 up = ld4(pc + ((j + 1) & m) * N + k), dn = ld4(pc + ((j - 1) & m) * N + k);
+            const float4 iu = ld4(pu + o), il = ld4(pl + o);
+            const float4 pi = ld4(pp + o);
+            float4 lap;
+            lap.x = (x.y + xl) + (up.x + dn.x) + (iu.x + il.x) - 6.f * x.x;
+            lap.y = (x.z + x.x) + (up.y + dn.y) + (iu.y + il.y) - 6.f * x.y;
+            lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
+            lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
+            float4 pin, xn;
+            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad));
+            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad));
+            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad));
+            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad));
+            xn.x = x.x + d * pin.x;
+            xn.y = x.y + d * pin.y;
+            xn.z = x.z + d * pin.z;
+            xn.w = x.w + d * pin.w;
+            st4(nw + o, xn);
+            if (store) {
+                st4(B.xd + gb + o, xn);
+                st4(B.pd + gb + o, pin);
+                rs1 += (xn.x + xn.y) + (xn.z + xn.w);
+                rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad) + split_v<TABLE>(xn.y, wv, nv, cv, bad)) +
+                       (split_v<TABLE>(xn.z, wv, nv, cv, bad) + split_v<TABLE>(xn.w, wv, nv, cv, bad));
+            }
+            xp2[v] = xp1[v];
+            xp1[v] = xn;
+        }
+        if (store) { s1.add(rs1); s2.add(rs2); }
+    }
+    // the last pair (CH-1, CH) along i
+    {
+        float rg = 0.f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const float4 xc = xp1[v], xo = xp2[v];
+            const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+            rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+        }
+        g.add(rg);
+    }
+    cp_wait<0>();
+    if (bad) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
+    }
+    double v3[3] = {g.value(), s1.value(), s2.value()};
+    finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
+}
+
+}  // namespace iegpu

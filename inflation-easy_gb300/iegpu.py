@@ -99,6 +99,25 @@ def load() -> C.CDLL:
         "iegpu_zero_above": (I, [P, I, D]),
         "iegpu_sum": (I, [P, I, dp]),
         "iegpu_shell_spectrum_noalloc": (I, [P, P, I, P, P, P]),
+        "iegpu_set_shape": (I, [P, I, I, I]),
+        "iegpu_ens_create": (I, [C.POINTER(Config), ip, I, C.POINTER(P)]),
+        "iegpu_ens_destroy": (I, [P]),
+        "iegpu_ens_last_error": (C.c_char_p, [P]),
+        "iegpu_ens_launch_count": (C.c_longlong, [P]),
+        "iegpu_ens_stream": (P, [P]),
+        "iegpu_ens_set_table": (I, [P, dp, dp, dp, I]),
+        "iegpu_ens_bunch_davies": (I, [P, ip, D, D, D, D, dp]),
+        "iegpu_ens_evolve_fields": (I, [P, dp, P]),
+        "iegpu_ens_leapfrog": (I, [P, dp, I, P, ip]),
+        "iegpu_ens_profile": (I, [P, I, P, dp, dp]),
+        "iegpu_ens_autotune": (I, [P, P, ip, ip, ip]),
+        "iegpu_ens_set_shape": (I, [P, I, I, I, I]),
+        "iegpu_ens_timer_start": (I, [P]),
+        "iegpu_ens_timer_stop": (I, [P, C.POINTER(C.c_float)]),
+        "iegpu_ens_download": (I, [P, I, I, dp]),
+        "iegpu_ens_deltaN": (I, [P, P, D, D, I, D, dp, fp]),
+        "iegpu_ens_zeta_spectra": (I, [P, ip, dp]),
+        "iegpu_ens_zeta_histogram": (I, [P, I, I, D, dp, dp, dp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -212,6 +231,9 @@ class Lattice:
         return tuple(out)
 
     # -- measurement ------------------------------------------------------
+    def set_shape(self, rows: int, prefetch: int, chunks: int) -> None:
+        self._check(self.lib.iegpu_set_shape(self.h, rows, prefetch, chunks))
+
     def autotune(self, bg: Bg):
         r, p, ch = C.c_int(), C.c_int(), C.c_int()
         self._check(self.lib.iegpu_autotune(self.h, C.byref(bg), C.byref(r), C.byref(p), C.byref(ch)))
@@ -298,3 +320,143 @@ class Lattice:
         v = C.c_double()
         self._check(self.lib.iegpu_sum(self.h, field, C.byref(v)))
         return v.value
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Ensemble:
+    """Many independent lattices evolved together in the split form (an
+    iegpu_ens).  `Ns` gives each lattice's size; per-lattice values (seeds,
+    af, background scalars) are arrays indexed by lattice."""
+
+    def __init__(self, Ns, L: float, dt: float, V0: float, ns: float = 0.97, rescale_B: float | None = None,
+                 rescale_s: float = 0.0, potential: int = POT_HILLTOP, criterion: int | None = None):
+        self.lib = load()
+        if rescale_B is None:
+            rescale_B = float(np.sqrt(V0))
+        if criterion is None:
+            criterion = CRIT_MONOTONIC if potential == POT_TABLE else CRIT_ANTIMONOTONIC
+        self.cfg = Config(0, potential, 0, FORM_SPLIT, criterion, L, dt, rescale_s, rescale_B, V0, ns)
+        self.Ns = np.ascontiguousarray(Ns, dtype=np.int32)
+        self.count = len(self.Ns)
+        h = C.c_void_p()
+        rc = self.lib.iegpu_ens_create(C.byref(self.cfg), _ip(self.Ns), self.count, C.byref(h))
+        if rc != OK:
+            raise IegpuError(rc, self.lib.iegpu_strerror(rc).decode())
+        self.h = h
+
+    def _check(self, rc: int) -> None:
+        if rc != OK:
+            raise IegpuError(rc, self.lib.iegpu_ens_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.iegpu_ens_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def launches(self) -> int:
+        return self.lib.iegpu_ens_launch_count(self.h)
+
+    def bgs(self, hubble) -> C.Array:
+        """Background scalars of every lattice at the start: t = 0, a = 1, ad = H."""
+        b = (Bg * self.count)()
+        for q, hq in enumerate(hubble):
+            b[q] = Bg(0.0, 1.0, float(hq), 0.0, 1.0)
+        return b
+
+    def set_table(self, phi, V, dV) -> None:
+        phi, V, dV = (np.ascontiguousarray(x, dtype=np.float64) for x in (phi, V, dV))
+        self._check(self.lib.iegpu_ens_set_table(self.h, _dp(phi), _dp(V), _dp(dV), len(phi)))
+
+    def bunch_davies(self, seeds, phi0: float, dphi0: float, high_cut: float = 0.0, low_cut: float = 0.0):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int32)
+        hub = np.zeros(self.count)
+        self._check(self.lib.iegpu_ens_bunch_davies(self.h, _ip(seeds), phi0, dphi0, high_cut, low_cut, _dp(hub)))
+        return hub
+
+    def evolve_fields(self, d, bg) -> None:
+        d = np.ascontiguousarray(np.broadcast_to(d, (self.count,)), dtype=np.float64)
+        self._check(self.lib.iegpu_ens_evolve_fields(self.h, _dp(d), bg))
+
+    def leapfrog(self, af, max_steps: int, bg):
+        af = np.ascontiguousarray(np.broadcast_to(af, (self.count,)), dtype=np.float64)
+        steps = np.zeros(self.count, dtype=np.int32)
+        self._check(self.lib.iegpu_ens_leapfrog(self.h, _dp(af), max_steps, bg, _ip(steps)))
+        return steps
+
+    def profile(self, nsteps: int, bg):
+        a, b = C.c_double(), C.c_double()
+        self._check(self.lib.iegpu_ens_profile(self.h, nsteps, bg, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def autotune(self, bg):
+        """Per lattice: rows per tile (N: whole planes), planes prefetched, plane chunks."""
+        r, p, ch = (np.zeros(self.count, dtype=np.int32) for _ in range(3))
+        self._check(self.lib.iegpu_ens_autotune(self.h, bg, _ip(r), _ip(p), _ip(ch)))
+        return {"rows": r, "prefetch": p, "chunks": ch}
+
+    def set_shape(self, N: int, rows: int, prefetch: int, chunks: int) -> None:
+        self._check(self.lib.iegpu_ens_set_shape(self.h, N, rows, prefetch, chunks))
+
+    def timer_start(self) -> None:
+        self._check(self.lib.iegpu_ens_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_float()
+        self._check(self.lib.iegpu_ens_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def download(self, lattice: int, field: int) -> np.ndarray:
+        out = np.empty(int(self.Ns[lattice]) ** 3, dtype=np.float64)
+        self._check(self.lib.iegpu_ens_download(self.h, lattice, field, _dp(out)))
+        return out
+
+    def deltaN(self, bg, dN: float, Nend: float, phiref_manual: float | None = None):
+        phiref = np.zeros(self.count)
+        nmean = np.zeros(self.count, dtype=np.float32)
+        self._check(self.lib.iegpu_ens_deltaN(self.h, bg, dN, Nend, int(phiref_manual is not None),
+                                              0.0 if phiref_manual is None else phiref_manual, _dp(phiref),
+                                              nmean.ctypes.data_as(C.POINTER(C.c_float))))
+        return phiref, nmean
+
+    def zeta_spectra(self):
+        """[(counts, f2)] per lattice, as iegpu_spectrum of that lattice's zeta (spectraN)."""
+        nbs = [self.lib.iegpu_numbins(int(n)) for n in self.Ns]
+        tot = int(sum(nbs))
+        counts = np.zeros(tot, dtype=np.int32)
+        f2 = np.zeros(tot)
+        self._check(self.lib.iegpu_ens_zeta_spectra(self.h, _ip(counts), _dp(f2)))
+        out, at = [], 0
+        for nb in nbs:
+            out.append((counts[at:at + nb], f2[at:at + nb]))
+            at += nb
+        return out
+
+    def zeta_histogram(self, N: int = 0, nbins: int = 200, nsigma: float = 10.0):
+        sigma, lo, width = C.c_double(), C.c_double(), C.c_double()
+        counts = np.zeros(nbins, dtype=np.int64)
+        outside = np.zeros(2, dtype=np.int64)
+        ll = C.POINTER(C.c_longlong)
+        self._check(self.lib.iegpu_ens_zeta_histogram(self.h, N, nbins, nsigma, C.byref(sigma), C.byref(lo),
+                                                      C.byref(width), counts.ctypes.data_as(ll),
+                                                      outside.ctypes.data_as(ll)))
+        return {"sigma": sigma.value, "lo": lo.value, "width": width.value, "counts": counts, "outside": outside}

@@ -1,0 +1,170 @@
+"""The ensemble form: many lattices of mixed sizes evolved together.
+
+1. Against one-lattice split runs of the same sizes, seeds and launch shape:
+   fields, background scalars, steps taken (per-lattice af), and the whole
+   deltaN stage (phiref, Nmean, zeta) bit for bit, the zeta spectra too.
+2. The pooled zeta histogram against numpy on the downloaded zeta maps
+   (counts exact, sigma relative 1e-10).
+3. Against the plain FP64 form on the same seeds: the split form's error
+   budget, perturbations within 1e-4 of their spread, a and ad relative 1e-9.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HILLTOP = dict(L=10.0, dt=1e-3, V0=3.338e-13, ns=0.965, phi0=0.0935, dphi0=0.000796)
+USR = dict(L=10.0, dt=1e-3, V0=3e-9, ns=0.97, phi0=2.9181235049318586, dphi0=-0.06727651095116181)
+NS = [32, 64, 32, 128]
+SEEDS = [3, 5, 7, 9]
+# launch shapes per size (rows per tile, planes prefetched, chunks); rows = N: whole planes
+ROWS = {32: (8, 2, 1), 64: (8, 2, 2), 128: (8, 2, 4)}
+PLANES = {32: (32, 4, 2), 64: (64, 2, 4), 128: (4, 1, 8)}
+
+
+def _case(usr):
+    return USR if usr else HILLTOP
+
+
+def _pot(engine, usr):
+    return engine.POT_TABLE if usr else engine.POT_HILLTOP
+
+
+def single_run(engine, tables, usr, N, seed, shape, af, steps, form=None):
+    w = _case(usr)
+    lat = engine.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], potential=_pot(engine, usr),
+                         form=engine.FORM_SPLIT if form is None else form)
+    if usr:
+        lat.set_table(*tables)
+    if form is None:
+        lat.set_shape(*shape)
+    H = lat.bunch_davies(seed, w["phi0"], w["dphi0"])
+    bg = engine.Bg(0.0, 1.0, H, 0.0, 1.0)
+    lat.evolve_fields(0.5 * w["dt"], bg)
+    taken = lat.leapfrog(af, steps, bg)
+    return lat, bg, taken
+
+
+def ensemble_run(engine, tables, usr, af, steps, Ns=NS, seeds=SEEDS, shapes=ROWS):
+    w = _case(usr)
+    ens = engine.Ensemble(Ns, w["L"], w["dt"], w["V0"], w["ns"], potential=_pot(engine, usr))
+    if usr:
+        ens.set_table(*tables)
+    if shapes is not None:
+        for N in sorted(set(Ns)):
+            ens.set_shape(N, *shapes[N])
+    hub = ens.bunch_davies(seeds, w["phi0"], w["dphi0"])
+    bg = ens.bgs(hub)
+    ens.evolve_fields(0.5 * w["dt"], bg)
+    taken = ens.leapfrog(af, steps, bg)
+    return ens, bg, taken
+
+
+def deltaN_single(engine, lat, bg, dN, Nend):
+    lat.initializeN(bg.a)
+    lat.evolve_fieldsN(0.5 * dN, 0.0)
+    phiref = lat.get_phiref()
+    n, Ne = 0, 0.0
+    while Ne <= Nend:
+        Ne += dN
+        n += 1
+    lat.deltaN_steps(dN, n, phiref)
+    lat.evolve_fieldsN(-0.5 * dN, phiref)
+    nmean = lat.saveN_mean(Nend - dN)
+    lat.shift(engine.DELTAN, nmean)
+    return phiref, nmean
+
+
+@pytest.mark.parametrize("usr,shapes", [(False, ROWS), (True, ROWS), (True, PLANES)])
+def test_ensemble_matches_single_lattices(usr, shapes, engine, tables):
+    w = _case(usr)
+    steps = 40
+    # lattice 2 stops on its own af, between the scale factors after steps 20 and 21
+    probe, pbg, _ = single_run(engine, tables, usr, NS[2], SEEDS[2], shapes[NS[2]], 1e30, 0)
+    with probe:
+        _, tr = probe.leapfrog(1e30, 25, pbg, trace=True)
+    af = np.full(len(NS), 1e30)
+    af[2] = 0.5 * (tr[19] + tr[20])
+    ens, ebg, etaken = ensemble_run(engine, tables, usr, af, steps, shapes=shapes)
+    with ens:
+        assert list(etaken) == [steps, steps, 21, steps]
+        # the end of run_evolution_loop: astep = a, then the half drift back
+        ds = []
+        for b in range(len(NS)):
+            ebg[b].astep = ebg[b].a
+            ds.append(w["dt"] / ebg[b].astep)
+        ens.evolve_fields(np.array(ds) * -0.5, ebg)
+        before = [ebg[b].as_tuple() for b in range(len(NS))]
+        fields = [(ens.download(b, engine.F), ens.download(b, engine.FD)) for b in range(len(NS))]
+        dN, Nend = 1e-4, 0.05
+        ephiref, enmean = ens.deltaN(ebg, dN, Nend)
+        spectra = ens.zeta_spectra()
+        for b, (N, seed) in enumerate(zip(NS, SEEDS)):
+            lat, bg, taken = single_run(engine, tables, usr, N, seed, shapes[N], af[b], steps)
+            with lat:
+                assert taken == etaken[b]
+                bg.astep = bg.a
+                lat.evolve_fields(-0.5 * w["dt"] / bg.astep, bg)
+                assert bg.as_tuple() == before[b], b
+                assert np.array_equal(lat.download(engine.F), fields[b][0]), b
+                assert np.array_equal(lat.download(engine.FD), fields[b][1]), b
+                phiref, nmean = deltaN_single(engine, lat, bg, dN, Nend)
+                assert phiref == ephiref[b] and np.float32(nmean) == enmean[b], b
+                zeta = lat.download(engine.DELTAN)
+                assert np.array_equal(zeta, ens.download(b, engine.DELTAN)), b
+                assert np.array_equal(lat.download(engine.F), ens.download(b, engine.F)), b
+                # spectraN of this lattice
+                lat.zero_above(engine.DELTAN, (Nend - dN) - float(nmean))
+                lat.shift(engine.DELTAN, lat.sum(engine.DELTAN) / N ** 3)
+                counts, f2 = lat.spectrum(engine.DELTAN)
+                assert np.array_equal(counts, spectra[b][0]) and np.array_equal(f2, spectra[b][1]), b
+
+
+def test_ensemble_zeta_histogram(engine, tables):
+    ens, bg, _ = ensemble_run(engine, tables, True, 1e30, 30)
+    with ens:
+        ens.deltaN(bg, 1e-4, 0.05)
+        h = ens.zeta_histogram(32, nbins=200, nsigma=10.0)
+        z = np.concatenate([ens.download(b, engine.DELTAN) for b, n in enumerate(NS) if n == 32])
+        sigma = np.sqrt(np.mean(z * z) - np.mean(z) ** 2)
+        assert abs(h["sigma"] - sigma) <= 1e-10 * sigma
+        assert h["lo"] == -10.0 * h["sigma"] and h["width"] == 20.0 * h["sigma"] / 200
+        u = (z - h["lo"]) / h["width"]
+        below, above = int(np.sum(~(u >= 0))), int(np.sum(u >= 200))
+        inside = u[(u >= 0) & (u < 200)]
+        ref = np.bincount(np.floor(inside).astype(np.int64), minlength=200)
+        assert np.array_equal(h["counts"], ref)
+        assert list(h["outside"]) == [below, above]
+        assert h["counts"].sum() + below + above == z.size
+
+
+def test_ensemble_against_fp64(engine, tables):
+    Ns, seeds = [32, 64], [11, 12]
+    steps = 300
+    ens, ebg, _ = ensemble_run(engine, tables, False, 1e30, steps, Ns=Ns, seeds=seeds, shapes=None)
+    with ens:
+        for b, (N, seed) in enumerate(zip(Ns, seeds)):
+            lat, bg, taken = single_run(engine, tables, False, N, seed, None, 1e30, steps, form=engine.FORM_FP64)
+            with lat:
+                assert taken == steps
+                for got, ref in ((ebg[b].a, bg.a), (ebg[b].ad, bg.ad), (ebg[b].t, bg.t)):
+                    assert abs(got - ref) <= 1e-9 * abs(ref)
+                for field in (engine.F, engine.FD):
+                    ref = lat.download(field)
+                    got = ens.download(b, field)
+                    assert np.max(np.abs(got - ref)) <= 1e-4 * np.std(ref - ref.mean())
+
+
+def test_ensemble_autotune_keeps_state(engine, tables):
+    ens, bg, _ = ensemble_run(engine, tables, True, 1e30, 5, shapes=None)
+    with ens:
+        before = [ens.download(b, engine.F) for b in range(len(NS))]
+        shape = ens.autotune(bg)
+        for b in range(len(NS)):
+            assert shape["rows"][b] in (4, 8, NS[b]) and shape["prefetch"][b] in (1, 2, 4)
+            assert 1 <= shape["chunks"][b] <= NS[b] // 8
+            assert np.array_equal(before[b], ens.download(b, engine.F))
+        steps = ens.leapfrog(1e30, 3, bg)
+        assert list(steps) == [3] * len(NS)

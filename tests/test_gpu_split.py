@@ -115,3 +115,23 @@ def test_split_autotune_keeps_state(engine, oracle_mod):
         o.leapfrog_steps(50)
         assert taken == 50
         assert pert_err(lat.download(engine.F), o.f) < 1e-4
+
+
+@pytest.mark.parametrize("N", [32, 64])
+def test_split_whole_plane_kernel(N, engine, oracle_mod, tables):
+    """The whole-plane step kernel (N <= 64) against the FP64 oracle and against
+    the row-tile kernel on the same state."""
+    p, o = oracle_state(oracle_mod, N, True, False, tables)
+    out = {}
+    for name, shape in (("plane", (N, 4, N // 16)), ("rows", (8, 2, N // 32))):
+        lat, bg = split_like(engine, p, o, True, False, tables)
+        with lat:
+            lat.set_shape(*shape)
+            assert lat.leapfrog(p.af, 200, bg) == 200
+            out[name] = (lat.download(engine.F), lat.download(engine.FD), bg.as_tuple())
+    o.leapfrog_steps(200)
+    for name in out:
+        assert pert_err(out[name][0], o.f) < 1e-4 and pert_err(out[name][1], o.fd) < 1e-4, name
+        assert abs(out[name][2][1] - o.scalars.a) <= 1e-9 * o.scalars.a
+    # the two kernels differ only in FP32 summation order
+    assert pert_err(out["plane"][0], out["rows"][0]) < 1e-5
