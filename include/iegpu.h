@@ -155,7 +155,10 @@ int  iegpu_profile_leapfrog(struct iegpu_ctx* ctx, double af, int nsteps, iegpu_
  * unchanged. */
 int  iegpu_autotune(struct iegpu_ctx* ctx, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
 /* Split form, 32 <= N <= 512: fix the step kernel's launch shape instead of
- * tuning it (rows 4 or 8, prefetch 1 or 2, 1 <= chunks <= N/8). */
+ * tuning it: rows per tile 4 or 8 with 1 or 2 planes prefetched (rows 4 at
+ * N >= 128 also 3 or 4), or rows = N for whole planes (N = 32, 64) with 2 or
+ * 4; 1 <= chunks <= N/8 plane chunks, or chunks = 0 (N >= 128) for one wave
+ * of CTAs that each take an equal share of the lattice. */
 int  iegpu_set_shape(struct iegpu_ctx* ctx, int rows, int prefetch, int chunks);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */

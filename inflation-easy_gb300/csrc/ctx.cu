@@ -271,8 +271,8 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
         if (phi[l - 1] == phi[l]) return set_error(c, IEGPU_ETABLE, "Interpolation failed due to repeated field grid points.\n");
         if (!(phi[l - 1] > phi[l])) return set_error(c, IEGPU_ETABLE, "field table must be sorted in descending order");
     }
-    // packed: x, V, dV, dxl, dyV, dydV, slopeV (n each) + keys
-    std::vector<double> h((size_t)7 * n, 0.0);
+    // packed: x, V, dV, dxl, dyV, dydV, slopeV, slopedV (n each) + keys
+    std::vector<double> h((size_t)8 * n, 0.0);
     std::vector<long long> k((size_t)n);
     for (int l = 0; l < n; ++l) {
         h[l] = phi[l];
@@ -284,6 +284,7 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
             h[4 * n + l] = V[l - 1] - V[l];
             h[5 * n + l] = dV[l - 1] - dV[l];
             h[6 * n + l] = (V[l - 1] - V[l]) / (phi[l - 1] - phi[l]);
+            h[7 * n + l] = (dV[l - 1] - dV[l]) / (phi[l - 1] - phi[l]);
         }
     }
     cudaFree(c->tab);
@@ -307,6 +308,7 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
     P.dyV = c->tab + 4 * n;
     P.dydV = c->tab + 5 * n;
     P.slopeV = c->tab + 6 * n;
+    P.slopedV = c->tab + 7 * n;
     P.key = c->tkey;
     fp64_destroy_graphs(c);  // graphs hold the potential by value
     split_destroy_graphs(c);

@@ -86,19 +86,23 @@ __device__ __forceinline__ EnsTile ens_tile(const EnsArgs& A, const int2* work, 
 
 template <bool TABLE, int C, int TJ, int PF>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_ens_rows(EnsArgs A, const int2* __restrict__ work) {
+    pdl_begin();
     const EnsTile t = ens_tile(A, work, TJ);
     rows_body<TABLE, C, TJ, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, t.j0, t.i0, t.CH, t.slot, t.nslots, t.st);
 }
 
 template <bool TABLE, int C4, int TJ, int PF>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_ens_rows4(EnsArgs A, const int2* __restrict__ work) {
+    pdl_begin();
     const EnsTile t = ens_tile(A, work, TJ);
-    rows4_body<TABLE, C4, TJ, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, t.j0, t.i0, t.CH, t.slot, t.nslots,
-                                  t.st);
+    constexpr int N = 128 * C4;
+    const long long u0 = (long long)(t.j0 / TJ) * N + t.i0;
+    rows4_body<TABLE, C4, TJ, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, u0, u0 + t.CH, t.slot, t.nslots, t.st);
 }
 
 template <bool TABLE, int N, int NT, int PF>
 __global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_ens_plane(EnsArgs A, const int2* __restrict__ work) {
+    pdl_begin();
     const EnsTile t = ens_tile(A, work, N);
     plane_body<TABLE, N, NT, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, t.i0, t.CH, t.slot, t.nslots, t.st);
 }
@@ -193,7 +197,8 @@ static size_t ens_smem(int N, int TJ, int PF) {
 static bool ens_shape_ok(int N, int TJ, int PF, int chunks) {
     if (chunks < 1 || chunks > N / 8) return false;
     if (ens_plane(N, TJ)) return PF == 2 || PF == 4;
-    return (TJ == 4 || TJ == 8) && (PF == 1 || PF == 2) && ens_smem(N, TJ, PF) <= 227 * 1024;
+    const bool deep = TJ == 4 && N >= 128 && (PF == 3 || PF == 4);
+    return (TJ == 4 || TJ == 8) && (PF == 1 || PF == 2 || deep) && ens_smem(N, TJ, PF) <= 227 * 1024;
 }
 
 static void ens_destroy_graph(iegpu_ens* e) {
@@ -210,7 +215,10 @@ static int ens_launch_class(iegpu_ens* e, const EnsClass& c, const EnsArgs& A, c
     const int nthr = ens_threads(N, TJ);
     const void* fn = nullptr;
 #define IEGPU_ENS_PICK(KERNEL) \
-    do { fn = reinterpret_cast<const void*>(&KERNEL); if (!set_attr) KERNEL<<<grid, nthr, c.smem, st>>>(A, c.work); } while (0)
+    do {                                                                                                   \
+        fn = reinterpret_cast<const void*>(&KERNEL);                                                       \
+        if (!set_attr) launch_pdl(KERNEL, dim3(grid), dim3(nthr), c.smem, st, A, (const int2*)c.work);     \
+    } while (0)
     if (ens_plane(N, TJ)) {
         if (N == 32) { if (PF == 4) IEGPU_ENS_PICK((k_ens_plane<TAB, 32, 256, 4>)); else IEGPU_ENS_PICK((k_ens_plane<TAB, 32, 256, 2>)); }
         else { if (PF == 4) IEGPU_ENS_PICK((k_ens_plane<TAB, 64, 512, 4>)); else IEGPU_ENS_PICK((k_ens_plane<TAB, 64, 512, 2>)); }
@@ -221,11 +229,19 @@ static int ens_launch_class(iegpu_ens* e, const EnsClass& c, const EnsArgs& A, c
         if (TJ == 4) { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows<TAB, 2, 4, 1>)); else IEGPU_ENS_PICK((k_ens_rows<TAB, 2, 4, 2>)); }
         else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows<TAB, 2, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows<TAB, 2, 8, 2>)); }
     } else if (N == 128) {
-        if (TJ == 4) { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 2>)); }
-        else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 8, 2>)); }
+        if (TJ == 4) {
+            if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 1>));
+            else if (PF == 2) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 2>));
+            else if (PF == 3) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 3>));
+            else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 4>));
+        } else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 8, 2>)); }
     } else {
-        if (TJ == 4) { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 2>)); }
-        else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 8, 2>)); }
+        if (TJ == 4) {
+            if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 1>));
+            else if (PF == 2) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 2>));
+            else if (PF == 3) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 3>));
+            else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 4>));
+        } else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 8, 2>)); }
     }
 #undef IEGPU_ENS_PICK
     if (set_attr)
@@ -252,10 +268,8 @@ static int ens_layout(iegpu_ens* e) {
         L.pslots = ens_prime_slots(e, N);
         L.part_off = (int)slots;
         slots += std::max(L.tiles, L.pslots);
-        L.K.dt = e->cfg.dt;
-        L.K.s = e->cfg.rescale_s;
-        L.K.dx = e->cfg.L / (double)N;
-        L.K.gs = (double)N * N * N;
+        L.K = make_split_const(e->cfg.dt, e->cfg.rescale_s, e->cfg.L / (double)N, (double)N * N * N,
+                               e->helper[0]->pot.B2);
         for (int s = 0; s < L.pslots; ++s) pw.push_back(make_int2(b, s));
     }
     if (int rc = ens_sync(e, "ensemble layout")) return rc;
@@ -485,7 +499,8 @@ static std::vector<int3> ens_candidates(const iegpu_ens* e, int N, int nlat) {
         for (int PF : {2, 4})
             for (int ch = N / 8; ch >= 1; ch /= 2) add(N, PF, ch);
     for (int TJ : {4, 8})
-        for (int PF : {1, 2}) {
+        for (int PF : {1, 2, 3, 4}) {
+            if (PF > 2 && (TJ != 4 || N < 128)) continue;
             // one or two waves of the whole class at an estimated 3 CTAs per SM
             const int per_lat = N / TJ;
             for (int waves : {1, 2}) add(TJ, PF, (waves * 3 * e->sms) / (per_lat * (nlat > 0 ? nlat : 1)));

@@ -64,7 +64,8 @@ struct PotDev {
     const double* dxl;      // x[l-1] - x[l]
     const double* dyV;      // V[l-1] - V[l]
     const double* dydV;     // dV[l-1] - dV[l]
-    const double* slopeV;   // dyV/dxl (reductions only)
+    const double* slopeV;   // dyV/dxl
+    const double* slopedV;  // dydV/dxl
 };
 
 // Split form (FP32 perturbations about an FP64 background).
@@ -93,10 +94,27 @@ struct SplitCtl {
 };
 
 // Per-lattice constants of the split step: base step, rescaling exponent,
-// lattice spacing, number of sites.
+// lattice spacing, number of sites, and the reciprocals the per-step scalar
+// update multiplies by (1/dt, 1/dx, 1/dx^2, 1/N^3, 1/(s+1), 1/B^2).
 struct SplitConst {
     double dt, s, dx, gs;
+    double idt, idx, idx2, igs, isfev1, iB2;
 };
+
+inline SplitConst make_split_const(double dt, double s, double dx, double gs, double B2) {
+    SplitConst K;
+    K.dt = dt;
+    K.s = s;
+    K.dx = dx;
+    K.gs = gs;
+    K.idt = 1.0 / dt;
+    K.idx = 1.0 / dx;
+    K.idx2 = 1.0 / (dx * dx);
+    K.igs = 1.0 / gs;
+    K.isfev1 = 1.0 / (s + 1.0);
+    K.iB2 = 1.0 / B2;
+    return K;
+}
 
 // Launch shape of the split row kernel (chosen by the autotuner).
 struct RowCfg {

@@ -38,16 +38,21 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
 }
 
 // Sum of part[b*NV + q] over b = 0..nb-1 by warp 0 in a fixed order; the
-// result is valid in lane 0.
+// result is valid in lane 0.  Each lane walks its slots once for all NV
+// values, several slots' loads in flight.
 template <int NV>
 __device__ __forceinline__ void sum_partials(const double* part, int nb, double (&out)[NV]) {
     const int lane = threadIdx.x & 31;
+    double s[NV];
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-        double s = 0.0;
-        for (int b = lane; b < nb; b += 32) s += __ldcg(&part[(size_t)b * NV + q]);
-        out[q] = warp_sum(s);
+    for (int q = 0; q < NV; ++q) s[q] = 0.0;
+#pragma unroll 4
+    for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) s[q] += __ldcg(&part[(size_t)b * NV + q]);
     }
+#pragma unroll
+    for (int q = 0; q < NV; ++q) out[q] = warp_sum(s[q]);
 }
 
 // Last-CTA detection after each CTA wrote its partials.

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    double v[3] = {g.value(), s1.value(), s2.value()};
+    df64 v[3] = {g.df(), s1.df(), s2.df()};
     finish_sums(v, ctl, P, K, part, counter, a_trace);
 }
 template <bool TABLE, int C, int TJ, int PF>
@@ -198,6 +198,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
                                                               double* part, unsigned* counter, double* a_trace,
                                                               int chunks) {
     constexpr int N = 32 * C;
+    pdl_begin();
     const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
     const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
     rows_body<TABLE, C, TJ, PF>(B, ctl, P, K, part, counter, a_trace, blockIdx.x * TJ, i0, CH,
@@ -210,16 +211,28 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, Spli
                                                                double* part, unsigned* counter, double* a_trace,
                                                                int chunks) {
     constexpr int N = 128 * C4;
-    const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
-    const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
-    rows4_body<TABLE, C4, TJ, PF>(B, ctl, P, K, part, counter, a_trace, blockIdx.x * TJ, i0, CH,
-                                  blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr);
+    pdl_begin();
+    long long u0, u1;
+    if (chunks == 0) {
+        // balanced: CTA c takes an equal share of the (row tile, plane) units
+        const long long total = (long long)(N / TJ) * N;
+        u0 = total * blockIdx.x / gridDim.x;
+        u1 = total * (blockIdx.x + 1) / gridDim.x;
+    } else {
+        const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
+        const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
+        u0 = (long long)blockIdx.x * N + i0;
+        u1 = u0 + CH;
+    }
+    rows4_body<TABLE, C4, TJ, PF>(B, ctl, P, K, part, counter, a_trace, u0, u1, blockIdx.x + gridDim.x * blockIdx.y,
+                                  gridDim.x * gridDim.y, nullptr);
 }
 
 // Whole planes (N = 32, 64): block y = chunk of planes.
 template <bool TABLE, int N, int NT, int PF>
 __global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_split_plane(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
                                                     unsigned* counter, double* a_trace, int chunks) {
+    pdl_begin();
     const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
     const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
     plane_body<TABLE, N, NT, PF>(B, ctl, P, K, part, counter, a_trace, i0, CH, blockIdx.x + gridDim.x * blockIdx.y,
@@ -374,12 +387,7 @@ __global__ void __launch_bounds__(kThreads) k_split_sums(const float* __restrict
 // ---------------------------------------------------------------------------
 
 static SplitConst split_const(const iegpu_ctx* c) {
-    SplitConst K;
-    K.dt = c->cfg.dt;
-    K.s = c->cfg.rescale_s;
-    K.dx = c->cfg.L / (double)c->N;
-    K.gs = (double)c->gs;
-    return K;
+    return make_split_const(c->cfg.dt, c->cfg.rescale_s, c->cfg.L / (double)c->N, (double)c->gs, c->pot.B2);
 }
 
 struct StepGeom {
@@ -387,6 +395,10 @@ struct StepGeom {
     size_t smem;
     bool rows;   // full-row kernel (32 <= N <= 512)
 };
+
+// chunks == 0 (N >= 128): one wave of CTAs, each with an equal share of the
+// (row tile, plane) units, so every SM carries the same load.
+static int balanced_ctas(const iegpu_ctx* c, int N, int TJ, int PF);
 
 // Shared memory one row-kernel CTA needs, and how many fit on an SM.  TJ = N
 // (N <= 64) selects the whole-plane kernel.
@@ -406,6 +418,13 @@ static int row_ctas_per_sm(int N, int TJ, int PF) {
     const int by_regs = 65536 / (nthr * 72);
     int n = by_smem < by_regs ? by_smem : by_regs;
     return n < 1 ? (smem <= 227 * 1024 ? 1 : 0) : n;
+}
+
+static int balanced_ctas(const iegpu_ctx* c, int N, int TJ, int PF) {
+    const int per_sm = row_ctas_per_sm(N, TJ, PF);
+    const long long units = (long long)(N / TJ) * N;
+    long long n = (long long)c->sms * (per_sm > 0 ? per_sm : 1);
+    return (int)(n < units ? n : units);
 }
 
 // Untuned choice: 8-row tiles (4 at N = 512), two planes prefetched, and a
@@ -434,9 +453,9 @@ static StepGeom step_geom(const iegpu_ctx* c) {
         if (rc.TJ == 0) rc = default_row_cfg(c);
         g.TJ = rc.TJ;
         g.PF = rc.PF;
-        g.tiles = N / g.TJ;
         g.chunks = rc.chunks;
-        g.CH = N / rc.chunks;
+        g.tiles = rc.chunks > 0 ? N / g.TJ : balanced_ctas(c, N, g.TJ, g.PF);
+        g.CH = rc.chunks > 0 ? N / rc.chunks : 0;
         g.smem = row_smem_bytes(N, g.TJ, g.PF);
         return g;
     }
@@ -482,8 +501,8 @@ static void rows_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
         cudaFuncSetAttribute(k_split_rows<TAB, CC, TJV, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
         attr = g.smem;
     }
-    k_split_rows<TAB, CC, TJV, PFV><<<grid, (TJV + 1) * 32, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part,
-                                                                                  c->counter, c->a_trace, g.chunks);
+    launch_pdl(k_split_rows<TAB, CC, TJV, PFV>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot, K,
+               c->part, c->counter, c->a_trace, g.chunks);
 }
 
 template <bool TAB, int C4, int TJV, int PFV>
@@ -493,8 +512,8 @@ static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim
         cudaFuncSetAttribute(k_split_rows4<TAB, C4, TJV, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
         attr = g.smem;
     }
-    k_split_rows4<TAB, C4, TJV, PFV><<<grid, (TJV + 1) * 32, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part,
-                                                                                   c->counter, c->a_trace, g.chunks);
+    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot, K,
+               c->part, c->counter, c->a_trace, g.chunks);
 }
 
 template <bool TAB, int NV, int PFV>
@@ -505,8 +524,8 @@ static void plane_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim
         cudaFuncSetAttribute(k_split_plane<TAB, NV, NT, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
         attr = g.smem;
     }
-    k_split_plane<TAB, NV, NT, PFV><<<grid, NT, g.smem, c->stream>>>(B, c->sctl, c->pot, K, c->part, c->counter,
-                                                                     c->a_trace, g.chunks);
+    launch_pdl(k_split_plane<TAB, NV, NT, PFV>, grid, dim3(NT), g.smem, c->stream, B, c->sctl, c->pot, K, c->part,
+               c->counter, c->a_trace, g.chunks);
 }
 
 template <bool TAB, int NV>
@@ -517,8 +536,20 @@ static void plane_pf(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
 
 template <bool TAB, int C4>
 static void rows4_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
-    if (g.TJ == 4) { if (g.PF == 1) rows4_one<TAB, C4, 4, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 4, 2>(c, B, K, grid, g); }
-    else { if (g.PF == 1) rows4_one<TAB, C4, 8, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 8, 2>(c, B, K, grid, g); }
+    if (g.TJ == 4) {
+        switch (g.PF) {
+            case 1: rows4_one<TAB, C4, 4, 1>(c, B, K, grid, g); break;
+            case 2: rows4_one<TAB, C4, 4, 2>(c, B, K, grid, g); break;
+            case 3: rows4_one<TAB, C4, 4, 3>(c, B, K, grid, g); break;
+            default: rows4_one<TAB, C4, 4, 4>(c, B, K, grid, g); break;
+        }
+    } else if (g.TJ == 8) {
+        if (g.PF == 1) rows4_one<TAB, C4, 8, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 8, 2>(c, B, K, grid, g);
+    } else if (C4 <= 2) {
+        // 16-row tiles: one CTA of 17 warps per SM
+        if (g.PF == 1) rows4_one<TAB, (C4 <= 2 ? C4 : 2), 16, 1>(c, B, K, grid, g);
+        else rows4_one<TAB, (C4 <= 2 ? C4 : 2), 16, 2>(c, B, K, grid, g);
+    }
 }
 
 template <bool TAB, int CC>
@@ -554,7 +585,7 @@ static void launch_step(iegpu_ctx* c, int src) {
     }
     const StepGeom g = step_geom(c);
     SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
-    dim3 grid(g.tiles, g.chunks);
+    dim3 grid(g.tiles, g.chunks > 0 ? g.chunks : 1);
     if (g.rows) {
         launch_rows(c, B, K, grid, g);
         return;
@@ -661,12 +692,20 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
                     cands.push_back(r);
                 }
     }
-    for (int TJ : {4, 8}) {
-        if (TJ > N) continue;
-        for (int PF : {1, 2}) {
+    for (int TJ : {4, 8, 16}) {
+        if (TJ > N || (TJ == 16 && (N < 128 || N > 256))) continue;
+        for (int PF : {1, 2, 3, 4}) {
+            if (PF > 2 && (TJ != 4 || N < 128)) continue;
             const int per_sm = row_ctas_per_sm(N, TJ, PF);
             if (per_sm < 1) continue;
             const int tiles = N / TJ;
+            if (N >= 128) {
+                RowCfg r;
+                r.TJ = TJ;
+                r.PF = PF;
+                r.chunks = 0;   // balanced
+                cands.push_back(r);
+            }
             for (int waves : {1, 2}) {
                 int ch = (waves * c->sms * per_sm) / tiles;
                 if (ch < 1) ch = 1;
@@ -714,12 +753,17 @@ int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     const int N = c->N;
     if (N < 32 || N > 512) return set_error(c, IEGPU_EUNSUPPORTED, "the row kernel covers 32 <= N <= 512");
     const bool plane = plane_shape(N, rows);
-    if ((!plane && ((rows != 4 && rows != 8) || (prefetch != 1 && prefetch != 2))) ||
-        (plane && prefetch != 2 && prefetch != 4) || chunks < 1 || chunks > N / 8)
+    const bool deep = rows == 4 && N >= 128 && (prefetch == 3 || prefetch == 4);
+    const bool balanced = chunks == 0 && !plane && N >= 128;
+    const bool wide = rows == 16 && N >= 128 && N <= 256;
+    if ((!plane && ((rows != 4 && rows != 8 && !wide) || ((prefetch != 1 && prefetch != 2) && !deep))) ||
+        (plane && prefetch != 2 && prefetch != 4) || (!balanced && (chunks < 1 || chunks > N / 8)))
         return set_error(c, IEGPU_EINVAL,
-                         "shape: rows 4|8 with prefetch 1|2, or rows N (N <= 64, whole planes) with prefetch 2|4; "
-                         "1 <= chunks <= N/8");
-    if (3LL * (N / rows) * chunks > c->part_cap || row_ctas_per_sm(N, rows, prefetch) < 1)
+                         "shape: rows 4|8 with prefetch 1|2 (rows 4 and N >= 128 also 3|4), or rows N "
+                         "(N <= 64, whole planes) with prefetch 2|4; 1 <= chunks <= N/8, or chunks 0 "
+                         "(N >= 128: one wave of CTAs with equal shares)");
+    const long long ctas = balanced ? balanced_ctas(c, N, rows, prefetch) : (long long)(N / rows) * chunks;
+    if (3LL * ctas > c->part_cap || row_ctas_per_sm(N, rows, prefetch) < 1)
         return set_error(c, IEGPU_EINVAL, "shape does not fit this lattice's scratch");
     c->row_cfg.TJ = rows;
     c->row_cfg.PF = prefetch;

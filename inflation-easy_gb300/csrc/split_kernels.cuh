@@ -75,6 +75,145 @@ __device__ __forceinline__ float split_v(float x, const float* wv, int nv, const
 }
 
 // ---------------------------------------------------------------------------
+// Kahan accumulator
+// ---------------------------------------------------------------------------
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ struct df64 df() const;
+};
+
+// ---------------------------------------------------------------------------
+// double-float arithmetic
+// ---------------------------------------------------------------------------
+//
+// A value hi + lo held in two floats (about 44 significant bits), with the
+// error-free sum and product of Dekker and Knuth built on FP32 adds and FMAs.
+// GB300's FP64 operations have hundreds of cycles of latency; these run on
+// the FP32 pipes.  The _rn intrinsics keep the compiler from contracting or
+// reassociating the error terms.
+struct df64 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df64 df_make(float h) { return df64{h, 0.f}; }
+
+__device__ __forceinline__ df64 df_quick(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return df64{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return df64{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ df64 df_add(df64 a, df64 b) {
+    const df64 s = df_two_sum(a.hi, b.hi);
+    const df64 t = df_two_sum(a.lo, b.lo);
+    const df64 u = df_quick(s.hi, __fadd_rn(s.lo, t.hi));
+    return df_quick(u.hi, __fadd_rn(u.lo, t.lo));
+}
+
+__device__ __forceinline__ df64 df_neg(df64 a) { return df64{-a.hi, -a.lo}; }
+__device__ __forceinline__ df64 df_sub(df64 a, df64 b) { return df_add(a, df_neg(b)); }
+
+__device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_quick(p, e);
+}
+
+// a / b: a float quotient and two corrections from the df64 remainder
+__device__ __forceinline__ df64 df_div(df64 a, df64 b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    df64 r = df_sub(a, df_mul(b, df_make(q1)));
+    const float q2 = __fdiv_rn(r.hi, b.hi);
+    const df64 q = df_quick(q1, q2);
+    r = df_sub(a, df_mul(b, q));
+    return df_add(q, df_make(__fdiv_rn(r.hi, b.hi)));
+}
+
+// sqrt(a), a > 0: the float root and one Newton correction in df64
+__device__ __forceinline__ df64 df_sqrt(df64 a) {
+    if (!(a.hi > 0.f)) return df64{0.f, 0.f};
+    const float s = __fsqrt_rn(a.hi);
+    const df64 r = df_sub(a, df_mul(df_make(s), df_make(s)));
+    return df_quick(s, __fdiv_rn(r.hi, __fmul_rn(2.f, s)));
+}
+
+__device__ __forceinline__ df64 df_from(double x) {
+    const float h = __double2float_rn(x);
+    return df64{h, __double2float_rn(x - (double)h)};
+}
+
+__device__ __forceinline__ double df_to(df64 a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ df64 df_shfl_down(df64 v, int o) {
+    return df64{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+__device__ __forceinline__ df64 Kahan::df() const { return df_two_sum(s, -c); }
+
+// Sum over the block of NV df64 values per thread in a fixed order (lane
+// trees, then warps in index order); result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum_df(df64 (&v)[NV]) {
+    __shared__ df64 sh[NV][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] = df_add(v[q], df_shfl_down(v[q], o));
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[q][w] = v[q];
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (int)(blockDim.x >> 5);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            v[q] = lane < nw ? sh[q][lane] : df64{0.f, 0.f};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[q] = df_add(v[q], df_shfl_down(v[q], o));
+        }
+    }
+    __syncthreads();
+}
+
+// Sum of the df64 partials p[b*NV + q], b < nb, by one warp in a fixed order;
+// result valid in lane 0.
+template <int NV>
+__device__ __forceinline__ void sum_partials_df(const df64* p, int nb, df64 (&out)[NV]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) out[q] = df64{0.f, 0.f};
+#pragma unroll 4
+    for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const float2 x = __ldcg(reinterpret_cast<const float2*>(p) + (size_t)b * NV + q);
+            out[q] = df_add(out[q], df64{x.x, x.y});
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) out[q] = df_add(out[q], df_shfl_down(out[q], o));
+}
+
+// ---------------------------------------------------------------------------
 // scalar update (one warp): Friedmann, background, coefficients, windows
 // ---------------------------------------------------------------------------
 //
@@ -99,9 +238,10 @@ __device__ __forceinline__ bool table_out_of_range(const PotDev& P, double v) {
     return !is_nan_bits(v) && (kv > __ldg(&P.key[0]) || kv < __ldg(&P.key[P.n - 1]));
 }
 
-// build_window by a warp: lane q writes node q and bracket q.
-__device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, const double* y, const double* dy,
-                                                  double phibar, int* err) {
+// build_window by a warp: lane q writes node q and bracket q.  slope[l] =
+// dy[l] / dxl[l], precomputed on the host (the same IEEE quotient).
+__device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, const double* y,
+                                                  const double* slope, double phibar, int* err) {
     const int lane = threadIdx.x & 31;
     if (lane == 0) W.ok = 0;
     if (!P.table) return;
@@ -115,11 +255,11 @@ __device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, 
     int n = kWin;
     if (l0 + n - 1 > P.n - 1) n = P.n - 1 - l0 + 1;
     // value of the tabulated function at phibar (its own bracket)
-    const double Fbar = y[lb] + (phibar - P.x[lb]) * (dy[lb] / P.dxl[lb]);
+    const double Fbar = y[lb] + (phibar - P.x[lb]) * slope[lb];
     if (lane <= n) W.u[lane] = (float)(P.x[l0 - 1 + lane] - phibar);
     if (lane < n) {
         const int l = l0 + lane;
-        const double s = dy[l] / P.dxl[l];
+        const double s = slope[l];
         W.s[lane] = (float)s;
         W.A[lane] = (float)((y[l] + (phibar - P.x[l]) * s) - Fbar);
     }
@@ -130,75 +270,96 @@ __device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, 
     }
 }
 
-// V(phibar)/B^2 and V'(phibar)/B^2 (src/potential.cpp:77-98), by a warp
-__device__ __forceinline__ void bar_potential_warp(const PotDev& P, double phibar, double* V, double* dV) {
+// V(phibar) and V'(phibar) times B^2 (src/potential.cpp:77-98) for the
+// bracket l of phibar (table) or the hilltop formula.
+__device__ __forceinline__ void bar_potential_at(const PotDev& P, double phibar, int l, double* V, double* dV) {
     if (P.table) {
-        const int l = warp_bracket(P, phibar);
-        *V = table_interp(P, P.V, P.dyV, phibar, l) / P.B2;
-        *dV = table_interp(P, P.dV, P.dydV, phibar, l) / P.B2;
+        const double u = phibar - P.x[l];
+        *V = P.V[l] + u * P.slopeV[l];
+        *dV = P.dV[l] + u * P.slopedV[l];
     } else {
-        *V = (P.V0 * (1.0 - P.c1 * (phibar * phibar))) / P.B2;
-        *dV = (P.c2 * phibar) / P.B2;
+        *V = P.V0 * (1.0 - P.c1 * (phibar * phibar));
+        *dV = P.c2 * phibar;
     }
 }
 
 // sums: [0] sum of squared forward differences of dphi, [1] sum dphi,
 // [2] hilltop: sum dphi^2 / table: sum of V differences (table units).
-// Called by the 32 lanes of one warp with the same sums.
+// Called by the 32 lanes of one warp with the same sums.  GB300's FP64 pipe
+// is narrow and a dependent FP64 operation takes hundreds of cycles, so the
+// recurrences run on lane 0 alone and multiply by precomputed reciprocals:
+// one division (1/a, beside d) and one square root lie on the path from the
+// sums to the next step's coefficients.  The table searches and window nodes
+// are shared out over the lanes.
 static __device__ __noinline__ void split_scalars_warp(SplitCtl& C, const PotDev& P, const SplitConst& K,
                                                        const double* sums, double* a_trace) {
     const bool w0 = (threadIdx.x & 31) == 0;
     const int mode = C.mode, steps_done = C.steps_done, steps_limit = C.steps_limit, error0 = C.error;
-    double t = C.bg.t, a = C.bg.a, ad = C.bg.ad, astep = C.bg.astep;
-    double phibar = C.phibar, pibar = C.pibar;
-    const double af = C.af, d_given = C.d_given;
+    const double phibar0 = C.phibar;
     __syncwarp();   // every lane has read the control block before lane 0 writes it
-    double d;
     if (mode == kModeLeapfrog) {
+        // the stop checks read the same values in every lane
         if (steps_done >= steps_limit) {
             if (w0) { C.active = 0; C.done = 1; }
             return;
         }
-        if (steps_done > 0) astep = a;
-        if (!(a <= af)) {
-            if (w0) { C.bg.astep = astep; C.active = 0; C.done = 1; }
+        const double a0 = C.bg.a, af = C.af;
+        if (!(a0 <= af)) {
+            if (w0) {
+                if (steps_done > 0) C.bg.astep = a0;
+                C.active = 0;
+                C.done = 1;
+            }
             return;
         }
-        d = K.dt * pow_exp(astep, K.s - 1.0);
-    } else {
-        d = d_given;
     }
-    const double s = K.s;
-    const double grad = 0.5 * sums[0] * ((1.0 / (a * K.dx)) * (1.0 / (a * K.dx))) / K.gs;
-    double Vbar, dVbar;
-    bar_potential_warp(P, phibar, &Vbar, &dVbar);
-    double pot;
-    if (P.table) pot = Vbar + (sums[2] / P.B2) / K.gs;
-    else pot = Vbar - (P.V0 * P.c1 / P.B2) * (2.0 * phibar * sums[1] + sums[2]) / K.gs;
-    const double sfev1 = s + 1.0, sfev2 = -2.0 * s + 2.0;
-    const double ad2 = (-2.0 * ad - 2.0 * a / d / sfev1 *
-                        (1.0 - sqrt(1.0 + 2.0 * d * sfev1 * ad / a +
-                                    (d * d) * sfev1 * pow_exp(a, sfev2) * (2.0 * grad / 3.0 + pot)))) / d;
-    ad += 0.5 * d * ad2;
-    const double laplnorm = pow_exp(a, -2.0 * s) / (K.dx * K.dx);
-    const double friction = (2.0 + s) * ad / a;
-    const double potnorm = pow_exp(a, 2.0 - 2.0 * s);
-    const double srcAmp = 2.0 * pow_exp(a, -2.0 * s);
-    ad += 0.5 * d * ad2;
-    // background kick (homogeneous mode of the lattice kick)
-    pibar = pibar + d * (-friction * pibar - potnorm * dVbar);
-    int err = 0;
-    build_window_warp(C.wk, P, P.dV, P.dydV, phibar, &err);
-    if (mode == kModeLeapfrog) {
-        phibar = phibar + d * pibar;
-        t += d;
-    }
+    const int lbar = P.table ? warp_bracket(P, phibar0) : 0;
+    double phibar_new = phibar0;
     if (w0) {
+        double t = C.bg.t, a = C.bg.a, ad = C.bg.ad, astep = C.bg.astep;
+        double phibar = phibar0, pibar = C.pibar;
+        const double s = K.s;
+        double d, rd;
+        if (mode == kModeLeapfrog) {
+            if (steps_done > 0) astep = a;
+            // d = dt astep^(s-1), 1/d = astep^(1-s) / dt
+            if (s == 0.0) {
+                d = K.dt / astep;
+                rd = astep * K.idt;
+            } else {
+                d = K.dt * pow_exp(astep, s - 1.0);
+                rd = pow_exp(astep, 1.0 - s) * K.idt;
+            }
+        } else {
+            d = C.d_given;
+            rd = 1.0 / d;
+        }
+        const double ra = 1.0 / a;
+        const double g1 = ra * K.idx;
+        const double grad = 0.5 * sums[0] * (g1 * g1) * K.igs;
+        double Vb, dVb;   // times B^2
+        bar_potential_at(P, phibar, lbar, &Vb, &dVb);
+        double pot;
+        if (P.table) pot = (Vb + sums[2] * K.igs) * K.iB2;
+        else pot = (Vb - P.V0 * P.c1 * (2.0 * phibar * sums[1] + sums[2]) * K.igs) * K.iB2;
+        const double sfev1 = s + 1.0, sfev2 = -2.0 * s + 2.0;
+        const double a_sfev2 = (s == 0.0) ? a * a : pow_exp(a, sfev2);
+        const double x = 2.0 * d * sfev1 * ad * ra + (d * d) * sfev1 * a_sfev2 * (2.0 * grad * (1.0 / 3.0) + pot);
+        const double ad2 = (-2.0 * ad - 2.0 * a * rd * K.isfev1 * (1.0 - sqrt(1.0 + x))) * rd;
+        ad += 0.5 * d * ad2;
+        const double a_m2s = (s == 0.0) ? 1.0 : pow_exp(a, -2.0 * s);
+        const double laplnorm = a_m2s * K.idx2;
+        const double friction = (2.0 + s) * ad * ra;
+        const double potnorm = (s == 0.0) ? a * a : pow_exp(a, 2.0 - 2.0 * s);
+        const double srcAmp = 2.0 * a_m2s;
+        ad += 0.5 * d * ad2;
+        // background kick (homogeneous mode of the lattice kick)
+        pibar = pibar + d * (-friction * pibar - potnorm * (dVb * K.iB2));
         C.d = (float)d;
         C.lapl = (float)laplnorm;
         C.fric = (float)friction;
-        C.pn = (float)(potnorm / P.B2);
-        C.kv = (float)(potnorm * P.c2 / P.B2);
+        C.pn = (float)(potnorm * K.iB2);
+        C.kv = (float)(potnorm * P.c2 * K.iB2);
         C.srcAmp = (float)srcAmp;
         C.dd = d;
         C.bg.astep = astep;
@@ -207,15 +368,21 @@ static __device__ __noinline__ void split_scalars_warp(SplitCtl& C, const PotDev
         C.pibar = pibar;
         C.active = 1;
         if (mode == kModeLeapfrog) {
+            phibar = phibar + d * pibar;
+            t += d;
             C.phibar = phibar;
             C.bg.t = t;
             C.bg.a = a + d * ad;
             if (a_trace) a_trace[steps_done] = C.bg.a;
             C.steps_done = steps_done + 1;
         }
+        phibar_new = phibar;
     }
-    build_window_warp(C.wv, P, P.V, P.dyV, phibar, &err);
-    if (err && !error0 && w0) { C.error = IEGPU_ERANGE; C.errval = phibar; C.active = 0; C.done = 1; }
+    phibar_new = __shfl_sync(0xffffffffu, phibar_new, 0);
+    int err = 0;
+    build_window_warp(C.wk, P, P.dV, P.slopedV, phibar0, &err);
+    build_window_warp(C.wv, P, P.V, P.slopeV, phibar_new, &err);
+    if (err && !error0 && w0) { C.error = IEGPU_ERANGE; C.errval = phibar_new; C.active = 0; C.done = 1; }
 }
 
 // One lane, for the diagnostics that build a window outside the step.
@@ -243,34 +410,20 @@ static __device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, c
     W.ok = 1;
 }
 
-// ---------------------------------------------------------------------------
-// Kahan accumulator
-// ---------------------------------------------------------------------------
-
-struct Kahan {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float v) {
-        const float y = v - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
 // Block sums into partial slot `slot` of `nslots`; the last of the nslots CTAs
 // to arrive adds the partials in slot order and runs the scalar update.
 // `state` (may be null) is the ensemble form's per-lattice word: that CTA
 // toggles its bit 0 (the ping-pong half) after a step (`toggle`), and sets
 // bit 1 once the lattice has stopped.
-__device__ __forceinline__ void finish_sums_slot(double (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+__device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                                  double* part, unsigned* counter, double* a_trace, int slot,
                                                  int nslots, int* state, bool toggle) {
-    block_sum<3>(v);
+    block_sum_df<3>(v);
+    df64* pd = reinterpret_cast<df64*>(part);   // one df64 per double slot
     if (threadIdx.x == 0) {
-        part[3 * slot] = v[0];
-        part[3 * slot + 1] = v[1];
-        part[3 * slot + 2] = v[2];
+        pd[3 * slot] = v[0];
+        pd[3 * slot + 1] = v[1];
+        pd[3 * slot + 2] = v[2];
     }
     __shared__ bool last;
     __threadfence();
@@ -279,32 +432,36 @@ __device__ __forceinline__ void finish_sums_slot(double (&v)[3], SplitCtl* ctl, 
     __syncthreads();
     if (!last) return;
     if (threadIdx.x < 32) {
-        double tot[3];
-        sum_partials<3>(part, nslots, tot);
+        df64 tot[3];
+        sum_partials_df<3>(pd, nslots, tot);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) tot[q] = __shfl_sync(0xffffffffu, tot[q], 0);
+        for (int q = 0; q < 3; ++q) {
+            tot[q].hi = __shfl_sync(0xffffffffu, tot[q].hi, 0);
+            tot[q].lo = __shfl_sync(0xffffffffu, tot[q].lo, 0);
+        }
         SplitCtl& C = *ctl;
+        const double sums[3] = {df_to(tot[0]), df_to(tot[1]), df_to(tot[2])};
         int error = 0;
         if (threadIdx.x == 0) {
             *counter = 0;
             if (state && toggle) *state ^= 1;
-            C.sums[0] = tot[0];
-            C.sums[1] = tot[1];
-            C.sums[2] = tot[2];
+            C.sums[0] = sums[0];
+            C.sums[1] = sums[1];
+            C.sums[2] = sums[2];
             error = C.error;
         }
         error = __shfl_sync(0xffffffffu, error, 0);
         if (error) {
             if (threadIdx.x == 0) { C.active = 0; C.done = 1; }
         } else {
-            split_scalars_warp(C, P, K, tot, a_trace);
+            split_scalars_warp(C, P, K, sums, a_trace);
         }
         __syncwarp();
         if (threadIdx.x == 0 && state && C.done) *state |= 2;
     }
 }
 
-__device__ __forceinline__ void finish_sums(double (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+__device__ __forceinline__ void finish_sums(df64 (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                             double* part, unsigned* counter, double* a_trace) {
     finish_sums_slot(v, ctl, P, K, part, counter, a_trace, blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y,
                      nullptr, false);
@@ -323,7 +480,7 @@ __device__ __forceinline__ void prime_body(const float* __restrict__ x, SplitCtl
     if (TABLE && threadIdx.x < 32) {
         // every CTA forms the window around the current phibar itself
         int err = 0;
-        build_window_warp(W, P, P.V, P.dyV, ctl->phibar, &err);
+        build_window_warp(W, P, P.V, P.slopeV, ctl->phibar, &err);
         __syncwarp();
         if (threadIdx.x == 0) sn = err ? -1 : W.n;
         if (!err) {
@@ -356,7 +513,7 @@ __device__ __forceinline__ void prime_body(const float* __restrict__ x, SplitCtl
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    double v[3] = {g.value(), s1.value(), s2.value()};
+    df64 v[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, false);
 }
 
@@ -378,6 +535,31 @@ __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+// Programmatic dependent launch: a step kernel lets the next one be launched
+// at once (its CTAs take SM slots as this kernel's CTAs exit) and waits for
+// the previous kernel to complete before it reads anything that kernel
+// wrote.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 template <int n>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory"); }
 
@@ -535,7 +717,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    double v[3] = {g.value(), s1.value(), s2.value()};
+    df64 v[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
 
@@ -554,8 +736,8 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 
 template <bool TABLE, int C4, int TJ, int PF>
 __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
-                                           double* part, unsigned* counter, double* a_trace, int j0, int i0, int CH,
-                                           int slot, int nslots, int* state) {
+                                           double* part, unsigned* counter, double* a_trace, long long u0,
+                                           long long u1, int slot, int nslots, int* state) {
     constexpr int N = 128 * C4, m = N - 1;
     constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
     constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
@@ -589,140 +771,148 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     const int nk = nk_s, nv = nv_s;
     const WinCache ck = win_cache<TABLE>(wk, nk), cv = win_cache<TABLE>(wv, nv);
 
-    auto issue_phi = [&](int i) {
-        float* dst = ring + ((i - i0 + 1) % PHS) * RP;
-        const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
-        constexpr int ops = (TJ + 3) * (N / 4);
-        for (int o = tid; o < ops; o += NTH) {
-            const int r = o / (N / 4), q = o - r * (N / 4);
-            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
-        }
-    };
-    auto issue_pi = [&](int i) {
-        float* dst = pis + ((i - i0) % PIS) * PP;
-        const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
-        constexpr int ops = (TJ + 1) * (N / 4);
-        for (int o = tid; o < ops; o += NTH) {
-            const int r = o / (N / 4), q = o - r * (N / 4);
-            cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
-        }
-    };
-
     Kahan g, s1, s2;
     bool bad = false;
     const int jl = w;
     const bool interior = jl < TJ;
-    float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
-    issue_phi(i0 - 1);
-    issue_phi(i0);
-    cp_commit();
-    for (int q = 0; q < PF; ++q) {
-        if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
-        if (q <= CH) issue_pi(i0 + q);
-        cp_commit();
-    }
-    // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
-    auto diffs = [&](int p, bool kj) {
-        const float* nr = nb + ((p - 1) & 1) * NBP;
-        float rg = 0.f;
-#pragma unroll
-        for (int v = 0; v < C4; ++v) {
-            const int k = 4 * (lane + 32 * v);
-            const float4 xc = xp1[v];
-            if (kj) {
-                // x(k+4): lane+1's first element, or the next vector's lane 0 (periodic)
-                const float nxt_same = __shfl_down_sync(0xffffffffu, xc.x, 1);
-                const float nxt_wrap = __shfl_sync(0xffffffffu, xp1[(v + 1) % C4].x, 0);
-                const float x4 = lane == 31 ? nxt_wrap : nxt_same;
-                const float4 up = ld4(nr + (jl + 1) * N + k);
-                const float a0 = xc.y - xc.x, a1 = xc.z - xc.y, a2 = xc.w - xc.z, a3 = x4 - xc.w;
-                const float b0 = up.x - xc.x, b1 = up.y - xc.y, b2 = up.z - xc.z, b3 = up.w - xc.w;
-                rg += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + b0 * b0 + b1 * b1 + b2 * b2 + b3 * b3;
+    // Units u0 .. u1-1, unit u = (row tile u / N, plane u mod N): one march
+    // along i per row tile the range touches.
+    for (long long u = u0; u < u1;) {
+        const int j0 = (int)(u / N) * TJ, i0 = (int)(u % N);
+        const int CH = (int)((u1 - u) < (long long)(N - i0) ? (u1 - u) : (long long)(N - i0));
+        u += CH;
+        auto issue_phi = [&](int i) {
+            float* dst = ring + ((i - i0 + 1) % PHS) * RP;
+            const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+            constexpr int ops = (TJ + 3) * (N / 4);
+            for (int o = tid; o < ops; o += NTH) {
+                const int r = o / (N / 4), q = o - r * (N / 4);
+                cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
             }
-            if (p >= 2) {
-                const float4 xo = xp2[v];
+        };
+        auto issue_pi = [&](int i) {
+            float* dst = pis + ((i - i0) % PIS) * PP;
+            const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+            constexpr int ops = (TJ + 1) * (N / 4);
+            for (int o = tid; o < ops; o += NTH) {
+                const int r = o / (N / 4), q = o - r * (N / 4);
+                cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
+            }
+        };
+        float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
+        issue_phi(i0 - 1);
+        issue_phi(i0);
+        cp_commit();
+        for (int q = 0; q < PF; ++q) {
+            if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+            if (q <= CH) issue_pi(i0 + q);
+            cp_commit();
+        }
+        // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
+        auto diffs = [&](int p, bool kj) {
+            const float* nr = nb + ((p - 1) & 1) * NBP;
+            float rg = 0.f;
+    #pragma unroll
+            for (int v = 0; v < C4; ++v) {
+                const int k = 4 * (lane + 32 * v);
+                const float4 xc = xp1[v];
+                if (kj) {
+                    // x(k+4): lane+1's first element, or the next vector's lane 0 (periodic)
+                    const float nxt_same = __shfl_down_sync(0xffffffffu, xc.x, 1);
+                    const float nxt_wrap = __shfl_sync(0xffffffffu, xp1[(v + 1) % C4].x, 0);
+                    const float x4 = lane == 31 ? nxt_wrap : nxt_same;
+                    const float4 up = ld4(nr + (jl + 1) * N + k);
+                    const float a0 = xc.y - xc.x, a1 = xc.z - xc.y, a2 = xc.w - xc.z, a3 = x4 - xc.w;
+                    const float b0 = up.x - xc.x, b1 = up.y - xc.y, b2 = up.z - xc.z, b3 = up.w - xc.w;
+                    rg += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + b0 * b0 + b1 * b1 + b2 * b2 + b3 * b3;
+                }
+                if (p >= 2) {
+                    const float4 xo = xp2[v];
+                    const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
+                    rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
+                }
+            }
+            g.add(rg);
+        };
+        for (int p = 0; p <= CH; ++p) {
+            const int i = i0 + p;
+            cp_wait<PF - 1>();
+            __syncthreads();
+            // planes PF ahead go into the slots of planes no longer read
+            if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
+            if (p + PF <= CH) issue_pi(i + PF);
+            cp_commit();
+            if (interior && p >= 1) diffs(p, true);
+            const float* pc = ring + ((p + 1) % PHS) * RP + (jl + 1) * N;
+            const float* pu = ring + ((p + 2) % PHS) * RP + (jl + 1) * N;
+            const float* pl = ring + (p % PHS) * RP + (jl + 1) * N;
+            const float* pp = pis + (p % PIS) * PP + jl * N;
+            float* nw = nb + (p & 1) * NBP + jl * N;
+            const bool store = interior && p < CH;
+            const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
+            float4 xs[C4];
+    #pragma unroll
+            for (int v = 0; v < C4; ++v) xs[v] = ld4(pc + 4 * (lane + 32 * v));
+            float rs1 = 0.f, rs2 = 0.f;
+    #pragma unroll
+            for (int v = 0; v < C4; ++v) {
+                const int k = 4 * (lane + 32 * v);
+                const float4 x = xs[v];
+                // k-1 and k+4 with periodic wrap across vectors and the row
+                const float lft_same = __shfl_up_sync(0xffffffffu, x.w, 1);
+                const float lft_wrap = __shfl_sync(0xffffffffu, xs[(v + C4 - 1) % C4].w, 31);
+                const float rgt_same = __shfl_down_sync(0xffffffffu, x.x, 1);
+                const float rgt_wrap = __shfl_sync(0xffffffffu, xs[(v + 1) % C4].x, 0);
+                const float xl = lane == 0 ? lft_wrap : lft_same;
+                const float xr = lane == 31 ? rgt_wrap : rgt_same;
+                const float4 up = ld4(pc + k + N), dn = ld4(pc + k - N), iu = ld4(pu + k), il = ld4(pl + k);
+                const float4 pi = ld4(pp + k);
+                float4 lap;
+                lap.x = (x.y + xl) + (up.x + dn.x) + (iu.x + il.x) - 6.f * x.x;
+                lap.y = (x.z + x.x) + (up.y + dn.y) + (iu.y + il.y) - 6.f * x.y;
+                lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
+                lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
+                float4 pin, xn;
+                pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad));
+                pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad));
+                pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad));
+                pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad));
+                xn.x = x.x + d * pin.x;
+                xn.y = x.y + d * pin.y;
+                xn.z = x.z + d * pin.z;
+                xn.w = x.w + d * pin.w;
+                st4(nw + k, xn);
+                if (store) {
+                    st4(B.xd + gb + k, xn);
+                    st4(B.pd + gb + k, pin);
+                    rs1 += (xn.x + xn.y) + (xn.z + xn.w);
+                    rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad) + split_v<TABLE>(xn.y, wv, nv, cv, bad)) +
+                           (split_v<TABLE>(xn.z, wv, nv, cv, bad) + split_v<TABLE>(xn.w, wv, nv, cv, bad));
+                }
+                xp2[v] = xp1[v];
+                xp1[v] = xn;
+            }
+            if (store) { s1.add(rs1); s2.add(rs2); }
+        }
+        // the last pair (CH-1, CH) along i
+        if (interior) {
+            float rg = 0.f;
+    #pragma unroll
+            for (int v = 0; v < C4; ++v) {
+                const float4 xc = xp1[v], xo = xp2[v];
                 const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
                 rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
             }
+            g.add(rg);
         }
-        g.add(rg);
-    };
-    for (int p = 0; p <= CH; ++p) {
-        const int i = i0 + p;
-        cp_wait<PF - 1>();
-        __syncthreads();
-        // planes PF ahead go into the slots of planes no longer read
-        if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
-        if (p + PF <= CH) issue_pi(i + PF);
-        cp_commit();
-        if (interior && p >= 1) diffs(p, true);
-        const float* pc = ring + ((p + 1) % PHS) * RP + (jl + 1) * N;
-        const float* pu = ring + ((p + 2) % PHS) * RP + (jl + 1) * N;
-        const float* pl = ring + (p % PHS) * RP + (jl + 1) * N;
-        const float* pp = pis + (p % PIS) * PP + jl * N;
-        float* nw = nb + (p & 1) * NBP + jl * N;
-        const bool store = interior && p < CH;
-        const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
-        float4 xs[C4];
-#pragma unroll
-        for (int v = 0; v < C4; ++v) xs[v] = ld4(pc + 4 * (lane + 32 * v));
-        float rs1 = 0.f, rs2 = 0.f;
-#pragma unroll
-        for (int v = 0; v < C4; ++v) {
-            const int k = 4 * (lane + 32 * v);
-            const float4 x = xs[v];
-            // k-1 and k+4 with periodic wrap across vectors and the row
-            const float lft_same = __shfl_up_sync(0xffffffffu, x.w, 1);
-            const float lft_wrap = __shfl_sync(0xffffffffu, xs[(v + C4 - 1) % C4].w, 31);
-            const float rgt_same = __shfl_down_sync(0xffffffffu, x.x, 1);
-            const float rgt_wrap = __shfl_sync(0xffffffffu, xs[(v + 1) % C4].x, 0);
-            const float xl = lane == 0 ? lft_wrap : lft_same;
-            const float xr = lane == 31 ? rgt_wrap : rgt_same;
-            const float4 up = ld4(pc + k + N), dn = ld4(pc + k - N), iu = ld4(pu + k), il = ld4(pl + k);
-            const float4 pi = ld4(pp + k);
-            float4 lap;
-            lap.x = (x.y + xl) + (up.x + dn.x) + (iu.x + il.x) - 6.f * x.x;
-            lap.y = (x.z + x.x) + (up.y + dn.y) + (iu.y + il.y) - 6.f * x.y;
-            lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
-            lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
-            float4 pin, xn;
-            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad));
-            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad));
-            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad));
-            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad));
-            xn.x = x.x + d * pin.x;
-            xn.y = x.y + d * pin.y;
-            xn.z = x.z + d * pin.z;
-            xn.w = x.w + d * pin.w;
-            st4(nw + k, xn);
-            if (store) {
-                st4(B.xd + gb + k, xn);
-                st4(B.pd + gb + k, pin);
-                rs1 += (xn.x + xn.y) + (xn.z + xn.w);
-                rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad) + split_v<TABLE>(xn.y, wv, nv, cv, bad)) +
-                       (split_v<TABLE>(xn.z, wv, nv, cv, bad) + split_v<TABLE>(xn.w, wv, nv, cv, bad));
-            }
-            xp2[v] = xp1[v];
-            xp1[v] = xn;
-        }
-        if (store) { s1.add(rs1); s2.add(rs2); }
-    }
-    // the last pair (CH-1, CH) along i
-    if (interior) {
-        float rg = 0.f;
-#pragma unroll
-        for (int v = 0; v < C4; ++v) {
-            const float4 xc = xp1[v], xo = xp2[v];
-            const float c0 = xc.x - xo.x, c1 = xc.y - xo.y, c2 = xc.z - xo.z, c3 = xc.w - xo.w;
-            rg += c0 * c0 + c1 * c1 + c2 * c2 + c3 * c3;
-        }
-        g.add(rg);
+        cp_wait<0>();
+        __syncthreads();   // the ring is refilled by the next march
     }
     cp_wait<0>();
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    double v3[3] = {g.value(), s1.value(), s2.value()};
+    df64 v3[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
 
@@ -900,7 +1090,7 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    double v3[3] = {g.value(), s1.value(), s2.value()};
+    df64 v3[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
 
