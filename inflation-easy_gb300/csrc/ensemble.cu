@@ -408,6 +408,8 @@ static void ens_fill(iegpu_ens* e, const iegpu_bg* bg, const double* af, int max
         C.done = 0;
         C.error = 0;
         C.active = 0;
+        C.pre_claim = 0;
+        C.pre.ok = 0;
         C.af = af ? af[b] : 1e300;
         e->cur_h[b] &= 1;
     }

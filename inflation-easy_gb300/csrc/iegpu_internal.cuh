@@ -81,6 +81,18 @@ struct SplitWin {
     float s[kWin];
 };
 
+// The part of the scalar update that does not depend on the step's lattice
+// sums, formed during the step by the first CTA to finish its tile:
+//   E = c0 + cS0 S0 + cS1 S1 + cS2 S2      (2 grad/3 + pot)
+//   x = cx0 + cx1 E,  ad2 = ca0 + ca1 sqrt(1 + x),  adh = ad + hd ad2
+//   friction = cf adh,  pibar' = cb0 + cb1 friction
+struct SplitPre {
+    int ok, pad;
+    double d, astep, hd;
+    double c0, cS0, cS1, cS2, cx0, cx1, ca0, ca1, cf, cb0, cb1;
+    float lapl, pn, kv, srcAmp;
+};
+
 struct SplitCtl {
     DevBg bg;
     double phibar, pibar;   // FP64 background
@@ -91,6 +103,8 @@ struct SplitCtl {
     SplitWin wk;   // V' window around phibar of the coming step (kick)
     SplitWin wv;   // V window around phibar after it (sums of the new dphi)
     double sums[3];
+    int pre_claim, pad2;
+    SplitPre pre;
 };
 
 // Per-lattice constants of the split step: base step, rescaling exponent,

@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
+    maybe_precompute(ctl, P, K);
     df64 v[3] = {g.df(), s1.df(), s2.df()};
     finish_sums(v, ctl, P, K, part, counter, a_trace);
 }
@@ -657,6 +658,8 @@ static void sctl_fill(iegpu_ctx* c, const iegpu_bg* bg, int mode) {
     C.done = 0;
     C.error = 0;
     C.active = 0;
+    C.pre_claim = 0;
+    C.pre.ok = 0;
 }
 
 static void sctl_bg(const iegpu_ctx* c, iegpu_bg* bg) {

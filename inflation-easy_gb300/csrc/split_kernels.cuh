@@ -385,6 +385,121 @@ static __device__ __noinline__ void split_scalars_warp(SplitCtl& C, const PotDev
     if (err && !error0 && w0) { C.error = IEGPU_ERANGE; C.errval = phibar_new; C.active = 0; C.done = 1; }
 }
 
+// The sum-independent part of the coming scalar update (leapfrog mode),
+// formed by one warp of the first CTA of a step to finish its tile: the FP64
+// latency is spent while the other CTAs still stream, and the last CTA only
+// runs the short chain from the sums (split_scalars_warp).  Same arithmetic
+// as the full update, regrouped into coefficients of S0, S1, S2.
+static __device__ __noinline__ void split_precompute(SplitCtl& C, const PotDev& P, const SplitConst& K) {
+    const bool w0 = (threadIdx.x & 31) == 0;
+    const int mode = C.mode, steps_done = C.steps_done, steps_limit = C.steps_limit;
+    const double phibar = C.phibar;
+    if (mode != kModeLeapfrog || steps_done >= steps_limit || !(C.bg.a <= C.af)) return;
+    const int lbar = P.table ? warp_bracket(P, phibar) : 0;
+    if (!w0) return;
+    const double a = C.bg.a, ad = C.bg.ad, pibar = C.pibar, s = K.s;
+    const double astep = steps_done > 0 ? a : C.bg.astep;
+    double d, rd;
+    if (s == 0.0) {
+        d = K.dt / astep;
+        rd = astep * K.idt;
+    } else {
+        d = K.dt * pow_exp(astep, s - 1.0);
+        rd = pow_exp(astep, 1.0 - s) * K.idt;
+    }
+    const double ra = 1.0 / a;
+    const double g1 = ra * K.idx;
+    const double cgrad = 0.5 * (g1 * g1) * K.igs;
+    double Vb, dVb;   // times B^2
+    bar_potential_at(P, phibar, lbar, &Vb, &dVb);
+    SplitPre& Q = C.pre;
+    Q.d = d;
+    Q.astep = astep;
+    Q.hd = 0.5 * d;
+    Q.c0 = Vb * K.iB2;
+    Q.cS0 = cgrad * (2.0 / 3.0);
+    if (P.table) {
+        Q.cS1 = 0.0;
+        Q.cS2 = K.igs * K.iB2;
+    } else {
+        const double h = -P.V0 * P.c1 * K.igs * K.iB2;
+        Q.cS1 = 2.0 * phibar * h;
+        Q.cS2 = h;
+    }
+    const double sfev1 = s + 1.0, sfev2 = -2.0 * s + 2.0;
+    const double a_sfev2 = (s == 0.0) ? a * a : pow_exp(a, sfev2);
+    Q.cx0 = 2.0 * d * sfev1 * ad * ra;
+    Q.cx1 = (d * d) * sfev1 * a_sfev2;
+    // ad2 = (-2ad - K (1 - sq)) rd, K = 2a rd / (s+1)
+    const double Kc = 2.0 * a * rd * K.isfev1;
+    Q.ca0 = (-2.0 * ad - Kc) * rd;
+    Q.ca1 = Kc * rd;
+    Q.cf = (2.0 + s) * ra;
+    const double a_m2s = (s == 0.0) ? 1.0 : pow_exp(a, -2.0 * s);
+    const double potnorm = (s == 0.0) ? a * a : pow_exp(a, 2.0 - 2.0 * s);
+    Q.cb0 = pibar - d * (potnorm * (dVb * K.iB2));
+    Q.cb1 = -d * pibar;
+    Q.lapl = (float)(a_m2s * K.idx2);
+    Q.pn = (float)(potnorm * K.iB2);
+    Q.kv = (float)(potnorm * P.c2 * K.iB2);
+    Q.srcAmp = (float)(2.0 * a_m2s);
+    Q.ok = 1;
+}
+
+// The last CTA's update when a precomputed part is there (leapfrog mode,
+// the stop checks already passed in split_precompute).
+static __device__ __noinline__ void split_scalars_pre(SplitCtl& C, const PotDev& P, const double* sums,
+                                                      double* a_trace) {
+    const bool w0 = (threadIdx.x & 31) == 0;
+    const int steps_done = C.steps_done, error0 = C.error;
+    const double phibar0 = C.phibar;
+    __syncwarp();
+    double phibar_new = phibar0;
+    if (w0) {
+        const SplitPre& Q = C.pre;
+        const double d = Q.d, a = C.bg.a, ad = C.bg.ad;
+        const double E = Q.c0 + Q.cS0 * sums[0] + Q.cS1 * sums[1] + Q.cS2 * sums[2];
+        const double x = Q.cx0 + Q.cx1 * E;
+        const double ad2 = Q.ca0 + Q.ca1 * sqrt(1.0 + x);
+        const double adh = ad + Q.hd * ad2;
+        const double friction = Q.cf * adh;
+        const double pibar = Q.cb0 + Q.cb1 * friction;
+        const double adn = adh + Q.hd * ad2;
+        C.fric = (float)friction;
+        C.d = (float)d;
+        C.lapl = Q.lapl;
+        C.pn = Q.pn;
+        C.kv = Q.kv;
+        C.srcAmp = Q.srcAmp;
+        C.dd = d;
+        C.bg.astep = Q.astep;
+        C.bg.ad = adn;
+        C.bg.ad2 = ad2;
+        C.pibar = pibar;
+        C.active = 1;
+        phibar_new = phibar0 + d * pibar;
+        C.phibar = phibar_new;
+        C.bg.t = C.bg.t + d;
+        C.bg.a = a + d * adn;
+        if (a_trace) a_trace[steps_done] = C.bg.a;
+        C.steps_done = steps_done + 1;
+    }
+    phibar_new = __shfl_sync(0xffffffffu, phibar_new, 0);
+    int err = 0;
+    build_window_warp(C.wk, P, P.dV, P.slopedV, phibar0, &err);
+    build_window_warp(C.wv, P, P.V, P.slopeV, phibar_new, &err);
+    if (err && !error0 && w0) { C.error = IEGPU_ERANGE; C.errval = phibar_new; C.active = 0; C.done = 1; }
+}
+
+// After its tile, the first CTA of the step to get here forms the
+// precomputed part (warp 0); the others go on at once.
+__device__ __forceinline__ void maybe_precompute(SplitCtl* ctl, const PotDev& P, const SplitConst& K) {
+    __shared__ int claimed;
+    if (threadIdx.x == 0) claimed = atomicCAS(&ctl->pre_claim, 0, 1) == 0;
+    __syncthreads();
+    if (claimed && threadIdx.x < 32) split_precompute(*ctl, P, K);
+}
+
 // One lane, for the diagnostics that build a window outside the step.
 static __device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, const double* y, const double* dy,
                                                  double phibar, int* err) {
@@ -451,8 +566,16 @@ __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, co
             error = C.error;
         }
         error = __shfl_sync(0xffffffffu, error, 0);
+        const int pre = C.pre_claim && C.pre.ok;
+        __syncwarp();
+        if (threadIdx.x == 0) {
+            C.pre_claim = 0;
+            C.pre.ok = 0;
+        }
         if (error) {
             if (threadIdx.x == 0) { C.active = 0; C.done = 1; }
+        } else if (pre) {
+            split_scalars_pre(C, P, sums, a_trace);
         } else {
             split_scalars_warp(C, P, K, sums, a_trace);
         }
@@ -717,6 +840,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
+    maybe_precompute(ctl, P, K);
     df64 v[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
@@ -912,6 +1036,7 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
+    maybe_precompute(ctl, P, K);
     df64 v3[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
@@ -1090,6 +1215,7 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
+    maybe_precompute(ctl, P, K);
     df64 v3[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
