@@ -53,6 +53,7 @@ UNIT = "site-updates/s"
 # algorithmic HBM bytes per site of the dominant kernel of one step
 BYTES_STEP_SPLIT = 16  # split form: read dphi, dpi; write dphi, dpi (FP32)
 BYTES_KICK_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
+BYTES_STEP_SIGW = 112  # split form with SIGW: 16 + read and write 6 h_ij and 6 h_ij' (FP32)
 
 
 def dist_env():
@@ -60,6 +61,25 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def replica_device(environ):
+    """Under torchrun every rank is a replica on its own GPU: the local rank
+    selects it unless CUDA_VISIBLE_DEVICES is already set for the process."""
+    ws = int(environ.get("WORLD_SIZE", "1"))
+    if ws > 1 and "CUDA_VISIBLE_DEVICES" not in environ:
+        return str(int(environ.get("LOCAL_RANK", "0")))
+    return None
+
+
+def ranks_max(value, dist):
+    """The slowest replica sets the time: max of a per-rank float over ranks."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 class Clocks:
@@ -211,18 +231,15 @@ def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None
         clk.__enter__()
     lat.timer_start()
     taken = lat.leapfrog(af, steps, bg)
-    ms = lat.timer_stop()
+    ms = lat.timer_stop()   # synchronises the lattice's stream
+    if dist:
+        dist.barrier()
     if clk:
         clk.__exit__(None, None, None)
     bg.astep = bg.a
     launches = lat.launches - launches0
     assert taken == steps
-    tmax = ms
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tmax = float(t.item())
+    tmax = ranks_max(ms, dist)
     out = {"ms": tmax, "launches": launches, "clocks": clk.summary() if clk else None, "shape": shape}
     # per-kernel device time, CUDA events around each launch (same stream)
     prof_steps = min(50, steps)
@@ -248,12 +265,7 @@ def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None
         lat.leapfrog(af, steps, bg)
         f_out = lat.download(iegpu.F)
         fd_out = lat.download(iegpu.FD)
-        te2e = time.perf_counter() - t0
-        if dist:
-            import torch
-            t = torch.tensor([te2e], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te2e = float(t.item())
+        te2e = ranks_max(time.perf_counter() - t0, dist)
         assert np.isfinite(f_out[:4]).all() and np.isfinite(fd_out[:4]).all()
         out["e2e_s"] = te2e
         out["pinned"] = pinned
@@ -339,6 +351,35 @@ def measure_ensemble(iegpu, steps, warmup, peak):
             "zeta_spectra_lattices": len(spectra)}
 
 
+def measure_sigw(iegpu, N, steps, warmup, peak):
+    """The split form with the SIGW tensor modes on (config: USR table
+    potential, 6 h_ij components and their momenta in FP32): K steps, and one
+    GW spectrum (TT projection and shell binning) of the evolved h'."""
+    w = USR
+    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], potential=iegpu.POT_TABLE, form=iegpu.FORM_SPLIT, sigw=True)
+    lat.set_table(*usr_tables())
+    H = lat.bunch_davies(8, w["phi0"], w["dphi0"])
+    bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
+    lat.evolve_fields(0.5 * w["dt"], bg)
+    lat.leapfrog(1e30, warmup, bg)
+    bg.astep = bg.a
+    lat.timer_start()
+    taken = lat.leapfrog(1e30, steps, bg)
+    ms = lat.timer_stop()
+    assert taken == steps
+    bg.astep = bg.a
+    t0 = time.perf_counter()
+    counts, f2 = lat.gw_spectrum(1, 1.0)
+    t_gw = time.perf_counter() - t0
+    lat.close()
+    per_step = ms / steps
+    achieved = BYTES_STEP_SIGW * N ** 3 / (per_step * 1e-3) / 1e9
+    return {"workload": f"SIGW on, N={N}^3, USR table potential, split form (FP32 dphi/dpi and 6 h_ij + h_ij')",
+            "steps": steps, "ms_per_step": per_step, "site_updates_per_s": N ** 3 / (per_step * 1e-3),
+            "algorithmic_bytes_per_site": BYTES_STEP_SIGW, "achieved_gbs": achieved,
+            "frac_of_measured_hbm": achieved / peak, "gw_spectrum_s": t_gw, "gw_bins": int((counts > 0).sum())}
+
+
 def engine_arm(args):
     ws, rank, local = dist_env()
     dist = None
@@ -371,6 +412,7 @@ def engine_arm(args):
     fp_value = ws * fp_steps * N ** 3 / (fp["ms"] * 1e-3)
     # the batched ensemble (fewer steps: each is ~5x the 256^3 step)
     ens = measure_ensemble(iegpu, max(20, min(args.steps // 30, 500)), args.warmup, peak)
+    sigw = measure_sigw(iegpu, N, max(10, min(args.steps // 75, 200)), args.warmup, peak)
     if rank != 0:
         return 0
 
@@ -399,7 +441,8 @@ def engine_arm(args):
                                "frac_of_measured_hbm": fp_achieved / peak,
                                "note": "per-site arithmetic in the reference's order (-fmad=false); FP64 ALU bound"},
                       "split_over_fp64": value / fp_value,
-                      "batched": ens},
+                      "batched": ens,
+                      "sigw": sigw},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None if tr is None else tr * N ** 3,
                          "kernel": "k_split_rows4 (fused kick + drift + next-step Friedmann sums, N >= 128; k_split_rows below)",
@@ -424,8 +467,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
-    if ws > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
-        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dev = replica_device(os.environ)
+    if dev is not None:
+        os.environ["CUDA_VISIBLE_DEVICES"] = dev
     if args.impl == "reference":
         return reference_arm(args)
     return engine_arm(args)
