@@ -94,16 +94,13 @@ struct Kahan {
 // double-float arithmetic
 // ---------------------------------------------------------------------------
 //
-// A value hi + lo held in two floats (about 44 significant bits), with the
-// error-free sum and product of Dekker and Knuth built on FP32 adds and FMAs.
-// GB300's FP64 operations have hundreds of cycles of latency; these run on
-// the FP32 pipes.  The _rn intrinsics keep the compiler from contracting or
-// reassociating the error terms.
+// A value hi + lo held in two floats (about 44 significant bits), added with
+// the error-free sum of Knuth and Dekker on FP32 adds.  GB300's FP64
+// operations have hundreds of cycles of latency; these run on the FP32 pipes.
+// The _rn intrinsics keep the compiler from reassociating the error terms.
 struct df64 {
     float hi, lo;
 };
-
-__device__ __forceinline__ df64 df_make(float h) { return df64{h, 0.f}; }
 
 __device__ __forceinline__ df64 df_quick(float a, float b) {   // |a| >= |b|
     const float s = __fadd_rn(a, b);
@@ -121,40 +118,6 @@ __device__ __forceinline__ df64 df_add(df64 a, df64 b) {
     const df64 t = df_two_sum(a.lo, b.lo);
     const df64 u = df_quick(s.hi, __fadd_rn(s.lo, t.hi));
     return df_quick(u.hi, __fadd_rn(u.lo, t.lo));
-}
-
-__device__ __forceinline__ df64 df_neg(df64 a) { return df64{-a.hi, -a.lo}; }
-__device__ __forceinline__ df64 df_sub(df64 a, df64 b) { return df_add(a, df_neg(b)); }
-
-__device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    return df_quick(p, e);
-}
-
-// a / b: a float quotient and two corrections from the df64 remainder
-__device__ __forceinline__ df64 df_div(df64 a, df64 b) {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
-    df64 r = df_sub(a, df_mul(b, df_make(q1)));
-    const float q2 = __fdiv_rn(r.hi, b.hi);
-    const df64 q = df_quick(q1, q2);
-    r = df_sub(a, df_mul(b, q));
-    return df_add(q, df_make(__fdiv_rn(r.hi, b.hi)));
-}
-
-// sqrt(a), a > 0: the float root and one Newton correction in df64
-__device__ __forceinline__ df64 df_sqrt(df64 a) {
-    if (!(a.hi > 0.f)) return df64{0.f, 0.f};
-    const float s = __fsqrt_rn(a.hi);
-    const df64 r = df_sub(a, df_mul(df_make(s), df_make(s)));
-    return df_quick(s, __fdiv_rn(r.hi, __fmul_rn(2.f, s)));
-}
-
-__device__ __forceinline__ df64 df_from(double x) {
-    const float h = __double2float_rn(x);
-    return df64{h, __double2float_rn(x - (double)h)};
 }
 
 __device__ __forceinline__ double df_to(df64 a) { return (double)a.hi + (double)a.lo; }
