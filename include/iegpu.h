@@ -158,7 +158,10 @@ int  iegpu_autotune(struct iegpu_ctx* ctx, const iegpu_bg* bg, int* rows, int* p
  * tuning it: rows per tile 4 or 8 with 1 or 2 planes prefetched (rows 4 at
  * N >= 128 also 3 or 4), or rows = N for whole planes (N = 32, 64) with 2 or
  * 4; 1 <= chunks <= N/8 plane chunks, or chunks = 0 (N >= 128) for one wave
- * of CTAs that each take an equal share of the lattice. */
+ * of CTAs that each take an equal share of the lattice.  prefetch + 10 stages
+ * the planes by bulk (TMA) copies instead (N >= 128: rows 8 with 2 planes
+ * ahead, rows 16 at N <= 256 with 1 to 3); iegpu_autotune reports that
+ * encoding too. */
 int  iegpu_set_shape(struct iegpu_ctx* ctx, int rows, int prefetch, int chunks);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */

@@ -528,7 +528,7 @@ int iegpu_autotune(iegpu_ctx* c, const iegpu_bg* bg, int* rows, int* prefetch, i
         if (int rc = split_autotune(c, bg)) return rc;
     }
     if (rows) *rows = c->row_cfg.TJ;
-    if (prefetch) *prefetch = c->row_cfg.PF;
+    if (prefetch) *prefetch = c->row_cfg.PF + (c->row_cfg.tma ? 10 : 0);
     if (chunks) *chunks = c->row_cfg.chunks;
     return IEGPU_OK;
 }

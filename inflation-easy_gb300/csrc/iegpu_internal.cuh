@@ -135,6 +135,7 @@ struct RowCfg {
     int TJ = 0;       // rows per tile (0: untuned default)
     int PF = 2;       // planes prefetched
     int chunks = 1;   // plane ranges along i
+    int tma = 0;      // planes staged by bulk (TMA) copies instead of cp.async
 };
 
 struct SigwSplit {

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
 }
 
 
-template <bool TABLE, int C4, int TJ, int PF>
+template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                                double* part, unsigned* counter, double* a_trace,
                                                                int chunks) {
@@ -225,8 +225,8 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, Spli
         u0 = (long long)blockIdx.x * N + i0;
         u1 = u0 + CH;
     }
-    rows4_body<TABLE, C4, TJ, PF>(B, ctl, P, K, part, counter, a_trace, u0, u1, blockIdx.x + gridDim.x * blockIdx.y,
-                                  gridDim.x * gridDim.y, nullptr);
+    rows4_body<TABLE, C4, TJ, PF, TMA>(B, ctl, P, K, part, counter, a_trace, u0, u1,
+                                       blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr);
 }
 
 // Whole planes (N = 32, 64): block y = chunk of planes.
@@ -446,7 +446,7 @@ static SplitConst split_const(const iegpu_ctx* c) {
 }
 
 struct StepGeom {
-    int TK, TJ, CH, tiles, chunks, PF = 0;
+    int TK, TJ, CH, tiles, chunks, PF = 0, tma = 0;
     size_t smem;
     bool rows;   // full-row kernel (32 <= N <= 512)
 };
@@ -508,6 +508,7 @@ static StepGeom step_geom(const iegpu_ctx* c) {
         if (rc.TJ == 0) rc = default_row_cfg(c);
         g.TJ = rc.TJ;
         g.PF = rc.PF;
+        g.tma = rc.tma;
         g.chunks = rc.chunks;
         g.tiles = rc.chunks > 0 ? N / g.TJ : balanced_ctas(c, N, g.TJ, g.PF);
         g.CH = rc.chunks > 0 ? N / rc.chunks : 0;
@@ -560,15 +561,16 @@ static void rows_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
                c->part, c->counter, c->a_trace, g.chunks);
 }
 
-template <bool TAB, int C4, int TJV, int PFV>
+template <bool TAB, int C4, int TJV, int PFV, bool TMA = false>
 static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
     static size_t attr = 0;
     if (attr < g.smem) {
-        cudaFuncSetAttribute(k_split_rows4<TAB, C4, TJV, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        cudaFuncSetAttribute(k_split_rows4<TAB, C4, TJV, PFV, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)g.smem);
         attr = g.smem;
     }
-    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot, K,
-               c->part, c->counter, c->a_trace, g.chunks);
+    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV, TMA>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot,
+               K, c->part, c->counter, c->a_trace, g.chunks);
 }
 
 template <bool TAB, int NV, int PFV>
@@ -591,6 +593,17 @@ static void plane_pf(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
 
 template <bool TAB, int C4>
 static void rows4_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (g.tma) {
+        // bulk-copy staging: 8-row tiles with 2 planes ahead, 16-row tiles with 1..3
+        if (g.TJ == 8) rows4_one<TAB, C4, 8, 2, true>(c, B, K, grid, g);
+        else if (C4 <= 2) {
+            constexpr int CW = C4 <= 2 ? C4 : 2;
+            if (g.PF == 1) rows4_one<TAB, CW, 16, 1, true>(c, B, K, grid, g);
+            else if (g.PF == 2) rows4_one<TAB, CW, 16, 2, true>(c, B, K, grid, g);
+            else rows4_one<TAB, CW, 16, 3, true>(c, B, K, grid, g);
+        }
+        return;
+    }
     if (g.TJ == 4) {
         switch (g.PF) {
             case 1: rows4_one<TAB, C4, 4, 1>(c, B, K, grid, g); break;
@@ -694,6 +707,8 @@ static int sctl_down(iegpu_ctx* c) {
     if (check_cuda(c, cudaMemcpyAsync(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost, c->stream), "split control download"))
         return IEGPU_ECUDA;
     if (sync_and_check(c, "split")) return IEGPU_ECUDA;
+    if (c->sctl_h->error == IEGPU_ETIMEOUT)
+        return set_error(c, IEGPU_ETIMEOUT, "a bulk copy into shared memory did not complete");
     if (c->sctl_h->error == IEGPU_ERANGE) {
         return set_error(c, IEGPU_ERANGE,
                          "Field value near %.17g is outside the numerical potential range [%.17g, %.17g].\n",
@@ -776,8 +791,33 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
                 r.PF = PF;
                 r.chunks = ch;
                 bool dup = false;
-                for (const RowCfg& q : cands) dup |= (q.TJ == r.TJ && q.PF == r.PF && q.chunks == r.chunks);
+                for (const RowCfg& q : cands)
+                    dup |= (q.TJ == r.TJ && q.PF == r.PF && q.chunks == r.chunks && q.tma == r.tma);
                 if (!dup) cands.push_back(r);
+            }
+        }
+    }
+    if (N >= 128) {
+        // bulk-copy (TMA) staging of the planes
+        auto add_tma = [&](int TJ, int PF, int ch) {
+            if (row_ctas_per_sm(N, TJ, PF) < 1) return;
+            RowCfg r;
+            r.TJ = TJ;
+            r.PF = PF;
+            r.chunks = ch;
+            r.tma = 1;
+            cands.push_back(r);
+        };
+        const int per8 = row_ctas_per_sm(N, 8, 2);
+        int ch8 = (c->sms * (per8 > 0 ? per8 : 1)) / (N / 8);
+        ch8 = ch8 < 1 ? 1 : (ch8 > N / 8 ? N / 8 : ch8);
+        add_tma(8, 2, ch8);
+        if (N <= 256) {
+            int ch16 = c->sms / (N / 16);
+            ch16 = ch16 < 1 ? 1 : (ch16 > N / 8 ? N / 8 : ch16);
+            for (int PF : {1, 2, 3}) {
+                add_tma(16, PF, ch16);
+                add_tma(16, PF, 0);
             }
         }
     }
@@ -812,6 +852,23 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
 
 int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     const int N = c->N;
+    if (prefetch >= 10) {
+        // bulk-copy (TMA) staging: prefetch - 10 planes ahead
+        const int pf = prefetch - 10;
+        const bool ok = N >= 128 && ((rows == 8 && pf == 2) || (rows == 16 && N <= 256 && pf >= 1 && pf <= 3)) &&
+                        (chunks == 0 || (chunks >= 1 && chunks <= N / 8));
+        if (!ok) return set_error(c, IEGPU_EINVAL, "bulk-copy shapes: rows 8 with 2 planes ahead, or rows 16 (N <= 256) with 1..3");
+        const long long ctas = chunks == 0 ? balanced_ctas(c, N, rows, pf) : (long long)(N / rows) * chunks;
+        if (3LL * ctas > c->part_cap || row_ctas_per_sm(N, rows, pf) < 1)
+            return set_error(c, IEGPU_EINVAL, "shape does not fit this lattice's scratch");
+        c->row_cfg.TJ = rows;
+        c->row_cfg.PF = pf;
+        c->row_cfg.chunks = chunks;
+        c->row_cfg.tma = 1;
+        c->tuned = 1;
+        split_destroy_graphs(c);
+        return IEGPU_OK;
+    }
     if (N < 32 || N > 512) return set_error(c, IEGPU_EUNSUPPORTED, "the row kernel covers 32 <= N <= 512");
     const bool plane = plane_shape(N, rows);
     const bool deep = rows == 4 && N >= 128 && (prefetch == 3 || prefetch == 4);
@@ -829,6 +886,7 @@ int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     c->row_cfg.TJ = rows;
     c->row_cfg.PF = prefetch;
     c->row_cfg.chunks = chunks;
+    c->row_cfg.tma = 0;
     c->tuned = 1;
     split_destroy_graphs(c);
     return IEGPU_OK;

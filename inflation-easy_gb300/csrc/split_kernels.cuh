@@ -649,6 +649,49 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 template <int n>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory"); }
 
+// Bulk asynchronous copies (TMA engine) into shared memory with mbarrier
+// completion: one instruction moves a whole row, and the threads only wait on
+// the barrier of the group.
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase of the given parity, at most `limit` polls; false if
+// it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned limit) {
+    for (unsigned t = 0; t < limit; ++t)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// Orders this thread's earlier shared-memory accesses before later bulk
+// copies into the same memory.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+constexpr unsigned kMbarPolls = 1u << 20;   // far beyond any copy's latency (about a second at most)
+
 constexpr int kPrefetch = 3;   // planes in flight ahead of the one being computed
 constexpr int kPhiSlots = 6;   // three stencil planes + kPrefetch
 constexpr int kPiSlots = 4;    // one plane in use + kPrefetch
@@ -821,7 +864,7 @@ __host__ __device__ inline int split_row4_smem_floats(int TJ, int N, int PF) {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
-template <bool TABLE, int C4, int TJ, int PF>
+template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
 __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                            double* part, unsigned* counter, double* a_trace, long long u0,
                                            long long u1, int slot, int nslots, int* state) {
@@ -862,6 +905,20 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     bool bad = false;
     const int jl = w;
     const bool interior = jl < TJ;
+    // TMA: group g of a march (g = -1: dphi planes i0-1, i0; g >= 0: dphi plane
+    // i0+g+1 and dpi plane i0+g; g > CH: empty) completes barrier G % NB,
+    // G = the CTA's running group count.
+    constexpr int NB = PF + 2;
+    __shared__ __align__(8) unsigned long long bars[TMA ? NB : 1];
+    unsigned G0 = 0;
+    bool tma_ok = true;
+    if (TMA) {
+        if (tid == 0) {
+            for (int q = 0; q < NB; ++q) mbar_init(&bars[q], 1);
+            mbar_init_fence();
+        }
+        __syncthreads();
+    }
     // Units u0 .. u1-1, unit u = (row tile u / N, plane u mod N): one march
     // along i per row tile the range touches.
     for (long long u = u0; u < u1;) {
@@ -886,14 +943,49 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
             }
         };
+        // TMA group g, issued by warp 0 (lane 0 arms the barrier first)
+        auto issue_group = [&](int gi) {
+            unsigned long long* bar = &bars[(G0 + (unsigned)(gi + 1)) % NB];
+            const int nphi = gi < 0 ? 2 * (TJ + 3) : (gi <= CH ? TJ + 3 : 0);
+            const int npi = (gi >= 0 && gi <= CH) ? TJ + 1 : 0;
+            if (lane == 0) mbar_expect_tx(bar, (unsigned)((nphi + npi) * N * 4));
+            __syncwarp();
+            for (int r = lane; r < nphi + npi; r += 32) {
+                if (r < nphi) {
+                    const int pl = gi < 0 ? (r < TJ + 3 ? i0 - 1 : i0) : i0 + gi + 1;
+                    const int rr = gi < 0 ? r % (TJ + 3) : r;
+                    float* dst = ring + ((pl - i0 + 1) % PHS) * RP + rr * N;
+                    const float* src = B.xs + ((long long)(pl & m) << (2 * lgN)) + ((long long)((j0 + rr - 1) & m) << lgN);
+                    bulk_g2s(dst, src, N * 4, bar);
+                } else {
+                    const int rr = r - nphi, pl = i0 + gi;
+                    float* dst = pis + ((pl - i0) % PIS) * PP + rr * N;
+                    const float* src = B.ps + ((long long)(pl & m) << (2 * lgN)) + ((long long)((j0 + rr) & m) << lgN);
+                    bulk_g2s(dst, src, N * 4, bar);
+                }
+            }
+        };
+        auto wait_group = [&](int gi) {
+            // after one wait has given up, the step is marked failed and no more waits are made
+            const unsigned Gq = G0 + (unsigned)(gi + 1);
+            if (tma_ok && !mbar_wait(&bars[Gq % NB], (Gq / NB) & 1u, kMbarPolls)) tma_ok = false;
+        };
         float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
-        issue_phi(i0 - 1);
-        issue_phi(i0);
-        cp_commit();
-        for (int q = 0; q < PF; ++q) {
-            if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
-            if (q <= CH) issue_pi(i0 + q);
+        if (TMA) {
+            if (w == 0) {
+                fence_proxy_async();
+                issue_group(-1);
+                for (int q = 0; q < PF; ++q) issue_group(q);
+            }
+        } else {
+            issue_phi(i0 - 1);
+            issue_phi(i0);
             cp_commit();
+            for (int q = 0; q < PF; ++q) {
+                if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
+                if (q <= CH) issue_pi(i0 + q);
+                cp_commit();
+            }
         }
         // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
         auto diffs = [&](int p, bool kj) {
@@ -923,12 +1015,24 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         };
         for (int p = 0; p <= CH; ++p) {
             const int i = i0 + p;
-            cp_wait<PF - 1>();
+            if (TMA) {
+                if (p == 0) wait_group(-1);
+                wait_group(p);
+            } else {
+                cp_wait<PF - 1>();
+            }
             __syncthreads();
             // planes PF ahead go into the slots of planes no longer read
-            if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
-            if (p + PF <= CH) issue_pi(i + PF);
-            cp_commit();
+            if (TMA) {
+                if (w == 0) {
+                    fence_proxy_async();
+                    issue_group(p + PF);
+                }
+            } else {
+                if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
+                if (p + PF <= CH) issue_pi(i + PF);
+                cp_commit();
+            }
             if (interior && p >= 1) diffs(p, true);
             const float* pc = ring + ((p + 1) % PHS) * RP + (jl + 1) * N;
             const float* pu = ring + ((p + 2) % PHS) * RP + (jl + 1) * N;
@@ -992,8 +1096,12 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             }
             g.add(rg);
         }
-        cp_wait<0>();
+        if (!TMA) cp_wait<0>();
+        G0 += (unsigned)(CH + PF + 2);
         __syncthreads();   // the ring is refilled by the next march
+    }
+    if (TMA && !tma_ok) {
+        if (atomicCAS(&ctl->error, 0, IEGPU_ETIMEOUT) == 0) ctl->errval = 0.0;
     }
     cp_wait<0>();
     if (bad) {

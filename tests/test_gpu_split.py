@@ -135,3 +135,32 @@ def test_split_whole_plane_kernel(N, engine, oracle_mod, tables):
         assert abs(out[name][2][1] - o.scalars.a) <= 1e-9 * o.scalars.a
     # the two kernels differ only in FP32 summation order
     assert pert_err(out["plane"][0], out["rows"][0]) < 1e-5
+
+
+@pytest.mark.parametrize("N,shapes", [(128, [(16, 12, 8), (16, 11, 0), (16, 13, 8), (8, 12, 4)]),
+                                      (256, [(16, 12, 9), (8, 12, 9)])])
+def test_split_bulk_copy_staging_matches(N, shapes, engine, tables):
+    """Planes staged by bulk (TMA) copies give the same bits as planes staged
+    by cp.async with the same tiling."""
+    w = dict(L=10.0, dt=1e-3, V0=3e-9, phi0=2.9181235049318586, dphi0=-0.06727651095116181)
+    out = {}
+    for sh in shapes + [(sh[0], sh[1] - 10 if sh[1] - 10 in (1, 2) else 2, sh[2]) for sh in shapes]:
+        lat = engine.Lattice(N, w["L"], w["dt"], w["V0"], potential=engine.POT_TABLE, form=engine.FORM_SPLIT)
+        with lat:
+            lat.set_table(*tables)
+            lat.set_shape(*sh)
+            H = lat.bunch_davies(5, w["phi0"], w["dphi0"])
+            bg = engine.Bg(0.0, 1.0, H, 0.0, 1.0)
+            lat.evolve_fields(0.5 * w["dt"], bg)
+            assert lat.leapfrog(1e30, 30, bg) == 30
+            out[sh] = (lat.download(engine.F), lat.download(engine.FD), bg.as_tuple())
+    for sh in shapes:
+        ref = (sh[0], sh[1] - 10 if sh[1] - 10 in (1, 2) else 2, sh[2])
+        if sh[1] - 10 != ref[1]:
+            continue   # no cp.async shape with that prefetch depth and rows
+        assert np.array_equal(out[sh][0], out[ref][0]) and np.array_equal(out[sh][1], out[ref][1]), sh
+        assert out[sh][2] == out[ref][2], sh
+    # every staging gives the same trajectory up to FP32 summation order
+    base = out[shapes[0]][0]
+    for sh, v in out.items():
+        assert np.max(np.abs(v[0] - base)) <= 1e-6 * np.std(base - base.mean()), sh
