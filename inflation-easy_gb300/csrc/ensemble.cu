@@ -97,7 +97,9 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_ens_rows4(EnsArgs A, const in
     const EnsTile t = ens_tile(A, work, TJ);
     constexpr int N = 128 * C4;
     const long long u0 = (long long)(t.j0 / TJ) * N + t.i0;
-    rows4_body<TABLE, C4, TJ, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, u0, u0 + t.CH, t.slot, t.nslots, t.st);
+    // the march direction follows the lattice's buffer parity, as in the one-lattice kernel
+    rows4_body<TABLE, C4, TJ, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, u0, u0 + t.CH, t.slot, t.nslots, t.st,
+                                  (*t.st & 1) != 0);
 }
 
 template <bool TABLE, int N, int NT, int PF>

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
 template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
 __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                                double* part, unsigned* counter, double* a_trace,
-                                                               int chunks) {
+                                                               int chunks, int rev) {
     constexpr int N = 128 * C4;
     pdl_begin();
     long long u0, u1;
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, Spli
         u1 = u0 + CH;
     }
     rows4_body<TABLE, C4, TJ, PF, TMA>(B, ctl, P, K, part, counter, a_trace, u0, u1,
-                                       blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr);
+                                       blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr, rev != 0);
 }
 
 // Whole planes (N = 32, 64): block y = chunk of planes.
@@ -447,6 +447,7 @@ static SplitConst split_const(const iegpu_ctx* c) {
 
 struct StepGeom {
     int TK, TJ, CH, tiles, chunks, PF = 0, tma = 0;
+    int rev = 0;   // the vector row kernel marches backwards (odd buffer parity)
     size_t smem;
     bool rows;   // full-row kernel (32 <= N <= 512)
 };
@@ -570,7 +571,7 @@ static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim
         attr = g.smem;
     }
     launch_pdl(k_split_rows4<TAB, C4, TJV, PFV, TMA>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot,
-               K, c->part, c->counter, c->a_trace, g.chunks);
+               K, c->part, c->counter, c->a_trace, g.chunks, g.rev);
 }
 
 template <bool TAB, int NV, int PFV>
@@ -655,7 +656,8 @@ static void launch_step(iegpu_ctx* c, int src) {
                                                                                 c->lg, hodx, 0);
         c->launches++;
     }
-    const StepGeom g = step_geom(c);
+    StepGeom g = step_geom(c);
+    g.rev = src & 1;
     SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
     dim3 grid(g.tiles, g.chunks > 0 ? g.chunks : 1);
     if (g.rows) {

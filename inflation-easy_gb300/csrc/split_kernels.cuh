@@ -867,7 +867,7 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
 __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                            double* part, unsigned* counter, double* a_trace, long long u0,
-                                           long long u1, int slot, int nslots, int* state) {
+                                           long long u1, int slot, int nslots, int* state, bool rev) {
     constexpr int N = 128 * C4, m = N - 1;
     constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
     constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
@@ -919,28 +919,45 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         }
         __syncthreads();
     }
+    // rev: march backwards (units from u1-1 down, planes from high i to low),
+    // so that a step first reads what the step before, marching the other
+    // way, wrote last, while part of it is still in L2.
     // Units u0 .. u1-1, unit u = (row tile u / N, plane u mod N): one march
     // along i per row tile the range touches.
-    for (long long u = u0; u < u1;) {
-        const int j0 = (int)(u / N) * TJ, i0 = (int)(u % N);
-        const int CH = (int)((u1 - u) < (long long)(N - i0) ? (u1 - u) : (long long)(N - i0));
-        u += CH;
-        auto issue_phi = [&](int i) {
-            float* dst = ring + ((i - i0 + 1) % PHS) * RP;
-            const float* src = B.xs + ((long long)(i & m) << (2 * lgN));
+    for (long long u = rev ? u1 : u0; rev ? u > u0 : u < u1;) {
+        // this march covers units [s, e) of one row tile
+        long long s, e;
+        if (rev) {
+            e = u;
+            s = ((e - 1) / N) * N;
+            if (s < u0) s = u0;
+            u = s;
+        } else {
+            s = u;
+            e = (s / N + 1) * N;
+            if (e > u1) e = u1;
+            u = e;
+        }
+        const int j0 = (int)(s / N) * TJ, i0 = (int)(s % N);
+        const int CH = (int)(e - s);
+        // march position q -> plane; q = -1 and q = CH are the halo planes
+        auto plane = [&](int q) { return rev ? i0 + CH - 1 - q : i0 + q; };
+        auto issue_phi = [&](int q) {
+            float* dst = ring + ((q + 1) % PHS) * RP;
+            const float* src = B.xs + ((long long)(plane(q) & m) << (2 * lgN));
             constexpr int ops = (TJ + 3) * (N / 4);
             for (int o = tid; o < ops; o += NTH) {
-                const int r = o / (N / 4), q = o - r * (N / 4);
-                cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * q);
+                const int r = o / (N / 4), c = o - r * (N / 4);
+                cp_async16(dst + r * N + 4 * c, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * c);
             }
         };
-        auto issue_pi = [&](int i) {
-            float* dst = pis + ((i - i0) % PIS) * PP;
-            const float* src = B.ps + ((long long)(i & m) << (2 * lgN));
+        auto issue_pi = [&](int q) {
+            float* dst = pis + (q % PIS) * PP;
+            const float* src = B.ps + ((long long)(plane(q) & m) << (2 * lgN));
             constexpr int ops = (TJ + 1) * (N / 4);
             for (int o = tid; o < ops; o += NTH) {
-                const int r = o / (N / 4), q = o - r * (N / 4);
-                cp_async16(dst + r * N + 4 * q, src + ((long long)((j0 + r) & m) << lgN) + 4 * q);
+                const int r = o / (N / 4), c = o - r * (N / 4);
+                cp_async16(dst + r * N + 4 * c, src + ((long long)((j0 + r) & m) << lgN) + 4 * c);
             }
         };
         // TMA group g, issued by warp 0 (lane 0 arms the barrier first)
@@ -952,15 +969,15 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             __syncwarp();
             for (int r = lane; r < nphi + npi; r += 32) {
                 if (r < nphi) {
-                    const int pl = gi < 0 ? (r < TJ + 3 ? i0 - 1 : i0) : i0 + gi + 1;
+                    const int q = gi < 0 ? (r < TJ + 3 ? -1 : 0) : gi + 1;
                     const int rr = gi < 0 ? r % (TJ + 3) : r;
-                    float* dst = ring + ((pl - i0 + 1) % PHS) * RP + rr * N;
-                    const float* src = B.xs + ((long long)(pl & m) << (2 * lgN)) + ((long long)((j0 + rr - 1) & m) << lgN);
+                    float* dst = ring + ((q + 1) % PHS) * RP + rr * N;
+                    const float* src = B.xs + ((long long)(plane(q) & m) << (2 * lgN)) + ((long long)((j0 + rr - 1) & m) << lgN);
                     bulk_g2s(dst, src, N * 4, bar);
                 } else {
-                    const int rr = r - nphi, pl = i0 + gi;
-                    float* dst = pis + ((pl - i0) % PIS) * PP + rr * N;
-                    const float* src = B.ps + ((long long)(pl & m) << (2 * lgN)) + ((long long)((j0 + rr) & m) << lgN);
+                    const int rr = r - nphi, q = gi;
+                    float* dst = pis + (q % PIS) * PP + rr * N;
+                    const float* src = B.ps + ((long long)(plane(q) & m) << (2 * lgN)) + ((long long)((j0 + rr) & m) << lgN);
                     bulk_g2s(dst, src, N * 4, bar);
                 }
             }
@@ -978,12 +995,12 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 for (int q = 0; q < PF; ++q) issue_group(q);
             }
         } else {
-            issue_phi(i0 - 1);
-            issue_phi(i0);
+            issue_phi(-1);
+            issue_phi(0);
             cp_commit();
             for (int q = 0; q < PF; ++q) {
-                if (q + 1 <= CH + 1) issue_phi(i0 + 1 + q);
-                if (q <= CH) issue_pi(i0 + q);
+                if (q + 1 <= CH + 1) issue_phi(1 + q);
+                if (q <= CH) issue_pi(q);
                 cp_commit();
             }
         }
@@ -1014,7 +1031,7 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             g.add(rg);
         };
         for (int p = 0; p <= CH; ++p) {
-            const int i = i0 + p;
+            const int i = plane(p);
             if (TMA) {
                 if (p == 0) wait_group(-1);
                 wait_group(p);
@@ -1029,8 +1046,8 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                     issue_group(p + PF);
                 }
             } else {
-                if (p + PF + 1 <= CH + 1) issue_phi(i + 1 + PF);
-                if (p + PF <= CH) issue_pi(i + PF);
+                if (p + PF + 1 <= CH + 1) issue_phi(p + 1 + PF);
+                if (p + PF <= CH) issue_pi(p + PF);
                 cp_commit();
             }
             if (interior && p >= 1) diffs(p, true);
