@@ -92,7 +92,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_ens_rows(EnsArgs A, const int
 }
 
 template <bool TABLE, int C4, int TJ, int PF>
-__global__ void __launch_bounds__((TJ + 1) * 32) k_ens_rows4(EnsArgs A, const int2* __restrict__ work) {
+__global__ void __launch_bounds__((TJ + 2) * 32) k_ens_rows4(EnsArgs A, const int2* __restrict__ work) {
     pdl_begin();
     const EnsTile t = ens_tile(A, work, TJ);
     constexpr int N = 128 * C4;
@@ -189,7 +189,9 @@ static int ens_prime_slots(const iegpu_ens* e, int N) {
 // PF = 1 or 2 planes prefetched, or TJ = N (N = 32, 64) for whole planes with
 // PF = 2 or 4.
 static bool ens_plane(int N, int TJ) { return TJ == N && (N == 32 || N == 64); }
-static int ens_threads(int N, int TJ) { return ens_plane(N, TJ) ? (N == 32 ? 256 : 512) : (TJ + 1) * 32; }
+static int ens_threads(int N, int TJ) {
+    return ens_plane(N, TJ) ? (N == 32 ? 256 : 512) : N >= 128 ? row4_threads(TJ) : (TJ + 1) * 32;
+}
 
 static size_t ens_smem(int N, int TJ, int PF) {
     if (ens_plane(N, TJ)) return sizeof(float) * (size_t)split_plane_smem_floats(N, PF);
@@ -412,6 +414,7 @@ static void ens_fill(iegpu_ens* e, const iegpu_bg* bg, const double* af, int max
         C.active = 0;
         C.pre_claim = 0;
         C.pre.ok = 0;
+        C.deferred = 0;
         C.af = af ? af[b] : 1e300;
         e->cur_h[b] &= 1;
     }
@@ -448,6 +451,8 @@ static int ens_finish(iegpu_ens* e, iegpu_bg* bg, int* steps) {
     }
     for (int b = 0; b < e->count; ++b) {
         const SplitCtl& C = e->ctl_h[b];
+        if (C.deferred)
+            return ens_error(e, IEGPU_ECUDA, "internal: a scalar update of lattice %d was left unapplied", b);
         if (C.error == IEGPU_ERANGE) {
             const iegpu_ctx* h = e->helper[0];
             return ens_error(e, IEGPU_ERANGE,

@@ -86,11 +86,19 @@ struct SplitWin {
 //   E = c0 + cS0 S0 + cS1 S1 + cS2 S2      (2 grad/3 + pot)
 //   x = cx0 + cx1 E,  ad2 = ca0 + ca1 sqrt(1 + x),  adh = ad + hd ad2
 //   friction = cf adh,  pibar' = cb0 + cb1 friction
+//
+// With `fast` set (hilltop potential, vector row kernel), the coefficients of
+// the friction's chain are also held as double-float pairs (hi[q] + lo[q],
+// q = kPreC0 .. kPreCf), so the last CTA of the step forms the friction on
+// the FP32 pipes and leaves the FP64 update of a, ad, t, phibar and pibar to
+// the next step (`deferred` in SplitCtl).
+enum { kPreC0, kPreS0, kPreS1, kPreS2, kPreX0, kPreX1, kPreA0, kPreA1, kPreAd, kPreHd, kPreCf, kPreN };
 struct SplitPre {
-    int ok, pad;
+    int ok, fast;
     double d, astep, hd;
     double c0, cS0, cS1, cS2, cx0, cx1, ca0, ca1, cf, cb0, cb1;
-    float lapl, pn, kv, srcAmp;
+    float lapl, pn, kv, srcAmp, d32, pad;
+    float hi[kPreN], lo[kPreN];
 };
 
 struct SplitCtl {
@@ -105,6 +113,10 @@ struct SplitCtl {
     double sums[3];
     int pre_claim, pad2;
     SplitPre pre;
+    // A scalar update whose FP64 part is still to be applied: the step's sums
+    // as double-float pairs and the index of its a_trace entry.
+    int deferred, def_step;
+    float dsum_hi[3], dsum_lo[3];
 };
 
 // Per-lattice constants of the split step: base step, rescaling exponent,

@@ -208,7 +208,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
 
 
 template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
-__global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
+__global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                                double* part, unsigned* counter, double* a_trace,
                                                                int chunks, int rev) {
     constexpr int N = 128 * C4;
@@ -470,7 +470,7 @@ static int row_ctas_per_sm(int N, int TJ, int PF) {
     const size_t smem = row_smem_bytes(N, TJ, PF) + 1024;
     const size_t per_sm = 228 * 1024;
     int by_smem = (int)(per_sm / smem);
-    const int nthr = plane_shape(N, TJ) ? plane_threads(N) : (TJ + 1) * 32;
+    const int nthr = plane_shape(N, TJ) ? plane_threads(N) : N >= 128 ? row4_threads(TJ) : (TJ + 1) * 32;
     const int by_regs = 65536 / (nthr * 72);
     int n = by_smem < by_regs ? by_smem : by_regs;
     return n < 1 ? (smem <= 227 * 1024 ? 1 : 0) : n;
@@ -570,7 +570,7 @@ static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim
                              (int)g.smem);
         attr = g.smem;
     }
-    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV, TMA>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot,
+    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV, TMA>, grid, dim3(row4_threads(TJV)), g.smem, c->stream, B, c->sctl, c->pot,
                K, c->part, c->counter, c->a_trace, g.chunks, g.rev);
 }
 
@@ -709,6 +709,8 @@ static int sctl_down(iegpu_ctx* c) {
     if (check_cuda(c, cudaMemcpyAsync(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost, c->stream), "split control download"))
         return IEGPU_ECUDA;
     if (sync_and_check(c, "split")) return IEGPU_ECUDA;
+    if (c->sctl_h->deferred)
+        return set_error(c, IEGPU_ECUDA, "internal: a scalar update was left unapplied at the end of a call");
     if (c->sctl_h->error == IEGPU_ETIMEOUT)
         return set_error(c, IEGPU_ETIMEOUT, "a bulk copy into shared memory did not complete");
     if (c->sctl_h->error == IEGPU_ERANGE) {
@@ -735,6 +737,7 @@ static void sctl_fill(iegpu_ctx* c, const iegpu_bg* bg, int mode) {
     C.active = 0;
     C.pre_claim = 0;
     C.pre.ok = 0;
+    C.deferred = 0;
 }
 
 static void sctl_bg(const iegpu_ctx* c, iegpu_bg* bg) {

@@ -122,6 +122,28 @@ __device__ __forceinline__ df64 df_add(df64 a, df64 b) {
 
 __device__ __forceinline__ double df_to(df64 a) { return (double)a.hi + (double)a.lo; }
 
+__device__ __forceinline__ df64 df_from(double x) {
+    const float h = (float)x;
+    return df64{h, (float)(x - (double)h)};
+}
+
+// Product with the exact error of hi*hi from an FMA (Dekker's product).
+__device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return df_quick(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+
+// Square root of a > 0: the FP32 root r corrected by one Newton step,
+// r + (a - r^2) / (2r), with r^2 formed exactly by an FMA.
+__device__ __forceinline__ df64 df_sqrt(df64 a) {
+    const float r = sqrtf(a.hi);
+    const float p = __fmul_rn(r, r);
+    const float e = __fmaf_rn(r, r, -p);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
+    return df_quick(r, __fmul_rn(res, __frcp_rn(__fadd_rn(r, r))));
+}
+
 __device__ __forceinline__ df64 df_shfl_down(df64 v, int o) {
     return df64{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
 }
@@ -353,7 +375,8 @@ static __device__ __noinline__ void split_scalars_warp(SplitCtl& C, const PotDev
 // latency is spent while the other CTAs still stream, and the last CTA only
 // runs the short chain from the sums (split_scalars_warp).  Same arithmetic
 // as the full update, regrouped into coefficients of S0, S1, S2.
-static __device__ __noinline__ void split_precompute(SplitCtl& C, const PotDev& P, const SplitConst& K) {
+static __device__ __noinline__ void split_precompute(SplitCtl& C, const PotDev& P, const SplitConst& K,
+                                                     bool allow_fast) {
     const bool w0 = (threadIdx.x & 31) == 0;
     const int mode = C.mode, steps_done = C.steps_done, steps_limit = C.steps_limit;
     const double phibar = C.phibar;
@@ -406,7 +429,44 @@ static __device__ __noinline__ void split_precompute(SplitCtl& C, const PotDev& 
     Q.pn = (float)(potnorm * K.iB2);
     Q.kv = (float)(potnorm * P.c2 * K.iB2);
     Q.srcAmp = (float)(2.0 * a_m2s);
+    Q.d32 = (float)d;
+    Q.fast = allow_fast && !P.table;
+    if (Q.fast) {
+        const double v[kPreN] = {Q.c0, Q.cS0, Q.cS1, Q.cS2, Q.cx0, Q.cx1, Q.ca0, Q.ca1, ad, Q.hd, Q.cf};
+#pragma unroll
+        for (int q = 0; q < kPreN; ++q) {
+            const df64 f = df_from(v[q]);
+            Q.hi[q] = f.hi;
+            Q.lo[q] = f.lo;
+        }
+    }
     Q.ok = 1;
+}
+
+// FP64 part of the precomputed update (lane 0): a, ad, ad2, t, astep, phibar
+// and pibar after the step with lattice sums `sums`, the a_trace entry
+// `step`; returns the friction and the new phibar.
+static __device__ __forceinline__ void pre_state_update(SplitCtl& C, const double* sums, double* a_trace, int step,
+                                                        double& friction, double& phibar_new) {
+    const SplitPre& Q = C.pre;
+    const double d = Q.d, a = C.bg.a, ad = C.bg.ad;
+    const double E = Q.c0 + Q.cS0 * sums[0] + Q.cS1 * sums[1] + Q.cS2 * sums[2];
+    const double x = Q.cx0 + Q.cx1 * E;
+    const double ad2 = Q.ca0 + Q.ca1 * sqrt(1.0 + x);
+    const double adh = ad + Q.hd * ad2;
+    friction = Q.cf * adh;
+    const double pibar = Q.cb0 + Q.cb1 * friction;
+    const double adn = adh + Q.hd * ad2;
+    C.dd = d;
+    C.bg.astep = Q.astep;
+    C.bg.ad = adn;
+    C.bg.ad2 = ad2;
+    C.pibar = pibar;
+    phibar_new = C.phibar + d * pibar;
+    C.phibar = phibar_new;
+    C.bg.t = C.bg.t + d;
+    C.bg.a = a + d * adn;
+    if (a_trace) a_trace[step] = C.bg.a;
 }
 
 // The last CTA's update when a precomputed part is there (leapfrog mode,
@@ -420,31 +480,15 @@ static __device__ __noinline__ void split_scalars_pre(SplitCtl& C, const PotDev&
     double phibar_new = phibar0;
     if (w0) {
         const SplitPre& Q = C.pre;
-        const double d = Q.d, a = C.bg.a, ad = C.bg.ad;
-        const double E = Q.c0 + Q.cS0 * sums[0] + Q.cS1 * sums[1] + Q.cS2 * sums[2];
-        const double x = Q.cx0 + Q.cx1 * E;
-        const double ad2 = Q.ca0 + Q.ca1 * sqrt(1.0 + x);
-        const double adh = ad + Q.hd * ad2;
-        const double friction = Q.cf * adh;
-        const double pibar = Q.cb0 + Q.cb1 * friction;
-        const double adn = adh + Q.hd * ad2;
+        double friction;
+        pre_state_update(C, sums, a_trace, steps_done, friction, phibar_new);
         C.fric = (float)friction;
-        C.d = (float)d;
+        C.d = Q.d32;
         C.lapl = Q.lapl;
         C.pn = Q.pn;
         C.kv = Q.kv;
         C.srcAmp = Q.srcAmp;
-        C.dd = d;
-        C.bg.astep = Q.astep;
-        C.bg.ad = adn;
-        C.bg.ad2 = ad2;
-        C.pibar = pibar;
         C.active = 1;
-        phibar_new = phibar0 + d * pibar;
-        C.phibar = phibar_new;
-        C.bg.t = C.bg.t + d;
-        C.bg.a = a + d * adn;
-        if (a_trace) a_trace[steps_done] = C.bg.a;
         C.steps_done = steps_done + 1;
     }
     phibar_new = __shfl_sync(0xffffffffu, phibar_new, 0);
@@ -454,13 +498,64 @@ static __device__ __noinline__ void split_scalars_pre(SplitCtl& C, const PotDev&
     if (err && !error0 && w0) { C.error = IEGPU_ERANGE; C.errval = phibar_new; C.active = 0; C.done = 1; }
 }
 
+// The last CTA's update on the fast path (lane 0): the friction of the coming
+// step from the double-float sums and coefficients; the FP64 update is left
+// to split_apply_deferred.  Hilltop only: its kernels need no window.
+static __device__ __forceinline__ void split_scalars_fast(SplitCtl& C, const df64 (&S)[3]) {
+    const SplitPre& Q = C.pre;
+    df64 f[kPreN];
+#pragma unroll
+    for (int q = 0; q < kPreN; ++q) f[q] = df64{Q.hi[q], Q.lo[q]};
+    const int steps_done = C.steps_done;
+    df64 E = df_add(f[kPreC0], df_mul(f[kPreS0], S[0]));
+    E = df_add(E, df_mul(f[kPreS1], S[1]));
+    E = df_add(E, df_mul(f[kPreS2], S[2]));
+    const df64 x = df_add(f[kPreX0], df_mul(f[kPreX1], E));
+    const df64 ad2 = df_add(f[kPreA0], df_mul(f[kPreA1], df_sqrt(df_add(df64{1.f, 0.f}, x))));
+    const df64 adh = df_add(f[kPreAd], df_mul(f[kPreHd], ad2));
+    const df64 fr = df_mul(f[kPreCf], adh);
+    C.fric = __fadd_rn(fr.hi, fr.lo);
+    C.d = Q.d32;
+    C.lapl = Q.lapl;
+    C.pn = Q.pn;
+    C.kv = Q.kv;
+    C.srcAmp = Q.srcAmp;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        C.dsum_hi[q] = S[q].hi;
+        C.dsum_lo[q] = S[q].lo;
+    }
+    C.def_step = steps_done;
+    C.deferred = 1;
+    C.active = 1;
+    C.steps_done = steps_done + 1;
+}
+
+// The FP64 part of a fast-path update, by lane 0 of the calling warp: the
+// same arithmetic as split_scalars_pre, from the sums the fast path saved.
+static __device__ __noinline__ void split_apply_deferred(SplitCtl& C, double* a_trace) {
+    if ((threadIdx.x & 31) != 0 || !C.deferred) return;
+    double sums[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        sums[q] = df_to(df64{C.dsum_hi[q], C.dsum_lo[q]});
+        C.sums[q] = sums[q];
+    }
+    double friction, phibar_new;
+    pre_state_update(C, sums, a_trace, C.def_step, friction, phibar_new);
+    C.deferred = 0;
+}
+
 // After its tile, the first CTA of the step to get here forms the
 // precomputed part (warp 0); the others go on at once.
 __device__ __forceinline__ void maybe_precompute(SplitCtl* ctl, const PotDev& P, const SplitConst& K) {
     __shared__ int claimed;
     if (threadIdx.x == 0) claimed = atomicCAS(&ctl->pre_claim, 0, 1) == 0;
     __syncthreads();
-    if (claimed && threadIdx.x < 32) split_precompute(*ctl, P, K);
+    if (claimed && threadIdx.x < 32) {
+        split_apply_deferred(*ctl, nullptr);
+        split_precompute(*ctl, P, K, false);
+    }
 }
 
 // One lane, for the diagnostics that build a window outside the step.
@@ -498,15 +593,16 @@ __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, co
                                                  int nslots, int* state, bool toggle) {
     block_sum_df<3>(v);
     df64* pd = reinterpret_cast<df64*>(part);   // one df64 per double slot
+    // Only the partials need ordering before the arrival: the field stores
+    // are read by the next kernel, after this grid has completed.
+    __shared__ bool last;
     if (threadIdx.x == 0) {
         pd[3 * slot] = v[0];
         pd[3 * slot + 1] = v[1];
         pd[3 * slot + 2] = v[2];
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == (unsigned)nslots - 1);
     }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == (unsigned)nslots - 1);
     __syncthreads();
     if (!last) return;
     if (threadIdx.x < 32) {
@@ -518,29 +614,39 @@ __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, co
             tot[q].lo = __shfl_sync(0xffffffffu, tot[q].lo, 0);
         }
         SplitCtl& C = *ctl;
-        const double sums[3] = {df_to(tot[0]), df_to(tot[1]), df_to(tot[2])};
         int error = 0;
         if (threadIdx.x == 0) {
             *counter = 0;
             if (state && toggle) *state ^= 1;
-            C.sums[0] = sums[0];
-            C.sums[1] = sums[1];
-            C.sums[2] = sums[2];
             error = C.error;
         }
         error = __shfl_sync(0xffffffffu, error, 0);
         const int pre = C.pre_claim && C.pre.ok;
+        const int fast = pre && C.pre.fast;
         __syncwarp();
         if (threadIdx.x == 0) {
             C.pre_claim = 0;
             C.pre.ok = 0;
         }
-        if (error) {
-            if (threadIdx.x == 0) { C.active = 0; C.done = 1; }
-        } else if (pre) {
-            split_scalars_pre(C, P, sums, a_trace);
+        if (fast && !error) {
+            if (threadIdx.x == 0) split_scalars_fast(C, tot);
         } else {
-            split_scalars_warp(C, P, K, sums, a_trace);
+            // an update still deferred (only when no CTA of this step claimed the precompute)
+            split_apply_deferred(C, a_trace);
+            __syncwarp();
+            const double sums[3] = {df_to(tot[0]), df_to(tot[1]), df_to(tot[2])};
+            if (threadIdx.x == 0) {
+                C.sums[0] = sums[0];
+                C.sums[1] = sums[1];
+                C.sums[2] = sums[2];
+            }
+            if (error) {
+                if (threadIdx.x == 0) { C.active = 0; C.done = 1; }
+            } else if (pre) {
+                split_scalars_pre(C, P, sums, a_trace);
+            } else {
+                split_scalars_warp(C, P, K, sums, a_trace);
+            }
         }
         __syncwarp();
         if (threadIdx.x == 0 && state && C.done) *state |= 2;
@@ -648,6 +754,9 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 }
 template <int n>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory"); }
+// Barrier 1 over the first NT threads of the block (the warps that march).
+template <int NT>
+__device__ __forceinline__ void march_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(NT) : "memory"); }
 
 // Bulk asynchronous copies (TMA engine) into shared memory with mbarrier
 // completion: one instruction moves a whole row, and the threads only wait on
@@ -856,7 +965,9 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
 // with 128-bit shared and global accesses and the k +- 1 neighbours across
 // lanes come by warp shuffles.  The new planes are double-buffered, which
 // leaves one barrier per plane: iteration p finishes the differences of plane
-// p-1 and computes plane p.
+// p-1 and computes plane p.  A block is TJ + 2 warps: TJ + 1 march (rows
+// j0 .. j0+TJ), the last forms the precomputed part of the scalar update.
+__host__ __device__ inline int row4_threads(int TJ) { return (TJ + 2) * 32; }
 __host__ __device__ inline int split_row4_smem_floats(int TJ, int N, int PF) {
     return (3 + PF) * (TJ + 3) * N + (1 + PF) * (TJ + 1) * N + 2 * (TJ + 1) * N + 2 * (3 * kWin + 1);
 }
@@ -924,7 +1035,23 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     // way, wrote last, while part of it is still in L2.
     // Units u0 .. u1-1, unit u = (row tile u / N, plane u mod N): one march
     // along i per row tile the range touches.
-    for (long long u = rev ? u1 : u0; rev ? u > u0 : u < u1;) {
+    // The warp after the march warps forms the sum-independent part of this
+    // step's scalar update (split_precompute) in the first CTA to claim it,
+    // while the march warps stream; the march warps meet on barrier 1.
+    if (w == TJ + 1) {
+        int claimed = 0;
+        if (lane == 0) claimed = atomicCAS(&ctl->pre_claim, 0, 1) == 0;
+        claimed = __shfl_sync(0xffffffffu, claimed, 0);
+        if (claimed) {
+            // the FP64 part of the update that started this step, then the
+            // sum-independent part of the one that ends it
+            split_apply_deferred(*ctl, a_trace);
+            split_precompute(*ctl, P, K, true);
+            __threadfence();
+        }
+    }
+    const bool marcher = w <= TJ;
+    for (long long u = rev ? u1 : u0; marcher && (rev ? u > u0 : u < u1);) {
         // this march covers units [s, e) of one row tile
         long long s, e;
         if (rev) {
@@ -1038,7 +1165,7 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             } else {
                 cp_wait<PF - 1>();
             }
-            __syncthreads();
+            march_sync<NTH>();
             // planes PF ahead go into the slots of planes no longer read
             if (TMA) {
                 if (w == 0) {
@@ -1115,7 +1242,7 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         }
         if (!TMA) cp_wait<0>();
         G0 += (unsigned)(CH + PF + 2);
-        __syncthreads();   // the ring is refilled by the next march
+        march_sync<NTH>();   // the ring is refilled by the next march
     }
     if (TMA && !tma_ok) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ETIMEOUT) == 0) ctl->errval = 0.0;
@@ -1124,7 +1251,6 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    maybe_precompute(ctl, P, K);
     df64 v3[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }

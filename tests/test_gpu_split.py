@@ -164,3 +164,51 @@ def test_split_bulk_copy_staging_matches(N, shapes, engine, tables):
     base = out[shapes[0]][0]
     for sh, v in out.items():
         assert np.max(np.abs(v[0] - base)) <= 1e-6 * np.std(base - base.mean()), sh
+
+
+ROWCASE = {False: dict(L=10.0, dt=1e-3, V0=3.338e-13, ns=0.965, phi0=0.0935, dphi0=0.000796),
+           True: dict(L=10.0, dt=1e-3, V0=3e-9, ns=0.97, phi0=2.9181235049318586, dphi0=-0.06727651095116181)}
+
+
+@pytest.mark.parametrize("N,usr,shape", [(128, False, (16, 2, 0)), (128, True, (16, 2, 0)), (256, False, (16, 2, 9)),
+                                         (256, False, (4, 2, 7))])
+def test_split_row_kernel_matches_fp64(N, usr, shape, engine, tables):
+    """The vector row kernel (N >= 128) against the plain FP64 form from the
+    same device initial conditions, 300 steps.  With the hilltop potential the
+    last CTA of each step forms the friction in double-float arithmetic and the
+    FP64 update of the background follows in the next step; with the table it
+    runs the precomputed FP64 update.  Fields within 1e-4 of their spread and
+    a, ad, t relative 1e-9 after 120 steps; then the a(t) trace of a second
+    call within relative 1e-9 of the FP64 run's, and the stop on af at the
+    step the FP64 trace puts it."""
+    w = ROWCASE[usr]
+    pot = engine.POT_TABLE if usr else engine.POT_HILLTOP
+    runs, af = {}, 1e30
+    for form in (engine.FORM_FP64, engine.FORM_SPLIT):
+        lat = engine.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], potential=pot, form=form)
+        if usr:
+            lat.set_table(*tables)
+        if form == engine.FORM_SPLIT:
+            lat.set_shape(*shape)
+        H = lat.bunch_davies(7, w["phi0"], w["dphi0"])
+        bg = engine.Bg(0.0, 1.0, H, 0.0, 1.0)
+        lat.evolve_fields(0.5 * w["dt"], bg)
+        # two calls, the second from the first's end state; the split run's
+        # second call stops on a(t) crossing af, midway between the FP64 run's
+        # a after steps 100 and 101 of that call
+        assert lat.leapfrog(1e30, 120, bg) == 120
+        fields = (lat.download(engine.F), lat.download(engine.FD), bg.a, bg.ad, bg.t)
+        bg.astep = bg.a
+        taken, tr = lat.leapfrog(af, 180, bg, trace=True)
+        runs[form] = (lat, bg, taken, tr, fields)
+        af = 0.5 * (tr[99] + tr[100])
+    lf, bf, tf, trf, ff = runs[engine.FORM_FP64]
+    ls, bs, ts, trs, fs = runs[engine.FORM_SPLIT]
+    with ls, lf:
+        # after the first call: fields within 1e-4 of their spread, a, ad, t relative 1e-9
+        assert pert_err(fs[0], ff[0]) < 1e-4 and pert_err(fs[1], ff[1]) < 1e-4
+        for got, ref in zip(fs[2:], ff[2:]):
+            assert abs(got - ref) <= 1e-9 * abs(ref)
+        assert tf == 180 and ts == 101
+        assert np.all(np.abs(trs - trf[:ts]) <= 1e-9 * trf[:ts])
+        assert abs(bs.a - trf[ts - 1]) <= 1e-9 * trf[ts - 1]
