@@ -151,9 +151,10 @@ __device__ __forceinline__ df64 df_shfl_down(df64 v, int o) {
 __device__ __forceinline__ df64 Kahan::df() const { return df_two_sum(s, -c); }
 
 // Sum over the block of NV df64 values per thread in a fixed order (lane
-// trees, then warps in index order); result valid in thread 0.
+// trees, then warps in index order); the result is valid in lane 0 of warp
+// `leader`.  The one barrier is the last the other warps take part in.
 template <int NV>
-__device__ __forceinline__ void block_sum_df(df64 (&v)[NV]) {
+__device__ __forceinline__ void block_sum_df(df64 (&v)[NV], int leader) {
     __shared__ df64 sh[NV][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -165,7 +166,7 @@ __device__ __forceinline__ void block_sum_df(df64 (&v)[NV]) {
         for (int q = 0; q < NV; ++q) sh[q][w] = v[q];
     }
     __syncthreads();
-    if (w == 0) {
+    if (w == leader) {
         const int nw = (int)(blockDim.x >> 5);
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
@@ -174,22 +175,33 @@ __device__ __forceinline__ void block_sum_df(df64 (&v)[NV]) {
             for (int o = 16; o > 0; o >>= 1) v[q] = df_add(v[q], df_shfl_down(v[q], o));
         }
     }
-    __syncthreads();
 }
 
-// Sum of the df64 partials p[b*NV + q], b < nb, by one warp in a fixed order;
-// result valid in lane 0.
+// Sum of the df64 partials p[b*NV + q], b < nb, by one warp in a fixed order
+// (lane l adds slots l, l+32, ... in turn, then a lane tree); result valid in
+// lane 0.  The loads of up to 32*kBatch slots are all issued before the adds,
+// so the sum waits for about one L2 round trip per batch.
 template <int NV>
 __device__ __forceinline__ void sum_partials_df(const df64* p, int nb, df64 (&out)[NV]) {
+    constexpr int kBatch = 8;
     const int lane = threadIdx.x & 31;
+    const float2* src = reinterpret_cast<const float2*>(p);
 #pragma unroll
     for (int q = 0; q < NV; ++q) out[q] = df64{0.f, 0.f};
-#pragma unroll 4
-    for (int b = lane; b < nb; b += 32) {
+    for (int b0 = 0; b0 < nb; b0 += 32 * kBatch) {
+        float2 x[kBatch][NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) {
-            const float2 x = __ldcg(reinterpret_cast<const float2*>(p) + (size_t)b * NV + q);
-            out[q] = df_add(out[q], df64{x.x, x.y});
+        for (int i = 0; i < kBatch; ++i) {
+            const int b = b0 + lane + 32 * i;
+#pragma unroll
+            for (int q = 0; q < NV; ++q)
+                x[i][q] = b < nb ? __ldcg(src + (size_t)b * NV + q) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+            if (b0 + lane + 32 * i >= nb) break;
+#pragma unroll
+            for (int q = 0; q < NV; ++q) out[q] = df_add(out[q], df64{x[i][q].x, x[i][q].y});
         }
     }
 #pragma unroll
@@ -585,72 +597,75 @@ static __device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, c
 
 // Block sums into partial slot `slot` of `nslots`; the last of the nslots CTAs
 // to arrive adds the partials in slot order and runs the scalar update.
-// `state` (may be null) is the ensemble form's per-lattice word: that CTA
-// toggles its bit 0 (the ping-pong half) after a step (`toggle`), and sets
-// bit 1 once the lattice has stopped.
+// Warp `leader` publishes the CTA's partials and, in the last CTA, runs the
+// update; the other warps are done after the block sum.  A leader that
+// stored no field data fences only its partials.  `state` (may be null) is
+// the ensemble form's per-lattice word: that CTA toggles its bit 0 (the
+// ping-pong half) after a step (`toggle`), and sets bit 1 once the lattice
+// has stopped.
 __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                                  double* part, unsigned* counter, double* a_trace, int slot,
-                                                 int nslots, int* state, bool toggle) {
-    block_sum_df<3>(v);
+                                                 int nslots, int* state, bool toggle, int leader = 0) {
+    block_sum_df<3>(v, leader);
+    if ((int)(threadIdx.x >> 5) != leader) return;
+    const int lane = threadIdx.x & 31;
     df64* pd = reinterpret_cast<df64*>(part);   // one df64 per double slot
     // Only the partials need ordering before the arrival: the field stores
     // are read by the next kernel, after this grid has completed.
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
+    int last = 0;
+    if (lane == 0) {
         pd[3 * slot] = v[0];
         pd[3 * slot + 1] = v[1];
         pd[3 * slot + 2] = v[2];
         __threadfence();
         last = (atomicAdd(counter, 1u) == (unsigned)nslots - 1);
     }
-    __syncthreads();
+    last = __shfl_sync(0xffffffffu, last, 0);
     if (!last) return;
-    if (threadIdx.x < 32) {
-        df64 tot[3];
-        sum_partials_df<3>(pd, nslots, tot);
+    df64 tot[3];
+    sum_partials_df<3>(pd, nslots, tot);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            tot[q].hi = __shfl_sync(0xffffffffu, tot[q].hi, 0);
-            tot[q].lo = __shfl_sync(0xffffffffu, tot[q].lo, 0);
-        }
-        SplitCtl& C = *ctl;
-        int error = 0;
-        if (threadIdx.x == 0) {
-            *counter = 0;
-            if (state && toggle) *state ^= 1;
-            error = C.error;
-        }
-        error = __shfl_sync(0xffffffffu, error, 0);
-        const int pre = C.pre_claim && C.pre.ok;
-        const int fast = pre && C.pre.fast;
-        __syncwarp();
-        if (threadIdx.x == 0) {
-            C.pre_claim = 0;
-            C.pre.ok = 0;
-        }
-        if (fast && !error) {
-            if (threadIdx.x == 0) split_scalars_fast(C, tot);
-        } else {
-            // an update still deferred (only when no CTA of this step claimed the precompute)
-            split_apply_deferred(C, a_trace);
-            __syncwarp();
-            const double sums[3] = {df_to(tot[0]), df_to(tot[1]), df_to(tot[2])};
-            if (threadIdx.x == 0) {
-                C.sums[0] = sums[0];
-                C.sums[1] = sums[1];
-                C.sums[2] = sums[2];
-            }
-            if (error) {
-                if (threadIdx.x == 0) { C.active = 0; C.done = 1; }
-            } else if (pre) {
-                split_scalars_pre(C, P, sums, a_trace);
-            } else {
-                split_scalars_warp(C, P, K, sums, a_trace);
-            }
-        }
-        __syncwarp();
-        if (threadIdx.x == 0 && state && C.done) *state |= 2;
+    for (int q = 0; q < 3; ++q) {
+        tot[q].hi = __shfl_sync(0xffffffffu, tot[q].hi, 0);
+        tot[q].lo = __shfl_sync(0xffffffffu, tot[q].lo, 0);
     }
+    SplitCtl& C = *ctl;
+    int error = 0;
+    if (lane == 0) {
+        *counter = 0;
+        if (state && toggle) *state ^= 1;
+        error = C.error;
+    }
+    error = __shfl_sync(0xffffffffu, error, 0);
+    const int pre = C.pre_claim && C.pre.ok;
+    const int fast = pre && C.pre.fast;
+    __syncwarp();
+    if (lane == 0) {
+        C.pre_claim = 0;
+        C.pre.ok = 0;
+    }
+    if (fast && !error) {
+        if (lane == 0) split_scalars_fast(C, tot);
+    } else {
+        // an update still deferred (only when no CTA of this step claimed the precompute)
+        split_apply_deferred(C, a_trace);
+        __syncwarp();
+        const double sums[3] = {df_to(tot[0]), df_to(tot[1]), df_to(tot[2])};
+        if (lane == 0) {
+            C.sums[0] = sums[0];
+            C.sums[1] = sums[1];
+            C.sums[2] = sums[2];
+        }
+        if (error) {
+            if (lane == 0) { C.active = 0; C.done = 1; }
+        } else if (pre) {
+            split_scalars_pre(C, P, sums, a_trace);
+        } else {
+            split_scalars_warp(C, P, K, sums, a_trace);
+        }
+    }
+    __syncwarp();
+    if (lane == 0 && state && C.done) *state |= 2;
 }
 
 __device__ __forceinline__ void finish_sums(df64 (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
@@ -1252,7 +1267,7 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
     df64 v3[3] = {g.df(), s1.df(), s2.df()};
-    finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
+    finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true, TJ + 1);
 }
 
 // Whole-plane variant of the step for small lattices (N = 32, 64): a CTA owns
