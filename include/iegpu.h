@@ -156,8 +156,9 @@ int  iegpu_profile_leapfrog(struct iegpu_ctx* ctx, double af, int nsteps, iegpu_
 int  iegpu_autotune(struct iegpu_ctx* ctx, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
 /* Split form, 32 <= N <= 512: fix the step kernel's launch shape instead of
  * tuning it: rows per tile 4 or 8 with 1 or 2 planes prefetched (rows 4 at
- * N >= 128 also 3 or 4), or rows = N for whole planes (N = 32, 64) with 2 or
- * 4; 1 <= chunks <= N/8 plane chunks, or chunks = 0 (N >= 128) for one wave
+ * N >= 128 also 3 or 4), rows 16 at 128 <= N <= 256 with 1 to 3, or rows = N
+ * for whole planes (N = 32, 64) with 2 or 4; 1 <= chunks <= N/8 plane
+ * chunks, or chunks = 0 (N >= 128) for one wave
  * of CTAs that each take an equal share of the lattice.  prefetch + 10 stages
  * the planes by bulk (TMA) copies instead (N >= 128: rows 8 with 2 planes
  * ahead, rows 16 at N <= 256 with 1 to 3); iegpu_autotune reports that

@@ -615,9 +615,10 @@ static void rows4_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
     } else if (g.TJ == 8) {
         if (g.PF == 1) rows4_one<TAB, C4, 8, 1>(c, B, K, grid, g); else rows4_one<TAB, C4, 8, 2>(c, B, K, grid, g);
     } else if (C4 <= 2) {
-        // 16-row tiles: one CTA of 17 warps per SM
+        // 16-row tiles: one CTA of 18 warps per SM
         if (g.PF == 1) rows4_one<TAB, (C4 <= 2 ? C4 : 2), 16, 1>(c, B, K, grid, g);
-        else rows4_one<TAB, (C4 <= 2 ? C4 : 2), 16, 2>(c, B, K, grid, g);
+        else if (g.PF == 2) rows4_one<TAB, (C4 <= 2 ? C4 : 2), 16, 2>(c, B, K, grid, g);
+        else rows4_one<TAB, (C4 <= 2 ? C4 : 2), 16, 3>(c, B, K, grid, g);
     }
 }
 
@@ -776,7 +777,7 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
     for (int TJ : {4, 8, 16}) {
         if (TJ > N || (TJ == 16 && (N < 128 || N > 256))) continue;
         for (int PF : {1, 2, 3, 4}) {
-            if (PF > 2 && (TJ != 4 || N < 128)) continue;
+            if (PF > 2 && !((TJ == 4 && N >= 128) || (TJ == 16 && PF == 3))) continue;
             const int per_sm = row_ctas_per_sm(N, TJ, PF);
             if (per_sm < 1) continue;
             const int tiles = N / TJ;
@@ -876,15 +877,17 @@ int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     }
     if (N < 32 || N > 512) return set_error(c, IEGPU_EUNSUPPORTED, "the row kernel covers 32 <= N <= 512");
     const bool plane = plane_shape(N, rows);
-    const bool deep = rows == 4 && N >= 128 && (prefetch == 3 || prefetch == 4);
+    const bool deep = (rows == 4 && N >= 128 && (prefetch == 3 || prefetch == 4)) ||
+                      (rows == 16 && N >= 128 && N <= 256 && prefetch == 3);
     const bool balanced = chunks == 0 && !plane && N >= 128;
     const bool wide = rows == 16 && N >= 128 && N <= 256;
     if ((!plane && ((rows != 4 && rows != 8 && !wide) || ((prefetch != 1 && prefetch != 2) && !deep))) ||
         (plane && prefetch != 2 && prefetch != 4) || (!balanced && (chunks < 1 || chunks > N / 8)))
         return set_error(c, IEGPU_EINVAL,
-                         "shape: rows 4|8 with prefetch 1|2 (rows 4 and N >= 128 also 3|4), or rows N "
-                         "(N <= 64, whole planes) with prefetch 2|4; 1 <= chunks <= N/8, or chunks 0 "
-                         "(N >= 128: one wave of CTAs with equal shares)");
+                         "shape: rows 4|8 with prefetch 1|2 (rows 4 and N >= 128 also 3|4), rows 16 "
+                         "(128 <= N <= 256) with prefetch 1..3, or rows N (N <= 64, whole planes) with "
+                         "prefetch 2|4; 1 <= chunks <= N/8, or chunks 0 (N >= 128: one wave of CTAs with "
+                         "equal shares)");
     const long long ctas = balanced ? balanced_ctas(c, N, rows, prefetch) : (long long)(N / rows) * chunks;
     if (3LL * ctas > c->part_cap || row_ctas_per_sm(N, rows, prefetch) < 1)
         return set_error(c, IEGPU_EINVAL, "shape does not fit this lattice's scratch");

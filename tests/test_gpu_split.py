@@ -170,7 +170,7 @@ ROWCASE = {False: dict(L=10.0, dt=1e-3, V0=3.338e-13, ns=0.965, phi0=0.0935, dph
            True: dict(L=10.0, dt=1e-3, V0=3e-9, ns=0.97, phi0=2.9181235049318586, dphi0=-0.06727651095116181)}
 
 
-@pytest.mark.parametrize("N,usr,shape", [(128, False, (16, 2, 0)), (128, True, (16, 2, 0)), (256, False, (16, 2, 9)),
+@pytest.mark.parametrize("N,usr,shape", [(128, False, (16, 2, 0)), (128, True, (16, 3, 0)), (256, False, (16, 3, 9)),
                                          (256, False, (4, 2, 7))])
 def test_split_row_kernel_matches_fp64(N, usr, shape, engine, tables):
     """The vector row kernel (N >= 128) against the plain FP64 form from the
