@@ -449,13 +449,14 @@ def engine_arm(args):
                       "sigw": sigw},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None if tr is None else tr * N ** 3,
-                         "kernel": "k_split_rows4 (fused kick + drift + next-step Friedmann sums, N >= 128; k_split_rows below)",
+                         "kernel": "k_split_rows4_persist (fused kick + drift + next-step Friedmann sums; 64 steps per cooperative "
+                                   "launch at 128 <= N <= 256, k_split_rows4 one step per launch otherwise)",
                          "algorithmic_bytes_per_site": BYTES_STEP_SPLIT, "kernel_ms": kernel_ms,
                          "kernel_ms_source": "timed region (CUDA events on the lattice's stream) less the one "
-                                             "priming reduction, divided by the step-kernel launches",
+                                             "priming reduction, divided by the steps",
                          "kernel_ms_isolated": sp["kernel_ms"],
-                         "kernel_ms_isolated_source": "the same kernel launched alone between two events with a "
-                                                     "host synchronisation (no overlap of consecutive launches)",
+                         "kernel_ms_isolated_source": "k_split_rows4, one step per launch, each launched alone "
+                                                     "between two events with a host synchronisation",
                          "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)"},
             "gpu_launches": sp["launches"], "clocks": sp["clocks"], "e2e": e2e}
     line["metric_note"] = ("value: split form at 256^3; forms.fp64: plain FP64 form, same workload; "

@@ -164,6 +164,12 @@ int  iegpu_autotune(struct iegpu_ctx* ctx, const iegpu_bg* bg, int* rows, int* p
  * ahead, rows 16 at N <= 256 with 1 to 3); iegpu_autotune reports that
  * encoding too. */
 int  iegpu_set_shape(struct iegpu_ctx* ctx, int rows, int prefetch, int chunks);
+/* Split form, 128 <= N <= 256 without SIGW: iegpu_leapfrog runs the step kernel for
+ * up to 64 steps per cooperative launch (on = 1, the default), each step's
+ * first copies overlapping the scalar update of the step before, or one
+ * launch per step in CUDA graphs (on = 0).  Both give the same bits.  No
+ * counterpart in the reference (its loop is serial host code). */
+int  iegpu_set_persistent(struct iegpu_ctx* ctx, int on);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */
 /* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */

@@ -208,7 +208,7 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
             }
         }
     }
-    if (!rc) rc = dalloc(c, &c->counter, 1);
+    if (!rc) rc = dalloc(c, &c->counter, 4);   // [0] last-CTA detection, [2..3] persistent step sync
     if (!rc) rc = dalloc(c, &c->spec_part, (size_t)c->spec_blocks * nb + 65536);
     if (!rc) rc = dalloc(c, &c->spec_cnt, (size_t)c->spec_blocks * nb);
     if (!rc) rc = dalloc(c, &c->misc, (size_t)4 * nb + N + 64);
@@ -230,7 +230,7 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
             cudaMemsetAsync(c->hdny[q], 0, sizeof(float) * ny, c->stream);
         }
         cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), c->stream);
-        cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream);
+        cudaMemsetAsync(c->counter, 0, 4 * sizeof(unsigned), c->stream);
         rc = sync_and_check(c, "create");
     }
     // hilltop constants with the reference's evaluation order (src/potential.cpp:77-83)
@@ -537,6 +537,13 @@ int iegpu_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     if (!c) return IEGPU_EINVAL;
     if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "the launch shape belongs to the split form");
     return split_set_shape(c, rows, prefetch, chunks);
+}
+
+int iegpu_set_persistent(iegpu_ctx* c, int on) {
+    if (!c) return IEGPU_EINVAL;
+    if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "persistent launches belong to the split form");
+    c->persist = on != 0;
+    return IEGPU_OK;
 }
 
 int iegpu_means(iegpu_ctx* c, double out[3]) {

@@ -175,6 +175,7 @@ struct iegpu_ctx {
     int N = 0, lg = 0;
     size_t gs = 0;          // N^3
     int sms = 0;
+    int persist = 1;   // split form, vector row kernel: many steps per cooperative launch
     cudaStream_t stream = nullptr;
     std::string err;
     long long launches = 0;

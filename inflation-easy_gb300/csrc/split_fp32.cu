@@ -229,6 +229,83 @@ __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4(SplitBufs B, Spli
                                        blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr, rev != 0);
 }
 
+// Polls *p (acquire) until it reaches v: at most kSpinPolls polls with a short
+// sleep between them (about half a second in all), far beyond any step's
+// length.  On giving up it marks the step IEGPU_ETIMEOUT and returns false.
+constexpr unsigned kSpinPolls = 1u << 20;
+__device__ __forceinline__ bool spin_until(const unsigned* p, unsigned v, SplitCtl* ctl) {
+    for (unsigned t = 0; t < kSpinPolls; ++t) {
+        if (ld_acquire(p) >= v) return true;
+        __nanosleep(64);
+    }
+    if (atomicCAS(&ctl->error, 0, IEGPU_ETIMEOUT) == 0) ctl->errval = 0.0;
+    return false;
+}
+
+// The vector row kernel for `nsteps` consecutive steps in one cooperative
+// launch (every CTA resident), cp.async staging.  Step s reads the buffers of
+// parity (start + s) & 1 and marches in that direction, as the one-step
+// kernel.  Between steps a CTA waits until all CTAs have arrived at the step
+// before (its fields are complete), issues the first copies of its range,
+// and only then waits for the step's scalar update (sync[1] = s): the copies
+// overlap the last CTA's sums and update.  sync[0] counts the arrivals of the
+// launch; both words are zero at the launch.  The waits are made by lane 0
+// of the precompute warp; a wait that gives up ends every CTA's loop.
+template <bool TABLE, int C4, int TJ, int PF>
+__global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4_persist(SplitBufs B0, SplitBufs B1, SplitCtl* ctl,
+                                                                       PotDev P, SplitConst K, double* part,
+                                                                       unsigned* sync, double* a_trace, int chunks,
+                                                                       int start, int nsteps) {
+    constexpr int N = 128 * C4, NTH = (TJ + 1) * 32, PHS = 3 + PF, RP = (TJ + 3) * N;
+    extern __shared__ __align__(16) float smem[];
+    float* ring = smem;
+    float* pis = ring + PHS * RP;
+    __shared__ int go_fields, go_update;
+    long long u0, u1;
+    if (chunks == 0) {
+        const long long total = (long long)(N / TJ) * N;
+        u0 = total * blockIdx.x / gridDim.x;
+        u1 = total * (blockIdx.x + 1) / gridDim.x;
+    } else {
+        const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
+        const int CH = (int)(((long long)(blockIdx.y + 1) * N) / chunks) - i0;
+        u0 = (long long)blockIdx.x * N + i0;
+        u1 = u0 + CH;
+    }
+    const int slot = blockIdx.x + gridDim.x * blockIdx.y, nslots = gridDim.x * gridDim.y;
+    for (int s = 0; s < nsteps; ++s) {
+        const int src = (start + s) & 1;
+        SplitBufs B;
+        B.xs = src ? B1.xs : B0.xs;
+        B.xd = src ? B1.xd : B0.xd;
+        B.ps = src ? B1.ps : B0.ps;
+        B.pd = src ? B1.pd : B0.pd;
+        const bool rev = src != 0;
+        if (s > 0) {
+            if (threadIdx.x == NTH) go_fields = spin_until(sync, (unsigned)(s * nslots), ctl);
+            __syncthreads();
+            if (!go_fields) break;
+            if (threadIdx.x < NTH && u0 < u1) {
+                long long u = rev ? u1 : u0;
+                row4_issue_start<C4, TJ, PF>(ring, pis, B, row4_march<N, TJ>(u, u0, u1, rev));
+            }
+            if (threadIdx.x == NTH) go_update = spin_until(sync + 1, (unsigned)s, ctl);
+            __syncthreads();
+            if (!go_update) {
+                cp_wait<0>();
+                break;
+            }
+        }
+        StepSeq sq;
+        sq.seq = sync + 1;
+        sq.base = (unsigned)(s * nslots);
+        sq.val = (unsigned)(s + 1);
+        if (!rows4_body<TABLE, C4, TJ, PF, false>(B, ctl, P, K, part, sync, a_trace, u0, u1, slot, nslots, nullptr, rev,
+                                                  s > 0, sq))
+            break;
+    }
+}
+
 // Whole planes (N = 32, 64): block y = chunk of planes.
 template <bool TABLE, int N, int NT, int PF>
 __global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_split_plane(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
@@ -676,6 +753,95 @@ static void launch_step(iegpu_ctx* c, int src) {
     c->launches++;
 }
 
+// ---- persistent launches (vector row kernel) ------------------------------
+
+constexpr int kPersistSteps = 64;   // steps per cooperative launch
+
+// Launches k_split_rows4_persist of one shape for `nsteps` steps from buffer
+// parity `start`; 1 if the shape's grid is not resident all at once (the
+// caller then steps kernel by kernel), -1 on a launch error.
+template <bool TAB, int C4, int TJV, int PFV>
+static int persist_one(iegpu_ctx* c, int start, int nsteps, dim3 grid, const StepGeom& g, bool check_only) {
+    auto kern = k_split_rows4_persist<TAB, C4, TJV, PFV>;
+    static size_t attr = 0;
+    if (attr < g.smem) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        attr = g.smem;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, row4_threads(TJV), g.smem) != cudaSuccess ||
+        (long long)per_sm * c->sms < (long long)grid.x * grid.y) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (check_only) return 0;
+    const SplitConst K = split_const(c);
+    const SplitBufs B0{c->sp[0], c->sp[1], c->spi[0], c->spi[1]};
+    const SplitBufs B1{c->sp[1], c->sp[0], c->spi[1], c->spi[0]};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(row4_threads(TJV));
+    cfg.dynamicSmemBytes = g.smem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    unsigned* sync = c->counter + 2;
+    if (cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), c->stream) != cudaSuccess) return -1;
+    if (cudaLaunchKernelEx(&cfg, kern, B0, B1, c->sctl, c->pot, K, c->part, sync, c->a_trace, g.chunks, start,
+                           nsteps) != cudaSuccess)
+        return -1;
+    c->launches++;
+    return 0;
+}
+
+template <bool TAB, int C4>
+static int persist_tj(iegpu_ctx* c, int start, int nsteps, dim3 grid, const StepGeom& g, bool check_only) {
+    if (g.TJ == 4) {
+        switch (g.PF) {
+            case 1: return persist_one<TAB, C4, 4, 1>(c, start, nsteps, grid, g, check_only);
+            case 2: return persist_one<TAB, C4, 4, 2>(c, start, nsteps, grid, g, check_only);
+            case 3: return persist_one<TAB, C4, 4, 3>(c, start, nsteps, grid, g, check_only);
+            default: return persist_one<TAB, C4, 4, 4>(c, start, nsteps, grid, g, check_only);
+        }
+    }
+    if (g.TJ == 8) {
+        if (g.PF == 1) return persist_one<TAB, C4, 8, 1>(c, start, nsteps, grid, g, check_only);
+        return persist_one<TAB, C4, 8, 2>(c, start, nsteps, grid, g, check_only);
+    }
+    if (C4 <= 2) {
+        constexpr int CW = C4 <= 2 ? C4 : 2;
+        if (g.PF == 1) return persist_one<TAB, CW, 16, 1>(c, start, nsteps, grid, g, check_only);
+        if (g.PF == 2) return persist_one<TAB, CW, 16, 2>(c, start, nsteps, grid, g, check_only);
+        return persist_one<TAB, CW, 16, 3>(c, start, nsteps, grid, g, check_only);
+    }
+    return 1;
+}
+
+// 0: launched (or would launch, check_only); 1: this lattice steps kernel by
+// kernel (persistent launches off, SIGW, N outside 128..256, bulk-copy
+// staging, or a grid that is not resident at once); -1: launch error.
+static int launch_persist(iegpu_ctx* c, int start, int nsteps, bool check_only) {
+    // At N = 512 the step is long enough that the launch gap is noise, and the
+    // persistent kernel measured slower (397 vs 378 us at 512^3).
+    if (!c->persist || c->cfg.sigw || c->N < 128 || c->N > 256) return 1;
+    const StepGeom g = step_geom(c);
+    if (!g.rows || g.tma) return 1;
+    const dim3 grid(g.tiles, g.chunks > 0 ? g.chunks : 1);
+    const bool tab = c->pot.table != 0;
+    switch (c->N) {
+        case 128: return tab ? persist_tj<true, 1>(c, start, nsteps, grid, g, check_only)
+                             : persist_tj<false, 1>(c, start, nsteps, grid, g, check_only);
+        case 256: return tab ? persist_tj<true, 2>(c, start, nsteps, grid, g, check_only)
+                             : persist_tj<false, 2>(c, start, nsteps, grid, g, check_only);
+        case 512: return tab ? persist_tj<true, 4>(c, start, nsteps, grid, g, check_only)
+                             : persist_tj<false, 4>(c, start, nsteps, grid, g, check_only);
+        default: return 1;
+    }
+}
+
 void split_destroy_graphs(iegpu_ctx* c) {
     for (int p = 0; p < 2; ++p) {
         if (c->sp_exec[p]) cudaGraphExecDestroy(c->sp_exec[p]);
@@ -713,7 +879,7 @@ static int sctl_down(iegpu_ctx* c) {
     if (c->sctl_h->deferred)
         return set_error(c, IEGPU_ECUDA, "internal: a scalar update was left unapplied at the end of a call");
     if (c->sctl_h->error == IEGPU_ETIMEOUT)
-        return set_error(c, IEGPU_ETIMEOUT, "a bulk copy into shared memory did not complete");
+        return set_error(c, IEGPU_ETIMEOUT, "a wait in the step kernel gave up (bulk copy or step barrier)");
     if (c->sctl_h->error == IEGPU_ERANGE) {
         return set_error(c, IEGPU_ERANGE,
                          "Field value near %.17g is outside the numerical potential range [%.17g, %.17g].\n",
@@ -919,7 +1085,8 @@ int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* st
         split_destroy_graphs(c);
         fp64_destroy_graphs(c);
     }
-    if (!c->sp_exec[0]) {
+    const bool persist = launch_persist(c, c->cur, 0, true) == 0;
+    if (!persist && !c->sp_exec[0]) {
         int rc = split_build_graphs(c);
         if (rc) return rc;
     }
@@ -929,11 +1096,20 @@ int split_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* st
     if (sctl_up(c)) return IEGPU_ECUDA;
     const int start = c->cur;
     launch_prime(c, start);  // sums of the current state -> coefficients of step 0
-    const int L = c->sp_steps;
-    const int launches = (max_steps + L - 1) / L;
-    for (int q = 0; q < launches; ++q) {
-        if (check_cuda(c, cudaGraphLaunch(c->sp_exec[start], c->stream), "graph launch")) return IEGPU_ECUDA;
-        c->launches += (long long)L * (c->cfg.sigw ? 2 : 1);
+    if (persist) {
+        for (int done = 0; done < max_steps; done += kPersistSteps) {
+            const int n = max_steps - done < kPersistSteps ? max_steps - done : kPersistSteps;
+            if (launch_persist(c, (start + done) & 1, n, false) != 0)
+                return check_cuda(c, cudaGetLastError(), "persistent launch") ? IEGPU_ECUDA
+                                                                                : set_error(c, IEGPU_ECUDA, "persistent launch");
+        }
+    } else {
+        const int L = c->sp_steps;
+        const int launches = (max_steps + L - 1) / L;
+        for (int q = 0; q < launches; ++q) {
+            if (check_cuda(c, cudaGraphLaunch(c->sp_exec[start], c->stream), "graph launch")) return IEGPU_ECUDA;
+            c->launches += (long long)L * (c->cfg.sigw ? 2 : 1);
+        }
     }
     int rc = sctl_down(c);
     const int taken = c->sctl_h->steps_done;

@@ -595,30 +595,49 @@ static __device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, c
     W.ok = 1;
 }
 
+// Publication of a step's scalar update to the other CTAs of a persistent
+// launch: `seq` is set to `val` after the update's writes.
+struct StepSeq {
+    unsigned* seq = nullptr;   // null: one step per kernel
+    unsigned base = 0;         // arrivals of the launch's earlier steps
+    unsigned val = 0;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
 // Block sums into partial slot `slot` of `nslots`; the last of the nslots CTAs
 // to arrive adds the partials in slot order and runs the scalar update.
 // Warp `leader` publishes the CTA's partials and, in the last CTA, runs the
-// update; the other warps are done after the block sum.  A leader that
-// stored no field data fences only its partials.  `state` (may be null) is
-// the ensemble form's per-lattice word: that CTA toggles its bit 0 (the
-// ping-pong half) after a step (`toggle`), and sets bit 1 once the lattice
-// has stopped.
+// update; the other warps are done after the block sum.  The CTA barrier in
+// the block sum orders every thread's field stores before the leader's fence
+// and arrival, which a persistent launch relies on (the next step of a
+// one-step kernel reads them after this grid has completed).  `state` (may be
+// null) is the ensemble form's per-lattice word: that CTA toggles its bit 0
+// (the ping-pong half) after a step (`toggle`), and sets bit 1 once the
+// lattice has stopped.  With `sq.seq`, arrivals count on from `sq.base`
+// without a reset and the last CTA sets *sq.seq = sq.val after the update.
 __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                                  double* part, unsigned* counter, double* a_trace, int slot,
-                                                 int nslots, int* state, bool toggle, int leader = 0) {
+                                                 int nslots, int* state, bool toggle, int leader = 0,
+                                                 StepSeq sq = StepSeq()) {
     block_sum_df<3>(v, leader);
     if ((int)(threadIdx.x >> 5) != leader) return;
     const int lane = threadIdx.x & 31;
     df64* pd = reinterpret_cast<df64*>(part);   // one df64 per double slot
-    // Only the partials need ordering before the arrival: the field stores
-    // are read by the next kernel, after this grid has completed.
     int last = 0;
     if (lane == 0) {
         pd[3 * slot] = v[0];
         pd[3 * slot + 1] = v[1];
         pd[3 * slot + 2] = v[2];
         __threadfence();
-        last = (atomicAdd(counter, 1u) == (unsigned)nslots - 1);
+        last = (atomicAdd(counter, 1u) == sq.base + (unsigned)nslots - 1);
     }
     last = __shfl_sync(0xffffffffu, last, 0);
     if (!last) return;
@@ -632,7 +651,7 @@ __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, co
     SplitCtl& C = *ctl;
     int error = 0;
     if (lane == 0) {
-        *counter = 0;
+        if (!sq.seq) *counter = 0;
         if (state && toggle) *state ^= 1;
         error = C.error;
     }
@@ -666,6 +685,10 @@ __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, co
     }
     __syncwarp();
     if (lane == 0 && state && C.done) *state |= 2;
+    if (lane == 0 && sq.seq) {
+        __threadfence();
+        st_release(sq.seq, sq.val);
+    }
 }
 
 __device__ __forceinline__ void finish_sums(df64 (&v)[3], SplitCtl* ctl, const PotDev& P, const SplitConst& K,
@@ -990,10 +1013,82 @@ __host__ __device__ inline int split_row4_smem_floats(int TJ, int N, int PF) {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
+// Geometry of one march of the vector row kernel: the units [s, e) of one
+// row tile that a march over a CTA's range [u0, u1) covers next, from the
+// running unit u (moved past them); planes i0 .. i0+CH-1 of rows j0 .. j0+TJ-1.
+struct Row4March {
+    long long s, e;
+    int j0, i0, CH;
+    bool rev;
+    __device__ __forceinline__ int plane(int q) const { return rev ? i0 + CH - 1 - q : i0 + q; }
+};
+template <int N, int TJ>
+__device__ __forceinline__ Row4March row4_march(long long& u, long long u0, long long u1, bool rev) {
+    Row4March M;
+    if (rev) {
+        M.e = u;
+        M.s = ((M.e - 1) / N) * N;
+        if (M.s < u0) M.s = u0;
+        u = M.s;
+    } else {
+        M.s = u;
+        M.e = (M.s / N + 1) * N;
+        if (M.e > u1) M.e = u1;
+        u = M.e;
+    }
+    M.j0 = (int)(M.s / N) * TJ;
+    M.i0 = (int)(M.s % N);
+    M.CH = (int)(M.e - M.s);
+    M.rev = rev;
+    return M;
+}
+
+// cp.async copies of march position q into its ring slots, by the NTH march
+// threads: dphi rows j0-1 .. j0+TJ+1 (slot (q+1) mod PHS), dpi rows j0 ..
+// j0+TJ (slot q mod PIS).
+template <int C4, int TJ, int PF>
+__device__ __forceinline__ void row4_issue_phi(float* ring, const float* xs, const Row4March& M, int q) {
+    constexpr int N = 128 * C4, m = N - 1, lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
+    constexpr int RP = (TJ + 3) * N, NTH = (TJ + 1) * 32, PHS = 3 + PF;
+    float* dst = ring + ((q + 1) % PHS) * RP;
+    const float* src = xs + ((long long)(M.plane(q) & m) << (2 * lgN));
+    constexpr int ops = (TJ + 3) * (N / 4);
+    for (int o = threadIdx.x; o < ops; o += NTH) {
+        const int r = o / (N / 4), c = o - r * (N / 4);
+        cp_async16(dst + r * N + 4 * c, src + ((long long)((M.j0 + r - 1) & m) << lgN) + 4 * c);
+    }
+}
+template <int C4, int TJ, int PF>
+__device__ __forceinline__ void row4_issue_pi(float* pis, const float* ps, const Row4March& M, int q) {
+    constexpr int N = 128 * C4, m = N - 1, lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
+    constexpr int PP = (TJ + 1) * N, NTH = (TJ + 1) * 32, PIS = 1 + PF;
+    float* dst = pis + (q % PIS) * PP;
+    const float* src = ps + ((long long)(M.plane(q) & m) << (2 * lgN));
+    constexpr int ops = (TJ + 1) * (N / 4);
+    for (int o = threadIdx.x; o < ops; o += NTH) {
+        const int r = o / (N / 4), c = o - r * (N / 4);
+        cp_async16(dst + r * N + 4 * c, src + ((long long)((M.j0 + r) & m) << lgN) + 4 * c);
+    }
+}
+// The copies a march starts with: dphi positions -1 and 0 (one group), then
+// PF groups of dphi position q+1 and dpi position q.
+template <int C4, int TJ, int PF>
+__device__ __forceinline__ void row4_issue_start(float* ring, float* pis, const SplitBufs& B, const Row4March& M) {
+    row4_issue_phi<C4, TJ, PF>(ring, B.xs, M, -1);
+    row4_issue_phi<C4, TJ, PF>(ring, B.xs, M, 0);
+    cp_commit();
+    for (int q = 0; q < PF; ++q) {
+        if (q + 1 <= M.CH + 1) row4_issue_phi<C4, TJ, PF>(ring, B.xs, M, 1 + q);
+        if (q <= M.CH) row4_issue_pi<C4, TJ, PF>(pis, B.ps, M, q);
+        cp_commit();
+    }
+}
+
 template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
-__device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
+__device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                            double* part, unsigned* counter, double* a_trace, long long u0,
-                                           long long u1, int slot, int nslots, int* state, bool rev) {
+                                           long long u1, int slot, int nslots, int* state, bool rev,
+                                           bool preissued = false, StepSeq sq = StepSeq()) {
     constexpr int N = 128 * C4, m = N - 1;
     constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
     constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
@@ -1007,22 +1102,28 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     __shared__ int nk_s, nv_s, active_s;
     __shared__ float cf[6];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    // the control block is read through L2: in a persistent launch the last
+    // CTA of the step before wrote it during this kernel
     if (tid == 0) {
         const SplitCtl& Cc = *ctl;
-        active_s = Cc.active;
-        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
-        nk_s = Cc.wk.n;
-        nv_s = Cc.wv.n;
+        active_s = __ldcg(&Cc.active);
+        cf[0] = __ldcg(&Cc.d); cf[1] = __ldcg(&Cc.lapl); cf[2] = __ldcg(&Cc.fric);
+        cf[3] = __ldcg(&Cc.pn); cf[4] = __ldcg(&Cc.kv);
+        nk_s = __ldcg(&Cc.wk.n);
+        nv_s = __ldcg(&Cc.wv.n);
     }
     if (TABLE) {
-        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q <= kWin; q += NTH) { wk[q] = __ldcg(&ctl->wk.u[q]); wv[q] = __ldcg(&ctl->wv.u[q]); }
         for (int q = tid; q < kWin; q += NTH) {
-            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
-            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+            wk[kWin + 1 + q] = __ldcg(&ctl->wk.A[q]); wk[2 * kWin + 1 + q] = __ldcg(&ctl->wk.s[q]);
+            wv[kWin + 1 + q] = __ldcg(&ctl->wv.A[q]); wv[2 * kWin + 1 + q] = __ldcg(&ctl->wv.s[q]);
         }
     }
     __syncthreads();
-    if (!active_s) return;
+    if (!active_s) {
+        if (!TMA) cp_wait<0>();   // copies a persistent launch issued ahead
+        return false;
+    }
     const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
     const int nk = nk_s, nv = nv_s;
     const WinCache ck = win_cache<TABLE>(wk, nk), cv = win_cache<TABLE>(wv, nv);
@@ -1066,42 +1167,15 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         }
     }
     const bool marcher = w <= TJ;
+    bool first = true;
     for (long long u = rev ? u1 : u0; marcher && (rev ? u > u0 : u < u1);) {
         // this march covers units [s, e) of one row tile
-        long long s, e;
-        if (rev) {
-            e = u;
-            s = ((e - 1) / N) * N;
-            if (s < u0) s = u0;
-            u = s;
-        } else {
-            s = u;
-            e = (s / N + 1) * N;
-            if (e > u1) e = u1;
-            u = e;
-        }
-        const int j0 = (int)(s / N) * TJ, i0 = (int)(s % N);
-        const int CH = (int)(e - s);
+        const Row4March M = row4_march<N, TJ>(u, u0, u1, rev);
+        const int j0 = M.j0, i0 = M.i0, CH = M.CH;
         // march position q -> plane; q = -1 and q = CH are the halo planes
-        auto plane = [&](int q) { return rev ? i0 + CH - 1 - q : i0 + q; };
-        auto issue_phi = [&](int q) {
-            float* dst = ring + ((q + 1) % PHS) * RP;
-            const float* src = B.xs + ((long long)(plane(q) & m) << (2 * lgN));
-            constexpr int ops = (TJ + 3) * (N / 4);
-            for (int o = tid; o < ops; o += NTH) {
-                const int r = o / (N / 4), c = o - r * (N / 4);
-                cp_async16(dst + r * N + 4 * c, src + ((long long)((j0 + r - 1) & m) << lgN) + 4 * c);
-            }
-        };
-        auto issue_pi = [&](int q) {
-            float* dst = pis + (q % PIS) * PP;
-            const float* src = B.ps + ((long long)(plane(q) & m) << (2 * lgN));
-            constexpr int ops = (TJ + 1) * (N / 4);
-            for (int o = tid; o < ops; o += NTH) {
-                const int r = o / (N / 4), c = o - r * (N / 4);
-                cp_async16(dst + r * N + 4 * c, src + ((long long)((j0 + r) & m) << lgN) + 4 * c);
-            }
-        };
+        auto plane = [&](int q) { return M.plane(q); };
+        auto issue_phi = [&](int q) { row4_issue_phi<C4, TJ, PF>(ring, B.xs, M, q); };
+        auto issue_pi = [&](int q) { row4_issue_pi<C4, TJ, PF>(pis, B.ps, M, q); };
         // TMA group g, issued by warp 0 (lane 0 arms the barrier first)
         auto issue_group = [&](int gi) {
             unsigned long long* bar = &bars[(G0 + (unsigned)(gi + 1)) % NB];
@@ -1136,16 +1210,10 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 issue_group(-1);
                 for (int q = 0; q < PF; ++q) issue_group(q);
             }
-        } else {
-            issue_phi(-1);
-            issue_phi(0);
-            cp_commit();
-            for (int q = 0; q < PF; ++q) {
-                if (q + 1 <= CH + 1) issue_phi(1 + q);
-                if (q <= CH) issue_pi(q);
-                cp_commit();
-            }
+        } else if (!(first && preissued)) {
+            row4_issue_start<C4, TJ, PF>(ring, pis, B, M);
         }
+        first = false;
         // differences of plane p-1 (k and j) and of the pair (p-2, p-1) (i)
         auto diffs = [&](int p, bool kj) {
             const float* nr = nb + ((p - 1) & 1) * NBP;
@@ -1267,7 +1335,8 @@ __device__ __forceinline__ void rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
     df64 v3[3] = {g.df(), s1.df(), s2.df()};
-    finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true, TJ + 1);
+    finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true, TJ + 1, sq);
+    return true;
 }
 
 // Whole-plane variant of the step for small lattices (N = 32, 64): a CTA owns

@@ -100,6 +100,7 @@ def load() -> C.CDLL:
         "iegpu_sum": (I, [P, I, dp]),
         "iegpu_shell_spectrum_noalloc": (I, [P, P, I, P, P, P]),
         "iegpu_set_shape": (I, [P, I, I, I]),
+        "iegpu_set_persistent": (I, [P, I]),
         "iegpu_ens_create": (I, [C.POINTER(Config), ip, I, C.POINTER(P)]),
         "iegpu_ens_destroy": (I, [P]),
         "iegpu_ens_last_error": (C.c_char_p, [P]),
@@ -233,6 +234,9 @@ class Lattice:
     # -- measurement ------------------------------------------------------
     def set_shape(self, rows: int, prefetch: int, chunks: int) -> None:
         self._check(self.lib.iegpu_set_shape(self.h, rows, prefetch, chunks))
+
+    def set_persistent(self, on: bool) -> None:
+        self._check(self.lib.iegpu_set_persistent(self.h, int(bool(on))))
 
     def autotune(self, bg: Bg):
         r, p, ch = C.c_int(), C.c_int(), C.c_int()

@@ -212,3 +212,40 @@ def test_split_row_kernel_matches_fp64(N, usr, shape, engine, tables):
         assert tf == 180 and ts == 101
         assert np.all(np.abs(trs - trf[:ts]) <= 1e-9 * trf[:ts])
         assert abs(bs.a - trf[ts - 1]) <= 1e-9 * trf[ts - 1]
+
+
+@pytest.mark.parametrize("N,usr,shape", [(128, False, (16, 3, 0)), (128, True, (8, 2, 4)), (256, False, (16, 3, 9)),
+                                         (256, True, (4, 2, 7))])
+def test_split_persistent_launch_matches(N, usr, shape, engine, tables):
+    """Many steps per cooperative launch against one launch per step: the
+    same fields, a(t) trace, background and steps taken, bit for bit, over
+    three calls (150 steps, then 70, then a call stopped by af), so launches
+    end mid-call and the buffer parity changes between calls."""
+    w = ROWCASE[usr]
+    pot = engine.POT_TABLE if usr else engine.POT_HILLTOP
+    out = []
+    for persist in (False, True):
+        lat = engine.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], potential=pot, form=engine.FORM_SPLIT)
+        if usr:
+            lat.set_table(*tables)
+        lat.set_shape(*shape)
+        lat.set_persistent(persist)
+        H = lat.bunch_davies(5, w["phi0"], w["dphi0"])
+        bg = engine.Bg(0.0, 1.0, H, 0.0, 1.0)
+        lat.evolve_fields(0.5 * w["dt"], bg)
+        rec = []
+        for steps, af in ((150, 1e30), (70, 1e30), (100, None)):
+            if af is None:
+                # about 42 steps past the end of the previous call
+                prev = rec[-1][1]
+                af = prev[-1] + 41.5 * (prev[-1] - prev[-2])
+            taken, tr = lat.leapfrog(af, steps, bg, trace=True)
+            bg.astep = bg.a
+            rec.append((taken, tr, bg.as_tuple(), lat.download(engine.F), lat.download(engine.FD)))
+        out.append(rec)
+        lat.close()
+    for (ta, tra, bga, fa, fda), (tb, trb, bgb, fb, fdb) in zip(*out):
+        assert ta == tb and np.array_equal(tra, trb) and bga == bgb
+        assert np.array_equal(fa, fb) and np.array_equal(fda, fdb)
+    taken = [r[0] for r in out[0]]
+    assert taken[:2] == [150, 70] and 0 < taken[2] < 100
