@@ -917,6 +917,7 @@ static void sctl_bg(const iegpu_ctx* c, iegpu_bg* bg) {
 }
 
 int split_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk);
+static int split_profile_persist(iegpu_ctx* c, int nsteps, iegpu_bg* bg, double* ms);
 
 // Autotuner of the row kernel's launch shape: rows per tile (TJ), planes
 // prefetched (PF) and plane chunks (grid height).  Each candidate runs one
@@ -1006,7 +1007,11 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
         c->row_cfg = r;
         iegpu_bg b = *bg0;
         double ms[2] = {0.0, 0.0};
-        int rc = split_profile(c, 1e300, 4, &b, ms, 2);
+        // each candidate is timed the way iegpu_leapfrog will run it: in one
+        // persistent launch where its shape allows, else one launch per step
+        int rc = split_profile_persist(c, 8, &b, &ms[1]);
+        if (rc == 0) ms[1] *= 0.5;   // per 4 steps, as the one-step timing below
+        else if (rc == 1) rc = split_profile(c, 1e300, 4, &b, ms, 2);
         // restore
         c->cur = cur0;
         *c->sctl_h = ctl0;
@@ -1157,6 +1162,32 @@ int split_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms,
         cudaEventElapsedTime(&t, c->ev[1], c->ev[2]);
         if (nk > 1) ms[1] += t;
     }
+    int rc = sctl_down(c);
+    c->cur = (start + c->sctl_h->steps_done) & 1;
+    if (rc) return rc;
+    sctl_bg(c, bg);
+    return IEGPU_OK;
+}
+
+// As split_leapfrog with persistent launches, `nsteps` steps timed between two
+// CUDA events (the priming reduction before them is not timed); 1 if the
+// current shape does not run persistently.
+static int split_profile_persist(iegpu_ctx* c, int nsteps, iegpu_bg* bg, double* ms) {
+    if (launch_persist(c, c->cur, 0, true) != 0) return 1;
+    sctl_fill(c, bg, kModeLeapfrog);
+    c->sctl_h->af = 1e300;
+    c->sctl_h->steps_limit = nsteps;
+    if (sctl_up(c)) return IEGPU_ECUDA;
+    const int start = c->cur;
+    launch_prime(c, start);
+    cudaEventRecord(c->ev[1], c->stream);
+    if (launch_persist(c, start, nsteps, false) != 0)
+        return check_cuda(c, cudaGetLastError(), "persistent launch") ? IEGPU_ECUDA : set_error(c, IEGPU_ECUDA, "persistent launch");
+    cudaEventRecord(c->ev[2], c->stream);
+    if (check_cuda(c, cudaEventSynchronize(c->ev[2]), "profile")) return IEGPU_ECUDA;
+    float t = 0.f;
+    cudaEventElapsedTime(&t, c->ev[1], c->ev[2]);
+    *ms = t;
     int rc = sctl_down(c);
     c->cur = (start + c->sctl_h->steps_done) & 1;
     if (rc) return rc;
