@@ -12,7 +12,7 @@ oracle/ref_driver.cpp, which runs the unmodified main() and dumps state.
 Nothing here is shipped or used by the product; only tests and the golden
 fixture generator call it, and only where the reference tree is present.
 
-    python oracle/build_ref.py --N 16 --numerical 0 --sigw 0 --deltaN 1
+    python oracle/build_ref.py --N 16 --numerical 0 --sigw 0 --deltaN 1 [--post 1]
 """
 from __future__ import annotations
 
@@ -31,15 +31,17 @@ def ref_available() -> bool:
     return (REF_ROOT / "src" / "evolution.cpp").is_file()
 
 
-def tag_for(N: int, numerical: int, sigw: int, deltaN: int) -> str:
-    return f"n{N}_{'usr' if numerical else 'hill'}_sigw{sigw}_dn{deltaN}"
+def tag_for(N: int, numerical: int, sigw: int, deltaN: int, post: int = 0) -> str:
+    return f"n{N}_{'usr' if numerical else 'hill'}_sigw{sigw}_dn{deltaN}" + ("_post1" if post else "")
 
 
-def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8) -> Path:
-    """Returns the path of the built driver binary (cached by configuration)."""
+def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8, post: int = 0) -> Path:
+    """Returns the path of the built driver binary (cached by configuration).
+    post = 1 keeps the reference's post-inflation phase (src/parameters.h:31),
+    which needs SIGW on."""
     if not ref_available():
         raise FileNotFoundError(f"reference sources not found under {REF_ROOT}")
-    tag = tag_for(N, numerical, sigw, deltaN)
+    tag = tag_for(N, numerical, sigw, deltaN, post)
     out = HERE / "_ref" / tag
     exe = out / "ie_ref"
     if exe.is_file():
@@ -56,7 +58,7 @@ def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8) -> Path
         (r"#define numerical_potential \d+", f"#define numerical_potential {numerical}"),
         (r"#define perform_deltaN \d+", f"#define perform_deltaN {deltaN}"),
         (r"#define calculate_SIGW \d+", f"#define calculate_SIGW {sigw}"),
-        (r"#define post_inflation \d+", "#define post_inflation 0"),
+        (r"#define post_inflation \d+", f"#define post_inflation {post}"),
         (r"const int N = \d+;", f"const int N = {N};"),
     ]
     for pat, rep in subs:
@@ -78,7 +80,8 @@ def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8) -> Path
     for p in procs:
         if p.wait() != 0:
             raise RuntimeError("reference compilation failed")
-    wrap = ["-Wl,--wrap=_Z4savei"] + (["-Wl,--wrap=_Z5saveNv"] if deltaN else [])
+    wrap = (["-Wl,--wrap=_Z4savei"] + (["-Wl,--wrap=_Z5saveNv"] if deltaN else []) +
+            (["-Wl,--wrap=_Z19save_post_inflationi"] if post else []))
     subprocess.check_call(["g++", "-fopenmp", *wrap, *objs, "-o", str(exe), "-lm"])
     for o in objs:
         os.unlink(o)
@@ -91,8 +94,9 @@ def main() -> None:
     ap.add_argument("--numerical", type=int, default=0)
     ap.add_argument("--sigw", type=int, default=0)
     ap.add_argument("--deltaN", type=int, default=1)
+    ap.add_argument("--post", type=int, default=0)
     a = ap.parse_args()
-    print(build(a.N, a.numerical, a.sigw, a.deltaN))
+    print(build(a.N, a.numerical, a.sigw, a.deltaN, post=a.post))
 
 
 if __name__ == "__main__":

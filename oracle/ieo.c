@@ -103,6 +103,14 @@ void ieo_params_defaults(ieo_params* p, int N, int numerical) {
     }
     p->use_phiref_manual = 0;
     p->phiref_manual_value = 0.0;
+    /* post-inflation controls, src/runtime_parameters.cpp:48-52 (off here:
+     * the reference switches the phase on at compile time) */
+    p->post_inflation = 0;
+    p->horizon_factor = 1.0;
+    p->omega = 1.0 / 3.0;
+    p->dt_post_inflation = 0.001;
+    p->af_post_inflation = 2.0 * N;
+    p->af_post_given = 0;
     p->high_cutoff_index = 0.0;
     p->low_cutoff_index = 0.0;
     p->forcing_cutoff = 0;
@@ -122,6 +130,7 @@ void ieo_params_defaults(ieo_params* p, int N, int numerical) {
 void ieo_params_finalize(ieo_params* p, int rescale_B_given, int af_given) {
     if (!rescale_B_given) p->rescale_B = sqrt(p->V0);
     if (!af_given) p->af = 2.0 * p->N;
+    if (!p->af_post_given) p->af_post_inflation = 2.0 * p->N;
     p->dx = p->L / (double)p->N;
 }
 
@@ -213,6 +222,11 @@ int ieo_params_load(ieo_params* p, const char* path) {
         KB("perform_deltaN", perform_deltaN)
         KB("calculate_SIGW", calculate_SIGW)
         KI("criterion", criterion)
+        KB("post_inflation", post_inflation)
+        KD("horizon_factor", horizon_factor)
+        KD("omega", omega)
+        KD("dt_post_inflation", dt_post_inflation)
+        else if (!strcmp(key, "af_post_inflation") && parse_d(val, &d)) { p->af_post_inflation = d; p->af_post_given = 1; }
 #undef KD
 #undef KI
 #undef KB
@@ -687,6 +701,143 @@ void ieo_evolve_fields(ieo_state* S, double d) {
     S->a += d * S->ad;
 }
 
+/* initialize_post_inflation(), src/initialize.cpp:245-290, without the
+ * save_post_inflation(1) it ends with (the program driver makes it).  With
+ * deltaN, f becomes Phi_from_zeta (deltaN - <deltaN>); fd keeps its value (the
+ * reference only resizes it); h and h' are zeroed; ad2 and astep are left as
+ * they are. */
+void ieo_initialize_post_inflation(ieo_state* S) {
+    const ieo_params* p = &S->p;
+    const size_t gs = S->gs;
+    S->t0 = 0.0;
+    S->t = 0.0;
+    for (int c = 0; c < 6; ++c) {
+        memset(S->h[c], 0, sizeof(float) * gs);
+        memset(S->hd[c], 0, sizeof(float) * gs);
+    }
+    const double Phi_from_zeta = 3.0 * (1.0 + p->omega) / (5.0 + 3.0 * p->omega);
+    if (p->perform_deltaN) {
+        double Nmean = 0.;
+        for (size_t id = 0; id < gs; ++id) Nmean += S->deltaN[id];
+        Nmean = Nmean / (double)gs;
+        for (size_t id = 0; id < gs; ++id) S->f[id] = Phi_from_zeta * (S->deltaN[id] - Nmean);
+    } else {
+        double fmean = 0.0, fdmean = 0.0;
+        for (size_t id = 0; id < gs; ++id) {
+            fmean += S->f[id];
+            fdmean += S->fd[id];
+        }
+        fmean = fmean / (double)gs;
+        fdmean = fdmean / (double)gs;
+        const double s = p->rescale_s;
+        for (size_t id = 0; id < gs; ++id)
+            S->f[id] = Phi_from_zeta * (S->f[id] - fmean) /
+                       (fdmean * pow(S->a, s - 1.0) / (S->ad * pow(S->a, s - 2.0)));
+    }
+    S->a = 1.0;
+    S->ad = p->horizon_factor * p->N * 2.0 * S->pi / p->L;
+}
+
+/* d2_cross_state, src/evolution.cpp:93-106: the neighbours are chosen per
+ * index from whether d1 or d2 names it, and the four corners are
+ * (ip, jp, kp), (ip, jm, km), (im, jp, kp), (im, jm, km).  For (d1, d2) =
+ * (1, 2) the i index does not move, so fpp = fmp and fpm = fmm and the value
+ * is the rounding residue of (fpp - fpm - fmp + fmm): kept as it is. */
+static inline double d2_cross_at(const double* f, int N, int d1, int d2, int i, int j, int k, double den) {
+    const int iu = (d1 == 0 || d2 == 0), ju = (d1 == 1 || d2 == 1), ku = (d1 == 2 || d2 == 2);
+    const int ip = iu ? (i == N - 1 ? 0 : i + 1) : i, im = iu ? (i == 0 ? N - 1 : i - 1) : i;
+    const int jp = ju ? (j == N - 1 ? 0 : j + 1) : j, jm = ju ? (j == 0 ? N - 1 : j - 1) : j;
+    const int kp = ku ? (k == N - 1 ? 0 : k + 1) : k, km = ku ? (k == 0 ? N - 1 : k - 1) : k;
+    const double fpp = f[IDX(N, ip, jp, kp)];
+    const double fpm = f[IDX(N, ip, jm, km)];
+    const double fmp = f[IDX(N, im, jp, kp)];
+    const double fmm = f[IDX(N, im, jm, km)];
+    return (fpp - fpm - fmp + fmm) / den;
+}
+
+/* evolve_derivs_post_inflation(d), src/evolution.cpp:1436-1555: radiation-era
+ * kick of fd and, with SIGW, of the six h' with the Hessian-based source
+ * (build_deriv_pack, src/evolution.cpp:1398-1418); the tensor source reads
+ * the fd just kicked.  ad2 depends on ad and a only. */
+void ieo_evolve_derivs_post_inflation(ieo_state* S, double d) {
+    const ieo_params* p = &S->p;
+    const int N = p->N;
+    const double s = p->rescale_s, omega = p->omega, dx = p->dx;
+    const double laplnorm = pow(S->a, -2.0 * s) / pw2(dx);
+    S->ad2 = -(s - 0.5 * (1.0 - 3.0 * omega)) * pw2(S->ad) / S->a;
+    S->ad += 0.5 * d * S->ad2;
+    const double a = S->a, ad = S->ad;
+    double* f = S->f;
+    double* fd = S->fd;
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; ++i) {
+        const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+        for (int j = 0; j < N; ++j) {
+            const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+            for (int k = 0; k < N; ++k) {
+                const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                const size_t id = IDX(N, i, j, k);
+                fd[id] += d * (omega * laplnorm * LAPL_AT(double, f, N, i, j, k, ip, im, jp, jm, kp, km)
+                               - (3.0 * (1.0 + omega) + s) * ad * fd[id] / a);
+            }
+        }
+    }
+    if (p->calculate_SIGW) {
+        const double Htilde = ad / a;
+        const double invH = 1.0 / Htilde;
+        const double coeffU = 4.0 / (3.0 * (1.0 + omega));
+        const double srcAmp = 2.0 * pow(a, -2.0 * s);
+        const double half_over_dx = 0.5 / dx;
+        const double inv_dx2 = 1.0 / (dx * dx);
+        const double den = 4.0 * dx * dx;
+        #pragma omp parallel for schedule(static)
+        for (int i = 0; i < N; ++i) {
+            const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+            for (int j = 0; j < N; ++j) {
+                const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+                for (int k = 0; k < N; ++k) {
+                    const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                    const size_t id = IDX(N, i, j, k);
+                    /* dfdx<double> of f and of the kicked fd, src/evolution.cpp:55-77 */
+                    const double gx = (f[IDX(N, ip, j, k)] - f[IDX(N, im, j, k)]) * half_over_dx;
+                    const double gy = (f[IDX(N, i, jp, k)] - f[IDX(N, i, jm, k)]) * half_over_dx;
+                    const double gz = (f[IDX(N, i, j, kp)] - f[IDX(N, i, j, km)]) * half_over_dx;
+                    const double gdx = (fd[IDX(N, ip, j, k)] - fd[IDX(N, im, j, k)]) * half_over_dx;
+                    const double gdy = (fd[IDX(N, i, jp, k)] - fd[IDX(N, i, jm, k)]) * half_over_dx;
+                    const double gdz = (fd[IDX(N, i, j, kp)] - fd[IDX(N, i, j, km)]) * half_over_dx;
+                    /* d2_same_state, src/evolution.cpp:79-91 */
+                    const double Hxx = (f[IDX(N, ip, j, k)] - 2.0 * f[id] + f[IDX(N, im, j, k)]) * inv_dx2;
+                    const double Hyy = (f[IDX(N, i, jp, k)] - 2.0 * f[id] + f[IDX(N, i, jm, k)]) * inv_dx2;
+                    const double Hzz = (f[IDX(N, i, j, kp)] - 2.0 * f[id] + f[IDX(N, i, j, km)]) * inv_dx2;
+                    const double Hxy = d2_cross_at(f, N, 0, 1, i, j, k, den);
+                    const double Hxz = d2_cross_at(f, N, 0, 2, i, j, k, den);
+                    const double Hyz = d2_cross_at(f, N, 1, 2, i, j, k, den);
+                    const double Phi = f[id];
+                    const double dux = gdx * invH + gx;
+                    const double duy = gdy * invH + gy;
+                    const double duz = gdz * invH + gz;
+                    const double Sc[6] = {
+                        4.0 * Phi * Hxx + 2.0 * gx * gx - coeffU * (dux * dux),
+                        4.0 * Phi * Hyy + 2.0 * gy * gy - coeffU * (duy * duy),
+                        4.0 * Phi * Hzz + 2.0 * gz * gz - coeffU * (duz * duz),
+                        4.0 * Phi * Hxy + 2.0 * gx * gy - coeffU * (dux * duy),
+                        4.0 * Phi * Hxz + 2.0 * gx * gz - coeffU * (dux * duz),
+                        4.0 * Phi * Hyz + 2.0 * gy * gz - coeffU * (duy * duz)};
+                    for (int c = 0; c < 6; ++c) {
+                        const float* h = S->h[c];
+                        const float lapf = LAPL_AT(float, h, N, i, j, k, ip, im, jp, jm, kp, km);
+                        const double lap_h = (double)lapf;
+                        const double rhs = d * (laplnorm * lap_h - (2.0 + s) * ad * (double)S->hd[c][id] / a +
+                                                srcAmp * Sc[c]);
+                        S->hd[c][id] += (float)rhs;
+                    }
+                }
+            }
+        }
+    }
+    S->ad += 0.5 * d * S->ad2;
+}
+
 /* inflation_rescaled_step, src/evolution.cpp:338-340 */
 double ieo_rescaled_step(const ieo_state* S, double astep) {
     return S->p.dt * pow(astep, S->p.rescale_s - 1.0);
@@ -1083,6 +1234,9 @@ typedef struct {
     FILE *output, *means, *vars, *velocity, *sf, *energy, *conservation, *spectra, *spectratimes,
          *histogram, *histogramtimes, *spectraGW, *spectraGWdot, *modes, *spectraN, *histogramN,
          *histogramtimesN, *box2d_phi, *box2d_phidot, *box2d_deltaN, *box3d, *info;
+    /* results/post_inflation/, src/output.cpp:1573-1867 */
+    FILE *pmeans, *pvars, *pvelocity, *psf, *pspectra, *pspectratimes, *pspectraGW, *pspectraGWdot, *phistogram,
+         *phistogramtimes;
     time_t tstart;
 } outfiles;
 
@@ -1112,11 +1266,13 @@ static void print_spectrum(FILE* out, int N, double L, const int* counts, double
     fflush(out);
 }
 
-/* meansvars, src/output.cpp:204-269 */
-static int out_meansvars(ieo_state* S, outfiles* O) {
-    FILE* m = open_out(S, O, &O->means, "means");
-    FILE* v = open_out(S, O, &O->vars, "variance");
-    FILE* ve = open_out(S, O, &O->velocity, "velocity");
+/* meansvars, src/output.cpp:204-269; post: meansvars_post_inflation,
+ * src/output.cpp:1576-1639 (same columns, results/post_inflation/) */
+static int out_meansvars(ieo_state* S, outfiles* O, int post) {
+    FILE* m = post ? open_out(S, O, &O->pmeans, "post_inflation/means") : open_out(S, O, &O->means, "means");
+    FILE* v = post ? open_out(S, O, &O->pvars, "post_inflation/variance") : open_out(S, O, &O->vars, "variance");
+    FILE* ve = post ? open_out(S, O, &O->pvelocity, "post_inflation/velocity")
+                    : open_out(S, O, &O->velocity, "velocity");
     if (S->err) return 1;
     fprintf(m, "%f", S->t); fprintf(m, " %e", S->a);
     fprintf(ve, "%f", S->t); fprintf(ve, " %e", S->a);
@@ -1129,7 +1285,7 @@ static int out_meansvars(ieo_state* S, outfiles* O) {
     fprintf(m, " %e", av); fprintf(ve, " %e", vel); fprintf(v, " %e", var - pw2(av));
     {
         const double q[5] = {S->t, S->a, av, vel, S->ad * S->p.rescale_B * pow(S->a, S->p.rescale_s - 2.0)};
-        prec_line("means", q, 5);
+        prec_line(post ? "post_means" : "means", q, 5);
     }
     if (av + DBL_MAX == av || (av != 0. && av / av != 1.)) {
         set_err(S, "Unstable solution developed. Scalar field not numerical at t=%f\n", S->t);
@@ -1141,9 +1297,9 @@ static int out_meansvars(ieo_state* S, outfiles* O) {
     return 0;
 }
 
-/* scale, src/output.cpp:272-293 */
-static void out_scale(ieo_state* S, outfiles* O) {
-    FILE* fp = open_out(S, O, &O->sf, "sf");
+/* scale, src/output.cpp:272-293; post: scale_post_inflation, src/output.cpp:1642-1662 */
+static void out_scale(ieo_state* S, outfiles* O, int post) {
+    FILE* fp = post ? open_out(S, O, &O->psf, "post_inflation/sf") : open_out(S, O, &O->sf, "sf");
     if (!fp) return;
     const double s = S->p.rescale_s, B = S->p.rescale_B, a = S->a;
     fprintf(fp, "%f %f %e %e\n", S->t, a, S->ad * B * pow(a, s - 2.0),
@@ -1208,21 +1364,30 @@ static void out_box2d(ieo_state* S, FILE* fp, const double* x, double scale, int
     fflush(fp);
 }
 
-/* spectraGW / spectraGWdot printing, src/output.cpp:618-624 */
-static void out_gw(ieo_state* S, outfiles* O, int which) {
-    FILE* fp = which ? open_out(S, O, &O->spectraGWdot, "spectraGWdot") : open_out(S, O, &O->spectraGW, "spectraGW");
+/* spectraGW / spectraGWdot printing, src/output.cpp:618-624.  Post:
+ * spectraGW_post_inflation / spectraGWdot_post_inflation, src/output.cpp:652-669;
+ * the latter scales h' in float by (float)(B a^(s-1)), which gives the same
+ * bits as rounding (double)h' * (double)(float)(B a^(s-1)) to float (the
+ * double product of two floats is exact). */
+static void out_gw(ieo_state* S, outfiles* O, int which, int post) {
+    FILE* fp = post ? (which ? open_out(S, O, &O->pspectraGWdot, "post_inflation/spectraGWdot")
+                             : open_out(S, O, &O->pspectraGW, "post_inflation/spectraGW"))
+                    : (which ? open_out(S, O, &O->spectraGWdot, "spectraGWdot")
+                             : open_out(S, O, &O->spectraGW, "spectraGW"));
     if (!fp) return;
     const int N = S->p.N;
     const int numbins = (int)(sqrt(3.0) * (N / 2)) + 1;
     int* counts = (int*)calloc(numbins, sizeof(int));
     float* f2 = (float*)calloc(numbins, sizeof(float));
-    const double to_phys = which ? S->p.rescale_B * pow(S->a, S->p.rescale_s - 1.0) : 1.0;
+    double to_phys = which ? S->p.rescale_B * pow(S->a, S->p.rescale_s - 1.0) : 1.0;
+    if (post && which) to_phys = (double)(float)to_phys;
     double* f2d = (double*)calloc(numbins, sizeof(double));
     ieo_gw_spectrum(S, which, to_phys, counts, f2, f2d);
     if (g_prec) {
         const double n1 = 0.5 * pow(S->p.L / S->p.rescale_B, 3) / pow((double)N, 6);
         for (int i = 0; i < numbins; ++i) f2d[i] = counts[i] > 0 ? n1 * f2d[i] / counts[i] : 0.0;
-        prec_line(which ? "spectrumGWdot" : "spectrumGW", f2d, numbins);
+        prec_line(which ? (post ? "post_spectrumGWdot" : "spectrumGWdot") : (post ? "post_spectrumGW" : "spectrumGW"),
+                  f2d, numbins);
     }
     free(f2d);
     const float dp = 2.f * (float)S->pi / (float)S->p.L;
@@ -1243,8 +1408,8 @@ static int out_save(ieo_state* S, outfiles* O, int infrequent) {
     if (g_trace)
         fprintf(g_trace, "save %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, S->t, S->a, S->ad, S->ad2, S->astep);
     if (S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt * pow(S->astep, p->rescale_s - 1));
-    if (out_meansvars(S, O)) return 1;
-    out_scale(S, O);
+    if (out_meansvars(S, O, 0)) return 1;
+    out_scale(S, O, 0);
     if (infrequent) {
         if (p->output_box3D) {
             FILE* fp = open_out(S, O, &O->box3d, "box");
@@ -1276,13 +1441,54 @@ static int out_save(ieo_state* S, outfiles* O, int infrequent) {
             }
             ieo_fftrn_d(S->f, S->fny, p->N, -1);
             free(counts); free(f2);
-            if (p->calculate_SIGW) { out_gw(S, O, 0); out_gw(S, O, 1); }
+            if (p->calculate_SIGW) { out_gw(S, O, 0, 0); out_gw(S, O, 1, 0); }
         }
         if (p->output_histogram)
             out_histogram(S, S->f, open_out(S, O, &O->histogram, "histogram"),
                           open_out(S, O, &O->histogramtimes, "histogramtimes"), 0);
     }
     if (S->t > 0.) ieo_evolve_fields(S, .5 * p->dt * pow(S->astep, p->rescale_s - 1));
+    return S->err;
+}
+
+/* save_post_inflation(), src/output.cpp:1840-1865 (leapfrog: staggered) */
+static int out_save_post(ieo_state* S, outfiles* O, int infrequent) {
+    const ieo_params* p = &S->p;
+    if (g_trace)
+        fprintf(g_trace, "savep %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, S->t, S->a, S->ad, S->ad2, S->astep);
+    if (S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt_post_inflation);
+    if (out_meansvars(S, O, 1)) return 1;
+    out_scale(S, O, 1);
+    if (infrequent) {
+        if (p->output_spectra) {
+            /* spectraf_post_inflation(), src/output.cpp:1667-1770 */
+            FILE* sp = open_out(S, O, &O->pspectra, "post_inflation/spectra");
+            FILE* st = open_out(S, O, &O->pspectratimes, "post_inflation/spectratimes");
+            if (S->err) return 1;
+            const int nb = ieo_numbins(p->N);
+            int* counts = (int*)calloc(nb, sizeof(int));
+            double* f2 = (double*)calloc(nb, sizeof(double));
+            const double norm1 = pow(p->L / p->rescale_B, 3) / pow((double)p->N, 6);
+            ieo_fftrn_d(S->f, S->fny, p->N, 1);
+            ieo_bin_spectrum(p->N, S->f, S->fny, counts, f2);
+            print_spectrum(sp, p->N, p->L, counts, f2, norm1, "post_spectrum");
+            fprintf(st, "%f %e\n", S->t, S->a);
+            fflush(st);
+            if (p->high_cutoff_index > 0 && p->forcing_cutoff) {
+                set_err(S, "forcing_cutoff is not supported by this oracle\n");
+                free(counts); free(f2);
+                return 1;
+            }
+            ieo_fftrn_d(S->f, S->fny, p->N, -1);
+            free(counts); free(f2);
+            out_gw(S, O, 0, 1);
+            out_gw(S, O, 1, 1);
+        }
+        if (p->output_histogram)
+            out_histogram(S, S->f, open_out(S, O, &O->phistogram, "post_inflation/histogram"),
+                          open_out(S, O, &O->phistogramtimes, "post_inflation/histogramtimes"), 0);
+    }
+    if (S->t > 0.) ieo_evolve_fields(S, .5 * p->dt_post_inflation);
     return S->err;
 }
 
@@ -1379,7 +1585,9 @@ static void close_all(outfiles* O) {
     FILE** all[] = {&O->output, &O->means, &O->vars, &O->velocity, &O->sf, &O->energy, &O->conservation,
                     &O->spectra, &O->spectratimes, &O->histogram, &O->histogramtimes, &O->spectraGW,
                     &O->spectraGWdot, &O->modes, &O->spectraN, &O->histogramN, &O->histogramtimesN,
-                    &O->box2d_phi, &O->box2d_phidot, &O->box2d_deltaN, &O->box3d, &O->info};
+                    &O->box2d_phi, &O->box2d_phidot, &O->box2d_deltaN, &O->box3d, &O->info,
+                    &O->pmeans, &O->pvars, &O->pvelocity, &O->psf, &O->pspectra, &O->pspectratimes,
+                    &O->pspectraGW, &O->pspectraGWdot, &O->phistogram, &O->phistogramtimes};
     for (size_t q = 0; q < sizeof(all) / sizeof(all[0]); ++q)
         if (*all[q]) { fclose(*all[q]); *all[q] = NULL; }
 }
@@ -1492,6 +1700,31 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
         if (out_saveN(S, &O)) goto done;
         fflush(O.output);
         ieo_evolve_fieldsN(S, -0.5 * p->dN);
+    }
+    /* run_post_inflation_loop(), leapfrog branch, src/evolution.cpp:1561-1653 */
+    if (p->post_inflation) {
+        if (!p->calculate_SIGW) {
+            set_err(S, "post_inflation requires calculate_SIGW = 1\n");
+            goto done;
+        }
+        snprintf(path, sizeof path, "%s/post_inflation", results_dir);
+        mkdir(path, 0777);
+        ieo_initialize_post_inflation(S);
+        if (out_save_post(S, &O, 1)) goto done;
+        int numsteps = 0;
+        ieo_evolve_fields(S, 0.5 * p->dt_post_inflation);
+        while (S->a <= p->af_post_inflation) {
+            ieo_evolve_derivs_post_inflation(S, p->dt_post_inflation);
+            ieo_evolve_fields(S, p->dt_post_inflation);
+            numsteps++;
+            if (numsteps % p->output_freq == 0)
+                if (out_save_post(S, &O, (numsteps % p->output_infrequent_freq == 0) ? 1 : 0)) goto done;
+            fprintf(O.output, "scale factor a = %f\n", S->a);
+            fprintf(O.output, "numsteps %i\n\n", numsteps);
+            if (numsteps % p->output_freq == 0) fflush(O.output);
+        }
+        fflush(O.output);
+        if (out_save_post(S, &O, 1)) goto done;
     }
     fprintf(O.output, "InflationEasy program finished\n");
     if (dump_dir) {

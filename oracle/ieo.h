@@ -47,6 +47,9 @@ typedef struct {
     int output_spectra, output_histogram, output_energy, output_box3D, output_box2D;
     int screen_updates, nbins, int_err, int_errN;
     double dx;
+    /* post-inflation phase (src/parameters.h:31 switch, src/runtime_parameters.cpp:48-52, 295-299) */
+    int post_inflation, af_post_given;
+    double horizon_factor, omega, dt_post_inflation, af_post_inflation;
 } ieo_params;
 
 typedef struct ieo_state ieo_state;
@@ -106,6 +109,10 @@ double ieo_rescaled_step(const ieo_state* S, double astep);
  * src/evolution.cpp:937-945 without output; stops early once a > af.
  * Returns the number of steps taken (or -1 on error). */
 int ieo_leapfrog_steps(ieo_state* S, int nsteps);
+
+/* ---- post-inflation phase: src/initialize.cpp:245-290, src/evolution.cpp:1378-1653 ---- */
+void ieo_initialize_post_inflation(ieo_state* S);
+void ieo_evolve_derivs_post_inflation(ieo_state* S, double d);
 
 /* ---- FFT: src/ffteasy.hpp ---- */
 void ieo_fftrn_d(double* f, double* fny, int N, int forward);

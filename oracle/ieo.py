@@ -43,7 +43,9 @@ class Params(C.Structure):
                 ("high_cutoff_index", C.c_double), ("low_cutoff_index", C.c_double), ("forcing_cutoff", C.c_int),
                 ("output_spectra", C.c_int), ("output_histogram", C.c_int), ("output_energy", C.c_int),
                 ("output_box3D", C.c_int), ("output_box2D", C.c_int), ("screen_updates", C.c_int),
-                ("nbins", C.c_int), ("int_err", C.c_int), ("int_errN", C.c_int), ("dx", C.c_double)]
+                ("nbins", C.c_int), ("int_err", C.c_int), ("int_errN", C.c_int), ("dx", C.c_double),
+                ("post_inflation", C.c_int), ("af_post_given", C.c_int), ("horizon_factor", C.c_double),
+                ("omega", C.c_double), ("dt_post_inflation", C.c_double), ("af_post_inflation", C.c_double)]
 
 
 class Scalars(C.Structure):
@@ -80,6 +82,7 @@ def load() -> C.CDLL:
         "ieo_potential": (D, [P, D]), "ieo_potential_energy": (D, [P]),
         "ieo_gradient_energy": (D, [P]), "ieo_kin_energy": (D, [P]),
         "ieo_evolve_derivs": (I, [P, D]), "ieo_evolve_fields": (None, [P, D]),
+        "ieo_initialize_post_inflation": (None, [P]), "ieo_evolve_derivs_post_inflation": (None, [P, D]),
         "ieo_rescaled_step": (D, [P, D]), "ieo_leapfrog_steps": (I, [P, I]),
         "ieo_fftrn_d": (None, [dp, dp, I, I]), "ieo_fftrn_f": (None, [fp, fp, I, I]),
         "ieo_numbins": (I, [I]),
@@ -107,6 +110,8 @@ def default_params(N: int, numerical: bool, **kw) -> Params:
     af_given = "af" in kw
     for k, v in kw.items():
         setattr(p, k, v)
+    if "af_post_inflation" in kw:
+        p.af_post_given = 1
     lib.ieo_params_finalize(C.byref(p), int(B_given), int(af_given))
     return p
 
@@ -218,6 +223,12 @@ class Oracle:
     def evolve_derivs(self, d):
         self._check(self.lib.ieo_evolve_derivs(self.h, d))
 
+    def initialize_post_inflation(self):
+        self.lib.ieo_initialize_post_inflation(self.h)
+
+    def evolve_derivs_post_inflation(self, d):
+        self.lib.ieo_evolve_derivs_post_inflation(self.h, d)
+
     def rescaled_step(self, astep):
         return self.lib.ieo_rescaled_step(self.h, astep)
 
@@ -314,7 +325,8 @@ def read_state(path: Path) -> dict:
     return out
 
 
-def params_from_text(text: str, N: int, numerical: bool, sigw: bool, deltaN: bool = True) -> Params:
+def params_from_text(text: str, N: int, numerical: bool, sigw: bool, deltaN: bool = True,
+                     post: bool = False) -> Params:
     """Params for a params.txt body, with the compile-time switches given."""
     kw = {}
     for line in text.splitlines():
@@ -327,4 +339,5 @@ def params_from_text(text: str, N: int, numerical: bool, sigw: bool, deltaN: boo
         kw[k] = float(v) if any(ch in v for ch in ".eE") else int(v)
     kw["calculate_SIGW"] = int(sigw)
     kw["perform_deltaN"] = int(deltaN)
+    kw["post_inflation"] = int(post)
     return default_params(N, numerical, **kw)

@@ -5,8 +5,9 @@
 // compile-time lines of src/parameters.h set per configuration) together with
 // this file.  The reference's main() (src/main.cpp:103-146) is compiled as
 // ie_ref_main() and run unchanged; this driver only observes it:
-//   * the linker wraps save(int) and saveN() (--wrap) so the background
-//     scalars are traced at full precision each time the reference saves;
+//   * the linker wraps save(int), saveN() and, with the post-inflation phase,
+//     save_post_inflation(int) (--wrap) so the background scalars are traced
+//     at full precision each time the reference saves;
 //   * after the run the final lattice state is written in binary.
 // Usage: ie_ref <workdir>   (workdir holds params.txt and inputs/)
 #include "main.h"
@@ -31,6 +32,15 @@ extern "C" void __real__Z5saveNv();
 extern "C" void __wrap__Z5saveNv() {
     if (g_trace) std::fprintf(g_trace, "saveN %.17g %.17g %.17g %.17g\n", t, a, Ne, phiref);
     __real__Z5saveNv();
+}
+#endif
+
+#if post_inflation
+extern "C" void __real__Z19save_post_inflationi(int);
+extern "C" void __wrap__Z19save_post_inflationi(int infrequent) {
+    if (g_trace)
+        std::fprintf(g_trace, "savep %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, t, a, ad, ad2, astep);
+    __real__Z19save_post_inflationi(infrequent);
 }
 #endif
 

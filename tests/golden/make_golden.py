@@ -6,10 +6,12 @@ sources by oracle/build_ref.py) on small lattices and stores, per case:
   <case>/trace.txt         background scalars at every save(), full precision
   <case>/state.npz         final f, fd, deltaN (and h, hd) in binary
   <case>/params.txt        the params file the reference read
-This script needs the reference tree, so it runs only where that exists; the
-fixtures it writes are committed and travel without it.
+A post-inflation case keeps only results/post_inflation/ (its inflation and
+deltaN outputs are those of the case without the phase).  This script needs
+the reference tree, so it runs only where that exists; the fixtures it writes
+are committed and travel without it.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -35,11 +37,12 @@ USR = dict(seed=8, dt=0.001, V0=3e-9, initial_field=2.9181235049318586, initial_
            output_energy=1, output_box3D=0, output_box2D=1, output_bispectrum=0, screen_updates=0, nbins=256,
            dN=1e-4, Nend=2.0, use_phiref_manual=0, output_LOG=0)
 
-# name: (N, numerical, sigw, deltaN, params)
+# name: (N, numerical, sigw, deltaN, post-inflation phase, params)
 CASES = {
-    "n16_hilltop": (16, 0, 0, 1, HILLTOP),
-    "n16_usr_sigw": (16, 1, 1, 1, USR),
-    "n32_hilltop": (32, 0, 0, 1, HILLTOP),
+    "n16_hilltop": (16, 0, 0, 1, 0, HILLTOP),
+    "n16_usr_sigw": (16, 1, 1, 1, 0, USR),
+    "n32_hilltop": (32, 0, 0, 1, 0, HILLTOP),
+    "n16_usr_sigw_post": (16, 1, 1, 1, 1, USR),
 }
 
 
@@ -69,8 +72,11 @@ def read_state(path: Path):
 def main() -> None:
     if not build_ref.ref_available():
         raise SystemExit("reference tree not available; fixtures are generated where it is")
-    for name, (N, num, sigw, dn, p) in CASES.items():
-        exe = build_ref.build(N, num, sigw, dn)
+    only = set(sys.argv[1:])
+    for name, (N, num, sigw, dn, post, p) in CASES.items():
+        if only and name not in only:
+            continue
+        exe = build_ref.build(N, num, sigw, dn, post=post)
         work = ROOT / "oracle" / "_ref" / f"golden_{name}"
         if work.exists():
             shutil.rmtree(work)
@@ -82,10 +88,15 @@ def main() -> None:
         if dst.exists():
             shutil.rmtree(dst)
         (dst / "results").mkdir(parents=True)
-        for f in sorted((work / "results").iterdir()):
-            if f.name in ("info.dat", "output.txt"):
-                continue
-            shutil.copy(f, dst / "results" / f.name)
+        if post:
+            (dst / "results" / "post_inflation").mkdir()
+            for f in sorted((work / "results" / "post_inflation").iterdir()):
+                shutil.copy(f, dst / "results" / "post_inflation" / f.name)
+        else:
+            for f in sorted((work / "results").iterdir()):
+                if f.name in ("info.dat", "output.txt") or f.is_dir():
+                    continue
+                shutil.copy(f, dst / "results" / f.name)
         shutil.copy(work / "trace.txt", dst / "trace.txt")
         shutil.copy(work / "params.txt", dst / "params.txt")
         st = read_state(work / "state.bin")

@@ -12,21 +12,23 @@ import pytest
 
 from conftest import GOLDEN, INPUTS
 
+# case: (N, numerical, SIGW, post-inflation phase)
 CASES = {
-    "n16_hilltop": (16, False, False),
-    "n16_usr_sigw": (16, True, True),
-    "n32_hilltop": (32, False, False),
+    "n16_hilltop": (16, False, False, False),
+    "n16_usr_sigw": (16, True, True, False),
+    "n32_hilltop": (32, False, False, False),
+    "n16_usr_sigw_post": (16, True, True, True),
 }
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_oracle_reproduces_reference_outputs(case, oracle_mod, tmp_path):
-    N, numerical, sigw = CASES[case]
+    N, numerical, sigw, post = CASES[case]
     src = GOLDEN / case
-    p = oracle_mod.params_from_text((src / "params.txt").read_text(), N, numerical, sigw)
+    p = oracle_mod.params_from_text((src / "params.txt").read_text(), N, numerical, sigw, post=post)
     rc = oracle_mod.run_program(p, tmp_path / "results", INPUTS, tmp_path)
     assert rc == 0
-    golden_files = sorted(x.name for x in (src / "results").iterdir())
+    golden_files = sorted(str(x.relative_to(src / "results")) for x in (src / "results").rglob("*") if x.is_file())
     assert golden_files, "empty fixture"
     for name in golden_files:
         a = (src / "results" / name).read_bytes()

@@ -24,27 +24,30 @@ pytestmark = pytest.mark.skipif(not build_ref.ref_available(), reason="reference
 HILL = (GOLDEN / "n16_hilltop" / "params.txt").read_text()
 USR = (GOLDEN / "n16_usr_sigw" / "params.txt").read_text()
 
+# (N, numerical, SIGW, post-inflation phase, params text)
 CASES = [
-    (16, False, True, HILL),
-    (16, True, False, USR),
-    (32, True, True, USR),
+    (16, False, True, False, HILL),
+    (16, True, False, False, USR),
+    (32, True, True, False, USR),
+    (16, False, True, True, HILL),
 ]
 
 
-@pytest.mark.parametrize("N,numerical,sigw,text", CASES)
-def test_oracle_matches_reference(N, numerical, sigw, text, oracle_mod, tmp_path):
-    exe = build_ref.build(N, int(numerical), int(sigw), 1)
+@pytest.mark.parametrize("N,numerical,sigw,post,text", CASES)
+def test_oracle_matches_reference(N, numerical, sigw, post, text, oracle_mod, tmp_path):
+    exe = build_ref.build(N, int(numerical), int(sigw), 1, post=int(post))
     wd = tmp_path / "ref"
     wd.mkdir()
     (wd / "params.txt").write_text(text)
     os.symlink(INPUTS, wd / "inputs")
     subprocess.run([str(exe), str(wd)], check=True, stdout=subprocess.DEVNULL)
-    p = oracle_mod.params_from_text(text, N, numerical, sigw)
+    p = oracle_mod.params_from_text(text, N, numerical, sigw, post=post)
     assert oracle_mod.run_program(p, tmp_path / "results", INPUTS, tmp_path) == 0
-    for f in sorted((wd / "results").iterdir()):
-        if f.name == "info.dat":
+    for f in sorted((wd / "results").rglob("*")):
+        if f.is_dir() or f.name == "info.dat":
             continue
-        assert f.read_bytes() == (tmp_path / "results" / f.name).read_bytes(), f.name
+        rel = f.relative_to(wd / "results")
+        assert f.read_bytes() == (tmp_path / "results" / rel).read_bytes(), str(rel)
     assert (wd / "trace.txt").read_text() == (tmp_path / "trace.txt").read_text()
     ref = oracle_mod.read_state(wd / "state.bin")
     got = oracle_mod.read_state(tmp_path / "state.bin")
