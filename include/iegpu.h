@@ -171,6 +171,27 @@ int  iegpu_set_shape(struct iegpu_ctx* ctx, int rows, int prefetch, int chunks);
  * counterpart in the reference (its loop is serial host code). */
 int  iegpu_set_persistent(struct iegpu_ctx* ctx, int on);
 
+/* ---- post-inflation phase (plain FP64 form, SIGW on) ------------------- */
+/* initialize_post_inflation(), src/initialize.cpp:245-290, without its save:
+ * f = Phi (deltaN - <deltaN>) with Phi = 3(1+omega)/(5+3 omega) (from_deltaN
+ * = 1), or Phi (f - <f>) / (<fd> a^(s-1) / (ad a^(s-2))) otherwise, the means
+ * summed serially in the reference's loop order; fd is kept; h and h' are
+ * zeroed; bg gets t = 0, a = 1, ad = horizon_factor N 2 pi / L (ad2 and astep
+ * are kept, as in the reference). */
+int  iegpu_initialize_post_inflation(struct iegpu_ctx* ctx, double horizon_factor, double omega, int from_deltaN,
+                                     iegpu_bg* bg);
+/* evolve_derivs_post_inflation(d), src/evolution.cpp:1436-1555: ad2 and the
+ * half kicks of ad on the host, the radiation-era kick of fd and the tensor
+ * kick with the Hessian source (build_deriv_pack, :1398-1418) on the device. */
+int  iegpu_evolve_derivs_post_inflation(struct iegpu_ctx* ctx, double d, double omega, iegpu_bg* bg);
+/* The leapfrog loop body of run_post_inflation_loop, src/evolution.cpp:1589-1597:
+ * while bg->a <= af_post, evolve_derivs_post_inflation(dt_post) then
+ * evolve_fields(dt_post), at most max_steps times; *steps = steps taken.  The
+ * half drift before the loop and the saves are the caller's, as in the
+ * reference.  The steps are enqueued without synchronisation. */
+int  iegpu_post_inflation_leapfrog(struct iegpu_ctx* ctx, double af_post, double dt_post, double omega, int max_steps,
+                                   iegpu_bg* bg, int* steps);
+
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */
 /* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */
 int  iegpu_means(struct iegpu_ctx* ctx, double out[3]);

@@ -539,6 +539,35 @@ int iegpu_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     return split_set_shape(c, rows, prefetch, chunks);
 }
 
+// The post-inflation phase runs on the plain FP64 state with SIGW on, as
+// the reference requires (src/parameters.h:33-35).
+static int post_ok(iegpu_ctx* c) {
+    if (is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "the post-inflation phase runs on the plain FP64 form");
+    if (!c->cfg.sigw) return set_error(c, IEGPU_EUNSUPPORTED, "post_inflation requires calculate_SIGW = 1");
+    return IEGPU_OK;
+}
+
+int iegpu_initialize_post_inflation(iegpu_ctx* c, double horizon_factor, double omega, int from_deltaN, iegpu_bg* bg) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (int rc = post_ok(c)) return rc;
+    return fp64_post_init(c, horizon_factor, omega, from_deltaN != 0, bg);
+}
+
+int iegpu_evolve_derivs_post_inflation(iegpu_ctx* c, double d, double omega, iegpu_bg* bg) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (int rc = post_ok(c)) return rc;
+    return fp64_post_derivs(c, d, omega, bg);
+}
+
+int iegpu_post_inflation_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps,
+                                  iegpu_bg* bg, int* steps) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (steps) *steps = 0;
+    if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
+    if (int rc = post_ok(c)) return rc;
+    return fp64_post_leapfrog(c, af_post, dt_post, omega, max_steps, bg, steps);
+}
+
 int iegpu_set_persistent(iegpu_ctx* c, int on) {
     if (!c) return IEGPU_EINVAL;
     if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "persistent launches belong to the split form");

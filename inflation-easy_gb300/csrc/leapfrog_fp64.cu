@@ -480,3 +480,207 @@ int fp64_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]) {
 }
 
 }  // namespace iegpu
+
+namespace iegpu {
+
+// ---------------------------------------------------------------------------
+// post-inflation phase: src/initialize.cpp:245-290, src/evolution.cpp:1378-1653
+// ---------------------------------------------------------------------------
+//
+// The background has no lattice sums in this phase (a'' = -(s - (1 - 3w)/2)
+// a'^2 / a), so every scalar is formed on the host with the reference's
+// expressions, and the kernels take the step's coefficients as arguments: a
+// run of steps is enqueued with no synchronisation.  Per-site expressions are
+// the reference's, in its order (this unit is compiled with -fmad=false).
+
+// initialize_post_inflation's field, src/initialize.cpp:258-283:
+// f = Phi (x - mean), or Phi (x - mean) / den without deltaN.
+__global__ void __launch_bounds__(kThreads) k_post_field(double* __restrict__ f, const double* x, long long gs,
+                                                         double Phi, double mean, double den, int divide) {
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (id >= gs) return;
+    const double v = x[id];
+    f[id] = divide ? Phi * (v - mean) / den : Phi * (v - mean);
+}
+
+// fd kick of evolve_derivs_post_inflation, src/evolution.cpp:1448-1457:
+// fd += d (w laplnorm lapl(f) - (3 (1 + w) + s) ad fd / a), with
+// c_lap = w laplnorm and c_fr = (3 (1 + w) + s) ad formed on the host.
+__global__ void __launch_bounds__(kThreads) k_post_kick(const double* __restrict__ f, double* __restrict__ fd, int lg,
+                                                        double d, double c_lap, double c_fr, double a) {
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const Nbr n = neighbours(id, lg);
+    const double lap = lapl7(f, n, __ldg(&f[id]));
+    const double fdo = fd[id];
+    fd[id] = fdo + d * (c_lap * lap - c_fr * fdo / a);
+}
+
+struct PostSigwK {
+    double d, laplnorm, c_hf, a, invH, coeffU, srcAmp, half_over_dx, inv_dx2, den;
+};
+
+// (fpp - fpm - fmp + fmm) / den of d2_cross_state, src/evolution.cpp:93-106
+__device__ __forceinline__ double cross4(const double* __restrict__ f, long long pp, long long pm, long long mp,
+                                         long long mm, double den) {
+    return (__ldg(&f[pp]) - __ldg(&f[pm]) - __ldg(&f[mp]) + __ldg(&f[mm])) / den;
+}
+
+// Tensor kick of evolve_derivs_post_inflation, src/evolution.cpp:1459-1551,
+// with the derivative pack of build_deriv_pack (:1398-1418): central first
+// derivatives of f and of the fd just kicked, the Hessian of f (d2_same_state
+// :79-91; d2_cross_state :93-106, whose neighbours are chosen per index from
+// whether d1 or d2 names it: for (y, z) the i index does not move, so the
+// corners pair up and the value is the rounding residue the reference gets).
+__global__ void __launch_bounds__(kThreads) k_post_sigw(const double* __restrict__ f, const double* __restrict__ fd,
+                                                        SigwPtrs sg, int lg, PostSigwK K) {
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const Nbr n = neighbours(id, lg);
+    const long long dip = n.ip - id, dim = n.im - id, djp = n.jp - id, djm = n.jm - id, dkp = n.kp - id,
+                    dkm = n.km - id;
+    const double fc = __ldg(&f[id]);
+    const double gx = (__ldg(&f[n.ip]) - __ldg(&f[n.im])) * K.half_over_dx;
+    const double gy = (__ldg(&f[n.jp]) - __ldg(&f[n.jm])) * K.half_over_dx;
+    const double gz = (__ldg(&f[n.kp]) - __ldg(&f[n.km])) * K.half_over_dx;
+    const double gdx = (__ldg(&fd[n.ip]) - __ldg(&fd[n.im])) * K.half_over_dx;
+    const double gdy = (__ldg(&fd[n.jp]) - __ldg(&fd[n.jm])) * K.half_over_dx;
+    const double gdz = (__ldg(&fd[n.kp]) - __ldg(&fd[n.km])) * K.half_over_dx;
+    const double Hxx = (__ldg(&f[n.ip]) - 2.0 * fc + __ldg(&f[n.im])) * K.inv_dx2;
+    const double Hyy = (__ldg(&f[n.jp]) - 2.0 * fc + __ldg(&f[n.jm])) * K.inv_dx2;
+    const double Hzz = (__ldg(&f[n.kp]) - 2.0 * fc + __ldg(&f[n.km])) * K.inv_dx2;
+    // corners (ip, jp, kp), (ip, jm, km), (im, jp, kp), (im, jm, km) with the
+    // indices d1, d2 do not name left in place
+    const double Hxy = cross4(f, id + dip + djp, id + dip + djm, id + dim + djp, id + dim + djm, K.den);
+    const double Hxz = cross4(f, id + dip + dkp, id + dip + dkm, id + dim + dkp, id + dim + dkm, K.den);
+    const double Hyz = cross4(f, id + djp + dkp, id + djm + dkm, id + djp + dkp, id + djm + dkm, K.den);
+    const double dux = gdx * K.invH + gx;
+    const double duy = gdy * K.invH + gy;
+    const double duz = gdz * K.invH + gz;
+    const double S[6] = {4.0 * fc * Hxx + 2.0 * gx * gx - K.coeffU * (dux * dux),
+                         4.0 * fc * Hyy + 2.0 * gy * gy - K.coeffU * (duy * duy),
+                         4.0 * fc * Hzz + 2.0 * gz * gz - K.coeffU * (duz * duz),
+                         4.0 * fc * Hxy + 2.0 * gx * gy - K.coeffU * (dux * duy),
+                         4.0 * fc * Hxz + 2.0 * gx * gz - K.coeffU * (dux * duz),
+                         4.0 * fc * Hyz + 2.0 * gy * gz - K.coeffU * (duy * duz)};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const float* h = sg.hs[c];
+        const float lf = lapl7(h, n, __ldg(&h[id]));
+        const float hdo = sg.hd[c][id];
+        const double rhs = K.d * (K.laplnorm * (double)lf - K.c_hf * (double)hdo / K.a + K.srcAmp * S[c]);
+        sg.hd[c][id] = hdo + (float)rhs;
+    }
+}
+
+// initialize_post_inflation(), src/initialize.cpp:245-290 (without its save):
+// the means are serial sums over the downloaded field in the reference's
+// loop order, so that f is the reference's bit for bit.
+int fp64_post_init(iegpu_ctx* c, double horizon_factor, double omega, int from_deltaN, iegpu_bg* bg) {
+    const size_t gs = c->gs;
+    double* f = c->f[c->cur];
+    std::vector<double> x(gs);
+    const double* src = from_deltaN ? c->dn : f;
+    if (check_cuda(c, cudaMemcpyAsync(x.data(), src, sizeof(double) * gs, cudaMemcpyDeviceToHost, c->stream), "post init"))
+        return IEGPU_ECUDA;
+    std::vector<double> y;
+    if (!from_deltaN) {
+        y.resize(gs);
+        if (check_cuda(c, cudaMemcpyAsync(y.data(), c->fd, sizeof(double) * gs, cudaMemcpyDeviceToHost, c->stream), "post init"))
+            return IEGPU_ECUDA;
+    }
+    if (sync_and_check(c, "post init")) return IEGPU_ECUDA;
+    const double Phi_from_zeta = 3.0 * (1.0 + omega) / (5.0 + 3.0 * omega);
+    double mean = 0.0, den = 1.0;
+    if (from_deltaN) {
+        for (size_t id = 0; id < gs; ++id) mean += x[id];
+        mean = mean / (double)gs;
+    } else {
+        double fdmean = 0.0;
+        for (size_t id = 0; id < gs; ++id) {
+            mean += x[id];
+            fdmean += y[id];
+        }
+        mean = mean / (double)gs;
+        fdmean = fdmean / (double)gs;
+        const double s = c->cfg.rescale_s;
+        den = fdmean * pow(bg->a, s - 1.0) / (bg->ad * pow(bg->a, s - 2.0));
+    }
+    const unsigned grid = (unsigned)((gs + kThreads - 1) / kThreads);
+    k_post_field<<<grid, kThreads, 0, c->stream>>>(f, src, (long long)gs, Phi_from_zeta, mean, den, !from_deltaN);
+    c->launches++;
+    for (int q = 0; q < 6 && c->cfg.sigw; ++q) {
+        cudaMemsetAsync(c->h[c->cur][q], 0, sizeof(float) * gs, c->stream);
+        cudaMemsetAsync(c->hd[q], 0, sizeof(float) * gs, c->stream);
+    }
+    const double pi = 2.0 * asin(1.0);
+    bg->t = 0.0;
+    bg->a = 1.0;
+    bg->ad = horizon_factor * c->N * 2.0 * pi / c->cfg.L;
+    return sync_and_check(c, "post init");
+}
+
+// evolve_derivs_post_inflation(d), src/evolution.cpp:1436-1555, enqueued.
+static void post_kick(iegpu_ctx* c, double d, double omega, iegpu_bg* bg) {
+    const double s = c->cfg.rescale_s, dx = c->cfg.L / (double)c->N;
+    const double a = bg->a;
+    const double laplnorm = pow(a, -2.0 * s) / (dx * dx);
+    bg->ad2 = -(s - 0.5 * (1.0 - 3.0 * omega)) * (bg->ad * bg->ad) / a;
+    bg->ad += 0.5 * d * bg->ad2;
+    const double ad = bg->ad;
+    const unsigned grid = (unsigned)(c->gs / kThreads);
+    double* f = c->f[c->cur];
+    k_post_kick<<<grid, kThreads, 0, c->stream>>>(f, c->fd, c->lg, d, omega * laplnorm, (3.0 * (1.0 + omega) + s) * ad, a);
+    c->launches++;
+    if (c->cfg.sigw) {
+        SigwPtrs sg{};
+        for (int q = 0; q < 6; ++q) { sg.hs[q] = c->h[c->cur][q]; sg.hd[q] = c->hd[q]; }
+        const double Htilde = ad / a;
+        PostSigwK K;
+        K.d = d;
+        K.laplnorm = laplnorm;
+        K.c_hf = (2.0 + s) * ad;
+        K.a = a;
+        K.invH = 1.0 / Htilde;
+        K.coeffU = 4.0 / (3.0 * (1.0 + omega));
+        K.srcAmp = 2.0 * pow(a, -2.0 * s);
+        K.half_over_dx = 0.5 / dx;
+        K.inv_dx2 = 1.0 / (dx * dx);
+        K.den = 4.0 * dx * dx;
+        k_post_sigw<<<grid, kThreads, 0, c->stream>>>(f, c->fd, sg, c->lg, K);
+        c->launches++;
+    }
+    bg->ad += 0.5 * d * bg->ad2;
+}
+
+// evolve_fields(d), src/evolution.cpp:260-284, enqueued.
+static void post_drift(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    bg->t += d;
+    const unsigned grid = (unsigned)((c->gs + kThreads - 1) / kThreads);
+    SigwPtrs sg{};
+    if (c->cfg.sigw)
+        for (int q = 0; q < 6; ++q) { sg.hdst[q] = c->h[c->cur][q]; sg.hd[q] = c->hd[q]; }
+    if (c->cfg.sigw) k_drift<true><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, sg, (long long)c->gs, d);
+    else k_drift<false><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, sg, (long long)c->gs, d);
+    c->launches++;
+    bg->a += d * bg->ad;
+}
+
+int fp64_post_derivs(iegpu_ctx* c, double d, double omega, iegpu_bg* bg) {
+    post_kick(c, d, omega, bg);
+    return sync_and_check(c, "post-inflation kick");
+}
+
+// The leapfrog loop body of run_post_inflation_loop, src/evolution.cpp:1589-1597:
+// while a <= af_post: kick, drift; at most max_steps steps.
+int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg,
+                       int* steps) {
+    int n = 0;
+    while (n < max_steps && bg->a <= af_post) {
+        post_kick(c, dt_post, omega, bg);
+        post_drift(c, dt_post, bg);
+        ++n;
+    }
+    if (steps) *steps = n;
+    return sync_and_check(c, "post-inflation leapfrog");
+}
+
+}  // namespace iegpu

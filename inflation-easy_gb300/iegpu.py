@@ -101,6 +101,9 @@ def load() -> C.CDLL:
         "iegpu_shell_spectrum_noalloc": (I, [P, P, I, P, P, P]),
         "iegpu_set_shape": (I, [P, I, I, I]),
         "iegpu_set_persistent": (I, [P, I]),
+        "iegpu_initialize_post_inflation": (I, [P, D, D, I, C.POINTER(Bg)]),
+        "iegpu_evolve_derivs_post_inflation": (I, [P, D, D, C.POINTER(Bg)]),
+        "iegpu_post_inflation_leapfrog": (I, [P, D, D, D, I, C.POINTER(Bg), C.POINTER(I)]),
         "iegpu_ens_create": (I, [C.POINTER(Config), ip, I, C.POINTER(P)]),
         "iegpu_ens_destroy": (I, [P]),
         "iegpu_ens_last_error": (C.c_char_p, [P]),
@@ -234,6 +237,22 @@ class Lattice:
     # -- measurement ------------------------------------------------------
     def set_shape(self, rows: int, prefetch: int, chunks: int) -> None:
         self._check(self.lib.iegpu_set_shape(self.h, rows, prefetch, chunks))
+
+    # -- post-inflation phase (plain FP64 form, SIGW on) ------------------
+    def initialize_post_inflation(self, bg: Bg, horizon_factor: float = 1.0, omega: float = 1.0 / 3.0,
+                                  from_deltaN: bool = True) -> None:
+        self._check(self.lib.iegpu_initialize_post_inflation(self.h, horizon_factor, omega, int(from_deltaN),
+                                                             C.byref(bg)))
+
+    def evolve_derivs_post_inflation(self, d: float, bg: Bg, omega: float = 1.0 / 3.0) -> None:
+        self._check(self.lib.iegpu_evolve_derivs_post_inflation(self.h, d, omega, C.byref(bg)))
+
+    def post_inflation_leapfrog(self, af_post: float, dt_post: float, max_steps: int, bg: Bg,
+                                omega: float = 1.0 / 3.0) -> int:
+        steps = C.c_int(0)
+        self._check(self.lib.iegpu_post_inflation_leapfrog(self.h, af_post, dt_post, omega, max_steps, C.byref(bg),
+                                                           C.byref(steps)))
+        return steps.value
 
     def set_persistent(self, on: bool) -> None:
         self._check(self.lib.iegpu_set_persistent(self.h, int(bool(on))))
