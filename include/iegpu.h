@@ -188,9 +188,10 @@ int  iegpu_evolve_derivs_post_inflation(struct iegpu_ctx* ctx, double d, double 
  * while bg->a <= af_post, evolve_derivs_post_inflation(dt_post) then
  * evolve_fields(dt_post), at most max_steps times; *steps = steps taken.  The
  * half drift before the loop and the saves are the caller's, as in the
- * reference.  The steps are enqueued without synchronisation. */
+ * reference.  The steps are enqueued without synchronisation.  a_trace (may
+ * be null, else max_steps entries) receives a after each step taken. */
 int  iegpu_post_inflation_leapfrog(struct iegpu_ctx* ctx, double af_post, double dt_post, double omega, int max_steps,
-                                   iegpu_bg* bg, int* steps);
+                                   iegpu_bg* bg, int* steps, double* a_trace);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */
 /* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */

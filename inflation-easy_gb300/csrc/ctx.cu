@@ -560,12 +560,12 @@ int iegpu_evolve_derivs_post_inflation(iegpu_ctx* c, double d, double omega, ieg
 }
 
 int iegpu_post_inflation_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps,
-                                  iegpu_bg* bg, int* steps) {
+                                  iegpu_bg* bg, int* steps, double* a_trace) {
     if (!c || !bg) return IEGPU_EINVAL;
     if (steps) *steps = 0;
     if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
     if (int rc = post_ok(c)) return rc;
-    return fp64_post_leapfrog(c, af_post, dt_post, omega, max_steps, bg, steps);
+    return fp64_post_leapfrog(c, af_post, dt_post, omega, max_steps, bg, steps, a_trace);
 }
 
 int iegpu_set_persistent(iegpu_ctx* c, int on) {

@@ -267,7 +267,7 @@ int fp64_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
 int fp64_post_init(iegpu_ctx* c, double horizon_factor, double omega, int from_deltaN, iegpu_bg* bg);
 int fp64_post_derivs(iegpu_ctx* c, double d, double omega, iegpu_bg* bg);
 int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg,
-                       int* steps);
+                       int* steps, double* a_trace);
 int fp64_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]);
 int fp64_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk);
 void fp64_destroy_graphs(iegpu_ctx* c);

@@ -672,11 +672,12 @@ int fp64_post_derivs(iegpu_ctx* c, double d, double omega, iegpu_bg* bg) {
 // The leapfrog loop body of run_post_inflation_loop, src/evolution.cpp:1589-1597:
 // while a <= af_post: kick, drift; at most max_steps steps.
 int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg,
-                       int* steps) {
+                       int* steps, double* a_trace) {
     int n = 0;
     while (n < max_steps && bg->a <= af_post) {
         post_kick(c, dt_post, omega, bg);
         post_drift(c, dt_post, bg);
+        if (a_trace) a_trace[n] = bg->a;
         ++n;
     }
     if (steps) *steps = n;

@@ -1,7 +1,7 @@
 // ie_main.cpp -- host program of the GB300 InflationEasy engine.
 //
 // The reference's driver (src/main.cpp:103-146), leapfrog loops
-// (src/evolution.cpp:909-997, 1291-1375), initial conditions
+// (src/evolution.cpp:909-997, 1291-1375, 1561-1653), initial conditions
 // (src/initialize.cpp) and output routines (src/output.cpp), with every
 // lattice operation sent through the C ABI of include/iegpu.h.  It reads
 // params.txt from the working directory and writes results/ in the
@@ -73,6 +73,19 @@ FILE* open_or_die(const std::string& name, const char* mode = "w") {
     const std::string path = RES + "/" + name + ".dat";
     FILE* fp = std::fopen(path.c_str(), mode);
     if (!fp) fatal("Failed to open output file: %s\n", path.c_str());
+    return fp;
+}
+
+// The output files of the inflation phase (post = 0) or of the post-inflation
+// phase (post = 1, results/post_inflation/, src/output.cpp:1573-1867), opened
+// on first use and kept open, as the reference's static FILE pointers.
+FILE* out_file(const char* name, int post) {
+    static std::vector<std::pair<std::string, FILE*>> files;
+    const std::string key = std::string(post ? "post_inflation/" : "") + name;
+    for (auto& e : files)
+        if (e.first == key) return e.second;
+    FILE* fp = open_or_die(key);
+    files.emplace_back(key, fp);
     return fp;
 }
 
@@ -279,9 +292,11 @@ void print_spectrum(FILE* out, const std::vector<int>& counts, std::vector<doubl
     std::fflush(out);
 }
 
-void meansvars() {
-    static FILE *m = nullptr, *v = nullptr, *ve = nullptr;
-    if (!m) { m = open_or_die("means"); v = open_or_die("variance"); ve = open_or_die("velocity"); }
+// meansvars(), src/output.cpp:204-269; post: meansvars_post_inflation, :1576-1639
+void meansvars(int post = 0) {
+    FILE* m = out_file("means", post);
+    FILE* v = out_file("variance", post);
+    FILE* ve = out_file("velocity", post);
     std::fprintf(m, "%f", bg.t); std::fprintf(m, " %e", bg.a);
     std::fprintf(ve, "%f", bg.t); std::fprintf(ve, " %e", bg.a);
     std::fprintf(v, "%f", bg.t); std::fprintf(v, " %e", bg.a);
@@ -296,7 +311,7 @@ void meansvars() {
     std::fprintf(v, " %e", s[2] - pw2(av));
     {
         const double q[5] = {bg.t, bg.a, av, vel, bg.ad * P.rescale_B * std::pow(bg.a, P.rescale_s - 2.0)};
-        prec_line("means", q, 5);
+        prec_line(post ? "post_means" : "means", q, 5);
     }
     if (av + DBL_MAX == av || (av != 0. && av / av != 1.)) {
         std::printf("Unstable solution developed. Scalar field not numerical at t=%f\n", bg.t);
@@ -307,9 +322,9 @@ void meansvars() {
     std::fflush(m); std::fflush(v); std::fflush(ve);
 }
 
-void scale() {
-    static FILE* sf = nullptr;
-    if (!sf) sf = open_or_die("sf");
+// scale(), src/output.cpp:272-293; post: scale_post_inflation, :1642-1662
+void scale(int post = 0) {
+    FILE* sf = out_file("sf", post);
     const double B = P.rescale_B, s = P.rescale_s, a = bg.a;
     std::fprintf(sf, "%f %f %e %e\n", bg.t, a, bg.ad * B * std::pow(a, s - 2.0),
                  pw2(B) * std::pow(a, 2.0 * s - 2.0) * (bg.ad2 + (s - 1.0) * pw2(bg.ad) / a));
@@ -332,45 +347,50 @@ void energy() {
     std::fflush(c);
 }
 
-void spectraf() {
-    static FILE *sp = nullptr, *st = nullptr;
-    if (!sp) { sp = open_or_die("spectra"); st = open_or_die("spectratimes"); }
+// spectraf(), src/output.cpp:297-406; post: spectraf_post_inflation, :1667-1770
+void spectraf(int post = 0) {
+    FILE* sp = out_file("spectra", post);
+    FILE* st = out_file("spectratimes", post);
     const int nb = iegpu_numbins(P.N);
     std::vector<int> counts(nb);
     std::vector<double> f2(nb);
     const double norm1 = std::pow(P.L / P.rescale_B, 3) / std::pow((double)P.N, 6);
     ck(iegpu_spectrum(G, IEGPU_F, counts.data(), f2.data(), nb));
-    print_spectrum(sp, counts, f2, norm1, "spectrum");
+    print_spectrum(sp, counts, f2, norm1, post ? "post_spectrum" : "spectrum");
     std::fprintf(st, "%f %e\n", bg.t, bg.a);
     std::fflush(st);
 }
 
 // spectraGW / spectraGWdot, src/output.cpp:618-648: the per-bin sums come
 // back in double; division and normalisation are the reference's float ones.
-void spectra_gw(int which) {
-    static FILE* fp[2] = {nullptr, nullptr};
-    if (!fp[which]) fp[which] = open_or_die(which ? "spectraGWdot" : "spectraGW");
+// Post (src/output.cpp:652-669): spectraGWdot_post_inflation multiplies h' in
+// float by (float)(B a^(s-1)); rounding (double)h' * (double)(float)(B a^(s-1))
+// to float gives the same bits, the double product of two floats being exact.
+void spectra_gw(int which, int post = 0) {
+    FILE* fp = out_file(which ? "spectraGWdot" : "spectraGW", post);
     const int nb = iegpu_numbins(P.N);
     std::vector<int> counts(nb);
     std::vector<double> f2(nb);
-    const double to_phys = which ? P.rescale_B * std::pow(bg.a, P.rescale_s - 1.0) : 1.0;
+    double to_phys = which ? P.rescale_B * std::pow(bg.a, P.rescale_s - 1.0) : 1.0;
+    if (post && which) to_phys = (double)(float)to_phys;
     ck(iegpu_gw_spectrum(G, which, to_phys, counts.data(), f2.data(), nb));
     const int numbins = (int)(std::sqrt(3.0) * (P.N / 2)) + 1;
     if (g_prec) {
         const double n1 = 0.5 * std::pow(P.L / P.rescale_B, 3) / std::pow((double)P.N, 6);
         std::vector<double> pv((size_t)numbins);
         for (int i = 0; i < numbins; ++i) pv[(size_t)i] = counts[i] > 0 ? n1 * f2[i] / counts[i] : 0.0;
-        prec_line(which ? "spectrumGWdot" : "spectrumGW", pv.data(), numbins);
+        prec_line(which ? (post ? "post_spectrumGWdot" : "spectrumGWdot") : (post ? "post_spectrumGW" : "spectrumGW"),
+                  pv.data(), numbins);
     }
     const float dp = 2.f * (float)pi / (float)P.L;
     const float norm1 = 0.5f * std::pow(P.L / P.rescale_B, 3) / std::pow((float)P.N, 6);
     for (int i = 0; i < numbins; ++i) {
         float v = (float)f2[i];
         if (counts[i] > 0) v /= (float)counts[i];
-        std::fprintf(fp[which], "%e %d %e\n", dp * i, counts[i], norm1 * v);
+        std::fprintf(fp, "%e %d %e\n", dp * i, counts[i], norm1 * v);
     }
-    std::fprintf(fp[which], "\n");
-    std::fflush(fp[which]);
+    std::fprintf(fp, "\n");
+    std::fflush(fp);
 }
 
 void histogram_out(int field, FILE* hist, FILE* times, bool deltaN_style) {
@@ -604,6 +624,66 @@ void run_deltaN_loop() {
     evolve_fieldsN(-0.5 * P.dN);
 }
 
+// save_post_inflation(), src/output.cpp:1840-1865 (leapfrog: staggered)
+void save_post(int infrequent) {
+    if (g_trace)
+        std::fprintf(g_trace, "savep %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, bg.t, bg.a, bg.ad, bg.ad2, bg.astep);
+    if (bg.t > 0.) evolve_fields(-.5 * P.dt_post_inflation);
+    meansvars(1);
+    scale(1);
+    if (infrequent) {
+        if (P.output_spectra) {
+            spectraf(1);
+            spectra_gw(0, 1);
+            spectra_gw(1, 1);
+        }
+        if (P.output_histogram) histogram_out(IEGPU_F, out_file("histogram", 1), out_file("histogramtimes", 1), false);
+    }
+    if (bg.t > 0.) evolve_fields(.5 * P.dt_post_inflation);
+}
+
+// run_post_inflation_loop, leapfrog branch (src/evolution.cpp:1561-1653),
+// with initialize_post_inflation (src/initialize.cpp:245-290).  The device
+// runs the steps between two outputs in one call.
+void run_post_inflation_loop() {
+    const std::string dir = RES + "/post_inflation";
+    struct stat st;
+    if (stat(dir.c_str(), &st) != 0 && mkdir(dir.c_str(), 0777) != 0)
+        fatal("Failed to create '%s' directory.\n", dir.c_str());
+    t0 = 0.0;
+    ck(iegpu_initialize_post_inflation(G, P.horizon_factor, P.omega, P.perform_deltaN, &bg));
+    save_post(1);
+    int numsteps = 0;
+    evolve_fields(0.5 * P.dt_post_inflation);
+    std::vector<double> trace;
+    while (bg.a <= P.af_post_inflation) {
+        const int chunk = P.output_freq - numsteps % P.output_freq;
+        trace.assign((size_t)chunk, 0.0);
+        int taken = 0;
+        ck(iegpu_post_inflation_leapfrog(G, P.af_post_inflation, P.dt_post_inflation, P.omega, chunk, &bg, &taken,
+                                         trace.data()));
+        for (int s = 0; s < taken; ++s) {
+            numsteps++;
+            double a_now = trace[(size_t)s];
+            if (s == taken - 1 && numsteps % P.output_freq == 0) {
+                save_post((numsteps % P.output_infrequent_freq == 0) ? 1 : 0);
+                a_now = bg.a;
+            }
+            if (P.screen_updates && numsteps % P.output_freq == 0) {
+                std::printf("scale factor a = %f\n", a_now);
+                std::printf("numsteps %i\n\n", numsteps);
+            }
+            std::fprintf(output_, "scale factor a = %f\n", a_now);
+            std::fprintf(output_, "numsteps %i\n\n", numsteps);
+            if (numsteps % P.output_freq == 0) std::fflush(output_);
+        }
+        if (taken == 0) break;
+    }
+    std::printf("Saving final inflaton data\n");
+    std::fflush(output_);
+    save_post(1);
+}
+
 // Final state in the binary layout of the oracle's state.bin.
 void write_state(const std::string& path) {
     FILE* fp = std::fopen(path.c_str(), "wb");
@@ -646,6 +726,10 @@ int main(int argc, char** argv) {
         fatal("Only the leapfrog integrator is provided by this engine (got %s / %s).\n",
               P.inflation_integrator.c_str(), P.deltaN_integrator.c_str());
     if (P.forcing_cutoff && P.high_cutoff_index > 0) fatal("forcing_cutoff is not provided by this engine.\n");
+    if (P.post_inflation && !P.calculate_SIGW) fatal("post_inflation requires calculate_SIGW = 1\n");
+    if (P.post_inflation && P.form != 0) fatal("the post-inflation phase runs on the plain FP64 form (form = fp64)\n");
+    if (P.post_inflation && P.post_inflation_integrator != "leapfrog")
+        fatal("Only the leapfrog integrator is provided by this engine (got %s).\n", P.post_inflation_integrator.c_str());
     if (P.output_bispectrum || P.output_LOG)
         std::fprintf(stderr, "Ignoring output_bispectrum / output_LOG: not provided by this engine.\n");
     struct stat st;
@@ -685,6 +769,7 @@ int main(int argc, char** argv) {
 
     run_evolution_loop();
     if (P.perform_deltaN) run_deltaN_loop();
+    if (P.post_inflation) run_post_inflation_loop();
 
     output_parameters(false);
     if (!dump_dir.empty()) {

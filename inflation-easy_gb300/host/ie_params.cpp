@@ -91,7 +91,7 @@ bool ie_params_load(IeParams& p, const char* path) {
     if (kv.count("N")) to_int(kv["N"], N);
     if (kv.count("numerical_potential")) to_int(kv["numerical_potential"], numerical);
     ie_params_defaults(p, N, numerical != 0);
-    bool B_given = false, af_given = false;
+    bool B_given = false, af_given = false, af_post_given = false;
     for (const auto& [k, v] : kv) {
         double d;
         int i;
@@ -114,9 +114,14 @@ bool ie_params_load(IeParams& p, const char* path) {
         else if (k == "dt" && to_double(v, d)) p.dt = d;
         else if (k == "inflation_integrator") p.inflation_integrator = v;
         else if (k == "deltaN_integrator") p.deltaN_integrator = v;
-        else if (k == "post_inflation_integrator" || k == "horizon_factor" || k == "omega" ||
-                 k == "dt_post_inflation" || k == "af_post_inflation" || k.rfind("rk45_", 0) == 0) {
-            // accepted for compatibility; those paths are not part of this engine
+        else if (k == "post_inflation" && to_int(v, i)) p.post_inflation = (i != 0);
+        else if (k == "horizon_factor" && to_double(v, d)) p.horizon_factor = d;
+        else if (k == "omega" && to_double(v, d)) p.omega = d;
+        else if (k == "dt_post_inflation" && to_double(v, d)) p.dt_post_inflation = d;
+        else if (k == "af_post_inflation" && to_double(v, d)) { p.af_post_inflation = d; af_post_given = true; }
+        else if (k == "post_inflation_integrator") p.post_inflation_integrator = v;
+        else if (k.rfind("rk45_", 0) == 0) {
+            // accepted for compatibility; the RK45 integrators are not part of this engine
         }
         else if (k == "output_freq" && to_int(v, i)) p.output_freq = i;
         else if (k == "output_infrequent_freq" && to_int(v, i)) p.output_infrequent_freq = i;
@@ -144,6 +149,7 @@ bool ie_params_load(IeParams& p, const char* path) {
     }
     if (!B_given) p.rescale_B = std::sqrt(p.V0);
     if (!af_given) p.af = 2.0 * p.N;
+    if (!af_post_given) p.af_post_inflation = 2.0 * p.N;
     p.dx = p.L / (double)p.N;
     if (p.criterion == 99) p.criterion = p.numerical_potential ? 1 : -1;
     return true;

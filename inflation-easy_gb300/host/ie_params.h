@@ -3,8 +3,9 @@
 // The keys, defaults and derived values of the reference's params.txt handling
 // (src/runtime_parameters.cpp:17-112, 195-365).  The switches the reference
 // fixes at compile time in src/parameters.h (N, numerical_potential,
-// perform_deltaN, calculate_SIGW, the deltaN criterion) are run-time keys
-// here, plus `form` (fp64 | split) for the engine's arithmetic form.
+// perform_deltaN, calculate_SIGW, post_inflation, the deltaN criterion) are
+// run-time keys here, plus `form` (fp64 | split) for the engine's arithmetic
+// form.
 #pragma once
 
 #include <string>
@@ -52,6 +53,14 @@ struct IeParams {
     double dx = 0.0;
     std::string inflation_integrator = "leapfrog";
     std::string deltaN_integrator = "leapfrog";
+    // post-inflation phase (src/parameters.h:31 switch, run-time here and off
+    // by default; src/runtime_parameters.cpp:48-52, 295-299)
+    int post_inflation = 0;
+    double horizon_factor = 1.0;
+    double omega = 1.0 / 3.0;
+    double dt_post_inflation = 0.001;
+    double af_post_inflation = 0.0;   // 2N unless given
+    std::string post_inflation_integrator = "leapfrog";
 };
 
 // Defaults of the reference for the given potential kind and N.

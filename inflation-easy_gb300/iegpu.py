@@ -103,7 +103,7 @@ def load() -> C.CDLL:
         "iegpu_set_persistent": (I, [P, I]),
         "iegpu_initialize_post_inflation": (I, [P, D, D, I, C.POINTER(Bg)]),
         "iegpu_evolve_derivs_post_inflation": (I, [P, D, D, C.POINTER(Bg)]),
-        "iegpu_post_inflation_leapfrog": (I, [P, D, D, D, I, C.POINTER(Bg), C.POINTER(I)]),
+        "iegpu_post_inflation_leapfrog": (I, [P, D, D, D, I, C.POINTER(Bg), C.POINTER(I), dp]),
         "iegpu_ens_create": (I, [C.POINTER(Config), ip, I, C.POINTER(P)]),
         "iegpu_ens_destroy": (I, [P]),
         "iegpu_ens_last_error": (C.c_char_p, [P]),
@@ -248,11 +248,13 @@ class Lattice:
         self._check(self.lib.iegpu_evolve_derivs_post_inflation(self.h, d, omega, C.byref(bg)))
 
     def post_inflation_leapfrog(self, af_post: float, dt_post: float, max_steps: int, bg: Bg,
-                                omega: float = 1.0 / 3.0) -> int:
+                                omega: float = 1.0 / 3.0, trace: bool = False):
         steps = C.c_int(0)
+        tr = np.zeros(max(1, max_steps), dtype=np.float64) if trace else None
         self._check(self.lib.iegpu_post_inflation_leapfrog(self.h, af_post, dt_post, omega, max_steps, C.byref(bg),
-                                                           C.byref(steps)))
-        return steps.value
+                                                           C.byref(steps),
+                                                           None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
+        return (steps.value, tr[:steps.value]) if trace else steps.value
 
     def set_persistent(self, on: bool) -> None:
         self._check(self.lib.iegpu_set_persistent(self.h, int(bool(on))))

@@ -170,3 +170,52 @@ def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mo
         ca = [r[1] for r in parse_numbers(wd / "results" / name)]
         cb = [r[1] for r in parse_numbers(od / "results" / name)]
         assert ca == cb
+
+
+def test_program_post_inflation_matches_reference_fixture(tmp_path):
+    """The program with the post-inflation phase on (16^3, USR, SIGW, deltaN)
+    against the reference program's own outputs of that phase
+    (tests/golden/n16_usr_sigw_post): results/post_inflation/* number by
+    number, and the final fields.  The phase starts from the deltaN map, which
+    the engine reproduces to round-off (its sums are re-associated), so the
+    tolerances are those of the inflation outputs above."""
+    src = GOLDEN / "n16_usr_sigw_post"
+    text = (src / "params.txt").read_text() + "post_inflation = 1\n"
+    wd = run_main(tmp_path, text, 16, 1, 1)
+    names = sorted(x.name for x in (src / "results" / "post_inflation").iterdir())
+    got_names = sorted(x.name for x in (wd / "results" / "post_inflation").iterdir())
+    assert names == got_names
+    ref_state = np.load(src / "state.npz")
+    for name in names:
+        a = src / "results" / "post_inflation" / name
+        b = wd / "results" / "post_inflation" / name
+        A = np.concatenate([np.array(r) for r in parse_numbers(a)])
+        B = np.concatenate([np.array(r) for r in parse_numbers(b)])
+        assert A.shape == B.shape, name
+        rel = np.max(np.abs(A - B) / (np.abs(A) + 1e-300 + 1e-12 * np.max(np.abs(A))))
+        print(f"post {name}: max rel dev {rel:.3e}")
+        if name.startswith("histogram") and not name.startswith("histogramtimes"):
+            assert np.max(np.abs(A - B)) <= 2.0 / 16 ** 3 + 1e-12, name
+        elif name.startswith("spectraGW"):
+            compare_text(a, b, 2e-5)
+        else:
+            compare_text(a, b, 2e-6)
+    import ieo
+    got = ieo.read_state(wd / "dump" / "state.bin")
+    for key in ("f", "fd"):
+        ref = ref_state[key]
+        d = np.max(np.abs(got[key] - ref)) / np.std(ref)
+        print(f"post {key}: max dev / std {d:.3e}")
+        assert d < 1e-6, key
+    for key in ("h", "hd"):
+        ref = ref_state[key].astype(np.float64)
+        d = np.max(np.abs(got[key].astype(np.float64) - ref)) / np.std(ref)
+        print(f"post {key}: max dev / std {d:.3e}")
+        assert d < 1e-4, key
+    ta = [l.split() for l in (src / "trace.txt").read_text().splitlines() if l.startswith("savep")]
+    tb = [l.split() for l in (wd / "dump" / "trace.txt").read_text().splitlines() if l.startswith("savep")]
+    assert len(ta) == len(tb) and len(ta) > 2
+    for x, y in zip(ta, tb):
+        for u, v in zip(x[2:], y[2:]):
+            u, v = float(u), float(v)
+            assert abs(u - v) <= 1e-10 * abs(u) + 1e-300, (x, y)
