@@ -54,6 +54,7 @@ UNIT = "site-updates/s"
 BYTES_STEP_SPLIT = 16  # split form: read dphi, dpi; write dphi, dpi (FP32)
 BYTES_KICK_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
 BYTES_STEP_SIGW = 112  # split form with SIGW: 16 + read and write 6 h_ij and 6 h_ij' (FP32)
+BYTES_STEP_POST = 128  # post-inflation phase: read and write f, fd (FP64) and 6 h_ij, 6 h_ij' (FP32)
 
 
 def dist_env():
@@ -380,6 +381,35 @@ def measure_sigw(iegpu, N, steps, warmup, peak):
             "frac_of_measured_hbm": achieved / peak, "gw_spectrum_s": t_gw, "gw_bins": int((counts > 0).sum())}
 
 
+def measure_post_inflation(iegpu, N, steps, warmup, peak):
+    """The post-inflation phase (radiation era, plain FP64 form, SIGW on): the
+    hilltop lattice's device initial conditions turned into Phi by
+    initialize_post_inflation (without deltaN), then K leapfrog steps of the
+    fd kick, the Hessian-sourced tensor kick and the drift."""
+    w = WORKLOAD
+    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=iegpu.FORM_FP64, sigw=True)
+    H = lat.bunch_davies(w["seed"], w["phi0"], w["dphi0"])
+    bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
+    lat.initialize_post_inflation(bg, 1.0, 1.0 / 3.0, from_deltaN=False)
+    dt = 0.001   # dt_post_inflation of the reference's presets
+    lat.evolve_fields(0.5 * dt, bg)
+    lat.post_inflation_leapfrog(1e30, dt, warmup, bg)
+    lat.timer_start()
+    taken = lat.post_inflation_leapfrog(1e30, dt, steps, bg)
+    ms = lat.timer_stop()
+    assert taken == steps
+    lat.close()
+    per_step = ms / steps
+    achieved = BYTES_STEP_POST * N ** 3 / (per_step * 1e-3) / 1e9
+    return {"workload": f"post-inflation phase, N={N}^3, plain FP64 form with SIGW (omega = 1/3, from the hilltop "
+                        f"device initial conditions)",
+            "steps": steps, "ms_per_step": per_step, "site_updates_per_s": N ** 3 / (per_step * 1e-3),
+            "algorithmic_bytes_per_site": BYTES_STEP_POST, "achieved_gbs": achieved,
+            "frac_of_measured_hbm": achieved / peak,
+            "note": "three kernels per step (fd kick, tensor kick with the 19-point Hessian source, drift), "
+                    "FP64 per-site arithmetic in the reference's order"}
+
+
 def engine_arm(args):
     ws, rank, local = dist_env()
     dist = None
@@ -413,6 +443,7 @@ def engine_arm(args):
     # the batched ensemble (fewer steps: each is ~5x the 256^3 step)
     ens = measure_ensemble(iegpu, max(20, min(args.steps // 30, 500)), args.warmup, peak)
     sigw = measure_sigw(iegpu, N, max(10, min(args.steps // 75, 200)), args.warmup, peak)
+    post = measure_post_inflation(iegpu, N, max(10, min(args.steps // 300, 100)), args.warmup, peak)
     if rank != 0:
         return 0
 
@@ -446,7 +477,8 @@ def engine_arm(args):
                                "note": "per-site arithmetic in the reference's order (-fmad=false); FP64 ALU bound"},
                       "split_over_fp64": value / fp_value,
                       "batched": ens,
-                      "sigw": sigw},
+                      "sigw": sigw,
+                      "post_inflation": post},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None if tr is None else tr * N ** 3,
                          "kernel": "k_split_rows4_persist (fused kick + drift + next-step Friedmann sums; 64 steps per cooperative "

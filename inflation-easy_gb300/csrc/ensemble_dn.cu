@@ -16,6 +16,8 @@
 #include <cmath>
 #include <vector>
 
+#include <thread>
+
 #include "ensemble.cuh"
 #include "pot.cuh"
 #include "reduce.cuh"
@@ -183,28 +185,6 @@ __global__ void k_ens_phiref_pick(EnsDn A, int S, const double* pval, const long
     out[b] = A.f[A.lat[b].off + bi];
 }
 
-// saveN's float accumulator per lattice (src/output.cpp:1527-1537), one warp
-// per lattice replaying the recurrence in site order (as k_saveN_mean).
-__global__ void k_ens_saveN_mean(EnsDn A, double cutoff, float* out) {
-    const int b = blockIdx.x;
-    const int lane = threadIdx.x & 31;
-    const EnsLat& L = A.lat[b];
-    const long long gs = 1LL << (3 * L.lg);
-    const double* dn = A.dn + L.off;
-    float m = 0.f;
-    for (long long base = 0; base < gs; base += 32) {
-        const long long id = base + lane;
-        const double v = id < gs ? dn[id] : 0.0;
-#pragma unroll 8
-        for (int q = 0; q < 32; ++q) {
-            const double x = __shfl_sync(0xffffffffu, v, q);
-            if (base + q < gs && x <= cutoff) m = (float)((double)m + x);
-        }
-    }
-    m = m / (float)gs;
-    if (lane == 0) out[b] = m;
-}
-
 // zeta = deltaN - Nmean (deltaN[idx] -= Nmean, a float promoted to double)
 __global__ void __launch_bounds__(256) k_ens_shift(EnsDn A, const float* __restrict__ nmean) {
     const int b = block_lattice(A.lat, A.count);
@@ -365,14 +345,30 @@ int ens_phiref(iegpu_ens* e, double* phiref_h) {
     return IEGPU_OK;
 }
 
+// saveN's float accumulator of every lattice (float_mean_serial): the maps
+// are copied down and the lattices' recurrences run on host threads.
 int ens_saveN_mean(iegpu_ens* e, double cutoff, float* nmean_h) {
-    float* d = reinterpret_cast<float*>(e->iscr);
-    k_ens_saveN_mean<<<e->count, 32, 0, e->stream>>>(ens_dn(e), cutoff, d);
-    e->launches++;
-    if (int rc = ens_cuda(e, cudaMemcpyAsync(nmean_h, d, sizeof(float) * (size_t)e->count, cudaMemcpyDeviceToHost,
+    const long long total = e->lat_h.back().off + (1LL << (3 * e->lat_h.back().lg));
+    std::vector<double> x((size_t)total);
+    if (int rc = ens_cuda(e, cudaMemcpyAsync(x.data(), e->dn, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost,
                                              e->stream), "saveN mean"))
         return rc;
-    return ens_dsync(e, "saveN mean");
+    if (int rc = ens_dsync(e, "saveN mean")) return rc;
+    const int count = e->count;
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt < 1) nt = 1;
+    if (nt > 16) nt = 16;
+    if ((int)nt > count) nt = (unsigned)count;
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t)
+        pool.emplace_back([&, t] {
+            for (int b = (int)t; b < count; b += (int)nt) {
+                const EnsLat& L = e->lat_h[(size_t)b];
+                nmean_h[b] = float_mean_serial(x.data() + L.off, 1LL << (3 * L.lg), cutoff);
+            }
+        });
+    for (auto& th : pool) th.join();
+    return IEGPU_OK;
 }
 
 int ens_shift(iegpu_ens* e, const float* nmean_h) {

@@ -259,6 +259,20 @@ __host__ __device__ inline double pow_exp(double x, double y) {
     return pow(x, y);
 }
 
+// saveN's float accumulator, src/output.cpp:1527-1537: over the sites with
+// x <= cutoff, in site order, Nmean += x with a float Nmean and a double x
+// (the sum formed in double, then rounded to float), and Nmean / gridsize in
+// float.  The recurrence is serial by definition.  On GB300 each step of a
+// device replay is a chain of dependent FP64 operations (about 150 ns a
+// site); the host runs it at a few ns a site, so the map is copied down and
+// replayed here.
+inline float float_mean_serial(const double* x, long long n, double cutoff) {
+    float m = 0.f;
+    for (long long i = 0; i < n; ++i)
+        if (x[i] <= cutoff) m = (float)((double)m + x[i]);
+    return m / (float)n;
+}
+
 // --- launchers implemented in the .cu files ---------------------------------
 // leapfrog_fp64.cu
 int fp64_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace);

@@ -7,7 +7,8 @@
 //                      exact min/max, then integer bin counts
 //   get_phiref         first extremal site in loop order (src/evolution.cpp:1271-1288)
 //   saveN_mean         the float accumulator of saveN (src/output.cpp:1527-1537),
-//                      a sequential recurrence evaluated by one warp in site order
+//                      a serial recurrence, replayed on the host in site order
+//                      (float_mean_serial)
 //   field_add / field_zero_above   element-wise updates
 // Sums are formed in a fixed order (block trees, then CTA partials summed on
 // the host in CTA order).  Compiled with -fmad=false.
@@ -129,25 +130,6 @@ __global__ void __launch_bounds__(kThreads) k_phiref(const double* __restrict__ 
     }
 }
 
-// Nmean = (float)((double)Nmean + deltaN[id]) in site order over sites with
-// deltaN <= cutoff, then Nmean / (float)N^3 (src/output.cpp:1527-1537).  One
-// warp: lanes load 32 consecutive sites, every lane replays the recurrence.
-__global__ void k_saveN_mean(const double* __restrict__ dn, long long gs, double cutoff, float* out) {
-    const int lane = threadIdx.x & 31;
-    float m = 0.f;
-    for (long long base = 0; base < gs; base += 32) {
-        const long long id = base + lane;
-        const double v = id < gs ? dn[id] : 0.0;
-#pragma unroll 8
-        for (int q = 0; q < 32; ++q) {
-            const double x = __shfl_sync(0xffffffffu, v, q);
-            if (base + q < gs && x <= cutoff) m = (float)((double)m + x);
-        }
-    }
-    m = m / (float)gs;
-    if (lane == 0) *out = m;
-}
-
 __global__ void k_add(double* x, long long gs, double v) {
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id < gs) x[id] = x[id] + v;
@@ -244,10 +226,10 @@ int get_phiref(iegpu_ctx* c, double* out) {
 }
 
 int saveN_mean(iegpu_ctx* c, double cutoff, float* out) {
-    float* d = reinterpret_cast<float*>(c->misc);
-    k_saveN_mean<<<1, 32, 0, c->stream>>>(c->dn, (long long)c->gs, cutoff, d);
-    c->launches++;
-    return fetch(c, out, d, sizeof(float), "saveN mean");
+    std::vector<double> x(c->gs);
+    if (fetch(c, x.data(), c->dn, sizeof(double) * c->gs, "saveN mean")) return IEGPU_ECUDA;
+    *out = float_mean_serial(x.data(), (long long)c->gs, cutoff);
+    return IEGPU_OK;
 }
 
 int field_add(iegpu_ctx* c, int field, double v) {
