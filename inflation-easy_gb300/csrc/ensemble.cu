@@ -186,8 +186,9 @@ static int ens_prime_slots(const iegpu_ens* e, int N) {
 }
 
 // Launch shapes, as in the one-lattice form: TJ rows per tile (4 or 8) with
-// PF = 1 or 2 planes prefetched, or TJ = N (N = 32, 64) for whole planes with
-// PF = 2 or 4.
+// PF = 1 or 2 planes prefetched (4-row tiles at N >= 128 also 3 or 4), 16-row
+// tiles at 128 <= N <= 256 with PF = 1 to 3, or TJ = N (N = 32, 64) for whole
+// planes with PF = 2 or 4.
 static bool ens_plane(int N, int TJ) { return TJ == N && (N == 32 || N == 64); }
 static int ens_threads(int N, int TJ) {
     return ens_plane(N, TJ) ? (N == 32 ? 256 : 512) : N >= 128 ? row4_threads(TJ) : (TJ + 1) * 32;
@@ -202,6 +203,7 @@ static bool ens_shape_ok(int N, int TJ, int PF, int chunks) {
     if (chunks < 1 || chunks > N / 8) return false;
     if (ens_plane(N, TJ)) return PF == 2 || PF == 4;
     const bool deep = TJ == 4 && N >= 128 && (PF == 3 || PF == 4);
+    if (TJ == 16) return N >= 128 && N <= 256 && PF >= 1 && PF <= 3 && ens_smem(N, TJ, PF) <= 227 * 1024;
     return (TJ == 4 || TJ == 8) && (PF == 1 || PF == 2 || deep) && ens_smem(N, TJ, PF) <= 227 * 1024;
 }
 
@@ -238,6 +240,10 @@ static int ens_launch_class(iegpu_ens* e, const EnsClass& c, const EnsArgs& A, c
             else if (PF == 2) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 2>));
             else if (PF == 3) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 3>));
             else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 4, 4>));
+        } else if (TJ == 16) {
+            if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 16, 1>));
+            else if (PF == 2) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 16, 2>));
+            else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 16, 3>));
         } else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 1, 8, 2>)); }
     } else {
         if (TJ == 4) {
@@ -245,6 +251,10 @@ static int ens_launch_class(iegpu_ens* e, const EnsClass& c, const EnsArgs& A, c
             else if (PF == 2) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 2>));
             else if (PF == 3) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 3>));
             else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 4, 4>));
+        } else if (TJ == 16) {
+            if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 16, 1>));
+            else if (PF == 2) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 16, 2>));
+            else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 16, 3>));
         } else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows4<TAB, 2, 8, 2>)); }
     }
 #undef IEGPU_ENS_PICK
@@ -514,6 +524,8 @@ static std::vector<int3> ens_candidates(const iegpu_ens* e, int N, int nlat) {
             const int per_lat = N / TJ;
             for (int waves : {1, 2}) add(TJ, PF, (waves * 3 * e->sms) / (per_lat * (nlat > 0 ? nlat : 1)));
         }
+    // 16-row tiles are accepted by iegpu_ens_set_shape but not tuned over: for
+    // the 8 x 128^3 class they measured slower than 8-row tiles (154 vs 145 us).
     return out;
 }
 
@@ -846,8 +858,9 @@ int iegpu_ens_set_shape(iegpu_ens* e, int N, int rows, int prefetch, int chunks)
         if (c.N != N) continue;
         if (!ens_shape_ok(N, rows, prefetch, chunks))
             return ens_error(e, IEGPU_EINVAL,
-                             "shape: rows 4|8 with prefetch 1|2, or rows N (N <= 64, whole planes) with prefetch 2|4; "
-                             "1 <= chunks <= N/8");
+                             "shape: rows 4|8 with prefetch 1|2 (rows 4 and N >= 128 also 3|4), rows 16 "
+                             "(128 <= N <= 256) with prefetch 1..3, or rows N (N <= 64, whole planes) with "
+                             "prefetch 2|4; 1 <= chunks <= N/8");
         c.TJ = rows;
         c.PF = prefetch;
         c.chunks = chunks;

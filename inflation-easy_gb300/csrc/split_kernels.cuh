@@ -32,21 +32,37 @@ __device__ __forceinline__ int window_find(const float* u, int n, float v) {
     return q;
 }
 
-// The window's bracket of the background value (dphi = 0), kept in registers:
-// nearly every site of a step falls in it, so the lookup below is two
-// compares; the others walk the window.
+// The window's bracket of the background value (dphi = 0), kept in registers
+// with the bounds of its two neighbours.  Perturbations are a small fraction
+// of a bracket, so nearly every site falls in the bracket (two compares) and
+// nearly all the rest in a neighbour (two more compares and the neighbour's
+// coefficients from shared memory, the same address across most of a warp).
+// Only a site beyond the neighbours walks the window.  Any of these finds the
+// same bracket, which is unique.
 struct WinCache {
-    float hi, lo, A, s;
+    float hi, lo, A, s;   // bracket q: lo < v <= hi, value A + s v
+    float hi2, lo2;       // u[q-1] and u[q+2] (hi and lo when there is no such neighbour)
+    int q;
 };
 
 template <bool TABLE>
 __device__ __forceinline__ WinCache win_cache(const float* w, int n) {
-    WinCache c{-1.f, 1.f, 0.f, 0.f};   // empty interval
+    WinCache c{-1.f, 1.f, 0.f, 0.f, -1.f, 1.f, 0};   // empty interval
     if (TABLE) {
         const int q = window_find(w, n, 0.f);
-        if (q >= 0) c = WinCache{w[q], w[q + 1], w[kWin + 1 + q], w[2 * kWin + 1 + q]};
+        if (q >= 0) {
+            c = WinCache{w[q], w[q + 1], w[kWin + 1 + q], w[2 * kWin + 1 + q], q > 0 ? w[q - 1] : w[q],
+                         q + 2 <= n ? w[q + 2] : w[q + 1], q};
+        }
     }
     return c;
+}
+
+// Bracket of v for a site outside the cached bracket: a neighbour, or the
+// walk; -1 outside the window.
+__device__ __forceinline__ int window_near(const float* w, int n, const WinCache& c, float v) {
+    if (v <= c.hi2 && v > c.lo2) return v > c.hi ? c.q - 1 : c.q + 1;
+    return window_find(w, n, v);
 }
 
 // potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop)
@@ -55,7 +71,7 @@ __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, cons
                                           bool& bad) {
     if (TABLE) {
         if (x <= c.hi && x > c.lo) return pn * (c.A + c.s * x);
-        const int q = window_find(wk, nk, x);
+        const int q = window_near(wk, nk, c, x);
         if (q < 0) { bad = true; return 0.f; }
         return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
     }
@@ -67,7 +83,7 @@ template <bool TABLE>
 __device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad) {
     if (TABLE) {
         if (x <= c.hi && x > c.lo) return c.A + c.s * x;
-        const int q = window_find(wv, nv, x);
+        const int q = window_near(wv, nv, c, x);
         if (q < 0) { bad = true; return 0.f; }
         return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
     }
@@ -993,7 +1009,9 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    maybe_precompute(ctl, P, K);
+    // a lattice stepped by one CTA runs its update straight after its tile:
+    // there is nothing for a precomputed part to overlap with
+    if (nslots > 1) maybe_precompute(ctl, P, K);
     df64 v[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }
@@ -1513,7 +1531,7 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
     if (bad) {
         if (atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = ctl->phibar;
     }
-    maybe_precompute(ctl, P, K);
+    if (nslots > 1) maybe_precompute(ctl, P, K);   // as in rows_body
     df64 v3[3] = {g.df(), s1.df(), s2.df()};
     finish_sums_slot(v3, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
 }

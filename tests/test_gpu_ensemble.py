@@ -22,6 +22,7 @@ SEEDS = [3, 5, 7, 9]
 # launch shapes per size (rows per tile, planes prefetched, chunks); rows = N: whole planes
 ROWS = {32: (8, 2, 1), 64: (8, 2, 2), 128: (8, 2, 4)}
 PLANES = {32: (32, 4, 2), 64: (64, 2, 4), 128: (4, 1, 8)}
+WIDE = {32: (32, 2, 1), 64: (64, 2, 2), 128: (16, 3, 2)}   # one CTA per 32^3 lattice, 16-row tiles
 
 
 def _case(usr):
@@ -77,7 +78,7 @@ def deltaN_single(engine, lat, bg, dN, Nend):
     return phiref, nmean
 
 
-@pytest.mark.parametrize("usr,shapes", [(False, ROWS), (True, ROWS), (True, PLANES)])
+@pytest.mark.parametrize("usr,shapes", [(False, ROWS), (True, ROWS), (True, PLANES), (True, WIDE), (False, WIDE)])
 def test_ensemble_matches_single_lattices(usr, shapes, engine, tables):
     w = _case(usr)
     steps = 40
