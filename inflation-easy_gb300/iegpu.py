@@ -199,9 +199,14 @@ class Lattice:
         ny = None if nyquist is None else np.ascontiguousarray(nyquist, dtype=dt)
         self._check(self.lib.iegpu_upload(self.h, field, _ptr(host, dt), None if ny is None else _ptr(ny, dt)))
 
-    def download(self, field: int, nyquist: bool = False):
+    def download(self, field: int, nyquist: bool = False, out: np.ndarray | None = None):
+        """The field as a host array; `out` (contiguous, N^3 elements of the
+        field's type) is filled and returned instead of a new array."""
         dt = np.float64 if field in (F, FD, DELTAN) else np.float32
-        out = np.empty(self.N ** 3, dtype=dt)
+        if out is None:
+            out = np.empty(self.N ** 3, dtype=dt)
+        elif out.dtype != dt or out.size != self.N ** 3 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a contiguous {dt.__name__} array of {self.N ** 3} elements")
         ny = np.empty(2 * self.N * self.N, dtype=dt) if nyquist else None
         self._check(self.lib.iegpu_download(self.h, field, _ptr(out, dt), None if ny is None else _ptr(ny, dt)))
         return (out, ny) if nyquist else out
