@@ -51,6 +51,9 @@ struct ieo_state {
     double sm_norm, sm_hbterm;
     int err;
     char errmsg[512];
+    /* RK4 scratch (allocated on first use), src/evolution.cpp:288-321 */
+    double *ftmp, *fdtmp, *kf[4], *kfd[4];
+    float *htmp[6], *hdtmp[6], *kh[4][6], *khd[4][6];
 };
 
 static inline double pw2(double x) { return x * x; }
@@ -227,6 +230,17 @@ int ieo_params_load(ieo_params* p, const char* path) {
         KD("omega", omega)
         KD("dt_post_inflation", dt_post_inflation)
         else if (!strcmp(key, "af_post_inflation") && parse_d(val, &d)) { p->af_post_inflation = d; p->af_post_given = 1; }
+        else if (!strcmp(key, "inflation_integrator")) {
+            /* parse_integrator, src/runtime_parameters.cpp:141-166 */
+            char lw[64];
+            size_t q = 0;
+            for (; val[q] && q < sizeof lw - 1; ++q) lw[q] = (char)((val[q] >= 'A' && val[q] <= 'Z') ? val[q] + 32 : val[q]);
+            lw[q] = 0;
+            if (!strcmp(lw, "leapfrog") || !strcmp(lw, "lf")) p->inflation_integrator = 0;
+            else if (!strcmp(lw, "rk4")) p->inflation_integrator = 1;
+            else if (!strcmp(lw, "rk45") || !strcmp(lw, "rkf45") || !strcmp(lw, "dopri5")) p->inflation_integrator = 2;
+            else if (parse_i(val, &i) && i >= 0 && i <= 2) p->inflation_integrator = i;
+        }
 #undef KD
 #undef KI
 #undef KB
@@ -280,6 +294,12 @@ void ieo_destroy(ieo_state* S) {
     free(S->f); free(S->fd); free(S->deltaN); free(S->fny); free(S->fdny);
     for (int c = 0; c < 6; ++c) { free(S->h[c]); free(S->hd[c]); free(S->hny[c]); free(S->hdny[c]); }
     free(S->tphi); free(S->tV); free(S->tdV); free(S->lstart);
+    free(S->ftmp); free(S->fdtmp);
+    for (int q = 0; q < 4; ++q) { free(S->kf[q]); free(S->kfd[q]); }
+    for (int c = 0; c < 6; ++c) {
+        free(S->htmp[c]); free(S->hdtmp[c]);
+        for (int q = 0; q < 4; ++q) { free(S->kh[q][c]); free(S->khd[q][c]); }
+    }
     free(S);
 }
 
@@ -836,6 +856,175 @@ void ieo_evolve_derivs_post_inflation(ieo_state* S, double d) {
         }
     }
     S->ad += 0.5 * d * S->ad2;
+}
+
+/* compute_inflation_rhs, inflation branch, src/evolution.cpp:418-512: the time
+ * derivatives of a stage state (fs, fds; hs, hds with SIGW) into kf, kfd (kh,
+ * khd), and dadt, daddt from the stage's lattice sums.  The sums run serially
+ * in loop order (the reference's OpenMP reduction with one thread); the table
+ * lookup keeps the per-site hint (evaluate_potential_from_value,
+ * src/potential.cpp:123-146). */
+static int rk_rhs(ieo_state* S, const double* fs, const double* fds, float* const* hs, float* const* hds, double* kf,
+                  double* kfd, float* const* kh, float* const* khd, double a_st, double ad_st, double* dadt,
+                  double* daddt) {
+    const ieo_params* p = &S->p;
+    const int N = p->N;
+    const double s = p->rescale_s, dx = p->dx, B2 = pw2(p->rescale_B);
+    const double laplnorm = pow(a_st, -2.0 * s) / pw2(dx);
+    const double friction = (2.0 + s) * ad_st / a_st;
+    const double potnorm = pow(a_st, 2.0 - 2.0 * s);
+    const double srcAmp = 2.0 * pow(a_st, -2.0 * s);
+    const double half_over_dx = 0.5 / dx;
+    double gradient_sum = 0.0, potential_sum = 0.0;
+    for (int i = 0; i < N; ++i) {
+        const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+        for (int j = 0; j < N; ++j) {
+            const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+            for (int k = 0; k < N; ++k) {
+                const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                const size_t id = IDX(N, i, j, k);
+                const double field = fs[id];
+                const double lap = LAPL_AT(double, fs, N, i, j, k, ip, im, jp, jm, kp, km);
+                double pot, dpot;
+                if (p->numerical_potential) {
+                    const int l = bracket(S, field, S->lstart[id]);
+                    if (l < 0) return 1;
+                    pot = interp(S, field, l, S->tV) / B2;
+                    dpot = interp(S, field, l, S->tdV) / B2;
+                    const int back = p->int_err > 1 ? p->int_err : 1;
+                    S->lstart[id] = (l - back) > 1 ? (l - back) : 1;
+                } else {
+                    pot = hill_V(p, field);
+                    dpot = hill_dV(p, field);
+                }
+                kf[id] = fds[id];
+                kfd[id] = laplnorm * lap - friction * fds[id] - potnorm * dpot;
+                gradient_sum -= field * lap;
+                potential_sum += pot;
+                if (p->calculate_SIGW) {
+                    const double gx = (fs[IDX(N, ip, j, k)] - fs[IDX(N, im, j, k)]) * half_over_dx;
+                    const double gy = (fs[IDX(N, i, jp, k)] - fs[IDX(N, i, jm, k)]) * half_over_dx;
+                    const double gz = (fs[IDX(N, i, j, kp)] - fs[IDX(N, i, j, km)]) * half_over_dx;
+                    const double T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+                    for (int c = 0; c < 6; ++c) {
+                        const float lapf = LAPL_AT(float, hs[c], N, i, j, k, ip, im, jp, jm, kp, km);
+                        kh[c][id] = hds[c][id];
+                        khd[c][id] = (float)(laplnorm * (double)lapf - friction * (double)hds[c][id] + srcAmp * T[c]);
+                    }
+                }
+            }
+        }
+    }
+    const double gradient = 0.5 * gradient_sum * pw2(1.0 / (a_st * dx)) / (double)S->gs;
+    const double potential_avg = potential_sum / (double)S->gs;
+    const double source = 2.0 * gradient / 3.0 + potential_avg;
+    *dadt = ad_st;
+    *daddt = pow(a_st, 3.0 - 2.0 * s) * source - (s + 1.0) * pw2(ad_st) / a_st;
+    return 0;
+}
+
+static const double RK4_A[4][4] = {{0.0, 0.0, 0.0, 0.0}, {0.5, 0.0, 0.0, 0.0}, {0.0, 0.5, 0.0, 0.0}, {0.0, 0.0, 1.0, 0.0}};
+static const double RK4_B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+
+static void rk_scratch(ieo_state* S) {
+    if (S->ftmp) return;
+    const size_t gs = S->gs;
+    S->ftmp = (double*)calloc(gs, sizeof(double));
+    S->fdtmp = (double*)calloc(gs, sizeof(double));
+    for (int q = 0; q < 4; ++q) {
+        S->kf[q] = (double*)calloc(gs, sizeof(double));
+        S->kfd[q] = (double*)calloc(gs, sizeof(double));
+    }
+    if (S->p.calculate_SIGW)
+        for (int c = 0; c < 6; ++c) {
+            S->htmp[c] = (float*)calloc(gs, sizeof(float));
+            S->hdtmp[c] = (float*)calloc(gs, sizeof(float));
+            for (int q = 0; q < 4; ++q) {
+                S->kh[q][c] = (float*)calloc(gs, sizeof(float));
+                S->khd[q][c] = (float*)calloc(gs, sizeof(float));
+            }
+        }
+}
+
+/* rk4_step_inflation(h), src/evolution.cpp:760-779, with the stage states of
+ * prepare_inflation_stage_state (:641-671), the background stages of
+ * prepare_inflation_background_state (:673-690) and the update of
+ * apply_inflation_weighted_update (:717-758).  ad2 is not touched. */
+int ieo_rk4_step_inflation(ieo_state* S, double h) {
+    rk_scratch(S);
+    const size_t gs = S->gs;
+    const int sigw = S->p.calculate_SIGW;
+    double ka[4] = {0.0, 0.0, 0.0, 0.0}, kad[4] = {0.0, 0.0, 0.0, 0.0};
+    if (rk_rhs(S, S->f, S->fd, S->h, S->hd, S->kf[0], S->kfd[0], S->kh[0], S->khd[0], S->a, S->ad, &ka[0], &kad[0]))
+        return 1;
+    for (int stage = 1; stage < 4; ++stage) {
+        for (size_t id = 0; id < gs; ++id) {
+            double sum_f = 0.0, sum_fd = 0.0;
+            for (int q = 0; q < stage; ++q) {
+                const double c = RK4_A[stage][q];
+                if (c == 0.0) continue;
+                sum_f += c * S->kf[q][id];
+                sum_fd += c * S->kfd[q][id];
+            }
+            S->ftmp[id] = S->f[id] + h * sum_f;
+            S->fdtmp[id] = S->fd[id] + h * sum_fd;
+        }
+        if (sigw)
+            for (int c = 0; c < 6; ++c)
+                for (size_t id = 0; id < gs; ++id) {
+                    double sum_h = 0.0, sum_hd = 0.0;
+                    for (int q = 0; q < stage; ++q) {
+                        const double cs = RK4_A[stage][q];
+                        if (cs == 0.0) continue;
+                        sum_h += cs * (double)S->kh[q][c][id];
+                        sum_hd += cs * (double)S->khd[q][c][id];
+                    }
+                    S->htmp[c][id] = (float)((double)S->h[c][id] + h * sum_h);
+                    S->hdtmp[c][id] = (float)((double)S->hd[c][id] + h * sum_hd);
+                }
+        double a_st = S->a, ad_st = S->ad;
+        for (int q = 0; q < stage; ++q) {
+            const double c = RK4_A[stage][q];
+            if (c == 0.0) continue;
+            a_st += h * c * ka[q];
+            ad_st += h * c * kad[q];
+        }
+        if (rk_rhs(S, S->ftmp, S->fdtmp, S->htmp, S->hdtmp, S->kf[stage], S->kfd[stage], S->kh[stage], S->khd[stage],
+                   a_st, ad_st, &ka[stage], &kad[stage]))
+            return 1;
+    }
+    for (size_t id = 0; id < gs; ++id) {
+        double sum_f = 0.0, sum_fd = 0.0;
+        for (int q = 0; q < 4; ++q) {
+            const double bs = RK4_B[q];
+            if (bs == 0.0) continue;
+            sum_f += bs * S->kf[q][id];
+            sum_fd += bs * S->kfd[q][id];
+        }
+        S->f[id] += h * sum_f;
+        S->fd[id] += h * sum_fd;
+    }
+    if (sigw)
+        for (int c = 0; c < 6; ++c)
+            for (size_t id = 0; id < gs; ++id) {
+                double sum_h = 0.0, sum_hd = 0.0;
+                for (int q = 0; q < 4; ++q) {
+                    const double bs = RK4_B[q];
+                    if (bs == 0.0) continue;
+                    sum_h += bs * (double)S->kh[q][c][id];
+                    sum_hd += bs * (double)S->khd[q][c][id];
+                }
+                S->h[c][id] = (float)((double)S->h[c][id] + h * sum_h);
+                S->hd[c][id] = (float)((double)S->hd[c][id] + h * sum_hd);
+            }
+    for (int q = 0; q < 4; ++q) {
+        const double bs = RK4_B[q];
+        if (bs == 0.0) continue;
+        S->a += h * bs * ka[q];
+        S->ad += h * bs * kad[q];
+    }
+    S->t += h;
+    return 0;
 }
 
 /* inflation_rescaled_step, src/evolution.cpp:338-340 */
@@ -1407,7 +1596,9 @@ static int out_save(ieo_state* S, outfiles* O, int infrequent) {
     const ieo_params* p = &S->p;
     if (g_trace)
         fprintf(g_trace, "save %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, S->t, S->a, S->ad, S->ad2, S->astep);
-    if (S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt * pow(S->astep, p->rescale_s - 1));
+    /* the half-step sync is the leapfrog's (inflation_uses_staggered_derivatives, src/main.h:184-186) */
+    const int stag = p->inflation_integrator == 0;
+    if (stag && S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt * pow(S->astep, p->rescale_s - 1));
     if (out_meansvars(S, O, 0)) return 1;
     out_scale(S, O, 0);
     if (infrequent) {
@@ -1447,7 +1638,7 @@ static int out_save(ieo_state* S, outfiles* O, int infrequent) {
             out_histogram(S, S->f, open_out(S, O, &O->histogram, "histogram"),
                           open_out(S, O, &O->histogramtimes, "histogramtimes"), 0);
     }
-    if (S->t > 0.) ieo_evolve_fields(S, .5 * p->dt * pow(S->astep, p->rescale_s - 1));
+    if (stag && S->t > 0.) ieo_evolve_fields(S, .5 * p->dt * pow(S->astep, p->rescale_s - 1));
     return S->err;
 }
 
@@ -1659,14 +1850,23 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
     if (out_save(S, &O, 1)) goto done;
     S->t = S->t0;
 
-    /* run_evolution_loop(), leapfrog branch, src/evolution.cpp:909-997 */
+    /* run_evolution_loop(), leapfrog and RK4 branches, src/evolution.cpp:909-997 */
+    if (p->inflation_integrator == 2) {
+        set_err(S, "the rk45 inflation integrator is not restated by this oracle\n");
+        goto done;
+    }
     {
         int numsteps = 0;
-        ieo_evolve_fields(S, 0.5 * p->dt);
+        const int leap = p->inflation_integrator == 0;
+        if (leap) ieo_evolve_fields(S, 0.5 * p->dt);
         while (S->a <= p->af) {
             const double d = ieo_rescaled_step(S, S->astep);
-            if (ieo_evolve_derivs(S, d)) goto done;
-            ieo_evolve_fields(S, d);
+            if (leap) {
+                if (ieo_evolve_derivs(S, d)) goto done;
+                ieo_evolve_fields(S, d);
+            } else if (ieo_rk4_step_inflation(S, d)) {
+                goto done;
+            }
             numsteps++;
             if (numsteps % p->output_freq == 0 && S->a < p->af)
                 if (out_save(S, &O, (numsteps % p->output_infrequent_freq == 0) ? 1 : 0)) goto done;
@@ -1677,7 +1877,7 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
         }
         fflush(O.output);
         if (out_save(S, &O, 1)) goto done;
-        ieo_evolve_fields(S, -0.5 * ieo_rescaled_step(S, S->astep));
+        if (leap) ieo_evolve_fields(S, -0.5 * ieo_rescaled_step(S, S->astep));
         out_modes(S, &O);
     }
 

@@ -50,6 +50,8 @@ typedef struct {
     /* post-inflation phase (src/parameters.h:31 switch, src/runtime_parameters.cpp:48-52, 295-299) */
     int post_inflation, af_post_given;
     double horizon_factor, omega, dt_post_inflation, af_post_inflation;
+    /* inflation_integrator, src/runtime_parameters.cpp:141-166: 0 leapfrog, 1 rk4 (2 rk45 is not restated) */
+    int inflation_integrator, pad_;
 } ieo_params;
 
 typedef struct ieo_state ieo_state;
@@ -109,6 +111,11 @@ double ieo_rescaled_step(const ieo_state* S, double astep);
  * src/evolution.cpp:937-945 without output; stops early once a > af.
  * Returns the number of steps taken (or -1 on error). */
 int ieo_leapfrog_steps(ieo_state* S, int nsteps);
+
+/* ---- RK4 inflation step: rk4_step_inflation(h), src/evolution.cpp:760-779, with
+ * compute_inflation_rhs (:418-512); the RHS sums are serial in loop order, which is
+ * what the reference's OpenMP reduction gives with one thread. ---- */
+int ieo_rk4_step_inflation(ieo_state* S, double h);
 
 /* ---- post-inflation phase: src/initialize.cpp:245-290, src/evolution.cpp:1378-1653 ---- */
 void ieo_initialize_post_inflation(ieo_state* S);

@@ -45,7 +45,8 @@ class Params(C.Structure):
                 ("output_box3D", C.c_int), ("output_box2D", C.c_int), ("screen_updates", C.c_int),
                 ("nbins", C.c_int), ("int_err", C.c_int), ("int_errN", C.c_int), ("dx", C.c_double),
                 ("post_inflation", C.c_int), ("af_post_given", C.c_int), ("horizon_factor", C.c_double),
-                ("omega", C.c_double), ("dt_post_inflation", C.c_double), ("af_post_inflation", C.c_double)]
+                ("omega", C.c_double), ("dt_post_inflation", C.c_double), ("af_post_inflation", C.c_double),
+                ("inflation_integrator", C.c_int), ("pad_", C.c_int)]
 
 
 class Scalars(C.Structure):
@@ -83,6 +84,7 @@ def load() -> C.CDLL:
         "ieo_gradient_energy": (D, [P]), "ieo_kin_energy": (D, [P]),
         "ieo_evolve_derivs": (I, [P, D]), "ieo_evolve_fields": (None, [P, D]),
         "ieo_initialize_post_inflation": (None, [P]), "ieo_evolve_derivs_post_inflation": (None, [P, D]),
+        "ieo_rk4_step_inflation": (I, [P, D]),
         "ieo_rescaled_step": (D, [P, D]), "ieo_leapfrog_steps": (I, [P, I]),
         "ieo_fftrn_d": (None, [dp, dp, I, I]), "ieo_fftrn_f": (None, [fp, fp, I, I]),
         "ieo_numbins": (I, [I]),
@@ -223,6 +225,9 @@ class Oracle:
     def evolve_derivs(self, d):
         self._check(self.lib.ieo_evolve_derivs(self.h, d))
 
+    def rk4_step_inflation(self, h):
+        self._check(self.lib.ieo_rk4_step_inflation(self.h, h))
+
     def initialize_post_inflation(self):
         self.lib.ieo_initialize_post_inflation(self.h)
 
@@ -335,6 +340,11 @@ def params_from_text(text: str, N: int, numerical: bool, sigw: bool, deltaN: boo
             continue
         k, v = (x.strip() for x in line.split("=", 1))
         if k in ("output_bispectrum", "output_LOG"):
+            continue
+        if k == "inflation_integrator":
+            kw[k] = {"leapfrog": 0, "lf": 0, "rk4": 1, "rk45": 2, "rkf45": 2, "dopri5": 2}.get(v.lower(), 0)
+            continue
+        if k.endswith("_integrator"):
             continue
         kw[k] = float(v) if any(ch in v for ch in ".eE") else int(v)
     kw["calculate_SIGW"] = int(sigw)

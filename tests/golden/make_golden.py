@@ -43,6 +43,7 @@ CASES = {
     "n16_usr_sigw": (16, 1, 1, 1, 0, USR),
     "n32_hilltop": (32, 0, 0, 1, 0, HILLTOP),
     "n16_usr_sigw_post": (16, 1, 1, 1, 1, USR),
+    "n16_hilltop_rk4": (16, 0, 0, 1, 0, dict(HILLTOP, inflation_integrator="rk4")),
 }
 
 
@@ -83,7 +84,10 @@ def main() -> None:
         work.mkdir(parents=True)
         (work / "params.txt").write_text(params_text(p))
         os.symlink(HERE / "inputs", work / "inputs")
-        subprocess.run([str(exe), str(work)], check=True, stdout=subprocess.DEVNULL)
+        # the RK right-hand side sums with an OpenMP reduction, whose order follows
+        # the thread count: one thread gives the serial loop order
+        env = dict(os.environ, OMP_NUM_THREADS="1") if "inflation_integrator" in p else None
+        subprocess.run([str(exe), str(work)], check=True, stdout=subprocess.DEVNULL, env=env)
         dst = HERE / name
         if dst.exists():
             shutil.rmtree(dst)

@@ -18,6 +18,7 @@ CASES = {
     "n16_usr_sigw": (16, True, True, False),
     "n32_hilltop": (32, False, False, False),
     "n16_usr_sigw_post": (16, True, True, True),
+    "n16_hilltop_rk4": (16, False, False, False),
 }
 
 

@@ -30,6 +30,7 @@ CASES = [
     (16, True, False, False, USR),
     (32, True, True, False, USR),
     (16, False, True, True, HILL),
+    (16, True, True, False, USR + "inflation_integrator = rk4\n"),
 ]
 
 
@@ -40,7 +41,10 @@ def test_oracle_matches_reference(N, numerical, sigw, post, text, oracle_mod, tm
     wd.mkdir()
     (wd / "params.txt").write_text(text)
     os.symlink(INPUTS, wd / "inputs")
-    subprocess.run([str(exe), str(wd)], check=True, stdout=subprocess.DEVNULL)
+    # the RK right-hand side sums with an OpenMP reduction, whose order follows
+    # the thread count; one thread gives the serial loop order the oracle uses
+    env = dict(os.environ, OMP_NUM_THREADS="1") if "integrator" in text else None
+    subprocess.run([str(exe), str(wd)], check=True, stdout=subprocess.DEVNULL, env=env)
     p = oracle_mod.params_from_text(text, N, numerical, sigw, post=post)
     assert oracle_mod.run_program(p, tmp_path / "results", INPUTS, tmp_path) == 0
     for f in sorted((wd / "results").rglob("*")):
