@@ -133,6 +133,20 @@ int  iegpu_evolve_derivs(struct iegpu_ctx* ctx, double d, iegpu_bg* bg);
  * and then sets bg->astep = bg->a before the next call. */
 int  iegpu_leapfrog(struct iegpu_ctx* ctx, double af, int max_steps, iegpu_bg* bg,
                     int* steps_taken, double* a_trace);
+/* rk4_step_inflation(h), src/evolution.cpp:760-779 (inflation_integrator =
+ * rk4; plain FP64 form): four evaluations of compute_inflation_rhs
+ * (:418-512) on the stage states of :641-690, then the weighted update of
+ * f, fd (h, hd with SIGW) and of a, ad (:717-758), and t += h.  ad2 is not
+ * touched.  The stage's lattice sums are combined on the device in a fixed
+ * order, so a, ad agree with the reference to rounding of those sums; every
+ * per-site expression is the reference's. */
+int  iegpu_rk4_step_inflation(struct iegpu_ctx* ctx, double h, iegpu_bg* bg);
+/* The RK4 branch of run_evolution_loop, src/evolution.cpp:948-956: as
+ * iegpu_leapfrog (same stepping, a_trace and "astep = a" contract), with
+ * rk4_step_inflation(dt*astep^(s-1)) as the step.  No half drift precedes
+ * or follows the loop for this integrator. */
+int  iegpu_rk4(struct iegpu_ctx* ctx, double af, int max_steps, iegpu_bg* bg,
+               int* steps_taken, double* a_trace);
 /* kin_energy(), gradient_energy(), potential_energy():
  * src/evolution.cpp:130-145, src/potential.cpp:151-171.  out[3] = {kin, grad, pot}. */
 int  iegpu_energies(struct iegpu_ctx* ctx, const iegpu_bg* bg, double out[3]);

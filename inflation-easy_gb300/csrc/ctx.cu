@@ -106,6 +106,7 @@ static void free_all(iegpu_ctx* c) {
     for (int q = 0; q < 6; ++q) {
         cudaFree(c->h[0][q]); cudaFree(c->h[1][q]); cudaFree(c->hd[q]); cudaFree(c->hny[q]); cudaFree(c->hdny[q]);
     }
+    cudaFree(c->rk_d); cudaFree(c->rk_h);
     cudaFree(c->tab); cudaFree(c->tkey);
     cudaFree(c->ctl); cudaFree(c->part); cudaFree(c->counter); cudaFree(c->a_trace);
     cudaFree(c->spec_part); cudaFree(c->spec_cnt); cudaFree(c->misc);
@@ -537,6 +538,27 @@ int iegpu_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     if (!c) return IEGPU_EINVAL;
     if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "the launch shape belongs to the split form");
     return split_set_shape(c, rows, prefetch, chunks);
+}
+
+// The RK4 integrator runs on the plain FP64 state (the split form's step is
+// the leapfrog).
+static int rk_ok(iegpu_ctx* c) {
+    if (is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "the rk4 integrator runs on the plain FP64 form");
+    return need_table(c);
+}
+
+int iegpu_rk4_step_inflation(iegpu_ctx* c, double h, iegpu_bg* bg) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (int rc = rk_ok(c)) return rc;
+    return fp64_rk4_step(c, h, bg);
+}
+
+int iegpu_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps_taken, double* a_trace) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (steps_taken) *steps_taken = 0;
+    if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
+    if (int rc = rk_ok(c)) return rc;
+    return fp64_rk4(c, af, max_steps, bg, steps_taken, a_trace);
 }
 
 // The post-inflation phase runs on the plain FP64 state with SIGW on, as

@@ -192,6 +192,10 @@ struct iegpu_ctx {
     float* hd[6] = {};
     float* hny[6] = {};
     float* hdny[6] = {};
+    // RK4 scratch, allocated on the first RK4 step: stage f, fd, k_fd
+    // (doubles) and stage h, hd, k_hd (floats, SIGW)
+    double* rk_d = nullptr;
+    float* rk_h = nullptr;
 
     // table (device copies, plus the host copy for scalar evaluations)
     std::vector<double> htab_x, htab_V, htab_dV;
@@ -279,6 +283,8 @@ int fp64_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* ste
 int fp64_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg);
 int fp64_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
 int fp64_post_init(iegpu_ctx* c, double horizon_factor, double omega, int from_deltaN, iegpu_bg* bg);
+int fp64_rk4_step(iegpu_ctx* c, double h, iegpu_bg* bg);
+int fp64_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace);
 int fp64_post_derivs(iegpu_ctx* c, double d, double omega, iegpu_bg* bg);
 int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg,
                        int* steps, double* a_trace);

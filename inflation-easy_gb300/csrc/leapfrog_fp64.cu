@@ -685,3 +685,331 @@ int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omeg
 }
 
 }  // namespace iegpu
+
+namespace iegpu {
+
+// ---------------------------------------------------------------------------
+// RK4 inflation integrator: rk4_step_inflation, src/evolution.cpp:760-779,
+// with compute_inflation_rhs (:418-512), the stage states of
+// prepare_inflation_stage_state (:641-671), the background stages of
+// prepare_inflation_background_state (:673-690) and the weighted update of
+// apply_inflation_weighted_update (:717-758).
+// ---------------------------------------------------------------------------
+//
+// A stage's derivatives are k_f = fd and k_fd = laplnorm lapl(f) - friction fd
+// - potnorm V'(f) (k_h = hd, k_hd = (float)(laplnorm lapl(h) - friction hd +
+// srcAmp T) with SIGW).  k_f of a stage is that stage's fd, so it is read from
+// the stage state instead of being stored.  Scratch per site, in doubles: f of
+// the current stage, fd of stages 1-3 and k_fd of stages 0-3; with SIGW, in
+// floats: h of the current stage (6), hd of stages 1-3 (18) and k_hd of
+// stages 0-3 (24).  The background stages need each stage's two lattice sums,
+// so they are formed on the host with the reference's expressions: one
+// 16-byte read-back per stage.
+
+struct RkSigw {
+    const float* hs[6];
+    const float* hds[6];
+    float* khd[6];
+};
+
+struct RkCoef {
+    double laplnorm, friction, potnorm, srcAmp, half_over_dx;
+};
+
+// compute_inflation_rhs on one stage state: k_fd (and k_hd) per site, and the
+// sums of f lapl(f) and V(f); the last CTA combines the block partials in a
+// fixed order into sums[0..1].
+template <bool TABLE, bool SIGW>
+__global__ void __launch_bounds__(kThreads) k_rk_rhs(const double* __restrict__ fs, const double* __restrict__ fds,
+                                                     double* __restrict__ kfd, RkSigw sg, PotDev P, DevCtl* ctl,
+                                                     double* part, unsigned* counter, double* sums, int lg, RkCoef K) {
+    const long long gs = 1LL << (3 * lg);
+    double v[2] = {0.0, 0.0};
+    for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
+        const Nbr n = neighbours(id, lg);
+        const double field = __ldg(&fs[id]);
+        const double lap = lapl7(fs, n, field);
+        double pot, dpot;
+        if (TABLE) {
+            bool oor;
+            const int l = table_bracket(P, field, &oor);
+            if (oor) flag_error(ctl, IEGPU_ERANGE, field);
+            pot = table_interp(P, P.V, P.dyV, field, l) / P.B2;
+            dpot = table_interp(P, P.dV, P.dydV, field, l) / P.B2;
+        } else {
+            bool oor;
+            pot = V_exact<false>(P, field, &oor);
+            dpot = dV_exact<false>(P, field, &oor);
+        }
+        kfd[id] = K.laplnorm * lap - K.friction * __ldg(&fds[id]) - K.potnorm * dpot;
+        v[0] += field * lap;
+        v[1] += pot;
+        if (SIGW) {
+            const double gx = (__ldg(&fs[n.ip]) - __ldg(&fs[n.im])) * K.half_over_dx;
+            const double gy = (__ldg(&fs[n.jp]) - __ldg(&fs[n.jm])) * K.half_over_dx;
+            const double gz = (__ldg(&fs[n.kp]) - __ldg(&fs[n.km])) * K.half_over_dx;
+            const double T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const float* h = sg.hs[c];
+                const float lf = lapl7(h, n, __ldg(&h[id]));
+                sg.khd[c][id] = (float)(K.laplnorm * (double)lf - K.friction * (double)__ldg(&sg.hds[c][id]) +
+                                        K.srcAmp * T[c]);
+            }
+        }
+    }
+    block_sum<2>(v);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = v[0];
+        part[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!arrive_last(counter)) return;
+    if (threadIdx.x < 32) {
+        double tot[2];
+        sum_partials<2>(part, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            *counter = 0;
+            sums[0] = tot[0];
+            sums[1] = tot[1];
+        }
+    }
+}
+
+// One row of the tableau: out = base + h sum_q c_q k_q over the nonzero c_q,
+// the sum started from 0.0 in q order (prepare_inflation_stage_state and
+// apply_inflation_weighted_update).  out may alias base.
+struct RkRow {
+    const double* kf[4];
+    const double* kfd[4];
+    const float* kh[4][6];
+    const float* khd[4][6];
+    double c[4];
+    int nq;
+};
+
+struct RkH {
+    const float* hb[6];
+    const float* hdb[6];
+    float* ho[6];
+    float* hdo[6];
+};
+
+// Plain loads throughout: the final update writes f, fd, h and hd in place,
+// and k_f, k_h of stage 0 are fd, hd themselves (each site is read by its own
+// thread before that thread writes it).
+template <bool SIGW>
+__global__ void __launch_bounds__(kThreads) k_rk_combine(const double* f, const double* fd, double* fout,
+                                                         double* fdout, RkRow R, RkH H, double h) {
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    double sum_f = 0.0, sum_fd = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (q >= R.nq || R.c[q] == 0.0) continue;
+        sum_f += R.c[q] * R.kf[q][id];
+        sum_fd += R.c[q] * R.kfd[q][id];
+    }
+    const double fo = f[id] + h * sum_f;
+    const double fdo = fd[id] + h * sum_fd;
+    fout[id] = fo;
+    fdout[id] = fdo;
+    if (SIGW) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            double sum_h = 0.0, sum_hd = 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q >= R.nq || R.c[q] == 0.0) continue;
+                sum_h += R.c[q] * (double)R.kh[q][c][id];
+                sum_hd += R.c[q] * (double)R.khd[q][c][id];
+            }
+            const float ho = (float)((double)H.hb[c][id] + h * sum_h);
+            const float hdo = (float)((double)H.hdb[c][id] + h * sum_hd);
+            H.ho[c][id] = ho;
+            H.hdo[c][id] = hdo;
+        }
+    }
+}
+
+static const double kRk4A[4][4] = {{0.0, 0.0, 0.0, 0.0}, {0.5, 0.0, 0.0, 0.0}, {0.0, 0.5, 0.0, 0.0}, {0.0, 0.0, 1.0, 0.0}};
+static const double kRk4B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+
+struct RkBufs {
+    double* f;            // stage f (stages 1-3)
+    double* fd[4];        // stage fd: [0] is the state's own fd
+    double* kfd[4];
+    float* h[6];          // stage h
+    float* hd[4][6];      // stage hd: [0] is the state's own hd
+    float* khd[4][6];
+};
+
+static int rk_bufs(iegpu_ctx* c, RkBufs& B) {
+    const size_t gs = c->gs;
+    if (!c->rk_d) {
+        if (cudaMalloc(&c->rk_d, sizeof(double) * 8 * gs) != cudaSuccess) {
+            cudaGetLastError();
+            c->rk_d = nullptr;
+            return set_error(c, IEGPU_ENOMEM, "device allocation of the RK4 scratch (%zu bytes) failed", sizeof(double) * 8 * gs);
+        }
+    }
+    if (c->cfg.sigw && !c->rk_h) {
+        if (cudaMalloc(&c->rk_h, sizeof(float) * 48 * gs) != cudaSuccess) {
+            cudaGetLastError();
+            c->rk_h = nullptr;
+            return set_error(c, IEGPU_ENOMEM, "device allocation of the RK4 tensor scratch (%zu bytes) failed", sizeof(float) * 48 * gs);
+        }
+    }
+    B.f = c->rk_d;
+    B.fd[0] = c->fd;
+    for (int q = 1; q < 4; ++q) B.fd[q] = c->rk_d + q * gs;
+    for (int q = 0; q < 4; ++q) B.kfd[q] = c->rk_d + (4 + q) * gs;
+    for (int k = 0; k < 6; ++k) {
+        B.h[k] = c->cfg.sigw ? c->rk_h + k * gs : nullptr;
+        B.hd[0][k] = c->hd[k];
+        for (int q = 1; q < 4; ++q) B.hd[q][k] = c->cfg.sigw ? c->rk_h + (6 + 6 * (q - 1) + k) * gs : nullptr;
+        for (int q = 0; q < 4; ++q) B.khd[q][k] = c->cfg.sigw ? c->rk_h + (24 + 6 * q + k) * gs : nullptr;
+    }
+    return IEGPU_OK;
+}
+
+// compute_inflation_rhs for one stage: launches the kernel, reads the two
+// sums back and forms dadt, daddt on the host (src/evolution.cpp:500-511).
+static int rk_rhs(iegpu_ctx* c, const double* fs, const double* fds, const float* const* hs, const float* const* hds,
+                  double* kfd, float* const* khd, double a_st, double ad_st, double* dadt, double* daddt) {
+    const double s = c->cfg.rescale_s, dx = c->cfg.L / (double)c->N;
+    RkCoef K;
+    K.laplnorm = pow(a_st, -2.0 * s) / (dx * dx);
+    K.friction = (2.0 + s) * ad_st / a_st;
+    K.potnorm = pow(a_st, 2.0 - 2.0 * s);
+    K.srcAmp = 2.0 * pow(a_st, -2.0 * s);
+    K.half_over_dx = 0.5 / dx;
+    RkSigw sg{};
+    for (int k = 0; k < 6 && c->cfg.sigw; ++k) {
+        sg.hs[k] = hs[k];
+        sg.hds[k] = hds[k];
+        sg.khd[k] = khd[k];
+    }
+    const bool tab = c->pot.table != 0, sig = c->cfg.sigw != 0;
+    const dim3 g(c->red_grid), b(kThreads);
+    if (tab && sig) k_rk_rhs<true, true><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
+    else if (tab) k_rk_rhs<true, false><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
+    else if (sig) k_rk_rhs<false, true><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
+    else k_rk_rhs<false, false><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
+    c->launches++;
+    if (check_cuda(c, cudaMemcpyAsync(c->misc_h, c->misc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "RK4 sums"))
+        return IEGPU_ECUDA;
+    if (check_cuda(c, cudaMemcpyAsync(&c->ctl_h->error, &c->ctl->error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "RK4 status"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "RK4 stage")) return IEGPU_ECUDA;
+    if (c->ctl_h->error) return read_ctl(c);
+    const double gradient_sum = -c->misc_h[0];
+    const double potential_sum = c->misc_h[1];
+    const double gsd = (double)c->gs;
+    const double gradient = 0.5 * gradient_sum * ((1.0 / (a_st * dx)) * (1.0 / (a_st * dx))) / gsd;
+    const double potential_avg = potential_sum / gsd;
+    const double source = 2.0 * gradient / 3.0 + potential_avg;
+    *dadt = ad_st;
+    *daddt = pow(a_st, 3.0 - 2.0 * s) * source - (s + 1.0) * (ad_st * ad_st) / a_st;
+    return IEGPU_OK;
+}
+
+static void rk_combine(iegpu_ctx* c, const RkBufs& B, const double* coef, int nq, const double* f, const double* fd,
+                       double* fout, double* fdout, const float* const* hb, const float* const* hdb, float* const* hout,
+                       float* const* hdout, double h) {
+    RkRow R{};
+    for (int q = 0; q < nq; ++q) {
+        R.kf[q] = B.fd[q];
+        R.kfd[q] = B.kfd[q];
+        for (int k = 0; k < 6; ++k) {
+            R.kh[q][k] = B.hd[q][k];
+            R.khd[q][k] = B.khd[q][k];
+        }
+        R.c[q] = coef[q];
+    }
+    R.nq = nq;
+    RkH H{};
+    for (int k = 0; k < 6 && c->cfg.sigw; ++k) {
+        H.hb[k] = hb[k];
+        H.hdb[k] = hdb[k];
+        H.ho[k] = hout[k];
+        H.hdo[k] = hdout[k];
+    }
+    const unsigned grid = (unsigned)(c->gs / kThreads);
+    if (c->cfg.sigw) k_rk_combine<true><<<grid, kThreads, 0, c->stream>>>(f, fd, fout, fdout, R, H, h);
+    else k_rk_combine<false><<<grid, kThreads, 0, c->stream>>>(f, fd, fout, fdout, R, H, h);
+    c->launches++;
+}
+
+// rk4_step_inflation(h): four right-hand sides, three stage states, the
+// weighted update of the lattice and of (a, ad), then t += h.  ad2 is not
+// touched.
+static int rk4_step(iegpu_ctx* c, const RkBufs& B, double h, iegpu_bg* bg) {
+    double* f = c->f[c->cur];
+    float* hcur[6] = {};
+    for (int k = 0; k < 6 && c->cfg.sigw; ++k) hcur[k] = c->h[c->cur][k];
+    double ka[4] = {0.0, 0.0, 0.0, 0.0}, kad[4] = {0.0, 0.0, 0.0, 0.0};
+    if (int rc = rk_rhs(c, f, B.fd[0], hcur, B.hd[0], B.kfd[0], B.khd[0], bg->a, bg->ad, &ka[0], &kad[0])) return rc;
+    for (int stage = 1; stage < 4; ++stage) {
+        rk_combine(c, B, kRk4A[stage], stage, f, c->fd, B.f, B.fd[stage], hcur, c->hd, B.h, B.hd[stage], h);
+        double a_st = bg->a, ad_st = bg->ad;
+        for (int q = 0; q < stage; ++q) {
+            const double cq = kRk4A[stage][q];
+            if (cq == 0.0) continue;
+            a_st += h * cq * ka[q];
+            ad_st += h * cq * kad[q];
+        }
+        if (int rc = rk_rhs(c, B.f, B.fd[stage], B.h, B.hd[stage], B.kfd[stage], B.khd[stage], a_st, ad_st, &ka[stage],
+                            &kad[stage]))
+            return rc;
+    }
+    rk_combine(c, B, kRk4B, 4, f, c->fd, f, c->fd, hcur, c->hd, hcur, c->hd, h);
+    for (int q = 0; q < 4; ++q) {
+        const double bq = kRk4B[q];
+        if (bq == 0.0) continue;
+        bg->a += h * bq * ka[q];
+        bg->ad += h * bq * kad[q];
+    }
+    bg->t += h;
+    return IEGPU_OK;
+}
+
+static int rk_begin(iegpu_ctx* c, const iegpu_bg* bg, RkBufs& B) {
+    if (int rc = rk_bufs(c, B)) return rc;
+    fill_ctl(c, bg, kModeLeapfrog);
+    c->ctl_h->st.active = 0;
+    c->ctl_h->done = 1;
+    return upload_ctl(c);
+}
+
+int fp64_rk4_step(iegpu_ctx* c, double h, iegpu_bg* bg) {
+    RkBufs B;
+    if (int rc = rk_begin(c, bg, B)) return rc;
+    if (int rc = rk4_step(c, B, h, bg)) return rc;
+    return sync_and_check(c, "RK4 step");
+}
+
+// The RK4 branch of run_evolution_loop, src/evolution.cpp:948-956: while
+// a <= af, one step of d = dt astep^(s-1), then "astep = a".  As in
+// fp64_leapfrog, the "astep = a" after the last step of a call is left to the
+// caller, who reports that step first.
+int fp64_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace) {
+    if (steps) *steps = 0;
+    RkBufs B;
+    if (int rc = rk_begin(c, bg, B)) return rc;
+    const double s = c->cfg.rescale_s;
+    int n = 0;
+    while (n < max_steps) {
+        if (n > 0) bg->astep = bg->a;
+        if (!(bg->a <= af)) break;
+        const double d = c->cfg.dt * pow(bg->astep, s - 1.0);
+        if (int rc = rk4_step(c, B, d, bg)) {
+            if (steps) *steps = n;
+            return rc;
+        }
+        if (a_trace) a_trace[n] = bg->a;
+        ++n;
+    }
+    if (steps) *steps = n;
+    return sync_and_check(c, "RK4");
+}
+
+}  // namespace iegpu

@@ -1,7 +1,8 @@
 // ie_main.cpp -- host program of the GB300 InflationEasy engine.
 //
 // The reference's driver (src/main.cpp:103-146), leapfrog loops
-// (src/evolution.cpp:909-997, 1291-1375, 1561-1653), initial conditions
+// (src/evolution.cpp:909-997, 1291-1375, 1561-1653) and the RK4 inflation
+// loop (src/evolution.cpp:948-956), initial conditions
 // (src/initialize.cpp) and output routines (src/output.cpp), with every
 // lattice operation sent through the C ABI of include/iegpu.h.  It reads
 // params.txt from the working directory and writes results/ in the
@@ -425,7 +426,10 @@ void box2d(FILE* fp, int field, double scale, bool scaled) {
 void save(int infrequent) {
     if (g_trace)
         std::fprintf(g_trace, "save %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, bg.t, bg.a, bg.ad, bg.ad2, bg.astep);
-    if (bg.t > 0.) evolve_fields(-.5 * P.dt * std::pow(bg.astep, P.rescale_s - 1));
+    // the staggered (leapfrog) state is synchronised around the outputs
+    // (src/output.cpp:1471-1472, 1501-1502); RK4 states need no sync
+    const bool sync = P.inflation_integrator == IE_LEAPFROG && bg.t > 0.;
+    if (sync) evolve_fields(-.5 * P.dt * std::pow(bg.astep, P.rescale_s - 1));
     meansvars();
     scale();
     if (infrequent) {
@@ -454,7 +458,7 @@ void save(int infrequent) {
             histogram_out(IEGPU_F, h, ht, false);
         }
     }
-    if (bg.t > 0.) evolve_fields(.5 * P.dt * std::pow(bg.astep, P.rescale_s - 1));
+    if (sync) evolve_fields(.5 * P.dt * std::pow(bg.astep, P.rescale_s - 1));
 }
 
 // get_modes, src/output.cpp:674-738
@@ -497,8 +501,10 @@ void output_parameters(bool first) {
         std::fprintf(info, "Grid size=%d^%d\n", P.N, 3);
         std::fprintf(info, "L=%f\nf0=%f\nfd0=%f\n", P.L, P.initial_field, P.initial_derivative);
         std::fprintf(info, "dt=%f, dt/dx=%f\n", P.dt, P.dt / P.dx);
-        std::fprintf(info, "inflation_integrator=leapfrog\n");
-        if (P.perform_deltaN) std::fprintf(info, "deltaN_integrator=leapfrog\n");
+        std::fprintf(info, "inflation_integrator=%s\n", ie_integrator_name(P.inflation_integrator));
+        if (P.perform_deltaN) std::fprintf(info, "deltaN_integrator=%s\n", ie_integrator_name(P.deltaN_integrator));
+        if (P.post_inflation)
+            std::fprintf(info, "post_inflation_integrator=%s\n", ie_integrator_name(P.post_inflation_integrator));
         std::fprintf(info, "rescale_s=%f\nrescale_B=%e\n", P.rescale_s, P.rescale_B);
         std::fprintf(info, "engine=iegpu %d (GB300, %s)\n", iegpu_version(), P.form ? "split FP32" : "plain FP64");
         time(&tstart);
@@ -514,17 +520,20 @@ void output_parameters(bool first) {
 
 // ---- loops ------------------------------------------------------------------
 
-// run_evolution_loop, leapfrog branch (src/evolution.cpp:909-997).  The
-// device runs the steps between two outputs in one call.
+// run_evolution_loop, leapfrog and RK4 branches (src/evolution.cpp:909-997).
+// The device runs the steps between two outputs in one call.  Only the
+// leapfrog has the half drifts before and after the loop.
 void run_evolution_loop() {
     int numsteps = 0;
-    evolve_fields(0.5 * P.dt);
+    const bool leap = P.inflation_integrator == IE_LEAPFROG;
+    if (leap) evolve_fields(0.5 * P.dt);
     std::vector<double> trace;
     while (bg.a <= P.af) {
         const int chunk = P.output_freq - numsteps % P.output_freq;
         trace.assign((size_t)chunk, 0.0);
         int taken = 0;
-        ck(iegpu_leapfrog(G, P.af, chunk, &bg, &taken, trace.data()));
+        if (leap) ck(iegpu_leapfrog(G, P.af, chunk, &bg, &taken, trace.data()));
+        else ck(iegpu_rk4(G, P.af, chunk, &bg, &taken, trace.data()));
         for (int s = 0; s < taken; ++s) {
             numsteps++;
             double a_now = trace[(size_t)s];
@@ -547,7 +556,7 @@ void run_evolution_loop() {
     std::printf("Saving final inflaton data\n");
     std::fflush(output_);
     save(1);
-    evolve_fields(-0.5 * rescaled_step(bg.astep));
+    if (leap) evolve_fields(-0.5 * rescaled_step(bg.astep));
     get_modes();
 }
 
@@ -722,14 +731,19 @@ int main(int argc, char** argv) {
     ie_params_load(P, params_path);
     if (P.seed < 1)
         std::printf("Warning: The parameter seed has been set to %d, which will result in incorrect output.\n", P.seed);
-    if (P.inflation_integrator != "leapfrog" || P.deltaN_integrator != "leapfrog")
-        fatal("Only the leapfrog integrator is provided by this engine (got %s / %s).\n",
-              P.inflation_integrator.c_str(), P.deltaN_integrator.c_str());
+    if (P.inflation_integrator == IE_RK45)
+        fatal("The rk45 inflation integrator is not provided by this engine (leapfrog and rk4 are).\n");
+    if (P.inflation_integrator == IE_RK4 && P.form != 0)
+        fatal("the rk4 inflation integrator runs on the plain FP64 form (form = fp64)\n");
+    if (P.perform_deltaN && P.deltaN_integrator != IE_LEAPFROG)
+        fatal("Only the leapfrog deltaN integrator is provided by this engine (got %s).\n",
+              ie_integrator_name(P.deltaN_integrator));
     if (P.forcing_cutoff && P.high_cutoff_index > 0) fatal("forcing_cutoff is not provided by this engine.\n");
     if (P.post_inflation && !P.calculate_SIGW) fatal("post_inflation requires calculate_SIGW = 1\n");
     if (P.post_inflation && P.form != 0) fatal("the post-inflation phase runs on the plain FP64 form (form = fp64)\n");
-    if (P.post_inflation && P.post_inflation_integrator != "leapfrog")
-        fatal("Only the leapfrog integrator is provided by this engine (got %s).\n", P.post_inflation_integrator.c_str());
+    if (P.post_inflation && P.post_inflation_integrator != IE_LEAPFROG)
+        fatal("Only the leapfrog post-inflation integrator is provided by this engine (got %s).\n",
+              ie_integrator_name(P.post_inflation_integrator));
     if (P.output_bispectrum || P.output_LOG)
         std::fprintf(stderr, "Ignoring output_bispectrum / output_LOG: not provided by this engine.\n");
     struct stat st;

@@ -63,6 +63,29 @@ static bool to_int(const std::string& v, int& out) {
     return true;
 }
 
+// parse_integrator, src/runtime_parameters.cpp:141-166: the names (any case)
+// leapfrog/lf, rk4, rk45/rkf45/dopri5, or the integer code 0-2.
+static bool parse_integrator(const std::string& raw, int& out) {
+    std::string s = raw;
+    for (char& ch : s) ch = (char)std::tolower((unsigned char)ch);
+    if (s == "leapfrog" || s == "lf") { out = IE_LEAPFROG; return true; }
+    if (s == "rk4") { out = IE_RK4; return true; }
+    if (s == "rk45" || s == "rkf45" || s == "dopri5") { out = IE_RK45; return true; }
+    int iv = 0;
+    if (to_int(s, iv) && iv >= IE_LEAPFROG && iv <= IE_RK45) { out = iv; return true; }
+    return false;
+}
+
+// integrator_name, src/runtime_parameters.cpp:367-374
+const char* ie_integrator_name(int integrator) {
+    switch (integrator) {
+        case IE_LEAPFROG: return "leapfrog";
+        case IE_RK4: return "rk4";
+        case IE_RK45: return "rk45";
+        default: return "unknown";
+    }
+}
+
 bool ie_params_load(IeParams& p, const char* path) {
     std::ifstream in(path);
     std::map<std::string, std::string> kv;
@@ -112,14 +135,23 @@ bool ie_params_load(IeParams& p, const char* path) {
         else if (k == "initial_derivative" && to_double(v, d)) p.initial_derivative = d;
         else if (k == "L" && to_double(v, d)) p.L = d;
         else if (k == "dt" && to_double(v, d)) p.dt = d;
-        else if (k == "inflation_integrator") p.inflation_integrator = v;
-        else if (k == "deltaN_integrator") p.deltaN_integrator = v;
+        else if (k == "inflation_integrator") {
+            if (!parse_integrator(v, p.inflation_integrator))
+                std::fprintf(stderr, "Ignoring invalid inflation_integrator '%s' on line %d.\n", v.c_str(), line_of[k]);
+        }
+        else if (k == "deltaN_integrator") {
+            if (!parse_integrator(v, p.deltaN_integrator))
+                std::fprintf(stderr, "Ignoring invalid deltaN_integrator '%s' on line %d.\n", v.c_str(), line_of[k]);
+        }
         else if (k == "post_inflation" && to_int(v, i)) p.post_inflation = (i != 0);
         else if (k == "horizon_factor" && to_double(v, d)) p.horizon_factor = d;
         else if (k == "omega" && to_double(v, d)) p.omega = d;
         else if (k == "dt_post_inflation" && to_double(v, d)) p.dt_post_inflation = d;
         else if (k == "af_post_inflation" && to_double(v, d)) { p.af_post_inflation = d; af_post_given = true; }
-        else if (k == "post_inflation_integrator") p.post_inflation_integrator = v;
+        else if (k == "post_inflation_integrator") {
+            if (!parse_integrator(v, p.post_inflation_integrator))
+                std::fprintf(stderr, "Ignoring invalid post_inflation_integrator '%s' on line %d.\n", v.c_str(), line_of[k]);
+        }
         else if (k.rfind("rk45_", 0) == 0) {
             // accepted for compatibility; the RK45 integrators are not part of this engine
         }

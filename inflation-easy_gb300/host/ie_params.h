@@ -10,6 +10,10 @@
 
 #include <string>
 
+// Integrators of src/parameters.h (INTEGRATOR_LEAPFROG, _RK4, _RK45).
+enum { IE_LEAPFROG = 0, IE_RK4 = 1, IE_RK45 = 2 };
+const char* ie_integrator_name(int integrator);
+
 struct IeParams {
     // compile-time switches of the reference, run-time here
     int N = 128;
@@ -51,8 +55,8 @@ struct IeParams {
     int int_err = 5;
     int int_errN = 5;
     double dx = 0.0;
-    std::string inflation_integrator = "leapfrog";
-    std::string deltaN_integrator = "leapfrog";
+    int inflation_integrator = IE_LEAPFROG;
+    int deltaN_integrator = IE_LEAPFROG;
     // post-inflation phase (src/parameters.h:31 switch, run-time here and off
     // by default; src/runtime_parameters.cpp:48-52, 295-299)
     int post_inflation = 0;
@@ -60,7 +64,7 @@ struct IeParams {
     double omega = 1.0 / 3.0;
     double dt_post_inflation = 0.001;
     double af_post_inflation = 0.0;   // 2N unless given
-    std::string post_inflation_integrator = "leapfrog";
+    int post_inflation_integrator = IE_LEAPFROG;
 };
 
 // Defaults of the reference for the given potential kind and N.

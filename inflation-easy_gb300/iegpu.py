@@ -77,6 +77,8 @@ def load() -> C.CDLL:
         "iegpu_evolve_fields": (I, [P, D, C.POINTER(Bg)]),
         "iegpu_evolve_derivs": (I, [P, D, C.POINTER(Bg)]),
         "iegpu_leapfrog": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
+        "iegpu_rk4_step_inflation": (I, [P, D, C.POINTER(Bg)]),
+        "iegpu_rk4": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
         "iegpu_energies": (I, [P, C.POINTER(Bg), dp]),
         "iegpu_means": (I, [P, dp]),
         "iegpu_bunch_davies": (I, [P, I, D, D, D, D, dp]),
@@ -232,6 +234,16 @@ class Lattice:
         tr = np.zeros(max(1, max_steps), dtype=np.float64) if trace else None
         self._check(self.lib.iegpu_leapfrog(self.h, af, max_steps, C.byref(bg), C.byref(steps),
                                             None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
+        return (steps.value, tr[:steps.value]) if trace else steps.value
+
+    def rk4_step_inflation(self, h: float, bg: Bg) -> None:
+        self._check(self.lib.iegpu_rk4_step_inflation(self.h, h, C.byref(bg)))
+
+    def rk4(self, af: float, max_steps: int, bg: Bg, trace: bool = False):
+        steps = C.c_int(0)
+        tr = np.zeros(max(1, max_steps), dtype=np.float64) if trace else None
+        self._check(self.lib.iegpu_rk4(self.h, af, max_steps, C.byref(bg), C.byref(steps),
+                                       None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
         return (steps.value, tr[:steps.value]) if trace else steps.value
 
     def energies(self, bg: Bg):

@@ -26,6 +26,7 @@ MAIN = PKG / "_build" / "ie_gpu_main"
 
 CASES = {
     "n16_hilltop": (16, 0, 0),
+    "n16_hilltop_rk4": (16, 0, 0),   # inflation_integrator = rk4
     "n16_usr_sigw": (16, 1, 1),
     "n32_hilltop": (32, 0, 0),
 }
