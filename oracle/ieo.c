@@ -51,9 +51,11 @@ struct ieo_state {
     double sm_norm, sm_hbterm;
     int err;
     char errmsg[512];
-    /* RK4 scratch (allocated on first use), src/evolution.cpp:288-321 */
-    double *ftmp, *fdtmp, *kf[4], *kfd[4];
-    float *htmp[6], *hdtmp[6], *kh[4][6], *khd[4][6];
+    /* RK scratch (allocated on first use), src/evolution.cpp:288-321 */
+    double *ftmp, *fdtmp, *kf[7], *kfd[7];
+    float *htmp[6], *hdtmp[6], *kh[7][6], *khd[7][6];
+    int rk_post;        /* post-inflation right-hand side (g_use_post_inflation_rhs) */
+    double rk45_err;    /* error norm of the last RK45 attempt */
 };
 
 static inline double pw2(double x) { return x * x; }
@@ -114,6 +116,16 @@ void ieo_params_defaults(ieo_params* p, int N, int numerical) {
     p->dt_post_inflation = 0.001;
     p->af_post_inflation = 2.0 * N;
     p->af_post_given = 0;
+    p->inflation_integrator = 0;
+    p->post_inflation_integrator = 0;
+    p->deltaN_integrator = 0;
+    p->rk45_abs_tol = 1e-8;
+    p->rk45_rel_tol = 1e-6;
+    p->rk45_min_dt = -1.0;
+    p->rk45_max_dt = -1.0;
+    p->rk45_safety = 0.9;
+    p->rk45_min_given = 0;
+    p->rk45_max_given = 0;
     p->high_cutoff_index = 0.0;
     p->low_cutoff_index = 0.0;
     p->forcing_cutoff = 0;
@@ -135,6 +147,31 @@ void ieo_params_finalize(ieo_params* p, int rescale_B_given, int af_given) {
     if (!af_given) p->af = 2.0 * p->N;
     if (!p->af_post_given) p->af_post_inflation = 2.0 * p->N;
     p->dx = p->L / (double)p->N;
+    /* src/runtime_parameters.cpp:351-353 and sanitize_rk45_controls (:184-192) */
+    if (!p->rk45_min_given || p->rk45_min_dt <= 0.0) p->rk45_min_dt = fabs(p->dt) * 1e-6;
+    if (!p->rk45_max_given || p->rk45_max_dt <= 0.0) p->rk45_max_dt = fabs(p->dt);
+    if (!(p->rk45_min_dt > 0.0)) p->rk45_min_dt = fabs(p->dt) * 1e-6;
+    if (!(p->rk45_max_dt > 0.0)) p->rk45_max_dt = fabs(p->dt);
+    if (p->rk45_min_dt <= 0.0) p->rk45_min_dt = 1e-16;
+    if (p->rk45_max_dt < p->rk45_min_dt) p->rk45_max_dt = p->rk45_min_dt;
+    if (!(p->rk45_abs_tol > 0.0)) p->rk45_abs_tol = 1e-8;
+    if (!(p->rk45_rel_tol > 0.0)) p->rk45_rel_tol = 1e-6;
+    if (!(p->rk45_safety > 0.0 && p->rk45_safety < 1.0)) p->rk45_safety = 0.9;
+}
+
+/* parse_integrator, src/runtime_parameters.cpp:141-166 */
+static int parse_integrator(const char* val, int* out) {
+    char lw[64];
+    size_t q = 0;
+    for (; val[q] && q < sizeof lw - 1; ++q) lw[q] = (char)((val[q] >= 'A' && val[q] <= 'Z') ? val[q] + 32 : val[q]);
+    lw[q] = 0;
+    if (!strcmp(lw, "leapfrog") || !strcmp(lw, "lf")) { *out = 0; return 1; }
+    if (!strcmp(lw, "rk4")) { *out = 1; return 1; }
+    if (!strcmp(lw, "rk45") || !strcmp(lw, "rkf45") || !strcmp(lw, "dopri5")) { *out = 2; return 1; }
+    char* end;
+    const long v = strtol(val, &end, 10);
+    if (end != val && !*end && v >= 0 && v <= 2) { *out = (int)v; return 1; }
+    return 0;
 }
 
 static char* trim(char* s) {
@@ -230,17 +267,14 @@ int ieo_params_load(ieo_params* p, const char* path) {
         KD("omega", omega)
         KD("dt_post_inflation", dt_post_inflation)
         else if (!strcmp(key, "af_post_inflation") && parse_d(val, &d)) { p->af_post_inflation = d; p->af_post_given = 1; }
-        else if (!strcmp(key, "inflation_integrator")) {
-            /* parse_integrator, src/runtime_parameters.cpp:141-166 */
-            char lw[64];
-            size_t q = 0;
-            for (; val[q] && q < sizeof lw - 1; ++q) lw[q] = (char)((val[q] >= 'A' && val[q] <= 'Z') ? val[q] + 32 : val[q]);
-            lw[q] = 0;
-            if (!strcmp(lw, "leapfrog") || !strcmp(lw, "lf")) p->inflation_integrator = 0;
-            else if (!strcmp(lw, "rk4")) p->inflation_integrator = 1;
-            else if (!strcmp(lw, "rk45") || !strcmp(lw, "rkf45") || !strcmp(lw, "dopri5")) p->inflation_integrator = 2;
-            else if (parse_i(val, &i) && i >= 0 && i <= 2) p->inflation_integrator = i;
-        }
+        else if (!strcmp(key, "inflation_integrator")) parse_integrator(val, &p->inflation_integrator);
+        else if (!strcmp(key, "post_inflation_integrator")) parse_integrator(val, &p->post_inflation_integrator);
+        else if (!strcmp(key, "deltaN_integrator")) parse_integrator(val, &p->deltaN_integrator);
+        KD("rk45_abs_tol", rk45_abs_tol)
+        KD("rk45_rel_tol", rk45_rel_tol)
+        else if (!strcmp(key, "rk45_min_dt") && parse_d(val, &d)) { p->rk45_min_dt = d; p->rk45_min_given = 1; }
+        else if (!strcmp(key, "rk45_max_dt") && parse_d(val, &d)) { p->rk45_max_dt = d; p->rk45_max_given = 1; }
+        KD("rk45_safety", rk45_safety)
 #undef KD
 #undef KI
 #undef KB
@@ -295,10 +329,10 @@ void ieo_destroy(ieo_state* S) {
     for (int c = 0; c < 6; ++c) { free(S->h[c]); free(S->hd[c]); free(S->hny[c]); free(S->hdny[c]); }
     free(S->tphi); free(S->tV); free(S->tdV); free(S->lstart);
     free(S->ftmp); free(S->fdtmp);
-    for (int q = 0; q < 4; ++q) { free(S->kf[q]); free(S->kfd[q]); }
+    for (int q = 0; q < 7; ++q) { free(S->kf[q]); free(S->kfd[q]); }
     for (int c = 0; c < 6; ++c) {
         free(S->htmp[c]); free(S->hdtmp[c]);
-        for (int q = 0; q < 4; ++q) { free(S->kh[q][c]); free(S->khd[q][c]); }
+        for (int q = 0; q < 7; ++q) { free(S->kh[q][c]); free(S->khd[q][c]); }
     }
     free(S);
 }
@@ -858,12 +892,15 @@ void ieo_evolve_derivs_post_inflation(ieo_state* S, double d) {
     S->ad += 0.5 * d * S->ad2;
 }
 
-/* compute_inflation_rhs, inflation branch, src/evolution.cpp:418-512: the time
- * derivatives of a stage state (fs, fds; hs, hds with SIGW) into kf, kfd (kh,
- * khd), and dadt, daddt from the stage's lattice sums.  The sums run serially
- * in loop order (the reference's OpenMP reduction with one thread); the table
- * lookup keeps the per-site hint (evaluate_potential_from_value,
- * src/potential.cpp:123-146). */
+/* compute_inflation_rhs, src/evolution.cpp:418-599: the time derivatives of a
+ * stage state (fs, fds; hs, hds with SIGW) into kf, kfd (kh, khd), and dadt,
+ * daddt.  S->rk_post selects the post-inflation equations (the reference's
+ * g_use_post_inflation_rhs, set for the RK branches of
+ * run_post_inflation_loop).  Inflation: the sums run serially in loop order
+ * (the reference's OpenMP reduction with one thread); the table lookup keeps
+ * the per-site hint (evaluate_potential_from_value, src/potential.cpp:123-146).
+ * Post-inflation: no lattice sums; the tensor source is the Hessian form of
+ * build_deriv_pack with the stage's fd (src/evolution.cpp:532-595). */
 static int rk_rhs(ieo_state* S, const double* fs, const double* fds, float* const* hs, float* const* hds, double* kf,
                   double* kfd, float* const* kh, float* const* khd, double a_st, double ad_st, double* dadt,
                   double* daddt) {
@@ -871,10 +908,66 @@ static int rk_rhs(ieo_state* S, const double* fs, const double* fds, float* cons
     const int N = p->N;
     const double s = p->rescale_s, dx = p->dx, B2 = pw2(p->rescale_B);
     const double laplnorm = pow(a_st, -2.0 * s) / pw2(dx);
-    const double friction = (2.0 + s) * ad_st / a_st;
-    const double potnorm = pow(a_st, 2.0 - 2.0 * s);
     const double srcAmp = 2.0 * pow(a_st, -2.0 * s);
     const double half_over_dx = 0.5 / dx;
+    if (S->rk_post) {
+        const double omega = p->omega;
+        const double scalar_friction = (3.0 * (1.0 + omega) + s) * ad_st / a_st;
+        const double tensor_friction = (2.0 + s) * ad_st / a_st;
+        const double Htilde = ad_st / a_st;
+        const double invH = 1.0 / Htilde;
+        const double coeffU = 4.0 / (3.0 * (1.0 + omega));
+        const double inv_dx2 = 1.0 / (dx * dx);
+        const double den = 4.0 * dx * dx;
+        for (int i = 0; i < N; ++i) {
+            const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+            for (int j = 0; j < N; ++j) {
+                const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+                for (int k = 0; k < N; ++k) {
+                    const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                    const size_t id = IDX(N, i, j, k);
+                    const double lap = LAPL_AT(double, fs, N, i, j, k, ip, im, jp, jm, kp, km);
+                    kf[id] = fds[id];
+                    kfd[id] = omega * laplnorm * lap - scalar_friction * fds[id];
+                    if (!p->calculate_SIGW) continue;
+                    const double gx = (fs[IDX(N, ip, j, k)] - fs[IDX(N, im, j, k)]) * half_over_dx;
+                    const double gy = (fs[IDX(N, i, jp, k)] - fs[IDX(N, i, jm, k)]) * half_over_dx;
+                    const double gz = (fs[IDX(N, i, j, kp)] - fs[IDX(N, i, j, km)]) * half_over_dx;
+                    const double gdx = (fds[IDX(N, ip, j, k)] - fds[IDX(N, im, j, k)]) * half_over_dx;
+                    const double gdy = (fds[IDX(N, i, jp, k)] - fds[IDX(N, i, jm, k)]) * half_over_dx;
+                    const double gdz = (fds[IDX(N, i, j, kp)] - fds[IDX(N, i, j, km)]) * half_over_dx;
+                    const double Hxx = (fs[IDX(N, ip, j, k)] - 2.0 * fs[id] + fs[IDX(N, im, j, k)]) * inv_dx2;
+                    const double Hyy = (fs[IDX(N, i, jp, k)] - 2.0 * fs[id] + fs[IDX(N, i, jm, k)]) * inv_dx2;
+                    const double Hzz = (fs[IDX(N, i, j, kp)] - 2.0 * fs[id] + fs[IDX(N, i, j, km)]) * inv_dx2;
+                    const double Hxy = d2_cross_at(fs, N, 0, 1, i, j, k, den);
+                    const double Hxz = d2_cross_at(fs, N, 0, 2, i, j, k, den);
+                    const double Hyz = d2_cross_at(fs, N, 1, 2, i, j, k, den);
+                    const double dux = gdx * invH + gx;
+                    const double duy = gdy * invH + gy;
+                    const double duz = gdz * invH + gz;
+                    const double Phi = fs[id];
+                    const double Sc[6] = {
+                        4.0 * Phi * Hxx + 2.0 * gx * gx - coeffU * (dux * dux),
+                        4.0 * Phi * Hyy + 2.0 * gy * gy - coeffU * (duy * duy),
+                        4.0 * Phi * Hzz + 2.0 * gz * gz - coeffU * (duz * duz),
+                        4.0 * Phi * Hxy + 2.0 * gx * gy - coeffU * (dux * duy),
+                        4.0 * Phi * Hxz + 2.0 * gx * gz - coeffU * (dux * duz),
+                        4.0 * Phi * Hyz + 2.0 * gy * gz - coeffU * (duy * duz)};
+                    for (int c = 0; c < 6; ++c) {
+                        const float lapf = LAPL_AT(float, hs[c], N, i, j, k, ip, im, jp, jm, kp, km);
+                        kh[c][id] = hds[c][id];
+                        khd[c][id] = (float)(laplnorm * (double)lapf - tensor_friction * (double)hds[c][id] +
+                                             srcAmp * Sc[c]);
+                    }
+                }
+            }
+        }
+        *dadt = ad_st;
+        *daddt = -(s - 0.5 * (1.0 - 3.0 * omega)) * pw2(ad_st) / a_st;
+        return 0;
+    }
+    const double friction = (2.0 + s) * ad_st / a_st;
+    const double potnorm = pow(a_st, 2.0 - 2.0 * s);
     double gradient_sum = 0.0, potential_sum = 0.0;
     for (int i = 0; i < N; ++i) {
         const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
@@ -923,15 +1016,33 @@ static int rk_rhs(ieo_state* S, const double* fs, const double* fds, float* cons
     return 0;
 }
 
-static const double RK4_A[4][4] = {{0.0, 0.0, 0.0, 0.0}, {0.5, 0.0, 0.0, 0.0}, {0.0, 0.5, 0.0, 0.0}, {0.0, 0.0, 1.0, 0.0}};
-static const double RK4_B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+/* RK4_A, RK4_B and the Dormand-Prince 5(4) tableau (DormandPrince45Coefficients,
+ * src/evolution.cpp:366-414, 601-637): the published coefficients; e = b - b*. */
+static const double RK4_A[7][7] = {{0.0}, {0.5}, {0.0, 0.5}, {0.0, 0.0, 1.0}};
+static const double RK4_B[7] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+#define DP_B1 (35.0 / 384.0)
+#define DP_B3 (500.0 / 1113.0)
+#define DP_B4 (125.0 / 192.0)
+#define DP_B5 (-2187.0 / 6784.0)
+#define DP_B6 (11.0 / 84.0)
+static const double DP_A[7][7] = {
+    {0.0},
+    {1.0 / 5.0},
+    {3.0 / 40.0, 9.0 / 40.0},
+    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0},
+    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0},
+    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0},
+    {DP_B1, 0.0, DP_B3, DP_B4, DP_B5, DP_B6}};
+static const double DP_B[7] = {DP_B1, 0.0, DP_B3, DP_B4, DP_B5, DP_B6, 0.0};
+static const double DP_E[7] = {DP_B1 - 5179.0 / 57600.0, 0.0, DP_B3 - 7571.0 / 16695.0, DP_B4 - 393.0 / 640.0,
+                               DP_B5 - -92097.0 / 339200.0, DP_B6 - 187.0 / 2100.0, -(1.0 / 40.0)};
 
 static void rk_scratch(ieo_state* S) {
     if (S->ftmp) return;
     const size_t gs = S->gs;
     S->ftmp = (double*)calloc(gs, sizeof(double));
     S->fdtmp = (double*)calloc(gs, sizeof(double));
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 7; ++q) {
         S->kf[q] = (double*)calloc(gs, sizeof(double));
         S->kfd[q] = (double*)calloc(gs, sizeof(double));
     }
@@ -939,60 +1050,64 @@ static void rk_scratch(ieo_state* S) {
         for (int c = 0; c < 6; ++c) {
             S->htmp[c] = (float*)calloc(gs, sizeof(float));
             S->hdtmp[c] = (float*)calloc(gs, sizeof(float));
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < 7; ++q) {
                 S->kh[q][c] = (float*)calloc(gs, sizeof(float));
                 S->khd[q][c] = (float*)calloc(gs, sizeof(float));
             }
         }
 }
 
-/* rk4_step_inflation(h), src/evolution.cpp:760-779, with the stage states of
- * prepare_inflation_stage_state (:641-671), the background stages of
- * prepare_inflation_background_state (:673-690) and the update of
- * apply_inflation_weighted_update (:717-758).  ad2 is not touched. */
+/* evaluate_inflation_stage, src/evolution.cpp:692-715: the stage state of
+ * prepare_inflation_stage_state (:639-671), the background stage of
+ * prepare_inflation_background_state (:673-690) and the stage's derivatives. */
+static int rk_stage(ieo_state* S, double h, int stage, const double (*A)[7], double* ka, double* kad) {
+    const size_t gs = S->gs;
+    for (size_t id = 0; id < gs; ++id) {
+        double sum_f = 0.0, sum_fd = 0.0;
+        for (int q = 0; q < stage; ++q) {
+            const double c = A[stage][q];
+            if (c == 0.0) continue;
+            sum_f += c * S->kf[q][id];
+            sum_fd += c * S->kfd[q][id];
+        }
+        S->ftmp[id] = S->f[id] + h * sum_f;
+        S->fdtmp[id] = S->fd[id] + h * sum_fd;
+    }
+    if (S->p.calculate_SIGW)
+        for (int c = 0; c < 6; ++c)
+            for (size_t id = 0; id < gs; ++id) {
+                double sum_h = 0.0, sum_hd = 0.0;
+                for (int q = 0; q < stage; ++q) {
+                    const double cs = A[stage][q];
+                    if (cs == 0.0) continue;
+                    sum_h += cs * (double)S->kh[q][c][id];
+                    sum_hd += cs * (double)S->khd[q][c][id];
+                }
+                S->htmp[c][id] = (float)((double)S->h[c][id] + h * sum_h);
+                S->hdtmp[c][id] = (float)((double)S->hd[c][id] + h * sum_hd);
+            }
+    double a_st = S->a, ad_st = S->ad;
+    for (int q = 0; q < stage; ++q) {
+        const double c = A[stage][q];
+        if (c == 0.0) continue;
+        a_st += h * c * ka[q];
+        ad_st += h * c * kad[q];
+    }
+    return rk_rhs(S, S->ftmp, S->fdtmp, S->htmp, S->hdtmp, S->kf[stage], S->kfd[stage], S->kh[stage], S->khd[stage],
+                  a_st, ad_st, &ka[stage], &kad[stage]);
+}
+
+/* rk4_step_inflation(h), src/evolution.cpp:760-779, with the weighted update
+ * of apply_inflation_weighted_update (:717-758).  ad2 is not touched. */
 int ieo_rk4_step_inflation(ieo_state* S, double h) {
     rk_scratch(S);
     const size_t gs = S->gs;
     const int sigw = S->p.calculate_SIGW;
-    double ka[4] = {0.0, 0.0, 0.0, 0.0}, kad[4] = {0.0, 0.0, 0.0, 0.0};
+    double ka[7] = {0.0}, kad[7] = {0.0};
     if (rk_rhs(S, S->f, S->fd, S->h, S->hd, S->kf[0], S->kfd[0], S->kh[0], S->khd[0], S->a, S->ad, &ka[0], &kad[0]))
         return 1;
-    for (int stage = 1; stage < 4; ++stage) {
-        for (size_t id = 0; id < gs; ++id) {
-            double sum_f = 0.0, sum_fd = 0.0;
-            for (int q = 0; q < stage; ++q) {
-                const double c = RK4_A[stage][q];
-                if (c == 0.0) continue;
-                sum_f += c * S->kf[q][id];
-                sum_fd += c * S->kfd[q][id];
-            }
-            S->ftmp[id] = S->f[id] + h * sum_f;
-            S->fdtmp[id] = S->fd[id] + h * sum_fd;
-        }
-        if (sigw)
-            for (int c = 0; c < 6; ++c)
-                for (size_t id = 0; id < gs; ++id) {
-                    double sum_h = 0.0, sum_hd = 0.0;
-                    for (int q = 0; q < stage; ++q) {
-                        const double cs = RK4_A[stage][q];
-                        if (cs == 0.0) continue;
-                        sum_h += cs * (double)S->kh[q][c][id];
-                        sum_hd += cs * (double)S->khd[q][c][id];
-                    }
-                    S->htmp[c][id] = (float)((double)S->h[c][id] + h * sum_h);
-                    S->hdtmp[c][id] = (float)((double)S->hd[c][id] + h * sum_hd);
-                }
-        double a_st = S->a, ad_st = S->ad;
-        for (int q = 0; q < stage; ++q) {
-            const double c = RK4_A[stage][q];
-            if (c == 0.0) continue;
-            a_st += h * c * ka[q];
-            ad_st += h * c * kad[q];
-        }
-        if (rk_rhs(S, S->ftmp, S->fdtmp, S->htmp, S->hdtmp, S->kf[stage], S->kfd[stage], S->kh[stage], S->khd[stage],
-                   a_st, ad_st, &ka[stage], &kad[stage]))
-            return 1;
-    }
+    for (int stage = 1; stage < 4; ++stage)
+        if (rk_stage(S, h, stage, RK4_A, ka, kad)) return 1;
     for (size_t id = 0; id < gs; ++id) {
         double sum_f = 0.0, sum_fd = 0.0;
         for (int q = 0; q < 4; ++q) {
@@ -1026,6 +1141,147 @@ int ieo_rk4_step_inflation(ieo_state* S, double h) {
     S->t += h;
     return 0;
 }
+
+/* std::max / std::min / std::clamp as the reference calls them */
+static inline double smax(double a, double b) { return (a < b) ? b : a; }
+static inline double smin(double a, double b) { return (b < a) ? b : a; }
+
+/* clamp_rk45_step, src/evolution.cpp:326-332 */
+double ieo_rk45_clamp(const ieo_state* S, double h, double hmax) {
+    const double hmin = smax(1e-16, S->p.rk45_min_dt);
+    const double hhi = smax(hmin, hmax);
+    if (h < hmin) return hmin;
+    if (h > hhi) return hhi;
+    return h;
+}
+
+/* rk45_hmax_from_base_step, src/evolution.cpp:341-343 */
+double ieo_rk45_hmax(const ieo_state* S, double base_step) {
+    return smin(S->p.rk45_max_dt, smax(S->p.rk45_min_dt, 2.0 * base_step));
+}
+
+/* rk45_step_inflation(h, hmax, h_next), src/evolution.cpp:781-904: one
+ * Dormand-Prince 5(4) attempt; on acceptance the 5th-order state is taken
+ * and *accepted = 1.  The error norm is the weighted RMS over f, fd (and the
+ * twelve tensor arrays) and a, ad, summed in the reference's order. */
+int ieo_rk45_step_inflation(ieo_state* S, double h, double hmax, double* h_next, int* accepted) {
+    rk_scratch(S);
+    const ieo_params* p = &S->p;
+    const size_t gs = S->gs;
+    const double atol = p->rk45_abs_tol, rtol = p->rk45_rel_tol;
+    double ka[7] = {0.0}, kad[7] = {0.0};
+    if (rk_rhs(S, S->f, S->fd, S->h, S->hd, S->kf[0], S->kfd[0], S->kh[0], S->khd[0], S->a, S->ad, &ka[0], &kad[0]))
+        return 1;
+    for (int stage = 1; stage < 7; ++stage)
+        if (rk_stage(S, h, stage, DP_A, ka, kad)) return 1;
+    double a5 = S->a, ad5 = S->ad, erra = 0.0, errad = 0.0;
+    for (int q = 0; q < 7; ++q) {
+        const double bs = DP_B[q], es = DP_E[q];
+        if (bs != 0.0) {
+            a5 += h * bs * ka[q];
+            ad5 += h * bs * kad[q];
+        }
+        if (es != 0.0) {
+            erra += h * es * ka[q];
+            errad += h * es * kad[q];
+        }
+    }
+    double err_acc = 0.0;
+    size_t nvars = 2 * gs + 2;
+    for (size_t id = 0; id < gs; ++id) {
+        double y5f = S->f[id], y5fd = S->fd[id], errf = 0.0, errfd = 0.0;
+        for (int q = 0; q < 7; ++q) {
+            const double bs = DP_B[q], es = DP_E[q];
+            if (bs != 0.0) {
+                y5f += h * bs * S->kf[q][id];
+                y5fd += h * bs * S->kfd[q][id];
+            }
+            if (es != 0.0) {
+                errf += h * es * S->kf[q][id];
+                errfd += h * es * S->kfd[q][id];
+            }
+        }
+        S->ftmp[id] = y5f;
+        S->fdtmp[id] = y5fd;
+        const double sf = atol + rtol * smax(fabs(S->f[id]), fabs(y5f));
+        const double sfd = atol + rtol * smax(fabs(S->fd[id]), fabs(y5fd));
+        err_acc += pw2(errf / sf) + pw2(errfd / sfd);
+    }
+    if (p->calculate_SIGW) {
+        nvars += 12 * gs;
+        for (int c = 0; c < 6; ++c)
+            for (size_t id = 0; id < gs; ++id) {
+                double y5h = (double)S->h[c][id], y5hd = (double)S->hd[c][id], errh = 0.0, errhd = 0.0;
+                for (int q = 0; q < 7; ++q) {
+                    const double bs = DP_B[q], es = DP_E[q];
+                    if (bs != 0.0) {
+                        y5h += h * bs * (double)S->kh[q][c][id];
+                        y5hd += h * bs * (double)S->khd[q][c][id];
+                    }
+                    if (es != 0.0) {
+                        errh += h * es * (double)S->kh[q][c][id];
+                        errhd += h * es * (double)S->khd[q][c][id];
+                    }
+                }
+                S->htmp[c][id] = (float)y5h;
+                S->hdtmp[c][id] = (float)y5hd;
+                const double sh = atol + rtol * smax(fabs((double)S->h[c][id]), fabs(y5h));
+                const double shd = atol + rtol * smax(fabs((double)S->hd[c][id]), fabs(y5hd));
+                err_acc += pw2(errh / sh) + pw2(errhd / shd);
+            }
+    }
+    const double sa = atol + rtol * smax(fabs(S->a), fabs(a5));
+    const double sad = atol + rtol * smax(fabs(S->ad), fabs(ad5));
+    err_acc += pw2(erra / sa) + pw2(errad / sad);
+    const double err_norm = sqrt(err_acc / (double)nvars);
+    const double safe_err = smax(err_norm, 1e-16);
+    double factor = p->rk45_safety * pow(safe_err, -0.2);
+    factor = (factor < 0.1) ? 0.1 : (5.0 < factor) ? 5.0 : factor;
+    S->rk45_err = err_norm;
+    if (err_norm <= 1.0) {
+        double* t;
+        t = S->f; S->f = S->ftmp; S->ftmp = t;
+        t = S->fd; S->fd = S->fdtmp; S->fdtmp = t;
+        if (p->calculate_SIGW)
+            for (int c = 0; c < 6; ++c) {
+                float* u = S->h[c]; S->h[c] = S->htmp[c]; S->htmp[c] = u;
+                u = S->hd[c]; S->hd[c] = S->hdtmp[c]; S->hdtmp[c] = u;
+            }
+        S->a = a5;
+        S->ad = ad5;
+        S->t += h;
+        *h_next = ieo_rk45_clamp(S, h * factor, hmax);
+        *accepted = 1;
+        return 0;
+    }
+    *h_next = ieo_rk45_clamp(S, h * smax(0.1, smin(0.5, factor)), hmax);
+    *accepted = 0;
+    return 0;
+}
+
+/* rk45_accept_step, src/evolution.cpp:345-363: attempts until one is
+ * accepted; fails after 25 rejections or at the minimum step.  Returns the
+ * step proposed for the next call in *h. */
+int ieo_rk45_accept(ieo_state* S, double* h, double hmax) {
+    int accepted = 0, attempts = 0;
+    while (!accepted) {
+        double hs = *h;
+        if (ieo_rk45_step_inflation(S, *h, hmax, &hs, &accepted)) return 1;
+        *h = hs;
+        ++attempts;
+        if (!accepted && (attempts > 25 || *h <= S->p.rk45_min_dt * (1.0 + 1e-12))) {
+            if (S->rk_post)
+                set_err(S, "RK45 failed to converge in post-inflation at a=%e, t=%e (attempts=%d, h=%e)\n", S->a, S->t,
+                        attempts, *h);
+            else
+                set_err(S, "RK45 failed to converge at a=%e, t=%e (attempts=%d, h=%e)\n", S->a, S->t, attempts, *h);
+            return 1;
+        }
+    }
+    return 0;
+}
+
+void ieo_set_rk_post(ieo_state* S, int post) { S->rk_post = post != 0; }
 
 /* inflation_rescaled_step, src/evolution.cpp:338-340 */
 double ieo_rescaled_step(const ieo_state* S, double astep) {
@@ -1647,7 +1903,9 @@ static int out_save_post(ieo_state* S, outfiles* O, int infrequent) {
     const ieo_params* p = &S->p;
     if (g_trace)
         fprintf(g_trace, "savep %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, S->t, S->a, S->ad, S->ad2, S->astep);
-    if (S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt_post_inflation);
+    /* the sync is the leapfrog's (post_inflation_uses_staggered_derivatives, src/main.h:193-195) */
+    const int stag = p->post_inflation_integrator == 0;
+    if (stag && S->t > 0.) ieo_evolve_fields(S, -.5 * p->dt_post_inflation);
     if (out_meansvars(S, O, 1)) return 1;
     out_scale(S, O, 1);
     if (infrequent) {
@@ -1679,7 +1937,7 @@ static int out_save_post(ieo_state* S, outfiles* O, int infrequent) {
             out_histogram(S, S->f, open_out(S, O, &O->phistogram, "post_inflation/histogram"),
                           open_out(S, O, &O->phistogramtimes, "post_inflation/histogramtimes"), 0);
     }
-    if (S->t > 0.) ieo_evolve_fields(S, .5 * p->dt_post_inflation);
+    if (stag && S->t > 0.) ieo_evolve_fields(S, .5 * p->dt_post_inflation);
     return S->err;
 }
 
@@ -1850,22 +2108,28 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
     if (out_save(S, &O, 1)) goto done;
     S->t = S->t0;
 
-    /* run_evolution_loop(), leapfrog and RK4 branches, src/evolution.cpp:909-997 */
-    if (p->inflation_integrator == 2) {
-        set_err(S, "the rk45 inflation integrator is not restated by this oracle\n");
+    /* run_evolution_loop(), src/evolution.cpp:909-997 */
+    if (p->perform_deltaN && p->deltaN_integrator != 0) {
+        set_err(S, "the deltaN loop's RK integrators are not restated by this oracle\n");
         goto done;
     }
     {
         int numsteps = 0;
         const int leap = p->inflation_integrator == 0;
+        /* RK45: the first h, src/evolution.cpp:959 */
+        double h45 = ieo_rk45_clamp(S, ieo_rescaled_step(S, S->astep), p->rk45_max_dt);
         if (leap) ieo_evolve_fields(S, 0.5 * p->dt);
         while (S->a <= p->af) {
             const double d = ieo_rescaled_step(S, S->astep);
             if (leap) {
                 if (ieo_evolve_derivs(S, d)) goto done;
                 ieo_evolve_fields(S, d);
-            } else if (ieo_rk4_step_inflation(S, d)) {
-                goto done;
+            } else if (p->inflation_integrator == 1) {
+                if (ieo_rk4_step_inflation(S, d)) goto done;
+            } else {
+                const double hmax = ieo_rk45_hmax(S, d);
+                h45 = ieo_rk45_clamp(S, h45, hmax);
+                if (ieo_rk45_accept(S, &h45, hmax)) goto done;
             }
             numsteps++;
             if (numsteps % p->output_freq == 0 && S->a < p->af)
@@ -1901,7 +2165,7 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
         fflush(O.output);
         ieo_evolve_fieldsN(S, -0.5 * p->dN);
     }
-    /* run_post_inflation_loop(), leapfrog branch, src/evolution.cpp:1561-1653 */
+    /* run_post_inflation_loop(), leapfrog, RK4 and RK45 branches, src/evolution.cpp:1561-1653 */
     if (p->post_inflation) {
         if (!p->calculate_SIGW) {
             set_err(S, "post_inflation requires calculate_SIGW = 1\n");
@@ -1912,10 +2176,22 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
         ieo_initialize_post_inflation(S);
         if (out_save_post(S, &O, 1)) goto done;
         int numsteps = 0;
-        ieo_evolve_fields(S, 0.5 * p->dt_post_inflation);
+        const int pint = p->post_inflation_integrator;
+        /* RK branches: the post-inflation right-hand side (ScopedPostInflationRhsMode) */
+        S->rk_post = pint != 0;
+        double h45 = ieo_rk45_clamp(S, p->dt_post_inflation, p->rk45_max_dt);
+        if (pint == 0) ieo_evolve_fields(S, 0.5 * p->dt_post_inflation);
         while (S->a <= p->af_post_inflation) {
-            ieo_evolve_derivs_post_inflation(S, p->dt_post_inflation);
-            ieo_evolve_fields(S, p->dt_post_inflation);
+            if (pint == 0) {
+                ieo_evolve_derivs_post_inflation(S, p->dt_post_inflation);
+                ieo_evolve_fields(S, p->dt_post_inflation);
+            } else if (pint == 1) {
+                if (ieo_rk4_step_inflation(S, p->dt_post_inflation)) goto done;
+            } else {
+                const double hmax = ieo_rk45_hmax(S, p->dt_post_inflation);
+                h45 = ieo_rk45_clamp(S, h45, hmax);
+                if (ieo_rk45_accept(S, &h45, hmax)) goto done;
+            }
             numsteps++;
             if (numsteps % p->output_freq == 0)
                 if (out_save_post(S, &O, (numsteps % p->output_infrequent_freq == 0) ? 1 : 0)) goto done;

@@ -50,8 +50,13 @@ typedef struct {
     /* post-inflation phase (src/parameters.h:31 switch, src/runtime_parameters.cpp:48-52, 295-299) */
     int post_inflation, af_post_given;
     double horizon_factor, omega, dt_post_inflation, af_post_inflation;
-    /* inflation_integrator, src/runtime_parameters.cpp:141-166: 0 leapfrog, 1 rk4 (2 rk45 is not restated) */
+    /* integrators, src/runtime_parameters.cpp:141-166: 0 leapfrog, 1 rk4, 2 rk45 (the deltaN loop's RK
+     * branches are not restated) */
     int inflation_integrator, pad_;
+    int post_inflation_integrator, deltaN_integrator;
+    /* RK45 controls, src/runtime_parameters.cpp:82-86, 184-192, 351-353 */
+    double rk45_abs_tol, rk45_rel_tol, rk45_min_dt, rk45_max_dt, rk45_safety;
+    int rk45_min_given, rk45_max_given;
 } ieo_params;
 
 typedef struct ieo_state ieo_state;
@@ -116,6 +121,14 @@ int ieo_leapfrog_steps(ieo_state* S, int nsteps);
  * compute_inflation_rhs (:418-512); the RHS sums are serial in loop order, which is
  * what the reference's OpenMP reduction gives with one thread. ---- */
 int ieo_rk4_step_inflation(ieo_state* S, double h);
+/* RK45 (Dormand-Prince 5(4)): one attempt, the clamp and hmax helpers and the
+ * accept/reject driver of src/evolution.cpp:326-363, 781-904 */
+int ieo_rk45_step_inflation(ieo_state* S, double h, double hmax, double* h_next, int* accepted);
+int ieo_rk45_accept(ieo_state* S, double* h, double hmax);
+double ieo_rk45_clamp(const ieo_state* S, double h, double hmax);
+double ieo_rk45_hmax(const ieo_state* S, double base_step);
+/* selects the post-inflation right-hand side for the RK steps */
+void ieo_set_rk_post(ieo_state* S, int post);
 
 /* ---- post-inflation phase: src/initialize.cpp:245-290, src/evolution.cpp:1378-1653 ---- */
 void ieo_initialize_post_inflation(ieo_state* S);

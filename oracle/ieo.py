@@ -46,7 +46,11 @@ class Params(C.Structure):
                 ("nbins", C.c_int), ("int_err", C.c_int), ("int_errN", C.c_int), ("dx", C.c_double),
                 ("post_inflation", C.c_int), ("af_post_given", C.c_int), ("horizon_factor", C.c_double),
                 ("omega", C.c_double), ("dt_post_inflation", C.c_double), ("af_post_inflation", C.c_double),
-                ("inflation_integrator", C.c_int), ("pad_", C.c_int)]
+                ("inflation_integrator", C.c_int), ("pad_", C.c_int),
+                ("post_inflation_integrator", C.c_int), ("deltaN_integrator", C.c_int),
+                ("rk45_abs_tol", C.c_double), ("rk45_rel_tol", C.c_double), ("rk45_min_dt", C.c_double),
+                ("rk45_max_dt", C.c_double), ("rk45_safety", C.c_double),
+                ("rk45_min_given", C.c_int), ("rk45_max_given", C.c_int)]
 
 
 class Scalars(C.Structure):
@@ -85,6 +89,8 @@ def load() -> C.CDLL:
         "ieo_evolve_derivs": (I, [P, D]), "ieo_evolve_fields": (None, [P, D]),
         "ieo_initialize_post_inflation": (None, [P]), "ieo_evolve_derivs_post_inflation": (None, [P, D]),
         "ieo_rk4_step_inflation": (I, [P, D]),
+        "ieo_rk45_step_inflation": (I, [P, D, D, dp, ip]), "ieo_rk45_accept": (I, [P, dp, D]),
+        "ieo_rk45_clamp": (D, [P, D, D]), "ieo_rk45_hmax": (D, [P, D]), "ieo_set_rk_post": (None, [P, I]),
         "ieo_rescaled_step": (D, [P, D]), "ieo_leapfrog_steps": (I, [P, I]),
         "ieo_fftrn_d": (None, [dp, dp, I, I]), "ieo_fftrn_f": (None, [fp, fp, I, I]),
         "ieo_numbins": (I, [I]),
@@ -114,6 +120,10 @@ def default_params(N: int, numerical: bool, **kw) -> Params:
         setattr(p, k, v)
     if "af_post_inflation" in kw:
         p.af_post_given = 1
+    if "rk45_min_dt" in kw:
+        p.rk45_min_given = 1
+    if "rk45_max_dt" in kw:
+        p.rk45_max_given = 1
     lib.ieo_params_finalize(C.byref(p), int(B_given), int(af_given))
     return p
 
@@ -228,6 +238,27 @@ class Oracle:
     def rk4_step_inflation(self, h):
         self._check(self.lib.ieo_rk4_step_inflation(self.h, h))
 
+    def rk45_step_inflation(self, h, hmax):
+        """One RK45 attempt: (accepted, h_next)."""
+        hn, acc = C.c_double(h), C.c_int(0)
+        self._check(self.lib.ieo_rk45_step_inflation(self.h, h, hmax, C.byref(hn), C.byref(acc)))
+        return bool(acc.value), hn.value
+
+    def rk45_accept(self, h, hmax):
+        """rk45_accept_step: attempts until one is accepted; the next step's h."""
+        hh = C.c_double(h)
+        self._check(self.lib.ieo_rk45_accept(self.h, C.byref(hh), hmax))
+        return hh.value
+
+    def rk45_clamp(self, h, hmax):
+        return self.lib.ieo_rk45_clamp(self.h, h, hmax)
+
+    def rk45_hmax(self, base_step):
+        return self.lib.ieo_rk45_hmax(self.h, base_step)
+
+    def set_rk_post(self, post):
+        self.lib.ieo_set_rk_post(self.h, int(bool(post)))
+
     def initialize_post_inflation(self):
         self.lib.ieo_initialize_post_inflation(self.h)
 
@@ -341,10 +372,8 @@ def params_from_text(text: str, N: int, numerical: bool, sigw: bool, deltaN: boo
         k, v = (x.strip() for x in line.split("=", 1))
         if k in ("output_bispectrum", "output_LOG"):
             continue
-        if k == "inflation_integrator":
-            kw[k] = {"leapfrog": 0, "lf": 0, "rk4": 1, "rk45": 2, "rkf45": 2, "dopri5": 2}.get(v.lower(), 0)
-            continue
         if k.endswith("_integrator"):
+            kw[k] = {"leapfrog": 0, "lf": 0, "rk4": 1, "rk45": 2, "rkf45": 2, "dopri5": 2}.get(v.lower(), 0)
             continue
         kw[k] = float(v) if any(ch in v for ch in ".eE") else int(v)
     kw["calculate_SIGW"] = int(sigw)

@@ -44,6 +44,10 @@ CASES = {
     "n32_hilltop": (32, 0, 0, 1, 0, HILLTOP),
     "n16_usr_sigw_post": (16, 1, 1, 1, 1, USR),
     "n16_hilltop_rk4": (16, 0, 0, 1, 0, dict(HILLTOP, inflation_integrator="rk4")),
+    # a step large enough for the RK45 step control to act (rejections, h below and above dt)
+    "n16_hilltop_rk45": (16, 0, 0, 1, 0, dict(HILLTOP, dt=0.05, inflation_integrator="rk45", rk45_abs_tol=1e-12,
+                                              rk45_rel_tol=1e-10)),
+    "n16_usr_sigw_post_rk45": (16, 1, 1, 1, 1, dict(USR, post_inflation_integrator="rk45")),
 }
 
 
@@ -86,7 +90,7 @@ def main() -> None:
         os.symlink(HERE / "inputs", work / "inputs")
         # the RK right-hand side sums with an OpenMP reduction, whose order follows
         # the thread count: one thread gives the serial loop order
-        env = dict(os.environ, OMP_NUM_THREADS="1") if "inflation_integrator" in p else None
+        env = dict(os.environ, OMP_NUM_THREADS="1") if any(k.endswith("_integrator") for k in p) else None
         subprocess.run([str(exe), str(work)], check=True, stdout=subprocess.DEVNULL, env=env)
         dst = HERE / name
         if dst.exists():

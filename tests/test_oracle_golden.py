@@ -19,6 +19,8 @@ CASES = {
     "n32_hilltop": (32, False, False, False),
     "n16_usr_sigw_post": (16, True, True, True),
     "n16_hilltop_rk4": (16, False, False, False),
+    "n16_hilltop_rk45": (16, False, False, False),
+    "n16_usr_sigw_post_rk45": (16, True, True, True),
 }
 
 

@@ -3,7 +3,8 @@
 Runs only where the reference tree is available (it is read at build time by
 oracle/build_ref.py); elsewhere the committed golden fixtures
 (test_oracle_golden.py) carry the same check.  Configurations beyond the
-fixtures: hilltop with SIGW, USR without SIGW, USR at N = 32.
+fixtures: hilltop with SIGW, USR without SIGW, USR at N = 32, and the RK4 /
+RK45 integrators of the inflation and post-inflation loops.
 """
 from __future__ import annotations
 
@@ -31,6 +32,13 @@ CASES = [
     (32, True, True, False, USR),
     (16, False, True, True, HILL),
     (16, True, True, False, USR + "inflation_integrator = rk4\n"),
+    (16, False, False, False, HILL + "inflation_integrator = rk45\n"),
+    # a step large enough for the step control to act: h from 6e-4 to 0.04, one rejection
+    (16, False, False, False, HILL.replace("dt = 0.001", "dt = 0.05")
+     + "inflation_integrator = rk45\nrk45_abs_tol = 1e-12\nrk45_rel_tol = 1e-10\n"),
+    (16, True, True, False, USR + "inflation_integrator = dopri5\nrk45_rel_tol = 1e-7\n"),
+    (16, False, True, True, HILL + "post_inflation_integrator = rk4\n"),
+    (16, True, True, True, USR + "post_inflation_integrator = rk45\n"),
 ]
 
 
