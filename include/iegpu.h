@@ -42,6 +42,7 @@ typedef struct iegpu_ctx iegpu_ctx;
 #define IEGPU_EUNSUPPORTED  8  /* feature not available in this form */
 #define IEGPU_ETIMEOUT      9  /* a bounded device wait gave up */
 #define IEGPU_ETOOBIG      10  /* size above a fixed, documented limit */
+#define IEGPU_ECONVERGE    11  /* RK45 step control gave up, src/evolution.cpp:974-979, 1629-1634 */
 
 /* ---- configuration --------------------------------------------------- */
 #define IEGPU_POT_HILLTOP   0  /* analytic hilltop, src/potential.cpp:77-83 */
@@ -71,6 +72,15 @@ typedef struct {
 typedef struct {
     double t, a, ad, ad2, astep;
 } iegpu_bg;
+
+/* RK45 controls, src/runtime_parameters.cpp:82-86 (keys rk45_abs_tol,
+ * rk45_rel_tol, rk45_min_dt, rk45_max_dt, rk45_safety).  The library applies
+ * sanitize_rk45_controls (:184-192) to a copy: min_dt <= 0 means 1e-6 |dt|,
+ * max_dt <= 0 means |dt|, and out-of-range tolerances or safety take the
+ * defaults 1e-8, 1e-6, 0.9. */
+typedef struct {
+    double abs_tol, rel_tol, min_dt, max_dt, safety;
+} iegpu_rk45_controls;
 
 /* Field selectors for upload/download/FFT/spectra. */
 #define IEGPU_F       0   /* phi             (f)        */
@@ -147,6 +157,23 @@ int  iegpu_rk4_step_inflation(struct iegpu_ctx* ctx, double h, iegpu_bg* bg);
  * or follows the loop for this integrator. */
 int  iegpu_rk4(struct iegpu_ctx* ctx, double af, int max_steps, iegpu_bg* bg,
                int* steps_taken, double* a_trace);
+/* rk45_step_inflation(h, hmax, h_next), src/evolution.cpp:781-904
+ * (inflation_integrator = rk45; plain FP64 form): one Dormand-Prince 5(4)
+ * attempt of step h.  The weighted-RMS error over f, fd (h, hd) and a, ad
+ * decides acceptance: *accepted = 1 and bg takes the 5th-order state, or
+ * *accepted = 0 and the state is kept.  *h_next is the step the reference's
+ * controller proposes (clamped to hmax). */
+int  iegpu_rk45_step_inflation(struct iegpu_ctx* ctx, const iegpu_rk45_controls* ctl, double h, double hmax,
+                               double* h_next, int* accepted, iegpu_bg* bg);
+/* The RK45 branch of run_evolution_loop, src/evolution.cpp:958-985: while
+ * a <= af, hmax = min(max_dt, max(min_dt, 2 dt astep^(s-1))), *h clamped to
+ * it, attempts until one is accepted (rk45_accept_step, :345-363), then
+ * "astep = a" (left to the caller after the last step, as iegpu_leapfrog).
+ * *h carries the proposed step between steps and calls; the first call takes
+ * dt astep^(s-1) (:959).  After 25 rejections, or at the minimum step, it
+ * returns IEGPU_ECONVERGE with the reference's message. */
+int  iegpu_rk45(struct iegpu_ctx* ctx, const iegpu_rk45_controls* ctl, double af, int max_steps, double* h,
+                iegpu_bg* bg, int* steps_taken, double* a_trace);
 /* kin_energy(), gradient_energy(), potential_energy():
  * src/evolution.cpp:130-145, src/potential.cpp:151-171.  out[3] = {kin, grad, pot}. */
 int  iegpu_energies(struct iegpu_ctx* ctx, const iegpu_bg* bg, double out[3]);
@@ -206,6 +233,17 @@ int  iegpu_evolve_derivs_post_inflation(struct iegpu_ctx* ctx, double d, double 
  * be null, else max_steps entries) receives a after each step taken. */
 int  iegpu_post_inflation_leapfrog(struct iegpu_ctx* ctx, double af_post, double dt_post, double omega, int max_steps,
                                    iegpu_bg* bg, int* steps, double* a_trace);
+/* The RK4 and RK45 branches of run_post_inflation_loop,
+ * src/evolution.cpp:1606-1641: the post-inflation equations of
+ * compute_inflation_rhs (:515-598) in rk4_step_inflation with step dt_post,
+ * or in the RK45 step control with hmax from dt_post (*h as in iegpu_rk45,
+ * the first call taking dt_post), while bg->a <= af_post, at most max_steps
+ * steps.  No half drift precedes the loop for these integrators, and the
+ * saves do not re-synchronise. */
+int  iegpu_post_inflation_rk4(struct iegpu_ctx* ctx, double af_post, double dt_post, double omega, int max_steps,
+                              iegpu_bg* bg, int* steps, double* a_trace);
+int  iegpu_post_inflation_rk45(struct iegpu_ctx* ctx, const iegpu_rk45_controls* ctl, double af_post, double dt_post,
+                               double omega, int max_steps, double* h, iegpu_bg* bg, int* steps, double* a_trace);
 
 /* ---- diagnostics (src/output.cpp) ------------------------------------- */
 /* Sums of meansvars(), src/output.cpp:235-240: out[3] = {sum f, sum fd, sum f^2}. */

@@ -138,6 +138,7 @@ const char* iegpu_strerror(int code) {
         case IEGPU_EUNSUPPORTED: return "unsupported in this form";
         case IEGPU_ETIMEOUT: return "device wait timed out";
         case IEGPU_ETOOBIG: return "size above the fixed limit of this entry point";
+        case IEGPU_ECONVERGE: return "RK45 step control failed to converge";
         default: return "unknown error";
     }
 }
@@ -561,6 +562,22 @@ int iegpu_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps_t
     return fp64_rk4(c, af, max_steps, bg, steps_taken, a_trace);
 }
 
+int iegpu_rk45_step_inflation(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double h, double hmax, double* h_next,
+                              int* accepted, iegpu_bg* bg) {
+    if (!c || !bg || !ctl || !h_next || !accepted) return IEGPU_EINVAL;
+    if (int rc = rk_ok(c)) return rc;
+    return fp64_rk45_step(c, ctl, h, hmax, h_next, accepted, bg);
+}
+
+int iegpu_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af, int max_steps, double* h, iegpu_bg* bg,
+               int* steps_taken, double* a_trace) {
+    if (!c || !bg || !ctl || !h) return IEGPU_EINVAL;
+    if (steps_taken) *steps_taken = 0;
+    if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
+    if (int rc = rk_ok(c)) return rc;
+    return fp64_rk45(c, ctl, af, max_steps, h, bg, steps_taken, a_trace);
+}
+
 // The post-inflation phase runs on the plain FP64 state with SIGW on, as
 // the reference requires (src/parameters.h:33-35).
 static int post_ok(iegpu_ctx* c) {
@@ -588,6 +605,24 @@ int iegpu_post_inflation_leapfrog(iegpu_ctx* c, double af_post, double dt_post, 
     if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
     if (int rc = post_ok(c)) return rc;
     return fp64_post_leapfrog(c, af_post, dt_post, omega, max_steps, bg, steps, a_trace);
+}
+
+int iegpu_post_inflation_rk4(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg,
+                             int* steps, double* a_trace) {
+    if (!c || !bg) return IEGPU_EINVAL;
+    if (steps) *steps = 0;
+    if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
+    if (int rc = post_ok(c)) return rc;
+    return fp64_post_rk4(c, af_post, dt_post, omega, max_steps, bg, steps, a_trace);
+}
+
+int iegpu_post_inflation_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af_post, double dt_post,
+                              double omega, int max_steps, double* h, iegpu_bg* bg, int* steps, double* a_trace) {
+    if (!c || !bg || !ctl || !h) return IEGPU_EINVAL;
+    if (steps) *steps = 0;
+    if (max_steps < 0) return set_error(c, IEGPU_EINVAL, "max_steps must be >= 0");
+    if (int rc = post_ok(c)) return rc;
+    return fp64_post_rk45(c, ctl, af_post, dt_post, omega, max_steps, h, bg, steps, a_trace);
 }
 
 int iegpu_set_persistent(iegpu_ctx* c, int on) {

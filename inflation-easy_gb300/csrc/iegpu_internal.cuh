@@ -196,6 +196,7 @@ struct iegpu_ctx {
     // (doubles) and stage h, hd, k_hd (floats, SIGW)
     double* rk_d = nullptr;
     float* rk_h = nullptr;
+    int rk_nst = 0;   // stages the scratch is laid out for
 
     // table (device copies, plus the host copy for scalar evaluations)
     std::vector<double> htab_x, htab_V, htab_dV;
@@ -285,6 +286,14 @@ int fp64_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg);
 int fp64_post_init(iegpu_ctx* c, double horizon_factor, double omega, int from_deltaN, iegpu_bg* bg);
 int fp64_rk4_step(iegpu_ctx* c, double h, iegpu_bg* bg);
 int fp64_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace);
+int fp64_rk45_step(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double h, double hmax, double* h_next, int* accepted,
+                   iegpu_bg* bg);
+int fp64_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af, int max_steps, double* h, iegpu_bg* bg,
+              int* steps, double* a_trace);
+int fp64_post_rk4(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg, int* steps,
+                  double* a_trace);
+int fp64_post_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af_post, double dt_post, double omega,
+                   int max_steps, double* h, iegpu_bg* bg, int* steps, double* a_trace);
 int fp64_post_derivs(iegpu_ctx* c, double d, double omega, iegpu_bg* bg);
 int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg,
                        int* steps, double* a_trace);

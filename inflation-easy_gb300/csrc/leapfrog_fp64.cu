@@ -17,6 +17,7 @@
 // 32 B of which are the reference's own state update.
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 
 #include "iegpu_internal.cuh"
 #include "pot.cuh"
@@ -689,22 +690,30 @@ int fp64_post_leapfrog(iegpu_ctx* c, double af_post, double dt_post, double omeg
 namespace iegpu {
 
 // ---------------------------------------------------------------------------
-// RK4 inflation integrator: rk4_step_inflation, src/evolution.cpp:760-779,
-// with compute_inflation_rhs (:418-512), the stage states of
-// prepare_inflation_stage_state (:641-671), the background stages of
-// prepare_inflation_background_state (:673-690) and the weighted update of
-// apply_inflation_weighted_update (:717-758).
+// Runge-Kutta integrators (inflation_integrator / post_inflation_integrator =
+// rk4 | rk45): rk4_step_inflation and rk45_step_inflation,
+// src/evolution.cpp:760-904, with compute_inflation_rhs (:418-599: the
+// inflation equations, or the post-inflation ones that the RK branches of
+// run_post_inflation_loop select), the stage states of
+// prepare_inflation_stage_state (:639-671), the background stages of
+// prepare_inflation_background_state (:673-690), the weighted update of
+// apply_inflation_weighted_update (:717-758) and the step control of
+// :326-363.
 // ---------------------------------------------------------------------------
 //
-// A stage's derivatives are k_f = fd and k_fd = laplnorm lapl(f) - friction fd
-// - potnorm V'(f) (k_h = hd, k_hd = (float)(laplnorm lapl(h) - friction hd +
-// srcAmp T) with SIGW).  k_f of a stage is that stage's fd, so it is read from
-// the stage state instead of being stored.  Scratch per site, in doubles: f of
-// the current stage, fd of stages 1-3 and k_fd of stages 0-3; with SIGW, in
-// floats: h of the current stage (6), hd of stages 1-3 (18) and k_hd of
-// stages 0-3 (24).  The background stages need each stage's two lattice sums,
-// so they are formed on the host with the reference's expressions: one
-// 16-byte read-back per stage.
+// A stage's derivatives are k_f = fd and k_fd (k_h = hd and k_hd with SIGW).
+// k_f of a stage is that stage's fd, so it is read from the stage state
+// instead of being stored.  Scratch per site for an s-stage method, in
+// doubles: f of the current stage, fd of stages 1..s-1, k_fd of stages
+// 0..s-1 and the RK45 candidate fd (2s + 1); with SIGW, in floats: h of the
+// current stage, hd of stages 1..s-1, k_hd of stages 0..s-1 and the candidate
+// hd (6 (2s + 1)).  The RK45 candidate f and h go to the stage f and h
+// buffers.  The background stages of the inflation equations need each
+// stage's two lattice sums, so they are formed on the host with the
+// reference's expressions from a 16-byte read-back per stage; the
+// post-inflation equations have no lattice sums.  So does the RK45 error
+// norm: its lattice part is summed on the device, the rest is the
+// reference's host arithmetic.
 
 struct RkSigw {
     const float* hs[6];
@@ -716,9 +725,9 @@ struct RkCoef {
     double laplnorm, friction, potnorm, srcAmp, half_over_dx;
 };
 
-// compute_inflation_rhs on one stage state: k_fd (and k_hd) per site, and the
-// sums of f lapl(f) and V(f); the last CTA combines the block partials in a
-// fixed order into sums[0..1].
+// compute_inflation_rhs on one stage state, inflation equations: k_fd (and
+// k_hd) per site, and the sums of f lapl(f) and V(f); the last CTA combines
+// the block partials in a fixed order into sums[0..1].
 template <bool TABLE, bool SIGW>
 __global__ void __launch_bounds__(kThreads) k_rk_rhs(const double* __restrict__ fs, const double* __restrict__ fds,
                                                      double* __restrict__ kfd, RkSigw sg, PotDev P, DevCtl* ctl,
@@ -775,15 +784,68 @@ __global__ void __launch_bounds__(kThreads) k_rk_rhs(const double* __restrict__ 
     }
 }
 
-// One row of the tableau: out = base + h sum_q c_q k_q over the nonzero c_q,
+struct RkPostCoef {
+    double omega, laplnorm, scalar_friction, tensor_friction, invH, coeffU, srcAmp, half_over_dx, inv_dx2, den;
+};
+
+// compute_inflation_rhs, post-inflation equations (src/evolution.cpp:515-598):
+// k_fd = omega laplnorm lapl(f) - scalar_friction fd; the tensor source is
+// the Hessian form with the gradients of the stage's f and fd (the pack of
+// k_post_sigw, here without the kick).
+template <bool SIGW>
+__global__ void __launch_bounds__(kThreads) k_rk_rhs_post(const double* __restrict__ fs,
+                                                          const double* __restrict__ fds, double* __restrict__ kfd,
+                                                          RkSigw sg, int lg, RkPostCoef K) {
+    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const Nbr n = neighbours(id, lg);
+    const double fc = __ldg(&fs[id]);
+    const double lap = lapl7(fs, n, fc);
+    kfd[id] = K.omega * K.laplnorm * lap - K.scalar_friction * __ldg(&fds[id]);
+    if (SIGW) {
+        const long long dip = n.ip - id, dim = n.im - id, djp = n.jp - id, djm = n.jm - id, dkp = n.kp - id,
+                        dkm = n.km - id;
+        const double gx = (__ldg(&fs[n.ip]) - __ldg(&fs[n.im])) * K.half_over_dx;
+        const double gy = (__ldg(&fs[n.jp]) - __ldg(&fs[n.jm])) * K.half_over_dx;
+        const double gz = (__ldg(&fs[n.kp]) - __ldg(&fs[n.km])) * K.half_over_dx;
+        const double gdx = (__ldg(&fds[n.ip]) - __ldg(&fds[n.im])) * K.half_over_dx;
+        const double gdy = (__ldg(&fds[n.jp]) - __ldg(&fds[n.jm])) * K.half_over_dx;
+        const double gdz = (__ldg(&fds[n.kp]) - __ldg(&fds[n.km])) * K.half_over_dx;
+        const double Hxx = (__ldg(&fs[n.ip]) - 2.0 * fc + __ldg(&fs[n.im])) * K.inv_dx2;
+        const double Hyy = (__ldg(&fs[n.jp]) - 2.0 * fc + __ldg(&fs[n.jm])) * K.inv_dx2;
+        const double Hzz = (__ldg(&fs[n.kp]) - 2.0 * fc + __ldg(&fs[n.km])) * K.inv_dx2;
+        const double Hxy = cross4(fs, id + dip + djp, id + dip + djm, id + dim + djp, id + dim + djm, K.den);
+        const double Hxz = cross4(fs, id + dip + dkp, id + dip + dkm, id + dim + dkp, id + dim + dkm, K.den);
+        const double Hyz = cross4(fs, id + djp + dkp, id + djm + dkm, id + djp + dkp, id + djm + dkm, K.den);
+        const double dux = gdx * K.invH + gx;
+        const double duy = gdy * K.invH + gy;
+        const double duz = gdz * K.invH + gz;
+        const double S[6] = {4.0 * fc * Hxx + 2.0 * gx * gx - K.coeffU * (dux * dux),
+                             4.0 * fc * Hyy + 2.0 * gy * gy - K.coeffU * (duy * duy),
+                             4.0 * fc * Hzz + 2.0 * gz * gz - K.coeffU * (duz * duz),
+                             4.0 * fc * Hxy + 2.0 * gx * gy - K.coeffU * (dux * duy),
+                             4.0 * fc * Hxz + 2.0 * gx * gz - K.coeffU * (dux * duz),
+                             4.0 * fc * Hyz + 2.0 * gy * gz - K.coeffU * (duy * duz)};
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float* h = sg.hs[c];
+            const float lf = lapl7(h, n, __ldg(&h[id]));
+            sg.khd[c][id] = (float)(K.laplnorm * (double)lf - K.tensor_friction * (double)__ldg(&sg.hds[c][id]) +
+                                    K.srcAmp * S[c]);
+        }
+    }
+}
+
+constexpr int kRkMax = 7;
+
+// One row of a tableau: out = base + h sum_q c_q k_q over the nonzero c_q,
 // the sum started from 0.0 in q order (prepare_inflation_stage_state and
 // apply_inflation_weighted_update).  out may alias base.
 struct RkRow {
-    const double* kf[4];
-    const double* kfd[4];
-    const float* kh[4][6];
-    const float* khd[4][6];
-    double c[4];
+    const double* kf[kRkMax];
+    const double* kfd[kRkMax];
+    const float* kh[kRkMax][6];
+    const float* khd[kRkMax][6];
+    double c[kRkMax];
     int nq;
 };
 
@@ -794,8 +856,8 @@ struct RkH {
     float* hdo[6];
 };
 
-// Plain loads throughout: the final update writes f, fd, h and hd in place,
-// and k_f, k_h of stage 0 are fd, hd themselves (each site is read by its own
+// Plain loads throughout: the RK4 update writes f, fd, h and hd in place, and
+// k_f, k_h of stage 0 are fd, hd themselves (each site is read by its own
 // thread before that thread writes it).
 template <bool SIGW>
 __global__ void __launch_bounds__(kThreads) k_rk_combine(const double* f, const double* fd, double* fout,
@@ -803,7 +865,7 @@ __global__ void __launch_bounds__(kThreads) k_rk_combine(const double* f, const 
     const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
     double sum_f = 0.0, sum_fd = 0.0;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < kRkMax; ++q) {
         if (q >= R.nq || R.c[q] == 0.0) continue;
         sum_f += R.c[q] * R.kf[q][id];
         sum_fd += R.c[q] * R.kfd[q][id];
@@ -817,7 +879,7 @@ __global__ void __launch_bounds__(kThreads) k_rk_combine(const double* f, const 
         for (int c = 0; c < 6; ++c) {
             double sum_h = 0.0, sum_hd = 0.0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < kRkMax; ++q) {
                 if (q >= R.nq || R.c[q] == 0.0) continue;
                 sum_h += R.c[q] * (double)R.kh[q][c][id];
                 sum_hd += R.c[q] * (double)R.khd[q][c][id];
@@ -830,76 +892,226 @@ __global__ void __launch_bounds__(kThreads) k_rk_combine(const double* f, const 
     }
 }
 
-static const double kRk4A[4][4] = {{0.0, 0.0, 0.0, 0.0}, {0.5, 0.0, 0.0, 0.0}, {0.0, 0.5, 0.0, 0.0}, {0.0, 0.0, 1.0, 0.0}};
-static const double kRk4B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+// std::max / std::min as the reference calls them
+__host__ __device__ __forceinline__ double ref_max(double a, double b) { return (a < b) ? b : a; }
+__host__ __device__ __forceinline__ double ref_min(double a, double b) { return (b < a) ? b : a; }
 
-struct RkBufs {
-    double* f;            // stage f (stages 1-3)
-    double* fd[4];        // stage fd: [0] is the state's own fd
-    double* kfd[4];
-    float* h[6];          // stage h
-    float* hd[4][6];      // stage hd: [0] is the state's own hd
-    float* khd[4][6];
+struct Rk45Fin {
+    const double* kf[kRkMax];
+    const double* kfd[kRkMax];
+    const float* kh[kRkMax][6];
+    const float* khd[kRkMax][6];
+    const float* hs[6];
+    const float* hds[6];
+    double* y5f;
+    double* y5fd;
+    float* y5h[6];
+    float* y5hd[6];
+    double b[kRkMax], e[kRkMax];
+    double h, atol, rtol;
 };
 
-static int rk_bufs(iegpu_ctx* c, RkBufs& B) {
+// The lattice part of rk45_step_inflation (src/evolution.cpp:826-874): the
+// 5th-order candidate y5 = y + sum_q h b_q k_q and the embedded error
+// sum_q h e_q k_q per variable, each term added in q order, and the sum over
+// variables of (err / (atol + rtol max(|y|, |y5|)))^2, combined by the last
+// CTA in a fixed order into sums[0].
+template <bool SIGW>
+__global__ void __launch_bounds__(kThreads) k_rk45_final(const double* f, const double* fd, Rk45Fin F, double* part,
+                                                         unsigned* counter, double* sums, long long gs) {
+    double v[1] = {0.0};
+    for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
+        const double f0 = f[id], fd0 = fd[id];
+        double y5f = f0, y5fd = fd0, errf = 0.0, errfd = 0.0;
+#pragma unroll
+        for (int q = 0; q < kRkMax; ++q) {
+            const double bs = F.b[q], es = F.e[q];
+            if (bs != 0.0) {
+                y5f += F.h * bs * F.kf[q][id];
+                y5fd += F.h * bs * F.kfd[q][id];
+            }
+            if (es != 0.0) {
+                errf += F.h * es * F.kf[q][id];
+                errfd += F.h * es * F.kfd[q][id];
+            }
+        }
+        F.y5f[id] = y5f;
+        F.y5fd[id] = y5fd;
+        const double sf = F.atol + F.rtol * ref_max(fabs(f0), fabs(y5f));
+        const double sfd = F.atol + F.rtol * ref_max(fabs(fd0), fabs(y5fd));
+        const double qf = errf / sf, qfd = errfd / sfd;
+        v[0] += qf * qf + qfd * qfd;
+        if (SIGW) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const double h0 = (double)F.hs[c][id], hd0 = (double)F.hds[c][id];
+                double y5h = h0, y5hd = hd0, errh = 0.0, errhd = 0.0;
+#pragma unroll
+                for (int q = 0; q < kRkMax; ++q) {
+                    const double bs = F.b[q], es = F.e[q];
+                    if (bs != 0.0) {
+                        y5h += F.h * bs * (double)F.kh[q][c][id];
+                        y5hd += F.h * bs * (double)F.khd[q][c][id];
+                    }
+                    if (es != 0.0) {
+                        errh += F.h * es * (double)F.kh[q][c][id];
+                        errhd += F.h * es * (double)F.khd[q][c][id];
+                    }
+                }
+                F.y5h[c][id] = (float)y5h;
+                F.y5hd[c][id] = (float)y5hd;
+                const double sh = F.atol + F.rtol * ref_max(fabs(h0), fabs(y5h));
+                const double shd = F.atol + F.rtol * ref_max(fabs(hd0), fabs(y5hd));
+                const double qh = errh / sh, qhd = errhd / shd;
+                v[0] += qh * qh + qhd * qhd;
+            }
+        }
+    }
+    block_sum<1>(v);
+    if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+    if (!arrive_last(counter)) return;
+    if (threadIdx.x < 32) {
+        double tot[1];
+        sum_partials<1>(part, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            *counter = 0;
+            sums[0] = tot[0];
+        }
+    }
+}
+
+// RK4_A, RK4_B and the Dormand-Prince 5(4) tableau (src/evolution.cpp:366-414,
+// 601-637): the published coefficients, e = b - b*.
+#define IE_DP_B1 (35.0 / 384.0)
+#define IE_DP_B3 (500.0 / 1113.0)
+#define IE_DP_B4 (125.0 / 192.0)
+#define IE_DP_B5 (-2187.0 / 6784.0)
+#define IE_DP_B6 (11.0 / 84.0)
+static const double kRk4A[kRkMax][kRkMax] = {{0.0}, {0.5}, {0.0, 0.5}, {0.0, 0.0, 1.0}};
+static const double kRk4B[kRkMax] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+static const double kDpA[kRkMax][kRkMax] = {
+    {0.0},
+    {1.0 / 5.0},
+    {3.0 / 40.0, 9.0 / 40.0},
+    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0},
+    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0},
+    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0},
+    {IE_DP_B1, 0.0, IE_DP_B3, IE_DP_B4, IE_DP_B5, IE_DP_B6}};
+static const double kDpB[kRkMax] = {IE_DP_B1, 0.0, IE_DP_B3, IE_DP_B4, IE_DP_B5, IE_DP_B6, 0.0};
+static const double kDpE[kRkMax] = {IE_DP_B1 - 5179.0 / 57600.0, 0.0, IE_DP_B3 - 7571.0 / 16695.0,
+                                    IE_DP_B4 - 393.0 / 640.0, IE_DP_B5 - -92097.0 / 339200.0,
+                                    IE_DP_B6 - 187.0 / 2100.0, -(1.0 / 40.0)};
+
+struct RkBufs {
+    double* f;                 // stage f; the RK45 candidate f
+    double* fd[kRkMax];        // stage fd: [0] is the state's own fd
+    double* kfd[kRkMax];
+    double* y5fd;              // RK45 candidate fd
+    float* h[6];               // stage h; the RK45 candidate h
+    float* hd[kRkMax][6];      // stage hd: [0] is the state's own hd
+    float* khd[kRkMax][6];
+    float* y5hd[6];
+};
+
+// Which equations the stages use: inflation, or post-inflation with omega.
+struct RkEq {
+    bool post;
+    double omega;
+};
+
+static int rk_bufs(iegpu_ctx* c, int nst, RkBufs& B) {
     const size_t gs = c->gs;
-    if (!c->rk_d) {
-        if (cudaMalloc(&c->rk_d, sizeof(double) * 8 * gs) != cudaSuccess) {
+    const size_t nd = 2 * (size_t)nst + 1, nf = 6 * nd;
+    if (c->rk_nst < nst) {
+        cudaFree(c->rk_d);
+        cudaFree(c->rk_h);
+        c->rk_d = nullptr;
+        c->rk_h = nullptr;
+        c->rk_nst = 0;
+        if (cudaMalloc(&c->rk_d, sizeof(double) * nd * gs) != cudaSuccess) {
             cudaGetLastError();
             c->rk_d = nullptr;
-            return set_error(c, IEGPU_ENOMEM, "device allocation of the RK4 scratch (%zu bytes) failed", sizeof(double) * 8 * gs);
+            return set_error(c, IEGPU_ENOMEM, "device allocation of the RK scratch (%zu bytes) failed", sizeof(double) * nd * gs);
         }
-    }
-    if (c->cfg.sigw && !c->rk_h) {
-        if (cudaMalloc(&c->rk_h, sizeof(float) * 48 * gs) != cudaSuccess) {
+        if (c->cfg.sigw && cudaMalloc(&c->rk_h, sizeof(float) * nf * gs) != cudaSuccess) {
             cudaGetLastError();
             c->rk_h = nullptr;
-            return set_error(c, IEGPU_ENOMEM, "device allocation of the RK4 tensor scratch (%zu bytes) failed", sizeof(float) * 48 * gs);
+            return set_error(c, IEGPU_ENOMEM, "device allocation of the RK tensor scratch (%zu bytes) failed", sizeof(float) * nf * gs);
         }
+        c->rk_nst = nst;
     }
+    memset(&B, 0, sizeof B);
     B.f = c->rk_d;
     B.fd[0] = c->fd;
-    for (int q = 1; q < 4; ++q) B.fd[q] = c->rk_d + q * gs;
-    for (int q = 0; q < 4; ++q) B.kfd[q] = c->rk_d + (4 + q) * gs;
-    for (int k = 0; k < 6; ++k) {
-        B.h[k] = c->cfg.sigw ? c->rk_h + k * gs : nullptr;
+    for (int q = 1; q < nst; ++q) B.fd[q] = c->rk_d + q * gs;
+    for (int q = 0; q < nst; ++q) B.kfd[q] = c->rk_d + (nst + q) * gs;
+    B.y5fd = c->rk_d + 2 * (size_t)nst * gs;
+    for (int k = 0; k < 6 && c->cfg.sigw; ++k) {
+        float* const base = c->rk_h;
+        B.h[k] = base + k * gs;
         B.hd[0][k] = c->hd[k];
-        for (int q = 1; q < 4; ++q) B.hd[q][k] = c->cfg.sigw ? c->rk_h + (6 + 6 * (q - 1) + k) * gs : nullptr;
-        for (int q = 0; q < 4; ++q) B.khd[q][k] = c->cfg.sigw ? c->rk_h + (24 + 6 * q + k) * gs : nullptr;
+        for (int q = 1; q < nst; ++q) B.hd[q][k] = base + (6 * (size_t)q + k) * gs;
+        for (int q = 0; q < nst; ++q) B.khd[q][k] = base + (6 * ((size_t)nst + q) + k) * gs;
+        B.y5hd[k] = base + (12 * (size_t)nst + k) * gs;
     }
     return IEGPU_OK;
 }
 
-// compute_inflation_rhs for one stage: launches the kernel, reads the two
-// sums back and forms dadt, daddt on the host (src/evolution.cpp:500-511).
-static int rk_rhs(iegpu_ctx* c, const double* fs, const double* fds, const float* const* hs, const float* const* hds,
-                  double* kfd, float* const* khd, double a_st, double ad_st, double* dadt, double* daddt) {
+// compute_inflation_rhs for one stage.  Inflation equations: launches the
+// kernel, reads the two sums back and forms dadt, daddt on the host
+// (src/evolution.cpp:500-511).  Post-inflation equations: enqueued; a'' from
+// a, a' (:596-597).
+static int rk_rhs(iegpu_ctx* c, const RkEq& E, const double* fs, const double* fds, const float* const* hs,
+                  const float* const* hds, double* kfd, float* const* khd, double a_st, double ad_st, double* dadt,
+                  double* daddt) {
     const double s = c->cfg.rescale_s, dx = c->cfg.L / (double)c->N;
+    const bool sig = c->cfg.sigw != 0;
+    RkSigw sg{};
+    for (int k = 0; k < 6 && sig; ++k) {
+        sg.hs[k] = hs[k];
+        sg.hds[k] = hds[k];
+        sg.khd[k] = khd[k];
+    }
+    if (E.post) {
+        const double omega = E.omega;
+        RkPostCoef K;
+        K.omega = omega;
+        K.laplnorm = pow(a_st, -2.0 * s) / (dx * dx);
+        K.scalar_friction = (3.0 * (1.0 + omega) + s) * ad_st / a_st;
+        K.tensor_friction = (2.0 + s) * ad_st / a_st;
+        const double Htilde = ad_st / a_st;
+        K.invH = 1.0 / Htilde;
+        K.coeffU = 4.0 / (3.0 * (1.0 + omega));
+        K.srcAmp = 2.0 * pow(a_st, -2.0 * s);
+        K.half_over_dx = 0.5 / dx;
+        K.inv_dx2 = 1.0 / (dx * dx);
+        K.den = 4.0 * dx * dx;
+        const unsigned grid = (unsigned)(c->gs / kThreads);
+        if (sig) k_rk_rhs_post<true><<<grid, kThreads, 0, c->stream>>>(fs, fds, kfd, sg, c->lg, K);
+        else k_rk_rhs_post<false><<<grid, kThreads, 0, c->stream>>>(fs, fds, kfd, sg, c->lg, K);
+        c->launches++;
+        *dadt = ad_st;
+        *daddt = -(s - 0.5 * (1.0 - 3.0 * omega)) * (ad_st * ad_st) / a_st;
+        return IEGPU_OK;
+    }
     RkCoef K;
     K.laplnorm = pow(a_st, -2.0 * s) / (dx * dx);
     K.friction = (2.0 + s) * ad_st / a_st;
     K.potnorm = pow(a_st, 2.0 - 2.0 * s);
     K.srcAmp = 2.0 * pow(a_st, -2.0 * s);
     K.half_over_dx = 0.5 / dx;
-    RkSigw sg{};
-    for (int k = 0; k < 6 && c->cfg.sigw; ++k) {
-        sg.hs[k] = hs[k];
-        sg.hds[k] = hds[k];
-        sg.khd[k] = khd[k];
-    }
-    const bool tab = c->pot.table != 0, sig = c->cfg.sigw != 0;
+    const bool tab = c->pot.table != 0;
     const dim3 g(c->red_grid), b(kThreads);
     if (tab && sig) k_rk_rhs<true, true><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
     else if (tab) k_rk_rhs<true, false><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
     else if (sig) k_rk_rhs<false, true><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
     else k_rk_rhs<false, false><<<g, b, 0, c->stream>>>(fs, fds, kfd, sg, c->pot, c->ctl, c->part, c->counter, c->misc, c->lg, K);
     c->launches++;
-    if (check_cuda(c, cudaMemcpyAsync(c->misc_h, c->misc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "RK4 sums"))
+    if (check_cuda(c, cudaMemcpyAsync(c->misc_h, c->misc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "RK sums"))
         return IEGPU_ECUDA;
-    if (check_cuda(c, cudaMemcpyAsync(&c->ctl_h->error, &c->ctl->error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "RK4 status"))
+    if (check_cuda(c, cudaMemcpyAsync(&c->ctl_h->error, &c->ctl->error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "RK status"))
         return IEGPU_ECUDA;
-    if (sync_and_check(c, "RK4 stage")) return IEGPU_ECUDA;
+    if (sync_and_check(c, "RK stage")) return IEGPU_ECUDA;
     if (c->ctl_h->error) return read_ctl(c);
     const double gradient_sum = -c->misc_h[0];
     const double potential_sum = c->misc_h[1];
@@ -939,29 +1151,48 @@ static void rk_combine(iegpu_ctx* c, const RkBufs& B, const double* coef, int nq
     c->launches++;
 }
 
-// rk4_step_inflation(h): four right-hand sides, three stage states, the
-// weighted update of the lattice and of (a, ad), then t += h.  ad2 is not
-// touched.
-static int rk4_step(iegpu_ctx* c, const RkBufs& B, double h, iegpu_bg* bg) {
-    double* f = c->f[c->cur];
-    float* hcur[6] = {};
-    for (int k = 0; k < 6 && c->cfg.sigw; ++k) hcur[k] = c->h[c->cur][k];
-    double ka[4] = {0.0, 0.0, 0.0, 0.0}, kad[4] = {0.0, 0.0, 0.0, 0.0};
-    if (int rc = rk_rhs(c, f, B.fd[0], hcur, B.hd[0], B.kfd[0], B.khd[0], bg->a, bg->ad, &ka[0], &kad[0])) return rc;
-    for (int stage = 1; stage < 4; ++stage) {
-        rk_combine(c, B, kRk4A[stage], stage, f, c->fd, B.f, B.fd[stage], hcur, c->hd, B.h, B.hd[stage], h);
+struct RkState {
+    double* f;
+    float* h[6];
+};
+
+static RkState rk_state(iegpu_ctx* c) {
+    RkState S{};
+    S.f = c->f[c->cur];
+    for (int k = 0; k < 6 && c->cfg.sigw; ++k) S.h[k] = c->h[c->cur][k];
+    return S;
+}
+
+// The stages 1..nst-1 of a tableau after the stage-0 derivatives
+// (evaluate_inflation_stage, src/evolution.cpp:692-715).
+static int rk_stages(iegpu_ctx* c, const RkEq& E, const RkBufs& B, const double (*A)[kRkMax], int nst, double h,
+                     const iegpu_bg* bg, double* ka, double* kad) {
+    const RkState S = rk_state(c);
+    for (int stage = 1; stage < nst; ++stage) {
+        rk_combine(c, B, A[stage], stage, S.f, c->fd, B.f, B.fd[stage], S.h, c->hd, B.h, B.hd[stage], h);
         double a_st = bg->a, ad_st = bg->ad;
         for (int q = 0; q < stage; ++q) {
-            const double cq = kRk4A[stage][q];
+            const double cq = A[stage][q];
             if (cq == 0.0) continue;
             a_st += h * cq * ka[q];
             ad_st += h * cq * kad[q];
         }
-        if (int rc = rk_rhs(c, B.f, B.fd[stage], B.h, B.hd[stage], B.kfd[stage], B.khd[stage], a_st, ad_st, &ka[stage],
-                            &kad[stage]))
+        if (int rc = rk_rhs(c, E, B.f, B.fd[stage], B.h, B.hd[stage], B.kfd[stage], B.khd[stage], a_st, ad_st,
+                            &ka[stage], &kad[stage]))
             return rc;
     }
-    rk_combine(c, B, kRk4B, 4, f, c->fd, f, c->fd, hcur, c->hd, hcur, c->hd, h);
+    return IEGPU_OK;
+}
+
+// rk4_step_inflation(h): four right-hand sides, three stage states, the
+// weighted update of the lattice and of (a, ad), then t += h.  ad2 is not
+// touched.
+static int rk4_step(iegpu_ctx* c, const RkEq& E, const RkBufs& B, double h, iegpu_bg* bg) {
+    const RkState S = rk_state(c);
+    double ka[kRkMax] = {0.0}, kad[kRkMax] = {0.0};
+    if (int rc = rk_rhs(c, E, S.f, B.fd[0], S.h, B.hd[0], B.kfd[0], B.khd[0], bg->a, bg->ad, &ka[0], &kad[0])) return rc;
+    if (int rc = rk_stages(c, E, B, kRk4A, 4, h, bg, ka, kad)) return rc;
+    rk_combine(c, B, kRk4B, 4, S.f, c->fd, S.f, c->fd, S.h, c->hd, S.h, c->hd, h);
     for (int q = 0; q < 4; ++q) {
         const double bq = kRk4B[q];
         if (bq == 0.0) continue;
@@ -972,8 +1203,140 @@ static int rk4_step(iegpu_ctx* c, const RkBufs& B, double h, iegpu_bg* bg) {
     return IEGPU_OK;
 }
 
-static int rk_begin(iegpu_ctx* c, const iegpu_bg* bg, RkBufs& B) {
-    if (int rc = rk_bufs(c, B)) return rc;
+// sanitize_rk45_controls, src/runtime_parameters.cpp:184-192
+static iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_controls* in) {
+    iegpu_rk45_controls K = *in;
+    const double dt = fabs(c->cfg.dt);
+    if (!(K.min_dt > 0.0)) K.min_dt = dt * 1e-6;
+    if (!(K.max_dt > 0.0)) K.max_dt = dt;
+    if (K.min_dt <= 0.0) K.min_dt = 1e-16;
+    if (K.max_dt < K.min_dt) K.max_dt = K.min_dt;
+    if (!(K.abs_tol > 0.0)) K.abs_tol = 1e-8;
+    if (!(K.rel_tol > 0.0)) K.rel_tol = 1e-6;
+    if (!(K.safety > 0.0 && K.safety < 1.0)) K.safety = 0.9;
+    return K;
+}
+
+// clamp_rk45_step, src/evolution.cpp:326-332
+static double rk45_clamp(const iegpu_rk45_controls& K, double h, double hmax) {
+    const double hmin = ref_max(1e-16, K.min_dt);
+    const double hhi = ref_max(hmin, hmax);
+    if (h < hmin) return hmin;
+    if (h > hhi) return hhi;
+    return h;
+}
+
+// rk45_hmax_from_base_step, src/evolution.cpp:341-343
+static double rk45_hmax(const iegpu_rk45_controls& K, double base_step) {
+    return ref_min(K.max_dt, ref_max(K.min_dt, 2.0 * base_step));
+}
+
+// rk45_step_inflation(h, hmax, h_next), src/evolution.cpp:781-904: seven
+// right-hand sides, the candidate and its error norm; on acceptance the
+// candidate becomes the state.
+static int rk45_attempt(iegpu_ctx* c, const RkEq& E, const RkBufs& B, const iegpu_rk45_controls& K, double h,
+                        double hmax, double* h_next, int* accepted, iegpu_bg* bg) {
+    const RkState S = rk_state(c);
+    const bool sig = c->cfg.sigw != 0;
+    double ka[kRkMax] = {0.0}, kad[kRkMax] = {0.0};
+    if (int rc = rk_rhs(c, E, S.f, B.fd[0], S.h, B.hd[0], B.kfd[0], B.khd[0], bg->a, bg->ad, &ka[0], &kad[0])) return rc;
+    if (int rc = rk_stages(c, E, B, kDpA, kRkMax, h, bg, ka, kad)) return rc;
+    double a5 = bg->a, ad5 = bg->ad, erra = 0.0, errad = 0.0;
+    for (int q = 0; q < kRkMax; ++q) {
+        const double bs = kDpB[q], es = kDpE[q];
+        if (bs != 0.0) {
+            a5 += h * bs * ka[q];
+            ad5 += h * bs * kad[q];
+        }
+        if (es != 0.0) {
+            erra += h * es * ka[q];
+            errad += h * es * kad[q];
+        }
+    }
+    Rk45Fin F{};
+    for (int q = 0; q < kRkMax; ++q) {
+        F.kf[q] = B.fd[q];
+        F.kfd[q] = B.kfd[q];
+        for (int k = 0; k < 6 && sig; ++k) {
+            F.kh[q][k] = B.hd[q][k];
+            F.khd[q][k] = B.khd[q][k];
+        }
+        F.b[q] = kDpB[q];
+        F.e[q] = kDpE[q];
+    }
+    for (int k = 0; k < 6 && sig; ++k) {
+        F.hs[k] = S.h[k];
+        F.hds[k] = c->hd[k];
+        F.y5h[k] = B.h[k];
+        F.y5hd[k] = B.y5hd[k];
+    }
+    F.y5f = B.f;
+    F.y5fd = B.y5fd;
+    F.h = h;
+    F.atol = K.abs_tol;
+    F.rtol = K.rel_tol;
+    if (sig) k_rk45_final<true><<<c->red_grid, kThreads, 0, c->stream>>>(S.f, c->fd, F, c->part, c->counter, c->misc, (long long)c->gs);
+    else k_rk45_final<false><<<c->red_grid, kThreads, 0, c->stream>>>(S.f, c->fd, F, c->part, c->counter, c->misc, (long long)c->gs);
+    c->launches++;
+    if (check_cuda(c, cudaMemcpyAsync(c->misc_h, c->misc, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "RK45 error"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "RK45 error")) return IEGPU_ECUDA;
+    double err_acc = c->misc_h[0];
+    size_t nvars = 2 * c->gs + 2;
+    if (sig) nvars += 12 * c->gs;
+    const double sa = K.abs_tol + K.rel_tol * ref_max(fabs(bg->a), fabs(a5));
+    const double sad = K.abs_tol + K.rel_tol * ref_max(fabs(bg->ad), fabs(ad5));
+    err_acc += (erra / sa) * (erra / sa) + (errad / sad) * (errad / sad);
+    const double err_norm = sqrt(err_acc / (double)nvars);
+    const double safe_err = ref_max(err_norm, 1e-16);
+    double factor = K.safety * pow(safe_err, -0.2);
+    factor = (factor < 0.1) ? 0.1 : (5.0 < factor) ? 5.0 : factor;
+    if (err_norm <= 1.0) {
+        const size_t bytes = sizeof(double) * c->gs;
+        cudaError_t e = cudaMemcpyAsync(S.f, B.f, bytes, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->fd, B.y5fd, bytes, cudaMemcpyDeviceToDevice, c->stream);
+        for (int k = 0; k < 6 && sig && e == cudaSuccess; ++k) {
+            e = cudaMemcpyAsync(S.h[k], B.h[k], bytes / 2, cudaMemcpyDeviceToDevice, c->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(c->hd[k], B.y5hd[k], bytes / 2, cudaMemcpyDeviceToDevice, c->stream);
+        }
+        if (check_cuda(c, e, "RK45 accept")) return IEGPU_ECUDA;
+        bg->a = a5;
+        bg->ad = ad5;
+        bg->t += h;
+        *h_next = rk45_clamp(K, h * factor, hmax);
+        *accepted = 1;
+        return IEGPU_OK;
+    }
+    *h_next = rk45_clamp(K, h * ref_max(0.1, ref_min(0.5, factor)), hmax);
+    *accepted = 0;
+    return IEGPU_OK;
+}
+
+// rk45_accept_step, src/evolution.cpp:345-363: attempts until one is
+// accepted; fails after 25 rejections or at the minimum step, with the
+// reference's message.  *h: in, the step to try; out, the step proposed for
+// the next one.
+static int rk45_accept(iegpu_ctx* c, const RkEq& E, const RkBufs& B, const iegpu_rk45_controls& K, double* h,
+                       double hmax, iegpu_bg* bg) {
+    int accepted = 0, attempts = 0;
+    while (!accepted) {
+        double hs = *h;
+        if (int rc = rk45_attempt(c, E, B, K, *h, hmax, &hs, &accepted, bg)) return rc;
+        *h = hs;
+        ++attempts;
+        if (!accepted && (attempts > 25 || *h <= K.min_dt * (1.0 + 1e-12))) {
+            if (E.post)
+                return set_error(c, IEGPU_ECONVERGE, "RK45 failed to converge in post-inflation at a=%e, t=%e (attempts=%d, h=%e)\n",
+                                 bg->a, bg->t, attempts, *h);
+            return set_error(c, IEGPU_ECONVERGE, "RK45 failed to converge at a=%e, t=%e (attempts=%d, h=%e)\n", bg->a,
+                             bg->t, attempts, *h);
+        }
+    }
+    return IEGPU_OK;
+}
+
+static int rk_begin(iegpu_ctx* c, const iegpu_bg* bg, int nst, RkBufs& B) {
+    if (int rc = rk_bufs(c, nst, B)) return rc;
     fill_ctl(c, bg, kModeLeapfrog);
     c->ctl_h->st.active = 0;
     c->ctl_h->done = 1;
@@ -982,8 +1345,8 @@ static int rk_begin(iegpu_ctx* c, const iegpu_bg* bg, RkBufs& B) {
 
 int fp64_rk4_step(iegpu_ctx* c, double h, iegpu_bg* bg) {
     RkBufs B;
-    if (int rc = rk_begin(c, bg, B)) return rc;
-    if (int rc = rk4_step(c, B, h, bg)) return rc;
+    if (int rc = rk_begin(c, bg, 4, B)) return rc;
+    if (int rc = rk4_step(c, RkEq{false, 0.0}, B, h, bg)) return rc;
     return sync_and_check(c, "RK4 step");
 }
 
@@ -994,14 +1357,14 @@ int fp64_rk4_step(iegpu_ctx* c, double h, iegpu_bg* bg) {
 int fp64_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, double* a_trace) {
     if (steps) *steps = 0;
     RkBufs B;
-    if (int rc = rk_begin(c, bg, B)) return rc;
+    if (int rc = rk_begin(c, bg, 4, B)) return rc;
     const double s = c->cfg.rescale_s;
     int n = 0;
     while (n < max_steps) {
         if (n > 0) bg->astep = bg->a;
         if (!(bg->a <= af)) break;
         const double d = c->cfg.dt * pow(bg->astep, s - 1.0);
-        if (int rc = rk4_step(c, B, d, bg)) {
+        if (int rc = rk4_step(c, RkEq{false, 0.0}, B, d, bg)) {
             if (steps) *steps = n;
             return rc;
         }
@@ -1010,6 +1373,86 @@ int fp64_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps, d
     }
     if (steps) *steps = n;
     return sync_and_check(c, "RK4");
+}
+
+int fp64_rk45_step(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double h, double hmax, double* h_next, int* accepted,
+                   iegpu_bg* bg) {
+    RkBufs B;
+    if (int rc = rk_begin(c, bg, kRkMax, B)) return rc;
+    const iegpu_rk45_controls K = rk45_sanitized(c, ctl);
+    if (int rc = rk45_attempt(c, RkEq{false, 0.0}, B, K, h, hmax, h_next, accepted, bg)) return rc;
+    return sync_and_check(c, "RK45 step");
+}
+
+// The RK45 branch of run_evolution_loop, src/evolution.cpp:958-985: while
+// a <= af, hmax from dt astep^(s-1), h clamped to it, then accepted attempts
+// (rk45_accept_step) and "astep = a".  *h carries the proposed step from one
+// step (and call) to the next.
+int fp64_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af, int max_steps, double* h, iegpu_bg* bg,
+              int* steps, double* a_trace) {
+    if (steps) *steps = 0;
+    RkBufs B;
+    if (int rc = rk_begin(c, bg, kRkMax, B)) return rc;
+    const iegpu_rk45_controls K = rk45_sanitized(c, ctl);
+    const double s = c->cfg.rescale_s;
+    int n = 0;
+    while (n < max_steps) {
+        if (n > 0) bg->astep = bg->a;
+        if (!(bg->a <= af)) break;
+        const double hmax = rk45_hmax(K, c->cfg.dt * pow(bg->astep, s - 1.0));
+        *h = rk45_clamp(K, *h, hmax);
+        if (int rc = rk45_accept(c, RkEq{false, 0.0}, B, K, h, hmax, bg)) {
+            if (steps) *steps = n;
+            return rc;
+        }
+        if (a_trace) a_trace[n] = bg->a;
+        ++n;
+    }
+    if (steps) *steps = n;
+    return sync_and_check(c, "RK45");
+}
+
+// The RK4 and RK45 branches of run_post_inflation_loop,
+// src/evolution.cpp:1606-1641: the post-inflation equations, steps of
+// dt_post (RK4) or adaptive steps with hmax from dt_post (RK45) while
+// a <= af_post.
+int fp64_post_rk4(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg, int* steps,
+                  double* a_trace) {
+    if (steps) *steps = 0;
+    RkBufs B;
+    if (int rc = rk_begin(c, bg, 4, B)) return rc;
+    int n = 0;
+    while (n < max_steps && bg->a <= af_post) {
+        if (int rc = rk4_step(c, RkEq{true, omega}, B, dt_post, bg)) {
+            if (steps) *steps = n;
+            return rc;
+        }
+        if (a_trace) a_trace[n] = bg->a;
+        ++n;
+    }
+    if (steps) *steps = n;
+    return sync_and_check(c, "post-inflation RK4");
+}
+
+int fp64_post_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af_post, double dt_post, double omega,
+                   int max_steps, double* h, iegpu_bg* bg, int* steps, double* a_trace) {
+    if (steps) *steps = 0;
+    RkBufs B;
+    if (int rc = rk_begin(c, bg, kRkMax, B)) return rc;
+    const iegpu_rk45_controls K = rk45_sanitized(c, ctl);
+    int n = 0;
+    while (n < max_steps && bg->a <= af_post) {
+        const double hmax = rk45_hmax(K, dt_post);
+        *h = rk45_clamp(K, *h, hmax);
+        if (int rc = rk45_accept(c, RkEq{true, omega}, B, K, h, hmax, bg)) {
+            if (steps) *steps = n;
+            return rc;
+        }
+        if (a_trace) a_trace[n] = bg->a;
+        ++n;
+    }
+    if (steps) *steps = n;
+    return sync_and_check(c, "post-inflation RK45");
 }
 
 }  // namespace iegpu

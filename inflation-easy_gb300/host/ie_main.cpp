@@ -1,8 +1,8 @@
 // ie_main.cpp -- host program of the GB300 InflationEasy engine.
 //
 // The reference's driver (src/main.cpp:103-146), leapfrog loops
-// (src/evolution.cpp:909-997, 1291-1375, 1561-1653) and the RK4 inflation
-// loop (src/evolution.cpp:948-956), initial conditions
+// (src/evolution.cpp:909-997, 1291-1375, 1561-1653), the RK4 and RK45
+// inflation and post-inflation loops (:948-985, 1606-1641), initial conditions
 // (src/initialize.cpp) and output routines (src/output.cpp), with every
 // lattice operation sent through the C ABI of include/iegpu.h.  It reads
 // params.txt from the working directory and writes results/ in the
@@ -126,6 +126,10 @@ void load_vector(const std::string& filename, std::vector<double>& vec) {
 // ---- scalar evolution pieces ------------------------------------------------
 
 double rescaled_step(double astep) { return P.dt * std::pow(astep, P.rescale_s - 1.0); }
+
+iegpu_rk45_controls rk45_controls() {
+    return {P.rk45_abs_tol, P.rk45_rel_tol, P.rk45_min_dt, P.rk45_max_dt, P.rk45_safety};
+}
 
 void evolve_fields(double d) { ck(iegpu_evolve_fields(G, d, &bg)); }
 
@@ -522,18 +526,22 @@ void output_parameters(bool first) {
 
 // run_evolution_loop, leapfrog and RK4 branches (src/evolution.cpp:909-997).
 // The device runs the steps between two outputs in one call.  Only the
-// leapfrog has the half drifts before and after the loop.
+// leapfrog has the half drifts before and after the loop; RK45 carries its
+// proposed step h from one call to the next.
 void run_evolution_loop() {
     int numsteps = 0;
     const bool leap = P.inflation_integrator == IE_LEAPFROG;
     if (leap) evolve_fields(0.5 * P.dt);
+    const iegpu_rk45_controls ctl = rk45_controls();
+    double h45 = rescaled_step(bg.astep);   // clamped by the library, src/evolution.cpp:959
     std::vector<double> trace;
     while (bg.a <= P.af) {
         const int chunk = P.output_freq - numsteps % P.output_freq;
         trace.assign((size_t)chunk, 0.0);
         int taken = 0;
         if (leap) ck(iegpu_leapfrog(G, P.af, chunk, &bg, &taken, trace.data()));
-        else ck(iegpu_rk4(G, P.af, chunk, &bg, &taken, trace.data()));
+        else if (P.inflation_integrator == IE_RK4) ck(iegpu_rk4(G, P.af, chunk, &bg, &taken, trace.data()));
+        else ck(iegpu_rk45(G, &ctl, P.af, chunk, &h45, &bg, &taken, trace.data()));
         for (int s = 0; s < taken; ++s) {
             numsteps++;
             double a_now = trace[(size_t)s];
@@ -633,11 +641,13 @@ void run_deltaN_loop() {
     evolve_fieldsN(-0.5 * P.dN);
 }
 
-// save_post_inflation(), src/output.cpp:1840-1865 (leapfrog: staggered)
+// save_post_inflation(), src/output.cpp:1840-1865 (the sync is the
+// leapfrog's: post_inflation_uses_staggered_derivatives, src/main.h:193-195)
 void save_post(int infrequent) {
     if (g_trace)
         std::fprintf(g_trace, "savep %d %.17g %.17g %.17g %.17g %.17g\n", infrequent, bg.t, bg.a, bg.ad, bg.ad2, bg.astep);
-    if (bg.t > 0.) evolve_fields(-.5 * P.dt_post_inflation);
+    const bool sync = P.post_inflation_integrator == IE_LEAPFROG && bg.t > 0.;
+    if (sync) evolve_fields(-.5 * P.dt_post_inflation);
     meansvars(1);
     scale(1);
     if (infrequent) {
@@ -648,10 +658,11 @@ void save_post(int infrequent) {
         }
         if (P.output_histogram) histogram_out(IEGPU_F, out_file("histogram", 1), out_file("histogramtimes", 1), false);
     }
-    if (bg.t > 0.) evolve_fields(.5 * P.dt_post_inflation);
+    if (sync) evolve_fields(.5 * P.dt_post_inflation);
 }
 
-// run_post_inflation_loop, leapfrog branch (src/evolution.cpp:1561-1653),
+
+// run_post_inflation_loop, leapfrog, RK4 and RK45 branches (src/evolution.cpp:1561-1653),
 // with initialize_post_inflation (src/initialize.cpp:245-290).  The device
 // runs the steps between two outputs in one call.
 void run_post_inflation_loop() {
@@ -663,14 +674,24 @@ void run_post_inflation_loop() {
     ck(iegpu_initialize_post_inflation(G, P.horizon_factor, P.omega, P.perform_deltaN, &bg));
     save_post(1);
     int numsteps = 0;
-    evolve_fields(0.5 * P.dt_post_inflation);
+    const int integ = P.post_inflation_integrator;
+    if (integ == IE_LEAPFROG) evolve_fields(0.5 * P.dt_post_inflation);
+    const iegpu_rk45_controls ctl = rk45_controls();
+    double h45 = P.dt_post_inflation;   // clamped by the library, src/evolution.cpp:1617
     std::vector<double> trace;
     while (bg.a <= P.af_post_inflation) {
         const int chunk = P.output_freq - numsteps % P.output_freq;
         trace.assign((size_t)chunk, 0.0);
         int taken = 0;
-        ck(iegpu_post_inflation_leapfrog(G, P.af_post_inflation, P.dt_post_inflation, P.omega, chunk, &bg, &taken,
-                                         trace.data()));
+        if (integ == IE_LEAPFROG)
+            ck(iegpu_post_inflation_leapfrog(G, P.af_post_inflation, P.dt_post_inflation, P.omega, chunk, &bg, &taken,
+                                             trace.data()));
+        else if (integ == IE_RK4)
+            ck(iegpu_post_inflation_rk4(G, P.af_post_inflation, P.dt_post_inflation, P.omega, chunk, &bg, &taken,
+                                        trace.data()));
+        else
+            ck(iegpu_post_inflation_rk45(G, &ctl, P.af_post_inflation, P.dt_post_inflation, P.omega, chunk, &h45, &bg,
+                                         &taken, trace.data()));
         for (int s = 0; s < taken; ++s) {
             numsteps++;
             double a_now = trace[(size_t)s];
@@ -731,19 +752,15 @@ int main(int argc, char** argv) {
     ie_params_load(P, params_path);
     if (P.seed < 1)
         std::printf("Warning: The parameter seed has been set to %d, which will result in incorrect output.\n", P.seed);
-    if (P.inflation_integrator == IE_RK45)
-        fatal("The rk45 inflation integrator is not provided by this engine (leapfrog and rk4 are).\n");
-    if (P.inflation_integrator == IE_RK4 && P.form != 0)
-        fatal("the rk4 inflation integrator runs on the plain FP64 form (form = fp64)\n");
+    if (P.inflation_integrator != IE_LEAPFROG && P.form != 0)
+        fatal("the %s inflation integrator runs on the plain FP64 form (form = fp64)\n",
+              ie_integrator_name(P.inflation_integrator));
     if (P.perform_deltaN && P.deltaN_integrator != IE_LEAPFROG)
         fatal("Only the leapfrog deltaN integrator is provided by this engine (got %s).\n",
               ie_integrator_name(P.deltaN_integrator));
     if (P.forcing_cutoff && P.high_cutoff_index > 0) fatal("forcing_cutoff is not provided by this engine.\n");
     if (P.post_inflation && !P.calculate_SIGW) fatal("post_inflation requires calculate_SIGW = 1\n");
     if (P.post_inflation && P.form != 0) fatal("the post-inflation phase runs on the plain FP64 form (form = fp64)\n");
-    if (P.post_inflation && P.post_inflation_integrator != IE_LEAPFROG)
-        fatal("Only the leapfrog post-inflation integrator is provided by this engine (got %s).\n",
-              ie_integrator_name(P.post_inflation_integrator));
     if (P.output_bispectrum || P.output_LOG)
         std::fprintf(stderr, "Ignoring output_bispectrum / output_LOG: not provided by this engine.\n");
     struct stat st;

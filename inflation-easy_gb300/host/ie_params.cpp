@@ -152,9 +152,11 @@ bool ie_params_load(IeParams& p, const char* path) {
             if (!parse_integrator(v, p.post_inflation_integrator))
                 std::fprintf(stderr, "Ignoring invalid post_inflation_integrator '%s' on line %d.\n", v.c_str(), line_of[k]);
         }
-        else if (k.rfind("rk45_", 0) == 0) {
-            // accepted for compatibility; the RK45 integrators are not part of this engine
-        }
+        else if (k == "rk45_abs_tol" && to_double(v, d)) p.rk45_abs_tol = d;
+        else if (k == "rk45_rel_tol" && to_double(v, d)) p.rk45_rel_tol = d;
+        else if (k == "rk45_min_dt" && to_double(v, d)) p.rk45_min_dt = d;
+        else if (k == "rk45_max_dt" && to_double(v, d)) p.rk45_max_dt = d;
+        else if (k == "rk45_safety" && to_double(v, d)) p.rk45_safety = d;
         else if (k == "output_freq" && to_int(v, i)) p.output_freq = i;
         else if (k == "output_infrequent_freq" && to_int(v, i)) p.output_infrequent_freq = i;
         else if (k == "dN" && to_double(v, d)) p.dN = d;

@@ -65,6 +65,13 @@ struct IeParams {
     double dt_post_inflation = 0.001;
     double af_post_inflation = 0.0;   // 2N unless given
     int post_inflation_integrator = IE_LEAPFROG;
+    // RK45 controls (src/runtime_parameters.cpp:82-86); non-positive steps
+    // mean the reference's defaults, applied by the library
+    double rk45_abs_tol = 1e-8;
+    double rk45_rel_tol = 1e-6;
+    double rk45_min_dt = -1.0;
+    double rk45_max_dt = -1.0;
+    double rk45_safety = 0.9;
 };
 
 // Defaults of the reference for the given potential kind and N.

@@ -15,7 +15,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "libiegpu.so"
 
-OK, EINVAL, ECUDA, ERANGE, ENAN, ECOURANT, ENOMEM, ETABLE, EUNSUPPORTED, ETIMEOUT, ETOOBIG = range(11)
+OK, EINVAL, ECUDA, ERANGE, ENAN, ECOURANT, ENOMEM, ETABLE, EUNSUPPORTED, ETIMEOUT, ETOOBIG, ECONVERGE = range(12)
 POT_HILLTOP, POT_TABLE = 0, 1
 FORM_FP64, FORM_SPLIT = 0, 1
 CRIT_GENERIC, CRIT_MONOTONIC, CRIT_ANTIMONOTONIC = 0, 1, -1
@@ -34,6 +34,16 @@ class Config(C.Structure):
     _fields_ = [("N", C.c_int), ("potential", C.c_int), ("sigw", C.c_int), ("form", C.c_int),
                 ("criterion", C.c_int), ("L", C.c_double), ("dt", C.c_double), ("rescale_s", C.c_double),
                 ("rescale_B", C.c_double), ("V0", C.c_double), ("ns", C.c_double)]
+
+
+class Rk45Controls(C.Structure):
+    """iegpu_rk45_controls: the reference's rk45_* keys (non-positive min/max
+    steps and out-of-range values take the reference's defaults)."""
+    _fields_ = [("abs_tol", C.c_double), ("rel_tol", C.c_double), ("min_dt", C.c_double),
+                ("max_dt", C.c_double), ("safety", C.c_double)]
+
+    def __init__(self, abs_tol=1e-8, rel_tol=1e-6, min_dt=-1.0, max_dt=-1.0, safety=0.9):
+        super().__init__(abs_tol, rel_tol, min_dt, max_dt, safety)
 
 
 class Bg(C.Structure):
@@ -79,6 +89,10 @@ def load() -> C.CDLL:
         "iegpu_leapfrog": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
         "iegpu_rk4_step_inflation": (I, [P, D, C.POINTER(Bg)]),
         "iegpu_rk4": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
+        "iegpu_rk45_step_inflation": (I, [P, C.POINTER(Rk45Controls), D, D, dp, ip, C.POINTER(Bg)]),
+        "iegpu_rk45": (I, [P, C.POINTER(Rk45Controls), D, I, dp, C.POINTER(Bg), ip, dp]),
+        "iegpu_post_inflation_rk4": (I, [P, D, D, D, I, C.POINTER(Bg), ip, dp]),
+        "iegpu_post_inflation_rk45": (I, [P, C.POINTER(Rk45Controls), D, D, D, I, dp, C.POINTER(Bg), ip, dp]),
         "iegpu_energies": (I, [P, C.POINTER(Bg), dp]),
         "iegpu_means": (I, [P, dp]),
         "iegpu_bunch_davies": (I, [P, I, D, D, D, D, dp]),
@@ -246,6 +260,23 @@ class Lattice:
                                        None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
         return (steps.value, tr[:steps.value]) if trace else steps.value
 
+    def rk45_step_inflation(self, h: float, hmax: float, bg: Bg, controls: "Rk45Controls | None" = None):
+        """One RK45 attempt: (accepted, h_next)."""
+        hn, acc = C.c_double(h), C.c_int(0)
+        self._check(self.lib.iegpu_rk45_step_inflation(self.h, C.byref(controls or Rk45Controls()), h, hmax,
+                                                       C.byref(hn), C.byref(acc), C.byref(bg)))
+        return bool(acc.value), hn.value
+
+    def rk45(self, af: float, max_steps: int, bg: Bg, h: float, controls: "Rk45Controls | None" = None,
+             trace: bool = False):
+        """RK45 steps while a <= af: (steps, h carried to the next call[, a trace])."""
+        steps, hh = C.c_int(0), C.c_double(h)
+        tr = np.zeros(max(1, max_steps), dtype=np.float64) if trace else None
+        self._check(self.lib.iegpu_rk45(self.h, C.byref(controls or Rk45Controls()), af, max_steps, C.byref(hh),
+                                        C.byref(bg), C.byref(steps),
+                                        None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
+        return (steps.value, hh.value, tr[:steps.value]) if trace else (steps.value, hh.value)
+
     def energies(self, bg: Bg):
         out = (C.c_double * 3)()
         self._check(self.lib.iegpu_energies(self.h, C.byref(bg), out))
@@ -272,6 +303,22 @@ class Lattice:
                                                            C.byref(steps),
                                                            None if tr is None else tr.ctypes.data_as(C.POINTER(C.c_double))))
         return (steps.value, tr[:steps.value]) if trace else steps.value
+
+    def post_inflation_rk4(self, af_post: float, dt_post: float, max_steps: int, bg: Bg,
+                           omega: float = 1.0 / 3.0) -> int:
+        steps = C.c_int(0)
+        self._check(self.lib.iegpu_post_inflation_rk4(self.h, af_post, dt_post, omega, max_steps, C.byref(bg),
+                                                      C.byref(steps), None))
+        return steps.value
+
+    def post_inflation_rk45(self, af_post: float, dt_post: float, max_steps: int, bg: Bg, h: float,
+                            omega: float = 1.0 / 3.0, controls: "Rk45Controls | None" = None):
+        """(steps, h carried to the next call)."""
+        steps, hh = C.c_int(0), C.c_double(h)
+        self._check(self.lib.iegpu_post_inflation_rk45(self.h, C.byref(controls or Rk45Controls()), af_post, dt_post,
+                                                       omega, max_steps, C.byref(hh), C.byref(bg), C.byref(steps),
+                                                       None))
+        return steps.value, hh.value
 
     def set_persistent(self, on: bool) -> None:
         self._check(self.lib.iegpu_set_persistent(self.h, int(bool(on))))

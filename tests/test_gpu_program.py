@@ -27,6 +27,7 @@ MAIN = PKG / "_build" / "ie_gpu_main"
 CASES = {
     "n16_hilltop": (16, 0, 0),
     "n16_hilltop_rk4": (16, 0, 0),   # inflation_integrator = rk4
+    "n16_hilltop_rk45": (16, 0, 0),  # inflation_integrator = rk45, dt = 0.05: the step control acts
     "n16_usr_sigw": (16, 1, 1),
     "n32_hilltop": (32, 0, 0),
 }
@@ -173,14 +174,16 @@ def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mo
         assert ca == cb
 
 
-def test_program_post_inflation_matches_reference_fixture(tmp_path):
-    """The program with the post-inflation phase on (16^3, USR, SIGW, deltaN)
-    against the reference program's own outputs of that phase
-    (tests/golden/n16_usr_sigw_post): results/post_inflation/* number by
-    number, and the final fields.  The phase starts from the deltaN map, which
-    the engine reproduces to round-off (its sums are re-associated), so the
-    tolerances are those of the inflation outputs above."""
-    src = GOLDEN / "n16_usr_sigw_post"
+@pytest.mark.parametrize("case", ["n16_usr_sigw_post", "n16_usr_sigw_post_rk45"])
+def test_program_post_inflation_matches_reference_fixture(case, tmp_path):
+    """The program with the post-inflation phase on (16^3, USR, SIGW, deltaN;
+    leapfrog, or RK45 with post_inflation_integrator = rk45) against the
+    reference program's own outputs of that phase (tests/golden/<case>):
+    results/post_inflation/* number by number, and the final fields.  The
+    phase starts from the deltaN map, which the engine reproduces to
+    round-off (its sums are re-associated), so the tolerances are those of
+    the inflation outputs above."""
+    src = GOLDEN / case
     text = (src / "params.txt").read_text() + "post_inflation = 1\n"
     wd = run_main(tmp_path, text, 16, 1, 1)
     names = sorted(x.name for x in (src / "results" / "post_inflation").iterdir())
