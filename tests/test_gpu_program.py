@@ -32,6 +32,13 @@ CASES = {
     "n32_hilltop": (32, 0, 0),
 }
 
+# Bounds for the final f (ulp) and the background trace (relative).  With the
+# RK45 step control acting, the embedded error estimate magnifies the
+# rounding of re-associated sums; the reference itself differs between its own
+# 1- and 8-thread runs of n16_hilltop_rk45 by 58626 ulp in f and 1.1e-9 in the
+# trace, so that case gets bounds above its own spread.
+BOUNDS = {"n16_hilltop_rk45": (1 << 17, 5e-9)}
+
 
 def run_main(tmp_path, params_text, N, numerical, sigw):
     wd = tmp_path / "gpu"
@@ -101,7 +108,8 @@ def test_program_matches_reference_fixtures(case, tmp_path):
     d = np.abs(got["f"] - ref)
     ulps = np.max(d / np.spacing(np.abs(ref)))
     print(f"{case} f: max dev {np.max(d):.3e} = {ulps:.0f} ulp of f, std {np.std(ref):.3e}")
-    assert ulps < 4096
+    max_ulps, trace_rel = BOUNDS.get(case, (4096, 1e-10))
+    assert ulps < max_ulps
     # fd ends the deltaN stage in e-fold units, near zero at many sites, so it
     # is compared against its own spread
     ref = ref_state["fd"]
@@ -130,7 +138,7 @@ def test_program_matches_reference_fixtures(case, tmp_path):
                 worst_ad2 = max(worst_ad2, abs(u - v) / max(abs(u), 1e-300))
                 assert abs(u - v) <= 1e-6 * abs(u) + 1e-300, (x, y)
             else:
-                assert abs(u - v) <= 1e-10 * abs(u) + 1e-300, (x, y)
+                assert abs(u - v) <= trace_rel * abs(u) + 1e-300, (x, y)
     print(f"{case} ad2: max rel dev {worst_ad2:.3e}")
 
 

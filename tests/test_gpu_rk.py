@@ -11,6 +11,15 @@ leapfrog parity:
   * t, a, ad: relative 1e-12; the RK45 step carried between steps 1e-10
 The post-inflation equations have no lattice sums, so RK4 there is compared
 bit for bit.
+
+With a step large enough for the RK45 controller to act (dt = 0.05 below),
+the embedded error estimate is a near-cancelling combination of the stage
+derivatives, so the rounding of the re-associated sums reaches the proposed
+step at ~1e-10 relative and the trajectory follows.  The reference itself
+shows more than that between its own runs on 1 and 8 OpenMP threads (16^3
+hilltop, dt = 0.05, to a = 32: a differs by 5.5e-10 relative, f by 58626 ulp).
+Those cases use tolerances above that spread: scalars and the step 5e-9
+relative, fields 1e-9 of their largest magnitude.
 """
 from __future__ import annotations
 
@@ -42,14 +51,19 @@ def _oracle_loop(o, af, n):
     return taken
 
 
-def _close(engine, o, lat, bg, sigw, what):
+def _close(engine, o, lat, bg, sigw, what, controlled=False):
     s = o.scalars
-    assert abs(bg.a - s.a) <= 1e-12 * s.a, (what, bg.a, s.a)
-    assert abs(bg.ad - s.ad) <= 1e-12 * abs(s.ad), (what, bg.ad, s.ad)
-    assert abs(bg.t - s.t) <= 1e-12 * s.t, what
+    rs = 5e-9 if controlled else 1e-12
+    assert abs(bg.a - s.a) <= rs * s.a, (what, bg.a, s.a)
+    assert abs(bg.ad - s.ad) <= rs * abs(s.ad), (what, bg.ad, s.ad)
+    assert abs(bg.t - s.t) <= rs * s.t, what
     assert bg.ad2 == s.ad2, what
-    assert rel_field_err(lat.download(engine.F), o.f) < 1e-9, what
-    assert rel_field_err(lat.download(engine.FD), o.fd) < 1e-9, what
+    for field, ref in ((engine.F, o.f), (engine.FD, o.fd)):
+        got = lat.download(field)
+        if controlled:
+            assert np.max(np.abs(got - ref)) <= 1e-9 * np.max(np.abs(ref)), what
+        else:
+            assert rel_field_err(got, ref) < 1e-9, what
     if sigw:
         for c in range(6):
             assert rel_field_err(lat.download(engine.H(c)), o.h_(c)) < 1e-5, (what, c)
@@ -150,6 +164,8 @@ def test_rk45_matches_oracle(N, usr, sigw, extra, engine, oracle_mod, tables):
     ctl = _controls(engine, p)
     h0 = o.rescaled_step(o.scalars.astep)
     hg = ho = h0
+    controlled = "dt" in extra
+    rh = 5e-9 if controlled else 1e-10
     with lat:
         total = 0
         for n in (1, 59, 140):
@@ -158,8 +174,8 @@ def test_rk45_matches_oracle(N, usr, sigw, extra, engine, oracle_mod, tables):
             t_o, ho = _oracle_rk45(o, p.af, n, ho)
             assert taken == t_o, (taken, t_o)
             total += taken
-            assert abs(hg - ho) <= 1e-10 * ho, (hg, ho)
-            _close(engine, o, lat, bg, sigw, f"after {total} steps")
+            assert abs(hg - ho) <= rh * ho, (hg, ho)
+            _close(engine, o, lat, bg, sigw, f"after {total} steps", controlled)
             if taken < n:
                 break
 
@@ -176,14 +192,14 @@ def test_rk45_attempts_accept_and_reject(engine, oracle_mod):
         acc, hn = lat.rk45_step_inflation(0.1, 0.1, bg, ctl)
         acc_o, hn_o = o.rk45_step_inflation(0.1, 0.1)
         assert not acc and not acc_o
-        assert abs(hn - hn_o) <= 1e-12 * hn_o
+        assert abs(hn - hn_o) <= 5e-9 * hn_o
         assert np.array_equal(lat.download(engine.F), f0) and bg.a == o.scalars.a == 1.0
         # the proposed step is accepted
         acc, hn2 = lat.rk45_step_inflation(hn, 0.1, bg, ctl)
         acc_o, hn2_o = o.rk45_step_inflation(hn_o, 0.1)
         assert acc and acc_o
-        assert abs(hn2 - hn2_o) <= 1e-10 * hn2_o
-        _close(engine, o, lat, bg, False, "after one accepted attempt")
+        assert abs(hn2 - hn2_o) <= 5e-9 * hn2_o
+        _close(engine, o, lat, bg, False, "after one accepted attempt", controlled=True)
 
 
 def test_rk45_failure_to_converge_is_reported(engine, oracle_mod):
