@@ -303,6 +303,24 @@ int  iegpu_evolve_derivsN(struct iegpu_ctx* ctx, double d);
 /* nsteps iterations of { evolve_derivsN(dN); evolve_fieldsN(dN); } with each
  * site's state held in registers for the whole run. */
 int  iegpu_deltaN_steps(struct iegpu_ctx* ctx, double dN, int nsteps, double phiref);
+/* nsteps of rk4_step_deltaN(dN) (deltaN_integrator = rk4,
+ * src/evolution.cpp:1176-1188, 1324-1332): per site, four evaluations of
+ * compute_deltaN_rhs (:1063-1113) held in registers, then the weighted
+ * update of f, fd and deltaN; bg->a (with its constant derivative ad) and
+ * bg->t advance as apply_deltaN_weighted_update advances them.  Ne is the
+ * caller's (Ne += dN per step).  No half drift precedes or follows the loop
+ * for this integrator. */
+int  iegpu_deltaN_rk4_steps(struct iegpu_ctx* ctx, double dN, int nsteps, double phiref, iegpu_bg* bg);
+/* The RK45 branch of run_deltaN_loop, src/evolution.cpp:1334-1367: while
+ * *Ne <= Nend (at most max_steps steps), hmax from dN, *h clamped to it,
+ * rk45_step_deltaN attempts (:1190-1267) until one is accepted, then
+ * *Ne += *h with the step proposed for the next iteration, as the reference
+ * adds it.  *h carries that step between calls; the first call takes dN.
+ * Ne_trace (may be NULL, else max_steps entries) receives Ne after each step.
+ * After 25 rejections, or at the minimum step, it returns IEGPU_ECONVERGE
+ * with the reference's message. */
+int  iegpu_deltaN_rk45(struct iegpu_ctx* ctx, const iegpu_rk45_controls* ctl, double dN, double Nend, int max_steps,
+                       double phiref, double* h, double* Ne, iegpu_bg* bg, int* steps, double* Ne_trace);
 /* saveN() mean, src/output.cpp:1527-1537: sequential float accumulation of
  * deltaN over sites with deltaN <= cutoff, divided by N^3 in float. */
 int  iegpu_saveN_mean(struct iegpu_ctx* ctx, double cutoff, float* nmean);

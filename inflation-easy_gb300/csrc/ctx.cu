@@ -106,7 +106,7 @@ static void free_all(iegpu_ctx* c) {
     for (int q = 0; q < 6; ++q) {
         cudaFree(c->h[0][q]); cudaFree(c->h[1][q]); cudaFree(c->hd[q]); cudaFree(c->hny[q]); cudaFree(c->hdny[q]);
     }
-    cudaFree(c->rk_d); cudaFree(c->rk_h);
+    cudaFree(c->rk_d); cudaFree(c->rk_h); cudaFree(c->dn_y5);
     cudaFree(c->tab); cudaFree(c->tkey);
     cudaFree(c->ctl); cudaFree(c->part); cudaFree(c->counter); cudaFree(c->a_trace);
     cudaFree(c->spec_part); cudaFree(c->spec_cnt); cudaFree(c->misc);
@@ -780,6 +780,46 @@ int iegpu_deltaN_steps(iegpu_ctx* c, double dN, int nsteps, double phiref) {
     if (!c || nsteps < 0) return IEGPU_EINVAL;
     if (nsteps == 0) return IEGPU_OK;
     return deltaN_run(c, dN, nsteps, phiref, 1, 1);
+}
+
+static int deltaN_ready(iegpu_ctx* c) {
+    if (int rc = need_table(c)) return rc;
+    if (is_split(c) && !c->split_mat)
+        return set_error(c, IEGPU_EINVAL, "call iegpu_initializeN before the deltaN steps");
+    if (check_cuda(c, cudaMemsetAsync(&c->ctl->error, 0, sizeof(int), c->stream), "memset")) return IEGPU_ECUDA;
+    return IEGPU_OK;
+}
+
+static int deltaN_range_status(iegpu_ctx* c, int rc) {
+    if (!rc) rc = sync_and_check(c, "deltaN");
+    if (!rc) {
+        int e = 0;
+        cudaMemcpy(&e, &c->ctl->error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e) {
+            double v = 0;
+            cudaMemcpy(&v, &c->ctl->errval, sizeof(double), cudaMemcpyDeviceToHost);
+            rc = set_error(c, IEGPU_ERANGE, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n", v,
+                           c->htab_x.back(), c->htab_x.front());
+        }
+    }
+    return rc;
+}
+
+int iegpu_deltaN_rk4_steps(iegpu_ctx* c, double dN, int nsteps, double phiref, iegpu_bg* bg) {
+    if (!c || !bg || nsteps < 0) return IEGPU_EINVAL;
+    if (nsteps == 0) return IEGPU_OK;
+    if (int rc = deltaN_ready(c)) return rc;
+    return deltaN_range_status(c, deltaN_rk4(c, dN, nsteps, phiref, bg));
+}
+
+int iegpu_deltaN_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double dN, double Nend, int max_steps,
+                      double phiref, double* h, double* Ne, iegpu_bg* bg, int* steps, double* Ne_trace) {
+    if (!c || !ctl || !h || !Ne || !bg || max_steps < 0) return IEGPU_EINVAL;
+    if (steps) *steps = 0;
+    if (int rc = deltaN_ready(c)) return rc;
+    const int rc = deltaN_rk45(c, ctl, dN, Nend, max_steps, phiref, h, Ne, bg, steps, Ne_trace);
+    if (rc) return rc;
+    return deltaN_range_status(c, rc);
 }
 
 int iegpu_saveN_mean(iegpu_ctx* c, double cutoff, float* nmean) {

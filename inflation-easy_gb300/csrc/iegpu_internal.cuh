@@ -197,6 +197,7 @@ struct iegpu_ctx {
     double* rk_d = nullptr;
     float* rk_h = nullptr;
     int rk_nst = 0;   // stages the scratch is laid out for
+    double* dn_y5 = nullptr;   // deltaN RK45 candidate (f, fd, deltaN), allocated on first use
 
     // table (device copies, plus the host copy for scalar evaluations)
     std::vector<double> htab_x, htab_V, htab_dV;
@@ -290,6 +291,13 @@ int fp64_rk45_step(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double h, doubl
                    iegpu_bg* bg);
 int fp64_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af, int max_steps, double* h, iegpu_bg* bg,
               int* steps, double* a_trace);
+// RK45 controls and step clamps shared by the lattice and deltaN integrators
+iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_controls* in);
+double rk45_clamp(const iegpu_rk45_controls& K, double h, double hmax);
+double rk45_hmax(const iegpu_rk45_controls& K, double base_step);
+int deltaN_rk4(iegpu_ctx* c, double h, int nsteps, double phiref, iegpu_bg* bg);
+int deltaN_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double dN, double Nend, int max_steps, double phiref,
+                double* h, double* Ne, iegpu_bg* bg, int* steps, double* Ne_trace);
 int fp64_post_rk4(iegpu_ctx* c, double af_post, double dt_post, double omega, int max_steps, iegpu_bg* bg, int* steps,
                   double* a_trace);
 int fp64_post_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af_post, double dt_post, double omega,

@@ -22,6 +22,7 @@
 #include "iegpu_internal.cuh"
 #include "pot.cuh"
 #include "reduce.cuh"
+#include "rk_tableau.cuh"
 
 namespace iegpu {
 
@@ -835,7 +836,7 @@ __global__ void __launch_bounds__(kThreads) k_rk_rhs_post(const double* __restri
     }
 }
 
-constexpr int kRkMax = 7;
+constexpr int kRkMax = IE_RK_STAGES;
 
 // One row of a tableau: out = base + h sum_q c_q k_q over the nonzero c_q,
 // the sum started from 0.0 in q order (prepare_inflation_stage_state and
@@ -980,27 +981,11 @@ __global__ void __launch_bounds__(kThreads) k_rk45_final(const double* f, const 
     }
 }
 
-// RK4_A, RK4_B and the Dormand-Prince 5(4) tableau (src/evolution.cpp:366-414,
-// 601-637): the published coefficients, e = b - b*.
-#define IE_DP_B1 (35.0 / 384.0)
-#define IE_DP_B3 (500.0 / 1113.0)
-#define IE_DP_B4 (125.0 / 192.0)
-#define IE_DP_B5 (-2187.0 / 6784.0)
-#define IE_DP_B6 (11.0 / 84.0)
-static const double kRk4A[kRkMax][kRkMax] = {{0.0}, {0.5}, {0.0, 0.5}, {0.0, 0.0, 1.0}};
-static const double kRk4B[kRkMax] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
-static const double kDpA[kRkMax][kRkMax] = {
-    {0.0},
-    {1.0 / 5.0},
-    {3.0 / 40.0, 9.0 / 40.0},
-    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0},
-    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0},
-    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0},
-    {IE_DP_B1, 0.0, IE_DP_B3, IE_DP_B4, IE_DP_B5, IE_DP_B6}};
-static const double kDpB[kRkMax] = {IE_DP_B1, 0.0, IE_DP_B3, IE_DP_B4, IE_DP_B5, IE_DP_B6, 0.0};
-static const double kDpE[kRkMax] = {IE_DP_B1 - 5179.0 / 57600.0, 0.0, IE_DP_B3 - 7571.0 / 16695.0,
-                                    IE_DP_B4 - 393.0 / 640.0, IE_DP_B5 - -92097.0 / 339200.0,
-                                    IE_DP_B6 - 187.0 / 2100.0, -(1.0 / 40.0)};
+static const double kRk4A[kRkMax][kRkMax] = IE_RK4_A_INIT;
+static const double kRk4B[kRkMax] = IE_RK4_B_INIT;
+static const double kDpA[kRkMax][kRkMax] = IE_DP_A_INIT;
+static const double kDpB[kRkMax] = IE_DP_B_INIT;
+static const double kDpE[kRkMax] = IE_DP_E_INIT;
 
 struct RkBufs {
     double* f;                 // stage f; the RK45 candidate f
@@ -1204,7 +1189,7 @@ static int rk4_step(iegpu_ctx* c, const RkEq& E, const RkBufs& B, double h, iegp
 }
 
 // sanitize_rk45_controls, src/runtime_parameters.cpp:184-192
-static iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_controls* in) {
+iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_controls* in) {
     iegpu_rk45_controls K = *in;
     const double dt = fabs(c->cfg.dt);
     if (!(K.min_dt > 0.0)) K.min_dt = dt * 1e-6;
@@ -1218,7 +1203,7 @@ static iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_c
 }
 
 // clamp_rk45_step, src/evolution.cpp:326-332
-static double rk45_clamp(const iegpu_rk45_controls& K, double h, double hmax) {
+double rk45_clamp(const iegpu_rk45_controls& K, double h, double hmax) {
     const double hmin = ref_max(1e-16, K.min_dt);
     const double hhi = ref_max(hmin, hmax);
     if (h < hmin) return hmin;
@@ -1227,7 +1212,7 @@ static double rk45_clamp(const iegpu_rk45_controls& K, double h, double hmax) {
 }
 
 // rk45_hmax_from_base_step, src/evolution.cpp:341-343
-static double rk45_hmax(const iegpu_rk45_controls& K, double base_step) {
+double rk45_hmax(const iegpu_rk45_controls& K, double base_step) {
     return ref_min(K.max_dt, ref_max(K.min_dt, 2.0 * base_step));
 }
 

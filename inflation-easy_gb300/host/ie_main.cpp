@@ -2,7 +2,7 @@
 //
 // The reference's driver (src/main.cpp:103-146), leapfrog loops
 // (src/evolution.cpp:909-997, 1291-1375, 1561-1653), the RK4 and RK45
-// inflation and post-inflation loops (:948-985, 1606-1641), initial conditions
+// branches of the inflation, deltaN and post-inflation loops, initial conditions
 // (src/initialize.cpp) and output routines (src/output.cpp), with every
 // lattice operation sent through the C ABI of include/iegpu.h.  It reads
 // params.txt from the working directory and writes results/ in the
@@ -571,8 +571,11 @@ void run_evolution_loop() {
 // saveN(), src/output.cpp:1522-1560
 void saveN() {
     if (g_trace) std::fprintf(g_trace, "saveN %.17g %.17g %.17g %.17g\n", bg.t, bg.a, Ne, phiref);
-    if (bg.t > 0.) evolve_fieldsN(-.5 * P.dN);
-    const double cutoff = P.Nend - P.dN;
+    // the sync and the dN below Nend are the leapfrog's
+    // (deltaN_uses_staggered_derivatives, src/output.cpp:1523-1527)
+    const bool stag = P.deltaN_integrator == IE_LEAPFROG;
+    if (stag && bg.t > 0.) evolve_fieldsN(-.5 * P.dN);
+    const double cutoff = P.Nend - (stag ? P.dN : 0.0);
     float Nmean = 0.f;
     ck(iegpu_saveN_mean(G, cutoff, &Nmean));
     ck(iegpu_shift(G, IEGPU_DELTAN, (double)Nmean));
@@ -603,32 +606,57 @@ void saveN() {
         print_spectrum(sp, counts, f2, norm1, "spectrumN");
         std::fclose(sp);
     }
-    if (bg.t > 0.) evolve_fieldsN(.5 * P.dN);
+    if (stag && bg.t > 0.) evolve_fieldsN(.5 * P.dN);
 }
 
-// run_deltaN_loop, leapfrog branch (src/evolution.cpp:1291-1375).  All sites
-// are integrated on the device in one call per output interval; the scalar
-// recurrences (t, a, Ne) are replayed here.
+// run_deltaN_loop, leapfrog, RK4 and RK45 branches (src/evolution.cpp:1291-1375).
+// All sites are integrated on the device in one call per output interval.
+// The leapfrog's scalar recurrences (t, a, Ne) are replayed here; the RK
+// calls advance t and a themselves, and RK45 also advances Ne.
 void run_deltaN_loop() {
     std::printf("Starting deltaN calculation\n");
     std::fprintf(output_, "Starting deltaN calculation\n");
     int numsteps = 0;
     Ne = 0.0;
     ck(iegpu_initializeN(G, bg.a));
-    evolve_fieldsN(0.5 * P.dN);
+    const int integ = P.deltaN_integrator;
+    if (integ == IE_LEAPFROG) evolve_fieldsN(0.5 * P.dN);
     if (P.use_phiref_manual) phiref = P.phiref_manual_value;
     else ck(iegpu_get_phiref(G, &phiref));
     if (P.criterion == 0) (void)potential(phiref);  // range check, src/evolution.cpp:1305
-    while (Ne <= P.Nend) {
+    if (integ == IE_RK45) {
+        // src/evolution.cpp:1334-1367: Ne advances by the step proposed for
+        // the next iteration; the library returns Ne after every step
+        const iegpu_rk45_controls ctl = rk45_controls();
+        double h45 = P.dN;
+        std::vector<double> ne_trace;
+        while (Ne <= P.Nend) {
+            const int limit = P.output_freq - numsteps % P.output_freq;
+            ne_trace.assign((size_t)limit, 0.0);
+            int taken = 0;
+            ck(iegpu_deltaN_rk45(G, &ctl, P.dN, P.Nend, limit, phiref, &h45, &Ne, &bg, &taken, ne_trace.data()));
+            for (int s = 0; s < taken; ++s) {
+                numsteps++;
+                if (P.screen_updates && numsteps % P.output_freq == 0) std::printf("N = %f\n\n", ne_trace[(size_t)s]);
+                std::fprintf(output_, "N = %f\n\n", ne_trace[(size_t)s]);
+                if (numsteps % P.output_freq == 0) std::fflush(output_);
+            }
+            if (taken == 0) break;
+        }
+    }
+    while (integ != IE_RK45 && Ne <= P.Nend) {
         // steps until the next flush point, or until Ne passes Nend
         int n = 0;
         double Ne_try = Ne;
         const int limit = P.output_freq - numsteps % P.output_freq;
         while (Ne_try <= P.Nend && n < limit) { Ne_try += P.dN; ++n; }
-        ck(iegpu_deltaN_steps(G, P.dN, n, phiref));
+        if (integ == IE_LEAPFROG) ck(iegpu_deltaN_steps(G, P.dN, n, phiref));
+        else ck(iegpu_deltaN_rk4_steps(G, P.dN, n, phiref, &bg));
         for (int s = 0; s < n; ++s) {
-            bg.t += P.dN;
-            bg.a += P.dN * bg.ad;
+            if (integ == IE_LEAPFROG) {
+                bg.t += P.dN;
+                bg.a += P.dN * bg.ad;
+            }
             Ne += P.dN;
             numsteps++;
             if (P.screen_updates && numsteps % P.output_freq == 0) std::printf("N = %f\n\n", Ne);
@@ -638,7 +666,7 @@ void run_deltaN_loop() {
     }
     saveN();
     std::fflush(output_);
-    evolve_fieldsN(-0.5 * P.dN);
+    if (integ == IE_LEAPFROG) evolve_fieldsN(-0.5 * P.dN);
 }
 
 // save_post_inflation(), src/output.cpp:1840-1865 (the sync is the
@@ -755,9 +783,6 @@ int main(int argc, char** argv) {
     if (P.inflation_integrator != IE_LEAPFROG && P.form != 0)
         fatal("the %s inflation integrator runs on the plain FP64 form (form = fp64)\n",
               ie_integrator_name(P.inflation_integrator));
-    if (P.perform_deltaN && P.deltaN_integrator != IE_LEAPFROG)
-        fatal("Only the leapfrog deltaN integrator is provided by this engine (got %s).\n",
-              ie_integrator_name(P.deltaN_integrator));
     if (P.forcing_cutoff && P.high_cutoff_index > 0) fatal("forcing_cutoff is not provided by this engine.\n");
     if (P.post_inflation && !P.calculate_SIGW) fatal("post_inflation requires calculate_SIGW = 1\n");
     if (P.post_inflation && P.form != 0) fatal("the post-inflation phase runs on the plain FP64 form (form = fp64)\n");

@@ -91,6 +91,8 @@ def load() -> C.CDLL:
         "iegpu_rk4": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
         "iegpu_rk45_step_inflation": (I, [P, C.POINTER(Rk45Controls), D, D, dp, ip, C.POINTER(Bg)]),
         "iegpu_rk45": (I, [P, C.POINTER(Rk45Controls), D, I, dp, C.POINTER(Bg), ip, dp]),
+        "iegpu_deltaN_rk4_steps": (I, [P, D, I, D, C.POINTER(Bg)]),
+        "iegpu_deltaN_rk45": (I, [P, C.POINTER(Rk45Controls), D, D, I, D, dp, dp, C.POINTER(Bg), ip, dp]),
         "iegpu_post_inflation_rk4": (I, [P, D, D, D, I, C.POINTER(Bg), ip, dp]),
         "iegpu_post_inflation_rk45": (I, [P, C.POINTER(Rk45Controls), D, D, D, I, dp, C.POINTER(Bg), ip, dp]),
         "iegpu_energies": (I, [P, C.POINTER(Bg), dp]),
@@ -390,6 +392,18 @@ class Lattice:
 
     def evolve_derivsN(self, d: float) -> None:
         self._check(self.lib.iegpu_evolve_derivsN(self.h, d))
+
+    def deltaN_rk4_steps(self, dN: float, nsteps: int, phiref: float, bg: Bg) -> None:
+        """nsteps of rk4_step_deltaN; bg.a and bg.t advance, Ne is the caller's."""
+        self._check(self.lib.iegpu_deltaN_rk4_steps(self.h, dN, nsteps, phiref, C.byref(bg)))
+
+    def deltaN_rk45(self, dN: float, Nend: float, max_steps: int, phiref: float, h: float, Ne: float, bg: Bg,
+                    controls: "Rk45Controls | None" = None):
+        """The RK45 deltaN loop: (steps, h carried, Ne)."""
+        hh, ne, steps = C.c_double(h), C.c_double(Ne), C.c_int(0)
+        self._check(self.lib.iegpu_deltaN_rk45(self.h, C.byref(controls or Rk45Controls()), dN, Nend, max_steps,
+                                               phiref, C.byref(hh), C.byref(ne), C.byref(bg), C.byref(steps), None))
+        return steps.value, hh.value, ne.value
 
     def deltaN_steps(self, dN: float, nsteps: int, phiref: float) -> None:
         self._check(self.lib.iegpu_deltaN_steps(self.h, dN, nsteps, phiref))

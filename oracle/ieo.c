@@ -54,6 +54,7 @@ struct ieo_state {
     /* RK scratch (allocated on first use), src/evolution.cpp:288-321 */
     double *ftmp, *fdtmp, *kf[7], *kfd[7];
     float *htmp[6], *hdtmp[6], *kh[7][6], *khd[7][6];
+    double *dntmp, *kdn[7];   /* deltaN RK scratch (DeltaNRKScratch, src/evolution.cpp:1040-1059) */
     int rk_post;        /* post-inflation right-hand side (g_use_post_inflation_rhs) */
     double rk45_err;    /* error norm of the last RK45 attempt */
 };
@@ -329,7 +330,8 @@ void ieo_destroy(ieo_state* S) {
     for (int c = 0; c < 6; ++c) { free(S->h[c]); free(S->hd[c]); free(S->hny[c]); free(S->hdny[c]); }
     free(S->tphi); free(S->tV); free(S->tdV); free(S->lstart);
     free(S->ftmp); free(S->fdtmp);
-    for (int q = 0; q < 7; ++q) { free(S->kf[q]); free(S->kfd[q]); }
+    for (int q = 0; q < 7; ++q) { free(S->kf[q]); free(S->kfd[q]); free(S->kdn[q]); }
+    free(S->dntmp);
     for (int c = 0; c < 6; ++c) {
         free(S->htmp[c]); free(S->hdtmp[c]);
         for (int q = 0; q < 7; ++q) { free(S->kh[q][c]); free(S->khd[q][c]); }
@@ -1638,6 +1640,175 @@ double ieo_get_phiref(ieo_state* S) {
     return fref;
 }
 
+/* compute_deltaN_rhs, src/evolution.cpp:1063-1113: per site, in e-fold time,
+ * k_f = fd and k_dn = 1 at active sites (0 and 0 where the site has crossed
+ * the end surface), k_fd = -(3 - fd^2/2)(fd + V'/V) with V, V' as
+ * evaluate_potential_from_value gives them (divided by B^2 each, the hint
+ * stepped back by int_errN).  dadt = ad. */
+static int rkN_rhs(ieo_state* S, const double* fs, const double* fds, double* kf, double* kfd, double* kdn) {
+    const ieo_params* p = &S->p;
+    const double B2 = pw2(p->rescale_B);
+    const double Vref = ieo_potential(S, S->phiref);
+    for (size_t id = 0; id < S->gs; ++id) {
+        const double field = fs[id], deriv = fds[id];
+        double pot, dpot;
+        if (p->numerical_potential) {
+            const int l = bracket(S, field, S->lstart[id]);
+            if (l < 0) return 1;
+            pot = interp(S, field, l, S->tV) / B2;
+            dpot = interp(S, field, l, S->tdV) / B2;
+            const int back = p->int_errN > 1 ? p->int_errN : 1;
+            S->lstart[id] = (l - back) > 1 ? (l - back) : 1;
+        } else {
+            pot = hill_V(p, field);
+            dpot = hill_dV(p, field);
+        }
+        const double ratio = dpot / pot;
+        int active;
+        if (p->criterion > 0) active = fabs(field) > fabs(S->phiref);
+        else if (p->criterion < 0) active = fabs(field) < fabs(S->phiref);
+        else active = pot > Vref;
+        kfd[id] = -(3.0 - 0.5 * pw2(deriv)) * (deriv + ratio);
+        kf[id] = active ? deriv : 0.0;
+        kdn[id] = active ? 1.0 : 0.0;
+    }
+    return 0;
+}
+
+static void rkN_scratch(ieo_state* S) {
+    rk_scratch(S);
+    if (S->dntmp) return;
+    S->dntmp = (double*)calloc(S->gs, sizeof(double));
+    for (int q = 0; q < 7; ++q) S->kdn[q] = (double*)calloc(S->gs, sizeof(double));
+}
+
+/* evaluate_deltaN_stage with prepare_deltaN_stage_state, src/evolution.cpp:1115-1145 */
+static int rkN_stage(ieo_state* S, double h, int stage, const double (*A)[7]) {
+    for (size_t id = 0; id < S->gs; ++id) {
+        double sum_f = 0.0, sum_fd = 0.0, sum_dn = 0.0;
+        for (int q = 0; q < stage; ++q) {
+            const double c = A[stage][q];
+            if (c == 0.0) continue;
+            sum_f += c * S->kf[q][id];
+            sum_fd += c * S->kfd[q][id];
+            sum_dn += c * S->kdn[q][id];
+        }
+        S->ftmp[id] = S->f[id] + h * sum_f;
+        S->fdtmp[id] = S->fd[id] + h * sum_fd;
+        S->dntmp[id] = S->deltaN[id] + h * sum_dn;
+    }
+    return rkN_rhs(S, S->ftmp, S->fdtmp, S->kf[stage], S->kfd[stage], S->kdn[stage]);
+}
+
+/* rk4_step_deltaN(h), src/evolution.cpp:1176-1188, with
+ * apply_deltaN_weighted_update (:1147-1174): a moves with its constant
+ * derivative ad, t += h. */
+int ieo_rk4_step_deltaN(ieo_state* S, double h) {
+    rkN_scratch(S);
+    if (rkN_rhs(S, S->f, S->fd, S->kf[0], S->kfd[0], S->kdn[0])) return 1;
+    for (int stage = 1; stage < 4; ++stage)
+        if (rkN_stage(S, h, stage, RK4_A)) return 1;
+    for (size_t id = 0; id < S->gs; ++id) {
+        double sum_f = 0.0, sum_fd = 0.0, sum_dn = 0.0;
+        for (int q = 0; q < 4; ++q) {
+            const double bs = RK4_B[q];
+            if (bs == 0.0) continue;
+            sum_f += bs * S->kf[q][id];
+            sum_fd += bs * S->kfd[q][id];
+            sum_dn += bs * S->kdn[q][id];
+        }
+        S->f[id] += h * sum_f;
+        S->fd[id] += h * sum_fd;
+        S->deltaN[id] += h * sum_dn;
+    }
+    for (int q = 0; q < 4; ++q) {
+        const double bs = RK4_B[q];
+        if (bs == 0.0) continue;
+        S->a += h * bs * S->ad;
+    }
+    S->t += h;
+    return 0;
+}
+
+/* rk45_step_deltaN(h, hmax, h_next), src/evolution.cpp:1190-1267 */
+int ieo_rk45_step_deltaN(ieo_state* S, double h, double hmax, double* h_next, int* accepted) {
+    rkN_scratch(S);
+    const ieo_params* p = &S->p;
+    const double atol = p->rk45_abs_tol, rtol = p->rk45_rel_tol;
+    if (rkN_rhs(S, S->f, S->fd, S->kf[0], S->kfd[0], S->kdn[0])) return 1;
+    for (int stage = 1; stage < 7; ++stage)
+        if (rkN_stage(S, h, stage, DP_A)) return 1;
+    double a5 = S->a, erra = 0.0;
+    for (int q = 0; q < 7; ++q) {
+        if (DP_B[q] != 0.0) a5 += h * DP_B[q] * S->ad;
+        if (DP_E[q] != 0.0) erra += h * DP_E[q] * S->ad;
+    }
+    double err_acc = 0.0;
+    const size_t nvars = 3 * S->gs + 1;
+    for (size_t id = 0; id < S->gs; ++id) {
+        double y5f = S->f[id], y5fd = S->fd[id], y5dn = S->deltaN[id];
+        double errf = 0.0, errfd = 0.0, errdn = 0.0;
+        for (int q = 0; q < 7; ++q) {
+            const double bs = DP_B[q], es = DP_E[q];
+            if (bs != 0.0) {
+                y5f += h * bs * S->kf[q][id];
+                y5fd += h * bs * S->kfd[q][id];
+                y5dn += h * bs * S->kdn[q][id];
+            }
+            if (es != 0.0) {
+                errf += h * es * S->kf[q][id];
+                errfd += h * es * S->kfd[q][id];
+                errdn += h * es * S->kdn[q][id];
+            }
+        }
+        S->ftmp[id] = y5f;
+        S->fdtmp[id] = y5fd;
+        S->dntmp[id] = y5dn;
+        const double sf = atol + rtol * smax(fabs(S->f[id]), fabs(y5f));
+        const double sfd = atol + rtol * smax(fabs(S->fd[id]), fabs(y5fd));
+        const double sdn = atol + rtol * smax(fabs(S->deltaN[id]), fabs(y5dn));
+        err_acc += pw2(errf / sf) + pw2(errfd / sfd) + pw2(errdn / sdn);
+    }
+    const double sa = atol + rtol * smax(fabs(S->a), fabs(a5));
+    err_acc += pw2(erra / sa);
+    const double err_norm = sqrt(err_acc / (double)nvars);
+    const double safe_err = smax(err_norm, 1e-16);
+    double factor = p->rk45_safety * pow(safe_err, -0.2);
+    factor = (factor < 0.1) ? 0.1 : (5.0 < factor) ? 5.0 : factor;
+    S->rk45_err = err_norm;
+    if (err_norm <= 1.0) {
+        double* t;
+        t = S->f; S->f = S->ftmp; S->ftmp = t;
+        t = S->fd; S->fd = S->fdtmp; S->fdtmp = t;
+        t = S->deltaN; S->deltaN = S->dntmp; S->dntmp = t;
+        S->a = a5;
+        S->t += h;
+        *h_next = ieo_rk45_clamp(S, h * factor, hmax);
+        *accepted = 1;
+        return 0;
+    }
+    *h_next = ieo_rk45_clamp(S, h * smax(0.1, smin(0.5, factor)), hmax);
+    *accepted = 0;
+    return 0;
+}
+
+/* rk45_accept_step around rk45_step_deltaN, src/evolution.cpp:1338-1366 */
+int ieo_rk45_accept_deltaN(ieo_state* S, double* h, double hmax) {
+    int accepted = 0, attempts = 0;
+    while (!accepted) {
+        double hs = *h;
+        if (ieo_rk45_step_deltaN(S, *h, hmax, &hs, &accepted)) return 1;
+        *h = hs;
+        ++attempts;
+        if (!accepted && (attempts > 25 || *h <= S->p.rk45_min_dt * (1.0 + 1e-12))) {
+            set_err(S, "RK45 failed to converge in deltaN loop at N=%e, t=%e (attempts=%d, h=%e)\n", S->Ne, S->t,
+                    attempts, *h);
+            return 1;
+        }
+    }
+    return 0;
+}
+
 int ieo_deltaN_steps(ieo_state* S, int max_steps) {
     int n = 0;
     while (n < max_steps && S->Ne <= S->p.Nend) {
@@ -1983,8 +2154,10 @@ static void out_modes(ieo_state* S, outfiles* O) {
 static int out_saveN(ieo_state* S, outfiles* O) {
     const ieo_params* p = &S->p;
     if (g_trace) fprintf(g_trace, "saveN %.17g %.17g %.17g %.17g\n", S->t, S->a, S->Ne, S->phiref);
-    if (S->t > 0.) ieo_evolve_fieldsN(S, -.5 * p->dN);
-    const double cutoff = p->Nend - p->dN;
+    /* the sync and the dN below Nend are the leapfrog's (deltaN_uses_staggered_derivatives, src/output.cpp:1523-1527) */
+    const int stag = p->deltaN_integrator == 0;
+    if (stag && S->t > 0.) ieo_evolve_fieldsN(S, -.5 * p->dN);
+    const double cutoff = p->Nend - (stag ? p->dN : 0.0);
     const float Nmean = ieo_saveN_mean(S, cutoff);
     for (size_t id = 0; id < S->gs; ++id) S->deltaN[id] -= Nmean;
     out_histogram(S, S->deltaN, open_out(S, O, &O->histogramN, "histogramN"),
@@ -2009,7 +2182,7 @@ static int out_saveN(ieo_state* S, outfiles* O) {
         ieo_fftrn_d(S->deltaN, S->fny, p->N, -1);
         free(counts); free(f2);
     }
-    if (S->t > 0.) ieo_evolve_fieldsN(S, .5 * p->dN);
+    if (stag && S->t > 0.) ieo_evolve_fieldsN(S, .5 * p->dN);
     return S->err;
 }
 
@@ -2109,10 +2282,6 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
     S->t = S->t0;
 
     /* run_evolution_loop(), src/evolution.cpp:909-997 */
-    if (p->perform_deltaN && p->deltaN_integrator != 0) {
-        set_err(S, "the deltaN loop's RK integrators are not restated by this oracle\n");
-        goto done;
-    }
     {
         int numsteps = 0;
         const int leap = p->inflation_integrator == 0;
@@ -2145,25 +2314,37 @@ int ieo_run_program_dump(const ieo_params* p, const char* results_dir, const cha
         out_modes(S, &O);
     }
 
-    /* run_deltaN_loop(), leapfrog branch, src/evolution.cpp:1291-1375 */
+    /* run_deltaN_loop(), leapfrog, RK4 and RK45 branches, src/evolution.cpp:1291-1375 */
     if (p->perform_deltaN) {
         fprintf(O.output, "Starting deltaN calculation\n");
         int numsteps = 0;
+        const int nint = p->deltaN_integrator;
         S->Ne = 0.0;
         if (ieo_initializeN(S)) goto done;
-        ieo_evolve_fieldsN(S, 0.5 * p->dN);
+        if (nint == 0) ieo_evolve_fieldsN(S, 0.5 * p->dN);
         S->phiref = p->use_phiref_manual ? p->phiref_manual_value : ieo_get_phiref(S);
+        double hN = ieo_rk45_clamp(S, p->dN, p->rk45_max_dt);
         while (S->Ne <= p->Nend) {
-            if (ieo_evolve_derivsN(S, p->dN)) goto done;
-            ieo_evolve_fieldsN(S, p->dN);
-            S->Ne += p->dN;
+            if (nint == 0) {
+                if (ieo_evolve_derivsN(S, p->dN)) goto done;
+                ieo_evolve_fieldsN(S, p->dN);
+                S->Ne += p->dN;
+            } else if (nint == 1) {
+                if (ieo_rk4_step_deltaN(S, p->dN)) goto done;
+                S->Ne += p->dN;
+            } else {
+                const double hmax = ieo_rk45_hmax(S, p->dN);
+                hN = ieo_rk45_clamp(S, hN, hmax);
+                if (ieo_rk45_accept_deltaN(S, &hN, hmax)) goto done;
+                S->Ne += hN;   /* the step proposed for the next iteration, as the reference adds it */
+            }
             numsteps++;
             fprintf(O.output, "N = %f\n\n", S->Ne);
             if (numsteps % p->output_freq == 0) fflush(O.output);
         }
         if (out_saveN(S, &O)) goto done;
         fflush(O.output);
-        ieo_evolve_fieldsN(S, -0.5 * p->dN);
+        if (nint == 0) ieo_evolve_fieldsN(S, -0.5 * p->dN);
     }
     /* run_post_inflation_loop(), leapfrog, RK4 and RK45 branches, src/evolution.cpp:1561-1653 */
     if (p->post_inflation) {

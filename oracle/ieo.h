@@ -50,8 +50,7 @@ typedef struct {
     /* post-inflation phase (src/parameters.h:31 switch, src/runtime_parameters.cpp:48-52, 295-299) */
     int post_inflation, af_post_given;
     double horizon_factor, omega, dt_post_inflation, af_post_inflation;
-    /* integrators, src/runtime_parameters.cpp:141-166: 0 leapfrog, 1 rk4, 2 rk45 (the deltaN loop's RK
-     * branches are not restated) */
+    /* integrators, src/runtime_parameters.cpp:141-166: 0 leapfrog, 1 rk4, 2 rk45 */
     int inflation_integrator, pad_;
     int post_inflation_integrator, deltaN_integrator;
     /* RK45 controls, src/runtime_parameters.cpp:82-86, 184-192, 351-353 */
@@ -127,6 +126,10 @@ int ieo_rk45_step_inflation(ieo_state* S, double h, double hmax, double* h_next,
 int ieo_rk45_accept(ieo_state* S, double* h, double hmax);
 double ieo_rk45_clamp(const ieo_state* S, double h, double hmax);
 double ieo_rk45_hmax(const ieo_state* S, double base_step);
+/* the deltaN loop's RK4 step, RK45 attempt and accept driver, src/evolution.cpp:1063-1267, 1338-1366 */
+int ieo_rk4_step_deltaN(ieo_state* S, double h);
+int ieo_rk45_step_deltaN(ieo_state* S, double h, double hmax, double* h_next, int* accepted);
+int ieo_rk45_accept_deltaN(ieo_state* S, double* h, double hmax);
 /* selects the post-inflation right-hand side for the RK steps */
 void ieo_set_rk_post(ieo_state* S, int post);
 

@@ -90,6 +90,8 @@ def load() -> C.CDLL:
         "ieo_initialize_post_inflation": (None, [P]), "ieo_evolve_derivs_post_inflation": (None, [P, D]),
         "ieo_rk4_step_inflation": (I, [P, D]),
         "ieo_rk45_step_inflation": (I, [P, D, D, dp, ip]), "ieo_rk45_accept": (I, [P, dp, D]),
+        "ieo_rk4_step_deltaN": (I, [P, D]), "ieo_rk45_step_deltaN": (I, [P, D, D, dp, ip]),
+        "ieo_rk45_accept_deltaN": (I, [P, dp, D]),
         "ieo_rk45_clamp": (D, [P, D, D]), "ieo_rk45_hmax": (D, [P, D]), "ieo_set_rk_post": (None, [P, I]),
         "ieo_rescaled_step": (D, [P, D]), "ieo_leapfrog_steps": (I, [P, I]),
         "ieo_fftrn_d": (None, [dp, dp, I, I]), "ieo_fftrn_f": (None, [fp, fp, I, I]),
@@ -248,6 +250,19 @@ class Oracle:
         """rk45_accept_step: attempts until one is accepted; the next step's h."""
         hh = C.c_double(h)
         self._check(self.lib.ieo_rk45_accept(self.h, C.byref(hh), hmax))
+        return hh.value
+
+    def rk4_step_deltaN(self, h):
+        self._check(self.lib.ieo_rk4_step_deltaN(self.h, h))
+
+    def rk45_step_deltaN(self, h, hmax):
+        hn, acc = C.c_double(h), C.c_int(0)
+        self._check(self.lib.ieo_rk45_step_deltaN(self.h, h, hmax, C.byref(hn), C.byref(acc)))
+        return bool(acc.value), hn.value
+
+    def rk45_accept_deltaN(self, h, hmax):
+        hh = C.c_double(h)
+        self._check(self.lib.ieo_rk45_accept_deltaN(self.h, C.byref(hh), hmax))
         return hh.value
 
     def rk45_clamp(self, h, hmax):

@@ -48,6 +48,7 @@ CASES = {
     "n16_hilltop_rk45": (16, 0, 0, 1, 0, dict(HILLTOP, dt=0.05, inflation_integrator="rk45", rk45_abs_tol=1e-12,
                                               rk45_rel_tol=1e-10)),
     "n16_usr_sigw_post_rk45": (16, 1, 1, 1, 1, dict(USR, post_inflation_integrator="rk45")),
+    "n16_usr_dn_rk45": (16, 1, 0, 1, 0, dict(USR, deltaN_integrator="rk45")),
 }
 
 

@@ -29,6 +29,7 @@ CASES = {
     "n16_hilltop_rk4": (16, 0, 0),   # inflation_integrator = rk4
     "n16_hilltop_rk45": (16, 0, 0),  # inflation_integrator = rk45, dt = 0.05: the step control acts
     "n16_usr_sigw": (16, 1, 1),
+    "n16_usr_dn_rk45": (16, 1, 0),   # deltaN_integrator = rk45
     "n32_hilltop": (32, 0, 0),
 }
 

@@ -1,6 +1,7 @@
-"""The Runge-Kutta integrators on the plain FP64 form against the oracle:
-RK4 and RK45 (Dormand-Prince 5(4) with the reference's step control) for the
-inflation loop, and both for the post-inflation loop.
+"""The Runge-Kutta integrators against the oracle: RK4 and RK45
+(Dormand-Prince 5(4) with the reference's step control) for the inflation
+loop and the post-inflation loop on the plain FP64 form, and for the
+per-site deltaN loop.
 
 Every per-site expression of the stages, the weighted update and the RK45
 candidate is the reference's.  The inflation equations combine two lattice
@@ -9,8 +10,9 @@ different order from the reference, so the tolerances are those of the
 leapfrog parity:
   * fields: max|x_gpu - x_oracle| <= 1e-9 * std(x_oracle); h, h': 1e-5
   * t, a, ad: relative 1e-12; the RK45 step carried between steps 1e-10
-The post-inflation equations have no lattice sums, so RK4 there is compared
-bit for bit.
+The post-inflation and deltaN equations have no lattice sums, so RK4 there is
+compared bit for bit; deltaN RK45 differs only in the summation order of its
+error norm.
 
 With a step large enough for the RK45 controller to act (dt = 0.05 below),
 the embedded error estimate is a near-cancelling combination of the stage
@@ -283,3 +285,67 @@ def test_post_inflation_rk_needs_sigw(engine):
     with engine.Lattice(16, 10.0, 1e-3, 3.338e-13, sigw=False) as lat:
         with pytest.raises(engine.IegpuError):
             lat.post_inflation_rk4(2.0, 1e-3, 1, bg)
+
+
+def _deltaN_setup(ieo, engine, usr, tables, median_phiref):
+    from test_gpu_parity import oracle_state
+    p, o2 = oracle_state(ieo, 16, usr, False, tables, steps=30)
+    lat, bg = lattice_like(engine, p, o2, usr, False, tables)
+    lat.initializeN(o2.scalars.a)
+    o2.initializeN()
+    phiref = float(np.median(o2.f)) if median_phiref else lat.get_phiref()
+    s = o2.scalars
+    s.phiref = phiref
+    s.Ne = 0.0
+    o2.set_scalars(s)
+    return p, o2, lat, bg, phiref
+
+
+# (USR, end surface at the median field value: sites go inactive during the run)
+DN_CASES = [(False, False), (True, False), (True, True)]
+
+
+@pytest.mark.parametrize("usr,median", DN_CASES)
+def test_deltaN_rk4_bit_exact(usr, median, engine, oracle_mod, tables):
+    """The deltaN stages have no lattice sums: RK4 matches bit for bit."""
+    p, o, lat, bg, phiref = _deltaN_setup(oracle_mod, engine, usr, tables, median)
+    with lat:
+        for n in (1, 399):
+            lat.deltaN_rk4_steps(p.dN, n, phiref, bg)
+            for _ in range(n):
+                o.rk4_step_deltaN(p.dN)
+            for fld, ref in ((engine.F, o.f), (engine.FD, o.fd), (engine.DELTAN, o.deltaN)):
+                assert np.array_equal(lat.download(fld), ref)
+            s = o.scalars
+            assert (bg.t, bg.a) == (s.t, s.a)
+        if median:
+            dn = lat.download(engine.DELTAN)
+            assert 0 < np.count_nonzero(dn < dn.max()) < dn.size   # some sites stopped
+
+
+@pytest.mark.parametrize("usr,median", DN_CASES)
+def test_deltaN_rk45_matches_oracle(usr, median, engine, oracle_mod, tables):
+    """Per-site stages are bit-exact; only the error norm's summation order
+    differs, so the step control agrees to rounding."""
+    p, o, lat, bg, phiref = _deltaN_setup(oracle_mod, engine, usr, tables, median)
+    ctl = _controls(engine, p)
+    with lat:
+        hg = ho = p.dN
+        Ne = 0.0
+        for n in (1, 200):
+            steps, hg, Ne = lat.deltaN_rk45(p.dN, p.Nend, n, phiref, hg, Ne, bg, ctl)
+            taken = 0
+            while taken < n and o.scalars.Ne <= p.Nend:
+                hmax = o.rk45_hmax(p.dN)
+                ho = o.rk45_accept_deltaN(o.rk45_clamp(ho, hmax), hmax)
+                s = o.scalars
+                s.Ne += ho
+                o.set_scalars(s)
+                taken += 1
+            assert steps == taken
+            s = o.scalars
+            assert abs(hg - ho) <= 1e-12 * ho and abs(Ne - s.Ne) <= 1e-12 * s.Ne
+            assert abs(bg.a - s.a) <= 1e-12 * s.a and abs(bg.t - s.t) <= 1e-12 * s.t
+            for fld, ref in ((engine.F, o.f), (engine.FD, o.fd), (engine.DELTAN, o.deltaN)):
+                got = lat.download(fld)
+                assert np.max(np.abs(got - ref)) <= 1e-10 * np.max(np.abs(ref)), fld

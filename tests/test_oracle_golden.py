@@ -21,6 +21,7 @@ CASES = {
     "n16_hilltop_rk4": (16, False, False, False),
     "n16_hilltop_rk45": (16, False, False, False),
     "n16_usr_sigw_post_rk45": (16, True, True, True),
+    "n16_usr_dn_rk45": (16, True, False, False),
 }
 
 

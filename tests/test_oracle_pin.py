@@ -4,7 +4,7 @@ Runs only where the reference tree is available (it is read at build time by
 oracle/build_ref.py); elsewhere the committed golden fixtures
 (test_oracle_golden.py) carry the same check.  Configurations beyond the
 fixtures: hilltop with SIGW, USR without SIGW, USR at N = 32, and the RK4 /
-RK45 integrators of the inflation and post-inflation loops.
+RK45 integrators of the inflation, deltaN and post-inflation loops.
 """
 from __future__ import annotations
 
@@ -39,6 +39,10 @@ CASES = [
     (16, True, True, False, USR + "inflation_integrator = dopri5\nrk45_rel_tol = 1e-7\n"),
     (16, False, True, True, HILL + "post_inflation_integrator = rk4\n"),
     (16, True, True, True, USR + "post_inflation_integrator = rk45\n"),
+    (16, False, False, False, HILL + "deltaN_integrator = rk4\n"),
+    (16, True, False, False, USR + "deltaN_integrator = rk4\n"),
+    (16, False, False, False, HILL + "deltaN_integrator = rk45\n"),
+    (16, True, False, False, USR + "deltaN_integrator = rkf45\n"),
 ]
 
 
