@@ -81,6 +81,9 @@ typedef struct {
 typedef struct {
     double abs_tol, rel_tol, min_dt, max_dt, safety;
 } iegpu_rk45_controls;
+/* The controls the RK45 entry points use for base step dt: *out = the
+ * sanitised copy of *in described above.  Needs no context or device. */
+int  iegpu_rk45_effective(const iegpu_rk45_controls* in, double dt, iegpu_rk45_controls* out);
 
 /* Field selectors for upload/download/FFT/spectra. */
 #define IEGPU_F       0   /* phi             (f)        */

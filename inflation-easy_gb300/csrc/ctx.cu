@@ -562,6 +562,12 @@ int iegpu_rk4(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* steps_t
     return fp64_rk4(c, af, max_steps, bg, steps_taken, a_trace);
 }
 
+int iegpu_rk45_effective(const iegpu_rk45_controls* in, double dt, iegpu_rk45_controls* out) {
+    if (!in || !out) return IEGPU_EINVAL;
+    *out = rk45_sanitized_dt(in, dt);
+    return IEGPU_OK;
+}
+
 int iegpu_rk45_step_inflation(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double h, double hmax, double* h_next,
                               int* accepted, iegpu_bg* bg) {
     if (!c || !bg || !ctl || !h_next || !accepted) return IEGPU_EINVAL;

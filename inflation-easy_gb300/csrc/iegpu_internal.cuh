@@ -293,6 +293,7 @@ int fp64_rk45(iegpu_ctx* c, const iegpu_rk45_controls* ctl, double af, int max_s
               int* steps, double* a_trace);
 // RK45 controls and step clamps shared by the lattice and deltaN integrators
 iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_controls* in);
+iegpu_rk45_controls rk45_sanitized_dt(const iegpu_rk45_controls* in, double dt);
 double rk45_clamp(const iegpu_rk45_controls& K, double h, double hmax);
 double rk45_hmax(const iegpu_rk45_controls& K, double base_step);
 int deltaN_rk4(iegpu_ctx* c, double h, int nsteps, double phiref, iegpu_bg* bg);

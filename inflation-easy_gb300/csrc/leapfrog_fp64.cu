@@ -1190,8 +1190,12 @@ static int rk4_step(iegpu_ctx* c, const RkEq& E, const RkBufs& B, double h, iegp
 
 // sanitize_rk45_controls, src/runtime_parameters.cpp:184-192
 iegpu_rk45_controls rk45_sanitized(const iegpu_ctx* c, const iegpu_rk45_controls* in) {
+    return rk45_sanitized_dt(in, c->cfg.dt);
+}
+
+iegpu_rk45_controls rk45_sanitized_dt(const iegpu_rk45_controls* in, double dt_in) {
     iegpu_rk45_controls K = *in;
-    const double dt = fabs(c->cfg.dt);
+    const double dt = fabs(dt_in);
     if (!(K.min_dt > 0.0)) K.min_dt = dt * 1e-6;
     if (!(K.max_dt > 0.0)) K.max_dt = dt;
     if (K.min_dt <= 0.0) K.min_dt = 1e-16;

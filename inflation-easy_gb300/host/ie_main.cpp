@@ -11,6 +11,7 @@
 // iegpu_leapfrog, where the device advances them between host visits.
 //
 // Usage: ie_gpu_main [params.txt] [results_dir] [dump_dir]
+//        ie_gpu_main --check-params [params.txt]   (resolved parameters; no device)
 // dump_dir (optional) receives trace.txt (background scalars at each save),
 // precise.txt (printed means and spectra at full precision) and state.bin.
 #include <sys/stat.h>
@@ -24,6 +25,7 @@
 #include <ctime>
 #include <fstream>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ie_params.h"
@@ -769,7 +771,33 @@ void write_state(const std::string& path) {
 
 }  // namespace
 
+// --check-params: the run-time parameters after params.txt, the reference's
+// defaults and derived values, and the RK45 controls the library will use,
+// one "key value" line each (%.17g).  Touches no device.
+int check_params(const char* path) {
+    ie_params_load(P, path);
+    const iegpu_rk45_controls raw = rk45_controls();
+    iegpu_rk45_controls eff;
+    if (iegpu_rk45_effective(&raw, P.dt, &eff) != IEGPU_OK) return 1;
+    const std::pair<const char*, double> kv[] = {
+        {"N", P.N}, {"numerical_potential", P.numerical_potential}, {"perform_deltaN", P.perform_deltaN},
+        {"calculate_SIGW", P.calculate_SIGW}, {"criterion", P.criterion}, {"seed", P.seed},
+        {"rescale_s", P.rescale_s}, {"af", P.af}, {"V0", P.V0}, {"rescale_B", P.rescale_B}, {"ns", P.ns},
+        {"initial_field", P.initial_field}, {"initial_derivative", P.initial_derivative}, {"L", P.L},
+        {"dt", P.dt}, {"dx", P.dx}, {"output_freq", P.output_freq},
+        {"output_infrequent_freq", P.output_infrequent_freq}, {"dN", P.dN}, {"Nend", P.Nend},
+        {"post_inflation", P.post_inflation}, {"horizon_factor", P.horizon_factor}, {"omega", P.omega},
+        {"dt_post_inflation", P.dt_post_inflation}, {"af_post_inflation", P.af_post_inflation},
+        {"inflation_integrator", P.inflation_integrator}, {"deltaN_integrator", P.deltaN_integrator},
+        {"post_inflation_integrator", P.post_inflation_integrator}, {"rk45_abs_tol", eff.abs_tol},
+        {"rk45_rel_tol", eff.rel_tol}, {"rk45_min_dt", eff.min_dt}, {"rk45_max_dt", eff.max_dt},
+        {"rk45_safety", eff.safety}};
+    for (const auto& e : kv) std::printf("%s %.17g\n", e.first, e.second);
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc > 1 && std::string(argv[1]) == "--check-params") return check_params(argc > 2 ? argv[2] : "params.txt");
     const char* params_path = argc > 1 ? argv[1] : "params.txt";
     if (argc > 2) RES = argv[2];
     std::string dump_dir = argc > 3 ? argv[3] : "";

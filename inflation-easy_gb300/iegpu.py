@@ -89,6 +89,7 @@ def load() -> C.CDLL:
         "iegpu_leapfrog": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
         "iegpu_rk4_step_inflation": (I, [P, D, C.POINTER(Bg)]),
         "iegpu_rk4": (I, [P, D, I, C.POINTER(Bg), ip, dp]),
+        "iegpu_rk45_effective": (I, [C.POINTER(Rk45Controls), D, C.POINTER(Rk45Controls)]),
         "iegpu_rk45_step_inflation": (I, [P, C.POINTER(Rk45Controls), D, D, dp, ip, C.POINTER(Bg)]),
         "iegpu_rk45": (I, [P, C.POINTER(Rk45Controls), D, I, dp, C.POINTER(Bg), ip, dp]),
         "iegpu_deltaN_rk4_steps": (I, [P, D, I, D, C.POINTER(Bg)]),
