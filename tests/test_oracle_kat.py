@@ -130,3 +130,131 @@ def test_homogeneous_background_matches_scalar_leapfrog(oracle_mod):
     assert np.isclose(sc.a, a, rtol=1e-13)
     assert np.allclose(o.f, phi, rtol=1e-13)
     assert np.allclose(o.fd, dphi, rtol=1e-12)
+
+
+def _hilltop_V(p):
+    B2 = p.rescale_B ** 2
+    V = lambda v: p.V0 * (1.0 - (1.0 - p.ns) / 4.0 * v * v) / B2
+    dV = lambda v: -p.V0 * (1.0 - p.ns) / 2.0 * v / B2
+    return V, dV
+
+
+def test_rk4_inflation_background_is_fourth_order(oracle_mod):
+    """With no fluctuations, rk4_step_inflation integrates the homogeneous
+    system f'' = -(2 a'/a) f' - a^2 V'(f), a'' = a^3 V(f) - a'^2/a (s = 0).
+    Against a tight independent solution its error falls by ~2^4 when the
+    step halves."""
+    solve_ivp = pytest.importorskip("scipy.integrate").solve_ivp
+    N = 8
+    p = oracle_mod.hilltop_params(N, inflation_integrator=1)
+    V, dV = _hilltop_V(p)
+    phi0, dphi0 = 0.0935, 0.000796
+    ad0 = np.sqrt((0.5 * dphi0 ** 2 + V(phi0)) / 3.0)
+    T = 1.0   # conformal time (s = 0): a ~ 1/(1 - H t) blows up near t = 1.7
+
+    def rhs(_, y):
+        f, fd, a, ad = y
+        return [fd, -(2.0 * ad / a) * fd - a * a * dV(f), ad, a ** 3 * V(f) - ad * ad / a]
+
+    exact = solve_ivp(rhs, (0.0, T), [phi0, dphi0, 1.0, ad0], method="DOP853", rtol=1e-13, atol=1e-15).y[:, -1]
+    errs = []
+    for h in (0.1, 0.05, 0.025):
+        o = oracle_mod.Oracle(p)
+        o.f[:] = phi0
+        o.fd[:] = dphi0
+        s = o.scalars
+        s.t, s.a, s.ad = 0.0, 1.0, ad0
+        o.set_scalars(s)
+        for _ in range(int(round(T / h))):
+            o.rk4_step_inflation(h)
+        got = np.array([o.f[0], o.fd[0], o.scalars.a, o.scalars.ad])
+        assert np.all(o.f == o.f[0]) and np.all(o.fd == o.fd[0])
+        errs.append(np.max(np.abs(got - exact) / np.abs(exact)))
+    r1, r2 = errs[0] / errs[1], errs[1] / errs[2]
+    assert 12.0 < r1 < 20.0 and 12.0 < r2 < 20.0, errs
+
+
+def test_rk45_inflation_background_meets_its_tolerance(oracle_mod):
+    """rk45 on the same homogeneous system: accepted steps stay within a small
+    multiple of the requested relative tolerance of the tight solution."""
+    solve_ivp = pytest.importorskip("scipy.integrate").solve_ivp
+    p = oracle_mod.hilltop_params(8, inflation_integrator=2, rk45_rel_tol=1e-9, rk45_abs_tol=1e-12,
+                                  rk45_max_dt=0.5)
+    V, dV = _hilltop_V(p)
+    phi0, dphi0 = 0.0935, 0.000796
+    ad0 = np.sqrt((0.5 * dphi0 ** 2 + V(phi0)) / 3.0)
+
+    def rhs(_, y):
+        f, fd, a, ad = y
+        return [fd, -(2.0 * ad / a) * fd - a * a * dV(f), ad, a ** 3 * V(f) - ad * ad / a]
+
+    o = oracle_mod.Oracle(p)
+    o.f[:] = phi0
+    o.fd[:] = dphi0
+    s = o.scalars
+    s.t, s.a, s.ad = 0.0, 1.0, ad0
+    o.set_scalars(s)
+    h, hmax = 0.1, 0.5
+    for _ in range(40):
+        h = o.rk45_accept(o.rk45_clamp(h, hmax), hmax)
+    T = o.scalars.t
+    exact = solve_ivp(rhs, (0.0, T), [phi0, dphi0, 1.0, ad0], method="DOP853", rtol=1e-13, atol=1e-15).y[:, -1]
+    got = np.array([o.f[0], o.fd[0], o.scalars.a, o.scalars.ad])
+    assert np.max(np.abs(got - exact) / np.abs(exact)) < 1e-7
+
+
+def test_rk4_deltaN_site_matches_an_independent_solution(oracle_mod):
+    """One deltaN site in e-fold time, f' = fd, fd' = -(3 - fd^2/2)(fd + V'/V),
+    while active: rk4_step_deltaN on a homogeneous lattice against a tight
+    solution, fourth order, and deltaN = N_e for a site that never stops."""
+    solve_ivp = pytest.importorskip("scipy.integrate").solve_ivp
+    p = oracle_mod.hilltop_params(8)          # antimonotonic: active while |f| < |phiref|
+    V, dV = _hilltop_V(p)
+    f0, fd0, Ntot = 0.0935, 0.02, 0.8
+
+    def rhs(_, y):
+        f, fd = y
+        return [fd, -(3.0 - 0.5 * fd * fd) * (fd + dV(f) / V(f))]
+
+    exact = solve_ivp(rhs, (0.0, Ntot), [f0, fd0], method="DOP853", rtol=1e-13, atol=1e-16).y[:, -1]
+    errs = []
+    for h in (0.1, 0.05, 0.025):
+        o = oracle_mod.Oracle(p)
+        o.f[:] = f0
+        o.fd[:] = fd0
+        o.deltaN[:] = 0.0
+        s = o.scalars
+        s.phiref = 10.0
+        o.set_scalars(s)
+        n = int(round(Ntot / h))
+        for _ in range(n):
+            o.rk4_step_deltaN(h)
+        errs.append(max(abs(o.f[0] - exact[0]) / abs(exact[0]), abs(o.fd[0] - exact[1]) / abs(exact[1])))
+        assert np.allclose(o.deltaN, n * h, rtol=1e-13)
+    r1, r2 = errs[0] / errs[1], errs[1] / errs[2]
+    assert 12.0 < r1 < 20.0 and 12.0 < r2 < 20.0, errs
+
+
+def test_post_inflation_rk_radiation_background_is_linear(oracle_mod):
+    """Radiation era (omega = 1/3, s = 0): a'' = 0, so with a homogeneous
+    lattice a(t) = 1 + a'_0 t and a' stays exact under RK4 and RK45."""
+    for integ in (1, 2):
+        p = oracle_mod.hilltop_params(8, calculate_SIGW=1, post_inflation=1, post_inflation_integrator=integ)
+        o = oracle_mod.Oracle(p)
+        o.f[:] = 0.01
+        o.fd[:] = 0.0
+        s = o.scalars
+        s.t, s.a, s.ad = 0.0, 1.0, 5.0
+        o.set_scalars(s)
+        o.set_rk_post(True)
+        h = 1e-3
+        for _ in range(100):
+            if integ == 1:
+                o.rk4_step_inflation(h)
+            else:
+                h = o.rk45_accept(o.rk45_clamp(h, 2e-3), 2e-3)
+        sc = o.scalars
+        assert sc.ad == 5.0
+        assert abs(sc.a - (1.0 + 5.0 * sc.t)) <= 1e-13 * sc.a
+        # the 7-point Laplacian of a constant is a rounding residue, not 0
+        assert np.allclose(o.f, 0.01, rtol=1e-15) and np.max(np.abs(o.fd)) < 1e-15
