@@ -511,6 +511,17 @@ void output_parameters(bool first) {
         if (P.perform_deltaN) std::fprintf(info, "deltaN_integrator=%s\n", ie_integrator_name(P.deltaN_integrator));
         if (P.post_inflation)
             std::fprintf(info, "post_inflation_integrator=%s\n", ie_integrator_name(P.post_inflation_integrator));
+        const bool rk45 = P.inflation_integrator == IE_RK45 ||
+                          (P.perform_deltaN && P.deltaN_integrator == IE_RK45) ||
+                          (P.post_inflation && P.post_inflation_integrator == IE_RK45);
+        if (rk45) {
+            // the controls in effect (src/output.cpp:1435-1448)
+            const iegpu_rk45_controls raw = rk45_controls();
+            iegpu_rk45_controls k;
+            iegpu_rk45_effective(&raw, P.dt, &k);
+            std::fprintf(info, "rk45_abs_tol=%e\nrk45_rel_tol=%e\nrk45_min_dt=%e\nrk45_max_dt=%e\nrk45_safety=%e\n",
+                         k.abs_tol, k.rel_tol, k.min_dt, k.max_dt, k.safety);
+        }
         std::fprintf(info, "rescale_s=%f\nrescale_B=%e\n", P.rescale_s, P.rescale_B);
         std::fprintf(info, "engine=iegpu %d (GB300, %s)\n", iegpu_version(), P.form ? "split FP32" : "plain FP64");
         time(&tstart);
