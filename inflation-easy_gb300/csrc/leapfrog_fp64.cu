@@ -1,4 +1,5 @@
-// leapfrog_fp64.cu -- plain FP64 leapfrog of src/evolution.cpp:150-284.
+// leapfrog_fp64.cu -- plain FP64 leapfrog of src/evolution.cpp:150-284, and the
+// other integrators of the plain FP64 state.
 //
 // Compiled with -fmad=false: every per-site expression is evaluated with the
 // reference's operation order and rounding (no contraction), so a site given
@@ -15,6 +16,11 @@
 //             h += (float)(d hd) (src/evolution.cpp:170-281).
 // Algorithmic HBM traffic per site-update: 40 B (read f twice, fd; write f, fd),
 // 32 B of which are the reference's own state update.
+//
+// The same unit holds the other integrators of the plain FP64 state, with the
+// same per-site rules: the post-inflation leapfrog (src/evolution.cpp:1378-1653)
+// and the Runge-Kutta steps (RK4, RK45) of the inflation and post-inflation
+// loops (src/evolution.cpp:286-905).
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
