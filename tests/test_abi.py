@@ -55,3 +55,30 @@ def test_no_cpu_fallback_without_gpu(engine):
         pass
     with pytest.raises(engine.IegpuError):
         engine.Lattice(16, 10.0, 1e-3, 3.338e-13)
+
+
+def test_rk_entry_points_reject_null_arguments(engine):
+    """The Runge-Kutta entry points check their arguments before any device
+    call: a null context returns IEGPU_EINVAL."""
+    lib = engine.load()
+    bg = engine.Bg(0.0, 1.0, 1.0, 0.0, 1.0)
+    ctl = engine.Rk45Controls()
+    h, ne, out = C.c_double(1e-3), C.c_double(0.0), C.c_double()
+    steps, acc = C.c_int(), C.c_int()
+    calls = [
+        lambda: lib.iegpu_rk4(None, 2.0, 1, C.byref(bg), C.byref(steps), None),
+        lambda: lib.iegpu_rk4_step_inflation(None, 1e-3, C.byref(bg)),
+        lambda: lib.iegpu_rk45(None, C.byref(ctl), 2.0, 1, C.byref(h), C.byref(bg), C.byref(steps), None),
+        lambda: lib.iegpu_rk45_step_inflation(None, C.byref(ctl), 1e-3, 1e-3, C.byref(out), C.byref(acc),
+                                              C.byref(bg)),
+        lambda: lib.iegpu_deltaN_rk4_steps(None, 1e-4, 1, 0.0, C.byref(bg)),
+        lambda: lib.iegpu_deltaN_rk45(None, C.byref(ctl), 1e-4, 1.0, 1, 0.0, C.byref(h), C.byref(ne), C.byref(bg),
+                                      C.byref(steps), None),
+        lambda: lib.iegpu_post_inflation_rk4(None, 2.0, 1e-3, 1.0 / 3.0, 1, C.byref(bg), C.byref(steps), None),
+        lambda: lib.iegpu_post_inflation_rk45(None, C.byref(ctl), 2.0, 1e-3, 1.0 / 3.0, 1, C.byref(h), C.byref(bg),
+                                              C.byref(steps), None),
+    ]
+    for call in calls:
+        assert call() == engine.EINVAL
+    assert lib.iegpu_rk45_effective(None, 1e-3, C.byref(ctl)) == engine.EINVAL
+    assert lib.iegpu_strerror(engine.ECONVERGE).decode().startswith("RK45")
