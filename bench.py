@@ -10,12 +10,17 @@ state (384 MB in FP64) is larger than L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
-The headline value is the split form (FP32 perturbations about an FP64
-background); the plain FP64 form is measured on the same workload and reported
-under "forms".  forms.batched is the ensemble form: 512 x 32^3 + 64 x 64^3 +
-8 x 128^3 lattices with the USR table potential advanced together, with the
-same number of steps of one lattice of each size alone as the sequential
-comparison (lattices/s ratio for equal work), and its deltaN stage.
+The headline value is the plain FP64 form, the reference's own precision and
+per-site arithmetic (like for like with the reference arm).  Beside it, under
+"forms": the split form (FP32 perturbations about an FP64 background) on the
+same workload with its error statement against the FP64 form over a whole run
+(inflation to af = 512 and the deltaN stage: P_dphi and P_zeta per k-bin,
+<dphi^2>, H(t) at every save); the batched ensemble (512 x 32^3 + 64 x 64^3 +
+8 x 128^3 lattices, USR table potential, advanced together, against the same
+number of steps of one lattice of each size alone, and its deltaN stage); the
+SIGW split step at 256^3 and 512^3 with the Omega_GW comparison against the
+FP64 form; the post-inflation phase; the FFT + binning, deltaN and RK4
+kernels.
 
 --impl reference times the reference's own CPU algorithm for the same step
 (the oracle port of it, oracle/ieo.c, OpenMP on all host cores; the reference
@@ -52,7 +57,11 @@ METRIC = "site-updates/s at 256^3: FP64 plain vs split-FP32 vs batched; % of HBM
 UNIT = "site-updates/s"
 # algorithmic HBM bytes per site of the dominant kernel of one step
 BYTES_STEP_SPLIT = 16  # split form: read dphi, dpi; write dphi, dpi (FP32)
-BYTES_KICK_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
+BYTES_STEP_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
+# FP64 thread instructions per site of one plain FP64 leapfrog step (k_lsum +
+# k_kick, hilltop) and per deltaN site-step (k_deltaN, hilltop), from ncu
+FP64_INST_STEP = 19
+DN_FP64_INST = 25
 BYTES_STEP_SIGW = 112  # split form with SIGW: 16 + read and write 6 h_ij and 6 h_ij' (FP32)
 BYTES_STEP_POST = 128  # post-inflation phase: read and write f, fd (FP64) and 6 h_ij, 6 h_ij' (FP32)
 
@@ -212,8 +221,11 @@ def reference_arm(args):
     return 0
 
 
-def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None):
-    """Times `steps` leapfrog steps of one form; returns a dict of figures."""
+def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None, settle_s=0.0, tail_s=0.0):
+    """Times `steps` leapfrog steps of one form; returns a dict of figures.
+    With clocks_index set, nvidia-smi samples the SM clocks from settle_s
+    seconds of untimed steps before the warm-up to tail_s seconds of untimed
+    steps after the timed region, so the samples bracket it."""
     import numpy as np
     w = WORKLOAD
     lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=form)
@@ -221,24 +233,33 @@ def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None
     bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
     lat.evolve_fields(0.5 * w["dt"], bg)   # first half drift, src/evolution.cpp:935
     af = 1e30  # a fixed number of steps is timed
-    lat.leapfrog(af, warmup, bg)   # the first call also runs the launch-shape autotuner (split form)
-    bg.astep = bg.a  # the loop's "astep = a", src/evolution.cpp:944
     shape = lat.autotune(bg) if form == iegpu.FORM_SPLIT else None
-    if dist:
-        dist.barrier()
-    launches0 = lat.launches
     clk = Clocks(clocks_index) if clocks_index is not None else None
     if clk:
         clk.__enter__()
+
+    def hold(seconds):
+        t_end = time.perf_counter() + seconds
+        while time.perf_counter() < t_end:
+            lat.leapfrog(af, 16, bg)
+            bg.astep = bg.a
+
+    hold(settle_s)
+    lat.leapfrog(af, warmup, bg)
+    bg.astep = bg.a  # the loop's "astep = a", src/evolution.cpp:944
+    if dist:
+        dist.barrier()
+    launches0 = lat.launches
     lat.timer_start()
     taken = lat.leapfrog(af, steps, bg)
     ms = lat.timer_stop()   # synchronises the lattice's stream
     if dist:
         dist.barrier()
-    if clk:
-        clk.__exit__(None, None, None)
     bg.astep = bg.a
     launches = lat.launches - launches0
+    hold(tail_s)
+    if clk:
+        clk.__exit__(None, None, None)
     assert taken == steps
     tmax = ranks_max(ms, dist)
     out = {"ms": tmax, "launches": launches, "clocks": clk.summary() if clk else None, "shape": shape}
@@ -415,6 +436,106 @@ def measure_post_inflation(iegpu, N, steps, warmup, peak):
                     "FP64 per-site arithmetic in the reference's order"}
 
 
+def measure_split_error(N, workdir):
+    """The split form's error statement over a whole run at N^3 (hilltop
+    preset, seed 8, af = 2N, deltaN stage): the host program run in both
+    forms from the same device initial conditions, every save compared."""
+    import form_error as fe
+    text = fe.preset_text(fe.HILLTOP, N)
+    t0 = time.perf_counter()
+    ref = fe.run_program(text, Path(workdir) / "fp64", "fp64")
+    t1 = time.perf_counter()
+    got = fe.run_program(text, Path(workdir) / "split", "split")
+    t2 = time.perf_counter()
+    err = fe.compare(ref, got)
+    err.update({"workload": f"hilltop, N={N}^3, seed 8, inflation to af={2 * N} and the deltaN stage "
+                            f"(dN=1e-7, Nend=1e-3), split vs plain FP64 form from the same device initial conditions",
+                "program_s": {"fp64": t1 - t0, "split": t2 - t1}})
+    return err
+
+
+def measure_sigw_error(N, workdir):
+    """Config: SIGW on, USR table, N^3: Omega_GW(k) per k-bin at every save,
+    split against the plain FP64 form (host program, same device initial
+    conditions, inflation to af = 2N, no deltaN stage)."""
+    import form_error as fe
+    text = fe.preset_text(fe.USR, N, calculate_SIGW=1, perform_deltaN=0)
+    t0 = time.perf_counter()
+    ref = fe.run_program(text, Path(workdir) / "sigw_fp64", "fp64", inputs=TABLES)
+    t1 = time.perf_counter()
+    got = fe.run_program(text, Path(workdir) / "sigw_split", "split", inputs=TABLES)
+    t2 = time.perf_counter()
+    err = fe.compare(ref, got)
+    out = {"workload": f"USR table, SIGW on, N={N}^3, seed 8, inflation to af={2 * N}, split vs plain FP64 form",
+           "Omega_GW": fe.compare_omega_gw(ref, got, USR["L"]),
+           "spectrumGW": err.get("spectrumGW"), "spectrumGWdot": err.get("spectrumGWdot"),
+           "P_dphi": err["P_dphi"], "H_max": err["H_max"], "saves": err["saves"],
+           "program_s": {"fp64": t1 - t0, "split": t2 - t1}}
+    return out
+
+
+def measure_kernels(iegpu, N, fp64_rate, peak):
+    """The hot path's other kernels at N^3 (FP64): one forward + inverse 3D FFT
+    with the shell binning of the modes (16 B/site per transform, 8 B/site per
+    binning), the deltaN integration (register resident, FP64 operations per
+    site-step) and one RK4 step (336 B/site)."""
+    import numpy as np
+    w = WORKLOAD
+    out = {}
+    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=iegpu.FORM_FP64)
+    H = lat.bunch_davies(w["seed"], w["phi0"], w["dphi0"])
+    bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
+    lat.evolve_fields(0.5 * w["dt"], bg)
+    # FFT forward + inverse (the spectrum's pair) and the binning
+    lat.spectrum(iegpu.F)
+    reps = 5
+    lat.timer_start()
+    for _ in range(reps):
+        lat.fft(iegpu.F, 1)
+        lat.fft(iegpu.F, -1)
+    ms_fft = lat.timer_stop() / (2 * reps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        lat.spectrum(iegpu.F)
+    ms_spec = 1e3 * (time.perf_counter() - t0) / reps
+    gbs = 16 * N ** 3 / (ms_fft * 1e-3) / 1e9
+    out["fft"] = {"ms_per_transform": ms_fft, "algorithmic_bytes_per_site": 16, "achieved_gbs": gbs,
+                  "frac_of_measured_hbm": gbs / peak,
+                  "spectrum_ms": ms_spec,
+                  "note": "ffteasy-exact radix-2 passes in FP64; spectrum = forward FFT + binning + inverse FFT "
+                          "(the reference's spectraf), wall clock with its read-back"}
+    # deltaN: hilltop preset, dN = 1e-7
+    lat.initializeN(bg.a)
+    phiref = lat.get_phiref()
+    steps = 2000
+    lat.deltaN_steps(1e-7, 20, phiref)
+    lat.timer_start()
+    lat.deltaN_steps(1e-7, steps, phiref)
+    ms_dn = lat.timer_stop()
+    site_steps = steps * N ** 3
+    out["deltaN"] = {"site_steps_per_s": site_steps / (ms_dn * 1e-3), "steps": steps,
+                     "fp64_inst_per_site_step": DN_FP64_INST,
+                     "fp64_inst_per_s": DN_FP64_INST * site_steps / (ms_dn * 1e-3),
+                     "fp64_frac_of_measured_rate": DN_FP64_INST * site_steps / (ms_dn * 1e-3) / fp64_rate,
+                     "note": "k_deltaN, hilltop, per-site state in registers (0 B/site-step of HBM); the FP64 "
+                             "operation count per site-step is from ncu (DADD+DMUL+DFMA thread instructions)"}
+    lat.close()
+    # RK4 (inflation_integrator = rk4), FP64 form
+    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=iegpu.FORM_FP64)
+    H = lat.bunch_davies(w["seed"], w["phi0"], w["dphi0"])
+    bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
+    lat.rk4(1e30, 2, bg)
+    nrk = 10
+    lat.timer_start()
+    lat.rk4(1e30, nrk, bg)
+    ms_rk = lat.timer_stop() / nrk
+    gbs = 336 * N ** 3 / (ms_rk * 1e-3) / 1e9
+    out["rk4"] = {"ms_per_step": ms_rk, "site_updates_per_s": N ** 3 / (ms_rk * 1e-3),
+                  "algorithmic_bytes_per_site": 336, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+    lat.close()
+    return out
+
+
 def engine_arm(args):
     ws, rank, local = dist_env()
     dist = None
@@ -432,72 +553,87 @@ def engine_arm(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    traffic_per_site = {}
+    traffic = {}
     try:
-        traffic_per_site = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
+        traffic = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
     except (OSError, ValueError):
         pass
+    # the FP64 pipe's measured rate (thread instructions per second), the
+    # plain FP64 form's compute roofline
+    fp64_rate = iegpu.measure_fp64_rate(1)
 
-    # headline: the split form (FP32 perturbations, FP64 background)
-    sp = measure_form(iegpu, iegpu.FORM_SPLIT, N, args.steps, args.warmup, smi_index, True, dist)
-    value = ws * args.steps * N ** 3 / (sp["ms"] * 1e-3)
-    # the plain FP64 form on the same workload (fewer steps: it is ~15x slower)
-    fp_steps = max(3, min(args.steps, 300))
-    fp = measure_form(iegpu, iegpu.FORM_FP64, N, fp_steps, args.warmup, None, False, dist)
-    fp_value = ws * fp_steps * N ** 3 / (fp["ms"] * 1e-3)
-    # the batched ensemble (fewer steps: each is ~5x the 256^3 step)
-    ens = measure_ensemble(iegpu, max(20, min(args.steps // 30, 500)), args.warmup, peak)
-    sigw = measure_sigw(iegpu, N, max(10, min(args.steps // 75, 200)), args.warmup, peak)
-    post = measure_post_inflation(iegpu, N, max(10, min(args.steps // 300, 100)), args.warmup, peak)
+    # headline: the plain FP64 form (the reference's precision and per-site
+    # arithmetic); the clocks are sampled from 1.5 s before to 0.5 s after the
+    # timed region
+    fp = measure_form(iegpu, iegpu.FORM_FP64, N, args.steps, args.warmup, smi_index, True, dist,
+                      settle_s=1.5, tail_s=0.5)
+    value = ws * args.steps * N ** 3 / (fp["ms"] * 1e-3)
+    # the split form on the same workload
+    sp = measure_form(iegpu, iegpu.FORM_SPLIT, N, args.steps, args.warmup, None, False, dist)
+    sp_value = ws * args.steps * N ** 3 / (sp["ms"] * 1e-3)
     if rank != 0:
         return 0
+    with tempfile.TemporaryDirectory(prefix="ie_bench_") as wd:
+        err = measure_split_error(N, wd) if not args.quick else None
+        sigw_err = measure_sigw_error(N, wd) if not args.quick else None
+    ens = measure_ensemble(iegpu, max(20, min(args.steps // 30, 500)), args.warmup, peak)
+    sigw = measure_sigw(iegpu, N, max(10, min(args.steps // 75, 200)), args.warmup, peak)
+    sigw512 = measure_sigw(iegpu, 512, 10, 3, peak) if not args.quick else None
+    post = measure_post_inflation(iegpu, N, max(10, min(args.steps // 300, 100)), args.warmup, peak)
+    kern = measure_kernels(iegpu, N, fp64_rate, peak)
 
-    # the step kernel's average launch duration over the timed region: the
-    # region holds one priming reduction (timed on its own, aux_ms) and then
-    # `steps` launches of the step kernel, back to back in CUDA graphs
-    kernel_ms = (sp["ms"] - sp["aux_ms"]) / args.steps
-    achieved = BYTES_STEP_SPLIT * N ** 3 / (kernel_ms * 1e-3) / 1e9
-    fp_achieved = BYTES_KICK_FP64 * N ** 3 / (fp["kernel_ms"] * 1e-3) / 1e9
-    tr = traffic_per_site.get("split_step_bytes_per_site")
+    step_ms = fp["ms"] / args.steps
+    achieved = BYTES_STEP_FP64 * N ** 3 / (step_ms * 1e-3) / 1e9
+    inst_rate = FP64_INST_STEP * N ** 3 / (step_ms * 1e-3)
+    tr = traffic.get("fp64_step_bytes_per_site")
+    # split form: the step kernel's average launch duration over its timed
+    # region (one priming reduction, timed on its own, taken out)
+    sp_kernel_ms = (sp["ms"] - sp["aux_ms"]) / args.steps
+    sp_achieved = BYTES_STEP_SPLIT * N ** 3 / (sp_kernel_ms * 1e-3) / 1e9
+    sp_tr = traffic.get("split_step_bytes_per_site")
     bytes_state = 2 * 8 * N ** 3
-    e2e = {"value": ws * args.steps * N ** 3 / sp["e2e_s"], "unit": UNIT,
+    e2e = {"value": ws * args.steps * N ** 3 / fp["e2e_s"], "unit": UNIT,
            "h2d_bytes_per_step": bytes_state / args.steps, "d2h_bytes_per_step": bytes_state / args.steps,
-           "note": f"iegpu_upload(f, fd as FP64) + iegpu_leapfrog({args.steps} steps) + iegpu_download(f, fd), "
-                   f"{sp['pinned']} host buffers (input and output, allocated before the timed region), wall clock"}
+           "note": f"iegpu_upload(f, fd) + iegpu_leapfrog({args.steps} steps) + iegpu_download(f, fd), FP64 form, "
+                   f"{fp['pinned']} host buffers (allocated before the timed region), wall clock"}
     cpu = cpu_baseline(N, os.cpu_count() or 1) if ws == 1 else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sp["ms"] / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": f"hilltop leapfrog, N={N}^3, split form: FP32 dphi/dpi about an FP64 background "
-                                   f"(params.analytic.txt, ns=0.965, seed 8, device Bunch-Davies initial conditions)",
-                       "N": N, "form": "split", "l2": "state > L2 (129 MB) each step: no flush needed",
-                       "autotuned_shape": sp["shape"],
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"hilltop leapfrog, N={N}^3, plain FP64 form (params.analytic.txt, ns=0.965, "
+                                   f"seed 8, device Bunch-Davies initial conditions)",
+                       "N": N, "form": "fp64", "l2": "state > L2 (129 MB) each step: no flush needed",
                        "parallelism": f"replicas x{ws}"},
-            "forms": {"split": {"value": value, "ms_per_step": sp["ms"] / args.steps, "steps": args.steps},
-                      "fp64": {"value": fp_value, "ms_per_step": fp["ms"] / fp_steps, "steps": fp_steps,
-                               "kernel": "k_kick (FP64 kick + drift)", "kernel_ms": fp["kernel_ms"],
-                               "reduce_kernel_ms": fp["aux_ms"], "achieved_gbs": fp_achieved,
-                               "frac_of_measured_hbm": fp_achieved / peak,
-                               "note": "per-site arithmetic in the reference's order (-fmad=false); FP64 ALU bound"},
-                      "split_over_fp64": value / fp_value,
-                      "batched": ens,
-                      "sigw": sigw,
-                      "post_inflation": post},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None if tr is None else tr * N ** 3,
-                         "kernel": "k_split_rows4_persist (fused kick + drift + next-step Friedmann sums; 64 steps per cooperative "
-                                   "launch at 128 <= N <= 256, k_split_rows4 one step per launch otherwise)",
-                         "algorithmic_bytes_per_site": BYTES_STEP_SPLIT, "kernel_ms": kernel_ms,
-                         "kernel_ms_source": "timed region (CUDA events on the lattice's stream) less the one "
-                                             "priming reduction, divided by the steps",
-                         "kernel_ms_isolated": sp["kernel_ms"],
-                         "kernel_ms_isolated_source": "k_split_rows4, one step per launch, each launched alone "
-                                                     "between two events with a host synchronisation",
-                         "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)"},
-            "gpu_launches": sp["launches"], "clocks": sp["clocks"], "e2e": e2e}
-    line["metric_note"] = ("value: split form at 256^3; forms.fp64: plain FP64 form, same workload; "
-                           "forms.batched: the ensemble form (site-updates/s and lattices/s over sequential runs)")
+                         "kernel": "k_lsum + k_kick (one FP64 leapfrog step: stored Laplacian and exact Friedmann "
+                                   "sums, then kick + drift)",
+                         "algorithmic_bytes_per_site": BYTES_STEP_FP64, "kernel_ms": step_ms,
+                         "kernel_ms_source": "timed region (CUDA events on the lattice's stream) divided by the steps",
+                         "kernel_ms_isolated": {"k_lsum": fp["aux_ms"], "k_kick": fp["kernel_ms"]},
+                         "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)",
+                         "compute_bound": "fp64",
+                         "fp64": {"inst_per_site": FP64_INST_STEP, "achieved_inst_per_s": inst_rate,
+                                  "peak_inst_per_s": fp64_rate, "frac": inst_rate / fp64_rate,
+                                  "peak_source": "measured: iegpu_measure_fp64_rate (independent DADD chains on "
+                                                 "every SM)",
+                                  "note": "GB300's FP64 pipe bounds this form: the FP64 thread instructions per "
+                                          "site of both kernels are from ncu; the lattice sums and the division "
+                                          "by B^2 run on the integer pipes"}},
+            "gpu_launches": fp["launches"], "clocks": fp["clocks"], "e2e": e2e,
+            "forms": {"split": {"value": sp_value, "ms_per_step": sp["ms"] / args.steps,
+                                "over_fp64": sp_value / value,
+                                "roofline": {"achieved": sp_achieved, "frac": sp_achieved / peak,
+                                             "kernel": "k_split_rows4_persist", "kernel_ms": sp_kernel_ms,
+                                             "kernel_ms_isolated": sp["kernel_ms"],
+                                             "algorithmic_bytes_per_site": BYTES_STEP_SPLIT,
+                                             "traffic": None if sp_tr is None else sp_tr * N ** 3},
+                                "shape": sp["shape"], "gpu_launches": sp["launches"], "error": err},
+                      "batched": ens, "sigw": dict(sigw, error=sigw_err), "sigw_512": sigw512,
+                      "post_inflation": post, "kernels": kern}}
+    line["metric_note"] = ("value: plain FP64 form at 256^3 (like for like with the reference arm); forms.split: "
+                           "the split form on the same workload and its whole-run error against FP64; "
+                           "forms.batched: the ensemble (site-updates/s, lattices/s over sequential runs)")
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -511,6 +647,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--quick", action="store_true", help="skip the whole-run error statements and 512^3")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()

@@ -192,6 +192,10 @@ int  iegpu_timer_stop(struct iegpu_ctx* ctx, float* ms);
  * ms_out[0] is the priming reduction, ms_out[1] the fused step kernels'
  * total.  For profiling only. */
 int  iegpu_profile_leapfrog(struct iegpu_ctx* ctx, double af, int nsteps, iegpu_bg* bg, double* ms_out, int nk);
+/* No counterpart in the reference: a throughput probe of the current device's
+ * FP64 pipe (op 0: DFMA, 1: DADD, 2: DMUL), in thread instructions per second,
+ * the denominator of the plain FP64 form's roofline.  Needs no context. */
+int  iegpu_measure_fp64_rate(int op, double* inst_per_s);
 
 /* Split form: run the launch-shape autotuner now (it otherwise runs on the
  * first iegpu_leapfrog call) and report the chosen shape of the step kernel:
@@ -214,6 +218,15 @@ int  iegpu_set_shape(struct iegpu_ctx* ctx, int rows, int prefetch, int chunks);
  * launch per step in CUDA graphs (on = 0).  Both give the same bits.  No
  * counterpart in the reference (its loop is serial host code). */
 int  iegpu_set_persistent(struct iegpu_ctx* ctx, int on);
+/* No counterpart in the reference: the bounds of the split form's device-side
+ * waits (the persistent step barrier and the bulk-copy barriers), which end
+ * a call with IEGPU_ETIMEOUT instead of hanging when a wait cannot finish.
+ * polls: poll limit of each wait (0: the default, 2^20, about half a second).
+ * unreachable != 0 makes the persistent step barrier wait for a count that no
+ * launch reaches, so that it gives up: a hook for failure-path tests (the
+ * context stays usable; the next call starts from the host's background).
+ * Persistent launches run at 128 <= N <= 256 without SIGW. */
+int  iegpu_set_wait_limit(struct iegpu_ctx* ctx, unsigned polls, int unreachable);
 
 /* ---- post-inflation phase (plain FP64 form, SIGW on) ------------------- */
 /* initialize_post_inflation(), src/initialize.cpp:245-290, without its save:

@@ -39,6 +39,7 @@ UNITS = {
     "split_fp32.cu": [],
     "ensemble.cu": [],
     "ensemble_dn.cu": ["-fmad=false"],
+    "measure.cu": [],
 }
 
 

@@ -102,12 +102,12 @@ static void free_all(iegpu_ctx* c) {
     if (c->sctl_h) cudaFreeHost(c->sctl_h);
     fft_free(c);
     for (int q = 0; q < 2; ++q) cudaFree(c->f[q]);
-    cudaFree(c->fd); cudaFree(c->dn); cudaFree(c->fny); cudaFree(c->fdny);
+    cudaFree(c->fd); cudaFree(c->dn); cudaFree(c->fny); cudaFree(c->fdny); cudaFree(c->lap);
     for (int q = 0; q < 6; ++q) {
         cudaFree(c->h[0][q]); cudaFree(c->h[1][q]); cudaFree(c->hd[q]); cudaFree(c->hny[q]); cudaFree(c->hdny[q]);
     }
     cudaFree(c->rk_d); cudaFree(c->rk_h); cudaFree(c->dn_y5);
-    cudaFree(c->tab); cudaFree(c->tkey);
+    cudaFree(c->tab); cudaFree(c->tkey); cudaFree(c->tdiv);
     cudaFree(c->ctl); cudaFree(c->part); cudaFree(c->counter); cudaFree(c->a_trace);
     cudaFree(c->spec_part); cudaFree(c->spec_cnt); cudaFree(c->misc);
     if (c->ctl_h) cudaFreeHost(c->ctl_h);
@@ -187,11 +187,12 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
     if (c->red_grid * 256LL > sites) c->red_grid = (int)((sites + 255) / 256);
     c->spec_blocks = c->sms * 2;
     const int nb = iegpu_numbins(N) + 1;
-    // partial sums: 6 per reduction CTA, or 3 per CTA of the split step kernel
+    // partial sums: up to 12 words (three exact sums) per reduction CTA, or 3
+    // per CTA of the split step kernel
     // (at most max(8 per SM, number of 8x32 tiles))
     const long long tiles = (long long)(N / (N >= 32 ? 8 : (N >= 16 ? 16 : 8))) * (N / (N >= 32 ? 32 : N));
     const long long step_ctas = tiles > 8LL * c->sms ? tiles : 8LL * c->sms;
-    c->part_cap = (int)(6 * c->red_grid + 3 * step_ctas + 64);
+    c->part_cap = (int)(12 * c->red_grid + 3 * step_ctas + 64);
     if (!rc) rc = dalloc(c, &c->ctl, 1);
     if (!rc) rc = dalloc(c, &c->part, (size_t)c->part_cap);
     if (!rc && cfg->form == IEGPU_FORM_SPLIT) {
@@ -242,6 +243,7 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
     P.c1 = (1.0 - cfg->ns) / 4.0;
     P.c2 = -cfg->V0 * (1.0 - cfg->ns) / 2.0;
     P.B2 = cfg->rescale_B * cfg->rescale_B;
+    P.divB2 = make_div_const(P.B2);
     for (int q = 0; q < 4 && !rc; ++q)
         if (check_cuda(c, cudaEventCreate(&c->ev[q]), "event create")) rc = IEGPU_ECUDA;
     if (!rc) rc = fft_init(c);
@@ -289,13 +291,19 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
             h[7 * n + l] = (dV[l - 1] - dV[l]) / (phi[l - 1] - phi[l]);
         }
     }
+    std::vector<DivConst> dv((size_t)n);
+    for (int l = 1; l < n; ++l) dv[l] = make_div_const(h[3 * n + l]);
+    dv[0] = make_div_const(1.0);
     cudaFree(c->tab);
     cudaFree(c->tkey);
+    cudaFree(c->tdiv);
     c->tab = nullptr;
     c->tkey = nullptr;
-    if (dalloc(c, &c->tab, h.size()) || dalloc(c, &c->tkey, k.size())) return IEGPU_ENOMEM;
+    c->tdiv = nullptr;
+    if (dalloc(c, &c->tab, h.size()) || dalloc(c, &c->tkey, k.size()) || dalloc(c, &c->tdiv, dv.size())) return IEGPU_ENOMEM;
     if (check_cuda(c, cudaMemcpy(c->tab, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice), "table upload") ||
-        check_cuda(c, cudaMemcpy(c->tkey, k.data(), sizeof(long long) * k.size(), cudaMemcpyHostToDevice), "table upload"))
+        check_cuda(c, cudaMemcpy(c->tkey, k.data(), sizeof(long long) * k.size(), cudaMemcpyHostToDevice), "table upload") ||
+        check_cuda(c, cudaMemcpy(c->tdiv, dv.data(), sizeof(DivConst) * dv.size(), cudaMemcpyHostToDevice), "table upload"))
         return IEGPU_ECUDA;
     c->htab_x.assign(phi, phi + n);
     c->htab_V.assign(V, V + n);
@@ -312,6 +320,7 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
     P.slopeV = c->tab + 6 * n;
     P.slopedV = c->tab + 7 * n;
     P.key = c->tkey;
+    P.ddx = c->tdiv;
     fp64_destroy_graphs(c);  // graphs hold the potential by value
     split_destroy_graphs(c);
     return IEGPU_OK;
@@ -635,6 +644,14 @@ int iegpu_set_persistent(iegpu_ctx* c, int on) {
     if (!c) return IEGPU_EINVAL;
     if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "persistent launches belong to the split form");
     c->persist = on != 0;
+    return IEGPU_OK;
+}
+
+int iegpu_set_wait_limit(iegpu_ctx* c, unsigned polls, int unreachable) {
+    if (!c) return IEGPU_EINVAL;
+    if (!is_split(c)) return set_error(c, IEGPU_EUNSUPPORTED, "bounded device waits belong to the split form");
+    c->wait_polls = polls;
+    c->wait_bias = unreachable ? 0x40000000u : 0u;
     return IEGPU_OK;
 }
 

@@ -49,8 +49,8 @@ __global__ void __launch_bounds__(256) k_deltaN(double* __restrict__ f, double* 
                 const double der = table_interp(P, P.dV, P.dydV, x, l);
                 ratio = der / pot;
             } else {
-                const double pot = (P.V0 * (1.0 - P.c1 * (x * x))) / P.B2;
-                const double der = (P.c2 * x) / P.B2;
+                const double pot = div_exact(P.V0 * (1.0 - P.c1 * (x * x)), P.divB2);
+                const double der = div_exact(P.c2 * x, P.divB2);
                 ratio = der / pot;
             }
             v = v + d * (-(3.0 - 0.5 * (v * v)) * (v + ratio));
@@ -150,11 +150,11 @@ __device__ __forceinline__ void rhsN(const PotDev& P, double x, double v, double
         bool oor;
         l = table_walk(P, x, l, &oor);
         bad |= oor;
-        pot = table_interp(P, P.V, P.dyV, x, l) / P.B2;
-        dpot = table_interp(P, P.dV, P.dydV, x, l) / P.B2;
+        pot = div_exact(table_interp(P, P.V, P.dyV, x, l), P.divB2);
+        dpot = div_exact(table_interp(P, P.dV, P.dydV, x, l), P.divB2);
     } else {
-        pot = (P.V0 * (1.0 - P.c1 * (x * x))) / P.B2;
-        dpot = (P.c2 * x) / P.B2;
+        pot = div_exact(P.V0 * (1.0 - P.c1 * (x * x)), P.divB2);
+        dpot = div_exact(P.c2 * x, P.divB2);
     }
     const double ratio = dpot / pot;
     bool act;

@@ -104,8 +104,8 @@ __global__ void __launch_bounds__(256) k_ens_deltaN(EnsDn A, const double* __res
                 const double der = table_interp(A.P, A.P.dV, A.P.dydV, x, l);
                 ratio = der / pot;
             } else {
-                const double pot = (A.P.V0 * (1.0 - A.P.c1 * (x * x))) / A.P.B2;
-                const double der = (A.P.c2 * x) / A.P.B2;
+                const double pot = div_exact(A.P.V0 * (1.0 - A.P.c1 * (x * x)), A.P.divB2);
+                const double der = div_exact(A.P.c2 * x, A.P.divB2);
                 ratio = der / pot;
             }
             v = v + d * (-(3.0 - 0.5 * (v * v)) * (v + ratio));

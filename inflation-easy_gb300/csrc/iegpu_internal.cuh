@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/iegpu.h"
+#include "exact.cuh"
 
 namespace iegpu {
 
@@ -45,7 +46,7 @@ struct DevCtl {
     int done;
     int mode;           // kModeLeapfrog or kModeKick
     int error;          // first device-side error code
-    int pad;
+    unsigned sumflags;  // exact lattice sums: bit q set, sum q met a non-finite term
     double errval;      // offending value for IEGPU_ERANGE
 };
 
@@ -57,6 +58,7 @@ struct PotDev {
     int table;          // 0 hilltop, 1 tabulated
     int n;              // table length
     double V0, c1, c2, B2;  // hilltop: V = V0(1 - c1 v^2)/B2, V' = (c2 v)/B2
+    DivConst divB2;         // x / B2, correctly rounded, on the integer pipes
     const double* x;        // table nodes (descending)
     const long long* key;   // monotone integer keys of x
     const double* V;        // V at nodes
@@ -66,6 +68,7 @@ struct PotDev {
     const double* dydV;     // dV[l-1] - dV[l]
     const double* slopeV;   // dyV/dxl
     const double* slopedV;  // dydV/dxl
+    const DivConst* ddx;    // x / dxl[l], correctly rounded, on the integer pipes
 };
 
 // Split form (FP32 perturbations about an FP64 background).
@@ -117,6 +120,10 @@ struct SplitCtl {
     // as double-float pairs and the index of its a_trace entry.
     int deferred, def_step;
     float dsum_hi[3], dsum_lo[3];
+    // bounded device waits: poll limit (0: the default) and, for tests, a
+    // bias added to the persistent step barrier's target so that it is never
+    // reached
+    unsigned spin_polls, spin_bias;
 };
 
 // Per-lattice constants of the split step: base step, rescaling exponent,
@@ -187,6 +194,7 @@ struct iegpu_ctx {
     double* dn = nullptr;
     double* fny = nullptr;
     double* fdny = nullptr;
+    double* lap = nullptr;      // lapl(f) of the current step (leapfrog), allocated on first use
     // SIGW state
     float* h[2][6] = {};
     float* hd[6] = {};
@@ -204,6 +212,7 @@ struct iegpu_ctx {
     int ntab = 0;
     double* tab = nullptr;      // packed arrays, see iegpu_set_table
     long long* tkey = nullptr;
+    iegpu::DivConst* tdiv = nullptr;   // per-bracket divisors of the interpolation
     iegpu::PotDev pot{};
 
     // control and scratch
@@ -232,6 +241,8 @@ struct iegpu_ctx {
     iegpu::RowCfg row_cfg;                // split row-kernel launch shape
     int tuned = 0;
     int part_cap = 0;
+    unsigned wait_polls = 0;              // bounded device waits: poll limit (0: default)
+    unsigned wait_bias = 0;               // test hook: persistent barrier target never reached
 
     // timing events
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

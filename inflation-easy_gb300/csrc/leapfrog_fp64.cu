@@ -6,16 +6,21 @@
 // the same inputs produces the same bits as the reference CPU code.
 //
 // One leapfrog step is two kernels, captured in a CUDA graph:
-//   k_reduce  reads f (7-point stencil) and accumulates sum f*lapl(f) and the
-//             potential sum (gradient_energy / potential_energy,
-//             src/evolution.cpp:130-136, src/potential.cpp:151-171); the last
-//             CTA to finish combines the partials in a fixed order and runs
-//             the Friedmann update of src/evolution.cpp:153-168 on the device.
-//   k_kick    kick of fd (and hd) with the fused Laplacian + V', then the
+//   k_lsum    reads f (7-point stencil), stores lapl(f) for the kick and adds
+//             f*lapl(f) and the potential term of every site exactly
+//             (gradient_energy / potential_energy, src/evolution.cpp:130-136,
+//             src/potential.cpp:151-171; exact sums, exact.cuh); the last CTA
+//             to finish rounds the two sums and runs the Friedmann update of
+//             src/evolution.cpp:153-168 on the device.
+//   k_kick    kick of fd (and hd) with the stored Laplacian and V', then the
 //             drift f += d fd into the other f buffer (ping-pong), and
 //             h += (float)(d hd) (src/evolution.cpp:170-281).
-// Algorithmic HBM traffic per site-update: 40 B (read f twice, fd; write f, fd),
-// 32 B of which are the reference's own state update.
+// GB300's FP64 pipe, not HBM, bounds this form: the Laplacian is formed once
+// per step (the reference forms it twice, in the sum and in the kick), the
+// sums' additions and the division by B^2 run on the integer pipes, so a
+// site costs 19 FP64 operations (hilltop).  Algorithmic HBM traffic per
+// site-update: 32 B of state (read f, fd; write f, fd); the stored Laplacian
+// adds 16 B and the second read of f 8 B.
 //
 // The same unit holds the other integrators of the plain FP64 state, with the
 // same per-site rules: the post-inflation leapfrog (src/evolution.cpp:1378-1653)
@@ -125,38 +130,121 @@ __device__ void step_scalars(DevCtl* ctl, const PotDev& P, const StepConst& K, d
     }
 }
 
+// Block combine of NV exact sums: the block's total is left in thread 0.
+template <int NV>
+__device__ __forceinline__ void acc_block_sum(Acc4 (&v)[NV]) {
+    __shared__ Acc4 sh[NV][kThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc_warp_sum(v[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[q][w] = v[q];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            if (lane < kThreads / 32) v[q] = sh[q][lane];
+            else acc_zero(v[q]);
+            acc_warp_sum(v[q]);
+        }
+    }
+}
+
+// Exact block partials: NV words of 4 limbs per CTA.
+template <int NV>
+__device__ __forceinline__ void acc_store_partial(unsigned long long* part, const Acc4 (&v)[NV]) {
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q)
+#pragma unroll
+            for (int l = 0; l < 4; ++l) part[((size_t)blockIdx.x * NV + q) * 4 + l] = v[q].w[l];
+    }
+}
+
+// Sum of the CTAs' exact partials by warp 0; the rounded totals are valid in
+// lane 0.  Integer sums: the order of the CTAs does not matter.
+template <int NV>
+__device__ __forceinline__ void acc_sum_partials(const unsigned long long* part, int nb, double (&out)[NV]) {
+    const int lane = threadIdx.x & 31;
+    Acc4 s[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc_zero(s[q]);
+    for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const unsigned long long* p = part + ((size_t)b * NV + q) * 4;
+            acc_add4(s[q], __ldcg(p), __ldcg(p + 1), __ldcg(p + 2), __ldcg(p + 3));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        acc_warp_sum(s[q]);
+        out[q] = lane == 0 ? acc_to_double(s[q]) : 0.0;
+    }
+}
+
+// Flags of the exact sums from every thread of the CTA into ctl->sumflags:
+// bit q: sum q met a non-finite term; a finite term of magnitude >= 2^30
+// (beyond the accumulator) raises IEGPU_ETOOBIG.
+template <int NV>
+__device__ __forceinline__ void acc_publish_flags(DevCtl* ctl, const unsigned (&fl)[NV]) {
+    unsigned nonfinite = 0, big = 0;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        nonfinite |= (fl[q] & 1u) << q;
+        big |= fl[q] & 2u;
+    }
+    nonfinite = __reduce_or_sync(0xffffffffu, nonfinite);
+    big = __reduce_or_sync(0xffffffffu, big);
+    if ((threadIdx.x & 31) == 0) {
+        if (nonfinite) atomicOr(&ctl->sumflags, nonfinite);
+        if (big) flag_error(ctl, IEGPU_ETOOBIG, 0.0);
+    }
+}
+
+// Pass 1 of a leapfrog step: lapl(f) of every site stored for the kick, and
+// the two lattice sums of the Friedmann update, exact: G = sum f lapl(f) and
+// Pn = sum f^2 (hilltop) or sum V B^2 (table).  The last CTA rounds them and
+// runs the scalar update.
 template <bool TABLE>
-__global__ void __launch_bounds__(kThreads) k_reduce(const double* __restrict__ f, PotDev P, DevCtl* ctl,
-                                                     double* part, unsigned* counter, double* a_trace, int lg,
-                                                     StepConst K) {
+__global__ void __launch_bounds__(kThreads) k_lsum(const double* __restrict__ f, double* __restrict__ lap, PotDev P,
+                                                   DevCtl* ctl, unsigned long long* part, unsigned* counter,
+                                                   double* a_trace, int lg, StepConst K) {
     if (ctl->mode == kModeLeapfrog && ctl->done) return;
     const long long gs = 1LL << (3 * lg);
-    double v[2] = {0.0, 0.0};
-    bool bad = false;
+    Acc4 v[2];
+    acc_zero(v[0]);
+    acc_zero(v[1]);
+    unsigned fl[2] = {0u, 0u};
     for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
         const Nbr n = neighbours(id, lg);
         const double fc = __ldg(&f[id]);
-        v[0] += fc * lapl7(f, n, fc);
+        const double L = lapl7(f, n, fc);
+        lap[id] = L;
+        acc_add_term(v[0], fc * L, fl[0]);
         if (TABLE) {
             bool oor;
-            v[1] += V_table_sum_term(P, fc, &oor);
-            if (oor) { flag_error(ctl, IEGPU_ERANGE, fc); bad = true; }
+            acc_add_term(v[1], V_table_sum_term(P, fc, &oor), fl[1]);
+            if (oor) flag_error(ctl, IEGPU_ERANGE, fc);
         } else {
-            v[1] += fc * fc;
+            acc_add_term(v[1], fc * fc, fl[1]);
         }
     }
-    (void)bad;
-    block_sum<2>(v);
-    if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = v[0];
-        part[2 * blockIdx.x + 1] = v[1];
-    }
+    acc_publish_flags<2>(ctl, fl);
+    acc_block_sum<2>(v);
+    acc_store_partial<2>(part, v);
     if (!arrive_last(counter)) return;
     if (threadIdx.x < 32) {
         double tot[2];
-        sum_partials<2>(part, gridDim.x, tot);
+        acc_sum_partials<2>(part, gridDim.x, tot);
         if (threadIdx.x == 0) {
             *counter = 0;
+            const unsigned nf = ctl->sumflags;
+            ctl->sumflags = 0;
+            if (nf & 1u) tot[0] = __longlong_as_double(0x7FF8000000000000LL);
+            if (nf & 2u) tot[1] = __longlong_as_double(0x7FF8000000000000LL);
             if (ctl->error) {
                 ctl->st.active = 0;
                 ctl->done = 1;
@@ -167,26 +255,29 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const double* __restrict__ 
     }
 }
 
+// Pass 2: kick of fd with the stored Laplacian, src/evolution.cpp:170-180,
+// and the drift into the other f buffer; with SIGW the tensor kick and drift
+// of src/evolution.cpp:183-254, 272-281.
 template <bool TABLE, bool SIGW, int MODE>
-__global__ void __launch_bounds__(kThreads) k_kick(const double* __restrict__ fs, double* __restrict__ fdst,
-                                                   double* __restrict__ fd, SigwPtrs sg, PotDev P, DevCtl* ctl,
-                                                   int lg, double half_over_dx) {
+__global__ void __launch_bounds__(kThreads) k_kick(const double* __restrict__ fs, const double* __restrict__ lap,
+                                                   double* __restrict__ fdst, double* __restrict__ fd, SigwPtrs sg,
+                                                   PotDev P, DevCtl* ctl, int lg, double half_over_dx) {
     const DevStep st = ctl->st;
     if (!st.active) return;
     const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
-    const Nbr n = neighbours(id, lg);
     const double fc = __ldg(&fs[id]);
-    const double lap = lapl7(fs, n, fc);
+    const double L = __ldg(&lap[id]);
     bool oor;
     const double dv = dV_exact<TABLE>(P, fc, &oor);
     if (TABLE && oor) flag_error(ctl, IEGPU_ERANGE, fc);
     const double fdo = fd[id];
-    const double fdn = fdo + st.d * (st.laplnorm * lap - st.friction * fdo - st.potnorm * dv);
+    const double fdn = fdo + st.d * (st.laplnorm * L - st.friction * fdo - st.potnorm * dv);
     fd[id] = fdn;
     if (MODE == kModeLeapfrog) fdst[id] = fc + st.d * fdn;
     if (SIGW) {
         // dfdx<double>, src/evolution.cpp:55-77, and the six tensor updates
         // of src/evolution.cpp:183-254 (float storage, double right-hand side).
+        const Nbr n = neighbours(id, lg);
         const double gx = (__ldg(&fs[n.ip]) - __ldg(&fs[n.im])) * half_over_dx;
         const double gy = (__ldg(&fs[n.jp]) - __ldg(&fs[n.jm])) * half_over_dx;
         const double gz = (__ldg(&fs[n.kp]) - __ldg(&fs[n.km])) * half_over_dx;
@@ -218,32 +309,34 @@ __global__ void __launch_bounds__(kThreads) k_drift(double* __restrict__ f, cons
     }
 }
 
-// Lattice sums for kin_energy / gradient_energy / potential_energy.
+// Lattice sums for kin_energy / gradient_energy / potential_energy, exact
+// (as the leapfrog's): sum f lapl(f), the potential sum and sum fd^2.
 template <bool TABLE>
 __global__ void __launch_bounds__(kThreads) k_energy_sums(const double* __restrict__ f, const double* __restrict__ fd,
-                                                          PotDev P, DevCtl* ctl, double* part, int lg) {
+                                                          PotDev P, DevCtl* ctl, unsigned long long* part, int lg) {
     const long long gs = 1LL << (3 * lg);
-    double v[3] = {0.0, 0.0, 0.0};
+    Acc4 v[3];
+    acc_zero(v[0]);
+    acc_zero(v[1]);
+    acc_zero(v[2]);
+    unsigned fl[3] = {0u, 0u, 0u};
     for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
         const Nbr n = neighbours(id, lg);
         const double fc = __ldg(&f[id]);
-        v[0] += fc * lapl7(f, n, fc);
+        acc_add_term(v[0], fc * lapl7(f, n, fc), fl[0]);
         if (TABLE) {
             bool oor;
-            v[1] += V_table_sum_term(P, fc, &oor);
+            acc_add_term(v[1], V_table_sum_term(P, fc, &oor), fl[1]);
             if (oor) flag_error(ctl, IEGPU_ERANGE, fc);
         } else {
-            v[1] += fc * fc;
+            acc_add_term(v[1], fc * fc, fl[1]);
         }
         const double q = __ldg(&fd[id]);
-        v[2] += q * q;
+        acc_add_term(v[2], q * q, fl[2]);
     }
-    block_sum<3>(v);
-    if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = v[0];
-        part[3 * blockIdx.x + 1] = v[1];
-        part[3 * blockIdx.x + 2] = v[2];
-    }
+    acc_publish_flags<3>(ctl, fl);
+    acc_block_sum<3>(v);
+    acc_store_partial<3>(part, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -271,12 +364,20 @@ static SigwPtrs sigw_ptrs(iegpu_ctx* c, int src) {
     return s;
 }
 
+// The stored Laplacian of the leapfrog (N^3 doubles), allocated on first use.
+static int ensure_lap(iegpu_ctx* c) {
+    if (c->lap) return IEGPU_OK;
+    if (check_cuda(c, cudaMalloc(&c->lap, sizeof(double) * c->gs), "Laplacian buffer")) return IEGPU_ENOMEM;
+    return IEGPU_OK;
+}
+
 static void launch_reduce(iegpu_ctx* c, int src) {
     const StepConst K = step_const(c);
+    unsigned long long* part = reinterpret_cast<unsigned long long*>(c->part);
     if (c->pot.table)
-        k_reduce<true><<<c->red_grid, kThreads, 0, c->stream>>>(c->f[src], c->pot, c->ctl, c->part, c->counter, c->a_trace, c->lg, K);
+        k_lsum<true><<<c->red_grid, kThreads, 0, c->stream>>>(c->f[src], c->lap, c->pot, c->ctl, part, c->counter, c->a_trace, c->lg, K);
     else
-        k_reduce<false><<<c->red_grid, kThreads, 0, c->stream>>>(c->f[src], c->pot, c->ctl, c->part, c->counter, c->a_trace, c->lg, K);
+        k_lsum<false><<<c->red_grid, kThreads, 0, c->stream>>>(c->f[src], c->lap, c->pot, c->ctl, part, c->counter, c->a_trace, c->lg, K);
     c->launches++;
 }
 
@@ -286,11 +387,12 @@ static void launch_kick(iegpu_ctx* c, int src) {
     const SigwPtrs sg = sigw_ptrs(c, src);
     const double hodx = 0.5 / (c->cfg.L / (double)c->N);
     double* fdst = c->f[src ^ 1];
+    const double* L = c->lap;
     const bool tab = c->pot.table != 0, sig = c->cfg.sigw != 0;
-    if (tab && sig) k_kick<true, true, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
-    else if (tab) k_kick<true, false, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
-    else if (sig) k_kick<false, true, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
-    else k_kick<false, false, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    if (tab && sig) k_kick<true, true, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], L, fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    else if (tab) k_kick<true, false, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], L, fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    else if (sig) k_kick<false, true, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], L, fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
+    else k_kick<false, false, MODE><<<grid, kThreads, 0, c->stream>>>(c->f[src], L, fdst, c->fd, sg, c->pot, c->ctl, c->lg, hodx);
     c->launches++;
 }
 
@@ -338,6 +440,8 @@ static int read_ctl(iegpu_ctx* c) {
         return set_error(c, IEGPU_ERANGE, "Field value %.17g is outside the numerical potential range [%.17g, %.17g].\n", v,
                          c->htab_x.empty() ? 0.0 : c->htab_x.back(), c->htab_x.empty() ? 0.0 : c->htab_x.front());
     }
+    if (c->ctl_h->error == IEGPU_ETOOBIG)
+        return set_error(c, IEGPU_ETOOBIG, "a lattice-sum term of magnitude >= 2^30 is beyond the exact accumulator\n");
     return IEGPU_OK;
 }
 
@@ -374,6 +478,7 @@ int fp64_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* ste
         c->a_trace_cap = cap;
         fp64_destroy_graphs(c);  // graphs captured the old pointer
     }
+    if (ensure_lap(c)) return IEGPU_ENOMEM;
     if (!c->lf_exec[0]) {
         int rc = build_graphs(c);
         if (rc) return rc;
@@ -407,6 +512,7 @@ int fp64_leapfrog(iegpu_ctx* c, double af, int max_steps, iegpu_bg* bg, int* ste
 
 int fp64_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, int nk) {
     for (int q = 0; q < nk; ++q) ms[q] = 0.0;
+    if (ensure_lap(c)) return IEGPU_ENOMEM;
     fill_ctl(c, bg, kModeLeapfrog);
     c->ctl_h->af = af;
     c->ctl_h->steps_limit = nsteps;
@@ -435,6 +541,7 @@ int fp64_profile(iegpu_ctx* c, double af, int nsteps, iegpu_bg* bg, double* ms, 
 }
 
 int fp64_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg) {
+    if (ensure_lap(c)) return IEGPU_ENOMEM;
     fill_ctl(c, bg, kModeKick);
     c->ctl_h->d_given = d;
     if (upload_ctl(c)) return IEGPU_ECUDA;
@@ -463,17 +570,36 @@ int fp64_evolve_fields(iegpu_ctx* c, double d, iegpu_bg* bg) {
 int fp64_energies(iegpu_ctx* c, const iegpu_bg* bg, double out[3]) {
     const int grid = c->red_grid;
     c->ctl_h->error = 0;
-    if (check_cuda(c, cudaMemsetAsync(&c->ctl->error, 0, sizeof(int), c->stream), "memset")) return IEGPU_ECUDA;
-    if (c->pot.table) k_energy_sums<true><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, c->pot, c->ctl, c->part, c->lg);
-    else k_energy_sums<false><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, c->pot, c->ctl, c->part, c->lg);
+    // error and sumflags are adjacent ints of the control block
+    if (check_cuda(c, cudaMemsetAsync(&c->ctl->error, 0, 2 * sizeof(int), c->stream), "memset")) return IEGPU_ECUDA;
+    unsigned long long* part = reinterpret_cast<unsigned long long*>(c->part);
+    if (c->pot.table) k_energy_sums<true><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, c->pot, c->ctl, part, c->lg);
+    else k_energy_sums<false><<<grid, kThreads, 0, c->stream>>>(c->f[c->cur], c->fd, c->pot, c->ctl, part, c->lg);
     c->launches++;
-    std::vector<double> h((size_t)grid * 3);
-    if (check_cuda(c, cudaMemcpyAsync(h.data(), c->part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream), "energy partials"))
+    std::vector<unsigned long long> h((size_t)grid * 12);
+    if (check_cuda(c, cudaMemcpyAsync(h.data(), part, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost, c->stream),
+                   "energy partials"))
         return IEGPU_ECUDA;
     int rc = read_ctl(c);
     if (rc) return rc;
-    double G = 0, Pn = 0, K2 = 0;
-    for (int b = 0; b < grid; ++b) { G += h[3 * b]; Pn += h[3 * b + 1]; K2 += h[3 * b + 2]; }
+    double tot[3];
+    for (int q = 0; q < 3; ++q) {
+        unsigned long long w[4] = {0, 0, 0, 0};
+        for (int b = 0; b < grid; ++b) {
+            unsigned carry = 0;
+            for (int l = 0; l < 4; ++l) {
+                const unsigned long long x = h[((size_t)b * 3 + q) * 4 + l];
+                const unsigned long long t = w[l] + x;
+                const unsigned c1 = t < x;
+                w[l] = t + carry;
+                carry = c1 | (w[l] < t);
+            }
+        }
+        Acc4 A;
+        for (int l = 0; l < 4; ++l) A.w[l] = w[l];
+        tot[q] = (c->ctl_h->sumflags >> q) & 1u ? __builtin_nan("") : acc_to_double(A);
+    }
+    const double G = tot[0], Pn = tot[1], K2 = tot[2];
     const double gs = (double)c->gs, a = bg->a, s = c->cfg.rescale_s, dx = c->cfg.L / (double)c->N;
     const double B2 = c->pot.B2;
     // kin_energy, src/evolution.cpp:139-145
@@ -750,8 +876,8 @@ __global__ void __launch_bounds__(kThreads) k_rk_rhs(const double* __restrict__ 
             bool oor;
             const int l = table_bracket(P, field, &oor);
             if (oor) flag_error(ctl, IEGPU_ERANGE, field);
-            pot = table_interp(P, P.V, P.dyV, field, l) / P.B2;
-            dpot = table_interp(P, P.dV, P.dydV, field, l) / P.B2;
+            pot = div_exact(table_interp(P, P.V, P.dyV, field, l), P.divB2);
+            dpot = div_exact(table_interp(P, P.dV, P.dydV, field, l), P.divB2);
         } else {
             bool oor;
             pot = V_exact<false>(P, field, &oor);

@@ -4,6 +4,8 @@
 // Hilltop (src/potential.cpp:77-83):
 //   V  = V0 (1 - c1 v^2) / B^2,  c1 = (1 - ns)/4
 //   V' = (c2 v) / B^2,           c2 = -V0 (1 - ns)/2
+// The division by B^2 is the correctly rounded quotient formed on the integer
+// pipes (div_exact, exact.cuh), bit-equal to the IEEE division.
 // Tabulated (src/potential.cpp:11-68): the bracket l is the unique index with
 // x[l-1] >= v > x[l] on the descending table, so the reference's hinted walk
 // and its binary search agree; here a binary search over monotone 64-bit
@@ -60,9 +62,10 @@ __device__ __forceinline__ int table_walk(const PotDev& P, double v, int l, bool
     return l;
 }
 
-// interpolate_from_table, src/potential.cpp:52-68
+// interpolate_from_table, src/potential.cpp:52-68; the division by the
+// bracket width x[l-1] - x[l] uses the bracket's precomputed divisor (exact).
 __device__ __forceinline__ double table_interp(const PotDev& P, const double* y, const double* dy, double v, int l) {
-    return __ldg(&y[l]) + ((v - __ldg(&P.x[l])) * __ldg(&dy[l])) / __ldg(&P.dxl[l]);
+    return __ldg(&y[l]) + div_exact((v - __ldg(&P.x[l])) * __ldg(&dy[l]), P.ddx[l]);
 }
 
 // potential_derivative at one site (src/potential.cpp:103-112), exact form.
@@ -70,10 +73,10 @@ template <bool TABLE>
 __device__ __forceinline__ double dV_exact(const PotDev& P, double v, bool* oor) {
     if (TABLE) {
         const int l = table_bracket(P, v, oor);
-        return table_interp(P, P.dV, P.dydV, v, l) / P.B2;
+        return div_exact(table_interp(P, P.dV, P.dydV, v, l), P.divB2);
     }
     *oor = false;
-    return (P.c2 * v) / P.B2;
+    return div_exact(P.c2 * v, P.divB2);
 }
 
 // potential(v) (src/potential.cpp:91-98), exact form.
@@ -81,10 +84,10 @@ template <bool TABLE>
 __device__ __forceinline__ double V_exact(const PotDev& P, double v, bool* oor) {
     if (TABLE) {
         const int l = table_bracket(P, v, oor);
-        return table_interp(P, P.V, P.dyV, v, l) / P.B2;
+        return div_exact(table_interp(P, P.V, P.dyV, v, l), P.divB2);
     }
     *oor = false;
-    return (P.V0 * (1.0 - P.c1 * (v * v))) / P.B2;
+    return div_exact(P.V0 * (1.0 - P.c1 * (v * v)), P.divB2);
 }
 
 // Table value of V for the lattice-mean reduction (times B^2, no divide):

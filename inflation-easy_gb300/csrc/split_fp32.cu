@@ -229,13 +229,16 @@ __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4(SplitBufs B, Spli
                                        blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr, rev != 0);
 }
 
-// Polls *p (acquire) until it reaches v: at most kSpinPolls polls with a short
-// sleep between them (about half a second in all), far beyond any step's
-// length.  On giving up it marks the step IEGPU_ETIMEOUT and returns false.
-constexpr unsigned kSpinPolls = 1u << 20;
+// Polls *p (acquire) until it reaches v: at most wait_limit(ctl) polls (by
+// default 2^20) with a short sleep between them (about half a second in all),
+// far beyond any step's length.  On giving up it marks the step
+// IEGPU_ETIMEOUT, ends the call's stepping (active = 0) and returns false.
+// The control block's spin_bias (a test hook, 0 otherwise) raises the target.
 __device__ __forceinline__ bool spin_until(const unsigned* p, unsigned v, SplitCtl* ctl) {
-    for (unsigned t = 0; t < kSpinPolls; ++t) {
-        if (ld_acquire(p) >= v) return true;
+    const unsigned lim = wait_limit(ctl);
+    const unsigned target = v + __ldcg(&ctl->spin_bias);
+    for (unsigned t = 0; t < lim; ++t) {
+        if (ld_acquire(p) >= target) return true;
         __nanosleep(64);
     }
     if (atomicCAS(&ctl->error, 0, IEGPU_ETIMEOUT) == 0) ctl->errval = 0.0;
@@ -876,10 +879,13 @@ static int sctl_down(iegpu_ctx* c) {
     if (check_cuda(c, cudaMemcpyAsync(c->sctl_h, c->sctl, sizeof(SplitCtl), cudaMemcpyDeviceToHost, c->stream), "split control download"))
         return IEGPU_ECUDA;
     if (sync_and_check(c, "split")) return IEGPU_ECUDA;
-    if (c->sctl_h->deferred)
-        return set_error(c, IEGPU_ECUDA, "internal: a scalar update was left unapplied at the end of a call");
+    // a wait that gave up ends the call's steps wherever they were, so a
+    // deferred scalar update may be left over; the next call starts from the
+    // host's copy of the background
     if (c->sctl_h->error == IEGPU_ETIMEOUT)
         return set_error(c, IEGPU_ETIMEOUT, "a wait in the step kernel gave up (bulk copy or step barrier)");
+    if (c->sctl_h->deferred)
+        return set_error(c, IEGPU_ECUDA, "internal: a scalar update was left unapplied at the end of a call");
     if (c->sctl_h->error == IEGPU_ERANGE) {
         return set_error(c, IEGPU_ERANGE,
                          "Field value near %.17g is outside the numerical potential range [%.17g, %.17g].\n",
@@ -905,6 +911,8 @@ static void sctl_fill(iegpu_ctx* c, const iegpu_bg* bg, int mode) {
     C.pre_claim = 0;
     C.pre.ok = 0;
     C.deferred = 0;
+    C.spin_polls = c->wait_polls;
+    C.spin_bias = c->wait_bias;
 }
 
 static void sctl_bg(const iegpu_ctx* c, iegpu_bg* bg) {

@@ -855,6 +855,13 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 constexpr unsigned kMbarPolls = 1u << 20;   // far beyond any copy's latency (about a second at most)
 
+// Poll limit of the step kernels' bounded waits: the control block's value
+// (set through iegpu_set_wait_limit), or the default.
+__device__ __forceinline__ unsigned wait_limit(const SplitCtl* ctl) {
+    const unsigned v = __ldcg(&ctl->spin_polls);
+    return v ? v : kMbarPolls;
+}
+
 constexpr int kPrefetch = 3;   // planes in flight ahead of the one being computed
 constexpr int kPhiSlots = 6;   // three stencil planes + kPrefetch
 constexpr int kPiSlots = 4;    // one plane in use + kPrefetch
@@ -1119,12 +1126,17 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     float* wv = wk + 3 * kWin + 1;
     __shared__ int nk_s, nv_s, active_s;
     __shared__ float cf[6];
+    __shared__ unsigned tma_fail_g, tma_issued, mbar_limit;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     // the control block is read through L2: in a persistent launch the last
     // CTA of the step before wrote it during this kernel
     if (tid == 0) {
         const SplitCtl& Cc = *ctl;
-        active_s = __ldcg(&Cc.active);
+        // a step that a failed wait of this call has marked is not taken
+        active_s = __ldcg(&Cc.active) && !__ldcg(&Cc.error);
+        tma_fail_g = 0xFFFFFFFFu;
+        tma_issued = 0u;
+        mbar_limit = wait_limit(ctl);
         cf[0] = __ldcg(&Cc.d); cf[1] = __ldcg(&Cc.lapl); cf[2] = __ldcg(&Cc.fric);
         cf[3] = __ldcg(&Cc.pn); cf[4] = __ldcg(&Cc.kv);
         nk_s = __ldcg(&Cc.wk.n);
@@ -1156,7 +1168,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     constexpr int NB = PF + 2;
     __shared__ __align__(8) unsigned long long bars[TMA ? NB : 1];
     unsigned G0 = 0;
-    bool tma_ok = true;
+    bool aborted = false;   // a bulk-copy wait gave up: no more copies are issued
     if (TMA) {
         if (tid == 0) {
             for (int q = 0; q < NB; ++q) mbar_init(&bars[q], 1);
@@ -1186,7 +1198,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     }
     const bool marcher = w <= TJ;
     bool first = true;
-    for (long long u = rev ? u1 : u0; marcher && (rev ? u > u0 : u < u1);) {
+    for (long long u = rev ? u1 : u0; marcher && !aborted && (rev ? u > u0 : u < u1);) {
         // this march covers units [s, e) of one row tile
         const Row4March M = row4_march<N, TJ>(u, u0, u1, rev);
         const int j0 = M.j0, i0 = M.i0, CH = M.CH;
@@ -1197,6 +1209,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         // TMA group g, issued by warp 0 (lane 0 arms the barrier first)
         auto issue_group = [&](int gi) {
             unsigned long long* bar = &bars[(G0 + (unsigned)(gi + 1)) % NB];
+            if (lane == 0) tma_issued = G0 + (unsigned)(gi + 2);   // groups issued so far
             const int nphi = gi < 0 ? 2 * (TJ + 3) : (gi <= CH ? TJ + 3 : 0);
             const int npi = (gi >= 0 && gi <= CH) ? TJ + 1 : 0;
             if (lane == 0) mbar_expect_tx(bar, (unsigned)((nphi + npi) * N * 4));
@@ -1217,9 +1230,10 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             }
         };
         auto wait_group = [&](int gi) {
-            // after one wait has given up, the step is marked failed and no more waits are made
+            // a wait that gives up records its group; after the next march
+            // barrier every marcher stops and warp 0 issues nothing more
             const unsigned Gq = G0 + (unsigned)(gi + 1);
-            if (tma_ok && !mbar_wait(&bars[Gq % NB], (Gq / NB) & 1u, kMbarPolls)) tma_ok = false;
+            if (!mbar_wait(&bars[Gq % NB], (Gq / NB) & 1u, mbar_limit)) atomicMin(&tma_fail_g, Gq);
         };
         float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
         if (TMA) {
@@ -1267,6 +1281,10 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 cp_wait<PF - 1>();
             }
             march_sync<NTH>();
+            if (TMA && *(volatile unsigned*)&tma_fail_g != 0xFFFFFFFFu) {
+                aborted = true;
+                break;
+            }
             // planes PF ahead go into the slots of planes no longer read
             if (TMA) {
                 if (w == 0) {
@@ -1345,8 +1363,20 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
         G0 += (unsigned)(CH + PF + 2);
         march_sync<NTH>();   // the ring is refilled by the next march
     }
-    if (TMA && !tma_ok) {
-        if (atomicCAS(&ctl->error, 0, IEGPU_ETIMEOUT) == 0) ctl->errval = 0.0;
+    if (TMA && marcher) {
+        // a wait gave up: drain the groups still in flight (bounded waits, in
+        // issue order, at most NB of them) before the CTA leaves, so no bulk
+        // copy lands in shared memory after it has exited
+        march_sync<NTH>();
+        const unsigned fg = *(volatile unsigned*)&tma_fail_g;
+        if (fg != 0xFFFFFFFFu) {
+            if (tid == 0) {
+                const unsigned last = *(volatile unsigned*)&tma_issued;
+                for (unsigned Gq = fg; Gq < last; ++Gq) mbar_wait(&bars[Gq % NB], (Gq / NB) & 1u, kMbarPolls);
+                if (atomicCAS(&ctl->error, 0, IEGPU_ETIMEOUT) == 0) ctl->errval = 0.0;
+            }
+            march_sync<NTH>();
+        }
     }
     cp_wait<0>();
     if (bad) {

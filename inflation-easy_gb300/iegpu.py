@@ -120,6 +120,8 @@ def load() -> C.CDLL:
         "iegpu_shell_spectrum_noalloc": (I, [P, P, I, P, P, P]),
         "iegpu_set_shape": (I, [P, I, I, I]),
         "iegpu_set_persistent": (I, [P, I]),
+        "iegpu_set_wait_limit": (I, [P, C.c_uint, I]),
+        "iegpu_measure_fp64_rate": (I, [I, dp]),
         "iegpu_initialize_post_inflation": (I, [P, D, D, I, C.POINTER(Bg)]),
         "iegpu_evolve_derivs_post_inflation": (I, [P, D, D, C.POINTER(Bg)]),
         "iegpu_post_inflation_leapfrog": (I, [P, D, D, D, I, C.POINTER(Bg), C.POINTER(I), dp]),
@@ -326,6 +328,11 @@ class Lattice:
     def set_persistent(self, on: bool) -> None:
         self._check(self.lib.iegpu_set_persistent(self.h, int(bool(on))))
 
+    def set_wait_limit(self, polls: int, unreachable: bool = False) -> None:
+        """Poll limit of the split form's bounded device waits (0: default);
+        unreachable makes the persistent step barrier give up (tests)."""
+        self._check(self.lib.iegpu_set_wait_limit(self.h, polls, int(unreachable)))
+
     def autotune(self, bg: Bg):
         r, p, ch = C.c_int(), C.c_int(), C.c_int()
         self._check(self.lib.iegpu_autotune(self.h, C.byref(bg), C.byref(r), C.byref(p), C.byref(ch)))
@@ -424,6 +431,16 @@ class Lattice:
         v = C.c_double()
         self._check(self.lib.iegpu_sum(self.h, field, C.byref(v)))
         return v.value
+
+
+def measure_fp64_rate(op: int) -> float:
+    """FP64 thread instructions per second of the current device (op 0: DFMA,
+    1: DADD, 2: DMUL)."""
+    out = C.c_double()
+    rc = load().iegpu_measure_fp64_rate(op, C.byref(out))
+    if rc:
+        raise IegpuError(rc, "FP64 rate probe failed")
+    return out.value
 
 
 def _dp(a: np.ndarray):

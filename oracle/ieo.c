@@ -6,7 +6,7 @@
  * with an explicit state struct.  Floating-point expressions are evaluated in
  * exactly the order the reference evaluates them, and reductions run serially
  * in the reference's loop order, because the oracle is pinned bit-for-bit
- * against the reference program built from source (oracle/build_ref.sh).
+ * against the reference program built from source (oracle/build_ref.py).
  * Compile with -ffp-contract=off: fused multiply-adds would change results.
  *
  * Parity: pinned (tests/test_oracle_pin.py compares the full results/ .dat
@@ -57,6 +57,7 @@ struct ieo_state {
     double *dntmp, *kdn[7];   /* deltaN RK scratch (DeltaNRKScratch, src/evolution.cpp:1040-1059) */
     int rk_post;        /* post-inflation right-hand side (g_use_post_inflation_rhs) */
     double rk45_err;    /* error norm of the last RK45 attempt */
+    int engine_arith;   /* the GPU engine's lattice-sum arithmetic (see ieo_set_engine_arith) */
 };
 
 static inline double pw2(double x) { return x * x; }
@@ -297,9 +298,14 @@ void ieo_set_threads(int n) {
 #endif
 }
 
+static int g_engine_arith_default = 0;
+
+void ieo_set_engine_arith_default(int on) { g_engine_arith_default = on != 0; }
+
 ieo_state* ieo_create(const ieo_params* p) {
     ieo_state* S = (ieo_state*)calloc(1, sizeof(ieo_state));
     if (!S) return NULL;
+    S->engine_arith = g_engine_arith_default;
     S->p = *p;
     S->p.dx = p->L / (double)p->N;
     const size_t N = (size_t)p->N;
@@ -428,6 +434,119 @@ double ieo_potential(ieo_state* S, double v) {
     return hill_V(&S->p, v);
 }
 
+
+/* ------------------------------------------------------------------------- */
+/* exact sums (engine-arithmetic mode)                                       */
+/* ------------------------------------------------------------------------- */
+
+/* A fixed-point accumulator over the whole double range (a "long
+ * accumulator", Kulisch): 32-bit chunks held in signed 64-bit limbs, least
+ * significant bit 2^-1074, so every finite double is added without error.
+ * The total is rounded once to the nearest double, ties to even.  This is an
+ * independent restatement of what the GPU engine's exact sums compute (the
+ * correctly rounded exact sum); Python's math.fsum gives the same value. */
+#define XS_LIMBS 70
+typedef struct { int64_t l[XS_LIMBS]; long count; int nonfinite; } xsum_t;
+
+static void xs_init(xsum_t* X) { memset(X, 0, sizeof *X); }
+
+static void xs_norm(xsum_t* X) {
+    int64_t carry = 0;
+    for (int k = 0; k < XS_LIMBS; ++k) {
+        const int64_t v = X->l[k] + carry;
+        const int64_t lo = v & 0xFFFFFFFFLL;
+        carry = (v - lo) / 4294967296LL;   /* exact: v - lo is a multiple of 2^32 */
+        X->l[k] = lo;
+    }
+    X->l[XS_LIMBS - 1] += carry * 4294967296LL;
+    X->count = 0;
+}
+
+static void xs_add(xsum_t* X, double t) {
+    uint64_t b;
+    memcpy(&b, &t, sizeof b);
+    int e = (int)((b >> 52) & 0x7FF);
+    uint64_t m = b & 0x000FFFFFFFFFFFFFULL;
+    if (e == 0x7FF) { X->nonfinite = 1; return; }
+    if (e == 0) { if (!m) return; e = 1; } else m |= 1ULL << 52;
+    const int pos = e - 1;                 /* bit position of m's lowest bit (2^-1074 is position 0) */
+    const int k = pos >> 5, r = pos & 31;
+    const unsigned __int128 v = (unsigned __int128)m << r;
+    const int64_t c0 = (int64_t)(uint64_t)(v & 0xFFFFFFFFu);
+    const int64_t c1 = (int64_t)(uint64_t)((v >> 32) & 0xFFFFFFFFu);
+    const int64_t c2 = (int64_t)(uint64_t)(v >> 64);
+    if (b >> 63) { X->l[k] -= c0; X->l[k + 1] -= c1; X->l[k + 2] -= c2; }
+    else { X->l[k] += c0; X->l[k + 1] += c1; X->l[k + 2] += c2; }
+    if (++X->count >= (1L << 29)) xs_norm(X);
+}
+
+static void xs_merge(xsum_t* X, const xsum_t* Y) {
+    for (int k = 0; k < XS_LIMBS; ++k) X->l[k] += Y->l[k];
+    X->nonfinite |= Y->nonfinite;
+    X->count += Y->count;
+    if (X->count >= (1L << 29)) xs_norm(X);
+}
+
+static double xs_round(xsum_t* X) {
+    if (X->nonfinite) return NAN;
+    xs_norm(X);
+    int neg = X->l[XS_LIMBS - 1] < 0;
+    uint32_t w[XS_LIMBS];
+    if (neg) {   /* magnitude of the two's-complement value in 32-bit chunks */
+        int64_t borrow = 0;
+        for (int k = 0; k < XS_LIMBS; ++k) {
+            int64_t v = -X->l[k] - borrow;
+            borrow = 0;
+            while (v < 0) { v += 4294967296LL; ++borrow; }
+            w[k] = (uint32_t)v;
+        }
+    } else {
+        for (int k = 0; k < XS_LIMBS; ++k) w[k] = (uint32_t)X->l[k];
+    }
+    int top = -1;
+    for (int k = XS_LIMBS - 1; k >= 0 && top < 0; --k)
+        if (w[k]) { int q = 31; while (!((w[k] >> q) & 1u)) --q; top = 32 * k + q; }
+    if (top < 0) return 0.0;
+#define XS_BIT(p) ((p) < 0 ? 0u : ((w[(p) >> 5] >> ((p) & 31)) & 1u))
+    int lsb = top - 52;
+    if (lsb < 0) lsb = 0;                  /* subnormal range: exact */
+    uint64_t M = 0;
+    for (int p = top; p >= lsb; --p) M = (M << 1) | XS_BIT(p);
+    if (lsb > 0) {
+        const unsigned rb = XS_BIT(lsb - 1);
+        int sticky = 0;
+        for (int p = lsb - 2; p >= 0 && !sticky; --p) sticky = XS_BIT(p) != 0;
+        if (rb && (sticky || (M & 1u))) {
+            M += 1;
+            if (M >> 53) { M >>= 1; lsb += 1; }
+        }
+    }
+#undef XS_BIT
+    const double v = ldexp((double)M, lsb - 1074);
+    return neg ? -v : v;
+}
+
+/* The correctly rounded exact sum of x[0..n). */
+double ieo_exact_sum(const double* x, size_t n) {
+    xsum_t X;
+    xs_init(&X);
+    for (size_t i = 0; i < n; ++i) xs_add(&X, x[i]);
+    return xs_round(&X);
+}
+
+void ieo_set_engine_arith(ieo_state* S, int on) { S->engine_arith = on != 0; }
+
+/* pow(x, y) as the engine evaluates the Friedmann update's powers: exact
+ * products and quotients for y = 0, 1, 2, -1, libm pow otherwise. */
+static double eng_pow(const ieo_state* S, double x, double y) {
+    if (!S->engine_arith) return pow(x, y);
+    if (y == 0.0) return 1.0;
+    if (y == 1.0) return x;
+    if (y == 2.0) return x * x;
+    if (y == -1.0) return 1.0 / x;
+    return pow(x, y);
+}
+
 /* potential_derivative(i,j,k), src/potential.cpp:103-112 */
 static inline double pot_deriv_site(ieo_state* S, size_t id) {
     if (S->p.numerical_potential) {
@@ -439,8 +558,46 @@ static inline double pot_deriv_site(ieo_state* S, size_t id) {
     return hill_dV(&S->p, S->f[id]);
 }
 
+/* The engine's potential sum: exact sum f^2 (hilltop, then
+ * V0 (N^3 - c1 sum) / B^2 / N^3) or exact sum of V + (v - x_l) slope_l
+ * (table, then sum / B^2 / N^3), slope_l = (V_{l-1} - V_l)/(x_{l-1} - x_l). */
+static double potential_energy_engine(ieo_state* S) {
+    const size_t gs = S->gs;
+    const long n = (long)gs;
+    const double* f = S->f;
+    xsum_t tot;
+    xs_init(&tot);
+    int bad = 0;
+    #pragma omp parallel
+    {
+        xsum_t X;
+        xs_init(&X);
+        #pragma omp for schedule(static) reduction(|:bad)
+        for (long id = 0; id < n; ++id) {
+            const double v = f[id];
+            if (S->p.numerical_potential) {
+                const int l = bracket(S, v, 1);
+                if (l < 0) { bad = 1; continue; }
+                const double slope = (S->tV[l - 1] - S->tV[l]) / (S->tphi[l - 1] - S->tphi[l]);
+                xs_add(&X, S->tV[l] + (v - S->tphi[l]) * slope);
+            } else {
+                xs_add(&X, v * v);
+            }
+        }
+        #pragma omp critical
+        xs_merge(&tot, &X);
+    }
+    if (bad) return 0.0;
+    const double Pn = xs_round(&tot);
+    const double g = (double)gs, B2 = pw2(S->p.rescale_B);
+    if (S->p.numerical_potential) return (Pn / B2) / g;
+    const double c1 = (1.0 - S->p.ns) / 4.0;
+    return (S->p.V0 * (g - c1 * Pn) / B2) / g;
+}
+
 /* potential_energy(), src/potential.cpp:151-171 (serial) */
 double ieo_potential_energy(ieo_state* S) {
+    if (S->engine_arith) return potential_energy_engine(S);
     double pot = 0.0;
     const size_t gs = S->gs;
     if (S->p.numerical_potential) {
@@ -642,8 +799,38 @@ void ieo_initializeGW(ieo_state* S) {
      (F)[IDX(N, i, jm, k)] + (F)[IDX(N, ip, j, k)] + (F)[IDX(N, im, j, k)] -   \
      (T)6 * (F)[IDX(N, i, j, k)])
 
+/* The engine's gradient sum: G = exact sum f lapl(f), gradient = -G. */
+static double gradient_energy_engine(ieo_state* S) {
+    const int N = S->p.N;
+    const double* f = S->f;
+    xsum_t tot;
+    xs_init(&tot);
+    #pragma omp parallel
+    {
+        xsum_t X;
+        xs_init(&X);
+        #pragma omp for schedule(static)
+        for (int i = 0; i < N; ++i) {
+            const int ip = (i == N - 1) ? 0 : i + 1, im = (i == 0) ? N - 1 : i - 1;
+            for (int j = 0; j < N; ++j) {
+                const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
+                for (int k = 0; k < N; ++k) {
+                    const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
+                    xs_add(&X, f[IDX(N, i, j, k)] * LAPL_AT(double, f, N, i, j, k, ip, im, jp, jm, kp, km));
+                }
+            }
+        }
+        #pragma omp critical
+        xs_merge(&tot, &X);
+    }
+    const double gradient = -xs_round(&tot);
+    const double norm = pw2(1.0 / (S->a * S->p.dx));
+    return 0.5 * gradient * norm / (double)S->gs;
+}
+
 /* gradient_energy(), src/evolution.cpp:130-136 (serial) */
 double ieo_gradient_energy(ieo_state* S) {
+    if (S->engine_arith) return gradient_energy_engine(S);
     const int N = S->p.N;
     const double* f = S->f;
     double gradient = 0.0;
@@ -664,7 +851,14 @@ double ieo_gradient_energy(ieo_state* S) {
 /* kin_energy(), src/evolution.cpp:139-145 */
 double ieo_kin_energy(ieo_state* S) {
     double e = 0.0;
-    for (size_t id = 0; id < S->gs; ++id) e += pw2(S->fd[id]);
+    if (S->engine_arith) {
+        xsum_t X;
+        xs_init(&X);
+        for (size_t id = 0; id < S->gs; ++id) xs_add(&X, pw2(S->fd[id]));
+        e = xs_round(&X);
+    } else {
+        for (size_t id = 0; id < S->gs; ++id) e += pw2(S->fd[id]);
+    }
     e /= (double)S->gs;
     return 0.5 * pow(S->a, 2.0 * S->p.rescale_s - 2.0) * e;
 }
@@ -674,7 +868,7 @@ int ieo_evolve_derivs(ieo_state* S, double d) {
     const ieo_params* p = &S->p;
     const int N = p->N;
     const double s = p->rescale_s;
-    const double laplnorm = pow(S->a, -2.0 * s) / pw2(p->dx);
+    const double laplnorm = eng_pow(S, S->a, -2.0 * s) / pw2(p->dx);
     const double sfev1 = s + 1.0;
     const double sfev2 = -2.0 * s + 2.0;
 
@@ -683,11 +877,11 @@ int ieo_evolve_derivs(ieo_state* S, double d) {
     if (S->err) return 1;
     S->ad2 = (-2.0 * S->ad - 2.0 * S->a / d / sfev1 * (
         1.0 - sqrt(1.0 + 2.0 * d * sfev1 * S->ad / S->a +
-        pw2(d) * sfev1 * pow(S->a, sfev2) * (2.0 * ge / 3.0 + pe)))) / d;
+        pw2(d) * sfev1 * eng_pow(S, S->a, sfev2) * (2.0 * ge / 3.0 + pe)))) / d;
     S->ad += 0.5 * d * S->ad2;
 
     const double friction = (2.0 + s) * S->ad / S->a;
-    const double potnorm = pow(S->a, 2.0 - 2.0 * s);
+    const double potnorm = eng_pow(S, S->a, 2.0 - 2.0 * s);
     double* f = S->f;
     double* fd = S->fd;
 
@@ -708,7 +902,7 @@ int ieo_evolve_derivs(ieo_state* S, double d) {
     if (S->err) return 1;
 
     if (p->calculate_SIGW) {
-        const double srcAmp = 2.0 * pow(S->a, -2.0 * s);
+        const double srcAmp = 2.0 * eng_pow(S, S->a, -2.0 * s);
         const double half_over_dx = 0.5 / p->dx;
         #pragma omp parallel for schedule(static)
         for (int i = 0; i < N; ++i) {
@@ -1287,7 +1481,7 @@ void ieo_set_rk_post(ieo_state* S, int post) { S->rk_post = post != 0; }
 
 /* inflation_rescaled_step, src/evolution.cpp:338-340 */
 double ieo_rescaled_step(const ieo_state* S, double astep) {
-    return S->p.dt * pow(astep, S->p.rescale_s - 1.0);
+    return S->p.dt * eng_pow(S, astep, S->p.rescale_s - 1.0);
 }
 
 int ieo_leapfrog_steps(ieo_state* S, int nsteps) {

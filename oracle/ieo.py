@@ -94,6 +94,8 @@ def load() -> C.CDLL:
         "ieo_rk45_accept_deltaN": (I, [P, dp, D]),
         "ieo_rk45_clamp": (D, [P, D, D]), "ieo_rk45_hmax": (D, [P, D]), "ieo_set_rk_post": (None, [P, I]),
         "ieo_rescaled_step": (D, [P, D]), "ieo_leapfrog_steps": (I, [P, I]),
+        "ieo_set_engine_arith": (None, [P, I]), "ieo_exact_sum": (D, [dp, C.c_size_t]),
+        "ieo_set_engine_arith_default": (None, [I]),
         "ieo_fftrn_d": (None, [dp, dp, I, I]), "ieo_fftrn_f": (None, [fp, fp, I, I]),
         "ieo_numbins": (I, [I]),
         "ieo_bin_spectrum": (None, [I, dp, dp, ip, dp]),
@@ -148,6 +150,12 @@ def usr_params(N: int, **kw) -> Params:
     return default_params(N, True, **base)
 
 
+def exact_sum(x) -> float:
+    """Correctly rounded exact sum (the oracle's long accumulator)."""
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    return load().ieo_exact_sum(a.ctypes.data_as(C.POINTER(C.c_double)), a.size)
+
+
 def load_tables(inputs_dir: Path):
     return tuple(np.loadtxt(inputs_dir / n) for n in ("field_values.dat", "potential.dat", "potential_derivative.dat"))
 
@@ -169,6 +177,11 @@ class Oracle:
             dp = C.POINTER(C.c_double)
             self.lib.ieo_set_table(self.h, phi.ctypes.data_as(dp), V.ctypes.data_as(dp), dV.ctypes.data_as(dp),
                                    len(phi))
+
+    def set_engine_arith(self, on: bool = True) -> None:
+        """The engine's lattice-sum arithmetic (exact sums, its potential sum
+        and pow forms) instead of the reference's serial sums."""
+        self.lib.ieo_set_engine_arith(self.h, int(on))
 
     def close(self):
         if self.h:
@@ -352,10 +365,17 @@ def bin_spectrum(N: int, ff: np.ndarray, nyq: np.ndarray):
     return counts, f2
 
 
-def run_program(params: Params, results_dir: Path, inputs_dir: Path, dump_dir: Path | None = None) -> int:
+def run_program(params: Params, results_dir: Path, inputs_dir: Path, dump_dir: Path | None = None,
+                engine_arith: bool = False) -> int:
+    """The reference program's main() restated; engine_arith runs it with the
+    engine's lattice-sum arithmetic (Oracle.set_engine_arith)."""
     lib = load()
-    return lib.ieo_run_program_dump(C.byref(params), str(results_dir).encode(), str(inputs_dir).encode(),
-                                    None if dump_dir is None else str(dump_dir).encode())
+    lib.ieo_set_engine_arith_default(int(engine_arith))
+    try:
+        return lib.ieo_run_program_dump(C.byref(params), str(results_dir).encode(), str(inputs_dir).encode(),
+                                        None if dump_dir is None else str(dump_dir).encode())
+    finally:
+        lib.ieo_set_engine_arith_default(0)
 
 
 def read_state(path: Path) -> dict:

@@ -1,9 +1,10 @@
 """Parity of the CUDA engine with the oracle, operation by operation.
 
 Bit-exact where the engine's per-site arithmetic is the reference's (FFT, the
-deltaN integration, the float mean of saveN, histograms, bin counts); within
-stated tolerances where a lattice-wide sum is formed in a different order
-(the Friedmann update, spectra sums):
+deltaN integration, the float mean of saveN, histograms, bin counts), and for
+whole leapfrog trajectories against the oracle in engine-arithmetic mode
+(the Friedmann update's lattice sums formed exactly, as the engine forms
+them).  Against the reference's serial sums, within stated tolerances:
   * fields after leapfrog steps: max|x_gpu - x_oracle| <= 1e-9 * std(x_oracle)
   * a, ad: relative 1e-12
   * spectrum bins: relative 1e-12 (same modes, different summation order)
@@ -94,6 +95,32 @@ def test_leapfrog_matches_oracle(N, usr, sigw, engine, oracle_mod, tables):
                 assert rel_field_err(lat.download(engine.HD(c)), o.hd_(c)) < 1e-5
 
 
+@pytest.mark.parametrize("N,usr,sigw", [(16, False, False), (32, False, False), (64, False, False),
+                                        (16, True, False), (32, True, False), (16, True, True)])
+def test_leapfrog_bit_exact_with_engine_arithmetic(N, usr, sigw, engine, oracle_mod, tables):
+    """300 leapfrog steps, engine against the oracle in engine-arithmetic mode:
+    the fields, the tensor modes and every background scalar bit for bit.
+    This checks each per-site operation (the stencil, V' with the exact
+    division by B^2, the kick and drift) and the exact lattice sums over a
+    whole trajectory."""
+    p, o = oracle_state(oracle_mod, N, usr, sigw, tables)
+    o.set_engine_arith(True)
+    lat, bg = lattice_like(engine, p, o, usr, sigw, tables)
+    with lat:
+        nsteps = 300
+        taken = lat.leapfrog(p.af, nsteps, bg)
+        assert taken == nsteps
+        o.leapfrog_steps(nsteps)
+        s = o.scalars
+        assert (bg.t, bg.a, bg.ad, bg.ad2) == (s.t, s.a, s.ad, s.ad2)
+        assert np.array_equal(lat.download(engine.F), o.f)
+        assert np.array_equal(lat.download(engine.FD), o.fd)
+        if sigw:
+            for c in range(6):
+                assert np.array_equal(lat.download(engine.H(c)), o.h_(c))
+                assert np.array_equal(lat.download(engine.HD(c)), o.hd_(c))
+
+
 def test_leapfrog_stops_at_af(engine, oracle_mod):
     p, o = oracle_state(oracle_mod, 16, False, False, None)
     lat, bg = lattice_like(engine, p, o, False, False, None)
@@ -124,6 +151,13 @@ def test_single_step_entry_points(engine, oracle_mod):
 
 
 def test_energies_and_means(engine, oracle_mod, tables):
+    """kin, gradient and potential energies.  The engine sums exactly, so it
+    equals the oracle in engine-arithmetic mode bit for bit, and its sum of
+    f lapl(f) equals math.fsum of the same per-site terms.  The reference's
+    serial sum of f lapl(f) cancels (the terms are of order |f| |lapl f|, the
+    total of order |grad f|^2), so it keeps only about six digits of the
+    gradient energy; that is the comparison with the reference mode below."""
+    import math
     for usr in (False, True):
         p, o = oracle_state(oracle_mod, 16, usr, False, tables, steps=20)
         lat, bg = lattice_like(engine, p, o, usr, False, tables)
@@ -132,6 +166,16 @@ def test_energies_and_means(engine, oracle_mod, tables):
             ko, go, vo = o.energies()
             assert np.isclose(k, ko, rtol=1e-12) and np.isclose(v, vo, rtol=1e-12)
             assert np.isclose(g, go, rtol=1e-6, atol=1e-12 * abs(vo))
+            o.set_engine_arith(True)
+            assert (k, g, v) == o.energies()
+            o.set_engine_arith(False)
+            N = p.N
+            f = o.f.reshape(N, N, N)
+            lap = (np.roll(f, -1, 2) + np.roll(f, 1, 2) + np.roll(f, -1, 1) + np.roll(f, 1, 1) + np.roll(f, -1, 0)
+                   + np.roll(f, 1, 0) - 6.0 * f)
+            G = math.fsum((f * lap).ravel())
+            a, dx = bg.a, p.L / N
+            assert g == 0.5 * (-G) * ((1.0 / (a * dx)) * (1.0 / (a * dx))) / N ** 3
             sf, sfd, sf2 = lat.means()
             assert np.isclose(sf, o.f.sum(), rtol=1e-13)
             assert np.isclose(sfd, o.fd.sum(), rtol=1e-12)

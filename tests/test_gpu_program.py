@@ -5,10 +5,12 @@ engine through the C ABI) with the reference.
    results file is compared number by number at its printed precision, the
    final lattice state element by element.
 2. Against the oracle program on the hilltop workload at N = 64 (the
-   reference's own CPU-sized case) at full precision:
-     a, H, <phi> at every save        relative 1e-10
-     P_dphi and P_zeta per k-bin      relative 1e-8 (bins with modes)
-     k-shell bin counts               exact
+   reference's own CPU-sized case) and the USR table at N = 32, at full
+   precision (details in test_program_full_precision_against_oracle):
+     engine-arithmetic oracle: a, H bit for bit; spectra per bin 1e-11
+     reference oracle: a, H, <phi> relative 1e-10; P_dphi, P_zeta per k-bin
+     relative 1e-8, or twice the reference's own rounding floor where that
+     is larger; k-shell bin counts exact
 """
 from __future__ import annotations
 
@@ -151,31 +153,59 @@ def _precise(path):
     return out
 
 
+def _bin_dev(got, ref):
+    """Largest relative deviation per k-bin over every save (bins where the
+    reference is zero: the absolute value)."""
+    dev = np.zeros(len(ref[0]))
+    for x, y in zip(got, ref):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            dev = np.maximum(dev, np.where(y != 0, np.abs(x / y - 1), np.abs(x)))
+    return dev
+
+
 @pytest.mark.parametrize("N,numerical", [(64, 0), (32, 1)])
 def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mod):
+    """The whole program (inflation to af, deltaN stage, spectra) against the
+    oracle program twice:
+      * in engine-arithmetic mode (lattice sums formed exactly, as the engine
+        forms them): a and H bit for bit at every save, <phi> to 1e-14 (its
+        output sum is formed in another order), P_dphi and P_zeta per k-bin to
+        1e-11 (the spectra's bin sums likewise);
+      * in reference mode (serial sums, libm pow): a, H, <phi> relative 1e-10;
+        P_dphi and P_zeta per k-bin relative 1e-8, except where the
+        reference's own rounding floor is larger.  The floor is measured here
+        as the deviation between the two oracle runs, i.e. between two valid
+        roundings of the reference's algorithm; a bin whose floor exceeds
+        5e-9 is held to twice its floor instead, and is printed.
+    Bin counts are exact in both."""
     src = GOLDEN / ("n16_usr_sigw" if numerical else "n16_hilltop")
     text = (src / "params.txt").read_text()
     wd = run_main(tmp_path, text, N, numerical, 0)
     p = oracle_mod.params_from_text(text, N, bool(numerical), False)
-    od = tmp_path / "oracle"
-    od.mkdir()
-    assert oracle_mod.run_program(p, od / "results", INPUTS, od) == 0
-    g, o = _precise(wd / "dump" / "precise.txt"), _precise(od / "precise.txt")
-    assert len(g["means"]) == len(o["means"])
-    for x, y in zip(g["means"], o["means"]):
+    od, oe = tmp_path / "oracle", tmp_path / "oracle_engine"
+    for d, mode in ((od, False), (oe, True)):
+        d.mkdir()
+        assert oracle_mod.run_program(p, d / "results", INPUTS, d, engine_arith=mode) == 0
+    g, o, e = (_precise(x / "precise.txt") for x in (wd / "dump", od, oe))
+    assert len(g["means"]) == len(o["means"]) == len(e["means"])
+    for x, y, z in zip(g["means"], o["means"], e["means"]):
         assert np.allclose(x[[1, 2, 4]], y[[1, 2, 4]], rtol=1e-10, atol=0)  # a, <phi>, H
-    worst = {}
+        assert x[1] == z[1] and x[4] == z[4]                                 # a, H
+        assert np.allclose(x[2], z[2], rtol=1e-14, atol=0)                   # <phi>
     for tag in ("spectrum", "spectrumN"):
-        assert len(g[tag]) == len(o[tag])
-        dev = np.zeros(len(o[tag][0]))
-        for x, y in zip(g[tag], o[tag]):
-            with np.errstate(divide="ignore", invalid="ignore"):
-                dev = np.maximum(dev, np.where(y != 0, np.abs(x / y - 1), np.abs(x)))
-        worst[tag] = dev
-        print(f"{tag} N={N}: max rel dev over bins>=1 = {dev[1:].max():.3e}; per bin: "
-              + " ".join(f"{v:.1e}" for v in dev))
-    for tag, dev in worst.items():
-        assert dev[1:].max() < 1e-7, tag
+        assert len(g[tag]) == len(o[tag]) == len(e[tag])
+        dev_ref = _bin_dev(g[tag], o[tag])
+        dev_eng = _bin_dev(g[tag], e[tag])
+        floor = _bin_dev(e[tag], o[tag])
+        bound = np.where(floor > 5e-9, 2.0 * floor, 1e-8)
+        exempt = np.nonzero(floor[1:] > 5e-9)[0] + 1
+        print(f"{tag} N={N}: vs engine-mode oracle max {dev_eng[1:].max():.2e}; vs reference max "
+              f"{dev_ref[1:].max():.2e}; reference floor max {floor[1:].max():.2e}; bins held to 2x floor: "
+              f"{exempt.tolist()}")
+        print(f"{tag} N={N} per bin vs reference: " + " ".join(f"{v:.1e}" for v in dev_ref))
+        print(f"{tag} N={N} per bin floor:        " + " ".join(f"{v:.1e}" for v in floor))
+        assert dev_eng[1:].max() < 1e-11, tag
+        assert np.all(dev_ref[1:] <= bound[1:]), tag
     # exact bin counts
     for name in ("spectra.dat", "spectraN.dat"):
         ca = [r[1] for r in parse_numbers(wd / "results" / name)]

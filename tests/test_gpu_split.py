@@ -249,3 +249,23 @@ def test_split_persistent_launch_matches(N, usr, shape, engine, tables):
         assert np.array_equal(fa, fb) and np.array_equal(fda, fdb)
     taken = [r[0] for r in out[0]]
     assert taken[:2] == [150, 70] and 0 < taken[2] < 100
+
+
+def test_split_whole_run_error_128(engine, tmp_path):
+    """The split form's error over a whole run: 128^3 hilltop (the reference's
+    params.analytic.txt with ns = 0.965, seed 8), the inflation loop to
+    af = 2N = 256 and the deltaN stage, split against the plain FP64 form from
+    the same device initial conditions, every save compared at full
+    precision.  Bars: P_zeta and P_dphi per k-bin relative 1e-4 at every save
+    (the split form's stated budget), <dphi^2> 1e-4, H and a relative 1e-9."""
+    import form_error as fe
+    text = fe.preset_text(fe.HILLTOP, 128)
+    ref = fe.run_program(text, tmp_path / "fp64", "fp64")
+    got = fe.run_program(text, tmp_path / "split", "split")
+    err = fe.compare(ref, got)
+    print({k: v for k, v in err.items() if k != "H_per_save"})
+    assert err["saves"] > 10
+    assert err["P_zeta"]["max"] <= 1e-4
+    assert err["P_dphi"]["max"] <= 1e-4
+    assert err["dphi2_max"] <= 1e-4
+    assert err["H_max"] <= 1e-9 and err["a_max"] <= 1e-9
