@@ -58,9 +58,11 @@ UNIT = "site-updates/s"
 # algorithmic HBM bytes per site of the dominant kernel of one step
 BYTES_STEP_SPLIT = 16  # split form: read dphi, dpi; write dphi, dpi (FP32)
 BYTES_STEP_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
-# FP64 thread instructions per site of one plain FP64 leapfrog step (k_lsum +
-# k_kick, hilltop) and per deltaN site-step (k_deltaN, hilltop), from ncu
-FP64_INST_STEP = 19
+# FP64 thread instructions per site of one plain FP64 leapfrog step (k_lsum:
+# six DADD and one DMUL of the Laplacian, the sums' products on the integer
+# pipes; k_kick: six DMUL, four DADD; hilltop) and per deltaN site-step
+# (k_deltaN, hilltop, from ncu)
+FP64_INST_STEP = 17
 DN_FP64_INST = 25
 BYTES_STEP_SIGW = 112  # split form with SIGW: 16 + read and write 6 h_ij and 6 h_ij' (FP32)
 BYTES_STEP_POST = 128  # post-inflation phase: read and write f, fd (FP64) and 6 h_ij, 6 h_ij' (FP32)
@@ -565,9 +567,22 @@ def engine_arm(args):
     # headline: the plain FP64 form (the reference's precision and per-site
     # arithmetic); the clocks are sampled from 1.5 s before to 0.5 s after the
     # timed region
-    fp = measure_form(iegpu, iegpu.FORM_FP64, N, args.steps, args.warmup, smi_index, True, dist,
-                      settle_s=1.5, tail_s=0.5)
+    if args.headline_only:
+        fp = measure_form(iegpu, iegpu.FORM_FP64, N, args.steps, args.warmup, None, False, dist)
+    else:
+        fp = measure_form(iegpu, iegpu.FORM_FP64, N, args.steps, args.warmup, smi_index, True, dist,
+                          settle_s=1.5, tail_s=0.5)
     value = ws * args.steps * N ** 3 / (fp["ms"] * 1e-3)
+    if args.headline_only:
+        # the FP64 step alone (a short run for profilers); no forms, no CPU baseline
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": fp["ms"] / args.steps,
+                              "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+                              "config": {"workload": f"hilltop leapfrog, N={N}^3, plain FP64 form", "N": N,
+                                         "form": "fp64"}, "gpu_launches": fp["launches"],
+                              "headline_only": True}), flush=True)
+        return 0
     # the split form on the same workload
     sp = measure_form(iegpu, iegpu.FORM_SPLIT, N, args.steps, args.warmup, None, False, dist)
     sp_value = ws * args.steps * N ** 3 / (sp["ms"] * 1e-3)
@@ -648,6 +663,8 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--quick", action="store_true", help="skip the whole-run error statements and 512^3")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="time the plain FP64 step only and print a short line (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()

@@ -50,6 +50,9 @@ typedef struct iegpu_ctx iegpu_ctx;
 
 #define IEGPU_FORM_FP64     0  /* plain FP64: per-site arithmetic in the reference's order */
 #define IEGPU_FORM_SPLIT    1  /* FP32 perturbations about an FP64 background */
+#define IEGPU_FORM_SPLIT_COMP 2 /* the split form with compensated (Kahan) steps:
+                                   FP32 perturbations plus bf16 residuals;
+                                   N = 128, 256 or 512 */
 
 #define IEGPU_CRIT_GENERIC        0  /* evolve while V(phi) > V(phiref) */
 #define IEGPU_CRIT_MONOTONIC      1  /* evolve while |phi| > |phiref| */

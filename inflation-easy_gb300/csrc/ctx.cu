@@ -6,6 +6,10 @@
 #include <cstring>
 #include <new>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "iegpu_internal.cuh"
 #include "pot.cuh"
 
@@ -97,7 +101,12 @@ static int dalloc(iegpu_ctx* c, T** p, size_t n) {
 static void free_all(iegpu_ctx* c) {
     fp64_destroy_graphs(c);
     split_destroy_graphs(c);
-    for (int q = 0; q < 2; ++q) { cudaFree(c->sp[q]); cudaFree(c->spi[q]); }
+    for (int q = 0; q < 2; ++q) {
+        cudaFree(c->sp[q]);
+        cudaFree(c->spi[q]);
+        cudaFree(c->sxl[q]);
+        cudaFree(c->spl[q]);
+    }
     cudaFree(c->sctl);
     if (c->sctl_h) cudaFreeHost(c->sctl_h);
     fft_free(c);
@@ -115,6 +124,24 @@ static void free_all(iegpu_ctx* c) {
     for (int q = 0; q < 4; ++q)
         if (c->ev[q]) cudaEventDestroy(c->ev[q]);
     if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+}  // namespace iegpu
+
+namespace iegpu {
+
+cudaError_t smem_optin(const void* fn, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> done;
+    int dev = 0;
+    const cudaError_t ge = cudaGetDevice(&dev);
+    if (ge != cudaSuccess) return ge;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& have = done[std::make_pair(fn, dev)];
+    if (have >= bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) have = bytes;
+    return e;
 }
 
 }  // namespace iegpu
@@ -148,7 +175,10 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
     *out = nullptr;
     const int N = cfg->N;
     if (N < 8 || N > 1024 || (N & (N - 1))) return IEGPU_EINVAL;
-    if (cfg->form != IEGPU_FORM_FP64 && cfg->form != IEGPU_FORM_SPLIT) return IEGPU_EINVAL;
+    if (cfg->form != IEGPU_FORM_FP64 && cfg->form != IEGPU_FORM_SPLIT && cfg->form != IEGPU_FORM_SPLIT_COMP)
+        return IEGPU_EINVAL;
+    // the compensated steps live in the row-tile kernel of 128 <= N <= 512
+    if (cfg->form == IEGPU_FORM_SPLIT_COMP && (N < 128 || N > 512)) return IEGPU_EUNSUPPORTED;
     if (!(cfg->L > 0) || !(cfg->dt > 0) || !(cfg->rescale_B > 0)) return IEGPU_EINVAL;
     iegpu_ctx* c = new (std::nothrow) iegpu_ctx();
     if (!c) return IEGPU_ENOMEM;
@@ -195,10 +225,13 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
     c->part_cap = (int)(12 * c->red_grid + 3 * step_ctas + 64);
     if (!rc) rc = dalloc(c, &c->ctl, 1);
     if (!rc) rc = dalloc(c, &c->part, (size_t)c->part_cap);
-    if (!rc && cfg->form == IEGPU_FORM_SPLIT) {
+    c->comp = cfg->form == IEGPU_FORM_SPLIT_COMP;
+    if (!rc && cfg->form != IEGPU_FORM_FP64) {
         for (int q = 0; q < 2 && !rc; ++q) {
             rc = dalloc(c, &c->sp[q], gs);
             if (!rc) rc = dalloc(c, &c->spi[q], gs);
+            if (!rc && c->comp) rc = dalloc(c, &c->sxl[q], gs);
+            if (!rc && c->comp) rc = dalloc(c, &c->spl[q], gs);
         }
         if (!rc) rc = dalloc(c, &c->sctl, 1);
         if (!rc && check_cuda(c, cudaMallocHost(&c->sctl_h, sizeof(SplitCtl)), "pinned alloc")) rc = IEGPU_ENOMEM;
@@ -208,6 +241,10 @@ int iegpu_create(const iegpu_config* cfg, iegpu_ctx** out) {
             for (int q = 0; q < 2; ++q) {
                 cudaMemsetAsync(c->sp[q], 0, sizeof(float) * gs, c->stream);
                 cudaMemsetAsync(c->spi[q], 0, sizeof(float) * gs, c->stream);
+                if (c->comp) {
+                    cudaMemsetAsync(c->sxl[q], 0, sizeof(unsigned short) * gs, c->stream);
+                    cudaMemsetAsync(c->spl[q], 0, sizeof(unsigned short) * gs, c->stream);
+                }
             }
         }
     }
@@ -326,7 +363,7 @@ int iegpu_set_table(iegpu_ctx* c, const double* phi, const double* V, const doub
     return IEGPU_OK;
 }
 
-static bool is_split(const iegpu_ctx* c) { return c->cfg.form == IEGPU_FORM_SPLIT; }
+static bool is_split(const iegpu_ctx* c) { return c->cfg.form != IEGPU_FORM_FP64; }
 // F or FD held in the split representation (not the FP64 buffers)
 static bool split_field(const iegpu_ctx* c, int field) {
     return is_split(c) && !c->split_mat && (field == IEGPU_F || field == IEGPU_FD);

@@ -19,6 +19,11 @@
 //   terms never carry such bits in practice: a Laplacian of fields of order
 //   0.01..10 is a multiple of their ulp (2^-59 or coarser).
 //
+//   The sums of products (f lapl(f), f^2, fd^2) add the exact 106-bit
+//   product of the two significands, so the multiplication needs no FP64
+//   pipe either: the total is the correctly rounded exact sum of the exact
+//   products.
+//
 // * Division by a divisor fixed for the whole run (B^2 in V' = (c2 v)/B^2).
 //   The correctly rounded quotient RN(x / y) is formed from the integer
 //   quotient of the significands: with precomputed R = floor(2^116 / M_y)
@@ -145,6 +150,51 @@ __host__ __device__ __forceinline__ void acc_add_term(Acc4& A, double t, unsigne
     else acc_add4(A, l0, l1, l2, l3);
 }
 
+__host__ __device__ __forceinline__ unsigned long long mulhi64(unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// Adds the exact product x y.  flags |= 1 for a non-finite operand, 2 when
+// the exponents allow a product of magnitude >= 2^30 (neither is added).
+// Bits of the product below 2^-192 are dropped toward zero.
+__host__ __device__ __forceinline__ void acc_add_product(Acc4& A, double x, double y, unsigned& flags) {
+    const unsigned long long bx = dbits(x), by = dbits(y);
+    int ex = (int)((bx >> 52) & 0x7FF), ey = (int)((by >> 52) & 0x7FF);
+    if (ex == 0x7FF || ey == 0x7FF) {
+        flags |= 1u;
+        return;
+    }
+    unsigned long long mx = bx & 0x000FFFFFFFFFFFFFull, my = by & 0x000FFFFFFFFFFFFFull;
+    if (ex) mx |= 1ull << 52; else ex = 1;
+    if (ey) my |= 1ull << 52; else ey = 1;
+    if (mx == 0 || my == 0) return;
+    if (ex + ey > 2074) {   // |x| < 2^(ex-1022), |y| < 2^(ey-1022)
+        flags |= 2u;
+        return;
+    }
+    unsigned long long lo = mx * my, hi = mulhi64(mx, my);
+    int s = ex + ey - 1958;   // accumulator bit of the product's lowest bit (<= 116)
+    if (s < 0) {
+        const int t = -s;
+        if (t >= 128) return;
+        if (t >= 64) { lo = hi >> (t - 64); hi = 0; }
+        else { lo = (lo >> t) | (hi << (64 - t)); hi >>= t; }
+        s = 0;
+    }
+    const int r = s & 63;
+    const unsigned long long w0 = lo << r;
+    const unsigned long long w1 = (hi << r) | (r ? lo >> (64 - r) : 0ull);
+    const unsigned long long w2 = r ? hi >> (64 - r) : 0ull;
+    const bool q1 = s >= 64;
+    const unsigned long long l0 = q1 ? 0ull : w0, l1 = q1 ? w0 : w1, l2 = q1 ? w1 : w2, l3 = q1 ? w2 : 0ull;
+    if ((bx ^ by) >> 63) acc_sub4(A, l0, l1, l2, l3);
+    else acc_add4(A, l0, l1, l2, l3);
+}
+
 __device__ __forceinline__ void acc_shfl_down_add(Acc4& A, int o) {
     Acc4 B;
 #pragma unroll
@@ -256,14 +306,6 @@ inline DivConst make_div_const(double y) {
     D.R = (unsigned long long)(one / D.My);
     D.mode = 1;
     return D;
-}
-
-__host__ __device__ __forceinline__ unsigned long long mulhi64(unsigned long long a, unsigned long long b) {
-#ifdef __CUDA_ARCH__
-    return __umul64hi(a, b);
-#else
-    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
-#endif
 }
 
 // RN(x / D.y), bit-equal to x / D.y for every x.

@@ -267,10 +267,8 @@ static void run_pass(iegpu_ctx* c, typename Cplx<T>::type* data, int kind, int f
     const int q = (g.M == N) ? 0 : 1;
     if (sizeof(T) == 8) tw = (const C2*)(forward > 0 ? (const void*)c->tw.c_fwd_d[q] : (const void*)c->tw.c_inv_d[q]);
     else tw = (const C2*)(forward > 0 ? (const void*)c->tw.c_fwd_f[q] : (const void*)c->tw.c_inv_f[q]);
-    static bool attr_set[2] = {false, false};
-    if (!attr_set[sizeof(T) == 8]) {
-        cudaFuncSetAttribute(k_fft_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set[sizeof(T) == 8] = true;
+    if (smem_optin((const void*)k_fft_pass<T>, 200 * 1024) != cudaSuccess) {
+        set_error(c, IEGPU_ECUDA, "shared memory opt-in of the FFT pass failed");   // the launch then fails
     }
     k_fft_pass<T><<<(unsigned)(lines / LPB), 256, smem, c->stream>>>(data, tw, g, LPB, forward < 0 ? 1 : 0);
     c->launches++;

@@ -76,8 +76,11 @@ constexpr int kWin = 24;  // table brackets per window
 
 // Window of table brackets around a background value phibar: brackets
 // l0 .. l0+n-1, node offsets u[q] = x[l0-1+q] - phibar (descending), and per
-// bracket the line A[q] + s[q]*dphi = F(phibar + dphi) - F(phibar).
+// bracket the line A[q] + s[q]*dphi = F(phibar + dphi) - F(phibar).  phibar
+// and Fbar = F(phibar) let a site beyond the window form its bracket's line
+// from the whole table (far_line).
 struct SplitWin {
+    double phibar, Fbar;
     int l0, n, ok, pad;
     float u[kWin + 1];
     float A[kWin];
@@ -233,6 +236,11 @@ struct iegpu_ctx {
     // split form state
     float* sp[2] = {nullptr, nullptr};    // dphi (ping-pong)
     float* spi[2] = {nullptr, nullptr};   // dpi  (ping-pong)
+    // compensated split form: Kahan residuals of dphi and dpi (bf16 bits,
+    // ping-pong with sp / spi; the value is x - residual)
+    unsigned short* sxl[2] = {nullptr, nullptr};
+    unsigned short* spl[2] = {nullptr, nullptr};
+    int comp = 0;
     iegpu::SplitCtl* sctl = nullptr;      // device
     iegpu::SplitCtl* sctl_h = nullptr;    // pinned host mirror
     cudaGraphExec_t sp_exec[2] = {nullptr, nullptr};
@@ -255,6 +263,10 @@ struct iegpu_ctx {
 namespace iegpu {
 
 int set_error(iegpu_ctx* c, int code, const char* fmt, ...);
+// Opts kernel `fn` in to `bytes` of dynamic shared memory on the current
+// device.  The opt-in is a per-device function attribute: it is made once per
+// (kernel, device, size) under a mutex, and its status is returned.
+cudaError_t smem_optin(const void* fn, size_t bytes);
 int check_cuda(iegpu_ctx* c, cudaError_t e, const char* what);
 int sync_and_check(iegpu_ctx* c, const char* what);
 bool is_double_field(int field);

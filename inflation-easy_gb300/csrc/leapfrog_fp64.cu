@@ -223,13 +223,13 @@ __global__ void __launch_bounds__(kThreads) k_lsum(const double* __restrict__ f,
         const double fc = __ldg(&f[id]);
         const double L = lapl7(f, n, fc);
         lap[id] = L;
-        acc_add_term(v[0], fc * L, fl[0]);
+        acc_add_product(v[0], fc, L, fl[0]);
         if (TABLE) {
             bool oor;
             acc_add_term(v[1], V_table_sum_term(P, fc, &oor), fl[1]);
             if (oor) flag_error(ctl, IEGPU_ERANGE, fc);
         } else {
-            acc_add_term(v[1], fc * fc, fl[1]);
+            acc_add_product(v[1], fc, fc, fl[1]);
         }
     }
     acc_publish_flags<2>(ctl, fl);
@@ -323,16 +323,16 @@ __global__ void __launch_bounds__(kThreads) k_energy_sums(const double* __restri
     for (long long id = (long long)blockIdx.x * kThreads + threadIdx.x; id < gs; id += (long long)gridDim.x * kThreads) {
         const Nbr n = neighbours(id, lg);
         const double fc = __ldg(&f[id]);
-        acc_add_term(v[0], fc * lapl7(f, n, fc), fl[0]);
+        acc_add_product(v[0], fc, lapl7(f, n, fc), fl[0]);
         if (TABLE) {
             bool oor;
             acc_add_term(v[1], V_table_sum_term(P, fc, &oor), fl[1]);
             if (oor) flag_error(ctl, IEGPU_ERANGE, fc);
         } else {
-            acc_add_term(v[1], fc * fc, fl[1]);
+            acc_add_product(v[1], fc, fc, fl[1]);
         }
         const double q = __ldg(&fd[id]);
-        acc_add_term(v[2], q * q, fl[2]);
+        acc_add_product(v[2], q, q, fl[2]);
     }
     acc_publish_flags<3>(ctl, fl);
     acc_block_sum<3>(v);
@@ -640,23 +640,26 @@ __global__ void __launch_bounds__(kThreads) k_post_field(double* __restrict__ f,
 // fd kick of evolve_derivs_post_inflation, src/evolution.cpp:1448-1457:
 // fd += d (w laplnorm lapl(f) - (3 (1 + w) + s) ad fd / a), with
 // c_lap = w laplnorm and c_fr = (3 (1 + w) + s) ad formed on the host.
+// The divisions by a and by 4 dx^2 (ten per site with SIGW) are exact
+// divisions by fixed divisors on the integer pipes (div_exact, exact.cuh).
 __global__ void __launch_bounds__(kThreads) k_post_kick(const double* __restrict__ f, double* __restrict__ fd, int lg,
-                                                        double d, double c_lap, double c_fr, double a) {
+                                                        double d, double c_lap, double c_fr, DivConst Da) {
     const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
     const Nbr n = neighbours(id, lg);
     const double lap = lapl7(f, n, __ldg(&f[id]));
     const double fdo = fd[id];
-    fd[id] = fdo + d * (c_lap * lap - c_fr * fdo / a);
+    fd[id] = fdo + d * (c_lap * lap - div_exact(c_fr * fdo, Da));
 }
 
 struct PostSigwK {
-    double d, laplnorm, c_hf, a, invH, coeffU, srcAmp, half_over_dx, inv_dx2, den;
+    double d, laplnorm, c_hf, invH, coeffU, srcAmp, half_over_dx, inv_dx2;
+    DivConst Da, Dden;   // a and 4 dx^2
 };
 
 // (fpp - fpm - fmp + fmm) / den of d2_cross_state, src/evolution.cpp:93-106
 __device__ __forceinline__ double cross4(const double* __restrict__ f, long long pp, long long pm, long long mp,
-                                         long long mm, double den) {
-    return (__ldg(&f[pp]) - __ldg(&f[pm]) - __ldg(&f[mp]) + __ldg(&f[mm])) / den;
+                                         long long mm, const DivConst& den) {
+    return div_exact(__ldg(&f[pp]) - __ldg(&f[pm]) - __ldg(&f[mp]) + __ldg(&f[mm]), den);
 }
 
 // Tensor kick of evolve_derivs_post_inflation, src/evolution.cpp:1459-1551,
@@ -683,9 +686,9 @@ __global__ void __launch_bounds__(kThreads) k_post_sigw(const double* __restrict
     const double Hzz = (__ldg(&f[n.kp]) - 2.0 * fc + __ldg(&f[n.km])) * K.inv_dx2;
     // corners (ip, jp, kp), (ip, jm, km), (im, jp, kp), (im, jm, km) with the
     // indices d1, d2 do not name left in place
-    const double Hxy = cross4(f, id + dip + djp, id + dip + djm, id + dim + djp, id + dim + djm, K.den);
-    const double Hxz = cross4(f, id + dip + dkp, id + dip + dkm, id + dim + dkp, id + dim + dkm, K.den);
-    const double Hyz = cross4(f, id + djp + dkp, id + djm + dkm, id + djp + dkp, id + djm + dkm, K.den);
+    const double Hxy = cross4(f, id + dip + djp, id + dip + djm, id + dim + djp, id + dim + djm, K.Dden);
+    const double Hxz = cross4(f, id + dip + dkp, id + dip + dkm, id + dim + dkp, id + dim + dkm, K.Dden);
+    const double Hyz = cross4(f, id + djp + dkp, id + djm + dkm, id + djp + dkp, id + djm + dkm, K.Dden);
     const double dux = gdx * K.invH + gx;
     const double duy = gdy * K.invH + gy;
     const double duz = gdz * K.invH + gz;
@@ -700,7 +703,7 @@ __global__ void __launch_bounds__(kThreads) k_post_sigw(const double* __restrict
         const float* h = sg.hs[c];
         const float lf = lapl7(h, n, __ldg(&h[id]));
         const float hdo = sg.hd[c][id];
-        const double rhs = K.d * (K.laplnorm * (double)lf - K.c_hf * (double)hdo / K.a + K.srcAmp * S[c]);
+        const double rhs = K.d * (K.laplnorm * (double)lf - div_exact(K.c_hf * (double)hdo, K.Da) + K.srcAmp * S[c]);
         sg.hd[c][id] = hdo + (float)rhs;
     }
 }
@@ -762,7 +765,8 @@ static void post_kick(iegpu_ctx* c, double d, double omega, iegpu_bg* bg) {
     const double ad = bg->ad;
     const unsigned grid = (unsigned)(c->gs / kThreads);
     double* f = c->f[c->cur];
-    k_post_kick<<<grid, kThreads, 0, c->stream>>>(f, c->fd, c->lg, d, omega * laplnorm, (3.0 * (1.0 + omega) + s) * ad, a);
+    const DivConst Da = make_div_const(a);
+    k_post_kick<<<grid, kThreads, 0, c->stream>>>(f, c->fd, c->lg, d, omega * laplnorm, (3.0 * (1.0 + omega) + s) * ad, Da);
     c->launches++;
     if (c->cfg.sigw) {
         SigwPtrs sg{};
@@ -772,13 +776,13 @@ static void post_kick(iegpu_ctx* c, double d, double omega, iegpu_bg* bg) {
         K.d = d;
         K.laplnorm = laplnorm;
         K.c_hf = (2.0 + s) * ad;
-        K.a = a;
+        K.Da = Da;
         K.invH = 1.0 / Htilde;
         K.coeffU = 4.0 / (3.0 * (1.0 + omega));
         K.srcAmp = 2.0 * pow(a, -2.0 * s);
         K.half_over_dx = 0.5 / dx;
         K.inv_dx2 = 1.0 / (dx * dx);
-        K.den = 4.0 * dx * dx;
+        K.Dden = make_div_const(4.0 * dx * dx);
         k_post_sigw<<<grid, kThreads, 0, c->stream>>>(f, c->fd, sg, c->lg, K);
         c->launches++;
     }
@@ -918,7 +922,8 @@ __global__ void __launch_bounds__(kThreads) k_rk_rhs(const double* __restrict__ 
 }
 
 struct RkPostCoef {
-    double omega, laplnorm, scalar_friction, tensor_friction, invH, coeffU, srcAmp, half_over_dx, inv_dx2, den;
+    double omega, laplnorm, scalar_friction, tensor_friction, invH, coeffU, srcAmp, half_over_dx, inv_dx2;
+    DivConst Dden;   // 4 dx^2
 };
 
 // compute_inflation_rhs, post-inflation equations (src/evolution.cpp:515-598):
@@ -946,9 +951,9 @@ __global__ void __launch_bounds__(kThreads) k_rk_rhs_post(const double* __restri
         const double Hxx = (__ldg(&fs[n.ip]) - 2.0 * fc + __ldg(&fs[n.im])) * K.inv_dx2;
         const double Hyy = (__ldg(&fs[n.jp]) - 2.0 * fc + __ldg(&fs[n.jm])) * K.inv_dx2;
         const double Hzz = (__ldg(&fs[n.kp]) - 2.0 * fc + __ldg(&fs[n.km])) * K.inv_dx2;
-        const double Hxy = cross4(fs, id + dip + djp, id + dip + djm, id + dim + djp, id + dim + djm, K.den);
-        const double Hxz = cross4(fs, id + dip + dkp, id + dip + dkm, id + dim + dkp, id + dim + dkm, K.den);
-        const double Hyz = cross4(fs, id + djp + dkp, id + djm + dkm, id + djp + dkp, id + djm + dkm, K.den);
+        const double Hxy = cross4(fs, id + dip + djp, id + dip + djm, id + dim + djp, id + dim + djm, K.Dden);
+        const double Hxz = cross4(fs, id + dip + dkp, id + dip + dkm, id + dim + dkp, id + dim + dkm, K.Dden);
+        const double Hyz = cross4(fs, id + djp + dkp, id + djm + dkm, id + djp + dkp, id + djm + dkm, K.Dden);
         const double dux = gdx * K.invH + gx;
         const double duy = gdy * K.invH + gy;
         const double duz = gdz * K.invH + gz;
@@ -1202,7 +1207,7 @@ static int rk_rhs(iegpu_ctx* c, const RkEq& E, const double* fs, const double* f
         K.srcAmp = 2.0 * pow(a_st, -2.0 * s);
         K.half_over_dx = 0.5 / dx;
         K.inv_dx2 = 1.0 / (dx * dx);
-        K.den = 4.0 * dx * dx;
+        K.Dden = make_div_const(4.0 * dx * dx);
         const unsigned grid = (unsigned)(c->gs / kThreads);
         if (sig) k_rk_rhs_post<true><<<grid, kThreads, 0, c->stream>>>(fs, fds, kfd, sg, c->lg, K);
         else k_rk_rhs_post<false><<<grid, kThreads, 0, c->stream>>>(fs, fds, kfd, sg, c->lg, K);

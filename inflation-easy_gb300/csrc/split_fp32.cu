@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
     float* wk = nw + 2 * NP;               // kick window: u[kWin+1], A[kWin], s[kWin]
     float* wv = wk + 3 * kWin + 1;         // potential window
     __shared__ int nk_s, nv_s, active_s;
+    __shared__ double wbar[4];
     __shared__ float cf[6];
     const int tid = threadIdx.x, nthr = blockDim.x;
     if (tid == 0) {
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
             wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
             wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
         }
+        load_win_centres<false>(wbar, ctl);
     }
     __syncthreads();
     if (!active_s) return;
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
             const float x = pc[o];
             const float lap = pc[o + 1] + pc[o - 1] + pc[o + RS] + pc[o - RS] + pu[o] + pl[o] - 6.f * x;
             const float pi0 = pp[jl * RS + kl + kColOff];
-            const float dv = split_dv<TABLE>(x, wk, nk_s, ck, pn, kv, bad);
+            const float dv = split_dv<TABLE>(x, wk, nk_s, ck, pn, kv, bad, P, wbar);
             const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
             const float xn = x + d * pin;
             nc[jl * NS + kl] = xn;
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(256, 4) k_split_step(SplitBufs B, SplitCtl* ct
                 B.xd[gi] = xn;
                 B.pd[gi] = pin;
                 s1.add(xn);
-                const float v2 = split_v<TABLE>(xn, wv, nv_s, cv, bad);
+                const float v2 = split_v<TABLE>(xn, wv, nv_s, cv, bad, P, wbar + 2);
                 if (!TABLE || !bad) s2.add(v2);
             }
         }
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
 }
 
 
-template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
+template <bool TABLE, int C4, int TJ, int PF, bool TMA = false, bool COMP = false>
 __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K,
                                                                double* part, unsigned* counter, double* a_trace,
                                                                int chunks, int rev) {
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4(SplitBufs B, Spli
         u0 = (long long)blockIdx.x * N + i0;
         u1 = u0 + CH;
     }
-    rows4_body<TABLE, C4, TJ, PF, TMA>(B, ctl, P, K, part, counter, a_trace, u0, u1,
+    rows4_body<TABLE, C4, TJ, PF, TMA, COMP>(B, ctl, P, K, part, counter, a_trace, u0, u1,
                                        blockIdx.x + gridDim.x * blockIdx.y, gridDim.x * gridDim.y, nullptr, rev != 0);
 }
 
@@ -254,7 +256,7 @@ __device__ __forceinline__ bool spin_until(const unsigned* p, unsigned v, SplitC
 // overlap the last CTA's sums and update.  sync[0] counts the arrivals of the
 // launch; both words are zero at the launch.  The waits are made by lane 0
 // of the precompute warp; a wait that gives up ends every CTA's loop.
-template <bool TABLE, int C4, int TJ, int PF>
+template <bool TABLE, int C4, int TJ, int PF, bool COMP = false>
 __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4_persist(SplitBufs B0, SplitBufs B1, SplitCtl* ctl,
                                                                        PotDev P, SplitConst K, double* part,
                                                                        unsigned* sync, double* a_trace, int chunks,
@@ -278,11 +280,7 @@ __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4_persist(SplitBufs
     const int slot = blockIdx.x + gridDim.x * blockIdx.y, nslots = gridDim.x * gridDim.y;
     for (int s = 0; s < nsteps; ++s) {
         const int src = (start + s) & 1;
-        SplitBufs B;
-        B.xs = src ? B1.xs : B0.xs;
-        B.xd = src ? B1.xd : B0.xd;
-        B.ps = src ? B1.ps : B0.ps;
-        B.pd = src ? B1.pd : B0.pd;
+        SplitBufs B = src ? B1 : B0;
         const bool rev = src != 0;
         if (s > 0) {
             if (threadIdx.x == NTH) go_fields = spin_until(sync, (unsigned)(s * nslots), ctl);
@@ -303,7 +301,7 @@ __global__ void __launch_bounds__((TJ + 2) * 32) k_split_rows4_persist(SplitBufs
         sq.seq = sync + 1;
         sq.base = (unsigned)(s * nslots);
         sq.val = (unsigned)(s + 1);
-        if (!rows4_body<TABLE, C4, TJ, PF, false>(B, ctl, P, K, part, sync, a_trace, u0, u1, slot, nslots, nullptr, rev,
+        if (!rows4_body<TABLE, C4, TJ, PF, false, COMP>(B, ctl, P, K, part, sync, a_trace, u0, u1, slot, nslots, nullptr, rev,
                                                   s > 0, sq))
             break;
     }
@@ -423,14 +421,16 @@ __global__ void k_split_drift(float* __restrict__ x, const float* __restrict__ p
 // Kick only (evolve_derivs): dpi += d(...) with the current coefficients.
 template <bool TABLE>
 __global__ void __launch_bounds__(kThreads) k_split_kick(const float* __restrict__ x, float* __restrict__ p,
-                                                         const SplitCtl* ctl, int lg) {
+                                                         SplitCtl* ctl, PotDev P, int lg) {
     __shared__ float wk[3 * kWin + 1];
+    __shared__ double wbar[4];
     __shared__ int nk;
     if (!ctl->active) return;
     if (TABLE) {
         for (int q = threadIdx.x; q <= kWin; q += blockDim.x) wk[q] = ctl->wk.u[q];
         for (int q = threadIdx.x; q < kWin; q += blockDim.x) { wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q]; }
         if (threadIdx.x == 0) nk = ctl->wk.n;
+        load_win_centres<false>(wbar, ctl);
         __syncthreads();
     }
     const float d = ctl->d, lap_n = ctl->lapl, fric = ctl->fric, pn = ctl->pn, kv = ctl->kv;
@@ -443,23 +443,30 @@ __global__ void __launch_bounds__(kThreads) k_split_kick(const float* __restrict
                       x[id + ((long long)(((i + 1) & m) - i) << (2 * lg))] +
                       x[id + ((long long)(((i - 1) & m) - i) << (2 * lg))] - 6.f * xc;
     float dv;
+    bool bad = false;
     if (TABLE) {
         const int q = window_find(wk, nk, xc);
-        dv = q < 0 ? 0.f : pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * xc);
+        dv = pn * (q < 0 ? far_line(P, P.dV, P.slopedV, wbar, xc, bad) : wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * xc);
     } else {
         dv = kv * xc;
     }
     const float p0 = p[id];
     p[id] = p0 + d * (lap_n * lap - fric * p0 - dv);
+    if (TABLE && bad && atomicCAS(&ctl->error, 0, IEGPU_ERANGE) == 0) ctl->errval = (double)xc + wbar[0];
 }
 
-// f64 = bar + (double)x  (materialise the full field)
-__global__ void k_split_materialize(const float* __restrict__ x, double* __restrict__ out, long long gs,
-                                    const SplitCtl* ctl, int which) {
+// residual of the compensated form as a double (0 without one)
+__device__ __forceinline__ double residual(const unsigned short* r, long long id) {
+    return r ? (double)__uint_as_float((unsigned)r[id] << 16) : 0.0;
+}
+
+// f64 = bar + (double)x (- residual)  (materialise the full field)
+__global__ void k_split_materialize(const float* __restrict__ x, const unsigned short* __restrict__ res,
+                                    double* __restrict__ out, long long gs, const SplitCtl* ctl, int which) {
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= gs) return;
     const double bar = which ? ctl->pibar : ctl->phibar;
-    out[id] = bar + (double)x[id];
+    out[id] = bar + ((double)x[id] - residual(res, id));
 }
 
 // x = (float)(in - bar) with bar = mean of in (given)
@@ -469,10 +476,11 @@ __global__ void k_split_absorb(const double* __restrict__ in, float* __restrict_
     x[id] = (float)(in[id] - bar);
 }
 
-// (double) x for spectra of the perturbation
-__global__ void k_split_to_double(const float* __restrict__ x, double* __restrict__ out, long long gs) {
+// (double) x (- residual) for spectra of the perturbation
+__global__ void k_split_to_double(const float* __restrict__ x, const unsigned short* __restrict__ res,
+                                  double* __restrict__ out, long long gs) {
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id < gs) out[id] = (double)x[id];
+    if (id < gs) out[id] = (double)x[id] - residual(res, id);
 }
 
 // Lattice sums of the split state for energies / means:
@@ -481,12 +489,15 @@ template <bool TABLE>
 __global__ void __launch_bounds__(kThreads) k_split_sums(const float* __restrict__ x, const float* __restrict__ p,
                                                          const SplitCtl* ctl, PotDev P, double* part, int lg) {
     __shared__ float su[kWin + 1], sA[kWin], ss[kWin];
+    __shared__ double wb[2];
     __shared__ int sn;
     if (TABLE && threadIdx.x == 0) {
         SplitWin W;
         int err = 0;
         build_window(W, P, P.V, P.dyV, ctl->phibar, &err);
         sn = err ? -1 : W.n;
+        wb[0] = W.phibar;
+        wb[1] = W.Fbar;
         for (int q = 0; q <= W.n && !err; ++q) su[q] = W.u[q];
         for (int q = 0; q < W.n && !err; ++q) { sA[q] = W.A[q]; ss[q] = W.s[q]; }
     }
@@ -506,9 +517,10 @@ __global__ void __launch_bounds__(kThreads) k_split_sums(const float* __restrict
         a2.add(pc);
         a3.add(pc * pc);
         a4.add(dk * dk + dj * dj + di * di);
-        if (TABLE) {
-            const int q = sn < 0 ? -1 : window_find(su, sn, xc);
-            if (q >= 0) a5.add(sA[q] + ss[q] * xc);
+        if (TABLE && sn >= 0) {
+            const int q = window_find(su, sn, xc);
+            bool bad = false;
+            a5.add(q >= 0 ? sA[q] + ss[q] * xc : far_line(P, P.V, P.slopeV, wb, xc, bad));
         }
     }
     double v[6] = {a0.value(), a1.value(), a2.value(), a3.value(), a4.value(), a5.value()};
@@ -569,7 +581,7 @@ static RowCfg default_row_cfg(const iegpu_ctx* c) {
     RowCfg r;
     const int N = c->N;
     r.TJ = N >= 512 ? 4 : 8;
-    r.PF = 2;
+    r.PF = 2;   // also a compensated shape
     const int per_sm = row_ctas_per_sm(N, r.TJ, r.PF);
     const int tiles = N / r.TJ;
     int chunks = (c->sms * (per_sm > 0 ? per_sm : 1)) / tiles;
@@ -620,6 +632,29 @@ static void launch_prime(iegpu_ctx* c, int src) {
     c->launches++;
 }
 
+// Step buffers reading parity src and writing src ^ 1 (with the residuals in
+// the compensated form).
+static SplitBufs split_bufs(const iegpu_ctx* c, int src) {
+    SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
+    if (c->comp) {
+        B.xls = c->sxl[src];
+        B.xld = c->sxl[src ^ 1];
+        B.pls = c->spl[src];
+        B.pld = c->spl[src ^ 1];
+    }
+    return B;
+}
+
+// Shapes of the compensated row kernel (instantiated for these alone): 16-row
+// tiles (N <= 256) with 2 or 3 planes ahead, 8-row tiles with 2, 4-row tiles
+// with 2 (N = 512); cp.async staging.
+static bool comp_shape_ok(int N, int TJ, int PF, int tma) {
+    if (tma || N < 128 || N > 512) return false;
+    if (TJ == 16) return N <= 256 && (PF == 2 || PF == 3);
+    if (TJ == 8) return PF == 2;
+    return TJ == 4 && N == 512 && PF == 2;
+}
+
 static SigwSplit sigw_split(iegpu_ctx* c, int src) {
     SigwSplit S{};
     if (!c->cfg.sigw) return S;
@@ -633,34 +668,27 @@ static SigwSplit sigw_split(iegpu_ctx* c, int src) {
 
 template <bool TAB, int CC, int TJV, int PFV>
 static void rows_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
-    static size_t attr = 0;
-    if (attr < g.smem) {
-        cudaFuncSetAttribute(k_split_rows<TAB, CC, TJV, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        attr = g.smem;
+    if (smem_optin((const void*)k_split_rows<TAB, CC, TJV, PFV>, g.smem) != cudaSuccess) {
+        set_error(c, IEGPU_ECUDA, "shared memory opt-in of the split step kernel failed");   // the launch then fails
     }
     launch_pdl(k_split_rows<TAB, CC, TJV, PFV>, grid, dim3((TJV + 1) * 32), g.smem, c->stream, B, c->sctl, c->pot, K,
                c->part, c->counter, c->a_trace, g.chunks);
 }
 
-template <bool TAB, int C4, int TJV, int PFV, bool TMA = false>
+template <bool TAB, int C4, int TJV, int PFV, bool TMA = false, bool COMP = false>
 static void rows4_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
-    static size_t attr = 0;
-    if (attr < g.smem) {
-        cudaFuncSetAttribute(k_split_rows4<TAB, C4, TJV, PFV, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)g.smem);
-        attr = g.smem;
+    if (smem_optin((const void*)k_split_rows4<TAB, C4, TJV, PFV, TMA, COMP>, g.smem) != cudaSuccess) {
+        set_error(c, IEGPU_ECUDA, "shared memory opt-in of the split step kernel failed");   // the launch then fails
     }
-    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV, TMA>, grid, dim3(row4_threads(TJV)), g.smem, c->stream, B, c->sctl, c->pot,
+    launch_pdl(k_split_rows4<TAB, C4, TJV, PFV, TMA, COMP>, grid, dim3(row4_threads(TJV)), g.smem, c->stream, B, c->sctl, c->pot,
                K, c->part, c->counter, c->a_trace, g.chunks, g.rev);
 }
 
 template <bool TAB, int NV, int PFV>
 static void plane_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
     constexpr int NT = NV == 32 ? 256 : 512;
-    static size_t attr = 0;
-    if (attr < g.smem) {
-        cudaFuncSetAttribute(k_split_plane<TAB, NV, NT, PFV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        attr = g.smem;
+    if (smem_optin((const void*)k_split_plane<TAB, NV, NT, PFV>, g.smem) != cudaSuccess) {
+        set_error(c, IEGPU_ECUDA, "shared memory opt-in of the split step kernel failed");   // the launch then fails
     }
     launch_pdl(k_split_plane<TAB, NV, NT, PFV>, grid, dim3(NT), g.smem, c->stream, B, c->sctl, c->pot, K, c->part,
                c->counter, c->a_trace, g.chunks);
@@ -674,6 +702,19 @@ static void plane_pf(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
 
 template <bool TAB, int C4>
 static void rows4_tj(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (c->comp) {
+        // the compensated shapes (comp_shape_ok)
+        if (g.TJ == 16 && C4 <= 2) {
+            constexpr int CW = C4 <= 2 ? C4 : 2;
+            if (g.PF == 2) rows4_one<TAB, CW, 16, 2, false, true>(c, B, K, grid, g);
+            else rows4_one<TAB, CW, 16, 3, false, true>(c, B, K, grid, g);
+        } else if (g.TJ == 8) {
+            rows4_one<TAB, C4, 8, 2, false, true>(c, B, K, grid, g);
+        } else if (C4 == 4) {
+            rows4_one<TAB, 4, 4, 2, false, true>(c, B, K, grid, g);
+        }
+        return;
+    }
     if (g.tma) {
         // bulk-copy staging: 8-row tiles with 2 planes ahead, 16-row tiles with 1..3
         if (g.TJ == 8) rows4_one<TAB, C4, 8, 2, true>(c, B, K, grid, g);
@@ -739,7 +780,7 @@ static void launch_step(iegpu_ctx* c, int src) {
     }
     StepGeom g = step_geom(c);
     g.rev = src & 1;
-    SplitBufs B{c->sp[src], c->sp[src ^ 1], c->spi[src], c->spi[src ^ 1]};
+    const SplitBufs B = split_bufs(c, src);
     dim3 grid(g.tiles, g.chunks > 0 ? g.chunks : 1);
     if (g.rows) {
         launch_rows(c, B, K, grid, g);
@@ -763,14 +804,11 @@ constexpr int kPersistSteps = 64;   // steps per cooperative launch
 // Launches k_split_rows4_persist of one shape for `nsteps` steps from buffer
 // parity `start`; 1 if the shape's grid is not resident all at once (the
 // caller then steps kernel by kernel), -1 on a launch error.
-template <bool TAB, int C4, int TJV, int PFV>
+template <bool TAB, int C4, int TJV, int PFV, bool COMP = false>
 static int persist_one(iegpu_ctx* c, int start, int nsteps, dim3 grid, const StepGeom& g, bool check_only) {
-    auto kern = k_split_rows4_persist<TAB, C4, TJV, PFV>;
-    static size_t attr = 0;
-    if (attr < g.smem) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        attr = g.smem;
-    }
+    auto kern = k_split_rows4_persist<TAB, C4, TJV, PFV, COMP>;
+    if (smem_optin((const void*)kern, g.smem) != cudaSuccess)
+        return set_error(c, IEGPU_ECUDA, "shared memory opt-in of the split step kernel failed");
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, row4_threads(TJV), g.smem) != cudaSuccess ||
         (long long)per_sm * c->sms < (long long)grid.x * grid.y) {
@@ -779,8 +817,8 @@ static int persist_one(iegpu_ctx* c, int start, int nsteps, dim3 grid, const Ste
     }
     if (check_only) return 0;
     const SplitConst K = split_const(c);
-    const SplitBufs B0{c->sp[0], c->sp[1], c->spi[0], c->spi[1]};
-    const SplitBufs B1{c->sp[1], c->sp[0], c->spi[1], c->spi[0]};
+    const SplitBufs B0 = split_bufs(c, 0);
+    const SplitBufs B1 = split_bufs(c, 1);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = dim3(row4_threads(TJV));
@@ -802,6 +840,15 @@ static int persist_one(iegpu_ctx* c, int start, int nsteps, dim3 grid, const Ste
 
 template <bool TAB, int C4>
 static int persist_tj(iegpu_ctx* c, int start, int nsteps, dim3 grid, const StepGeom& g, bool check_only) {
+    if (c->comp) {
+        if (g.TJ == 16 && C4 <= 2) {
+            constexpr int CW = C4 <= 2 ? C4 : 2;
+            if (g.PF == 2) return persist_one<TAB, CW, 16, 2, true>(c, start, nsteps, grid, g, check_only);
+            return persist_one<TAB, CW, 16, 3, true>(c, start, nsteps, grid, g, check_only);
+        }
+        if (g.TJ == 8 && C4 <= 2) return persist_one<TAB, C4, 8, 2, true>(c, start, nsteps, grid, g, check_only);
+        return 1;
+    }
     if (g.TJ == 4) {
         switch (g.PF) {
             case 1: return persist_one<TAB, C4, 4, 1>(c, start, nsteps, grid, g, check_only);
@@ -1002,12 +1049,25 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
             }
         }
     }
-    // save the live state into the idle FP64 buffer
+    if (c->comp) {
+        std::vector<RowCfg> keep;
+        for (const RowCfg& r : cands)
+            if (comp_shape_ok(N, r.TJ, r.PF, r.tma)) keep.push_back(r);
+        cands.swap(keep);
+        if (cands.empty()) cands.push_back(default_row_cfg(c));
+    }
+    // save the live state into the idle FP64 buffer (the residuals of the
+    // compensated form into the deltaN buffer)
     float* save = reinterpret_cast<float*>(c->f[c->cur ^ 1]);
+    unsigned short* save_r = reinterpret_cast<unsigned short*>(c->dn);
     const int cur0 = c->cur;
     const SplitCtl ctl0 = *c->sctl_h;
     if (check_cuda(c, cudaMemcpyAsync(save, c->sp[cur0], sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune save") ||
         check_cuda(c, cudaMemcpyAsync(save + c->gs, c->spi[cur0], sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune save"))
+        return IEGPU_ECUDA;
+    if (c->comp &&
+        (check_cuda(c, cudaMemcpyAsync(save_r, c->sxl[cur0], 2 * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune save") ||
+         check_cuda(c, cudaMemcpyAsync(save_r + c->gs, c->spl[cur0], 2 * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune save")))
         return IEGPU_ECUDA;
     double best = 1e300;
     RowCfg pick = default_row_cfg(c);
@@ -1026,6 +1086,10 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
         if (check_cuda(c, cudaMemcpyAsync(c->sp[cur0], save, sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune restore") ||
             check_cuda(c, cudaMemcpyAsync(c->spi[cur0], save + c->gs, sizeof(float) * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune restore"))
             return IEGPU_ECUDA;
+        if (c->comp &&
+            (check_cuda(c, cudaMemcpyAsync(c->sxl[cur0], save_r, 2 * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune restore") ||
+             check_cuda(c, cudaMemcpyAsync(c->spl[cur0], save_r + c->gs, 2 * c->gs, cudaMemcpyDeviceToDevice, c->stream), "tune restore")))
+            return IEGPU_ECUDA;
         if (rc) return rc;
         if (ms[1] < best) { best = ms[1]; pick = r; }
     }
@@ -1038,6 +1102,7 @@ int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
 int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
     const int N = c->N;
     if (prefetch >= 10) {
+        if (c->comp) return set_error(c, IEGPU_EINVAL, "the compensated form stages its planes with cp.async only");
         // bulk-copy (TMA) staging: prefetch - 10 planes ahead
         const int pf = prefetch - 10;
         const bool ok = N >= 128 && ((rows == 8 && pf == 2) || (rows == 16 && N <= 256 && pf >= 1 && pf <= 3)) &&
@@ -1055,6 +1120,9 @@ int split_set_shape(iegpu_ctx* c, int rows, int prefetch, int chunks) {
         return IEGPU_OK;
     }
     if (N < 32 || N > 512) return set_error(c, IEGPU_EUNSUPPORTED, "the row kernel covers 32 <= N <= 512");
+    if (c->comp && !comp_shape_ok(N, rows, prefetch, 0))
+        return set_error(c, IEGPU_EINVAL, "compensated shapes: rows 16 (N <= 256) with prefetch 2|3, rows 8 with 2, "
+                                          "rows 4 (N = 512) with 2");
     const bool plane = plane_shape(N, rows);
     const bool deep = (rows == 4 && N >= 128 && (prefetch == 3 || prefetch == 4)) ||
                       (rows == 16 && N >= 128 && N <= 256 && prefetch == 3);
@@ -1215,8 +1283,8 @@ int split_evolve_derivs(iegpu_ctx* c, double d, iegpu_bg* bg) {
         k_split_h<<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], sigw_split(c, c->cur), c->sctl, c->lg, hodx, 1);
         c->launches++;
     }
-    if (c->pot.table) k_split_kick<true><<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->lg);
-    else k_split_kick<false><<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->lg);
+    if (c->pot.table) k_split_kick<true><<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->pot, c->lg);
+    else k_split_kick<false><<<grid, kThreads, 0, c->stream>>>(c->sp[c->cur], c->spi[c->cur], c->sctl, c->pot, c->lg);
     c->launches++;
     int rc = sctl_down(c);
     if (rc) return rc;
@@ -1256,16 +1324,23 @@ int split_sums(iegpu_ctx* c, double out[6]) {
     return IEGPU_OK;
 }
 
+static const unsigned short* split_residual(const iegpu_ctx* c, int which) {
+    if (!c->comp) return nullptr;
+    return which ? c->spl[c->cur] : c->sxl[c->cur];
+}
+
 int split_materialize(iegpu_ctx* c, int which, double* out) {
     const float* x = which ? c->spi[c->cur] : c->sp[c->cur];
-    k_split_materialize<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(x, out, (long long)c->gs, c->sctl, which);
+    k_split_materialize<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(x, split_residual(c, which), out,
+                                                                               (long long)c->gs, c->sctl, which);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "materialize");
 }
 
 int split_to_double(iegpu_ctx* c, int which, double* out) {
     const float* x = which ? c->spi[c->cur] : c->sp[c->cur];
-    k_split_to_double<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(x, out, (long long)c->gs);
+    k_split_to_double<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(x, split_residual(c, which), out,
+                                                                             (long long)c->gs);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "to double");
 }
@@ -1275,6 +1350,10 @@ int split_absorb(iegpu_ctx* c, int which, const double* in, double mean) {
     float* x = which ? c->spi[c->cur] : c->sp[c->cur];
     k_split_absorb<<<(unsigned)((c->gs + 255) / 256), 256, 0, c->stream>>>(in, x, (long long)c->gs, mean);
     c->launches++;
+    if (c->comp) {
+        unsigned short* r = which ? c->spl[c->cur] : c->sxl[c->cur];
+        if (check_cuda(c, cudaMemsetAsync(r, 0, sizeof(unsigned short) * c->gs, c->stream), "absorb")) return IEGPU_ECUDA;
+    }
     if (which) c->sctl_h->pibar = mean;
     else c->sctl_h->phibar = mean;
     // only the background fields of the control block change here

@@ -65,29 +65,68 @@ __device__ __forceinline__ int window_near(const float* w, int n, const WinCache
     return window_find(w, n, v);
 }
 
-// potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop)
+// The line A + s x of a site beyond the window, from the whole table: its
+// bracket l (x[l-1] >= phibar + x > x[l]) by bisection, and the bracket's line
+// formed in FP64 as build_window_warp forms the window's lines, so that a
+// bracket the window also holds gives the same float coefficients.  wb =
+// {phibar, Fbar} of the window; y, slope: the tabulated function and its
+// bracket slopes.  On a coarsely tabulated stretch a perturbation is a small
+// fraction of a bracket and this path is rare; where the table is dense
+// (the USR plateau of inputs/*.dat has brackets of 2.7e-6) the perturbations
+// span many brackets and more sites take it.  bad: beyond the table.
+static __device__ __noinline__ float far_line(const PotDev& P, const double* y, const double* slope,
+                                              const double* wb, float x, bool& bad) {
+    const double phibar = wb[0], Fbar = wb[1];
+    bool oor;
+    const int l = table_bracket(P, phibar + (double)x, &oor);
+    if (oor) {
+        bad = true;
+        return 0.f;
+    }
+    const double s = __ldg(&slope[l]);
+    const float A = (float)((__ldg(&y[l]) + (phibar - __ldg(&P.x[l])) * s) - Fbar);
+    return A + (float)s * x;
+}
+
+// potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop).
+// wb: {phibar, Fbar} of the kick window, for sites beyond it.
 template <bool TABLE>
 __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, const WinCache& c, float pn, float kv,
-                                          bool& bad) {
+                                          bool& bad, const PotDev& P, const double* wb) {
     if (TABLE) {
         if (x <= c.hi && x > c.lo) return pn * (c.A + c.s * x);
         const int q = window_near(wk, nk, c, x);
-        if (q < 0) { bad = true; return 0.f; }
+        if (q < 0) return pn * far_line(P, P.dV, P.slopedV, wb, x, bad);
         return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
     }
     return kv * x;
 }
 
-// V(phibar + x) - V(phibar) in table units (table) or x^2 (hilltop)
+// V(phibar + x) - V(phibar) in table units (table) or x^2 (hilltop).
+// wb: {phibar, Fbar} of the potential window, for sites beyond it.
 template <bool TABLE>
-__device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad) {
+__device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad,
+                                         const PotDev& P, const double* wb) {
     if (TABLE) {
         if (x <= c.hi && x > c.lo) return c.A + c.s * x;
         const int q = window_near(wv, nv, c, x);
-        if (q < 0) { bad = true; return 0.f; }
+        if (q < 0) return far_line(P, P.V, P.slopeV, wb, x, bad);
         return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
     }
     return x * x;
+}
+
+// {phibar, Fbar} of the kick window (wb[0..1]) and of the potential window
+// (wb[2..3]) into shared memory, by thread 0; CG: read through L2 (the
+// control block of a persistent launch, written during the launch).
+template <bool CG>
+__device__ __forceinline__ void load_win_centres(double* wb, const SplitCtl* ctl) {
+    if (threadIdx.x == 0) {
+        wb[0] = CG ? __ldcg(&ctl->wk.phibar) : ctl->wk.phibar;
+        wb[1] = CG ? __ldcg(&ctl->wk.Fbar) : ctl->wk.Fbar;
+        wb[2] = CG ? __ldcg(&ctl->wv.phibar) : ctl->wv.phibar;
+        wb[3] = CG ? __ldcg(&ctl->wv.Fbar) : ctl->wv.Fbar;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -277,6 +316,8 @@ __device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, 
         W.A[lane] = (float)((y[l] + (phibar - P.x[l]) * s) - Fbar);
     }
     if (lane == 0) {
+        W.phibar = phibar;
+        W.Fbar = Fbar;
         W.l0 = l0;
         W.n = n;
         W.ok = 1;
@@ -601,6 +642,8 @@ static __device__ __noinline__ void build_window(SplitWin& W, const PotDev& P, c
     W.l0 = l0;
     W.n = n;
     const double Fbar = y[lb] + (phibar - P.x[lb]) * (dy[lb] / P.dxl[lb]);
+    W.phibar = phibar;
+    W.Fbar = Fbar;
     for (int q = 0; q <= n; ++q) W.u[q] = (float)(P.x[l0 - 1 + q] - phibar);
     for (int q = 0; q < n; ++q) {
         const int l = l0 + q;
@@ -749,9 +792,12 @@ __device__ __forceinline__ void prime_body(const float* __restrict__ x, SplitCtl
         g.add(dk * dk + dj * dj + di * di);
         s1.add(xc);
         if (TABLE) {
-            const int q = bad ? -1 : window_find(su, sn, xc);
-            if (q < 0) bad = true;
-            else s2.add(sA[q] + ss[q] * xc);
+            if (sn < 0) {
+                bad = true;
+            } else {
+                const int q = window_find(su, sn, xc);
+                s2.add(q >= 0 ? sA[q] + ss[q] * xc : far_line(P, P.V, P.slopeV, &W.phibar, xc, bad));
+            }
         } else {
             s2.add(xc * xc);
         }
@@ -768,7 +814,50 @@ struct SplitBufs {
     float* xd;         // dphi (step n+1)
     const float* ps;   // dpi  (n-1/2)
     float* pd;         // dpi  (n+1/2)
+    // compensated form: the Kahan residuals of dphi and dpi (bf16; the value
+    // is x - residual), read for step n and written for step n+1
+    const unsigned short* xls = nullptr;
+    unsigned short* xld = nullptr;
+    const unsigned short* pls = nullptr;
+    unsigned short* pld = nullptr;
 };
+
+// Compensated form: v + inc with Kahan's compensated summation (the value is
+// v - c); returns the new v and updates c.  Over a run's ~10^4 steps the
+// rounding of a plain FP32 update accumulates as a random walk; with the
+// residual carried from step to step the state keeps the precision of one
+// rounding (Kahan, CACM 8 (1965) 40).
+__device__ __forceinline__ float kahan_add(float v, float inc, float& c) {
+    const float y = inc - c;
+    const float t = v + y;
+    c = (t - v) - y;
+    return t;
+}
+
+// Four bf16 residuals <-> float4 (round to nearest even), through L2: in a
+// persistent launch the residuals a step reads were written by other CTAs
+// during the launch.
+__device__ __forceinline__ uint2 ld_res4(const unsigned short* p) {
+    uint2 u;
+    asm volatile("ld.global.cg.v2.u32 {%0, %1}, [%2];" : "=r"(u.x), "=r"(u.y) : "l"(p));
+    return u;
+}
+
+__device__ __forceinline__ float4 unpack_res4(uint2 u) {
+    return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u), __uint_as_float(u.y << 16),
+                       __uint_as_float(u.y & 0xFFFF0000u));
+}
+
+__device__ __forceinline__ unsigned bf16x2_rn(float lo, float hi) {
+    unsigned r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+__device__ __forceinline__ void st_res4(unsigned short* p, float4 v) {
+    const uint2 u = make_uint2(bf16x2_rn(v.x, v.y), bf16x2_rn(v.z, v.w));
+    *reinterpret_cast<uint2*>(p) = u;
+}
 
 // Asynchronous global -> shared copies (cp.async), so the planes a CTA will
 // need next are in flight while it works on the current one.
@@ -904,6 +993,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
     float* wk = nb + (TJ + 1) * N;
     float* wv = wk + 3 * kWin + 1;
     __shared__ int nk_s, nv_s, active_s;
+    __shared__ double wbar[4];
     __shared__ float cf[6];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (tid == 0) {
@@ -919,6 +1009,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
             wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
             wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
         }
+        load_win_centres<false>(wbar, ctl);
     }
     __syncthreads();
     if (!active_s) return;
@@ -975,7 +1066,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
             const float x = pc[k];
             const float lap = pc[(k + 1) & m] + pc[(k - 1) & m] + pc[k + N] + pc[k - N] + pu[k] + pl[k] - 6.f * x;
             const float pi0 = pp[k];
-            const float dv = split_dv<TABLE>(x, wk, nk_s, ck, pn, kv, bad);
+            const float dv = split_dv<TABLE>(x, wk, nk_s, ck, pn, kv, bad, P, wbar);
             const float pin = pi0 + d * (lap_n * lap - fric * pi0 - dv);
             const float xn = x + d * pin;
             xnew[c] = xn;
@@ -984,7 +1075,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
                 B.xd[gb + k] = xn;
                 B.pd[gb + k] = pin;
                 rs1 += xn;
-                rs2 += split_v<TABLE>(xn, wv, nv_s, cv, bad);
+                rs2 += split_v<TABLE>(xn, wv, nv_s, cv, bad, P, wbar + 2);
             }
         }
         __syncthreads();
@@ -1109,7 +1200,7 @@ __device__ __forceinline__ void row4_issue_start(float* ring, float* pis, const 
     }
 }
 
-template <bool TABLE, int C4, int TJ, int PF, bool TMA = false>
+template <bool TABLE, int C4, int TJ, int PF, bool TMA = false, bool COMP = false>
 __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                            double* part, unsigned* counter, double* a_trace, long long u0,
                                            long long u1, int slot, int nslots, int* state, bool rev,
@@ -1125,6 +1216,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     float* wk = nb + 2 * NBP;
     float* wv = wk + 3 * kWin + 1;
     __shared__ int nk_s, nv_s, active_s;
+    __shared__ double wbar[4];
     __shared__ float cf[6];
     __shared__ unsigned tma_fail_g, tma_issued, mbar_limit;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -1148,6 +1240,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             wk[kWin + 1 + q] = __ldcg(&ctl->wk.A[q]); wk[2 * kWin + 1 + q] = __ldcg(&ctl->wk.s[q]);
             wv[kWin + 1 + q] = __ldcg(&ctl->wv.A[q]); wv[2 * kWin + 1 + q] = __ldcg(&ctl->wv.s[q]);
         }
+        load_win_centres<true>(wbar, ctl);
     }
     __syncthreads();
     if (!active_s) {
@@ -1236,6 +1329,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             if (!mbar_wait(&bars[Gq % NB], (Gq / NB) & 1u, mbar_limit)) atomicMin(&tma_fail_g, Gq);
         };
         float4 xp1[C4], xp2[C4];   // new values of this row: plane p-1 and p-2
+        uint2 rxn[C4], rpn[C4];    // compensated form: residuals of the next plane
         if (TMA) {
             if (w == 0) {
                 fence_proxy_async();
@@ -1303,8 +1397,28 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
             const float* pp = pis + (p % PIS) * PP + jl * N;
             float* nw = nb + (p & 1) * NBP + jl * N;
             const bool store = interior && p < CH;
-            const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)(j0 + jl) << lgN);
+            // (j0 + jl) & m: the halo row of the last tile wraps (its values
+            // are computed here, as its owner computes them, but not stored)
+            const long long gb = ((long long)(i & m) << (2 * lgN)) + ((long long)((j0 + jl) & m) << lgN);
             float4 xs[C4];
+            // compensated form: this plane's residuals (loaded one plane
+            // ahead), and the loads of the next plane's
+            uint2 rx[C4], rp[C4];
+            if (COMP) {
+    #pragma unroll
+                for (int v = 0; v < C4; ++v) {
+                    rx[v] = p == 0 ? ld_res4(B.xls + gb + 4 * (lane + 32 * v)) : rxn[v];
+                    rp[v] = p == 0 ? ld_res4(B.pls + gb + 4 * (lane + 32 * v)) : rpn[v];
+                }
+                if (p < CH) {
+                    const long long gn = ((long long)(plane(p + 1) & m) << (2 * lgN)) + ((long long)((j0 + jl) & m) << lgN);
+    #pragma unroll
+                    for (int v = 0; v < C4; ++v) {
+                        rxn[v] = ld_res4(B.xls + gn + 4 * (lane + 32 * v));
+                        rpn[v] = ld_res4(B.pls + gn + 4 * (lane + 32 * v));
+                    }
+                }
+            }
     #pragma unroll
             for (int v = 0; v < C4; ++v) xs[v] = ld4(pc + 4 * (lane + 32 * v));
             float rs1 = 0.f, rs2 = 0.f;
@@ -1327,21 +1441,37 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
                 lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
                 float4 pin, xn;
-                pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad));
-                pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad));
-                pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad));
-                pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad));
-                xn.x = x.x + d * pin.x;
-                xn.y = x.y + d * pin.y;
-                xn.z = x.z + d * pin.z;
-                xn.w = x.w + d * pin.w;
+                if (COMP) {
+                    float4 cx = unpack_res4(rx[v]), cp = unpack_res4(rp[v]);
+                    pin.x = kahan_add(pi.x, d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad, P, wbar)), cp.x);
+                    pin.y = kahan_add(pi.y, d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad, P, wbar)), cp.y);
+                    pin.z = kahan_add(pi.z, d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad, P, wbar)), cp.z);
+                    pin.w = kahan_add(pi.w, d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad, P, wbar)), cp.w);
+                    xn.x = kahan_add(x.x, d * pin.x, cx.x);
+                    xn.y = kahan_add(x.y, d * pin.y, cx.y);
+                    xn.z = kahan_add(x.z, d * pin.z, cx.z);
+                    xn.w = kahan_add(x.w, d * pin.w, cx.w);
+                    if (store) {
+                        st_res4(B.xld + gb + k, cx);
+                        st_res4(B.pld + gb + k, cp);
+                    }
+                } else {
+                    pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad, P, wbar));
+                    xn.x = x.x + d * pin.x;
+                    xn.y = x.y + d * pin.y;
+                    xn.z = x.z + d * pin.z;
+                    xn.w = x.w + d * pin.w;
+                }
                 st4(nw + k, xn);
                 if (store) {
                     st4(B.xd + gb + k, xn);
                     st4(B.pd + gb + k, pin);
                     rs1 += (xn.x + xn.y) + (xn.z + xn.w);
-                    rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad) + split_v<TABLE>(xn.y, wv, nv, cv, bad)) +
-                           (split_v<TABLE>(xn.z, wv, nv, cv, bad) + split_v<TABLE>(xn.w, wv, nv, cv, bad));
+                    rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE>(xn.y, wv, nv, cv, bad, P, wbar + 2)) +
+                           (split_v<TABLE>(xn.z, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE>(xn.w, wv, nv, cv, bad, P, wbar + 2));
                 }
                 xp2[v] = xp1[v];
                 xp1[v] = xn;
@@ -1414,6 +1544,7 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
     float* wk = nb + 2 * NN;
     float* wv = wk + 3 * kWin + 1;
     __shared__ int nk_s, nv_s, active_s;
+    __shared__ double wbar[4];
     __shared__ float cf[6];
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid == 0) {
@@ -1429,6 +1560,7 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
             wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
             wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
         }
+        load_win_centres<false>(wbar, ctl);
     }
     __syncthreads();
     if (!active_s) return;
@@ -1525,10 +1657,10 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
             lap.z = (x.w + x.y) + (up.z + dn.z) + (iu.z + il.z) - 6.f * x.z;
             lap.w = (xr + x.z) + (up.w + dn.w) + (iu.w + il.w) - 6.f * x.w;
             float4 pin, xn;
-            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad));
-            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad));
-            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad));
-            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad));
+            pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad, P, wbar));
+            pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad, P, wbar));
+            pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad, P, wbar));
+            pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad, P, wbar));
             xn.x = x.x + d * pin.x;
             xn.y = x.y + d * pin.y;
             xn.z = x.z + d * pin.z;
@@ -1538,8 +1670,8 @@ __device__ __forceinline__ void plane_body(const SplitBufs& B, SplitCtl* ctl, co
                 st4(B.xd + gb + o, xn);
                 st4(B.pd + gb + o, pin);
                 rs1 += (xn.x + xn.y) + (xn.z + xn.w);
-                rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad) + split_v<TABLE>(xn.y, wv, nv, cv, bad)) +
-                       (split_v<TABLE>(xn.z, wv, nv, cv, bad) + split_v<TABLE>(xn.w, wv, nv, cv, bad));
+                rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE>(xn.y, wv, nv, cv, bad, P, wbar + 2)) +
+                       (split_v<TABLE>(xn.z, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE>(xn.w, wv, nv, cv, bad, P, wbar + 2));
             }
             xp2[v] = xp1[v];
             xp1[v] = xn;

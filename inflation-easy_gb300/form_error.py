@@ -123,6 +123,22 @@ def compare(ref_dir: Path, got_dir: Path) -> dict:
     return out
 
 
+def deltaN_steps_off(ref_dir: Path, got_dir: Path, dN: float) -> dict:
+    """How the final deltaN maps (dump/state.bin) of two runs differ, in steps
+    of dN: the fraction of sites whose deltaN differs from the reference's by
+    a nonzero whole number of steps (after the constant shift of the float
+    Nmean, the median difference), and the largest deviation from a whole
+    number of steps (in steps)."""
+    def dn(d):
+        hdr = np.fromfile(Path(d) / "dump" / "state.bin", dtype=np.int32, count=4)
+        gs = int(hdr[0]) ** 3
+        return np.fromfile(Path(d) / "dump" / "state.bin", dtype=np.float64, count=gs, offset=16 + 64 + 16 * gs)
+    x = (dn(got_dir) - dn(ref_dir)) / dN
+    x = x - np.median(x)
+    k = np.rint(x)
+    return {"sites_off": float(np.mean(k != 0)), "off_by_fraction": float(np.max(np.abs(x - k)))}
+
+
 def omega_gw(precise: dict, L: float) -> np.ndarray:
     """Omega_GW(k) per save as the reference's notebook forms it
     (notebooks/plot.ipynb, section 8) from spectraGW (P_h), spectraGWdot

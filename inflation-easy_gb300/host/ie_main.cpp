@@ -269,8 +269,8 @@ void initialize_fields_host() {
 }
 
 void initialize_fields() {
-    if (P.ic_on_host && P.form == 1)
-        std::fprintf(stderr, "ic_on_host applies to the FP64 form; the split form draws its modes on the device.\n");
+    if (P.ic_on_host && P.form != 0)
+        std::fprintf(stderr, "ic_on_host applies to the FP64 form; the split forms draw their modes on the device.\n");
     if (P.ic_on_host && P.form == 0) {
         initialize_fields_host();
         return;
@@ -523,7 +523,7 @@ void output_parameters(bool first) {
                          k.abs_tol, k.rel_tol, k.min_dt, k.max_dt, k.safety);
         }
         std::fprintf(info, "rescale_s=%f\nrescale_B=%e\n", P.rescale_s, P.rescale_B);
-        std::fprintf(info, "engine=iegpu %d (GB300, %s)\n", iegpu_version(), P.form ? "split FP32" : "plain FP64");
+        std::fprintf(info, "engine=iegpu %d (GB300, %s)\n", iegpu_version(), P.form == 2 ? "compensated split FP32" : P.form ? "split FP32" : "plain FP64");
         time(&tstart);
         std::fprintf(info, "\nRun began at %s", ctime(&tstart));
     } else if (info) {

@@ -123,7 +123,7 @@ bool ie_params_load(IeParams& p, const char* path) {
         else if (k == "perform_deltaN" && to_int(v, i)) p.perform_deltaN = (i != 0);
         else if (k == "calculate_SIGW" && to_int(v, i)) p.calculate_SIGW = (i != 0);
         else if (k == "criterion" && to_int(v, i)) p.criterion = i;
-        else if (k == "form") p.form = (v == "split" || v == "1") ? 1 : 0;
+        else if (k == "form") p.form = (v == "split" || v == "1") ? 1 : (v == "split_comp" || v == "2") ? 2 : 0;
         else if (k == "ic_on_host" && to_int(v, i)) p.ic_on_host = (i != 0);
         else if (k == "seed" && to_int(v, i)) p.seed = i;
         else if (k == "rescale_s" && to_double(v, d)) p.rescale_s = d;

@@ -4,8 +4,8 @@
 // (src/runtime_parameters.cpp:17-112, 195-365).  The switches the reference
 // fixes at compile time in src/parameters.h (N, numerical_potential,
 // perform_deltaN, calculate_SIGW, post_inflation, the deltaN criterion) are
-// run-time keys here, plus `form` (fp64 | split) for the engine's arithmetic
-// form.
+// run-time keys here, plus `form` (fp64 | split | split_comp) for the engine's
+// arithmetic form.
 #pragma once
 
 #include <string>
@@ -21,7 +21,7 @@ struct IeParams {
     int perform_deltaN = 1;
     int calculate_SIGW = 0;
     int criterion = 99;          // 99: derive from numerical_potential (src/parameters.h:65-71)
-    int form = 0;                // 0 fp64, 1 split
+    int form = 0;                // 0 fp64, 1 split, 2 compensated split
     int ic_on_host = 0;          // 1: draw the initial modes on the host (bit-identical to the reference)
     // src/runtime_parameters.cpp:17-112
     int seed = 8;

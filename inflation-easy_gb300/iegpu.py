@@ -17,7 +17,7 @@ LIB_PATH = PKG / "_build" / "libiegpu.so"
 
 OK, EINVAL, ECUDA, ERANGE, ENAN, ECOURANT, ENOMEM, ETABLE, EUNSUPPORTED, ETIMEOUT, ETOOBIG, ECONVERGE = range(12)
 POT_HILLTOP, POT_TABLE = 0, 1
-FORM_FP64, FORM_SPLIT = 0, 1
+FORM_FP64, FORM_SPLIT, FORM_SPLIT_COMP = 0, 1, 2
 CRIT_GENERIC, CRIT_MONOTONIC, CRIT_ANTIMONOTONIC = 0, 1, -1
 F, FD, DELTAN = 0, 1, 2
 

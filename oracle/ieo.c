@@ -439,13 +439,16 @@ double ieo_potential(ieo_state* S, double v) {
 /* exact sums (engine-arithmetic mode)                                       */
 /* ------------------------------------------------------------------------- */
 
-/* A fixed-point accumulator over the whole double range (a "long
- * accumulator", Kulisch): 32-bit chunks held in signed 64-bit limbs, least
- * significant bit 2^-1074, so every finite double is added without error.
- * The total is rounded once to the nearest double, ties to even.  This is an
- * independent restatement of what the GPU engine's exact sums compute (the
- * correctly rounded exact sum); Python's math.fsum gives the same value. */
-#define XS_LIMBS 70
+/* A fixed-point accumulator over the whole double range and the range of
+ * products of two doubles (a "long accumulator", Kulisch): 32-bit chunks
+ * held in signed 64-bit limbs, least significant bit 2^-2150, so every finite
+ * double and every exact product of two finite doubles is added without
+ * error.  The total is rounded once to the nearest double, ties to even
+ * (subnormal results at 2^-1074).  This is an independent restatement of what
+ * the GPU engine's exact sums compute (the correctly rounded exact sum);
+ * Python's math.fsum gives the same value for sums of doubles. */
+#define XS_LIMBS 136   /* up to 2^(4352 - 2150): every product of two finite doubles */
+#define XS_SUBNORMAL_LSB 1076   /* bit position of 2^-1074 */
 typedef struct { int64_t l[XS_LIMBS]; long count; int nonfinite; } xsum_t;
 
 static void xs_init(xsum_t* X) { memset(X, 0, sizeof *X); }
@@ -462,6 +465,25 @@ static void xs_norm(xsum_t* X) {
     X->count = 0;
 }
 
+/* adds (negative ? -1 : 1) * v * 2^(pos - 2150) for v < 2^107 */
+static void xs_add_bits(xsum_t* X, unsigned __int128 v, int pos, int negative) {
+    const int k = pos >> 5, r = pos & 31;
+    unsigned __int128 w = v;
+    int64_t c[5];
+    /* chunks of v << r: at most 107 + 31 = 138 bits, five 32-bit chunks */
+    c[0] = (int64_t)(uint64_t)((w << r) & 0xFFFFFFFFu);
+    w >>= (32 - r);
+    for (int q = 1; q < 5; ++q) {
+        c[q] = (int64_t)(uint64_t)(w & 0xFFFFFFFFu);
+        w >>= 32;
+    }
+    for (int q = 0; q < 5; ++q) {
+        if (negative) X->l[k + q] -= c[q];
+        else X->l[k + q] += c[q];
+    }
+    if (++X->count >= (1L << 29)) xs_norm(X);
+}
+
 static void xs_add(xsum_t* X, double t) {
     uint64_t b;
     memcpy(&b, &t, sizeof b);
@@ -469,15 +491,21 @@ static void xs_add(xsum_t* X, double t) {
     uint64_t m = b & 0x000FFFFFFFFFFFFFULL;
     if (e == 0x7FF) { X->nonfinite = 1; return; }
     if (e == 0) { if (!m) return; e = 1; } else m |= 1ULL << 52;
-    const int pos = e - 1;                 /* bit position of m's lowest bit (2^-1074 is position 0) */
-    const int k = pos >> 5, r = pos & 31;
-    const unsigned __int128 v = (unsigned __int128)m << r;
-    const int64_t c0 = (int64_t)(uint64_t)(v & 0xFFFFFFFFu);
-    const int64_t c1 = (int64_t)(uint64_t)((v >> 32) & 0xFFFFFFFFu);
-    const int64_t c2 = (int64_t)(uint64_t)(v >> 64);
-    if (b >> 63) { X->l[k] -= c0; X->l[k + 1] -= c1; X->l[k + 2] -= c2; }
-    else { X->l[k] += c0; X->l[k + 1] += c1; X->l[k + 2] += c2; }
-    if (++X->count >= (1L << 29)) xs_norm(X);
+    xs_add_bits(X, (unsigned __int128)m, e + 1075, (int)(b >> 63));
+}
+
+/* adds the exact product x y */
+static void xs_add_product(xsum_t* X, double x, double y) {
+    uint64_t bx, by;
+    memcpy(&bx, &x, sizeof bx);
+    memcpy(&by, &y, sizeof by);
+    int ex = (int)((bx >> 52) & 0x7FF), ey = (int)((by >> 52) & 0x7FF);
+    if (ex == 0x7FF || ey == 0x7FF) { X->nonfinite = 1; return; }
+    uint64_t mx = bx & 0x000FFFFFFFFFFFFFULL, my = by & 0x000FFFFFFFFFFFFFULL;
+    if (ex) mx |= 1ULL << 52; else ex = 1;
+    if (ey) my |= 1ULL << 52; else ey = 1;
+    if (!mx || !my) return;
+    xs_add_bits(X, (unsigned __int128)mx * my, ex + ey, (int)((bx ^ by) >> 63));
 }
 
 static void xs_merge(xsum_t* X, const xsum_t* Y) {
@@ -509,20 +537,18 @@ static double xs_round(xsum_t* X) {
     if (top < 0) return 0.0;
 #define XS_BIT(p) ((p) < 0 ? 0u : ((w[(p) >> 5] >> ((p) & 31)) & 1u))
     int lsb = top - 52;
-    if (lsb < 0) lsb = 0;                  /* subnormal range: exact */
+    if (lsb < XS_SUBNORMAL_LSB) lsb = XS_SUBNORMAL_LSB;   /* subnormal results: 2^-1074 steps */
     uint64_t M = 0;
     for (int p = top; p >= lsb; --p) M = (M << 1) | XS_BIT(p);
-    if (lsb > 0) {
-        const unsigned rb = XS_BIT(lsb - 1);
-        int sticky = 0;
-        for (int p = lsb - 2; p >= 0 && !sticky; --p) sticky = XS_BIT(p) != 0;
-        if (rb && (sticky || (M & 1u))) {
-            M += 1;
-            if (M >> 53) { M >>= 1; lsb += 1; }
-        }
+    const unsigned rb = XS_BIT(lsb - 1);
+    int sticky = 0;
+    for (int p = lsb - 2; p >= 0 && !sticky; --p) sticky = XS_BIT(p) != 0;
+    if (rb && (sticky || (M & 1u))) {
+        M += 1;
+        if (M >> 53) { M >>= 1; lsb += 1; }
     }
 #undef XS_BIT
-    const double v = ldexp((double)M, lsb - 1074);
+    const double v = ldexp((double)M, lsb - 2150);
     return neg ? -v : v;
 }
 
@@ -531,6 +557,14 @@ double ieo_exact_sum(const double* x, size_t n) {
     xsum_t X;
     xs_init(&X);
     for (size_t i = 0; i < n; ++i) xs_add(&X, x[i]);
+    return xs_round(&X);
+}
+
+/* The correctly rounded exact sum of the exact products x[i] y[i]. */
+double ieo_exact_dot(const double* x, const double* y, size_t n) {
+    xsum_t X;
+    xs_init(&X);
+    for (size_t i = 0; i < n; ++i) xs_add_product(&X, x[i], y[i]);
     return xs_round(&X);
 }
 
@@ -581,7 +615,7 @@ static double potential_energy_engine(ieo_state* S) {
                 const double slope = (S->tV[l - 1] - S->tV[l]) / (S->tphi[l - 1] - S->tphi[l]);
                 xs_add(&X, S->tV[l] + (v - S->tphi[l]) * slope);
             } else {
-                xs_add(&X, v * v);
+                xs_add_product(&X, v, v);
             }
         }
         #pragma omp critical
@@ -816,7 +850,7 @@ static double gradient_energy_engine(ieo_state* S) {
                 const int jp = (j == N - 1) ? 0 : j + 1, jm = (j == 0) ? N - 1 : j - 1;
                 for (int k = 0; k < N; ++k) {
                     const int kp = (k == N - 1) ? 0 : k + 1, km = (k == 0) ? N - 1 : k - 1;
-                    xs_add(&X, f[IDX(N, i, j, k)] * LAPL_AT(double, f, N, i, j, k, ip, im, jp, jm, kp, km));
+                    xs_add_product(&X, f[IDX(N, i, j, k)], LAPL_AT(double, f, N, i, j, k, ip, im, jp, jm, kp, km));
                 }
             }
         }
@@ -854,7 +888,7 @@ double ieo_kin_energy(ieo_state* S) {
     if (S->engine_arith) {
         xsum_t X;
         xs_init(&X);
-        for (size_t id = 0; id < S->gs; ++id) xs_add(&X, pw2(S->fd[id]));
+        for (size_t id = 0; id < S->gs; ++id) xs_add_product(&X, S->fd[id], S->fd[id]);
         e = xs_round(&X);
     } else {
         for (size_t id = 0; id < S->gs; ++id) e += pw2(S->fd[id]);

@@ -107,8 +107,9 @@ double ieo_potential_energy(ieo_state* S);
 
 /* ---- engine-arithmetic mode ----
  * The GPU engine forms the Friedmann update's lattice sums exactly (the
- * correctly rounded exact sum, in any order), sums f^2 (hilltop) or the
- * slope form of V (table) for the potential, and evaluates pow(a, y) as
+ * correctly rounded exact sum of exact products f lapl(f), in any order),
+ * sums the exact f^2 (hilltop) or the slope form of V (table) for the
+ * potential, and evaluates pow(a, y) as
  * exact products and quotients for y = 0, 1, 2, -1.  With the mode on, the
  * oracle's leapfrog does the same, so the engine can be compared with it bit
  * for bit; with it off (the default) the oracle is the reference: serial sums
@@ -117,8 +118,10 @@ double ieo_potential_energy(ieo_state* S);
 void ieo_set_engine_arith(ieo_state* S, int on);
 /* The mode of states created from now on (ieo_create, ieo_run_program). */
 void ieo_set_engine_arith_default(int on);
-/* Correctly rounded exact sum of n doubles (the mode's summation). */
+/* Correctly rounded exact sum of n doubles, and of the exact products
+ * x[i] y[i] (the mode's summations). */
 double ieo_exact_sum(const double* x, size_t n);
+double ieo_exact_dot(const double* x, const double* y, size_t n);
 
 /* ---- leapfrog: src/evolution.cpp ---- */
 double ieo_gradient_energy(ieo_state* S);

@@ -96,6 +96,7 @@ def load() -> C.CDLL:
         "ieo_rescaled_step": (D, [P, D]), "ieo_leapfrog_steps": (I, [P, I]),
         "ieo_set_engine_arith": (None, [P, I]), "ieo_exact_sum": (D, [dp, C.c_size_t]),
         "ieo_set_engine_arith_default": (None, [I]),
+        "ieo_exact_dot": (D, [dp, dp, C.c_size_t]),
         "ieo_fftrn_d": (None, [dp, dp, I, I]), "ieo_fftrn_f": (None, [fp, fp, I, I]),
         "ieo_numbins": (I, [I]),
         "ieo_bin_spectrum": (None, [I, dp, dp, ip, dp]),
@@ -154,6 +155,14 @@ def exact_sum(x) -> float:
     """Correctly rounded exact sum (the oracle's long accumulator)."""
     a = np.ascontiguousarray(x, dtype=np.float64)
     return load().ieo_exact_sum(a.ctypes.data_as(C.POINTER(C.c_double)), a.size)
+
+
+def exact_dot(x, y) -> float:
+    """Correctly rounded exact sum of the exact products x[i] y[i]."""
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    b = np.ascontiguousarray(y, dtype=np.float64)
+    return load().ieo_exact_dot(a.ctypes.data_as(C.POINTER(C.c_double)), b.ctypes.data_as(C.POINTER(C.c_double)),
+                                a.size)
 
 
 def load_tables(inputs_dir: Path):

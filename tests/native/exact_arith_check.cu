@@ -6,6 +6,8 @@
 //                    the number of mismatching results
 //   sum FILE         the exact sum of the doubles in FILE (raw little-endian
 //                    binary); prints its bits in hex and the flags
+//   sumprod FILE     the exact sum of the products of the pairs of doubles in
+//                    FILE (x0 y0 x1 y1 ...); prints its bits and the flags
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -73,9 +75,25 @@ static int check_sum(const char* path) {
     return 0;
 }
 
+static int check_sumprod(const char* path) {
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return 2;
+    std::vector<double> x;
+    double v;
+    while (std::fread(&v, sizeof v, 1, fp) == 1) x.push_back(v);
+    std::fclose(fp);
+    Acc4 A;
+    acc_zero(A);
+    unsigned flags = 0;
+    for (size_t i = 0; i + 1 < x.size(); i += 2) acc_add_product(A, x[i], x[i + 1], flags);
+    std::printf("%016llx %u\n", dbits(acc_to_double(A)), flags);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc >= 4 && !std::strcmp(argv[1], "div")) return check_div(std::strtoull(argv[2], 0, 10), std::atol(argv[3]));
     if (argc >= 3 && !std::strcmp(argv[1], "sum")) return check_sum(argv[2]);
-    std::fprintf(stderr, "usage: %s div SEED COUNT | sum FILE\n", argv[0]);
+    if (argc >= 3 && !std::strcmp(argv[1], "sumprod")) return check_sumprod(argv[2]);
+    std::fprintf(stderr, "usage: %s div SEED COUNT | sum FILE | sumprod FILE\n", argv[0]);
     return 2;
 }

@@ -5,8 +5,9 @@ form that run on the integer pipes: the exact lattice sum (256-bit fixed
 point, rounded once) and the exact division by a fixed divisor (B^2).  Its
 host build (tests/native/exact_arith_check.cu, compiled with nvcc) is checked
 here: the division bit for bit against IEEE division over random dividends
-and divisors, and the sum against Python's math.fsum (Shewchuk's correctly
-rounded sum) and the oracle's long accumulator.
+and divisors, the sum against Python's math.fsum (Shewchuk's correctly
+rounded sum) and the oracle's long accumulator, and the sum of exact
+products against exact rational arithmetic.
 """
 from __future__ import annotations
 
@@ -68,6 +69,37 @@ def test_exact_sum_is_the_correctly_rounded_sum(checker, tmp_path, oracle_mod):
         want = math.fsum(x)
         assert s == want, (s, want)
         assert oracle_mod.exact_sum(x) == want
+
+
+def test_exact_sum_of_products(checker, tmp_path, oracle_mod):
+    """Sums of exact products (the engine's sums of f lapl(f), f^2, fd^2)
+    against Fractions and the oracle's long accumulator."""
+    from fractions import Fraction
+    rng = np.random.default_rng(11)
+    f = 0.0935 + 1e-6 * rng.standard_normal(3000)
+    lap = np.roll(f, 1) + np.roll(f, -1) - 2.0 * f
+    cases = [(f, lap), (f, f), (rng.standard_normal(3000) * 1e-3, rng.standard_normal(3000)),
+             # a cancelling pair and a small product whose bits all lie above 2^-192
+             (np.array([3.0, -3.0, 1e-12]), np.array([1.0 / 3.0, 1.0 / 3.0, 1e-12]))]
+    for x, y in cases:
+        p = tmp_path / "pairs.bin"
+        np.ascontiguousarray(np.stack([x, y], axis=1).ravel(), dtype="<f8").tofile(p)
+        out = subprocess.run([str(checker), "sumprod", str(p)], capture_output=True, text=True,
+                             check=True).stdout.split()
+        got = struct.unpack("<d", bytes.fromhex(out[0])[::-1])[0]
+        assert int(out[1]) == 0
+        want = float(sum((Fraction(a) * Fraction(b) for a, b in zip(x, y)), Fraction(0)))
+        assert got == want
+        assert oracle_mod.exact_dot(x, y) == want
+
+
+def test_exact_sum_drops_bits_below_its_range(checker, tmp_path):
+    """The accumulator's least significant bit is 2^-192: a product below it
+    adds nothing (lattice terms never come near it)."""
+    p = tmp_path / "pairs.bin"
+    np.array([1.0, 1.0, 1e-40, 1e-40], dtype="<f8").tofile(p)
+    out = subprocess.run([str(checker), "sumprod", str(p)], capture_output=True, text=True, check=True).stdout.split()
+    assert struct.unpack("<d", bytes.fromhex(out[0])[::-1])[0] == 1.0
 
 
 def test_exact_sum_flags_terms_it_cannot_hold(checker, tmp_path):

@@ -41,11 +41,14 @@ def test_bounded_wait_gives_up_and_context_recovers(engine):
         assert e.value.code == engine.ETIMEOUT
         assert "gave up" in str(e.value)
         # the context still runs a normal call: restore the state and the
-        # limits, and step as the untouched context does
+        # limits, and step as the untouched context does from the same
+        # uploaded state (an upload re-splits f into its mean and FP32
+        # perturbations, so both contexts take the same round trip)
         lat.set_wait_limit(0, unreachable=False)
-        lat.upload(engine.F, f0)
-        lat.upload(engine.FD, fd0)
-        bg = engine.Bg(*bg0)
+        for x in (lat, ref):
+            x.upload(engine.F, f0)
+            x.upload(engine.FD, fd0)
+        bg, bg_r = engine.Bg(*bg0), engine.Bg(*bg0)
         assert lat.leapfrog(1e30, 40, bg) == 40
         assert ref.leapfrog(1e30, 40, bg_r) == 40
         assert bg.as_tuple() == bg_r.as_tuple()

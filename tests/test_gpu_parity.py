@@ -153,11 +153,11 @@ def test_single_step_entry_points(engine, oracle_mod):
 def test_energies_and_means(engine, oracle_mod, tables):
     """kin, gradient and potential energies.  The engine sums exactly, so it
     equals the oracle in engine-arithmetic mode bit for bit, and its sum of
-    f lapl(f) equals math.fsum of the same per-site terms.  The reference's
+    f lapl(f) is the correctly rounded sum of the exact products f lapl(f)
+    (the products are not rounded before they are added).  The reference's
     serial sum of f lapl(f) cancels (the terms are of order |f| |lapl f|, the
     total of order |grad f|^2), so it keeps only about six digits of the
     gradient energy; that is the comparison with the reference mode below."""
-    import math
     for usr in (False, True):
         p, o = oracle_state(oracle_mod, 16, usr, False, tables, steps=20)
         lat, bg = lattice_like(engine, p, o, usr, False, tables)
@@ -173,7 +173,7 @@ def test_energies_and_means(engine, oracle_mod, tables):
             f = o.f.reshape(N, N, N)
             lap = (np.roll(f, -1, 2) + np.roll(f, 1, 2) + np.roll(f, -1, 1) + np.roll(f, 1, 1) + np.roll(f, -1, 0)
                    + np.roll(f, 1, 0) - 6.0 * f)
-            G = math.fsum((f * lap).ravel())
+            G = oracle_mod.exact_dot(f.ravel(), lap.ravel())
             a, dx = bg.a, p.L / N
             assert g == 0.5 * (-G) * ((1.0 / (a * dx)) * (1.0 / (a * dx))) / N ** 3
             sf, sfd, sf2 = lat.means()

@@ -163,14 +163,20 @@ def _bin_dev(got, ref):
     return dev
 
 
-@pytest.mark.parametrize("N,numerical", [(64, 0), (32, 1)])
-def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mod):
+@pytest.mark.parametrize("N,numerical,extra", [(64, 0, ""), (32, 1, ""),
+                                              # the USR table at 128^3 (its workload's size), inflation
+                                              # shortened to af = 1.35 (about 520 steps) and the deltaN
+                                              # stage to Nend = 0.1 (1000 steps) so the oracle ends in
+                                              # seconds
+                                              (128, 1, "af = 1.35\nNend = 0.1\n")])
+def test_program_full_precision_against_oracle(N, numerical, extra, tmp_path, oracle_mod):
     """The whole program (inflation to af, deltaN stage, spectra) against the
     oracle program twice:
       * in engine-arithmetic mode (lattice sums formed exactly, as the engine
-        forms them): a and H bit for bit at every save, <phi> to 1e-14 (its
-        output sum is formed in another order), P_dphi and P_zeta per k-bin to
-        1e-11 (the spectra's bin sums likewise);
+        forms them): a and H bit for bit at every save, <phi> to 1e-12 (the
+        output's sum of the field is a tree sum here and a serial one there),
+        P_dphi and P_zeta per k-bin to 1e-11 (the spectra's bin sums
+        likewise);
       * in reference mode (serial sums, libm pow): a, H, <phi> relative 1e-10;
         P_dphi and P_zeta per k-bin relative 1e-8, except where the
         reference's own rounding floor is larger.  The floor is measured here
@@ -179,7 +185,7 @@ def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mo
         5e-9 is held to twice its floor instead, and is printed.
     Bin counts are exact in both."""
     src = GOLDEN / ("n16_usr_sigw" if numerical else "n16_hilltop")
-    text = (src / "params.txt").read_text()
+    text = (src / "params.txt").read_text() + "\n" + extra
     wd = run_main(tmp_path, text, N, numerical, 0)
     p = oracle_mod.params_from_text(text, N, bool(numerical), False)
     od, oe = tmp_path / "oracle", tmp_path / "oracle_engine"
@@ -191,7 +197,7 @@ def test_program_full_precision_against_oracle(N, numerical, tmp_path, oracle_mo
     for x, y, z in zip(g["means"], o["means"], e["means"]):
         assert np.allclose(x[[1, 2, 4]], y[[1, 2, 4]], rtol=1e-10, atol=0)  # a, <phi>, H
         assert x[1] == z[1] and x[4] == z[4]                                 # a, H
-        assert np.allclose(x[2], z[2], rtol=1e-14, atol=0)                   # <phi>
+        assert np.allclose(x[2], z[2], rtol=1e-12, atol=0)                   # <phi>
     for tag in ("spectrum", "spectrumN"):
         assert len(g[tag]) == len(o[tag]) == len(e[tag])
         dev_ref = _bin_dev(g[tag], o[tag])
