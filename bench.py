@@ -12,10 +12,11 @@ state (384 MB in FP64) is larger than L2, so no flush is needed between steps.
 
 The headline value is the plain FP64 form, the reference's own precision and
 per-site arithmetic (like for like with the reference arm).  Beside it, under
-"forms": the split form (FP32 perturbations about an FP64 background) on the
-same workload with its error statement against the FP64 form over a whole run
-(inflation to af = 512 and the deltaN stage: P_dphi and P_zeta per k-bin,
-<dphi^2>, H(t) at every save); the batched ensemble (512 x 32^3 + 64 x 64^3 +
+"forms": the split form (FP32 perturbations about an FP64 background) and the
+compensated split form (the same with Kahan residuals carried from step to
+step) on the same workload, each with its error statement against the FP64
+form over a whole run (inflation to af = 512 and the deltaN stage: P_dphi and
+P_zeta per k-bin, <dphi^2>, H(t) at every save); the batched ensemble (512 x 32^3 + 64 x 64^3 +
 8 x 128^3 lattices, USR table potential, advanced together, against the same
 number of steps of one lattice of each size alone, and its deltaN stage); the
 SIGW split step at 256^3 and 512^3 with the Omega_GW comparison against the
@@ -57,6 +58,7 @@ METRIC = "site-updates/s at 256^3: FP64 plain vs split-FP32 vs batched; % of HBM
 UNIT = "site-updates/s"
 # algorithmic HBM bytes per site of the dominant kernel of one step
 BYTES_STEP_SPLIT = 16  # split form: read dphi, dpi; write dphi, dpi (FP32)
+BYTES_STEP_COMP = 24   # compensated split form: 16 + read and write the bf16 residuals of dphi and dpi
 BYTES_STEP_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
 # FP64 thread instructions per site of one plain FP64 leapfrog step (k_lsum:
 # six DADD and one DMUL of the Laplacian, the sums' products on the integer
@@ -235,7 +237,7 @@ def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None
     bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
     lat.evolve_fields(0.5 * w["dt"], bg)   # first half drift, src/evolution.cpp:935
     af = 1e30  # a fixed number of steps is timed
-    shape = lat.autotune(bg) if form == iegpu.FORM_SPLIT else None
+    shape = lat.autotune(bg) if form != iegpu.FORM_FP64 else None
     clk = Clocks(clocks_index) if clocks_index is not None else None
     if clk:
         clk.__enter__()
@@ -309,8 +311,10 @@ def usr_tables():
 
 def measure_ensemble(iegpu, steps, warmup, peak):
     """The batched form: every lattice of the ensemble advanced `steps` leapfrog
-    steps together (one kernel per lattice size per step, the sizes side by
-    side), then the deltaN stage, zeta spectra and the pooled zeta histogram;
+    steps together, timed in both modes (one kernel per lattice size per
+    step, the sizes side by side in CUDA graphs; one cooperative launch per 64
+    steps over a queue of every lattice's tiles), then the deltaN stage, zeta
+    spectra and the pooled zeta histogram;
     against the same number of steps of one lattice of each size run alone
     (the sequential way: one lattice after another)."""
     w = USR
@@ -326,14 +330,25 @@ def measure_ensemble(iegpu, steps, warmup, peak):
     for b in range(len(Ns)):
         bg[b].astep = bg[b].a
     shape = ens.autotune(bg)
-    launches0 = ens.launches
-    ens.timer_start()
-    taken = ens.leapfrog(1e30, steps, bg)
-    ms = ens.timer_stop()
-    launches = ens.launches - launches0
-    assert int(taken.min()) == steps
-    for b in range(len(Ns)):
-        bg[b].astep = bg[b].a
+    modes = {}
+    for persistent in (False, True):
+        # per-size launches (CUDA graphs, autotuned shapes), then one
+        # cooperative launch per 64 steps over the mixed queue
+        ens.set_persistent(persistent)
+        ens.leapfrog(1e30, warmup, bg)
+        for b in range(len(Ns)):
+            bg[b].astep = bg[b].a
+        launches0 = ens.launches
+        ens.timer_start()
+        taken = ens.leapfrog(1e30, steps, bg)
+        ms_mode = ens.timer_stop()
+        assert int(taken.min()) == steps
+        for b in range(len(Ns)):
+            bg[b].astep = bg[b].a
+        modes["persistent" if persistent else "per_size"] = (ms_mode, ens.launches - launches0)
+    best = min(modes, key=lambda k: modes[k][0])
+    ms, launches = modes[best]
+    ens.set_persistent(False)
     prof_steps = min(20, steps)
     _, kms = ens.profile(prof_steps, bg)
     for b in range(len(Ns)):
@@ -361,13 +376,19 @@ def measure_ensemble(iegpu, steps, warmup, peak):
         seq[n] = lat.timer_stop() / steps
         lat.close()
     t_seq = sum(c * steps * seq[n] for n, c in ENSEMBLE)
-    kernel_ms = kms / prof_steps
-    achieved = BYTES_STEP_SPLIT * sites / (kernel_ms * 1e-3) / 1e9
+    # HBM figure from the timed region (the faster mode), 16 B per site-update
+    achieved = BYTES_STEP_SPLIT * sites * steps / (ms * 1e-3) / 1e9
+    mode_figs = {k: {"ms_per_step": v[0] / steps, "gpu_launches": v[1],
+                     "frac_of_measured_hbm": BYTES_STEP_SPLIT * sites * steps / (v[0] * 1e-3) / 1e9 / peak}
+                 for k, v in modes.items()}
     return {"workload": "512 x 32^3 + 64 x 64^3 + 8 x 128^3 lattices, USR table potential (params.numerical.txt), "
                         "split form, device Bunch-Davies initial conditions, seeds 1..584",
             "lattices": len(Ns), "sites": sites, "steps": steps,
             "site_updates_per_s": steps * sites / (ms * 1e-3), "ms_per_step": ms / steps,
-            "kernel_ms_per_step": kernel_ms, "achieved_gbs": achieved, "frac_of_measured_hbm": achieved / peak,
+            "mode": best, "modes": mode_figs,
+            "achieved_gbs": achieved, "frac_of_measured_hbm": achieved / peak,
+            "frac_source": "timed region of the faster mode (CUDA events), 16 B per site-update",
+            "per_size_kernel_ms_isolated": kms / prof_steps,
             "gpu_launches": launches,
             "shapes": {str(n): [int(shape["rows"][Ns.index(n)]), int(shape["prefetch"][Ns.index(n)]),
                                 int(shape["chunks"][Ns.index(n)])] for n, _ in ENSEMBLE},
@@ -439,21 +460,28 @@ def measure_post_inflation(iegpu, N, steps, warmup, peak):
 
 
 def measure_split_error(N, workdir):
-    """The split form's error statement over a whole run at N^3 (hilltop
-    preset, seed 8, af = 2N, deltaN stage): the host program run in both
-    forms from the same device initial conditions, every save compared."""
+    """The split forms' error statement over a whole run at N^3 (hilltop
+    preset, seed 8, af = 2N, deltaN stage): the host program run in the FP64
+    form and in each split form from the same device initial conditions,
+    every save compared; plus how many sites' deltaN is a whole dN step off."""
     import form_error as fe
     text = fe.preset_text(fe.HILLTOP, N)
     t0 = time.perf_counter()
     ref = fe.run_program(text, Path(workdir) / "fp64", "fp64")
-    t1 = time.perf_counter()
-    got = fe.run_program(text, Path(workdir) / "split", "split")
-    t2 = time.perf_counter()
-    err = fe.compare(ref, got)
-    err.update({"workload": f"hilltop, N={N}^3, seed 8, inflation to af={2 * N} and the deltaN stage "
-                            f"(dN=1e-7, Nend=1e-3), split vs plain FP64 form from the same device initial conditions",
-                "program_s": {"fp64": t1 - t0, "split": t2 - t1}})
-    return err
+    secs = {"fp64": time.perf_counter() - t0}
+    out = {}
+    for form in ("split", "split_comp"):
+        t0 = time.perf_counter()
+        got = fe.run_program(text, Path(workdir) / form, form)
+        secs[form] = time.perf_counter() - t0
+        err = fe.compare(ref, got)
+        err["deltaN_steps_off"] = fe.deltaN_steps_off(ref, got, fe.HILLTOP["dN"])
+        err.pop("H_per_save", None)
+        err["workload"] = (f"hilltop, N={N}^3, seed 8, inflation to af={2 * N} and the deltaN stage (dN=1e-7, "
+                           f"Nend=1e-3), {form} vs plain FP64 form from the same device initial conditions")
+        out[form] = err
+    out["program_s"] = secs
+    return out
 
 
 def measure_sigw_error(N, workdir):
@@ -586,6 +614,8 @@ def engine_arm(args):
     # the split form on the same workload
     sp = measure_form(iegpu, iegpu.FORM_SPLIT, N, args.steps, args.warmup, None, False, dist)
     sp_value = ws * args.steps * N ** 3 / (sp["ms"] * 1e-3)
+    spc = measure_form(iegpu, iegpu.FORM_SPLIT_COMP, N, args.steps, args.warmup, None, False, dist)
+    spc_value = ws * args.steps * N ** 3 / (spc["ms"] * 1e-3)
     if rank != 0:
         return 0
     with tempfile.TemporaryDirectory(prefix="ie_bench_") as wd:
@@ -606,6 +636,8 @@ def engine_arm(args):
     sp_kernel_ms = (sp["ms"] - sp["aux_ms"]) / args.steps
     sp_achieved = BYTES_STEP_SPLIT * N ** 3 / (sp_kernel_ms * 1e-3) / 1e9
     sp_tr = traffic.get("split_step_bytes_per_site")
+    spc_kernel_ms = (spc["ms"] - spc["aux_ms"]) / args.steps
+    spc_achieved = BYTES_STEP_COMP * N ** 3 / (spc_kernel_ms * 1e-3) / 1e9
     bytes_state = 2 * 8 * N ** 3
     e2e = {"value": ws * args.steps * N ** 3 / fp["e2e_s"], "unit": UNIT,
            "h2d_bytes_per_step": bytes_state / args.steps, "d2h_bytes_per_step": bytes_state / args.steps,
@@ -643,11 +675,24 @@ def engine_arm(args):
                                              "kernel_ms_isolated": sp["kernel_ms"],
                                              "algorithmic_bytes_per_site": BYTES_STEP_SPLIT,
                                              "traffic": None if sp_tr is None else sp_tr * N ** 3},
-                                "shape": sp["shape"], "gpu_launches": sp["launches"], "error": err},
+                                "shape": sp["shape"], "gpu_launches": sp["launches"],
+                                "error": err["split"] if err else None},
+                      "split_comp": {"value": spc_value, "ms_per_step": spc["ms"] / args.steps,
+                                     "over_fp64": spc_value / value,
+                                     "roofline": {"achieved": spc_achieved, "frac": spc_achieved / peak,
+                                                  "kernel": "k_split_rows4_persist (compensated)",
+                                                  "kernel_ms": spc_kernel_ms, "kernel_ms_isolated": spc["kernel_ms"],
+                                                  "algorithmic_bytes_per_site": BYTES_STEP_COMP},
+                                     "shape": spc["shape"], "gpu_launches": spc["launches"],
+                                     "error": err["split_comp"] if err else None,
+                                     "note": "dphi, dpi in FP32 plus their Kahan residuals in bf16, carried from "
+                                             "step to step"},
+                      "error_program_s": err["program_s"] if err else None,
                       "batched": ens, "sigw": dict(sigw, error=sigw_err), "sigw_512": sigw512,
                       "post_inflation": post, "kernels": kern}}
-    line["metric_note"] = ("value: plain FP64 form at 256^3 (like for like with the reference arm); forms.split: "
-                           "the split form on the same workload and its whole-run error against FP64; "
+    line["metric_note"] = ("value: plain FP64 form at 256^3 (like for like with the reference arm); forms.split, "
+                           "forms.split_comp: the split forms on the same workload and their whole-run errors "
+                           "against FP64; "
                            "forms.batched: the ensemble (site-updates/s, lattices/s over sequential runs)")
     if cpu:
         line["cpu_baseline"] = cpu

@@ -388,6 +388,15 @@ int  iegpu_ens_profile(struct iegpu_ens* ens, int nsteps, iegpu_bg* bg, double* 
 int  iegpu_ens_autotune(struct iegpu_ens* ens, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
 /* Sets the launch shape of the lattices of size N, as iegpu_set_shape. */
 int  iegpu_ens_set_shape(struct iegpu_ens* ens, int N, int rows, int prefetch, int chunks);
+/* No counterpart in the reference (it runs one lattice per process).  on = 1:
+ * iegpu_ens_leapfrog advances every lattice in cooperative launches of up to
+ * 64 steps each, the CTAs pulling (lattice, row tile, step) items of every
+ * size from one queue, the largest lattices first; an item waits only for its
+ * own lattice's update of the step before (bounded: IEGPU_ETIMEOUT).  Every
+ * lattice uses 8-row tiles with 2 planes ahead and 32 planes per item.
+ * on = 0: one kernel per lattice size and step, the sizes as parallel
+ * branches of a CUDA graph (the default).  N in {32, 64, 128} for on = 1. */
+int  iegpu_ens_set_persistent(struct iegpu_ens* ens, int on);
 int  iegpu_ens_timer_start(struct iegpu_ens* ens);
 int  iegpu_ens_timer_stop(struct iegpu_ens* ens, float* ms);
 /* N_b^3 doubles of lattice b: IEGPU_F / IEGPU_FD (phibar + dphi, pibar + dpi,

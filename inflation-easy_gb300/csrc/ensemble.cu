@@ -109,6 +109,85 @@ __global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_ens_plane(EnsArgs A, co
     plane_body<TABLE, N, NT, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, t.i0, t.CH, t.slot, t.nslots, t.st);
 }
 
+// Persistent ensemble step: one cooperative launch advances every lattice by
+// up to `nsteps` leapfrog steps.  Item q of the launch is step q / nitems of
+// entry q % nitems of `queue` (one step's (lattice, tile) pairs, the largest
+// lattices first); CTAs claim items in order from qsync[0].  Before an item of
+// step s a CTA waits until its lattice's update of step s - 1 is published
+// (qsync[2 + b] >= s, written by the lattice's last CTA of that step after
+// its Friedmann update) or the lattice has stopped.  Items are claimed in
+// queue order and an item waits only for items earlier in the queue, which
+// resident CTAs hold, so every wait ends; it is still bounded (`polls`), after
+// which the lattice's step is marked IEGPU_ETIMEOUT, qsync[1] is raised and
+// every CTA leaves.  Every lattice runs the 8-row tile body of its size and
+// its scalar update with the one-lattice arithmetic.
+constexpr int kEnsPersistTJ = 8, kEnsPersistPF = 2;
+
+__device__ __forceinline__ int ld_acquire_int(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <bool TABLE>
+__global__ void __launch_bounds__((kEnsPersistTJ + 1) * 32, 3) k_ens_persist(EnsArgs A, const int2* __restrict__ queue,
+                                                                         int nitems, int nsteps, unsigned* qsync,
+                                                                         unsigned polls) {
+    constexpr int TJ = kEnsPersistTJ, PF = kEnsPersistPF;
+    __shared__ int item_s, go_s;
+    unsigned* done_step = qsync + 2;
+    const long long total = (long long)nitems * nsteps;
+    for (;;) {
+        if (threadIdx.x == 0) item_s = (int)atomicAdd(qsync, 1u);
+        __syncthreads();
+        const long long q = item_s;
+        if (q >= total) break;
+        const int s = (int)(q / nitems);
+        const int2 w = queue[q % nitems];
+        const int b = w.x;
+        if (threadIdx.x == 0) {
+            int go = 0;   // 1: step the item; 2: the lattice has stopped; 0: leave
+            for (unsigned t = 0; t < polls; ++t) {
+                if (ld_acquire(qsync + 1)) break;
+                if (ld_acquire_int(A.cur + b) & 2) { go = 2; break; }
+                if (ld_acquire(done_step + b) >= (unsigned)s) { go = 1; break; }
+                __nanosleep(64);
+            }
+            if (go == 0 && !ld_acquire(qsync + 1)) {
+                if (atomicCAS(&A.ctl[b].error, 0, IEGPU_ETIMEOUT) == 0) A.ctl[b].errval = 0.0;
+                atomicExch(qsync + 1, 1u);
+            }
+            go_s = go;
+        }
+        __syncthreads();
+        if (go_s == 0) break;
+        if (go_s == 1) {
+            const EnsLat& L = A.lat[b];
+            const int c = __ldcg(A.cur + b) & 1;
+            const SplitBufs B{A.x[c] + L.off, A.x[c ^ 1] + L.off, A.p[c] + L.off, A.p[c ^ 1] + L.off};
+            const int N = 1 << L.lg;
+            const int rt = w.y % L.rowtiles, ch = w.y / L.rowtiles;
+            const int i0 = (int)(((long long)ch * N) / L.chunks);
+            const int CH = (int)(((long long)(ch + 1) * N) / L.chunks) - i0;
+            StepSeq sq;
+            sq.seq = done_step + b;
+            sq.base = (unsigned)s * (unsigned)L.tiles;
+            sq.val = (unsigned)(s + 1);
+            SplitCtl* ctl = A.ctl + b;
+            double* part = A.part + 3LL * L.part_off;
+            switch (L.lg) {
+                case 5: rows_body<TABLE, 1, TJ, PF>(B, ctl, A.P, L.K, part, A.counter + b, nullptr, rt * TJ, i0, CH, w.y,
+                                                    L.tiles, A.cur + b, sq); break;
+                case 6: rows_body<TABLE, 2, TJ, PF>(B, ctl, A.P, L.K, part, A.counter + b, nullptr, rt * TJ, i0, CH, w.y,
+                                                    L.tiles, A.cur + b, sq); break;
+                default: rows_body<TABLE, 4, TJ, PF>(B, ctl, A.P, L.K, part, A.counter + b, nullptr, rt * TJ, i0, CH,
+                                                     w.y, L.tiles, A.cur + b, sq); break;
+            }
+        }
+        __syncthreads();   // the item's shared memory is free before the next claim
+    }
+}
+
 // evolve_fields of every lattice with its own step d[b]: dphi += d dpi and
 // phibar += d pibar (the one-lattice split drift, lattice by lattice).
 __global__ void __launch_bounds__(256) k_ens_drift(EnsArgs A, const double* __restrict__ d, int count) {
@@ -576,11 +655,144 @@ static int ens_autotune(iegpu_ens* e, const iegpu_bg* bg0) {
     return ens_sync(e, "autotune");
 }
 
+// ---- persistent mode -------------------------------------------------------
+
+static constexpr int kEnsPersistSteps = 64;   // steps per cooperative launch
+
+static bool ens_persist_ok(const iegpu_ens* e) {
+    for (int N : e->sizes)
+        if (N != 32 && N != 64 && N != 128) return false;
+    return true;
+}
+
+// Plane chunks of a lattice in the persistent mode: 32 planes per item.
+static int ens_persist_chunks(int N) { return N / 32; }
+
+// Shapes of the persistent mode (8-row tiles, 2 planes ahead, 32 planes per
+// item), the layout, the grid (every CTA resident) and the shared memory.
+static int ens_persist_setup(iegpu_ens* e) {
+    for (EnsClass& c : e->cls) {
+        c.TJ = kEnsPersistTJ;
+        c.PF = kEnsPersistPF;
+        c.chunks = ens_persist_chunks(c.N);
+    }
+    if (int rc = ens_layout(e)) return rc;
+    size_t smem = 0;
+    for (int N : e->sizes) smem = std::max(smem, sizeof(float) * (size_t)split_row_smem_floats(kEnsPersistTJ, N, kEnsPersistPF));
+    const void* fn = e->helper[0]->pot.table ? (const void*)k_ens_persist<true> : (const void*)k_ens_persist<false>;
+    if (int rc = ens_cuda(e, smem_optin(fn, smem), "shared memory attribute")) return rc;
+    int per_sm = 0;
+    if (int rc = ens_cuda(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (kEnsPersistTJ + 1) * 32, smem),
+                          "occupancy"))
+        return rc;
+    if (per_sm < 1) return ens_error(e, IEGPU_EUNSUPPORTED, "the persistent ensemble kernel does not fit an SM");
+    e->persist_grid = per_sm * e->sms;
+    e->persist_smem = smem;
+    e->tuned = 1;
+    return IEGPU_OK;
+}
+
+// One step's queue over the lattices with active[b]: every tile of every
+// lattice, the largest lattices first (their items then come early in each
+// step, and a step's items of a lattice long before its next step's).
+static int ens_persist_queue(iegpu_ens* e, const std::vector<char>& active) {
+    std::vector<int2> q;
+    for (size_t ci = e->cls.size(); ci-- > 0;)
+        for (int b : e->cls[ci].lats)
+            if (active[(size_t)b])
+                for (int t = 0; t < e->lat_h[(size_t)b].tiles; ++t) q.push_back(make_int2(b, t));
+    if ((int)q.size() > e->queue_cap) {
+        if (int rc = ens_sync(e, "queue")) return rc;
+        if (e->queue) cudaFree(e->queue);
+        e->queue = nullptr;
+        e->queue_cap = 0;
+        if (int rc = ens_alloc(e, &e->queue, q.size())) return rc;
+        e->queue_cap = (int)q.size();
+    }
+    e->nqueue = (int)q.size();
+    if (q.empty()) return IEGPU_OK;
+    return ens_cuda(e, cudaMemcpyAsync(e->queue, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, e->stream),
+                    "queue");
+}
+
+static int ens_persist_launch(iegpu_ens* e, int nsteps) {
+    const EnsArgs A = ens_args(e);
+    const size_t words = 2 + (size_t)e->count;
+    if (int rc = ens_cuda(e, cudaMemsetAsync(e->qsync, 0, sizeof(unsigned) * words, e->stream), "queue reset")) return rc;
+    if (int rc = ens_cuda(e, cudaMemsetAsync(e->counter, 0, sizeof(unsigned) * (size_t)e->count, e->stream),
+                          "counter reset"))
+        return rc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)e->persist_grid);
+    cfg.blockDim = dim3((kEnsPersistTJ + 1) * 32);
+    cfg.dynamicSmemBytes = e->persist_smem;
+    cfg.stream = e->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const unsigned polls = 1u << 20;
+    const cudaError_t err = A.P.table
+        ? cudaLaunchKernelEx(&cfg, k_ens_persist<true>, A, (const int2*)e->queue, e->nqueue, nsteps, e->qsync, polls)
+        : cudaLaunchKernelEx(&cfg, k_ens_persist<false>, A, (const int2*)e->queue, e->nqueue, nsteps, e->qsync, polls);
+    e->launches++;
+    return ens_cuda(e, err, "persistent ensemble launch");
+}
+
+static int ens_leapfrog_persist(iegpu_ens* e, const double* af, int max_steps, iegpu_bg* bg, int* steps) {
+    e->mat = 0;
+    bool shaped = e->persist_grid != 0;
+    for (const EnsClass& c : e->cls)
+        shaped = shaped && c.TJ == kEnsPersistTJ && c.PF == kEnsPersistPF && c.chunks == ens_persist_chunks(c.N);
+    if (!shaped)
+        if (int rc = ens_persist_setup(e)) return rc;
+    ens_fill(e, bg, af, max_steps);
+    if (int rc = ens_upload_ctl(e)) return rc;
+    std::vector<char> active((size_t)e->count, 1);
+    if (int rc = ens_persist_queue(e, active)) return rc;
+    ens_launch_prime(e);
+    int* seen = e->cur_h + e->count;
+    long long launched = 0;
+    int rc = IEGPU_OK;
+    while (!rc && launched < max_steps && e->nqueue > 0) {
+        const int n = (int)std::min<long long>(kEnsPersistSteps, max_steps - launched);
+        if ((rc = ens_persist_launch(e, n))) break;
+        launched += n;
+        if ((rc = ens_cuda(e, cudaMemcpyAsync(seen, e->cur, sizeof(int) * (size_t)e->count, cudaMemcpyDeviceToHost,
+                                              e->stream), "state copy")))
+            break;
+        if ((rc = ens_sync(e, "persistent ensemble step"))) break;
+        int alive = 0, dead = 0;
+        for (int b = 0; b < e->count; ++b) {
+            if ((seen[b] & 2) == 0) alive++;
+            else if (active[(size_t)b]) dead++;
+        }
+        if (alive == 0) break;
+        if (dead > 0) {
+            // drop the stopped lattices from the queue
+            for (int b = 0; b < e->count; ++b) active[(size_t)b] = (seen[b] & 2) == 0;
+            if ((rc = ens_persist_queue(e, active))) break;
+        }
+    }
+    // the one-launch-per-step kernels and the priming reduction expect zeroed counters
+    const int rc2 = ens_cuda(e, cudaMemsetAsync(e->counter, 0, sizeof(unsigned) * (size_t)e->count, e->stream),
+                             "counter reset");
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (int r = ens_finish(e, bg, steps)) return r;
+    for (int b = 0; b < e->count; ++b)
+        if (e->ctl_h[b].error == IEGPU_ETIMEOUT)
+            return ens_error(e, IEGPU_ETIMEOUT, "a wait of the persistent ensemble kernel gave up (lattice %d)", b);
+    return IEGPU_OK;
+}
+
 static int ens_leapfrog(iegpu_ens* e, const double* af, int max_steps, iegpu_bg* bg, int* steps) {
     if (steps)
         for (int b = 0; b < e->count; ++b) steps[b] = 0;
     if (max_steps < 0) return ens_error(e, IEGPU_EINVAL, "max_steps must be >= 0");
     if (max_steps == 0) return IEGPU_OK;
+    if (e->persist) return ens_leapfrog_persist(e, af, max_steps, bg, steps);
     if (!e->tuned)
         if (int rc = ens_autotune(e, bg)) return rc;
     e->mat = 0;
@@ -687,6 +899,7 @@ int iegpu_ens_create(const iegpu_config* cfg, const int* Ns, int count, iegpu_en
     if (!rc) rc = ens_alloc(e, &e->cur, (size_t)count);
     if (!rc) rc = ens_alloc(e, &e->lat, (size_t)count);
     if (!rc) rc = ens_alloc(e, &e->counter, (size_t)count);
+    if (!rc) rc = ens_alloc(e, &e->qsync, 2 + (size_t)count);
     if (!rc) rc = ens_alloc(e, &e->dctl, 1);
     if (!rc) rc = ens_alloc(e, &e->dscr, 4 * (size_t)count + 64);
     if (!rc) rc = ens_alloc(e, &e->iscr, 4 * (size_t)count + 64);
@@ -740,7 +953,7 @@ int iegpu_ens_destroy(iegpu_ens* e) {
     ens_destroy_graph(e);
     for (iegpu_ctx* h : e->helper) iegpu_destroy(h);
     void* dev[] = {e->x[0], e->x[1], e->p[0], e->p[1], e->f, e->fd, e->dn, e->ctl, e->cur, e->lat,
-                   e->pwork, e->part, e->counter, e->dscr, e->iscr, e->red, e->dctl};
+                   e->pwork, e->part, e->counter, e->dscr, e->iscr, e->red, e->dctl, e->queue, e->qsync};
     for (void* q : dev)
         if (q) cudaFree(q);
     for (EnsClass& c : e->cls) {
@@ -849,6 +1062,15 @@ int iegpu_ens_autotune(iegpu_ens* e, const iegpu_bg* bg, int* rows, int* prefetc
         if (prefetch) prefetch[b] = c.PF;
         if (chunks) chunks[b] = c.chunks;
     }
+    return IEGPU_OK;
+}
+
+int iegpu_ens_set_persistent(iegpu_ens* e, int on) {
+    if (!e) return IEGPU_EINVAL;
+    if (on && !ens_persist_ok(e))
+        return ens_error(e, IEGPU_EUNSUPPORTED, "the persistent ensemble launch covers lattices of N = 32, 64, 128");
+    e->persist = on != 0;
+    e->persist_grid = 0;
     return IEGPU_OK;
 }
 

@@ -109,6 +109,15 @@ struct iegpu_ens {
     std::vector<double> phiref;
 
     int tuned = 0;
+    // persistent mode: one cooperative launch of up to kEnsPersistSteps steps
+    // over a queue of (lattice, tile) items of every size, big lattices first
+    int persist = 0;
+    int2* queue = nullptr;               // one step's items
+    int queue_cap = 0;
+    int nqueue = 0;
+    unsigned* qsync = nullptr;           // [0] claim counter, [1] abort flag, then the per-lattice published steps
+    int persist_grid = 0;
+    size_t persist_smem = 0;
     cudaGraphExec_t exec = nullptr;
     int graph_steps = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};

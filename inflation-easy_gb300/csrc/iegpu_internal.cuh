@@ -248,6 +248,7 @@ struct iegpu_ctx {
     int split_mat = 0;                    // FP64 buffers hold the field (deltaN stage)
     iegpu::RowCfg row_cfg;                // split row-kernel launch shape
     int tuned = 0;
+    int tuning = 0;                       // the autotuner is timing shapes: no tensor kernel
     int part_cap = 0;
     unsigned wait_polls = 0;              // bounded device waits: poll limit (0: default)
     unsigned wait_bias = 0;               // test hook: persistent barrier target never reached

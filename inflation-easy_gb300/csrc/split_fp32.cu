@@ -768,7 +768,9 @@ static void launch_rows(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, d
 
 static void launch_step(iegpu_ctx* c, int src) {
     const SplitConst K = split_const(c);
-    if (c->cfg.sigw) {
+    // the autotuner times the scalar step's shapes on a saved copy of dphi and
+    // dpi alone: the tensors must not be stepped by its trial steps
+    if (c->cfg.sigw && !c->tuning) {
         const float hodx = (float)(0.5 / K.dx);
         if (c->gs % (4 * kThreads) == 0)
             k_split_h4<<<(unsigned)(c->gs / (4 * kThreads)), kThreads, 0, c->stream>>>(c->sp[src], sigw_split(c, src),
@@ -977,9 +979,19 @@ static int split_profile_persist(iegpu_ctx* c, int nsteps, iegpu_bg* bg, double*
 // Autotuner of the row kernel's launch shape: rows per tile (TJ), planes
 // prefetched (PF) and plane chunks (grid height).  Each candidate runs one
 // warm-up and three timed steps (CUDA events, stream-ordered) from a saved copy
-// of the live state, which is restored afterwards; the fastest shape is kept
-// for the life of the context.
+// of dphi and dpi (and their residuals), which is restored afterwards; the
+// trial steps do not step the tensors.  The fastest shape is kept for the
+// life of the context.
+static int split_autotune_shapes(iegpu_ctx* c, const iegpu_bg* bg0);
+
 int split_autotune(iegpu_ctx* c, const iegpu_bg* bg0) {
+    c->tuning = 1;
+    const int rc = split_autotune_shapes(c, bg0);
+    c->tuning = 0;
+    return rc;
+}
+
+static int split_autotune_shapes(iegpu_ctx* c, const iegpu_bg* bg0) {
     const int N = c->N;
     c->tuned = 1;
     if (N < 32 || N > 512) return IEGPU_OK;

@@ -697,6 +697,9 @@ __device__ __forceinline__ void finish_sums_slot(df64 (&v)[3], SplitCtl* ctl, co
         pd[3 * slot + 2] = v[2];
         __threadfence();
         last = (atomicAdd(counter, 1u) == sq.base + (unsigned)nslots - 1);
+        // in a persistent launch this SM may have read earlier steps' partials:
+        // the fence orders the reads below after the other CTAs' writes
+        if (last && sq.seq) __threadfence();
     }
     last = __shfl_sync(0xffffffffu, last, 0);
     if (!last) return;
@@ -978,10 +981,11 @@ __host__ __device__ inline int split_row_smem_floats(int TJ, int N, int PF) {
 // nearly equal plane ranges (any count, so the grid can match the SMs).
 // One CTA: rows j0 .. j0+TJ-1, planes i0 .. i0+CH-1; its sums go to partial
 // slot `slot` of `nslots`.
+// sq: the publication of the step's update (persistent ensemble launch).
 template <bool TABLE, int C, int TJ, int PF>
 __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, const PotDev& P, const SplitConst& K,
                                           double* part, unsigned* counter, double* a_trace, int j0, int i0, int CH,
-                                          int slot, int nslots, int* state) {
+                                          int slot, int nslots, int* state, StepSeq sq = StepSeq()) {
     constexpr int kRowPrefetch = PF, kRowPhiSlots = 3 + PF, kRowPiSlots = 1 + PF;
     constexpr int N = 32 * C, m = N - 1;
     constexpr int lgN = (C == 1) ? 5 : (C == 2) ? 6 : (C == 4) ? 7 : (C == 8) ? 8 : 9;
@@ -996,20 +1000,23 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
     __shared__ double wbar[4];
     __shared__ float cf[6];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    // the control block is read through L2: in a persistent ensemble launch
+    // another CTA wrote it during the launch
     if (tid == 0) {
         const SplitCtl& Cc = *ctl;
-        active_s = Cc.active;
-        cf[0] = Cc.d; cf[1] = Cc.lapl; cf[2] = Cc.fric; cf[3] = Cc.pn; cf[4] = Cc.kv;
-        nk_s = Cc.wk.n;
-        nv_s = Cc.wv.n;
+        active_s = __ldcg(&Cc.active);
+        cf[0] = __ldcg(&Cc.d); cf[1] = __ldcg(&Cc.lapl); cf[2] = __ldcg(&Cc.fric); cf[3] = __ldcg(&Cc.pn);
+        cf[4] = __ldcg(&Cc.kv);
+        nk_s = __ldcg(&Cc.wk.n);
+        nv_s = __ldcg(&Cc.wv.n);
     }
     if (TABLE) {
-        for (int q = tid; q <= kWin; q += NTH) { wk[q] = ctl->wk.u[q]; wv[q] = ctl->wv.u[q]; }
+        for (int q = tid; q <= kWin; q += NTH) { wk[q] = __ldcg(&ctl->wk.u[q]); wv[q] = __ldcg(&ctl->wv.u[q]); }
         for (int q = tid; q < kWin; q += NTH) {
-            wk[kWin + 1 + q] = ctl->wk.A[q]; wk[2 * kWin + 1 + q] = ctl->wk.s[q];
-            wv[kWin + 1 + q] = ctl->wv.A[q]; wv[2 * kWin + 1 + q] = ctl->wv.s[q];
+            wk[kWin + 1 + q] = __ldcg(&ctl->wk.A[q]); wk[2 * kWin + 1 + q] = __ldcg(&ctl->wk.s[q]);
+            wv[kWin + 1 + q] = __ldcg(&ctl->wv.A[q]); wv[2 * kWin + 1 + q] = __ldcg(&ctl->wv.s[q]);
         }
-        load_win_centres<false>(wbar, ctl);
+        load_win_centres<true>(wbar, ctl);
     }
     __syncthreads();
     if (!active_s) return;
@@ -1111,7 +1118,7 @@ __device__ __forceinline__ void rows_body(const SplitBufs& B, SplitCtl* ctl, con
     // there is nothing for a precomputed part to overlap with
     if (nslots > 1) maybe_precompute(ctl, P, K);
     df64 v[3] = {g.df(), s1.df(), s2.df()};
-    finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, true);
+    finish_sums_slot(v, ctl, P, K, part, counter, a_trace, slot, nslots, state, true, 0, sq);
 }
 
 // Vector variant of the row kernel for N >= 128: lane l owns the four

@@ -137,6 +137,7 @@ def load() -> C.CDLL:
         "iegpu_ens_profile": (I, [P, I, P, dp, dp]),
         "iegpu_ens_autotune": (I, [P, P, ip, ip, ip]),
         "iegpu_ens_set_shape": (I, [P, I, I, I, I]),
+        "iegpu_ens_set_persistent": (I, [P, I]),
         "iegpu_ens_timer_start": (I, [P]),
         "iegpu_ens_timer_stop": (I, [P, C.POINTER(C.c_float)]),
         "iegpu_ens_download": (I, [P, I, I, dp]),
@@ -537,6 +538,11 @@ class Ensemble:
 
     def set_shape(self, N: int, rows: int, prefetch: int, chunks: int) -> None:
         self._check(self.lib.iegpu_ens_set_shape(self.h, N, rows, prefetch, chunks))
+
+    def set_persistent(self, on: bool) -> None:
+        """One cooperative launch of up to 64 steps over a queue of every
+        lattice's tiles (on), or one kernel per size and step (off)."""
+        self._check(self.lib.iegpu_ens_set_persistent(self.h, 1 if on else 0))
 
     def timer_start(self) -> None:
         self._check(self.lib.iegpu_ens_timer_start(self.h))

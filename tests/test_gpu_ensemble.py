@@ -48,12 +48,14 @@ def single_run(engine, tables, usr, N, seed, shape, af, steps, form=None):
     return lat, bg, taken
 
 
-def ensemble_run(engine, tables, usr, af, steps, Ns=NS, seeds=SEEDS, shapes=ROWS):
+def ensemble_run(engine, tables, usr, af, steps, Ns=NS, seeds=SEEDS, shapes=ROWS, persistent=False):
     w = _case(usr)
     ens = engine.Ensemble(Ns, w["L"], w["dt"], w["V0"], w["ns"], potential=_pot(engine, usr))
     if usr:
         ens.set_table(*tables)
-    if shapes is not None:
+    if persistent:
+        ens.set_persistent(True)
+    elif shapes is not None:
         for N in sorted(set(Ns)):
             ens.set_shape(N, *shapes[N])
     hub = ens.bunch_davies(seeds, w["phi0"], w["dphi0"])
@@ -121,6 +123,63 @@ def test_ensemble_matches_single_lattices(usr, shapes, engine, tables):
                 lat.shift(engine.DELTAN, lat.sum(engine.DELTAN) / N ** 3)
                 counts, f2 = lat.spectrum(engine.DELTAN)
                 assert np.array_equal(counts, spectra[b][0]) and np.array_equal(f2, spectra[b][1]), b
+
+
+# the persistent launch's shapes: 8-row tiles, 2 planes ahead, 32 planes per item
+PERSIST = {32: (8, 2, 1), 64: (8, 2, 2), 128: (8, 2, 4)}
+
+
+@pytest.mark.parametrize("usr", [False, True])
+def test_ensemble_persistent_matches_per_size_launches(usr, engine, tables):
+    """One cooperative launch over a queue of every lattice's tiles against one
+    kernel per size and step with the same 8-row tiles (32^3 and 64^3, whose
+    per-size kernel runs the same tile body): fields, background and steps
+    taken bit for bit, over 150 steps (three launches of up to 64 steps), with
+    two lattices stopping on their own af inside a launch (one after 71 steps,
+    in the second launch)."""
+    Ns, seeds = [64, 32, 32, 64, 32, 32], [2, 3, 4, 5, 6, 7]
+    w = _case(usr)
+    probe, pbg, _ = single_run(engine, tables, usr, 32, 4, PERSIST[32], 1e30, 0)
+    with probe:
+        _, tr = probe.leapfrog(1e30, 120, pbg, trace=True)
+    af = np.full(len(Ns), 1e30)
+    af[2] = 0.5 * (tr[69] + tr[70])    # a passes af in step 71, in the second launch
+    af[5] = 0.5 * (tr[9] + tr[10])     # a lattice seeded 7: its own trace, near step 10
+    out = []
+    for persistent in (False, True):
+        ens, bg, taken = ensemble_run(engine, tables, usr, af, 150, Ns=Ns, seeds=seeds, shapes=PERSIST,
+                                      persistent=persistent)
+        with ens:
+            out.append((list(taken), [b.as_tuple() for b in bg],
+                        [(ens.download(q, engine.F), ens.download(q, engine.FD)) for q in range(len(Ns))]))
+    (ta, ba, fa), (tb, bb, fb) = out
+    assert ta == tb and ta[2] == 71 and 0 < ta[5] < 150 and ta[0] == 150
+    assert ba == bb
+    for (x, y), (u, v) in zip(fa, fb):
+        assert np.array_equal(x, u) and np.array_equal(y, v)
+
+
+def test_ensemble_persistent_against_single_lattices(engine, tables):
+    """The persistent launch with a 128^3 lattice among 32^3 ones (its tile body
+    is the scalar row body, where a one-lattice run at 128^3 uses the vector
+    row body: the same per-site arithmetic, lattice sums in another FP32
+    order) against one-lattice split runs of the same seeds, 200 steps: fields
+    within 1e-5 of their spread, a, ad, t relative 1e-9."""
+    Ns, seeds = [128, 32, 32], [9, 3, 4]
+    ens, ebg, taken = ensemble_run(engine, tables, True, np.full(3, 1e30), 200, Ns=Ns, seeds=seeds, persistent=True)
+    with ens:
+        assert list(taken) == [200] * 3
+        for b, (N, seed) in enumerate(zip(Ns, seeds)):
+            lat, bg, t = single_run(engine, tables, True, N, seed, PERSIST[N], 1e30, 200)
+            with lat:
+                assert t == 200
+                for got, ref in ((ebg[b].a, bg.a), (ebg[b].ad, bg.ad), (ebg[b].t, bg.t)):
+                    assert abs(got - ref) <= 1e-9 * abs(ref)
+                for field in (engine.F, engine.FD):
+                    ref = lat.download(field)
+                    got = ens.download(b, field)
+                    tol = 1e-5 if N == 128 else 0.0
+                    assert np.max(np.abs(got - ref)) <= tol * np.std(ref - ref.mean()), (b, field)
 
 
 def test_ensemble_zeta_histogram(engine, tables):

@@ -52,7 +52,10 @@ def test_split_round_trip(engine, oracle_mod):
         assert np.isclose(g, go, rtol=1e-4)
 
 
-@pytest.mark.parametrize("N,usr,sigw", [(32, False, False), (32, True, False), (16, True, True), (64, False, False)])
+@pytest.mark.parametrize("N,usr,sigw", [(32, False, False), (32, True, False), (16, True, True), (64, False, False),
+                                        # N >= 32: the first call autotunes the step kernel's shape on
+                                        # trial steps, which must leave the tensors alone
+                                        (32, True, True), (64, False, True)])
 def test_split_leapfrog_matches_fp64(N, usr, sigw, engine, oracle_mod, tables):
     p, o = oracle_state(oracle_mod, N, usr, sigw, tables)
     lat, bg = split_like(engine, p, o, usr, sigw, tables)
