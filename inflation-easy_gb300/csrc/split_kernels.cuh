@@ -276,8 +276,26 @@ __device__ __forceinline__ void sum_partials_df(const df64* p, int nb, df64 (&ou
 
 // The bracket of v, as table_bracket: the count of nodes with key >= key(v),
 // clamped to [1, n-1] (the nodes descend strictly), counted by the warp.
-__device__ __forceinline__ int warp_bracket(const PotDev& P, double v) {
+// hint: a bracket near v (the last step's, from its window), or < 0.  The
+// warp first looks at the 32 nodes around it: when v lies among them the
+// count is their offset plus one ballot, one load per lane; otherwise it
+// counts over the whole table.
+__device__ __forceinline__ int warp_bracket(const PotDev& P, double v, int hint = -1) {
     const long long kv = order_key(v);
+    if (hint >= 0 && P.n >= 32) {
+        int base = hint - 16;
+        base = base < 0 ? 0 : (base > P.n - 32 ? P.n - 32 : base);
+        const bool ge = __ldg(&P.key[base + (threadIdx.x & 31)]) >= kv;
+        const unsigned m = __ballot_sync(0xffffffffu, ge);
+        // nodes before base are all >= kv when node base is (or base = 0),
+        // nodes after base + 31 all < kv when that one is (or it is the last)
+        const bool lo_ok = base == 0 || (m & 1u);
+        const bool hi_ok = base + 32 == P.n || !(m >> 31);
+        if (lo_ok && hi_ok) {
+            const int cnt = base + __popc(m);
+            return cnt < 1 ? 1 : (cnt > P.n - 1 ? P.n - 1 : cnt);
+        }
+    }
     int cnt = 0;
     for (int i = threadIdx.x & 31; i < P.n; i += 32) cnt += (__ldg(&P.key[i]) >= kv) ? 1 : 0;
 #pragma unroll
@@ -295,13 +313,16 @@ __device__ __forceinline__ bool table_out_of_range(const PotDev& P, double v) {
 __device__ __forceinline__ void build_window_warp(SplitWin& W, const PotDev& P, const double* y,
                                                   const double* slope, double phibar, int* err) {
     const int lane = threadIdx.x & 31;
+    // the window being replaced holds last step's bracket (ok = 0: none yet)
+    const int hint = W.ok ? W.l0 + kWin / 2 : -1;
+    __syncwarp();
     if (lane == 0) W.ok = 0;
     if (!P.table) return;
     if (table_out_of_range(P, phibar)) {
         *err = 1;
         return;
     }
-    const int lb = warp_bracket(P, phibar);
+    const int lb = warp_bracket(P, phibar, hint);
     int l0 = lb - kWin / 2;
     if (l0 < 1) l0 = 1;
     int n = kWin;
@@ -367,7 +388,7 @@ static __device__ __noinline__ void split_scalars_warp(SplitCtl& C, const PotDev
             return;
         }
     }
-    const int lbar = P.table ? warp_bracket(P, phibar0) : 0;
+    const int lbar = P.table ? warp_bracket(P, phibar0, C.wk.ok ? C.wk.l0 + kWin / 2 : -1) : 0;
     double phibar_new = phibar0;
     if (w0) {
         double t = C.bg.t, a = C.bg.a, ad = C.bg.ad, astep = C.bg.astep;
@@ -450,7 +471,7 @@ static __device__ __noinline__ void split_precompute(SplitCtl& C, const PotDev& 
     const int mode = C.mode, steps_done = C.steps_done, steps_limit = C.steps_limit;
     const double phibar = C.phibar;
     if (mode != kModeLeapfrog || steps_done >= steps_limit || !(C.bg.a <= C.af)) return;
-    const int lbar = P.table ? warp_bracket(P, phibar) : 0;
+    const int lbar = P.table ? warp_bracket(P, phibar, C.wk.ok ? C.wk.l0 + kWin / 2 : -1) : 0;
     if (!w0) return;
     const double a = C.bg.a, ad = C.bg.ad, pibar = C.pibar, s = K.s;
     const double astep = steps_done > 0 ? a : C.bg.astep;
