@@ -588,9 +588,22 @@ def engine_arm(args):
         traffic = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
     except (OSError, ValueError):
         pass
+    if args.only in ("split", "split_comp", "sigw"):
+        # one form's timed steps alone (a short run for profilers); no other forms, no CPU baseline
+        if args.only == "sigw":
+            r = measure_sigw(iegpu, N, args.steps, args.warmup, peak)
+            ms = r["ms_per_step"]
+        else:
+            form = iegpu.FORM_SPLIT if args.only == "split" else iegpu.FORM_SPLIT_COMP
+            r = measure_form(iegpu, form, N, args.steps, args.warmup, None, False, dist)
+            ms = r["ms"] / args.steps
+        if rank == 0:
+            print(json.dumps({"only": args.only, "N": N, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": ms, "site_updates_per_s": N ** 3 / (ms * 1e-3)}), flush=True)
+        return 0
     # the FP64 pipe's measured rate (thread instructions per second), the
     # plain FP64 form's compute roofline
-    fp64_rate = iegpu.measure_fp64_rate(1)
+    fp64_rate = iegpu.measure_fp64_rate(1) if not args.headline_only else None
 
     # headline: the plain FP64 form (the reference's precision and per-site
     # arithmetic); the clocks are sampled from 1.5 s before to 0.5 s after the
@@ -710,6 +723,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the whole-run error statements and 512^3")
     ap.add_argument("--headline-only", action="store_true",
                     help="time the plain FP64 step only and print a short line (for profiler runs)")
+    ap.add_argument("--only", choices=["split", "split_comp", "sigw"], default=None,
+                    help="time one other form alone at --n and print a short line (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
