@@ -225,14 +225,18 @@ def reference_arm(args):
     return 0
 
 
-def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None, settle_s=0.0, tail_s=0.0):
+def measure_form(iegpu, form, N, steps, warmup, clocks_index, e2e_too, dist=None, settle_s=0.0, tail_s=0.0,
+                 usr=False):
     """Times `steps` leapfrog steps of one form; returns a dict of figures.
     With clocks_index set, nvidia-smi samples the SM clocks from settle_s
     seconds of untimed steps before the warm-up to tail_s seconds of untimed
     steps after the timed region, so the samples bracket it."""
     import numpy as np
-    w = WORKLOAD
-    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=form)
+    w = dict(USR, ns=0.97, seed=8) if usr else WORKLOAD
+    lat = iegpu.Lattice(N, w["L"], w["dt"], w["V0"], w["ns"], form=form,
+                        potential=iegpu.POT_TABLE if usr else iegpu.POT_HILLTOP)
+    if usr:
+        lat.set_table(*usr_tables())
     H = lat.bunch_davies(w["seed"], w["phi0"], w["dphi0"])
     bg = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
     lat.evolve_fields(0.5 * w["dt"], bg)   # first half drift, src/evolution.cpp:935
@@ -595,10 +599,10 @@ def engine_arm(args):
             ms = r["ms_per_step"]
         else:
             form = iegpu.FORM_SPLIT if args.only == "split" else iegpu.FORM_SPLIT_COMP
-            r = measure_form(iegpu, form, N, args.steps, args.warmup, None, False, dist)
+            r = measure_form(iegpu, form, N, args.steps, args.warmup, None, False, dist, usr=args.usr)
             ms = r["ms"] / args.steps
         if rank == 0:
-            print(json.dumps({"only": args.only, "N": N, "steps": args.steps, "warmup": args.warmup,
+            print(json.dumps({"only": args.only, "usr": args.usr, "N": N, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": ms, "site_updates_per_s": N ** 3 / (ms * 1e-3)}), flush=True)
         return 0
     # the FP64 pipe's measured rate (thread instructions per second), the
@@ -725,6 +729,7 @@ def main():
                     help="time the plain FP64 step only and print a short line (for profiler runs)")
     ap.add_argument("--only", choices=["split", "split_comp", "sigw"], default=None,
                     help="time one other form alone at --n and print a short line (for profiler runs)")
+    ap.add_argument("--usr", action="store_true", help="with --only split|split_comp: the USR table potential")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()

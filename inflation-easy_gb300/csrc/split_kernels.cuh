@@ -32,6 +32,23 @@ __device__ __forceinline__ int window_find(const float* u, int n, float v) {
     return q;
 }
 
+// The same bracket without branches, for lattices whose perturbations span
+// several brackets (512^3: a third of the sites lie outside the background's
+// bracket, and divergent walks cost more than the search): the brackets with
+// u[q] >= v form a prefix of the descending nodes (n + 1 of them, n <= kWin
+// < 32) and q is its last index, found by binary lifting over the node
+// indices with one shared-memory load per step.
+__device__ __forceinline__ int window_lift(const float* u, int n, float v) {
+    int q = 0;
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1) {
+        const int jn = q + st;
+        const float uj = u[jn < n ? jn : n];
+        q = (jn < n && uj >= v) ? jn : q;
+    }
+    return (v <= u[0] && v > u[n]) ? q : -1;
+}
+
 // The window's bracket of the background value (dphi = 0), kept in registers
 // with the bounds of its two neighbours.  Perturbations are a small fraction
 // of a bracket, so nearly every site falls in the bracket (two compares) and
@@ -90,12 +107,13 @@ static __device__ __noinline__ float far_line(const PotDev& P, const double* y, 
 
 // potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop).
 // wb: {phibar, Fbar} of the kick window, for sites beyond it.
-template <bool TABLE>
+// LIFT: every site searches the window branch-free (window_lift).
+template <bool TABLE, bool LIFT = false>
 __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, const WinCache& c, float pn, float kv,
                                           bool& bad, const PotDev& P, const double* wb) {
     if (TABLE) {
-        if (x <= c.hi && x > c.lo) return pn * (c.A + c.s * x);
-        const int q = window_near(wk, nk, c, x);
+        if (!LIFT && x <= c.hi && x > c.lo) return pn * (c.A + c.s * x);
+        const int q = LIFT ? window_lift(wk, nk, x) : window_near(wk, nk, c, x);
         if (q < 0) return pn * far_line(P, P.dV, P.slopedV, wb, x, bad);
         return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
     }
@@ -104,12 +122,12 @@ __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, cons
 
 // V(phibar + x) - V(phibar) in table units (table) or x^2 (hilltop).
 // wb: {phibar, Fbar} of the potential window, for sites beyond it.
-template <bool TABLE>
+template <bool TABLE, bool LIFT = false>
 __device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad,
                                          const PotDev& P, const double* wb) {
     if (TABLE) {
-        if (x <= c.hi && x > c.lo) return c.A + c.s * x;
-        const int q = window_near(wv, nv, c, x);
+        if (!LIFT && x <= c.hi && x > c.lo) return c.A + c.s * x;
+        const int q = LIFT ? window_lift(wv, nv, x) : window_near(wv, nv, c, x);
         if (q < 0) return far_line(P, P.V, P.slopeV, wb, x, bad);
         return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
     }
@@ -1234,6 +1252,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                                            long long u1, int slot, int nslots, int* state, bool rev,
                                            bool preissued = false, StepSeq sq = StepSeq()) {
     constexpr int N = 128 * C4, m = N - 1;
+    constexpr bool kLift = C4 >= 4;   // 512^3: the branch-free window search
     constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
     constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
     constexpr int PHS = 3 + PF, PIS = 1 + PF;
@@ -1471,10 +1490,10 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 float4 pin, xn;
                 if (COMP) {
                     float4 cx = unpack_res4(rx[v]), cp = unpack_res4(rp[v]);
-                    pin.x = kahan_add(pi.x, d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad, P, wbar)), cp.x);
-                    pin.y = kahan_add(pi.y, d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad, P, wbar)), cp.y);
-                    pin.z = kahan_add(pi.z, d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad, P, wbar)), cp.z);
-                    pin.w = kahan_add(pi.w, d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad, P, wbar)), cp.w);
+                    pin.x = kahan_add(pi.x, d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE, kLift>(x.x, wk, nk, ck, pn, kv, bad, P, wbar)), cp.x);
+                    pin.y = kahan_add(pi.y, d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE, kLift>(x.y, wk, nk, ck, pn, kv, bad, P, wbar)), cp.y);
+                    pin.z = kahan_add(pi.z, d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE, kLift>(x.z, wk, nk, ck, pn, kv, bad, P, wbar)), cp.z);
+                    pin.w = kahan_add(pi.w, d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE, kLift>(x.w, wk, nk, ck, pn, kv, bad, P, wbar)), cp.w);
                     xn.x = kahan_add(x.x, d * pin.x, cx.x);
                     xn.y = kahan_add(x.y, d * pin.y, cx.y);
                     xn.z = kahan_add(x.z, d * pin.z, cx.z);
@@ -1484,10 +1503,10 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                         st_res4(B.pld + gb + k, cp);
                     }
                 } else {
-                    pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE>(x.x, wk, nk, ck, pn, kv, bad, P, wbar));
-                    pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE>(x.y, wk, nk, ck, pn, kv, bad, P, wbar));
-                    pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE>(x.z, wk, nk, ck, pn, kv, bad, P, wbar));
-                    pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE>(x.w, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE, kLift>(x.x, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE, kLift>(x.y, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE, kLift>(x.z, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE, kLift>(x.w, wk, nk, ck, pn, kv, bad, P, wbar));
                     xn.x = x.x + d * pin.x;
                     xn.y = x.y + d * pin.y;
                     xn.z = x.z + d * pin.z;
@@ -1498,8 +1517,8 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                     st4(B.xd + gb + k, xn);
                     st4(B.pd + gb + k, pin);
                     rs1 += (xn.x + xn.y) + (xn.z + xn.w);
-                    rs2 += (split_v<TABLE>(xn.x, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE>(xn.y, wv, nv, cv, bad, P, wbar + 2)) +
-                           (split_v<TABLE>(xn.z, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE>(xn.w, wv, nv, cv, bad, P, wbar + 2));
+                    rs2 += (split_v<TABLE, kLift>(xn.x, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE, kLift>(xn.y, wv, nv, cv, bad, P, wbar + 2)) +
+                           (split_v<TABLE, kLift>(xn.z, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE, kLift>(xn.w, wv, nv, cv, bad, P, wbar + 2));
                 }
                 xp2[v] = xp1[v];
                 xp1[v] = xn;
