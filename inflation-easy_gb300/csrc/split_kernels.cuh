@@ -33,8 +33,9 @@ __device__ __forceinline__ int window_find(const float* u, int n, float v) {
 }
 
 // The same bracket without branches, for lattices whose perturbations span
-// several brackets (512^3: a third of the sites lie outside the background's
-// bracket, and divergent walks cost more than the search): the brackets with
+// several brackets (512^3: 1 % of the sites lie beyond the background's
+// bracket and its neighbours, enough for divergent walks in a quarter of the
+// warps to cost more than the search): the brackets with
 // u[q] >= v form a prefix of the descending nodes (n + 1 of them, n <= kWin
 // < 32) and q is its last index, found by binary lifting over the node
 // indices with one shared-memory load per step.
@@ -49,38 +50,34 @@ __device__ __forceinline__ int window_lift(const float* u, int n, float v) {
     return (v <= u[0] && v > u[n]) ? q : -1;
 }
 
-// The window's bracket of the background value (dphi = 0), kept in registers
-// with the bounds of its two neighbours.  Perturbations are a small fraction
-// of a bracket, so nearly every site falls in the bracket (two compares) and
-// nearly all the rest in a neighbour (two more compares and the neighbour's
-// coefficients from shared memory, the same address across most of a warp).
-// Only a site beyond the neighbours walks the window.  Any of these finds the
-// same bracket, which is unique.
+// The window's bracket of the background value (dphi = 0) and its two
+// neighbours, bounds and lines kept in registers.  Perturbations are a small
+// fraction of a bracket, so nearly every site falls in one of the three, which
+// is chosen by selects without a branch (a warp's lanes do not diverge when a
+// few of its sites lie in a neighbour).  Only a site beyond the neighbours
+// searches the window.  Any of these finds the same bracket, which is unique.
 struct WinCache {
     float hi, lo, A, s;   // bracket q: lo < v <= hi, value A + s v
     float hi2, lo2;       // u[q-1] and u[q+2] (hi and lo when there is no such neighbour)
+    float Al, sl, Ar, sr; // lines of brackets q-1 and q+1 (q's own when there is no such neighbour)
     int q;
 };
 
 template <bool TABLE>
 __device__ __forceinline__ WinCache win_cache(const float* w, int n) {
-    WinCache c{-1.f, 1.f, 0.f, 0.f, -1.f, 1.f, 0};   // empty interval
+    WinCache c{-1.f, 1.f, 0.f, 0.f, -1.f, 1.f, 0.f, 0.f, 0.f, 0.f, 0};   // empty interval
     if (TABLE) {
         const int q = window_find(w, n, 0.f);
         if (q >= 0) {
+            const int ql = q > 0 ? q - 1 : q, qr = q + 1 < n ? q + 1 : q;
             c = WinCache{w[q], w[q + 1], w[kWin + 1 + q], w[2 * kWin + 1 + q], q > 0 ? w[q - 1] : w[q],
-                         q + 2 <= n ? w[q + 2] : w[q + 1], q};
+                         q + 2 <= n ? w[q + 2] : w[q + 1], w[kWin + 1 + ql], w[2 * kWin + 1 + ql],
+                         w[kWin + 1 + qr], w[2 * kWin + 1 + qr], q};
         }
     }
     return c;
 }
 
-// Bracket of v for a site outside the cached bracket: a neighbour, or the
-// walk; -1 outside the window.
-__device__ __forceinline__ int window_near(const float* w, int n, const WinCache& c, float v) {
-    if (v <= c.hi2 && v > c.lo2) return v > c.hi ? c.q - 1 : c.q + 1;
-    return window_find(w, n, v);
-}
 
 // The line A + s x of a site beyond the window, from the whole table: its
 // bracket l (x[l-1] >= phibar + x > x[l]) by bisection, and the bracket's line
@@ -107,13 +104,19 @@ static __device__ __noinline__ float far_line(const PotDev& P, const double* y, 
 
 // potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop).
 // wb: {phibar, Fbar} of the kick window, for sites beyond it.
-// LIFT: every site searches the window branch-free (window_lift).
+// LIFT: a site beyond the three brackets searches the window branch-free
+// (window_lift), else by a walk (window_find).
 template <bool TABLE, bool LIFT = false>
 __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, const WinCache& c, float pn, float kv,
                                           bool& bad, const PotDev& P, const double* wb) {
     if (TABLE) {
-        if (!LIFT && x <= c.hi && x > c.lo) return pn * (c.A + c.s * x);
-        const int q = LIFT ? window_lift(wk, nk, x) : window_near(wk, nk, c, x);
+        if (x <= c.hi2 && x > c.lo2) {
+            // the background's bracket or a neighbour, chosen without a branch
+            const float A = x > c.hi ? c.Al : (x <= c.lo ? c.Ar : c.A);
+            const float sl = x > c.hi ? c.sl : (x <= c.lo ? c.sr : c.s);
+            return pn * (A + sl * x);
+        }
+        const int q = LIFT ? window_lift(wk, nk, x) : window_find(wk, nk, x);
         if (q < 0) return pn * far_line(P, P.dV, P.slopedV, wb, x, bad);
         return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
     }
@@ -126,8 +129,12 @@ template <bool TABLE, bool LIFT = false>
 __device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad,
                                          const PotDev& P, const double* wb) {
     if (TABLE) {
-        if (!LIFT && x <= c.hi && x > c.lo) return c.A + c.s * x;
-        const int q = LIFT ? window_lift(wv, nv, x) : window_near(wv, nv, c, x);
+        if (x <= c.hi2 && x > c.lo2) {
+            const float A = x > c.hi ? c.Al : (x <= c.lo ? c.Ar : c.A);
+            const float sl = x > c.hi ? c.sl : (x <= c.lo ? c.sr : c.s);
+            return A + sl * x;
+        }
+        const int q = LIFT ? window_lift(wv, nv, x) : window_find(wv, nv, x);
         if (q < 0) return far_line(P, P.V, P.slopeV, wb, x, bad);
         return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
     }
