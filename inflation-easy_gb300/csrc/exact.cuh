@@ -308,74 +308,6 @@ inline DivConst make_div_const(double y) {
     return D;
 }
 
-// ---------------------------------------------------------------------------
-// exact addition
-// ---------------------------------------------------------------------------
-
-__host__ __device__ __forceinline__ int clz64(unsigned long long x) {
-#ifdef __CUDA_ARCH__
-    return __clzll((long long)x);
-#else
-    return x ? __builtin_clzll(x) : 64;
-#endif
-}
-
-// RN(a + b) on the integer pipes, bit-equal to the IEEE sum: the larger
-// magnitude's significand with 10 guard bits, the other aligned to it with
-// the bits shifted out kept as a sticky bit, added or subtracted as 64-bit
-// integers, normalised and rounded to nearest, ties to even.  With two or
-// more guard bits a subtraction whose operands are two or more binades apart
-// normalises by at most one place, so the guard, round and sticky bits decide
-// the rounding as in the IEEE adder; operands closer than that are aligned
-// without loss.  Zero, subnormal, infinite and NaN operands, operands more
-// than 60 binades apart, and results that are subnormal or overflow take the
-// FP64 pipe; an exact cancellation gives +0, as IEEE round-to-nearest does.
-__host__ __device__ __forceinline__ double add_exact(double a, double b) {
-    unsigned long long ba = dbits(a), bb = dbits(b);
-    unsigned long long ma = ba & 0x7FFFFFFFFFFFFFFFull, mb = bb & 0x7FFFFFFFFFFFFFFFull;
-    if (mb > ma) {
-        const unsigned long long t = ba;
-        ba = bb;
-        bb = t;
-        const unsigned long long u = ma;
-        ma = mb;
-        mb = u;
-    }
-    const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
-    const int d = ea - eb;
-    if (ea == 0x7FF || eb == 0 || d > 60) return a + b;
-    const unsigned long long xa = ((ma & 0x000FFFFFFFFFFFFFull) | (1ull << 52)) << 10;   // bits 62..10
-    unsigned long long xb = ((mb & 0x000FFFFFFFFFFFFFull) | (1ull << 52)) << 10;
-    if (d) xb = (xb >> d) | (unsigned long long)((xb << (64 - d)) != 0);
-    int e = ea;
-    unsigned long long r;
-    if (!((ba ^ bb) >> 63)) {
-        r = xa + xb;   // < 2^64
-        if (r >> 63) {
-            r = (r >> 1) | (r & 1ull);
-            e += 1;
-        }
-    } else {
-        r = xa - xb;
-        if (r == 0) return 0.0;
-        const int lz = clz64(r) - 1;   // the leading bit to position 62
-        r <<= lz;
-        e -= lz;
-        if (e <= 0) return a + b;
-    }
-    unsigned long long M = r >> 10;   // 53 bits, the hidden bit at 52
-    const bool rb = ((r >> 9) & 1ull) != 0, st = (r & 0x1FFull) != 0;
-    if (rb && (st || (M & 1ull))) {
-        M += 1ull;
-        if (M >> 53) {
-            M >>= 1;
-            e += 1;
-        }
-    }
-    if (e >= 0x7FF) return a + b;
-    return bitsd((ba & 0x8000000000000000ull) | ((unsigned long long)e << 52) | (M & 0x000FFFFFFFFFFFFFull));
-}
-
 // RN(x / D.y), bit-equal to x / D.y for every x.
 __host__ __device__ __forceinline__ double div_exact(double x, const DivConst& D) {
     if (D.mode == 2) return x * D.inv;

@@ -8,8 +8,6 @@
 //                    binary); prints its bits in hex and the flags
 //   sumprod FILE     the exact sum of the products of the pairs of doubles in
 //                    FILE (x0 y0 x1 y1 ...); prints its bits and the flags
-//   add SEED COUNT   the integer-pipe addition against the IEEE sum for COUNT
-//                    random operand pairs; prints the mismatch count
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -77,59 +75,6 @@ static int check_sum(const char* path) {
     return 0;
 }
 
-static int check_add(unsigned long long seed, long count) {
-    long bad = 0;
-    auto one = [&](double x, double y) {
-        const double a = add_exact(x, y), b = x + y;
-        if (dbits(a) != dbits(b) && !((a != a) && (b != b))) {
-            if (bad < 10) std::printf("mismatch x=%a y=%a got %a want %a\n", x, y, a, b);
-            ++bad;
-        }
-    };
-    for (long i = 0; i < count; ++i) {
-        const unsigned long long r1 = splitmix(seed), r2 = splitmix(seed), r3 = splitmix(seed);
-        double x, y;
-        switch (i % 6) {
-            case 0: x = bitsd(r1); y = bitsd(r2); break;   // any bit patterns
-            case 1: {   // exponents within a few binades, either sign (cancellations, carries)
-                const unsigned long long e = 900 + r3 % 200;
-                x = bitsd((r1 & 0x800FFFFFFFFFFFFFull) | (e << 52));
-                y = bitsd((r2 & 0x800FFFFFFFFFFFFFull) | ((e + (r3 >> 32) % 5 - 2) << 52));
-                break;
-            }
-            case 2: {   // exponents up to 64 binades apart (alignment, sticky bits)
-                const unsigned long long e = 900 + r3 % 200;
-                x = bitsd((r1 & 0x800FFFFFFFFFFFFFull) | (e << 52));
-                y = bitsd((r2 & 0x800FFFFFFFFFFFFFull) | ((e - (r3 >> 32) % 65) << 52));
-                break;
-            }
-            case 3: {   // nearly equal magnitudes of opposite sign (massive cancellation)
-                x = bitsd(((r1 & 0x000FFFFFFFFFFFFFull) | (1000ull << 52)));
-                y = -bitsd(dbits(x) + (unsigned long long)(r2 % 64) - 32ull);
-                break;
-            }
-            case 4: {   // short significands: exact sums and ties
-                x = (double)((long long)(r1 % 2000001) - 1000000) * 0x1p-20;
-                y = (double)((long long)(r2 % 2000001) - 1000000) * 0x1p-73;
-                break;
-            }
-            default: {   // lattice-like values: a field and a small increment
-                x = 0.0935 + (double)(long long)(r1 % 2000001 - 1000000) * 1e-12;
-                y = (double)(long long)(r2 % 2000001 - 1000000) * 1e-15 * (double)(1 + r3 % 1000);
-                break;
-            }
-        }
-        one(x, y);
-        one(y, x);
-    }
-    const double edge[] = {0.0, -0.0, 1.0, -1.0, 0x1p-1022, -0x1p-1022, 0x1p-1074, 0x1.fffffffffffffp+1023,
-                           -0x1.fffffffffffffp+1023, 1e308, 3.0, -3.0, 0x1p-60, 1.0 + 0x1p-52};
-    for (double x : edge)
-        for (double y : edge) one(x, y);
-    std::printf("checked %ld mismatches %ld\n", 2 * count + 196, bad);
-    return bad ? 1 : 0;
-}
-
 static int check_sumprod(const char* path) {
     FILE* fp = std::fopen(path, "rb");
     if (!fp) return 2;
@@ -149,7 +94,6 @@ int main(int argc, char** argv) {
     if (argc >= 4 && !std::strcmp(argv[1], "div")) return check_div(std::strtoull(argv[2], 0, 10), std::atol(argv[3]));
     if (argc >= 3 && !std::strcmp(argv[1], "sum")) return check_sum(argv[2]);
     if (argc >= 3 && !std::strcmp(argv[1], "sumprod")) return check_sumprod(argv[2]);
-    if (argc >= 4 && !std::strcmp(argv[1], "add")) return check_add(std::strtoull(argv[2], 0, 10), std::atol(argv[3]));
-    std::fprintf(stderr, "usage: %s div SEED COUNT | sum FILE | sumprod FILE | add SEED COUNT\n", argv[0]);
+    std::fprintf(stderr, "usage: %s div SEED COUNT | sum FILE | sumprod FILE\n", argv[0]);
     return 2;
 }

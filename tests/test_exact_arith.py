@@ -6,9 +6,8 @@ point, rounded once) and the exact division by a fixed divisor (B^2).  Its
 host build (tests/native/exact_arith_check.cu, compiled with nvcc) is checked
 here: the division bit for bit against IEEE division over random dividends
 and divisors, the sum against Python's math.fsum (Shewchuk's correctly
-rounded sum) and the oracle's long accumulator, the sum of exact products
-against exact rational arithmetic, and the integer-pipe addition against
-IEEE addition.
+rounded sum) and the oracle's long accumulator, and the sum of exact
+products against exact rational arithmetic.
 """
 from __future__ import annotations
 
@@ -70,15 +69,6 @@ def test_exact_sum_is_the_correctly_rounded_sum(checker, tmp_path, oracle_mod):
         want = math.fsum(x)
         assert s == want, (s, want)
         assert oracle_mod.exact_sum(x) == want
-
-
-def test_addition_is_ieee(checker):
-    """The integer-pipe addition against the IEEE sum: random bit patterns,
-    nearby and distant exponents, massive cancellation, exact sums and ties,
-    lattice-like operands, and the special values."""
-    out = subprocess.run([str(checker), "add", "2024", "3000000"], capture_output=True, text=True)
-    assert out.returncode == 0, out.stdout
-    assert out.stdout.strip().endswith("mismatches 0"), out.stdout
 
 
 def test_exact_sum_of_products(checker, tmp_path, oracle_mod):
