@@ -60,19 +60,18 @@ struct WinCache {
     float hi, lo, A, s;   // bracket q: lo < v <= hi, value A + s v
     float hi2, lo2;       // u[q-1] and u[q+2] (hi and lo when there is no such neighbour)
     float Al, sl, Ar, sr; // lines of brackets q-1 and q+1 (q's own when there is no such neighbour)
-    int q;
 };
 
 template <bool TABLE>
 __device__ __forceinline__ WinCache win_cache(const float* w, int n) {
-    WinCache c{-1.f, 1.f, 0.f, 0.f, -1.f, 1.f, 0.f, 0.f, 0.f, 0.f, 0};   // empty interval
+    WinCache c{-1.f, 1.f, 0.f, 0.f, -1.f, 1.f, 0.f, 0.f, 0.f, 0.f};   // empty interval
     if (TABLE) {
         const int q = window_find(w, n, 0.f);
         if (q >= 0) {
             const int ql = q > 0 ? q - 1 : q, qr = q + 1 < n ? q + 1 : q;
             c = WinCache{w[q], w[q + 1], w[kWin + 1 + q], w[2 * kWin + 1 + q], q > 0 ? w[q - 1] : w[q],
                          q + 2 <= n ? w[q + 2] : w[q + 1], w[kWin + 1 + ql], w[2 * kWin + 1 + ql],
-                         w[kWin + 1 + qr], w[2 * kWin + 1 + qr], q};
+                         w[kWin + 1 + qr], w[2 * kWin + 1 + qr]};
         }
     }
     return c;
