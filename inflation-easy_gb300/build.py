@@ -37,6 +37,9 @@ UNITS = {
     "reduce_ops.cu": ["-fmad=false"],
     "ic.cu": ["-fmad=false"],
     "split_fp32.cu": [],
+    "split_rows4_128.cu": [],
+    "split_rows4_256.cu": [],
+    "split_rows4_512.cu": [],
     "ensemble.cu": [],
     "ensemble_dn.cu": ["-fmad=false"],
     "measure.cu": [],

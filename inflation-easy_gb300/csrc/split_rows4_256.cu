@@ -1,0 +1,17 @@
+// split_rows4_256.cu -- the split form's vector row kernel at N = 256: every
+// launch shape (one step per launch, and persistent) of both potentials.
+#include "split_rows4.cuh"
+
+namespace iegpu {
+
+void rows4_launch_256(iegpu_ctx* c, bool tab, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
+    if (tab) rows4_tj<true, 2>(c, B, K, grid, g);
+    else rows4_tj<false, 2>(c, B, K, grid, g);
+}
+
+int rows4_persist_256(iegpu_ctx* c, bool tab, int start, int nsteps, dim3 grid, const StepGeom& g, bool check_only) {
+    return tab ? persist_tj<true, 2>(c, start, nsteps, grid, g, check_only)
+               : persist_tj<false, 2>(c, start, nsteps, grid, g, check_only);
+}
+
+}  // namespace iegpu

@@ -103,13 +103,14 @@ def compare(ref_dir: Path, got_dir: Path) -> dict:
     g = _precise(Path(got_dir) / "dump" / "precise.txt")
     out: dict = {}
     assert len(r["means"]) == len(g["means"]), "different number of saves"
-    m_r, m_g = np.array(r["means"]), np.array(g["means"])
-    rel = np.abs(m_g / m_r - 1.0)
+    # columns that are 0 in the reference (the time of the first save) get
+    # the absolute deviation
+    rel = _bins(g["means"], r["means"])
     out["a_max"] = float(rel[:, 1].max())
     out["phibar_max"] = float(rel[:, 2].max())
     out["H_max"] = float(rel[:, 4].max())
     out["H_per_save"] = [float(x) for x in rel[:, 4]]
-    out["saves"] = int(len(m_r))
+    out["saves"] = int(rel.shape[0])
     out["P_dphi"] = _summary(_bins(g["spectrum"], r["spectrum"]))
     counts = _counts(Path(ref_dir) / "results" / "spectra.dat")
     var_r = np.array([np.sum(counts[1:] * x[1:len(counts)]) for x in r["spectrum"]])
