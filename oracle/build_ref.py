@@ -2,12 +2,15 @@
 
 TEST INFRASTRUCTURE ONLY.  The reference (caravangelo/inflation-easy) fixes N
 and its feature switches at compile time in src/parameters.h.  This recipe
-copies src/ of the read-only reference tree into a git-ignored build folder
-under oracle/_ref/<tag>/, sets the compile-time lines of parameters.h (the same
-regex patching the reference's own tests/regression_main_n16.py:71-76 does),
-and compiles it with g++ using the reference Makefile's flags plus
--ffp-contract=off (IEEE evaluation, so the x86 and Arm builds agree), linking
-oracle/ref_driver.cpp, which runs the unmodified main() and dumps state.
+compiles the .cpp files where they lie in the read-only reference tree.  Only
+parameters.h is patched, with the compile-time lines set (the same regex
+patching the reference's own tests/regression_main_n16.py:71-76 does).  The
+patched copy goes to a temporary folder beside symbolic links to the other
+source files; g++ compiles through the links, so a quoted include resolves in
+that folder and finds the patched header.  The build uses the reference Makefile's flags plus
+-ffp-contract=off (IEEE evaluation, so the x86 and Arm builds agree) and links
+oracle/ref_driver.cpp, which runs the unmodified main() and dumps state.  Only
+the binary is kept, in the git-ignored oracle/_ref/<tag>/.
 
 Nothing here is shipped or used by the product; only tests and the golden
 fixture generator call it, and only where the reference tree is present.
@@ -21,6 +24,7 @@ import os
 import re
 import shutil
 import subprocess
+import tempfile
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
@@ -46,14 +50,11 @@ def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8, post: i
     exe = out / "ie_ref"
     if exe.is_file():
         return exe
-    src = out / "src"
-    if src.exists():
-        shutil.rmtree(src)
-    src.mkdir(parents=True)
-    for p in (REF_ROOT / "src").iterdir():
-        shutil.copy(p, src / p.name)
-    ph = src / "parameters.h"
-    txt = ph.read_text()
+    ref_src = REF_ROOT / "src"
+    if (out / "src").exists():   # source copies left by an older version of this recipe
+        shutil.rmtree(out / "src")
+    out.mkdir(parents=True, exist_ok=True)
+    txt = (ref_src / "parameters.h").read_text()
     subs = [
         (r"#define numerical_potential \d+", f"#define numerical_potential {numerical}"),
         (r"#define perform_deltaN \d+", f"#define perform_deltaN {deltaN}"),
@@ -65,21 +66,29 @@ def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8, post: i
         txt, n = re.subn(pat, rep, txt, count=1)
         if n != 1:
             raise RuntimeError(f"could not patch {pat!r} in parameters.h")
-    ph.write_text(txt)
-    flags = ["-std=c++17", "-O3", "-DNDEBUG", "-ffp-contract=off", "-fopenmp", f"-I{src}"]
-    objs = []
-    procs = []
-    for cpp in sorted(src.glob("*.cpp")):
-        obj = out / (cpp.stem + ".o")
-        extra = ["-Dmain=ie_ref_main"] if cpp.name == "main.cpp" else []
-        procs.append(subprocess.Popen(["g++", *flags, *extra, "-c", str(cpp), "-o", str(obj)]))
-        objs.append(str(obj))
-    drv = out / "ref_driver.o"
-    procs.append(subprocess.Popen(["g++", *flags, "-c", str(HERE / "ref_driver.cpp"), "-o", str(drv)]))
-    objs.append(str(drv))
-    for p in procs:
-        if p.wait() != 0:
-            raise RuntimeError("reference compilation failed")
+    with tempfile.TemporaryDirectory(prefix="ie_ref_src_") as tmp:
+        lnk = Path(tmp)
+        for f in ref_src.iterdir():
+            if f.name != "parameters.h":
+                os.symlink(f, lnk / f.name)
+        (lnk / "parameters.h").write_text(txt)
+        flags = ["-std=c++17", "-O3", "-DNDEBUG", "-ffp-contract=off", "-fopenmp", f"-I{lnk}"]
+        objs = []
+        procs = []
+        for cpp in sorted(lnk.glob("*.cpp")):
+            obj = out / (cpp.stem + ".o")
+            extra = ["-Dmain=ie_ref_main"] if cpp.name == "main.cpp" else []
+            procs.append(subprocess.Popen(["g++", *flags, *extra, "-c", str(cpp), "-o", str(obj)],
+                                          stderr=subprocess.PIPE, text=True))
+            objs.append(str(obj))
+        drv = out / "ref_driver.o"
+        procs.append(subprocess.Popen(["g++", *flags, "-c", str(HERE / "ref_driver.cpp"), "-o", str(drv)],
+                                      stderr=subprocess.PIPE, text=True))
+        objs.append(str(drv))
+        errs = [(p, p.communicate()[1]) for p in procs]
+        bad = [e for p, e in errs if p.returncode != 0]
+        if bad:
+            raise RuntimeError("reference compilation failed:\n" + bad[0][-2000:])
     wrap = (["-Wl,--wrap=_Z4savei"] + (["-Wl,--wrap=_Z5saveNv"] if deltaN else []) +
             (["-Wl,--wrap=_Z19save_post_inflationi"] if post else []))
     subprocess.check_call(["g++", "-fopenmp", *wrap, *objs, "-o", str(exe), "-lm"])
