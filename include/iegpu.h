@@ -281,6 +281,18 @@ int  iegpu_numbins(int N);
  * src/output.cpp:63-151), inverse FFT.  counts[nbins] (exact integers) and
  * f2[nbins] = sum of weighted |X_k|^2 per bin (before /count and norm1). */
 int  iegpu_spectrum(struct iegpu_ctx* ctx, int field, int* counts, double* f2, int nbins);
+/* spectraf() with its forcing cutoff, src/output.cpp:297-406 (and
+ * spectraf_post_inflation, :1667-1770): forward FFT of f, the binning of
+ * iegpu_spectrum, then, when high_cutoff_index > 0, the k-space filter of
+ * :330-401 -- every mode of f and fd with |p| > high_cutoff_index or
+ * |p| < low_cutoff_index is zeroed (p the integer lattice momentum; fd is
+ * transformed forward and back; a low cutoff > 0 zeroes the k = 0 mode too)
+ * -- and the inverse FFT of f.  With high_cutoff_index <= 0 it is
+ * iegpu_spectrum(ctx, IEGPU_F, ...).  The reference runs it when
+ * forcing_cutoff is set.  Plain FP64 form only (IEGPU_EUNSUPPORTED on the
+ * split forms). */
+int  iegpu_spectrum_cutoff(struct iegpu_ctx* ctx, int* counts, double* f2, int nbins, double high_cutoff_index,
+                           double low_cutoff_index);
 /* spectraGW()/spectraGWdot() core, src/output.cpp:466-648: forward FFT of
  * the six h (which = 0) or h' (which = 1, scaled by to_phys), TT projection
  * per mode in float as the reference, binning (bins < floor(0.8*numbins)),

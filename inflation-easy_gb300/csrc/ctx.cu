@@ -756,6 +756,27 @@ int iegpu_spectrum(iegpu_ctx* c, int field, int* counts, double* f2, int nbins) 
     return rc;
 }
 
+int iegpu_spectrum_cutoff(iegpu_ctx* c, int* counts, double* f2, int nbins, double high_cutoff_index,
+                          double low_cutoff_index) {
+    if (!c || !counts || !f2) return IEGPU_EINVAL;
+    if (!(high_cutoff_index > 0)) return iegpu_spectrum(c, IEGPU_F, counts, f2, nbins);
+    if (is_split(c))
+        return set_error(c, IEGPU_EUNSUPPORTED, "the forcing cutoff is provided by the plain FP64 form");
+    if (nbins != iegpu_numbins(c->N)) return set_error(c, IEGPU_EINVAL, "nbins must be %d", iegpu_numbins(c->N));
+    double* x = dfield(c, IEGPU_F);
+    double* ny = dnyq(c, IEGPU_F);
+    double* xd = dfield(c, IEGPU_FD);
+    double* nyd = dnyq(c, IEGPU_FD);
+    int rc = fft_d(c, x, ny, 1);
+    if (!rc) rc = spectrum_bin_d(c, x, ny, counts, f2, nbins);
+    if (!rc) rc = fft_d(c, xd, nyd, 1);
+    if (!rc) rc = forcing_cutoff(c, x, ny, xd, nyd, high_cutoff_index, low_cutoff_index);
+    if (!rc) rc = fft_d(c, xd, nyd, -1);
+    if (!rc) rc = fft_d(c, x, ny, -1);
+    if (!rc) rc = sync_and_check(c, "spectrum with forcing cutoff");
+    return rc;
+}
+
 int iegpu_gw_spectrum(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins) {
     if (!c || !counts || !f2 || (which != 0 && which != 1)) return IEGPU_EINVAL;
     if (!c->cfg.sigw) return set_error(c, IEGPU_EUNSUPPORTED, "context was created without SIGW");

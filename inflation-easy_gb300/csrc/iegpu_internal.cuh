@@ -341,6 +341,8 @@ int fft_f(iegpu_ctx* c, float* f, float* fny, int forward);
 // spectra.cu
 int spectrum_bin_d(iegpu_ctx* c, const double* f, const double* fny, int* counts, double* f2, int nbins);
 int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins);
+// zeroes f's and fd's modes outside [low, high] (both in k-space), spectraf()'s forcing cutoff
+int forcing_cutoff(iegpu_ctx* c, double* f, double* fny, double* fd, double* fdny, double high, double low);
 // reduce.cu
 int field_means(iegpu_ctx* c, double out[3]);
 int field_sum(iegpu_ctx* c, int field, double* out);

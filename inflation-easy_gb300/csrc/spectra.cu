@@ -290,6 +290,58 @@ int spectrum_bin_d(iegpu_ctx* c, const double* f, const double* fny, int* counts
     return finish_bins(c, nbins, counts, f2);
 }
 
+// ---------------------------------------------------------------------------
+// The forcing cutoff of spectraf(), src/output.cpp:330-401 (the same block
+// closes spectraf_post_inflation, :1700-1765), on f and fd in k-space: every
+// mode whose lattice momentum has |p| = sqrt(px^2 + py^2 + pz^2) (exact
+// integers in double; IEEE square root) above high or below low is zeroed.
+// One thread per complex element (i, j, kz), kz = 0 .. N/2 (kz = N/2 is the
+// Nyquist plane ny[i][j]); each element is written by its own thread only.
+// Interior modes 0 < kz < N/2 are zeroed as (+0, +0).  On the kz = 0 and
+// Nyquist planes the reference walks one member of each conjugate pair
+// ((i, j) with j > N/2, or i > N/2 on the rows j = 0, N/2), zeroes it and
+// writes its partner (N - i, N - j) as the conjugate, so the partner holds
+// (+0, -0); the four self-conjugate points (i, j in {0, N/2}) are zeroed as
+// (+0, +0).  The partner's |p| equals the walked member's, so its thread
+// decides alone.  Nothing is read: the kernel writes the zeroed modes only.
+__global__ void k_forcing_cutoff(double2* __restrict__ f, double2* __restrict__ fny, double2* __restrict__ fd,
+                                 double2* __restrict__ fdny, int N, double high, double low) {
+    const int h = N >> 1;
+    const size_t n = (size_t)N * N * (h + 1);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int kz = (int)(t % (size_t)(h + 1));
+        const size_t ij = t / (size_t)(h + 1);
+        const int j = (int)(ij % (size_t)N), i = (int)(ij / (size_t)N);
+        const int px = i <= h ? i : i - N, py = j <= h ? j : j - N;
+        const double pd = sqrt((double)(px * px + py * py + kz * kz));
+        if (!(pd > high || pd < low)) continue;
+        const bool plane = kz == 0 || kz == h;
+        const bool walked = j > h || (i > h && (j == 0 || j == h));
+        const bool self = (i == 0 || i == h) && (j == 0 || j == h);
+        const double2 z = make_double2(0.0, (plane && !walked && !self) ? -0.0 : 0.0);
+        if (kz == h) {
+            fny[ij] = z;
+            fdny[ij] = z;
+        } else {
+            const size_t e = ij * (size_t)h + kz;
+            f[e] = z;
+            fd[e] = z;
+        }
+    }
+}
+
+int forcing_cutoff(iegpu_ctx* c, double* f, double* fny, double* fd, double* fdny, double high, double low) {
+    const int N = c->N;
+    const size_t n = (size_t)N * N * (N / 2 + 1);
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_forcing_cutoff<<<blocks, 256, 0, c->stream>>>(reinterpret_cast<double2*>(f), reinterpret_cast<double2*>(fny),
+                                                    reinterpret_cast<double2*>(fd), reinterpret_cast<double2*>(fdny),
+                                                    N, high, low);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "forcing cutoff") ? IEGPU_ECUDA : IEGPU_OK;
+}
+
 int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins) {
     const int N = c->N, M2 = N / 2;
     // kx table with the reference's float expression, src/output.cpp:493-495

@@ -362,7 +362,12 @@ void spectraf(int post = 0) {
     std::vector<int> counts(nb);
     std::vector<double> f2(nb);
     const double norm1 = std::pow(P.L / P.rescale_B, 3) / std::pow((double)P.N, 6);
-    ck(iegpu_spectrum(G, IEGPU_F, counts.data(), f2.data(), nb));
+    // with forcing_cutoff, f's and fd's modes outside [low, high] are zeroed
+    // after the binning (src/output.cpp:330-401)
+    if (P.forcing_cutoff && P.high_cutoff_index > 0)
+        ck(iegpu_spectrum_cutoff(G, counts.data(), f2.data(), nb, P.high_cutoff_index, P.low_cutoff_index));
+    else
+        ck(iegpu_spectrum(G, IEGPU_F, counts.data(), f2.data(), nb));
     print_spectrum(sp, counts, f2, norm1, post ? "post_spectrum" : "spectrum");
     std::fprintf(st, "%f %e\n", bg.t, bg.a);
     std::fflush(st);
@@ -822,7 +827,8 @@ int main(int argc, char** argv) {
     if (P.inflation_integrator != IE_LEAPFROG && P.form != 0)
         fatal("the %s inflation integrator runs on the plain FP64 form (form = fp64)\n",
               ie_integrator_name(P.inflation_integrator));
-    if (P.forcing_cutoff && P.high_cutoff_index > 0) fatal("forcing_cutoff is not provided by this engine.\n");
+    if (P.forcing_cutoff && P.high_cutoff_index > 0 && P.form != 0)
+        fatal("forcing_cutoff runs on the plain FP64 form (form = fp64)\n");
     if (P.post_inflation && !P.calculate_SIGW) fatal("post_inflation requires calculate_SIGW = 1\n");
     if (P.post_inflation && P.form != 0) fatal("the post-inflation phase runs on the plain FP64 form (form = fp64)\n");
     if (P.output_bispectrum || P.output_LOG)

@@ -107,6 +107,7 @@ def load() -> C.CDLL:
         "iegpu_fft": (I, [P, I, I]),
         "iegpu_numbins": (I, [I]),
         "iegpu_spectrum": (I, [P, I, ip, dp, I]),
+        "iegpu_spectrum_cutoff": (I, [P, ip, dp, I, D, D]),
         "iegpu_gw_spectrum": (I, [P, I, D, ip, dp, I]),
         "iegpu_initializeN": (I, [P, D]),
         "iegpu_get_phiref": (I, [P, dp]),
@@ -377,6 +378,17 @@ class Lattice:
         f2 = np.zeros(nb, dtype=np.float64)
         self._check(self.lib.iegpu_spectrum(self.h, field, counts.ctypes.data_as(C.POINTER(C.c_int)),
                                             f2.ctypes.data_as(C.POINTER(C.c_double)), nb))
+        return counts, f2
+
+    def spectrum_cutoff(self, high_cutoff: float, low_cutoff: float = 0.0):
+        """spectraf() with the forcing cutoff: f's spectrum, then f's and fd's
+        modes outside [low_cutoff, high_cutoff] zeroed (high_cutoff > 0)."""
+        nb = self.numbins()
+        counts = np.zeros(nb, dtype=np.int32)
+        f2 = np.zeros(nb, dtype=np.float64)
+        self._check(self.lib.iegpu_spectrum_cutoff(self.h, counts.ctypes.data_as(C.POINTER(C.c_int)),
+                                                   f2.ctypes.data_as(C.POINTER(C.c_double)), nb, high_cutoff,
+                                                   low_cutoff))
         return counts, f2
 
     def gw_spectrum(self, which: int, to_phys: float = 1.0):

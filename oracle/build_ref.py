@@ -48,7 +48,7 @@ def build(N: int, numerical: int, sigw: int, deltaN: int, jobs: int = 8, post: i
     tag = tag_for(N, numerical, sigw, deltaN, post)
     out = HERE / "_ref" / tag
     exe = out / "ie_ref"
-    if exe.is_file():
+    if exe.is_file() and exe.stat().st_mtime >= (HERE / "ref_driver.cpp").stat().st_mtime:
         return exe
     ref_src = REF_ROOT / "src"
     if (out / "src").exists():   # source copies left by an older version of this recipe

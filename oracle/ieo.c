@@ -1686,13 +1686,79 @@ void ieo_bin_spectrum(int N, const double* ff, const double* nyq, int* counts, d
     }
 }
 
-/* spectraf() without printing, src/output.cpp:297-406 (forcing cutoff off) */
-void ieo_spectrum_f(ieo_state* S, int* counts, double* f2) {
+/* Whether the mode of lattice momentum p (s = |p|^2, an exact integer in
+ * double) is outside [low, high]: sqrt(s) > high || sqrt(s) < low, the test
+ * of src/output.cpp:352-353. */
+static int mode_cut(double s, double high, double low) {
+    const double pd = sqrt(s);
+    return pd > high || pd < low;
+}
+
+static void zero_pair(double* a, double* b) { a[0] = 0.; a[1] = 0.; b[0] = 0.; b[1] = 0.; }
+
+/* The forcing cutoff of spectraf(), src/output.cpp:330-401 (the same block
+ * closes spectraf_post_inflation, :1700-1765), applied with f already in
+ * k-space: fd is transformed forward, every mode outside [low, high] is
+ * zeroed in f and fd, and fd is transformed back; f stays in k-space for the
+ * caller's inverse transform.  Modes 0 < kz < N/2 are tested one by one.  On
+ * the kz = 0 plane (f[(i N + j) N + 0, 1]) and the Nyquist plane (fny[i][2j,
+ * 2j + 1]) the reference walks one member of each conjugate pair (j > N/2,
+ * or i > N/2 on the rows j = 0 and j = N/2): it zeroes that member and writes
+ * its partner (N - i, N - j) as the conjugate, i.e. (+0, -0).  The four
+ * self-conjugate points (i, j in {0, N/2}) are zeroed alone.  The partner is
+ * never tested itself; its |p| is the walked member's. */
+void ieo_forcing_cutoff(ieo_state* S, double high, double low) {
+    const int N = S->p.N, h = N / 2;
+    double* f = S->f;
+    double* fd = S->fd;
+    double* fny = S->fny;
+    double* fdny = S->fdny;
+    ieo_fftrn_d(fd, fdny, N, 1);
+    for (int i = 0; i < N; ++i) {
+        const double px = (double)(i <= h ? i : i - N);
+        const int ic = i == 0 ? 0 : N - i;
+        for (int j = 0; j < N; ++j) {
+            const double py = (double)(j <= h ? j : j - N);
+            const size_t row = ((size_t)i * N + j) * N;
+            for (int k = 1; k < h; ++k)
+                if (mode_cut(px * px + py * py + (double)k * k, high, low))
+                    zero_pair(f + row + 2 * k, fd + row + 2 * k);
+            const int walked = j > h || (i > h && (j == 0 || j == h));
+            const int self = (i == 0 || i == h) && (j == 0 || j == h);
+            if (!walked && !self) continue;
+            const int jc = j == 0 ? 0 : N - j;
+            const size_t rowc = ((size_t)ic * N + jc) * N;
+            if (mode_cut(px * px + py * py, high, low)) {
+                zero_pair(f + row, fd + row);
+                if (walked) {
+                    f[rowc] = f[row]; f[rowc + 1] = -f[row + 1];
+                    fd[rowc] = fd[row]; fd[rowc + 1] = -fd[row + 1];
+                }
+            }
+            if (mode_cut(px * px + py * py + (double)h * h, high, low)) {
+                const size_t q = (size_t)i * 2 * N + 2 * j, qc = (size_t)ic * 2 * N + 2 * jc;
+                zero_pair(fny + q, fdny + q);
+                if (walked) {
+                    fny[qc] = fny[q]; fny[qc + 1] = -fny[q + 1];
+                    fdny[qc] = fdny[q]; fdny[qc + 1] = -fdny[q + 1];
+                }
+            }
+        }
+    }
+    ieo_fftrn_d(fd, fdny, N, -1);
+}
+
+/* spectraf() without printing, src/output.cpp:297-406: forward FFT of f,
+ * bin, the forcing cutoff when high > 0, inverse FFT of f. */
+void ieo_spectrum_f_cut(ieo_state* S, int* counts, double* f2, double high, double low) {
     const int N = S->p.N;
     ieo_fftrn_d(S->f, S->fny, N, 1);
     ieo_bin_spectrum(N, S->f, S->fny, counts, f2);
+    if (high > 0) ieo_forcing_cutoff(S, high, low);
     ieo_fftrn_d(S->f, S->fny, N, -1);
 }
+
+void ieo_spectrum_f(ieo_state* S, int* counts, double* f2) { ieo_spectrum_f_cut(S, counts, f2, 0.0, 0.0); }
 
 /* write_gw_spectrum_impl, src/output.cpp:466-625 (float arithmetic) */
 void ieo_gw_spectrum(ieo_state* S, int which, double to_phys, int* counts, float* f2, double* f2d) {
@@ -2280,11 +2346,8 @@ static int out_save(ieo_state* S, outfiles* O, int infrequent) {
             print_spectrum(sp, p->N, p->L, counts, f2, norm1, "spectrum");
             fprintf(st, "%f %e\n", S->t, S->a);
             fflush(st);
-            if (p->high_cutoff_index > 0 && p->forcing_cutoff) {
-                set_err(S, "forcing_cutoff is not supported by this oracle\n");
-                free(counts); free(f2);
-                return 1;
-            }
+            if (p->high_cutoff_index > 0 && p->forcing_cutoff)
+                ieo_forcing_cutoff(S, p->high_cutoff_index, p->low_cutoff_index);
             ieo_fftrn_d(S->f, S->fny, p->N, -1);
             free(counts); free(f2);
             if (p->calculate_SIGW) { out_gw(S, O, 0, 0); out_gw(S, O, 1, 0); }
@@ -2322,11 +2385,8 @@ static int out_save_post(ieo_state* S, outfiles* O, int infrequent) {
             print_spectrum(sp, p->N, p->L, counts, f2, norm1, "post_spectrum");
             fprintf(st, "%f %e\n", S->t, S->a);
             fflush(st);
-            if (p->high_cutoff_index > 0 && p->forcing_cutoff) {
-                set_err(S, "forcing_cutoff is not supported by this oracle\n");
-                free(counts); free(f2);
-                return 1;
-            }
+            if (p->high_cutoff_index > 0 && p->forcing_cutoff)
+                ieo_forcing_cutoff(S, p->high_cutoff_index, p->low_cutoff_index);
             ieo_fftrn_d(S->f, S->fny, p->N, -1);
             free(counts); free(f2);
             out_gw(S, O, 0, 1);

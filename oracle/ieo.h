@@ -167,6 +167,12 @@ void ieo_bin_spectrum(int N, const double* field_fft, const double* nyq, int* co
 /* spectraf(): forward FFT of f, bin, inverse FFT (f is modified in place at
  * round-off level, as in the reference). */
 void ieo_spectrum_f(ieo_state* S, int* counts, double* f2);
+/* The same with the forcing cutoff (src/output.cpp:330-401) applied to f and
+ * fd between the binning and the inverse FFT when high > 0: modes with
+ * |p| > high or |p| < low are zeroed. */
+void ieo_spectrum_f_cut(ieo_state* S, int* counts, double* f2, double high, double low);
+/* The cutoff alone, with f in k-space (fd is transformed forward and back). */
+void ieo_forcing_cutoff(ieo_state* S, double high, double low);
 /* GW TT spectrum, src/output.cpp:466-625.  mode: 0 = h, 1 = hd (DoubleThenFloat
  * scaling with to_phys).  f2_float gets the reference's float accumulators;
  * f2_double (may be NULL) gets the same per-mode float values summed in double. */

@@ -101,6 +101,7 @@ def load() -> C.CDLL:
         "ieo_numbins": (I, [I]),
         "ieo_bin_spectrum": (None, [I, dp, dp, ip, dp]),
         "ieo_spectrum_f": (None, [P, ip, dp]),
+        "ieo_spectrum_f_cut": (None, [P, ip, dp, D, D]),
         "ieo_gw_spectrum": (None, [P, I, D, ip, fp, dp]),
         "ieo_initializeN": (I, [P]), "ieo_evolve_derivsN": (I, [P, D]), "ieo_evolve_fieldsN": (None, [P, D]),
         "ieo_get_phiref": (D, [P]), "ieo_deltaN_steps": (I, [P, I]), "ieo_saveN_mean": (C.c_float, [P, D]),
@@ -315,12 +316,14 @@ class Oracle:
         return (self.lib.ieo_kin_energy(self.h), self.lib.ieo_gradient_energy(self.h),
                 self.lib.ieo_potential_energy(self.h))
 
-    def spectrum_f(self):
+    def spectrum_f(self, high_cutoff=0.0, low_cutoff=0.0):
+        """spectraf(): f's spectrum; with high_cutoff > 0 the forcing cutoff
+        also zeroes f's and fd's modes outside [low_cutoff, high_cutoff]."""
         nb = self.lib.ieo_numbins(self.N)
         counts = np.zeros(nb, dtype=np.int32)
         f2 = np.zeros(nb, dtype=np.float64)
-        self.lib.ieo_spectrum_f(self.h, counts.ctypes.data_as(C.POINTER(C.c_int)),
-                                f2.ctypes.data_as(C.POINTER(C.c_double)))
+        self.lib.ieo_spectrum_f_cut(self.h, counts.ctypes.data_as(C.POINTER(C.c_int)),
+                                    f2.ctypes.data_as(C.POINTER(C.c_double)), high_cutoff, low_cutoff)
         return counts, f2
 
     def gw_spectrum(self, which, to_phys=1.0):

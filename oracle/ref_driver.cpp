@@ -10,6 +10,15 @@
 //     at full precision each time the reference saves;
 //   * after the run the final lattice state is written in binary.
 // Usage: ie_ref <workdir>   (workdir holds params.txt and inputs/)
+//
+// A second mode runs the reference's spectraf() (src/output.cpp:297-406) once
+// on given fields, with the forcing cutoff on, to pin the mode filter of
+// :330-401 for any cutoffs (a low cutoff also zeroes the k = 0 mode, so a
+// whole run with one is no useful case):
+//   ie_ref --spectraf <workdir>
+// reads workdir/cut_in.bin (f, fd: N^3 doubles each; then high_cutoff_index,
+// low_cutoff_index), writes f and fd after the call to workdir/cut_out.bin;
+// the spectrum goes to workdir/results/spectra.dat as in a run.
 #include "main.h"
 
 #include <cstdio>
@@ -49,7 +58,35 @@ static void dump(FILE* fp, const std::vector<T>& v) {
     std::fwrite(v.data(), sizeof(T), v.size(), fp);
 }
 
+void spectraf();   // src/output.cpp:297 (not declared in src/main.h)
+
+static int run_spectraf() {
+    const size_t gs = (size_t)N * N * N;
+    f.assign(gs, 0.0);
+    fd.assign(gs, 0.0);
+    double cut[2];
+    FILE* in = std::fopen("cut_in.bin", "rb");
+    if (!in) return 2;
+    const bool ok = std::fread(f.data(), sizeof(double), gs, in) == gs &&
+                    std::fread(fd.data(), sizeof(double), gs, in) == gs && std::fread(cut, sizeof(double), 2, in) == 2;
+    std::fclose(in);
+    if (!ok) return 2;
+    high_cutoff_index = cut[0];
+    low_cutoff_index = cut[1];
+    forcing_cutoff = 1;
+    spectraf();
+    FILE* out = std::fopen("cut_out.bin", "wb");
+    dump(out, f);
+    dump(out, fd);
+    std::fclose(out);
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 3 && std::strcmp(argv[1], "--spectraf") == 0) {
+        if (chdir(argv[2]) != 0) return 2;
+        return run_spectraf();
+    }
     if (argc < 2 || chdir(argv[1]) != 0) {
         std::fprintf(stderr, "usage: ie_ref <workdir>\n");
         return 2;

@@ -6,6 +6,9 @@ sources by oracle/build_ref.py) on small lattices and stores, per case:
   <case>/trace.txt         background scalars at every save(), full precision
   <case>/state.npz         final f, fd, deltaN (and h, hd) in binary
   <case>/params.txt        the params file the reference read
+and, in forcing_cutoff/cut_n<N>.npz, the reference's spectraf() run once on
+seeded random f and fd with the forcing cutoff on (ie_ref --spectraf), for
+several (high_cutoff_index, low_cutoff_index) pairs: f and fd after the call.
 A post-inflation case keeps only results/post_inflation/ (its inflation and
 deltaN outputs are those of the case without the phase).  This script needs
 the reference tree, so it runs only where that exists; the fixtures it writes
@@ -49,7 +52,41 @@ CASES = {
                                               rk45_rel_tol=1e-10)),
     "n16_usr_sigw_post_rk45": (16, 1, 1, 1, 1, dict(USR, post_inflation_integrator="rk45")),
     "n16_usr_dn_rk45": (16, 1, 0, 1, 0, dict(USR, deltaN_integrator="rk45")),
+    # the forcing cutoff at every infrequent save (and the initial conditions' cutoff)
+    "n16_hilltop_cutoff": (16, 0, 0, 1, 0, dict(HILLTOP, high_cutoff_index=5.5, forcing_cutoff=1)),
 }
+
+# spectraf() alone: N -> (high_cutoff_index, low_cutoff_index) pairs.  |p| runs
+# up to 8 sqrt(3) = 13.9 at N = 16; a low cutoff > 0 also zeroes the k = 0
+# mode; high = N/2 keeps the on-axis Nyquist modes (|p| = N/2 is not > N/2).
+CUT_CASES = {
+    8: [(2.5, 0.0), (3.0, 1.0), (4.0, 0.0), (3.5, 1.5), (0.5, 0.0), (7.0, 0.0)],
+    16: [(5.5, 0.0), (6.0, 2.5)],
+}
+
+
+def make_cut_fixtures() -> None:
+    out = HERE / "forcing_cutoff"
+    out.mkdir(exist_ok=True)
+    for N, pairs in CUT_CASES.items():
+        exe = build_ref.build(N, 0, 0, 1)
+        rng = np.random.default_rng(1000 + N)
+        f = rng.standard_normal(N ** 3)
+        fd = rng.standard_normal(N ** 3)
+        res = {"f_in": f, "fd_in": fd, "cuts": np.array(pairs, dtype=np.float64)}
+        for q, (hi, lo) in enumerate(pairs):
+            work = ROOT / "oracle" / "_ref" / f"cut_n{N}_{q}"
+            if work.exists():
+                shutil.rmtree(work)
+            (work / "results").mkdir(parents=True)
+            with open(work / "cut_in.bin", "wb") as fp:
+                fp.write(f.tobytes()); fp.write(fd.tobytes()); fp.write(np.array([hi, lo]).tobytes())
+            subprocess.run([str(exe), "--spectraf", str(work)], check=True, stdout=subprocess.DEVNULL)
+            o = np.fromfile(work / "cut_out.bin", dtype=np.float64)
+            res[f"f_{q}"], res[f"fd_{q}"] = o[:N ** 3], o[N ** 3:]
+            shutil.rmtree(work)
+        np.savez_compressed(out / f"cut_n{N}.npz", **res)
+        print(f"forcing_cutoff/cut_n{N}", "ok")
 
 
 def params_text(p: dict) -> str:
@@ -79,6 +116,8 @@ def main() -> None:
     if not build_ref.ref_available():
         raise SystemExit("reference tree not available; fixtures are generated where it is")
     only = set(sys.argv[1:])
+    if not only or "forcing_cutoff" in only:
+        make_cut_fixtures()
     for name, (N, num, sigw, dn, post, p) in CASES.items():
         if only and name not in only:
             continue

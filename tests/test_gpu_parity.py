@@ -14,6 +14,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from conftest import GOLDEN
+
 pytestmark = pytest.mark.gpu
 
 
@@ -193,6 +195,44 @@ def test_spectrum_matches_oracle(N, engine, oracle_mod):
         assert np.allclose(f2, of2, rtol=1e-12, atol=0)
         # the in-place FFT round trip leaves the same bits as the reference's
         assert np.array_equal(lat.download(engine.F), o.f)
+
+
+def _bits(x):
+    return np.ascontiguousarray(x).view(np.uint64)
+
+
+@pytest.mark.parametrize("N", [16, 32, 64, 128])
+def test_spectrum_forcing_cutoff_matches_oracle(N, engine, oracle_mod):
+    """spectraf() with the forcing cutoff (src/output.cpp:330-401): counts
+    exact, bin sums 1e-12, and f and fd after the call bit for bit (signs of
+    zero included) with the oracle, for a high cutoff alone, one at N/2 (the
+    on-axis Nyquist modes stay), and high with low (the low one zeroes the
+    k = 0 mode as well)."""
+    for hi, lo in ((0.3 * N, 0.0), (N / 2, 0.0), (0.4 * N, 2.5)):
+        p, o = oracle_state(oracle_mod, N, False, False, None, steps=20)
+        lat, bg = lattice_like(engine, p, o, False, False, None)
+        with lat:
+            counts, f2 = lat.spectrum_cutoff(hi, lo)
+            oc, of2 = o.spectrum_f(hi, lo)
+            assert np.array_equal(counts, oc)
+            assert np.allclose(f2, of2, rtol=1e-12, atol=0)
+            assert np.array_equal(_bits(lat.download(engine.F)), _bits(o.f)), (N, hi, lo, "f")
+            assert np.array_equal(_bits(lat.download(engine.FD)), _bits(o.fd)), (N, hi, lo, "fd")
+
+
+@pytest.mark.parametrize("N", [8, 16])
+def test_spectrum_forcing_cutoff_matches_reference(N, engine):
+    """The same against the reference's own spectraf() on seeded random f and
+    fd (tests/golden/forcing_cutoff/, made by the reference program): f and fd
+    after the call bit for bit, for every cutoff pair of the fixture."""
+    g = np.load(GOLDEN / "forcing_cutoff" / f"cut_n{N}.npz")
+    for q, (hi, lo) in enumerate(g["cuts"]):
+        with engine.Lattice(N, 10.0, 1e-3, 3.338e-13) as lat:
+            lat.upload(engine.F, g["f_in"].copy())
+            lat.upload(engine.FD, g["fd_in"].copy())
+            lat.spectrum_cutoff(float(hi), float(lo))
+            assert np.array_equal(_bits(lat.download(engine.F)), _bits(g[f"f_{q}"])), (N, hi, lo, "f")
+            assert np.array_equal(_bits(lat.download(engine.FD)), _bits(g[f"fd_{q}"])), (N, hi, lo, "fd")
 
 
 def test_gw_spectrum_matches_oracle(engine, oracle_mod, tables):

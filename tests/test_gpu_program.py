@@ -33,6 +33,7 @@ CASES = {
     "n16_usr_sigw": (16, 1, 1),
     "n16_usr_dn_rk45": (16, 1, 0),   # deltaN_integrator = rk45
     "n32_hilltop": (32, 0, 0),
+    "n16_hilltop_cutoff": (16, 0, 0),   # forcing_cutoff = 1, high_cutoff_index = 5.5
 }
 
 # Bounds for the final f (ulp) and the background trace (relative).  With the

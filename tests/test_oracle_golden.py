@@ -22,6 +22,7 @@ CASES = {
     "n16_hilltop_rk45": (16, False, False, False),
     "n16_usr_sigw_post_rk45": (16, True, True, True),
     "n16_usr_dn_rk45": (16, True, False, False),
+    "n16_hilltop_cutoff": (16, False, False, False),   # forcing_cutoff = 1, high_cutoff_index = 5.5
 }
 
 
@@ -43,3 +44,19 @@ def test_oracle_reproduces_reference_outputs(case, oracle_mod, tmp_path):
     got = oracle_mod.read_state(tmp_path / "state.bin")
     for key in ref.files:
         assert np.array_equal(ref[key], got[key]), f"{case}: state {key} differs"
+
+
+@pytest.mark.parametrize("N", [8, 16])
+def test_oracle_forcing_cutoff_matches_reference(N, oracle_mod):
+    """spectraf() with the forcing cutoff (src/output.cpp:330-401) on seeded
+    random f and fd: the reference's f and fd after the call
+    (tests/golden/forcing_cutoff/, made by ie_ref --spectraf), bit for bit,
+    for high and low cutoffs (a low one zeroes the k = 0 mode too)."""
+    g = np.load(GOLDEN / "forcing_cutoff" / f"cut_n{N}.npz")
+    for q, (hi, lo) in enumerate(g["cuts"]):
+        o = oracle_mod.Oracle(oracle_mod.default_params(N, False))
+        o.f[:] = g["f_in"]
+        o.fd[:] = g["fd_in"]
+        o.spectrum_f(hi, lo)
+        assert np.array_equal(o.f.view(np.uint64), g[f"f_{q}"].view(np.uint64)), (N, hi, lo, "f")
+        assert np.array_equal(o.fd.view(np.uint64), g[f"fd_{q}"].view(np.uint64)), (N, hi, lo, "fd")
