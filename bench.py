@@ -405,6 +405,40 @@ def measure_ensemble(iegpu, steps, warmup, peak):
             "zeta_spectra_lattices": len(spectra)}
 
 
+def measure_batched_steps(iegpu, steps, warmup, shapes=None):
+    """The batched form's leapfrog steps alone (512 x 32^3 + 64 x 64^3 +
+    8 x 128^3, USR, per-size launches with the autotuned shapes): a short run
+    for profilers, without the deltaN stage or the comparisons.  shapes
+    ("N:rows:prefetch:chunks,..."): fixed launch shapes instead of the
+    autotuner's, whose trial timings mean nothing under a profiler."""
+    w = USR
+    Ns = [n for n, c in ENSEMBLE for _ in range(c)]
+    ens = iegpu.Ensemble(Ns, w["L"], w["dt"], w["V0"], potential=iegpu.POT_TABLE)
+    ens.set_table(*usr_tables())
+    hub = ens.bunch_davies(list(range(1, len(Ns) + 1)), w["phi0"], w["dphi0"])
+    bg = ens.bgs(hub)
+    ens.evolve_fields(0.5 * w["dt"], bg)
+    if shapes:
+        for t in shapes.split(","):
+            ens.set_shape(*(int(v) for v in t.split(":")))
+    ens.leapfrog(1e30, warmup, bg)   # without fixed shapes, the first call autotunes them
+    for b in range(len(Ns)):
+        bg[b].astep = bg[b].a
+    # the autotuner again on the warmed-up state, as measure_ensemble does (or the fixed shapes)
+    shape = ens.shapes() if shapes else ens.autotune(bg)
+    ens.leapfrog(1e30, warmup, bg)
+    for b in range(len(Ns)):
+        bg[b].astep = bg[b].a
+    ens.timer_start()
+    taken = ens.leapfrog(1e30, steps, bg)
+    ms = ens.timer_stop()
+    assert int(taken.min()) == steps
+    ens.close()
+    return {"ms_per_step": ms / steps, "site_updates_per_s": steps * sum(n ** 3 for n in Ns) / (ms * 1e-3),
+            "shapes": {str(n): [int(shape["rows"][Ns.index(n)]), int(shape["prefetch"][Ns.index(n)]),
+                                int(shape["chunks"][Ns.index(n)])] for n, _ in ENSEMBLE}}
+
+
 def measure_sigw(iegpu, N, steps, warmup, peak):
     """The split form with the SIGW tensor modes on (config: USR table
     potential, 6 h_ij components and their momenta in FP32): K steps, and one
@@ -592,6 +626,11 @@ def engine_arm(args):
         traffic = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
     except (OSError, ValueError):
         pass
+    if args.only == "batched":
+        r = measure_batched_steps(iegpu, args.steps, args.warmup, args.shapes)
+        if rank == 0:
+            print(json.dumps({"only": args.only, "steps": args.steps, "warmup": args.warmup, **r}), flush=True)
+        return 0
     if args.only in ("split", "split_comp", "sigw"):
         # one form's timed steps alone (a short run for profilers); no other forms, no CPU baseline
         if args.only == "sigw":
@@ -727,9 +766,12 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the whole-run error statements and 512^3")
     ap.add_argument("--headline-only", action="store_true",
                     help="time the plain FP64 step only and print a short line (for profiler runs)")
-    ap.add_argument("--only", choices=["split", "split_comp", "sigw"], default=None,
-                    help="time one other form alone at --n and print a short line (for profiler runs)")
+    ap.add_argument("--only", choices=["split", "split_comp", "sigw", "batched"], default=None,
+                    help="time one other form alone (at --n; batched: the ensemble's steps) and print a short line "
+                         "(for profiler runs)")
     ap.add_argument("--usr", action="store_true", help="with --only split|split_comp: the USR table potential")
+    ap.add_argument("--shapes", default=None,
+                    help="with --only batched: fixed launch shapes N:rows:prefetch:chunks,... (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()

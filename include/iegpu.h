@@ -400,6 +400,9 @@ int  iegpu_ens_profile(struct iegpu_ens* ens, int nsteps, iegpu_bg* bg, double* 
 int  iegpu_ens_autotune(struct iegpu_ens* ens, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks);
 /* Sets the launch shape of the lattices of size N, as iegpu_set_shape. */
 int  iegpu_ens_set_shape(struct iegpu_ens* ens, int N, int rows, int prefetch, int chunks);
+/* The current launch shape of each lattice (arrays of count, may be NULL),
+ * as iegpu_ens_autotune reports it, without tuning. */
+int  iegpu_ens_shapes(struct iegpu_ens* ens, int* rows, int* prefetch, int* chunks);
 /* No counterpart in the reference (it runs one lattice per process).  on = 1:
  * iegpu_ens_leapfrog advances every lattice in cooperative launches of up to
  * 64 steps each, the CTAs pulling (lattice, row tile, step) items of every

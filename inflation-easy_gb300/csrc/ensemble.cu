@@ -103,7 +103,7 @@ __global__ void __launch_bounds__((TJ + 2) * 32) k_ens_rows4(EnsArgs A, const in
 }
 
 template <bool TABLE, int N, int NT, int PF>
-__global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_ens_plane(EnsArgs A, const int2* __restrict__ work) {
+__global__ void __launch_bounds__(NT, plane_min_ctas(N)) k_ens_plane(EnsArgs A, const int2* __restrict__ work) {
     pdl_begin();
     const EnsTile t = ens_tile(A, work, N);
     plane_body<TABLE, N, NT, PF>(t.B, t.ctl, A.P, t.K, t.part, t.cnt, nullptr, t.i0, t.CH, t.slot, t.nslots, t.st);
@@ -270,7 +270,7 @@ static int ens_prime_slots(const iegpu_ens* e, int N) {
 // planes with PF = 2 or 4.
 static bool ens_plane(int N, int TJ) { return TJ == N && (N == 32 || N == 64); }
 static int ens_threads(int N, int TJ) {
-    return ens_plane(N, TJ) ? (N == 32 ? 256 : 512) : N >= 128 ? row4_threads(TJ) : (TJ + 1) * 32;
+    return ens_plane(N, TJ) ? plane_nt(N) : N >= 128 ? row4_threads(TJ) : (TJ + 1) * 32;
 }
 
 static size_t ens_smem(int N, int TJ, int PF) {
@@ -305,8 +305,8 @@ static int ens_launch_class(iegpu_ens* e, const EnsClass& c, const EnsArgs& A, c
         if (!set_attr) launch_pdl(KERNEL, dim3(grid), dim3(nthr), c.smem, st, A, (const int2*)c.work);     \
     } while (0)
     if (ens_plane(N, TJ)) {
-        if (N == 32) { if (PF == 4) IEGPU_ENS_PICK((k_ens_plane<TAB, 32, 256, 4>)); else IEGPU_ENS_PICK((k_ens_plane<TAB, 32, 256, 2>)); }
-        else { if (PF == 4) IEGPU_ENS_PICK((k_ens_plane<TAB, 64, 512, 4>)); else IEGPU_ENS_PICK((k_ens_plane<TAB, 64, 512, 2>)); }
+        if (N == 32) { if (PF == 4) IEGPU_ENS_PICK((k_ens_plane<TAB, 32, plane_nt(32), 4>)); else IEGPU_ENS_PICK((k_ens_plane<TAB, 32, plane_nt(32), 2>)); }
+        else { if (PF == 4) IEGPU_ENS_PICK((k_ens_plane<TAB, 64, plane_nt(64), 4>)); else IEGPU_ENS_PICK((k_ens_plane<TAB, 64, plane_nt(64), 2>)); }
     } else if (N == 32) {
         if (TJ == 4) { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows<TAB, 1, 4, 1>)); else IEGPU_ENS_PICK((k_ens_rows<TAB, 1, 4, 2>)); }
         else { if (PF == 1) IEGPU_ENS_PICK((k_ens_rows<TAB, 1, 8, 1>)); else IEGPU_ENS_PICK((k_ens_rows<TAB, 1, 8, 2>)); }
@@ -1051,6 +1051,17 @@ int iegpu_ens_profile(iegpu_ens* e, int nsteps, iegpu_bg* bg, double* ms_prime, 
     *ms_prime = ms[0];
     *ms_steps = ms[1];
     return rc;
+}
+
+int iegpu_ens_shapes(iegpu_ens* e, int* rows, int* prefetch, int* chunks) {
+    if (!e) return IEGPU_EINVAL;
+    for (int b = 0; b < e->count; ++b) {
+        const EnsClass& c = e->cls[(size_t)e->cls_of[(size_t)b]];
+        if (rows) rows[b] = c.TJ;
+        if (prefetch) prefetch[b] = c.PF;
+        if (chunks) chunks[b] = c.chunks;
+    }
+    return IEGPU_OK;
 }
 
 int iegpu_ens_autotune(iegpu_ens* e, const iegpu_bg* bg, int* rows, int* prefetch, int* chunks) {

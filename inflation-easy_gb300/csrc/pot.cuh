@@ -35,18 +35,23 @@ __device__ __forceinline__ bool is_nan_bits(double v) {
     return b > 0x7FF0000000000000LL;
 }
 
-// Bracket index and range flag (src/potential.cpp:19-38).
-__device__ __forceinline__ int table_bracket(const PotDev& P, double v, bool* out_of_range) {
+// Bracket index and range flag (src/potential.cpp:19-38), from the n
+// monotone keys of the descending nodes.
+__device__ __forceinline__ int table_bracket_keys(const long long* key, int n, double v, bool* out_of_range) {
     const long long kv = order_key(v);
     const bool nan = is_nan_bits(v);
-    *out_of_range = !nan && (kv > __ldg(&P.key[0]) || kv < __ldg(&P.key[P.n - 1]));
-    int lo = 0, hi = P.n - 1;
+    *out_of_range = !nan && (kv > __ldg(&key[0]) || kv < __ldg(&key[n - 1]));
+    int lo = 0, hi = n - 1;
     while (hi - lo > 1) {
         const int mid = lo + ((hi - lo) >> 1);
-        if (__ldg(&P.key[mid]) >= kv) lo = mid;
+        if (__ldg(&key[mid]) >= kv) lo = mid;
         else hi = mid;
     }
     return hi;
+}
+
+__device__ __forceinline__ int table_bracket(const PotDev& P, double v, bool* out_of_range) {
+    return table_bracket_keys(P.key, P.n, v, out_of_range);
 }
 
 // Hinted bracket for a slowly moving value (deltaN loop): walks from l.

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32) k_split_rows(SplitBufs B, Split
 
 // Whole planes (N = 32, 64): block y = chunk of planes.
 template <bool TABLE, int N, int NT, int PF>
-__global__ void __launch_bounds__(NT, N == 32 ? 4 : 1) k_split_plane(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
+__global__ void __launch_bounds__(NT, plane_min_ctas(N)) k_split_plane(SplitBufs B, SplitCtl* ctl, PotDev P, SplitConst K, double* part,
                                                     unsigned* counter, double* a_trace, int chunks) {
     pdl_begin();
     const int i0 = (int)(((long long)blockIdx.y * N) / chunks);
@@ -443,7 +443,7 @@ static int balanced_ctas(const iegpu_ctx* c, int N, int TJ, int PF);
 // Shared memory one row-kernel CTA needs, and how many fit on an SM.  TJ = N
 // (N <= 64) selects the whole-plane kernel.
 static bool plane_shape(int N, int TJ) { return TJ == N && (N == 32 || N == 64); }
-static int plane_threads(int N) { return N == 32 ? 256 : 512; }
+static int plane_threads(int N) { return plane_nt(N); }
 
 static size_t row_smem_bytes(int N, int TJ, int PF) {
     if (plane_shape(N, TJ)) return sizeof(float) * (size_t)split_plane_smem_floats(N, PF);
@@ -556,7 +556,7 @@ static void rows_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3
 
 template <bool TAB, int NV, int PFV>
 static void plane_one(iegpu_ctx* c, const SplitBufs& B, const SplitConst& K, dim3 grid, const StepGeom& g) {
-    constexpr int NT = NV == 32 ? 256 : 512;
+    constexpr int NT = plane_nt(NV);
     if (smem_optin((const void*)k_split_plane<TAB, NV, NT, PFV>, g.smem) != cudaSuccess) {
         set_error(c, IEGPU_ECUDA, "shared memory opt-in of the split step kernel failed");   // the launch then fails
     }

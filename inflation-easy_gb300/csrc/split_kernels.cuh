@@ -87,18 +87,29 @@ __device__ __forceinline__ WinCache win_cache(const float* w, int n) {
 // fraction of a bracket and this path is rare; where the table is dense
 // (the USR plateau of inputs/*.dat has brackets of 2.7e-6) the perturbations
 // span many brackets and more sites take it.  bad: beyond the table.
-static __device__ __noinline__ float far_line(const PotDev& P, const double* y, const double* slope,
-                                              const double* wb, float x, bool& bad) {
-    const double phibar = wb[0], Fbar = wb[1];
+// The out-of-line part takes plain pointers and returns its range flag, so
+// that a step loop calling it keeps the table descriptor and the flag in
+// registers (no address of either is taken).
+struct FarLine {
+    float v;
+    int oor;
+};
+
+static __device__ __noinline__ FarLine far_line_at(const long long* key, const double* xs, int n, const double* y,
+                                                   const double* slope, double phibar, double Fbar, float x) {
     bool oor;
-    const int l = table_bracket(P, phibar + (double)x, &oor);
-    if (oor) {
-        bad = true;
-        return 0.f;
-    }
+    const int l = table_bracket_keys(key, n, phibar + (double)x, &oor);
+    if (oor) return FarLine{0.f, 1};
     const double s = __ldg(&slope[l]);
-    const float A = (float)((__ldg(&y[l]) + (phibar - __ldg(&P.x[l])) * s) - Fbar);
-    return A + (float)s * x;
+    const float A = (float)((__ldg(&y[l]) + (phibar - __ldg(&xs[l])) * s) - Fbar);
+    return FarLine{A + (float)s * x, 0};
+}
+
+__device__ __forceinline__ float far_line(const PotDev& P, const double* y, const double* slope, const double* wb,
+                                          float x, bool& bad) {
+    const FarLine r = far_line_at(P.key, P.x, P.n, y, slope, wb[0], wb[1], x);
+    bad = bad || r.oor != 0;
+    return r.v;
 }
 
 // potnorm [V'(phibar + x) - V'(phibar)] / B^2 (table) or kv x (hilltop).
@@ -1578,6 +1589,13 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
 // the k +- 1 neighbours come by shuffles.  A plane of dphi and of dpi arrives
 // as one contiguous N^2-float cp.async copy, PF planes ahead; the new planes
 // are double-buffered (one barrier per plane), as in the vector row kernel.
+// Threads of a whole-plane CTA and the CTAs per SM its registers are sized
+// for: at N = 32, 128 threads with two vectors of each plane apiece and five
+// CTAs per SM (about 100 registers, so the window caches and sums stay in
+// registers); at N = 64, 512 threads and one CTA.
+__host__ __device__ constexpr int plane_nt(int N) { return N == 32 ? 128 : 512; }
+__host__ __device__ constexpr int plane_min_ctas(int N) { return N == 32 ? 5 : 1; }
+
 __host__ __device__ inline int split_plane_smem_floats(int N, int PF) {
     return ((3 + PF) + (1 + PF) + 2) * N * N + 2 * (3 * kWin + 1);
 }

@@ -137,6 +137,7 @@ def load() -> C.CDLL:
         "iegpu_ens_leapfrog": (I, [P, dp, I, P, ip]),
         "iegpu_ens_profile": (I, [P, I, P, dp, dp]),
         "iegpu_ens_autotune": (I, [P, P, ip, ip, ip]),
+        "iegpu_ens_shapes": (I, [P, ip, ip, ip]),
         "iegpu_ens_set_shape": (I, [P, I, I, I, I]),
         "iegpu_ens_set_persistent": (I, [P, I]),
         "iegpu_ens_timer_start": (I, [P]),
@@ -546,6 +547,12 @@ class Ensemble:
         """Per lattice: rows per tile (N: whole planes), planes prefetched, plane chunks."""
         r, p, ch = (np.zeros(self.count, dtype=np.int32) for _ in range(3))
         self._check(self.lib.iegpu_ens_autotune(self.h, bg, _ip(r), _ip(p), _ip(ch)))
+        return {"rows": r, "prefetch": p, "chunks": ch}
+
+    def shapes(self):
+        """The current launch shape of each lattice's size class, as autotune() returns it."""
+        r, p, ch = (np.zeros(self.count, dtype=np.int32) for _ in range(3))
+        self._check(self.lib.iegpu_ens_shapes(self.h, _ip(r), _ip(p), _ip(ch)))
         return {"rows": r, "prefetch": p, "chunks": ch}
 
     def set_shape(self, N: int, rows: int, prefetch: int, chunks: int) -> None:
