@@ -65,6 +65,10 @@ BYTES_STEP_FP64 = 32   # plain FP64 form: read f, fd; write f, fd
 # pipes; k_kick: six DMUL, four DADD; hilltop) and per deltaN site-step
 # (k_deltaN, hilltop, from ncu)
 FP64_INST_STEP = 17
+# FP64 thread instructions of one 3D FFT at 256^3, forward or inverse (ncu:
+# DADD + DMUL + DFMA of the three radix-2 passes and the row unpacking; each
+# butterfly is four DMUL and eight DADD in the reference's order)
+FFT_FP64_INST_256 = 1.3155e9
 DN_FP64_INST = 25
 BYTES_STEP_SIGW = 112  # split form with SIGW: 16 + read and write 6 h_ij and 6 h_ij' (FP32)
 BYTES_STEP_POST = 128  # post-inflation phase: read and write f, fd (FP64) and 6 h_ij, 6 h_ij' (FP32)
@@ -557,18 +561,25 @@ def measure_kernels(iegpu, N, fp64_rate, peak):
     # FFT forward + inverse (the spectrum's pair) and the binning
     lat.spectrum(iegpu.F)
     reps = 5
-    lat.timer_start()
+    ms_dir = {1: 0.0, -1: 0.0}
     for _ in range(reps):
-        lat.fft(iegpu.F, 1)
-        lat.fft(iegpu.F, -1)
-    ms_fft = lat.timer_stop() / (2 * reps)
+        for sgn in (1, -1):
+            lat.timer_start()
+            lat.fft(iegpu.F, sgn)
+            ms_dir[sgn] += lat.timer_stop() / reps
+    ms_fft = 0.5 * (ms_dir[1] + ms_dir[-1])
     t0 = time.perf_counter()
     for _ in range(reps):
         lat.spectrum(iegpu.F)
     ms_spec = 1e3 * (time.perf_counter() - t0) / reps
     gbs = 16 * N ** 3 / (ms_fft * 1e-3) / 1e9
-    out["fft"] = {"ms_per_transform": ms_fft, "algorithmic_bytes_per_site": 16, "achieved_gbs": gbs,
+    out["fft"] = {"ms_per_transform": ms_fft, "ms_forward": ms_dir[1], "ms_inverse": ms_dir[-1],
+                  "algorithmic_bytes_per_site": 16, "achieved_gbs": gbs,
                   "frac_of_measured_hbm": gbs / peak,
+                  "bound": "fp64" if N == 256 else None,
+                  "fp64_inst_per_transform": FFT_FP64_INST_256 if N == 256 else None,
+                  "fp64_frac_of_measured_rate": (FFT_FP64_INST_256 / (ms_fft * 1e-3) / fp64_rate
+                                                 if N == 256 and fp64_rate else None),
                   "spectrum_ms": ms_spec,
                   "note": "ffteasy-exact radix-2 passes in FP64; spectrum = forward FFT + binning + inverse FFT "
                           "(the reference's spectraf), wall clock with its read-back"}
@@ -626,6 +637,11 @@ def engine_arm(args):
         traffic = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())
     except (OSError, ValueError):
         pass
+    if args.only == "kernels":
+        r = measure_kernels(iegpu, N, iegpu.measure_fp64_rate(1), peak)
+        if rank == 0:
+            print(json.dumps({"only": args.only, "N": N, **r}), flush=True)
+        return 0
     if args.only == "batched":
         r = measure_batched_steps(iegpu, args.steps, args.warmup, args.shapes)
         if rank == 0:
@@ -766,7 +782,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the whole-run error statements and 512^3")
     ap.add_argument("--headline-only", action="store_true",
                     help="time the plain FP64 step only and print a short line (for profiler runs)")
-    ap.add_argument("--only", choices=["split", "split_comp", "sigw", "batched"], default=None,
+    ap.add_argument("--only", choices=["split", "split_comp", "sigw", "batched", "kernels"], default=None,
                     help="time one other form alone (at --n; batched: the ensemble's steps) and print a short line "
                          "(for profiler runs)")
     ap.add_argument("--usr", action="store_true", help="with --only split|split_comp: the USR table potential")

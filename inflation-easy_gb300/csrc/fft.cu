@@ -97,21 +97,25 @@ __global__ void __launch_bounds__(256) k_fft_pass(typename Cplx<T>::type* __rest
         }
         __syncthreads();
     }
-    // store (inverse: divide by the line length, src/ffteasy.hpp:64-69)
-    const T inv = (T)M;
+    // store (inverse: divide by the line length, src/ffteasy.hpp:64-69).  M is
+    // a power of two, so x / M and x * (1/M) are the same exact real number and
+    // both IEEE operations round it identically (subnormal results included):
+    // the multiplication by the exact reciprocal gives the division's bits
+    // without the division's FP64 iteration.
+    const T rinv = (T)1 / (T)M;
     if (g.kind == 0) {
         const long long base = l0 * M;
         for (int q = threadIdx.x; q < total; q += blockDim.x) {
             const int ll = q / M, e = q - ll * M;
             C2 v = sm[ll * ld + e];
-            if (inverse) { v.x /= inv; v.y /= inv; }
+            if (inverse) { v.x *= rinv; v.y *= rinv; }
             data[base + q] = v;
         }
     } else {
         for (int q = threadIdx.x; q < total; q += blockDim.x) {
             const int e = q / LPB, ll = q - e * LPB;
             C2 v = sm[ll * ld + e];
-            if (inverse) { v.x /= inv; v.y /= inv; }
+            if (inverse) { v.x *= rinv; v.y *= rinv; }
             data[line_base(g, l0 + ll) + (long long)e * g.stride] = v;
         }
     }
