@@ -13,70 +13,9 @@
 #include "iegpu_internal.cuh"
 #include "pot.cuh"
 #include "reduce.cuh"
+#include "split_window.cuh"
 
 namespace iegpu {
-
-// ---------------------------------------------------------------------------
-// windows of table brackets around a background value
-// ---------------------------------------------------------------------------
-
-// Bracket q of the window with u[q+1] < v <= u[q]; -1 outside the window.
-// The window is centred on the background value and a perturbation is a
-// small fraction of a bracket, so a walk from the middle bracket ends after
-// one or two compares (u descends strictly, so the bracket is unique).
-__device__ __forceinline__ int window_find(const float* u, int n, float v) {
-    if (!(v <= u[0] && v > u[n])) return -1;
-    int q = n >> 1;
-    while (v > u[q]) --q;
-    while (v <= u[q + 1]) ++q;
-    return q;
-}
-
-// The same bracket without branches, for lattices whose perturbations span
-// several brackets (512^3: 1 % of the sites lie beyond the background's
-// bracket and its neighbours, enough for divergent walks in a quarter of the
-// warps to cost more than the search): the brackets with
-// u[q] >= v form a prefix of the descending nodes (n + 1 of them, n <= kWin
-// < 32) and q is its last index, found by binary lifting over the node
-// indices with one shared-memory load per step.
-__device__ __forceinline__ int window_lift(const float* u, int n, float v) {
-    int q = 0;
-#pragma unroll
-    for (int st = 16; st > 0; st >>= 1) {
-        const int jn = q + st;
-        const float uj = u[jn < n ? jn : n];
-        q = (jn < n && uj >= v) ? jn : q;
-    }
-    return (v <= u[0] && v > u[n]) ? q : -1;
-}
-
-// The window's bracket of the background value (dphi = 0) and its two
-// neighbours, bounds and lines kept in registers.  Perturbations are a small
-// fraction of a bracket, so nearly every site falls in one of the three, which
-// is chosen by selects without a branch (a warp's lanes do not diverge when a
-// few of its sites lie in a neighbour).  Only a site beyond the neighbours
-// searches the window.  Any of these finds the same bracket, which is unique.
-struct WinCache {
-    float hi, lo, A, s;   // bracket q: lo < v <= hi, value A + s v
-    float hi2, lo2;       // u[q-1] and u[q+2] (hi and lo when there is no such neighbour)
-    float Al, sl, Ar, sr; // lines of brackets q-1 and q+1 (q's own when there is no such neighbour)
-};
-
-template <bool TABLE>
-__device__ __forceinline__ WinCache win_cache(const float* w, int n) {
-    WinCache c{-1.f, 1.f, 0.f, 0.f, -1.f, 1.f, 0.f, 0.f, 0.f, 0.f};   // empty interval
-    if (TABLE) {
-        const int q = window_find(w, n, 0.f);
-        if (q >= 0) {
-            const int ql = q > 0 ? q - 1 : q, qr = q + 1 < n ? q + 1 : q;
-            c = WinCache{w[q], w[q + 1], w[kWin + 1 + q], w[2 * kWin + 1 + q], q > 0 ? w[q - 1] : w[q],
-                         q + 2 <= n ? w[q + 2] : w[q + 1], w[kWin + 1 + ql], w[2 * kWin + 1 + ql],
-                         w[kWin + 1 + qr], w[2 * kWin + 1 + qr]};
-        }
-    }
-    return c;
-}
-
 
 // The line A + s x of a site beyond the window, from the whole table: its
 // bracket l (x[l-1] >= phibar + x > x[l]) by bisection, and the bracket's line
@@ -116,16 +55,13 @@ __device__ __forceinline__ float far_line(const PotDev& P, const double* y, cons
 // wb: {phibar, Fbar} of the kick window, for sites beyond it.
 // LIFT: a site beyond the three brackets searches the window branch-free
 // (window_lift), else by a walk (window_find).
-template <bool TABLE, bool LIFT = false>
+template <bool TABLE, bool LIFT = false, bool WIDE = false>
 __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, const WinCache& c, float pn, float kv,
                                           bool& bad, const PotDev& P, const double* wb) {
     if (TABLE) {
-        if (x <= c.hi2 && x > c.lo2) {
-            // the background's bracket or a neighbour, chosen without a branch
-            const float A = x > c.hi ? c.Al : (x <= c.lo ? c.Ar : c.A);
-            const float sl = x > c.hi ? c.sl : (x <= c.lo ? c.sr : c.s);
-            return pn * (A + sl * x);
-        }
+        float A, sl;
+        // the background's bracket or a neighbour, chosen without a branch
+        if (cache_line<WIDE>(c, x, A, sl)) return pn * (A + sl * x);
         const int q = LIFT ? window_lift(wk, nk, x) : window_find(wk, nk, x);
         if (q < 0) return pn * far_line(P, P.dV, P.slopedV, wb, x, bad);
         return pn * (wk[kWin + 1 + q] + wk[2 * kWin + 1 + q] * x);
@@ -135,15 +71,12 @@ __device__ __forceinline__ float split_dv(float x, const float* wk, int nk, cons
 
 // V(phibar + x) - V(phibar) in table units (table) or x^2 (hilltop).
 // wb: {phibar, Fbar} of the potential window, for sites beyond it.
-template <bool TABLE, bool LIFT = false>
+template <bool TABLE, bool LIFT = false, bool WIDE = false>
 __device__ __forceinline__ float split_v(float x, const float* wv, int nv, const WinCache& c, bool& bad,
                                          const PotDev& P, const double* wb) {
     if (TABLE) {
-        if (x <= c.hi2 && x > c.lo2) {
-            const float A = x > c.hi ? c.Al : (x <= c.lo ? c.Ar : c.A);
-            const float sl = x > c.hi ? c.sl : (x <= c.lo ? c.sr : c.s);
-            return A + sl * x;
-        }
+        float A, sl;
+        if (cache_line<WIDE>(c, x, A, sl)) return A + sl * x;
         const int q = LIFT ? window_lift(wv, nv, x) : window_find(wv, nv, x);
         if (q < 0) return far_line(P, P.V, P.slopeV, wb, x, bad);
         return wv[kWin + 1 + q] + wv[2 * kWin + 1 + q] * x;
@@ -1270,6 +1203,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                                            bool preissued = false, StepSeq sq = StepSeq()) {
     constexpr int N = 128 * C4, m = N - 1;
     constexpr bool kLift = C4 >= 4;   // 512^3: the branch-free window search
+    constexpr bool kWide = C4 >= 4;   // 512^3: five cached brackets
     constexpr int lgN = (C4 == 1) ? 7 : (C4 == 2) ? 8 : 9;
     constexpr int RP = (TJ + 3) * N, PP = (TJ + 1) * N, NBP = (TJ + 1) * N, NTH = (TJ + 1) * 32;
     constexpr int PHS = 3 + PF, PIS = 1 + PF;
@@ -1313,7 +1247,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     }
     const float d = cf[0], lap_n = cf[1], fric = cf[2], pn = cf[3], kv = cf[4];
     const int nk = nk_s, nv = nv_s;
-    const WinCache ck = win_cache<TABLE>(wk, nk), cv = win_cache<TABLE>(wv, nv);
+    const WinCache ck = win_cache<TABLE, kWide>(wk, nk), cv = win_cache<TABLE, kWide>(wv, nv);
 
     Kahan g, s1, s2;
     bool bad = false;
@@ -1507,10 +1441,10 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                 float4 pin, xn;
                 if (COMP) {
                     float4 cx = unpack_res4(rx[v]), cp = unpack_res4(rp[v]);
-                    pin.x = kahan_add(pi.x, d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE, kLift>(x.x, wk, nk, ck, pn, kv, bad, P, wbar)), cp.x);
-                    pin.y = kahan_add(pi.y, d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE, kLift>(x.y, wk, nk, ck, pn, kv, bad, P, wbar)), cp.y);
-                    pin.z = kahan_add(pi.z, d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE, kLift>(x.z, wk, nk, ck, pn, kv, bad, P, wbar)), cp.z);
-                    pin.w = kahan_add(pi.w, d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE, kLift>(x.w, wk, nk, ck, pn, kv, bad, P, wbar)), cp.w);
+                    pin.x = kahan_add(pi.x, d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE, kLift, kWide>(x.x, wk, nk, ck, pn, kv, bad, P, wbar)), cp.x);
+                    pin.y = kahan_add(pi.y, d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE, kLift, kWide>(x.y, wk, nk, ck, pn, kv, bad, P, wbar)), cp.y);
+                    pin.z = kahan_add(pi.z, d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE, kLift, kWide>(x.z, wk, nk, ck, pn, kv, bad, P, wbar)), cp.z);
+                    pin.w = kahan_add(pi.w, d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE, kLift, kWide>(x.w, wk, nk, ck, pn, kv, bad, P, wbar)), cp.w);
                     xn.x = kahan_add(x.x, d * pin.x, cx.x);
                     xn.y = kahan_add(x.y, d * pin.y, cx.y);
                     xn.z = kahan_add(x.z, d * pin.z, cx.z);
@@ -1520,10 +1454,10 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                         st_res4(B.pld + gb + k, cp);
                     }
                 } else {
-                    pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE, kLift>(x.x, wk, nk, ck, pn, kv, bad, P, wbar));
-                    pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE, kLift>(x.y, wk, nk, ck, pn, kv, bad, P, wbar));
-                    pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE, kLift>(x.z, wk, nk, ck, pn, kv, bad, P, wbar));
-                    pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE, kLift>(x.w, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.x = pi.x + d * (lap_n * lap.x - fric * pi.x - split_dv<TABLE, kLift, kWide>(x.x, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.y = pi.y + d * (lap_n * lap.y - fric * pi.y - split_dv<TABLE, kLift, kWide>(x.y, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.z = pi.z + d * (lap_n * lap.z - fric * pi.z - split_dv<TABLE, kLift, kWide>(x.z, wk, nk, ck, pn, kv, bad, P, wbar));
+                    pin.w = pi.w + d * (lap_n * lap.w - fric * pi.w - split_dv<TABLE, kLift, kWide>(x.w, wk, nk, ck, pn, kv, bad, P, wbar));
                     xn.x = x.x + d * pin.x;
                     xn.y = x.y + d * pin.y;
                     xn.z = x.z + d * pin.z;
@@ -1534,8 +1468,8 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
                     st4(B.xd + gb + k, xn);
                     st4(B.pd + gb + k, pin);
                     rs1 += (xn.x + xn.y) + (xn.z + xn.w);
-                    rs2 += (split_v<TABLE, kLift>(xn.x, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE, kLift>(xn.y, wv, nv, cv, bad, P, wbar + 2)) +
-                           (split_v<TABLE, kLift>(xn.z, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE, kLift>(xn.w, wv, nv, cv, bad, P, wbar + 2));
+                    rs2 += (split_v<TABLE, kLift, kWide>(xn.x, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE, kLift, kWide>(xn.y, wv, nv, cv, bad, P, wbar + 2)) +
+                           (split_v<TABLE, kLift, kWide>(xn.z, wv, nv, cv, bad, P, wbar + 2) + split_v<TABLE, kLift, kWide>(xn.w, wv, nv, cv, bad, P, wbar + 2));
                 }
                 xp2[v] = xp1[v];
                 xp1[v] = xn;
