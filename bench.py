@@ -639,6 +639,7 @@ def engine_arm(args):
         pass
     if args.only == "kernels":
         r = measure_kernels(iegpu, N, iegpu.measure_fp64_rate(1), peak)
+        r["post_inflation"] = measure_post_inflation(iegpu, N, 10, 3, peak)
         if rank == 0:
             print(json.dumps({"only": args.only, "N": N, **r}), flush=True)
         return 0

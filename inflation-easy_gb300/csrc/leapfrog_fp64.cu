@@ -994,38 +994,50 @@ struct RkH {
     float* hdo[6];
 };
 
-// Plain loads throughout: the RK4 update writes f, fd, h and hd in place, and
-// k_f, k_h of stage 0 are fd, hd themselves (each site is read by its own
-// thread before that thread writes it).
-template <bool SIGW>
+// y_out = y + h * sum_t c_t k_t over the NT nonzero coefficients of a stage
+// row, in stage order (the host drops the zero ones, which the reference's
+// loop skips too), each sum formed from 0.0 term by term as the reference
+// forms it.  Every load of a site is issued before its arithmetic; plain
+// loads throughout: the RK4 update writes f, fd, h and hd in place, and k_f,
+// k_h of stage 0 are fd, hd themselves (each site is read by its own thread
+// before that thread writes it).
+template <int NT, bool SIGW>
 __global__ void __launch_bounds__(kThreads) k_rk_combine(const double* f, const double* fd, double* fout,
                                                          double* fdout, RkRow R, RkH H, double h) {
     const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
+    double kf[NT > 0 ? NT : 1], kfd[NT > 0 ? NT : 1];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        kf[t] = R.kf[t][id];
+        kfd[t] = R.kfd[t][id];
+    }
+    const double f0 = f[id], fd0 = fd[id];
     double sum_f = 0.0, sum_fd = 0.0;
 #pragma unroll
-    for (int q = 0; q < kRkMax; ++q) {
-        if (q >= R.nq || R.c[q] == 0.0) continue;
-        sum_f += R.c[q] * R.kf[q][id];
-        sum_fd += R.c[q] * R.kfd[q][id];
+    for (int t = 0; t < NT; ++t) {
+        sum_f += R.c[t] * kf[t];
+        sum_fd += R.c[t] * kfd[t];
     }
-    const double fo = f[id] + h * sum_f;
-    const double fdo = fd[id] + h * sum_fd;
-    fout[id] = fo;
-    fdout[id] = fdo;
+    fout[id] = f0 + h * sum_f;
+    fdout[id] = fd0 + h * sum_fd;
     if (SIGW) {
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
+            float kh[NT > 0 ? NT : 1], khd[NT > 0 ? NT : 1];
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                kh[t] = R.kh[t][c][id];
+                khd[t] = R.khd[t][c][id];
+            }
+            const double hb = (double)H.hb[c][id], hdb = (double)H.hdb[c][id];
             double sum_h = 0.0, sum_hd = 0.0;
 #pragma unroll
-            for (int q = 0; q < kRkMax; ++q) {
-                if (q >= R.nq || R.c[q] == 0.0) continue;
-                sum_h += R.c[q] * (double)R.kh[q][c][id];
-                sum_hd += R.c[q] * (double)R.khd[q][c][id];
+            for (int t = 0; t < NT; ++t) {
+                sum_h += R.c[t] * (double)kh[t];
+                sum_hd += R.c[t] * (double)khd[t];
             }
-            const float ho = (float)((double)H.hb[c][id] + h * sum_h);
-            const float hdo = (float)((double)H.hdb[c][id] + h * sum_hd);
-            H.ho[c][id] = ho;
-            H.hdo[c][id] = hdo;
+            H.ho[c][id] = (float)(hb + h * sum_h);
+            H.hdo[c][id] = (float)(hdb + h * sum_hd);
         }
     }
 }
@@ -1246,20 +1258,31 @@ static int rk_rhs(iegpu_ctx* c, const RkEq& E, const double* fs, const double* f
     return IEGPU_OK;
 }
 
+template <int NT>
+static void rk_combine_launch(iegpu_ctx* c, unsigned grid, const double* f, const double* fd, double* fout,
+                              double* fdout, const RkRow& R, const RkH& H, double h) {
+    if (c->cfg.sigw) k_rk_combine<NT, true><<<grid, kThreads, 0, c->stream>>>(f, fd, fout, fdout, R, H, h);
+    else k_rk_combine<NT, false><<<grid, kThreads, 0, c->stream>>>(f, fd, fout, fdout, R, H, h);
+}
+
 static void rk_combine(iegpu_ctx* c, const RkBufs& B, const double* coef, int nq, const double* f, const double* fd,
                        double* fout, double* fdout, const float* const* hb, const float* const* hdb, float* const* hout,
                        float* const* hdout, double h) {
+    // the nonzero terms of the row, in stage order
     RkRow R{};
+    int nt = 0;
     for (int q = 0; q < nq; ++q) {
-        R.kf[q] = B.fd[q];
-        R.kfd[q] = B.kfd[q];
+        if (coef[q] == 0.0) continue;
+        R.kf[nt] = B.fd[q];
+        R.kfd[nt] = B.kfd[q];
         for (int k = 0; k < 6; ++k) {
-            R.kh[q][k] = B.hd[q][k];
-            R.khd[q][k] = B.khd[q][k];
+            R.kh[nt][k] = B.hd[q][k];
+            R.khd[nt][k] = B.khd[q][k];
         }
-        R.c[q] = coef[q];
+        R.c[nt] = coef[q];
+        ++nt;
     }
-    R.nq = nq;
+    R.nq = nt;
     RkH H{};
     for (int k = 0; k < 6 && c->cfg.sigw; ++k) {
         H.hb[k] = hb[k];
@@ -1268,8 +1291,17 @@ static void rk_combine(iegpu_ctx* c, const RkBufs& B, const double* coef, int nq
         H.hdo[k] = hdout[k];
     }
     const unsigned grid = (unsigned)(c->gs / kThreads);
-    if (c->cfg.sigw) k_rk_combine<true><<<grid, kThreads, 0, c->stream>>>(f, fd, fout, fdout, R, H, h);
-    else k_rk_combine<false><<<grid, kThreads, 0, c->stream>>>(f, fd, fout, fdout, R, H, h);
+    static_assert(kRkMax == 7, "one instance per term count 0..kRkMax");
+    switch (nt) {
+        case 0: rk_combine_launch<0>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        case 1: rk_combine_launch<1>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        case 2: rk_combine_launch<2>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        case 3: rk_combine_launch<3>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        case 4: rk_combine_launch<4>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        case 5: rk_combine_launch<5>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        case 6: rk_combine_launch<6>(c, grid, f, fd, fout, fdout, R, H, h); break;
+        default: rk_combine_launch<7>(c, grid, f, fd, fout, fdout, R, H, h); break;
+    }
     c->launches++;
 }
 
