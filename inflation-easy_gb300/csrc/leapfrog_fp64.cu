@@ -264,34 +264,46 @@ __global__ void __launch_bounds__(kThreads) k_kick(const double* __restrict__ fs
                                                    PotDev P, DevCtl* ctl, int lg, double half_over_dx) {
     const DevStep st = ctl->st;
     if (!st.active) return;
-    const long long id = (long long)blockIdx.x * kThreads + threadIdx.x;
-    const double fc = __ldg(&fs[id]);
-    const double L = __ldg(&lap[id]);
-    bool oor;
-    const double dv = dV_exact<TABLE>(P, fc, &oor);
-    if (TABLE && oor) flag_error(ctl, IEGPU_ERANGE, fc);
-    const double fdo = fd[id];
-    const double fdn = fdo + st.d * (st.laplnorm * L - st.friction * fdo - st.potnorm * dv);
-    fd[id] = fdn;
-    if (MODE == kModeLeapfrog) fdst[id] = fc + st.d * fdn;
-    if (SIGW) {
-        // dfdx<double>, src/evolution.cpp:55-77, and the six tensor updates
-        // of src/evolution.cpp:183-254 (float storage, double right-hand side).
-        const Nbr n = neighbours(id, lg);
-        const double gx = (__ldg(&fs[n.ip]) - __ldg(&fs[n.im])) * half_over_dx;
-        const double gy = (__ldg(&fs[n.jp]) - __ldg(&fs[n.jm])) * half_over_dx;
-        const double gz = (__ldg(&fs[n.kp]) - __ldg(&fs[n.km])) * half_over_dx;
-        const double T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+    // two consecutive sites per thread: 16-byte loads and stores, and the step
+    // coefficients read once for both
+    const long long id0 = 2 * ((long long)blockIdx.x * kThreads + threadIdx.x);
+    const double2 fc2 = __ldg(reinterpret_cast<const double2*>(fs + id0));
+    const double2 L2 = __ldg(reinterpret_cast<const double2*>(lap + id0));
+    const double2 fdo2 = *reinterpret_cast<const double2*>(fd + id0);
+    const double fcv[2] = {fc2.x, fc2.y}, Lv[2] = {L2.x, L2.y}, fdov[2] = {fdo2.x, fdo2.y};
+    double fdn[2], fnew[2];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const float* h = sg.hs[c];
-            const float hc = __ldg(&h[id]);
-            const float lf = lapl7(h, n, hc);
-            const float hdo = sg.hd[c][id];
-            const double rhs = st.d * (st.laplnorm * (double)lf - st.friction * (double)hdo + st.srcAmp * T[c]);
-            const float hdn = hdo + (float)rhs;
-            sg.hd[c][id] = hdn;
-            if (MODE == kModeLeapfrog) sg.hdst[c][id] = hc + (float)(st.d * (double)hdn);
+    for (int e = 0; e < 2; ++e) {
+        bool oor;
+        const double dv = dV_exact<TABLE>(P, fcv[e], &oor);
+        if (TABLE && oor) flag_error(ctl, IEGPU_ERANGE, fcv[e]);
+        fdn[e] = fdov[e] + st.d * (st.laplnorm * Lv[e] - st.friction * fdov[e] - st.potnorm * dv);
+        fnew[e] = fcv[e] + st.d * fdn[e];
+    }
+    *reinterpret_cast<double2*>(fd + id0) = make_double2(fdn[0], fdn[1]);
+    if (MODE == kModeLeapfrog) *reinterpret_cast<double2*>(fdst + id0) = make_double2(fnew[0], fnew[1]);
+    if (SIGW) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            // dfdx<double>, src/evolution.cpp:55-77, and the six tensor updates
+            // of src/evolution.cpp:183-254 (float storage, double right-hand side).
+            const long long id = id0 + e;
+            const Nbr n = neighbours(id, lg);
+            const double gx = (__ldg(&fs[n.ip]) - __ldg(&fs[n.im])) * half_over_dx;
+            const double gy = (__ldg(&fs[n.jp]) - __ldg(&fs[n.jm])) * half_over_dx;
+            const double gz = (__ldg(&fs[n.kp]) - __ldg(&fs[n.km])) * half_over_dx;
+            const double T[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const float* h = sg.hs[c];
+                const float hc = __ldg(&h[id]);
+                const float lf = lapl7(h, n, hc);
+                const float hdo = sg.hd[c][id];
+                const double rhs = st.d * (st.laplnorm * (double)lf - st.friction * (double)hdo + st.srcAmp * T[c]);
+                const float hdn = hdo + (float)rhs;
+                sg.hd[c][id] = hdn;
+                if (MODE == kModeLeapfrog) sg.hdst[c][id] = hc + (float)(st.d * (double)hdn);
+            }
         }
     }
 }
@@ -383,7 +395,7 @@ static void launch_reduce(iegpu_ctx* c, int src) {
 
 template <int MODE>
 static void launch_kick(iegpu_ctx* c, int src) {
-    const unsigned grid = (unsigned)(c->gs / kThreads);
+    const unsigned grid = (unsigned)(c->gs / (2 * kThreads));   // two sites per thread (gs >= 8^3)
     const SigwPtrs sg = sigw_ptrs(c, src);
     const double hodx = 0.5 / (c->cfg.L / (double)c->N);
     double* fdst = c->f[src ^ 1];
