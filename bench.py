@@ -69,6 +69,12 @@ FP64_INST_STEP = 17
 # DADD + DMUL + DFMA of the three radix-2 passes and the row unpacking; each
 # butterfly is four DMUL and eight DADD in the reference's order)
 FFT_FP64_INST_256 = 1.3155e9
+# FP64 thread instructions per site of one RK4 step (four k_rk_rhs at 20.1,
+# three one-term k_rk_combine at 8 and the final four-term one at 20) and of
+# one post-inflation step (k_post_kick 12, k_post_sigw 124, k_drift<SIGW> 8),
+# hilltop, from ncu (DADD + DMUL + DFMA; profiles/rk4_step_256.md)
+RK4_FP64_INST_SITE = 124.4
+POST_FP64_INST_SITE = 144.0
 DN_FP64_INST = 25
 BYTES_STEP_SIGW = 112  # split form with SIGW: 16 + read and write 6 h_ij and 6 h_ij' (FP32)
 BYTES_STEP_POST = 128  # post-inflation phase: read and write f, fd (FP64) and 6 h_ij, 6 h_ij' (FP32)
@@ -472,7 +478,7 @@ def measure_sigw(iegpu, N, steps, warmup, peak):
             "frac_of_measured_hbm": achieved / peak, "gw_spectrum_s": t_gw, "gw_bins": int((counts > 0).sum())}
 
 
-def measure_post_inflation(iegpu, N, steps, warmup, peak):
+def measure_post_inflation(iegpu, N, steps, warmup, peak, fp64_rate=None):
     """The post-inflation phase (radiation era, plain FP64 form, SIGW on): the
     hilltop lattice's device initial conditions turned into Phi by
     initialize_post_inflation (without deltaN), then K leapfrog steps of the
@@ -497,6 +503,9 @@ def measure_post_inflation(iegpu, N, steps, warmup, peak):
             "steps": steps, "ms_per_step": per_step, "site_updates_per_s": N ** 3 / (per_step * 1e-3),
             "algorithmic_bytes_per_site": BYTES_STEP_POST, "achieved_gbs": achieved,
             "frac_of_measured_hbm": achieved / peak,
+            "bound": "fp64", "fp64_inst_per_site": POST_FP64_INST_SITE,
+            "fp64_frac_of_measured_rate": (POST_FP64_INST_SITE * N ** 3 / (per_step * 1e-3) / fp64_rate
+                                           if fp64_rate else None),
             "note": "three kernels per step (fd kick, tensor kick with the 19-point Hessian source, drift), "
                     "FP64 per-site arithmetic in the reference's order"}
 
@@ -610,7 +619,10 @@ def measure_kernels(iegpu, N, fp64_rate, peak):
     ms_rk = lat.timer_stop() / nrk
     gbs = 336 * N ** 3 / (ms_rk * 1e-3) / 1e9
     out["rk4"] = {"ms_per_step": ms_rk, "site_updates_per_s": N ** 3 / (ms_rk * 1e-3),
-                  "algorithmic_bytes_per_site": 336, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+                  "algorithmic_bytes_per_site": 336, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak,
+                  "bound": "fp64", "fp64_inst_per_site": RK4_FP64_INST_SITE,
+                  "fp64_frac_of_measured_rate": (RK4_FP64_INST_SITE * N ** 3 / (ms_rk * 1e-3) / fp64_rate
+                                                 if fp64_rate else None)}
     lat.close()
     return out
 
@@ -638,8 +650,9 @@ def engine_arm(args):
     except (OSError, ValueError):
         pass
     if args.only == "kernels":
-        r = measure_kernels(iegpu, N, iegpu.measure_fp64_rate(1), peak)
-        r["post_inflation"] = measure_post_inflation(iegpu, N, 10, 3, peak)
+        rate = iegpu.measure_fp64_rate(1)
+        r = measure_kernels(iegpu, N, rate, peak)
+        r["post_inflation"] = measure_post_inflation(iegpu, N, 10, 3, peak, rate)
         if rank == 0:
             print(json.dumps({"only": args.only, "N": N, **r}), flush=True)
         return 0
@@ -697,7 +710,7 @@ def engine_arm(args):
     ens = measure_ensemble(iegpu, max(20, min(args.steps // 30, 500)), args.warmup, peak)
     sigw = measure_sigw(iegpu, N, max(10, min(args.steps // 75, 200)), args.warmup, peak)
     sigw512 = measure_sigw(iegpu, 512, 10, 3, peak) if not args.quick else None
-    post = measure_post_inflation(iegpu, N, max(10, min(args.steps // 300, 100)), args.warmup, peak)
+    post = measure_post_inflation(iegpu, N, max(10, min(args.steps // 300, 100)), args.warmup, peak, fp64_rate)
     kern = measure_kernels(iegpu, N, fp64_rate, peak)
 
     step_ms = fp["ms"] / args.steps
