@@ -72,7 +72,7 @@ FFT_FP64_INST_256 = 1.3155e9
 # FP64 thread instructions per site of one RK4 step (four k_rk_rhs at 20.1,
 # three one-term k_rk_combine at 8 and the final four-term one at 20) and of
 # one post-inflation step (k_post_kick 12, k_post_sigw 124, k_drift<SIGW> 8),
-# hilltop, from ncu (DADD + DMUL + DFMA; profiles/rk4_step_256.md)
+# hilltop, from ncu (DADD + DMUL + DFMA thread instructions of each kernel)
 RK4_FP64_INST_SITE = 124.4
 POST_FP64_INST_SITE = 144.0
 DN_FP64_INST = 25
