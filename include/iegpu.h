@@ -298,6 +298,15 @@ int  iegpu_spectrum_cutoff(struct iegpu_ctx* ctx, int* counts, double* f2, int n
  * per mode in float as the reference, binning (bins < floor(0.8*numbins)),
  * inverse FFT.  f2 accumulates the per-mode float values in double. */
 int  iegpu_gw_spectrum(struct iegpu_ctx* ctx, int which, double to_phys, int* counts, double* f2, int nbins);
+/* The same spectrum with the reference's own accumulators: f2[nbins] (float)
+ * is write_gw_spectrum_impl's f2 (src/output.cpp:478-612) before the
+ * division by the counts, i.e. the per-mode float values (2 fp2 for
+ * 0 < kz < N/2, fp2 on the kz = 0 and kz = N/2 planes) added in float in the
+ * reference's loop order (i, j, then kz); f2_sum (may be NULL) receives the
+ * same values added in double (in another order).  Given the same h, f2 is
+ * the reference's bit for bit. */
+int  iegpu_gw_spectrum_ref(struct iegpu_ctx* ctx, int which, double to_phys, int* counts, float* f2, double* f2_sum,
+                           int nbins);
 
 /* Allocation-free variant of the shell binning inside iegpu_spectrum, for
  * callers that cannot allocate device memory: a plugin whose host framework

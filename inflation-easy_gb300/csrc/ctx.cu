@@ -119,6 +119,7 @@ static void free_all(iegpu_ctx* c) {
     cudaFree(c->tab); cudaFree(c->tkey); cudaFree(c->tdiv);
     cudaFree(c->ctl); cudaFree(c->part); cudaFree(c->counter); cudaFree(c->a_trace);
     cudaFree(c->spec_part); cudaFree(c->spec_cnt); cudaFree(c->misc);
+    cudaFree(c->gw_pos); cudaFree(c->gw_start); cudaFree(c->gw_vals); cudaFree(c->gw_f2f); cudaFree(c->gw_f2d);
     if (c->ctl_h) cudaFreeHost(c->ctl_h);
     if (c->misc_h) cudaFreeHost(c->misc_h);
     for (int q = 0; q < 4; ++q)
@@ -774,6 +775,26 @@ int iegpu_spectrum_cutoff(iegpu_ctx* c, int* counts, double* f2, int nbins, doub
     if (!rc) rc = fft_d(c, xd, nyd, -1);
     if (!rc) rc = fft_d(c, x, ny, -1);
     if (!rc) rc = sync_and_check(c, "spectrum with forcing cutoff");
+    return rc;
+}
+
+int iegpu_gw_spectrum_ref(iegpu_ctx* c, int which, double to_phys, int* counts, float* f2, double* f2_sum,
+                          int nbins) {
+    if (!c || !counts || !f2 || (which != 0 && which != 1)) return IEGPU_EINVAL;
+    if (!c->cfg.sigw) return set_error(c, IEGPU_EUNSUPPORTED, "context was created without SIGW");
+    if (nbins != iegpu_numbins(c->N)) return set_error(c, IEGPU_EINVAL, "nbins must be %d", iegpu_numbins(c->N));
+    for (int q = 0; q < 6; ++q) {
+        float* x = which ? c->hd[q] : c->h[c->cur][q];
+        float* ny = which ? c->hdny[q] : c->hny[q];
+        if (int rc = fft_f(c, x, ny, 1)) return rc;
+    }
+    int rc = gw_bin_ref(c, which, to_phys, counts, f2, f2_sum, nbins);
+    for (int q = 0; q < 6 && !rc; ++q) {
+        float* x = which ? c->hd[q] : c->h[c->cur][q];
+        float* ny = which ? c->hdny[q] : c->hny[q];
+        rc = fft_f(c, x, ny, -1);
+    }
+    if (!rc) rc = sync_and_check(c, "gw spectrum");
     return rc;
 }
 

@@ -227,6 +227,13 @@ struct iegpu_ctx {
     double* a_trace = nullptr;
     int a_trace_cap = 0;
     double* spec_part = nullptr;       // spectrum partials [blocks][nbins]
+    // GW spectra in the reference's float accumulation order (built on first use)
+    int* gw_pos = nullptr;             // per mode slot: its place in the bin-major list, or -1
+    int* gw_start = nullptr;           // [nbins + 1] list offsets per bin
+    float* gw_vals = nullptr;          // per-mode values, bin-major, loop order within a bin
+    float* gw_f2f = nullptr;           // [nbins] float sums
+    double* gw_f2d = nullptr;          // [nbins] double sums
+    std::vector<int> gw_counts;        // the reference's numpoints per bin
     int* spec_cnt = nullptr;
     int spec_blocks = 0;
     double* misc = nullptr;            // small device scratch (sums, min/max)
@@ -341,6 +348,8 @@ int fft_f(iegpu_ctx* c, float* f, float* fny, int forward);
 // spectra.cu
 int spectrum_bin_d(iegpu_ctx* c, const double* f, const double* fny, int* counts, double* f2, int nbins);
 int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int nbins);
+// the same binning with the reference's float accumulators (and the same values summed in double)
+int gw_bin_ref(iegpu_ctx* c, int which, double to_phys, int* counts, float* f2, double* f2d, int nbins);
 // zeroes f's and fd's modes outside [low, high] (both in k-space), spectraf()'s forcing cutoff
 int forcing_cutoff(iegpu_ctx* c, double* f, double* fny, double* fd, double* fdny, double high, double low);
 // reduce.cu

@@ -370,6 +370,179 @@ int gw_bin(iegpu_ctx* c, int which, double to_phys, int* counts, double* f2, int
 }
 
 // ---------------------------------------------------------------------------
+// GW spectra with the reference's float accumulators
+// ---------------------------------------------------------------------------
+//
+// write_gw_spectrum_impl (src/output.cpp:478-612) adds each mode's float value
+// to a float accumulator of its bin, in its loop order: rows (i, j) in order,
+// in each row kz = 1 .. N/2-1 (2 fp2 each), then kz = 0 and kz = N/2 (fp2).
+// Mode slot (i N + j)(N/2 + 1) + t holds kz = t + 1 for t < N/2 - 1, kz = 0 for
+// t = N/2 - 1 and kz = N/2 for t = N/2.  The slots of each bin, in slot order,
+// form one list (a stable counting sort on the host, once per context):
+// k_gw_vals writes every mode's value to its place in its bin's list, and
+// k_gw_serial adds each list in order, one warp per bin, in float as the
+// reference does (and in double beside it, in another order).  Given the same
+// h, the float sums are the reference's bit for bit.
+
+__global__ void __launch_bounds__(kSpecThreads) k_gw_vals(GwArgs A, const int* __restrict__ pos,
+                                                         float* __restrict__ vals, int lgN) {
+    const int N = 1 << lgN, M2 = N >> 1, W = M2 + 1;
+    const long long S = (long long)N * N * W;
+    const float* ks = A.ksin + M2;
+    for (long long sl = (long long)blockIdx.x * blockDim.x + threadIdx.x; sl < S;
+         sl += (long long)gridDim.x * blockDim.x) {
+        const int at = pos[sl];
+        if (at < 0) continue;
+        const long long r = sl / W;
+        const int t = (int)(sl - r * W);
+        const int i = (int)(r >> lgN), j = (int)(r & (N - 1));
+        const int px = (i <= M2 ? i : i - N), py = (j <= M2 ? j : j - N);
+        const float kx = ks[px], ky = ks[py];
+        const bool interior = t < M2 - 1;
+        const int pz = interior ? t + 1 : (t == M2 - 1 ? 0 : M2);
+        const float kz = ks[pz];
+        const float kt2 = kx * kx + ky * ky + kz * kz;
+        float Cr[3][3], Ci[3][3];
+        if (interior) gw_load(A, false, r * M2 + pz, Cr, Ci);
+        else gw_load(A, pz != 0, pz ? r : r * M2, Cr, Ci);
+        const float fp2 = gw_tt(Cr, Ci, kx, ky, kz, kt2);
+        vals[at] = interior ? 2.f * fp2 : fp2;
+    }
+}
+
+// One warp per bin: the lanes load 128 values at a time (the next 128 while
+// the current ones are added), and every lane adds them in list order (the
+// shuffles broadcast them), so the float sum is one chain in the reference's
+// order.  The double sum (for full-precision output) is formed per chunk
+// across the lanes and off that chain: the same values, another order.
+__global__ void __launch_bounds__(32) k_gw_serial(const float* __restrict__ vals, const int* __restrict__ start,
+                                                  float* __restrict__ f2f, double* __restrict__ f2d) {
+    const int b = blockIdx.x, lane = threadIdx.x;
+    const int t0 = start[b], t1 = start[b + 1];
+    float sf = 0.f;
+    double sd = 0.0;
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int t = t0 + 4 * lane + q;
+        v[q] = t < t1 ? vals[t] : 0.f;
+    }
+    for (int base = t0; base < t1; base += 128) {
+        float vn[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int t = base + 128 + 4 * lane + q;
+            vn[q] = t < t1 ? vals[t] : 0.f;
+        }
+        const int n = t1 - base < 128 ? t1 - base : 128;
+        if (n == 128) {
+#pragma unroll
+            for (int l = 0; l < 32; ++l)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sf = __fadd_rn(sf, __shfl_sync(0xffffffffu, v[q], l));
+        } else {
+            for (int l = 0; l < 32; ++l)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float x = __shfl_sync(0xffffffffu, v[q], l);
+                    if (4 * l + q < n) sf = __fadd_rn(sf, x);
+                }
+        }
+        // lanes past the list hold 0, which adds nothing to the double sum
+        double d = ((double)v[0] + (double)v[1]) + ((double)v[2] + (double)v[3]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        sd += d;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = vn[q];
+    }
+    if (lane == 0) {
+        f2f[b] = sf;
+        f2d[b] = sd;
+    }
+}
+
+// The bin lists of the reference's loop order for this lattice size.
+static int gw_order_init(iegpu_ctx* c, int nbins) {
+    if (c->gw_pos) return IEGPU_OK;
+    const int N = c->N, M2 = N / 2, W = M2 + 1;
+    const int imax = (int)std::floor(0.80 * nbins);
+    const size_t S = (size_t)N * N * W;
+    std::vector<int> bin(S), cnt((size_t)nbins + 1, 0);
+    c->gw_counts.assign((size_t)nbins, 0);
+    for (int i = 0; i < N; ++i) {
+        const int px = i <= M2 ? i : i - N;
+        for (int j = 0; j < N; ++j) {
+            const int py = j <= M2 ? j : j - N;
+            const size_t row = ((size_t)i * N + j) * W;
+            for (int t = 0; t < W; ++t) {
+                const int pz = t < M2 - 1 ? t + 1 : (t == M2 - 1 ? 0 : M2);
+                const int sq = px * px + py * py + pz * pz;
+                // kt2 = 0 only at the k = 0 mode, which the reference skips
+                int b = sq == 0 ? -1 : (int)lroundf(std::sqrt((float)sq));
+                if (b >= imax) b = -1;
+                bin[row + t] = b;
+                if (b >= 0) {
+                    ++cnt[(size_t)b + 1];
+                    c->gw_counts[(size_t)b] += t < M2 - 1 ? 2 : 1;
+                }
+            }
+        }
+    }
+    for (int b = 0; b < nbins; ++b) cnt[(size_t)b + 1] += cnt[(size_t)b];
+    const std::vector<int> start(cnt);
+    std::vector<int> pos(S);
+    for (size_t sl = 0; sl < S; ++sl) pos[sl] = bin[sl] < 0 ? -1 : cnt[(size_t)bin[sl]]++;
+    const size_t total = (size_t)start[(size_t)nbins];
+    if (check_cuda(c, cudaMalloc(&c->gw_pos, sizeof(int) * S), "gw order") ||
+        check_cuda(c, cudaMalloc(&c->gw_start, sizeof(int) * start.size()), "gw order") ||
+        check_cuda(c, cudaMalloc(&c->gw_vals, sizeof(float) * (total > 0 ? total : 1)), "gw order") ||
+        check_cuda(c, cudaMalloc(&c->gw_f2f, sizeof(float) * nbins), "gw order") ||
+        check_cuda(c, cudaMalloc(&c->gw_f2d, sizeof(double) * nbins), "gw order") ||
+        check_cuda(c, cudaMemcpy(c->gw_pos, pos.data(), sizeof(int) * S, cudaMemcpyHostToDevice), "gw order") ||
+        check_cuda(c, cudaMemcpy(c->gw_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice),
+                   "gw order"))
+        return IEGPU_ENOMEM;
+    return IEGPU_OK;
+}
+
+int gw_bin_ref(iegpu_ctx* c, int which, double to_phys, int* counts, float* f2, double* f2d, int nbins) {
+    const int N = c->N, M2 = N / 2;
+    if (int rc = gw_order_init(c, nbins)) return rc;
+    const float pi_f = (float)(2.0 * std::asin(1.0));
+    const float dx_f = (float)(c->cfg.L / (double)N);
+    std::vector<float> ks((size_t)N + 1);
+    for (int p = -M2; p <= M2; ++p) ks[(size_t)(p + M2)] = (2.f / dx_f) * std::sin(pi_f * p / (float)N);
+    float* dks = reinterpret_cast<float*>(c->misc + 2 * (size_t)nbins + 8);
+    if (check_cuda(c, cudaMemcpyAsync(dks, ks.data(), sizeof(float) * ks.size(), cudaMemcpyHostToDevice, c->stream), "ksin"))
+        return IEGPU_ECUDA;
+    GwArgs A{};
+    for (int q = 0; q < 6; ++q) {
+        A.c[q] = reinterpret_cast<const float2*>(which ? c->hd[q] : c->h[c->cur][q]);
+        A.ny[q] = reinterpret_cast<const float2*>(which ? c->hdny[q] : c->hny[q]);
+    }
+    A.ksin = dks;
+    A.to_phys_d = to_phys;
+    A.scale = which ? 1 : 0;
+    A.imax = (int)std::floor(0.80 * nbins);
+    k_gw_vals<<<c->sms * 8, kSpecThreads, 0, c->stream>>>(A, c->gw_pos, c->gw_vals, c->lg);
+    k_gw_serial<<<nbins, 32, 0, c->stream>>>(c->gw_vals, c->gw_start, c->gw_f2f, c->gw_f2d);
+    c->launches += 2;
+    std::vector<double> hd((size_t)nbins);
+    if (check_cuda(c, cudaMemcpyAsync(f2, c->gw_f2f, sizeof(float) * nbins, cudaMemcpyDeviceToHost, c->stream),
+                   "gw spectrum download") ||
+        check_cuda(c, cudaMemcpyAsync(hd.data(), c->gw_f2d, sizeof(double) * nbins, cudaMemcpyDeviceToHost, c->stream),
+                   "gw spectrum download"))
+        return IEGPU_ECUDA;
+    if (sync_and_check(c, "gw spectrum")) return IEGPU_ECUDA;
+    for (int b = 0; b < nbins; ++b) {
+        counts[b] = c->gw_counts[(size_t)b];
+        if (f2d) f2d[b] = hd[(size_t)b];
+    }
+    return IEGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Allocation-free shell binning
 // ---------------------------------------------------------------------------
 //

@@ -374,7 +374,9 @@ void spectraf(int post = 0) {
 }
 
 // spectraGW / spectraGWdot, src/output.cpp:618-648: the per-bin sums come
-// back in double; division and normalisation are the reference's float ones.
+// back as the reference's own float accumulators (its loop order, bit for bit
+// given the same h); division and normalisation are the reference's float
+// ones.
 // Post (src/output.cpp:652-669): spectraGWdot_post_inflation multiplies h' in
 // float by (float)(B a^(s-1)); rounding (double)h' * (double)(float)(B a^(s-1))
 // to float gives the same bits, the double product of two floats being exact.
@@ -382,10 +384,11 @@ void spectra_gw(int which, int post = 0) {
     FILE* fp = out_file(which ? "spectraGWdot" : "spectraGW", post);
     const int nb = iegpu_numbins(P.N);
     std::vector<int> counts(nb);
-    std::vector<double> f2(nb);
+    std::vector<float> f2f(nb);   // the reference's float accumulators, its loop order
+    std::vector<double> f2(nb);   // the same values summed in double (full-precision dump)
     double to_phys = which ? P.rescale_B * std::pow(bg.a, P.rescale_s - 1.0) : 1.0;
     if (post && which) to_phys = (double)(float)to_phys;
-    ck(iegpu_gw_spectrum(G, which, to_phys, counts.data(), f2.data(), nb));
+    ck(iegpu_gw_spectrum_ref(G, which, to_phys, counts.data(), f2f.data(), f2.data(), nb));
     const int numbins = (int)(std::sqrt(3.0) * (P.N / 2)) + 1;
     if (g_prec) {
         const double n1 = 0.5 * std::pow(P.L / P.rescale_B, 3) / std::pow((double)P.N, 6);
@@ -397,7 +400,7 @@ void spectra_gw(int which, int post = 0) {
     const float dp = 2.f * (float)pi / (float)P.L;
     const float norm1 = 0.5f * std::pow(P.L / P.rescale_B, 3) / std::pow((float)P.N, 6);
     for (int i = 0; i < numbins; ++i) {
-        float v = (float)f2[i];
+        float v = f2f[i];
         if (counts[i] > 0) v /= (float)counts[i];
         std::fprintf(fp, "%e %d %e\n", dp * i, counts[i], norm1 * v);
     }

@@ -109,6 +109,7 @@ def load() -> C.CDLL:
         "iegpu_spectrum": (I, [P, I, ip, dp, I]),
         "iegpu_spectrum_cutoff": (I, [P, ip, dp, I, D, D]),
         "iegpu_gw_spectrum": (I, [P, I, D, ip, dp, I]),
+        "iegpu_gw_spectrum_ref": (I, [P, I, D, ip, C.POINTER(C.c_float), dp, I]),
         "iegpu_initializeN": (I, [P, D]),
         "iegpu_get_phiref": (I, [P, dp]),
         "iegpu_evolve_fieldsN": (I, [P, D, D]),
@@ -399,6 +400,18 @@ class Lattice:
         self._check(self.lib.iegpu_gw_spectrum(self.h, which, to_phys, counts.ctypes.data_as(C.POINTER(C.c_int)),
                                                f2.ctypes.data_as(C.POINTER(C.c_double)), nb))
         return counts, f2
+
+    def gw_spectrum_ref(self, which: int, to_phys: float = 1.0):
+        """(counts, f2 float32, f2 float64): the reference's float accumulators
+        (its loop order) and the same values summed in double (another order)."""
+        nb = self.numbins()
+        counts = np.zeros(nb, dtype=np.int32)
+        f2 = np.zeros(nb, dtype=np.float32)
+        f2d = np.zeros(nb, dtype=np.float64)
+        self._check(self.lib.iegpu_gw_spectrum_ref(self.h, which, to_phys, counts.ctypes.data_as(C.POINTER(C.c_int)),
+                                                   f2.ctypes.data_as(C.POINTER(C.c_float)),
+                                                   f2d.ctypes.data_as(C.POINTER(C.c_double)), nb))
+        return counts, f2, f2d
 
     # -- deltaN -----------------------------------------------------------
     def initializeN(self, a: float) -> None:

@@ -244,11 +244,43 @@ def test_gw_spectrum_matches_oracle(engine, oracle_mod, tables):
             oc, of2, of2d = o.gw_spectrum(which, tp)
             assert np.array_equal(counts, oc)
             assert np.allclose(f2, of2d, rtol=1e-12, atol=0)
-            # against the reference's float accumulators
+            # the tree-ordered double sums against the reference's float accumulators
             m = oc > 0
             assert np.allclose(f2[m], of2[m], rtol=1e-4)
+            # the reference's float accumulators themselves, in its loop order: bit for bit,
+            # and the same values summed in double (another order) to 1e-12
+            # (both sides' fields have been through one FFT round trip here)
+            rc, rf2, rf2d = lat.gw_spectrum_ref(which, tp)
+            oc, of2, of2d = o.gw_spectrum(which, tp)
+            assert np.array_equal(rc, oc)
+            assert np.array_equal(rf2.view(np.uint32), np.asarray(of2, dtype=np.float32).view(np.uint32))
+            assert np.allclose(rf2d, of2d, rtol=1e-12, atol=0)
         for c in range(6):
             assert np.array_equal(lat.download(engine.H(c)), o.h_(c))
+
+
+@pytest.mark.parametrize("N", [16, 32, 64])
+def test_gw_spectrum_reference_order_at_sizes(N, engine, oracle_mod, tables):
+    """The reference-order GW accumulators at several lattice sizes (random h
+    and h' uploaded to both): float sums bit for bit with the oracle's
+    write_gw_spectrum_impl, double sums to 1e-12, counts exact."""
+    rng = np.random.default_rng(N)
+    p = oracle_mod.usr_params(N, calculate_SIGW=1)
+    o = oracle_mod.Oracle(p, tables)
+    with engine.Lattice(N, p.L, p.dt, p.V0, sigw=True) as lat:
+        for c in range(6):
+            h = rng.standard_normal(N ** 3).astype(np.float32) * 1e-3
+            hd = rng.standard_normal(N ** 3).astype(np.float32) * 1e-3
+            o.h_(c)[:] = h
+            o.hd_(c)[:] = hd
+            lat.upload(engine.H(c), h.copy())
+            lat.upload(engine.HD(c), hd.copy())
+        for which, tp in ((0, 1.0), (1, 0.37)):
+            rc, rf2, rf2d = lat.gw_spectrum_ref(which, tp)
+            oc, of2, of2d = o.gw_spectrum(which, tp)
+            assert np.array_equal(rc, oc)
+            assert np.array_equal(rf2.view(np.uint32), np.asarray(of2, dtype=np.float32).view(np.uint32)), (N, which)
+            assert np.allclose(rf2d, of2d, rtol=1e-12, atol=0), (N, which)
 
 
 @pytest.mark.parametrize("usr", [False, True])

@@ -220,6 +220,22 @@ def test_program_full_precision_against_oracle(N, numerical, extra, tmp_path, or
         assert ca == cb
 
 
+def test_program_gw_spectra_byte_exact_with_engine_arithmetic(tmp_path, oracle_mod):
+    """spectraGW.dat and spectraGWdot.dat of the program (16^3 USR with SIGW,
+    inflation to af, deltaN stage) against the oracle program in
+    engine-arithmetic mode, byte for byte: h and h' are bit-exact there, and
+    the spectra use the reference's float accumulators in its loop order
+    (src/output.cpp:478-612), divided and normalised in float as it does."""
+    text = (GOLDEN / "n16_usr_sigw" / "params.txt").read_text()
+    wd = run_main(tmp_path, text, 16, 1, 1)
+    p = oracle_mod.params_from_text(text, 16, True, True)
+    d = tmp_path / "oracle_engine"
+    d.mkdir()
+    assert oracle_mod.run_program(p, d / "results", INPUTS, d, engine_arith=True) == 0
+    for name in ("spectraGW.dat", "spectraGWdot.dat"):
+        assert (wd / "results" / name).read_bytes() == (d / "results" / name).read_bytes(), name
+
+
 @pytest.mark.parametrize("case", ["n16_usr_sigw_post", "n16_usr_sigw_post_rk45"])
 def test_program_post_inflation_matches_reference_fixture(case, tmp_path):
     """The program with the post-inflation phase on (16^3, USR, SIGW, deltaN;
