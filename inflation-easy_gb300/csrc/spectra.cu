@@ -494,15 +494,31 @@ static int gw_order_init(iegpu_ctx* c, int nbins) {
     std::vector<int> pos(S);
     for (size_t sl = 0; sl < S; ++sl) pos[sl] = bin[sl] < 0 ? -1 : cnt[(size_t)bin[sl]]++;
     const size_t total = (size_t)start[(size_t)nbins];
-    if (check_cuda(c, cudaMalloc(&c->gw_pos, sizeof(int) * S), "gw order") ||
-        check_cuda(c, cudaMalloc(&c->gw_start, sizeof(int) * start.size()), "gw order") ||
-        check_cuda(c, cudaMalloc(&c->gw_vals, sizeof(float) * (total > 0 ? total : 1)), "gw order") ||
-        check_cuda(c, cudaMalloc(&c->gw_f2f, sizeof(float) * nbins), "gw order") ||
-        check_cuda(c, cudaMalloc(&c->gw_f2d, sizeof(double) * nbins), "gw order") ||
-        check_cuda(c, cudaMemcpy(c->gw_pos, pos.data(), sizeof(int) * S, cudaMemcpyHostToDevice), "gw order") ||
-        check_cuda(c, cudaMemcpy(c->gw_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice),
-                   "gw order"))
+    // published only when every buffer is in place (a failed call leaves none behind)
+    int *dpos = nullptr, *dstart = nullptr;
+    float *dvals = nullptr, *df2f = nullptr;
+    double* df2d = nullptr;
+    if (check_cuda(c, cudaMalloc(&dpos, sizeof(int) * S), "gw order") ||
+        check_cuda(c, cudaMalloc(&dstart, sizeof(int) * start.size()), "gw order") ||
+        check_cuda(c, cudaMalloc(&dvals, sizeof(float) * (total > 0 ? total : 1)), "gw order") ||
+        check_cuda(c, cudaMalloc(&df2f, sizeof(float) * nbins), "gw order") ||
+        check_cuda(c, cudaMalloc(&df2d, sizeof(double) * nbins), "gw order") ||
+        check_cuda(c, cudaMemcpy(dpos, pos.data(), sizeof(int) * S, cudaMemcpyHostToDevice), "gw order") ||
+        check_cuda(c, cudaMemcpy(dstart, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice),
+                   "gw order")) {
+        cudaFree(dpos);
+        cudaFree(dstart);
+        cudaFree(dvals);
+        cudaFree(df2f);
+        cudaFree(df2d);
+        c->gw_counts.clear();
         return IEGPU_ENOMEM;
+    }
+    c->gw_pos = dpos;
+    c->gw_start = dstart;
+    c->gw_vals = dvals;
+    c->gw_f2f = df2f;
+    c->gw_f2d = df2d;
     return IEGPU_OK;
 }
 
