@@ -81,3 +81,16 @@ def test_rk45_effective_without_a_device(engine):
     out = engine.Rk45Controls()
     assert lib.iegpu_rk45_effective(C.byref(ctl), -0.004, C.byref(out)) == 0
     assert (out.abs_tol, out.rel_tol, out.min_dt, out.max_dt, out.safety) == (1e-8, 2e-6, 0.004 * 1e-6, 0.004, 0.9)
+
+
+@pytest.mark.parametrize("form", ["split", "split_comp"])
+def test_forcing_cutoff_needs_the_fp64_form(form, tmp_path):
+    """forcing_cutoff with high_cutoff_index > 0 (src/output.cpp:330-401)
+    runs on the plain FP64 form; on the split forms the program stops with a
+    message before any device work."""
+    assert MAIN.exists(), "build the engine first (__graft_entry__.build())"
+    (tmp_path / "params.txt").write_text(f"N = 128\nnumerical_potential = 0\nform = {form}\nforcing_cutoff = 1\n"
+                                         "high_cutoff_index = 5.5\n")
+    r = subprocess.run([str(MAIN), "params.txt", "results", "dump"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1
+    assert "forcing_cutoff runs on the plain FP64 form" in r.stdout + r.stderr
