@@ -195,7 +195,9 @@ ROWCASE = {False: dict(L=10.0, dt=1e-3, V0=3.338e-13, ns=0.965, phi0=0.0935, dph
 
 
 @pytest.mark.parametrize("N,usr,shape", [(128, False, (16, 2, 0)), (128, True, (16, 3, 0)), (256, False, (16, 3, 9)),
-                                         (256, False, (4, 2, 7))])
+                                         (256, False, (4, 2, 7)),
+                                         # 512^3 with the table: the five-bracket window cache
+                                         (512, True, (8, 2, 0))])
 def test_split_row_kernel_matches_fp64(N, usr, shape, engine, tables):
     """The vector row kernel (N >= 128) against the plain FP64 form from the
     same device initial conditions, 300 steps.  With the hilltop potential the
