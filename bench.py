@@ -193,6 +193,31 @@ def cpu_baseline(N, threads, target_s=10.0):
                       f"serial energy sums as in the reference), {dt:.1f} s"}
 
 
+def cpu_usr_step_ms(N, tables, threads, target_s=1.0):
+    """ms per leapfrog step of one N^3 USR lattice in the oracle port of the
+    reference on the host cores (a bounded sample; CPU baseline of the batched
+    form)."""
+    import numpy as np
+
+    import ieo
+    p = ieo.usr_params(N, calculate_SIGW=0)
+    o = ieo.Oracle(p, tables, threads=threads)
+    rng = np.random.default_rng(2)
+    o.f[:] = USR["phi0"] + 1e-6 * rng.standard_normal(N ** 3)
+    o.fd[:] = USR["dphi0"] + 1e-6 * rng.standard_normal(N ** 3)
+    s = o.scalars
+    s.a, s.astep, s.ad = 1.0, 1.0, 1.0
+    o.set_scalars(s)
+    o.leapfrog_steps(1)
+    t0 = time.perf_counter()
+    o.leapfrog_steps(1)
+    t1 = time.perf_counter() - t0
+    steps = max(2, int(target_s / max(t1, 1e-4)))
+    t0 = time.perf_counter()
+    o.leapfrog_steps(steps)
+    return 1e3 * (time.perf_counter() - t0) / steps
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -390,6 +415,25 @@ def measure_ensemble(iegpu, steps, warmup, peak):
         seq[n] = lat.timer_stop() / steps
         lat.close()
     t_seq = sum(c * steps * seq[n] for n, c in ENSEMBLE)
+    # the same one lattice of each size in the plain FP64 form, and the oracle
+    # port of the reference on the host cores (a bounded CPU-baseline sample of
+    # a few steps per size)
+    seq64, cpu = {}, {}
+    for n, _ in ENSEMBLE:
+        lat = iegpu.Lattice(n, w["L"], w["dt"], w["V0"], potential=iegpu.POT_TABLE, form=iegpu.FORM_FP64)
+        lat.set_table(*tables)
+        H = lat.bunch_davies(1, w["phi0"], w["dphi0"])
+        b1 = iegpu.Bg(0.0, 1.0, H, 0.0, 1.0)
+        lat.evolve_fields(0.5 * w["dt"], b1)
+        lat.leapfrog(1e30, warmup, b1)
+        b1.astep = b1.a
+        lat.timer_start()
+        lat.leapfrog(1e30, steps, b1)
+        seq64[n] = lat.timer_stop() / steps
+        lat.close()
+        cpu[n] = cpu_usr_step_ms(n, tables, os.cpu_count() or 1)
+    t_seq64 = sum(c * steps * seq64[n] for n, c in ENSEMBLE)
+    t_cpu = sum(c * steps * cpu[n] for n, c in ENSEMBLE)
     # HBM figure from the timed region (the faster mode), 16 B per site-update
     achieved = BYTES_STEP_SPLIT * sites * steps / (ms * 1e-3) / 1e9
     mode_figs = {k: {"ms_per_step": v[0] / steps, "gpu_launches": v[1],
@@ -409,6 +453,11 @@ def measure_ensemble(iegpu, steps, warmup, peak):
             "sequential_ms_per_step": {str(n): seq[n] for n, _ in ENSEMBLE},
             "sequential_site_updates_per_s": steps * sites / (t_seq * 1e-3),
             "lattices_per_s_over_sequential": t_seq / ms,
+            "sequential_fp64_ms_per_step": {str(n): seq64[n] for n, _ in ENSEMBLE},
+            "lattices_per_s_over_sequential_fp64": t_seq64 / ms,
+            "cpu_oracle_ms_per_step": {str(n): cpu[n] for n, _ in ENSEMBLE},
+            "cpu_oracle_cores": os.cpu_count() or 1,
+            "lattices_per_s_over_cpu_oracle": t_cpu / ms,
             "deltaN_stage_s": t_dn, "zeta_spectra_s": t_sp,
             "zeta_sigma": {str(n): hists[n]["sigma"] for n, _ in ENSEMBLE},
             "zeta_outside_10sigma": {str(n): [int(x) for x in hists[n]["outside"]] for n, _ in ENSEMBLE},
