@@ -1292,7 +1292,7 @@ __device__ __forceinline__ bool rows4_body(const SplitBufs& B, SplitCtl* ctl, co
     for (long long u = rev ? u1 : u0; marcher && !aborted && (rev ? u > u0 : u < u1);) {
         // this march covers units [s, e) of one row tile
         const Row4March M = row4_march<N, TJ>(u, u0, u1, rev);
-        const int j0 = M.j0, i0 = M.i0, CH = M.CH;
+        const int j0 = M.j0, CH = M.CH;
         // march position q -> plane; q = -1 and q = CH are the halo planes
         auto plane = [&](int q) { return M.plane(q); };
         auto issue_phi = [&](int q) { row4_issue_phi<C4, TJ, PF>(ring, B.xs, M, q); };

@@ -34,7 +34,9 @@ __host__ __device__ __forceinline__ int window_find(const float* u, int n, float
 // indices with one shared-memory load per step.
 __host__ __device__ __forceinline__ int window_lift(const float* u, int n, float v) {
     int q = 0;
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
     for (int st = 16; st > 0; st >>= 1) {
         const int jn = q + st;
         const float uj = u[jn < n ? jn : n];
