@@ -369,6 +369,31 @@ def test_device_initial_conditions(N, usr, engine, oracle_mod, tables):
         assert abs(H - o.scalars.hubble_init) <= 1e-13 * H
 
 
+@pytest.mark.parametrize("hi,lo", [(5.5, 0.0), (6.0, 2.5)])
+def test_device_initial_conditions_with_mode_cutoffs(hi, lo, engine, oracle_mod):
+    """set_mode's cutoff (src/initialize.cpp:70): modes with |p| outside
+    [low_cutoff_index, high_cutoff_index] get no amplitude; the device draw
+    against the oracle's at 32^3, high cutoff alone and with a low one."""
+    N = 32
+    p = oracle_mod.hilltop_params(N, high_cutoff_index=hi, low_cutoff_index=lo)
+    o = oracle_mod.Oracle(p)
+    o.initialize_all()
+    with engine.Lattice(N, p.L, p.dt, p.V0, p.ns, p.rescale_B) as lat:
+        H = lat.bunch_davies(p.seed, p.initial_field, p.initial_derivative, hi, lo)
+        for fld, ref, base in ((engine.F, o.f, p.initial_field), (engine.FD, o.fd, p.initial_derivative)):
+            got = lat.download(fld)
+            tol = 1e-12 * np.std(ref) + 2 * np.spacing(abs(base))
+            assert np.max(np.abs(got - ref)) <= tol
+        assert abs(H - o.scalars.hubble_init) <= 1e-13 * H
+    # the cutoff removed power: the spectrum past the high cutoff is empty
+    f = o.f.reshape(N, N, N) - o.f.mean()
+    X = np.fft.rfftn(f)
+    px = np.fft.fftfreq(N, 1.0 / N)
+    pz = np.fft.rfftfreq(N, 1.0 / N)
+    k = np.sqrt(px[:, None, None] ** 2 + px[None, :, None] ** 2 + pz[None, None, :] ** 2)
+    assert np.max(np.abs(X[k > hi + 1])) <= 1e-9 * np.max(np.abs(X))
+
+
 def test_device_initial_conditions_seed_semantics(engine, oracle_mod):
     N = 8
     for seed in (0, 1, 12345):
