@@ -49,6 +49,19 @@ __device__ __forceinline__ long long line_base(const PassGeom& g, long long l) {
 
 __device__ __forceinline__ int bitrev(int x, int lg) { return (int)(__brev((unsigned)x) >> (32 - lg)); }
 
+// One Danielson-Lanczos butterfly, src/ffteasy.hpp:46-58, in the reference's
+// expression order (this file is compiled with -fmad=false).
+template <typename C2>
+__device__ __forceinline__ void butterfly(C2& t1, C2& t2, C2 wb) {
+    C2 o1, o2;
+    o1.x = t1.x + wb.x * t2.x - wb.y * t2.y;
+    o1.y = t1.y + wb.x * t2.y + wb.y * t2.x;
+    o2.x = t1.x - wb.x * t2.x + wb.y * t2.y;
+    o2.y = t1.y - wb.x * t2.y - wb.y * t2.x;
+    t1 = o1;
+    t2 = o2;
+}
+
 // One 1D complex FFT pass over LPB lines per CTA (fftc1, src/ffteasy.hpp:21-70).
 template <typename T>
 __global__ void __launch_bounds__(256) k_fft_pass(typename Cplx<T>::type* __restrict__ data,
@@ -75,9 +88,37 @@ __global__ void __launch_bounds__(256) k_fft_pass(typename Cplx<T>::type* __rest
         }
     }
     __syncthreads();
-    // Danielson-Lanczos stages
-    const int half_lines = M >> 1;
-    for (int s = 1; s <= lgM; ++s) {
+    // Danielson-Lanczos stages, two per pass through shared memory: stages s
+    // and s + 1 (half h = 2^(s-1)) touch the elements e, e + h, e + 2h, e + 3h
+    // of a block of 4h only among themselves, so one thread runs the four
+    // butterflies of such a group in registers (stage s: (e, e+h) and
+    // (e+2h, e+3h) with w_s[b]; stage s + 1: (e, e+2h) with w_{s+1}[b] and
+    // (e+h, e+3h) with w_{s+1}[b+h]).  Each butterfly is the reference's, on the
+    // same operands, so the bits do not change; an odd last stage runs alone.
+    const int half_lines = M >> 1, quarter_lines = M >> 2;
+    int s = 1;
+    for (; s + 1 <= lgM; s += 2) {
+        const int h = 1 << (s - 1);
+        const C2* w1 = tw + (h - 1);
+        const C2* w2 = tw + (2 * h - 1);
+        for (int q = threadIdx.x; q < LPB * quarter_lines; q += blockDim.x) {
+            const int ll = q / quarter_lines, r = q - ll * quarter_lines;
+            const int blk = r >> (s - 1), b = r & (h - 1);
+            const int e = blk * (h << 2) + b;
+            C2* line = sm + ll * ld;
+            C2 x0 = line[e], x1 = line[e + h], x2 = line[e + 2 * h], x3 = line[e + 3 * h];
+            butterfly(x0, x1, w1[b]);
+            butterfly(x2, x3, w1[b]);
+            butterfly(x0, x2, w2[b]);
+            butterfly(x1, x3, w2[b + h]);
+            line[e] = x0;
+            line[e + h] = x1;
+            line[e + 2 * h] = x2;
+            line[e + 3 * h] = x3;
+        }
+        __syncthreads();
+    }
+    if (s == lgM) {
         const int half = 1 << (s - 1);
         const C2* w = tw + (half - 1);
         for (int q = threadIdx.x; q < LPB * half_lines; q += blockDim.x) {
@@ -85,15 +126,10 @@ __global__ void __launch_bounds__(256) k_fft_pass(typename Cplx<T>::type* __rest
             const int trans = r >> (s - 1), b = r & (half - 1);
             const int i1 = trans * (half << 1) + b, i2 = i1 + half;
             C2* line = sm + ll * ld;
-            const C2 t1 = line[i1], t2 = line[i2];
-            const C2 wb = w[b];
-            C2 o1, o2;
-            o1.x = t1.x + wb.x * t2.x - wb.y * t2.y;
-            o1.y = t1.y + wb.x * t2.y + wb.y * t2.x;
-            o2.x = t1.x - wb.x * t2.x + wb.y * t2.y;
-            o2.y = t1.y - wb.x * t2.y - wb.y * t2.x;
-            line[i1] = o1;
-            line[i2] = o2;
+            C2 t1 = line[i1], t2 = line[i2];
+            butterfly(t1, t2, w[b]);
+            line[i1] = t1;
+            line[i2] = t2;
         }
         __syncthreads();
     }
