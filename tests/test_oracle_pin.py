@@ -69,3 +69,32 @@ def test_oracle_matches_reference(N, numerical, sigw, post, text, oracle_mod, tm
     got = oracle_mod.read_state(tmp_path / "state.bin")
     for k in ref:
         assert np.array_equal(ref[k], got[k]), k
+
+
+@pytest.mark.parametrize("N", [8, 16, 32])
+def test_oracle_forcing_cutoff_matches_fresh_reference_runs(N, oracle_mod, tmp_path):
+    """The reference's spectraf() with the forcing cutoff (src/output.cpp:297-406),
+    run afresh (ie_ref --spectraf) on random f and fd other than the committed
+    fixtures', for cutoffs across the whole range of |p| (with and without a low
+    one): f and fd after the call equal the oracle's bit for bit."""
+    exe = build_ref.build(N, 0, 0, 1)
+    rng = np.random.default_rng(7000 + N)
+    f = rng.standard_normal(N ** 3) * 1e-3 + 0.09
+    fd = rng.standard_normal(N ** 3) * 1e-5
+    pmax = np.sqrt(3.0) * N / 2
+    for q, (hi, lo) in enumerate([(0.3 * pmax, 0.0), (0.55 * pmax, 1.0), (0.8 * pmax, 0.5 * N / 4),
+                                  (N / 2, 0.0), (pmax + 1, 0.0)]):
+        wd = tmp_path / f"cut{q}"
+        (wd / "results").mkdir(parents=True)
+        with open(wd / "cut_in.bin", "wb") as fp:
+            fp.write(f.tobytes())
+            fp.write(fd.tobytes())
+            fp.write(np.array([hi, lo]).tobytes())
+        subprocess.run([str(exe), "--spectraf", str(wd)], check=True, stdout=subprocess.DEVNULL)
+        out = np.fromfile(wd / "cut_out.bin", dtype=np.float64)
+        o = oracle_mod.Oracle(oracle_mod.default_params(N, False))
+        o.f[:] = f
+        o.fd[:] = fd
+        o.spectrum_f(hi, lo)
+        assert np.array_equal(o.f.view(np.uint64), out[:N ** 3].view(np.uint64)), (N, hi, lo, "f")
+        assert np.array_equal(o.fd.view(np.uint64), out[N ** 3:].view(np.uint64)), (N, hi, lo, "fd")
