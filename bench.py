@@ -778,7 +778,7 @@ def engine_arm(args):
         sigw_err = measure_sigw_error(N, wd) if not args.quick else None
     ens = measure_ensemble(iegpu, max(20, min(args.steps // 30, 500)), args.warmup, peak)
     sigw = measure_sigw(iegpu, N, max(10, min(args.steps // 75, 200)), args.warmup, peak)
-    sigw512 = measure_sigw(iegpu, 512, 10, 3, peak) if not args.quick else None
+    sigw512 = measure_sigw(iegpu, 512, 20, 5, peak) if not args.quick else None
     post = measure_post_inflation(iegpu, N, max(10, min(args.steps // 300, 100)), args.warmup, peak, fp64_rate)
     kern = measure_kernels(iegpu, N, fp64_rate, peak)
 
