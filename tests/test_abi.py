@@ -82,3 +82,16 @@ def test_rk_entry_points_reject_null_arguments(engine):
         assert call() == engine.EINVAL
     assert lib.iegpu_rk45_effective(None, 1e-3, C.byref(ctl)) == engine.EINVAL
     assert lib.iegpu_strerror(engine.ECONVERGE).decode().startswith("RK45")
+
+
+def test_spectrum_and_ensemble_entry_points_reject_null_arguments(engine):
+    """The forcing-cutoff spectrum, the reference-order GW spectrum and the
+    ensemble's shape query check their arguments before any device call."""
+    lib = engine.load()
+    nb = lib.iegpu_numbins(16)
+    counts = (C.c_int * nb)()
+    f2 = (C.c_double * nb)()
+    f2f = (C.c_float * nb)()
+    assert lib.iegpu_spectrum_cutoff(None, counts, f2, nb, 5.5, 0.0) == engine.EINVAL
+    assert lib.iegpu_gw_spectrum_ref(None, 0, C.c_double(1.0), counts, f2f, f2, nb) == engine.EINVAL
+    assert lib.iegpu_ens_shapes(None, None, None, None) == engine.EINVAL
